@@ -1,0 +1,311 @@
+"""Benchmark of the isosurface-to-image path on GB300.
+
+Workload (default): one 512^3 float64 field, sum of 64 seeded Fourier modes
+with |k| in 1..16 and amplitude |k|^(-5/6), cut at +-0.5 std (two contour
+objects), rendered at 1920 x 1080.  A step is one frame: classify, scan,
+emit, smooth and rasterise both iso-surfaces into one image.
+
+  value  cell-thresholds per second with the field resident in HBM (device
+         entry point contour3d_gb300_render_device), CUDA events on the
+         launching stream
+  e2e    the same metric through the drop-in contour3d_execute with the field
+         in host memory: the host->device copy of the field, the device->host
+         copy of the image and the ppm write are inside the timed region
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference (oracle/, run
+with one thread per host core as emulated z-split ranks) on a bounded sample
+of the same workload.  Under torchrun, every rank renders its own replica of
+the workload (the path shards by z-slabs with one final reduction; each GPU
+here renders a whole field).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (512, 512, 512)
+NMODES, KMIN, KMAX, POWER, SEED = 64, 1, 16, 5.0 / 6.0, 1
+WIDTH, HEIGHT = 1920, 1080
+CAM = (2.5, 2.0, 1.5)
+CENTRE = (0.5, 0.5, 0.5)
+COLORS = ((0, 255, 255), (255, 255, 0))
+CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(field_sample: np.ndarray, std: float, cores: int):
+    """The CPU oracle on a z-slab sample of the same field, one thread per core."""
+    from contour3d_gb300 import _abi
+    from oracle.lib import Oracle
+    orc = Oracle()
+    nz = field_sample.shape[0]
+    g = _abi.unit_grid(SHAPE[2])
+    scene = _abi.make_scene(CAM, CENTRE, WIDTH, HEIGHT)
+    grids = (_abi.unit_grid(SHAPE[0]), _abi.unit_grid(SHAPE[1]), g[:nz])
+    scene.contours = [_abi.Contour(field_sample, -0.5 * std, COLORS[0], grids=grids),
+                      _abi.Contour(field_sample, 0.5 * std, COLORS[1], grids=grids)]
+    t0 = time.perf_counter()
+    orc.render(scene, nranks=cores)
+    dt = time.perf_counter() - t0
+    cells = 2 * (SHAPE[0] - 1) * (SHAPE[1] - 1) * (nz - 1)
+    return cells / dt, dt, cells
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the reference's algorithm restated in C (oracle/), all host cores."""
+    if rank != 0:
+        return
+    from contour3d_gb300 import fields
+    cores = os.cpu_count() or 1
+    nz = CPU_SAMPLE_SLICES
+    sample, std = fields.modes((nz, SHAPE[1], SHAPE[2]), NMODES, KMIN, KMAX, POWER, SEED,
+                               glshape=SHAPE)
+    for _ in range(args.warmup):
+        cpu_baseline(sample, std, cores)
+    times = []
+    cells = 0
+    for _ in range(args.steps):
+        v, dt, cells = cpu_baseline(sample, std, cores)
+        times.append(dt)
+    ms = 1000.0 * float(np.mean(times))
+    value = cells / (ms / 1000.0)
+    sample_desc = (f"z-slab of {nz} of 512 node layers (512x512x{nz} f64, two thresholds, "
+                   f"1920x1080), oracle with {cores} threads as emulated z-split ranks")
+    out = {
+        "metric": "cells_per_s", "value": value, "unit": "cell-thresholds/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fourier field)",
+        "impl": "reference",
+        "config": {"workload": "fourier-512^3-f64-2thr-1920x1080", "sample": sample_desc},
+        "cpu_baseline": {"value": value, "unit": "cell-thresholds/s", "cores": cores, "kind": "port",
+                         "sample": sample_desc},
+        "e2e": {"value": value, "unit": "cell-thresholds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gpu" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    torch.cuda.set_device(local)
+    from contour3d_gb300 import _abi, lib
+    gpu = lib.load()
+    nz, ny, nx = SHAPE
+    field = torch.empty(SHAPE, dtype=torch.float64, device="cuda")
+    std = gpu.fieldgen_modes_device(field.data_ptr(), 0, SHAPE, NMODES, KMIN, KMAX, POWER, SEED)
+    grids = [_abi.unit_grid(n) for n in (nx, ny, nz)]
+    thresholds = (-0.5 * std, 0.5 * std)
+    fdesc = [(field.data_ptr(), 0, (nx, ny, nz), grids, thr, col) for thr, col in zip(thresholds, COLORS)]
+    scene = _abi.make_scene(CAM, CENTRE, WIDTH, HEIGHT)
+    rgb = torch.empty(WIDTH * HEIGHT * 3, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        rc = gpu.render_device(scene, fdesc, rgb.data_ptr(), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError("render_device failed")
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    # untimed per-stage profile of one frame
+    gpu.set_stage_timing(True)
+    step()
+    prof = gpu.stats()
+    gpu.set_stage_timing(False)
+    step()
+    st = gpu.stats()
+    launches_per_step = int(st.kernel_launches)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cells_per_step = 2 * (nx - 1) * (ny - 1) * (nz - 1)
+    value = world * cells_per_step / (ms / 1000.0)
+
+    # ---- roofline of the dominant stage (per-stage event times of one frame) ----
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    T = float(prof.triangles)
+    nodes = float(nx * ny * nz)
+    cells = float((nx - 1) * (ny - 1) * (nz - 1))
+    stage_ms = {"classify": prof.ms_classify, "scan": prof.ms_scan, "emit": prof.ms_emit,
+                "normals": prof.ms_normals, "raster": prof.ms_raster}
+    # algorithmic bytes per frame (2 objects): see DESIGN.md "Kernels and rooflines"
+    stage_bytes = {
+        "classify": 2 * (nodes * 8 + cells * 1),
+        "scan": 2 * cells * (1 + 4),
+        "emit": T * (4 + 4 + 8 * 8 + 24 + 4 + 72),
+        "normals": T * (4 + 4 + 72) ,
+        "raster": T * (4 + 72 + 72),
+    }
+    dom = max(stage_ms, key=lambda k: stage_ms[k])
+    achieved = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9 if stage_ms[dom] > 0 else 0.0
+    fp64_per_tri = {"emit": 110 + 171, "normals": 150, "raster": 300}
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"
+                if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+                "stage_ms": stage_ms, "stage_gbs": {k: (stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9
+                                                        if stage_ms[k] > 0 else None) for k in stage_ms},
+                "note": "emit/normals/raster are FP64-pipe bound on GB300 (~0.6 T FP64 ops/s)"}
+
+    # ---- end to end through the drop-in C entry point ----
+    e2e = None
+    if not args.no_e2e:
+        host_field = field.cpu().numpy()
+        sc = _abi.make_scene(CAM, CENTRE, WIDTH, HEIGHT)
+        sc.contours = [_abi.Contour(host_field, thr, col, grids=tuple(grids)) for thr, col in zip(thresholds, COLORS)]
+        tmp = tempfile.mkdtemp()
+        path = os.path.join(tmp, "frame.ppm")
+        for _ in range(2):
+            if gpu.execute(sc, path) != 0:
+                raise RuntimeError("contour3d_execute failed")
+        steps2 = max(2, min(args.steps, 5))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps2):
+            gpu.execute(sc, path)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps2
+        e2e = {"value": world * cells_per_step / dt, "unit": "cell-thresholds/s",
+               "h2d_bytes_per_step": int(nodes * 8), "d2h_bytes_per_step": int(WIDTH * HEIGHT * 3),
+               "ms_per_step": dt * 1000.0, "path": "contour3d_execute (host field, ppm written)"}
+        os.unlink(path)
+        os.rmdir(tmp)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = field[:CPU_SAMPLE_SLICES].cpu().numpy()
+        cores = os.cpu_count() or 1
+        v, dt, c = cpu_baseline(sample, std, cores)
+        cpu = {"value": v, "unit": "cell-thresholds/s", "cores": cores, "kind": "port",
+               "sample": f"512x512x{CPU_SAMPLE_SLICES} z-slab of the same field, two thresholds, 1920x1080, "
+                         f"oracle/c3d_oracle.c with {cores} threads ({dt:.2f} s)"}
+
+    if rank == 0:
+        out = {
+            "metric": "cells_per_s", "value": value, "unit": "cell-thresholds/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fourier field)",
+            "config": {"workload": "fourier-512^3-f64-2thr-1920x1080", "field": "512^3 f64, 64 modes |k| 1..16",
+                       "thresholds": "+-0.5 std", "image": "1920x1080",
+                       "l2": "inputs larger than L2 (1.07 GB field)", "parallelism": f"replicas x{world}"},
+            "frames_per_s": 1000.0 / ms, "triangles_per_frame": int(st.triangles),
+            "triangles_per_s": world * st.triangles / (ms / 1000.0),
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+        }
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

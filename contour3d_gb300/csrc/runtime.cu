@@ -1,0 +1,1011 @@
+/*
+ * runtime.cu -- host runtime of the GB300 isosurface path: the drop-in
+ * contour3d_execute (reference src/contour3d/main.c:68-146) and the
+ * extension entry points of contour3d_gb300.h.
+ *
+ * Per call: scene constants on the host (same operations as main.c:25-63 and
+ * project.c:9-67, compiled without contraction), one device z-buffer of
+ * 16-byte slots, then per contour object the slab pipeline of kernels.cu,
+ * then the lines, then one resolve pass and one device->host copy of the
+ * image.  Device buffers are kept between calls (grow-only) so that repeated
+ * frames do not pay for cudaMalloc; contour3d_gb300_release() frees them.
+ */
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cerrno>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+#include "contour3d.h"
+#include "contour3d_gb300.h"
+#include "c3d_common.cuh"
+#include "c3d_host.h"
+#include "c3d_kernels.h"
+
+namespace c3d {
+
+#define C3D_CUDA(call)                                                           \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      log_error("%s failed: %s", #call, cudaGetErrorString(e_));                 \
+      return 1;                                                                  \
+    }                                                                            \
+  } while (0)
+
+typedef contour3d_vector_t V;
+
+/* ---------------- host vector algebra (vector.c:5-76) ---------------- */
+static inline V h_add(V a, V b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline V h_sub(V a, V b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline V h_mul(double w, V a) { return {w * a.x, w * a.y, w * a.z}; }
+static inline double h_dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline V h_cross(V a, V b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+static inline V h_normalise(V a) {
+  const double inv = 1. / sqrt(h_dot(a, a));
+  return {a.x * inv, a.y * inv, a.z * inv};
+}
+static inline d3 to_d3(V v) { return {v.x, v.y, v.z}; }
+
+/* host copy of the scene (main.c:13-63) */
+struct HostScene {
+  V cam, center, lx, ly, normal, light;
+  size_t W, H;
+};
+
+static HostScene make_scene(const V *cam, const V *light, const size_t sizes[2], const V *center, const V local[2]) {
+  HostScene s;
+  s.cam = *cam;
+  s.light = h_normalise(*light);
+  s.center = *center;
+  s.lx = local[0];
+  s.ly = local[1];
+  s.normal = h_normalise(h_cross(s.lx, s.ly));
+  s.W = sizes[0];
+  s.H = sizes[1];
+  return s;
+}
+
+static SceneDev scene_dev(const HostScene &s) {
+  SceneDev d;
+  d.cam = to_d3(s.cam);
+  d.center = to_d3(s.center);
+  d.lx = to_d3(s.lx);
+  d.ly = to_d3(s.ly);
+  d.normal = to_d3(s.normal);
+  d.light = to_d3(s.light);
+  d.nc = h_dot(s.normal, s.cam);
+  d.d = h_dot(s.normal, s.center);
+  d.lxx = h_dot(s.lx, s.lx);
+  d.lyy = h_dot(s.ly, s.ly);
+  d.width = (long long)s.W;
+  d.height = (long long)s.H;
+  return d;
+}
+
+/* project.c:9-67 on the host (line end points) */
+static int h_project(const HostScene &s, V p0, V *p1) {
+  const V ray = h_sub(p0, s.cam);
+  const double nc = h_dot(s.normal, s.cam);
+  const double nr = h_dot(s.normal, ray);
+  const double d = h_dot(s.normal, s.center);
+  const double small = 1.e-8;
+  if (-small < nr && nr < small) return 1;
+  const double t = (d - nc) / nr;
+  if (t <= 0. || 1. <= t) return 1;
+  const V delta = {s.cam.x + t * ray.x - s.center.x, s.cam.y + t * ray.y - s.center.y,
+                   s.cam.z + t * ray.z - s.center.z};
+  p1->x = h_dot(delta, s.lx) / h_dot(s.lx, s.lx);
+  p1->y = h_dot(delta, s.ly) / h_dot(s.ly, s.ly);
+  p1->z = nr;
+  return 0;
+}
+
+static long long h_key(double x) {
+  long long b;
+  memcpy(&b, &x, sizeof b);
+  if ((b << 1) == 0) b = 0;
+  return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+static unsigned long long h_depth_key(double x) { return (unsigned long long)h_key(x) ^ 0x8000000000000000ULL; }
+
+/* ---------------- marching-tetrahedra tables (triangulate.c) ---------------- */
+/* cube corners of the six tetrahedra sharing the 0-7 diagonal */
+static const int kTet[6][4] = {{0, 7, 3, 1}, {0, 7, 1, 5}, {0, 7, 5, 4}, {0, 7, 4, 6}, {0, 7, 6, 2}, {0, 7, 2, 3}};
+/* triangles of each folded mask as (tail, head) pairs of tetrahedron vertices */
+static const int kNtri[8] = {0, 1, 1, 2, 1, 2, 2, 1};
+static const int kTriPairs[8][2][3][2] = {
+    {{{0}}},
+    {{{0, 1}, {0, 3}, {0, 2}}},
+    {{{1, 0}, {1, 2}, {1, 3}}},
+    {{{0, 2}, {1, 3}, {0, 3}}, {{0, 2}, {1, 2}, {1, 3}}},
+    {{{2, 0}, {2, 3}, {2, 1}}},
+    {{{2, 1}, {0, 3}, {2, 3}}, {{2, 1}, {0, 1}, {0, 3}}},
+    {{{0, 2}, {2, 3}, {1, 3}}, {{0, 2}, {1, 3}, {0, 1}}},
+    {{{3, 0}, {3, 2}, {3, 1}}},
+};
+
+/* cube-edge id of two corners: 0-3 x, 4-7 y, 8-11 z, 12-17 face diagonals, 18 body diagonal */
+static int edge_id(int a, int b) {
+  if (a > b) std::swap(a, b);
+  switch (a ^ b) {
+    case 1: return a >> 1;
+    case 2: return 4 + ((a & 1) | ((a >> 2) << 1));
+    case 4: return 8 + (a & 3);
+    case 6: return 12 + (a & 1);
+    case 5: return 14 + ((a >> 1) & 1);
+    case 3: return 16 + (a >> 2);
+    case 7: return 18;
+    default: return 31;
+  }
+}
+
+/* normal.c:78-158 in table form: (dk, dj, di, local edge id) per cube edge */
+static const signed char kNb[19][4][4] = {
+    {{-1, -1, 0, 3}, {-1, 0, 0, 2}, {0, -1, 0, 1}, {0, 0, 0, 0}},
+    {{-1, 0, 0, 3}, {-1, 1, 0, 2}, {0, 0, 0, 1}, {0, 1, 0, 0}},
+    {{0, -1, 0, 3}, {0, 0, 0, 2}, {1, -1, 0, 1}, {1, 0, 0, 0}},
+    {{0, 0, 0, 3}, {0, 1, 0, 2}, {1, 0, 0, 1}, {1, 1, 0, 0}},
+    {{-1, 0, -1, 7}, {-1, 0, 0, 6}, {0, 0, -1, 5}, {0, 0, 0, 4}},
+    {{-1, 0, 0, 7}, {-1, 0, 1, 6}, {0, 0, 0, 5}, {0, 0, 1, 4}},
+    {{0, 0, -1, 7}, {0, 0, 0, 6}, {1, 0, -1, 5}, {1, 0, 0, 4}},
+    {{0, 0, 0, 7}, {0, 0, 1, 6}, {1, 0, 0, 5}, {1, 0, 1, 4}},
+    {{0, -1, -1, 11}, {0, -1, 0, 10}, {0, 0, -1, 9}, {0, 0, 0, 8}},
+    {{0, -1, 0, 11}, {0, -1, 1, 10}, {0, 0, 0, 9}, {0, 0, 1, 8}},
+    {{0, 0, -1, 11}, {0, 0, 0, 10}, {0, 1, -1, 9}, {0, 1, 0, 8}},
+    {{0, 0, 0, 11}, {0, 0, 1, 10}, {0, 1, 0, 9}, {0, 1, 1, 8}},
+    {{0, 0, -1, 13}, {0, 0, 0, 12}},
+    {{0, 0, 0, 13}, {0, 0, 1, 12}},
+    {{0, -1, 0, 15}, {0, 0, 0, 14}},
+    {{0, 0, 0, 15}, {0, 1, 0, 14}},
+    {{-1, 0, 0, 17}, {0, 0, 0, 16}},
+    {{0, 0, 0, 17}, {1, 0, 0, 16}},
+    {{0, 0, 0, 18}},
+};
+static const unsigned char kNbCount[19] = {4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 2, 2, 2, 2, 2, 2, 1};
+
+static void build_tables(std::vector<unsigned long long> &lut, unsigned char count[256]) {
+  lut.assign(kLutEntries, 0ULL);
+  for (int code = 0; code < 256; code++) {
+    int n = 0;
+    for (int t = 0; t < 6; t++) {
+      int mask = 0;
+      for (int m = 0; m < 4; m++) mask |= ((code >> kTet[t][m]) & 1) << m;
+      const bool rev = mask >= 8;
+      if (rev) mask = 15 - mask;
+      for (int s = 0; s < kNtri[mask]; s++) {
+        unsigned long long e = 0;
+        for (int q = 0; q < 3; q++) {
+          const int src = rev ? 2 - q : q;
+          const int a = kTet[t][kTriPairs[mask][s][src][0]];
+          const int b = kTet[t][kTriPairs[mask][s][src][1]];
+          e |= (unsigned long long)a << (6 * q);
+          e |= (unsigned long long)b << (6 * q + 3);
+          e |= (unsigned long long)edge_id(a, b) << (18 + 5 * q);
+        }
+        lut[code * 12 + n++] = e;
+      }
+    }
+    count[code] = (unsigned char)n;
+  }
+}
+
+/* ---------------- device context ---------------- */
+struct Buf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = bytes + bytes / 4 + 256;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      log_error("device allocation of %zu bytes failed", want);
+      return 1;
+    }
+    cap = want;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct HostBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      log_error("pinned host allocation of %zu bytes failed", bytes);
+      return 1;
+    }
+    cap = bytes;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct Ctx {
+  int device = -1;
+  bool ready = false;
+  cudaStream_t own_stream = nullptr;
+  Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
+  HostBuf h_small, h_rgb, h_slots;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[8] = {};
+  bool stage_timing = false;
+  unsigned long long slab_cells = 1ULL << 27;
+  contour3d_gb300_stats_t stats = {};
+  const void *field_src = nullptr; /* host array currently in `field` (valid within one call) */
+  size_t field_bytes = 0;
+  uint64_t stats_h2d = 0;
+};
+
+static Ctx g_ctx;
+static std::mutex g_mu;
+
+static int ctx_init(Ctx &c) {
+  int dev = 0;
+  C3D_CUDA(cudaGetDevice(&dev));
+  if (c.ready && c.device == dev) return 0;
+  if (c.ready) {
+    log_error("the library context is bound to device %d; call contour3d_gb300_release() first", c.device);
+    return 1;
+  }
+  C3D_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
+  C3D_CUDA(cudaEventCreate(&c.ev0));
+  C3D_CUDA(cudaEventCreate(&c.ev1));
+  for (auto &e : c.evs) C3D_CUDA(cudaEventCreate(&e));
+  std::vector<unsigned long long> lut;
+  unsigned char count[256];
+  build_tables(lut, count);
+  if (upload_tables(count, kNb, kNbCount)) {
+    log_error("constant table upload failed");
+    return 1;
+  }
+  if (c.lut.ensure(sizeof(unsigned long long) * kLutEntries)) return 1;
+  C3D_CUDA(cudaMemcpy(c.lut.p, lut.data(), sizeof(unsigned long long) * kLutEntries, cudaMemcpyHostToDevice));
+  if (c.h_small.ensure(64)) return 1;
+  c.device = dev;
+  c.ready = true;
+  return 0;
+}
+
+/* ---------------- identity converters ---------------- */
+typedef V (*conv_fn)(const V);
+static conv_fn g_identity[16];
+static int g_nidentity = 0;
+
+static bool is_identity(conv_fn f);
+
+/* ---------------- frame description ---------------- */
+struct ContourIn {
+  const void *data = nullptr;  /* field: host or device */
+  bool on_device = false;
+  bool f32 = false;
+  size_t sz[3] = {0, 0, 0};    /* extended block sizes */
+  size_t off[3] = {0, 0, 0};   /* global offset of the block */
+  const double *grid[3] = {nullptr, nullptr, nullptr}; /* host node coordinates of the block */
+  conv_fn converter = nullptr;
+  double threshold = 0.;
+  contour3d_color_t color = {0, 0, 0};
+};
+
+struct FrameIn {
+  HostScene scene;
+  contour3d_color_t bg;
+  std::vector<ContourIn> contours;
+  const contour3d_line_obj_t *lines = nullptr;
+  size_t nlines = 0;
+  cudaStream_t stream = nullptr;
+};
+
+/* host sink of rendered-triangle records (contour3d_gb300_debug_triangles) */
+struct TriRecord {
+  double vertices[9];
+  double vertex_normals[9];
+  double face_normal[3];
+  double area;
+  int64_t cell[3];
+  int64_t edge_ids[3];
+};
+static_assert(sizeof(TriRecord) == 224, "triangle record is 224 bytes");
+
+struct DebugSink {
+  TriRecord *out = nullptr;
+  long capacity = 0;
+  long count = 0;
+  long triangulated = 0;
+  bool triangulated_only = false; /* only count, do not render */
+};
+
+struct FrameOut {
+  uint8_t *rgb_host = nullptr;  /* ppm body */
+  uint8_t *rgb_dev = nullptr;   /* ppm body on the device */
+  double *depth_host = nullptr; /* canvas order */
+  PixelRec *pixels_host = nullptr; /* canvas order, for the multi-rank reduction */
+  DebugSink *sink = nullptr;
+};
+
+static const size_t kTriBytes = 21 * sizeof(double) + sizeof(unsigned);
+
+static TriDev tri_layout(void *base, size_t cap, double *dbg) {
+  TriDev t;
+  double *d = static_cast<double *>(base);
+  for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
+  for (int q = 0; q < 9; q++) t.proj[q] = d + (3 + q) * cap;
+  for (int q = 0; q < 9; q++) t.vn[q] = d + (12 + q) * cap;
+  t.meta = reinterpret_cast<unsigned *>(d + 21 * cap);
+  t.dbg_vert = dbg;
+  t.dbg_fn = dbg ? dbg + 9 * cap : nullptr;
+  t.dbg_area = dbg ? dbg + 12 * cap : nullptr;
+  return t;
+}
+
+static float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+/* one contour object through all of its slabs */
+static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn &ci,
+                          unsigned long long &order_base, const double *xs, const double *ys, DebugSink *sink) {
+  cudaStream_t st = f.stream;
+  const long long nx = (long long)ci.sz[0], ny = (long long)ci.sz[1], nz = (long long)ci.sz[2];
+  if (nx < 2 || ny < 2 || nz < 2) return 0;
+  const long long ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+  const size_t elem = ci.f32 ? 4 : 8;
+  const size_t nnodes = (size_t)(nx * ny * nz);
+  /* field */
+  const void *dfield = ci.data;
+  if (!ci.on_device) {
+    /* objects of one call that share a host array (the reference's example
+       draws two levels of one field) upload it once */
+    if (!(c.field_src == ci.data && c.field_bytes == nnodes * elem && c.field.p)) {
+      if (c.field.ensure(nnodes * elem)) return 1;
+      C3D_CUDA(cudaMemcpyAsync(c.field.p, ci.data, nnodes * elem, cudaMemcpyHostToDevice, st));
+      c.field_src = ci.data;
+      c.field_bytes = nnodes * elem;
+      c.stats_h2d += nnodes * elem;
+    }
+    dfield = c.field.p;
+  }
+  /* node coordinates */
+  if (c.grids.ensure(sizeof(double) * (size_t)(nx + ny + nz))) return 1;
+  double *g = c.grids.as<double>();
+  C3D_CUDA(cudaMemcpyAsync(g, ci.grid[0], sizeof(double) * nx, cudaMemcpyHostToDevice, st));
+  C3D_CUDA(cudaMemcpyAsync(g + nx, ci.grid[1], sizeof(double) * ny, cudaMemcpyHostToDevice, st));
+  C3D_CUDA(cudaMemcpyAsync(g + nx + ny, ci.grid[2], sizeof(double) * nz, cudaMemcpyHostToDevice, st));
+  const double *dnodes = nullptr;
+  std::vector<double> nodes;
+  if (!is_identity(ci.converter)) {
+    /* tabulate the converter once per node (triangulate.c:165-170 calls it per tetrahedron corner) */
+    nodes.resize(3 * nnodes);
+    size_t q = 0;
+    for (long long k = 0; k < nz; k++)
+      for (long long j = 0; j < ny; j++)
+        for (long long i = 0; i < nx; i++) {
+          const V p = ci.converter(V{ci.grid[0][i], ci.grid[1][j], ci.grid[2][k]});
+          nodes[q++] = p.x;
+          nodes[q++] = p.y;
+          nodes[q++] = p.z;
+        }
+    if (c.nodes.ensure(sizeof(double) * 3 * nnodes)) return 1;
+    C3D_CUDA(cudaMemcpyAsync(c.nodes.p, nodes.data(), sizeof(double) * 3 * nnodes, cudaMemcpyHostToDevice, st));
+    dnodes = c.nodes.as<double>();
+  }
+  FieldDev F;
+  F.data = dfield;
+  F.is_f32 = ci.f32 ? 1 : 0;
+  F.nx = nx;
+  F.ny = ny;
+  F.nz = nz;
+  F.gx = g;
+  F.gy = g + nx;
+  F.gz = g + nx + ny;
+  F.nodes = dnodes;
+  F.threshold = ci.threshold;
+  F.thr_key = h_key(ci.threshold);
+  F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
+  c.stats.cells += (uint64_t)(ncx * ncy * ncz);
+
+  /* rendered cell slices are [1, ncz - 2]; each slab also triangulates one
+     slice below and above for the vertex normals (contour/main.c:49-112) */
+  const long long per_slice = ncx * ncy;
+  long long slab_slices = (long long)(c.slab_cells / (unsigned long long)per_slice) - 2;
+  if (slab_slices < 1) slab_slices = 1;
+  const bool want_all = sink != nullptr;
+  /* a debug pass also counts the triangulated set over every slice */
+  const long long kr0 = want_all ? 0 : 1, kr1 = want_all ? ncz : ncz - 1;
+  unsigned *h_small = c.h_small.as<unsigned>();
+  unsigned long long *h_total = reinterpret_cast<unsigned long long *>(h_small + 4);
+  for (long long k0 = kr0; k0 < kr1; k0 += slab_slices) {
+    const long long k1 = std::min(k0 + slab_slices, kr1);
+    SlabDev S;
+    S.kfirst = std::max(k0 - 1, 0LL);
+    const long long klast = std::min(k1, ncz - 1); /* inclusive */
+    S.nslices = klast - S.kfirst + 1;
+    S.krender0 = std::max(k0, 1LL);
+    S.krender1 = std::min(k1, ncz - 1);
+    const long long ncell = S.nslices * per_slice;
+    if (c.counts.ensure((size_t)ncell) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1)) ||
+        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell)) || c.scratch.ensure(64))
+      return 1;
+    unsigned *d_counter = c.scratch.as<unsigned>();
+    unsigned *d_err = d_counter + 1;
+    unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2);
+    C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
+    if (c.stage_timing) cudaEventRecord(c.evs[0], st);
+    launch_classify(F, S, c.counts.as<unsigned char>(), st);
+    if (c.stage_timing) cudaEventRecord(c.evs[1], st);
+    launch_scan(c.counts.as<unsigned char>(), ncell, c.offsets.as<unsigned>(), c.tile_state.as<unsigned long long>(),
+                d_counter, d_total, d_err, st);
+    if (c.stage_timing) cudaEventRecord(c.evs[2], st);
+    c.stats.kernel_launches += 2;
+    C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    C3D_CUDA(cudaMemcpyAsync(h_total, d_total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    C3D_CUDA(cudaStreamSynchronize(st));
+    if (c.stage_timing) {
+      c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
+      c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
+    }
+    if (h_small[0]) {
+      log_error("device scan did not complete (error flags 0x%x)", h_small[0]);
+      return 1;
+    }
+    const unsigned long long T = *h_total;
+    if (T >= (1ULL << 32)) {
+      log_error("slab holds %llu triangles; lower the slab size", T);
+      return 1;
+    }
+    c.stats.triangles += T;
+    c.stats.slabs += 1;
+    if (T == 0) continue;
+    if (c.tri_cell.ensure(sizeof(unsigned) * T) || c.tri.ensure(kTriBytes * T)) return 1;
+    const size_t cap = c.tri.cap / kTriBytes;
+    double *dbg = nullptr;
+    if (sink) {
+      if (c.dbg.ensure(sizeof(double) * 13 * cap)) return 1;
+      dbg = c.dbg.as<double>();
+    }
+    const TriDev tri = tri_layout(c.tri.p, cap, dbg);
+    launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
+    if (c.stage_timing) cudaEventRecord(c.evs[3], st);
+    launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total,
+                (long long)T, tri, st);
+    if (c.stage_timing) cudaEventRecord(c.evs[4], st);
+    launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
+    if (c.stage_timing) cudaEventRecord(c.evs[5], st);
+    c.stats.kernel_launches += 3;
+    if (!(sink && sink->triangulated_only)) {
+      launch_raster(sd, d_total, (long long)T, tri, xs, ys, c.canvas.as<Slot>(), order_base,
+                    ((unsigned)ci.color.r << 16) | ((unsigned)ci.color.g << 8) | ci.color.b, st);
+      c.stats.kernel_launches += 1;
+    }
+    if (c.stage_timing) {
+      cudaEventRecord(c.evs[6], st);
+      C3D_CUDA(cudaEventSynchronize(c.evs[6]));
+      c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
+      c.stats.ms_normals += elapsed(c.evs[4], c.evs[5]);
+      c.stats.ms_raster += elapsed(c.evs[5], c.evs[6]);
+    }
+    order_base += T;
+    if (sink) {
+      /* copy this slab's triangles back and keep the rendered ones in order */
+      std::vector<unsigned> meta(T), cellv(T);
+      std::vector<double> vn(9 * T), dv(13 * cap);
+      C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
+      for (int q = 0; q < 9; q++)
+        C3D_CUDA(cudaMemcpyAsync(vn.data() + q * T, tri.vn[q], sizeof(double) * T, cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * 13 * cap, cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaStreamSynchronize(st));
+      for (unsigned long long t = 0; t < T; t++) {
+        const long long cl = cellv[t];
+        const long long i = cl % ncx, j = (cl / ncx) % ncy, k = S.kfirst + cl / (ncx * ncy);
+        if (k >= k0 && k < k1) sink->triangulated++;
+        if (!(meta[t] & kMetaRendered)) continue;
+        if (sink->out && sink->count < sink->capacity) {
+          TriRecord &r = sink->out[sink->count];
+          for (int q = 0; q < 9; q++) r.vertices[q] = dv[9 * t + q];
+          for (int q = 0; q < 9; q++) r.vertex_normals[q] = vn[q * T + t];
+          for (int q = 0; q < 3; q++) r.face_normal[q] = dv[9 * cap + 3 * t + q];
+          r.area = dv[12 * cap + t];
+          r.cell[0] = i + (long long)ci.off[0];
+          r.cell[1] = j + (long long)ci.off[1];
+          r.cell[2] = k + (long long)ci.off[2];
+          for (int q = 0; q < 3; q++) r.edge_ids[q] = (meta[t] >> (5 * q)) & 31;
+        }
+        sink->count++;
+      }
+    }
+  }
+  return 0;
+}
+
+/* line.c:121-170 on the host (segment end points and projections), pixels on the device */
+static int render_lines(Ctx &c, const FrameIn &f, unsigned long long &order_base) {
+  const HostScene &s = f.scene;
+  std::vector<LineSegDev> segs;
+  for (size_t n = 0; n < f.nlines; n++) {
+    const contour3d_line_obj_t *l = f.lines + n;
+    const size_t np = l->nitems;
+    if (np < 2) {
+      log_error("give more than two points to draw a line, received %zu", np);
+      log_error("line processing failed");
+      return 1;
+    }
+    const conv_fn conv = l->converter ? l->converter : contour3d_gb300_identity;
+    const V *heads = l->edges + 0, *tails = l->edges + 1;
+    const V deltas = h_mul(1. / (np - 1), h_sub(*tails, *heads));
+    const unsigned rgb = ((unsigned)l->color.r << 16) | ((unsigned)l->color.g << 8) | l->color.b;
+    for (size_t q = 0; q < np - 1; q++) {
+      const V a = h_add(*heads, h_mul(q + 0, deltas));
+      const V b = h_add(*heads, h_mul(q + 1, deltas));
+      const V pa = conv(a), pb = conv(b);
+      V p0 = {0., 0., 0.}, p1 = {0., 0., 0.};
+      LineSegDev sg = {};
+      sg.valid = !h_project(s, pa, &p0) && !h_project(s, pb, &p1);
+      if (sg.valid) {
+        sg.p0x = (0.5 + p0.x) * s.W;
+        sg.p0y = (0.5 + p0.y) * s.H;
+        sg.p1x = (0.5 + p1.x) * s.W;
+        sg.p1y = (0.5 + p1.y) * s.H;
+        sg.p0z = p0.z;
+        sg.p1z = p1.z;
+      }
+      sg.width = l->width;
+      sg.rgb = rgb;
+      segs.push_back(sg);
+    }
+  }
+  if (segs.empty()) return 0;
+  if (c.segs.ensure(sizeof(LineSegDev) * segs.size())) return 1;
+  C3D_CUDA(cudaMemcpyAsync(c.segs.p, segs.data(), sizeof(LineSegDev) * segs.size(), cudaMemcpyHostToDevice, f.stream));
+  launch_lines(c.segs.as<LineSegDev>(), (int)segs.size(), (long long)s.W, (long long)s.H, c.canvas.as<Slot>(),
+               order_base, f.stream);
+  c.stats.kernel_launches += 1;
+  /* the stream is synchronised before `segs` goes out of scope by the caller's resolve copy */
+  C3D_CUDA(cudaStreamSynchronize(f.stream));
+  order_base += segs.size();
+  return 0;
+}
+
+static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
+  const HostScene &s = f.scene;
+  const size_t W = s.W, H = s.H, npx = W * H;
+  if (W == 0 || H == 0) {
+    log_error("screen size must be positive (%zu x %zu)", W, H);
+    return 1;
+  }
+  c.stats = contour3d_gb300_stats_t{};
+  c.field_src = nullptr;
+  c.field_bytes = 0;
+  c.stats_h2d = 0;
+  cudaStream_t st = f.stream;
+  C3D_CUDA(cudaEventRecord(c.ev0, st));
+  const SceneDev sd = scene_dev(s);
+  /* pixel centres (render.c:100-104) */
+  std::vector<double> xy(W + H);
+  for (size_t i = 0; i < W; i++) xy[i] = 1. * (i + 0.5) / W - 0.5;
+  for (size_t j = 0; j < H; j++) xy[W + j] = 1. * (j + 0.5) / H - 0.5;
+  if (c.xy.ensure(sizeof(double) * (W + H)) || c.canvas.ensure(sizeof(Slot) * npx)) return 1;
+  C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy.data(), sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
+  const double *xs = c.xy.as<double>(), *ys = xs + W;
+  /* canvas: background colour at depth -DBL_MAX (main.c:90-103) */
+  const unsigned bg = ((unsigned)f.bg.r << 16) | ((unsigned)f.bg.g << 8) | f.bg.b;
+  launch_canvas_init(c.canvas.as<Slot>(), (long long)npx, h_depth_key(-1. * DBL_MAX), bg, st);
+  c.stats.kernel_launches += 1;
+  unsigned long long order_base = 1;
+  for (size_t n = 0; n < f.contours.size(); n++) {
+    if (render_contour(c, f, sd, f.contours[n], order_base, xs, ys, o.sink)) {
+      log_error("contour processing failed");
+      return 1;
+    }
+  }
+  if (render_lines(c, f, order_base)) return 1;
+  /* resolve */
+  uint8_t *rgb_dev = o.rgb_dev;
+  if (!rgb_dev && o.rgb_host) {
+    if (c.rgb.ensure(3 * npx)) return 1;
+    rgb_dev = c.rgb.as<uint8_t>();
+  }
+  if (rgb_dev) {
+    launch_resolve(c.canvas.as<Slot>(), (long long)W, (long long)H, rgb_dev, nullptr, st);
+    c.stats.kernel_launches += 1;
+  }
+  if (o.rgb_host) {
+    if (c.h_rgb.ensure(3 * npx)) return 1;
+    C3D_CUDA(cudaMemcpyAsync(c.h_rgb.p, rgb_dev, 3 * npx, cudaMemcpyDeviceToHost, st));
+  }
+  if (o.depth_host || o.pixels_host) {
+    if (c.h_slots.ensure(sizeof(Slot) * npx)) return 1;
+    C3D_CUDA(cudaMemcpyAsync(c.h_slots.p, c.canvas.p, sizeof(Slot) * npx, cudaMemcpyDeviceToHost, st));
+  }
+  C3D_CUDA(cudaEventRecord(c.ev1, st));
+  C3D_CUDA(cudaStreamSynchronize(st));
+  C3D_CUDA(cudaGetLastError());
+  c.stats.ms_total = elapsed(c.ev0, c.ev1);
+  if (o.rgb_host) memcpy(o.rgb_host, c.h_rgb.p, 3 * npx);
+  if (o.depth_host || o.pixels_host) {
+    const Slot *sl = c.h_slots.as<Slot>();
+    for (size_t p = 0; p < npx; p++) {
+      const double dep = depth_from_key(sl[p].hi);
+      if (o.depth_host) o.depth_host[p] = dep;
+      if (o.pixels_host) {
+        PixelRec &r = o.pixels_host[p];
+        r.depth = dep;
+        r.r = (uint8_t)(sl[p].lo >> 16);
+        r.g = (uint8_t)(sl[p].lo >> 8);
+        r.b = (uint8_t)(sl[p].lo);
+        memset(r.pad, 0, sizeof r.pad);
+      }
+    }
+  }
+  return 0;
+}
+
+static bool is_identity(conv_fn f) {
+  if (!f || f == contour3d_gb300_identity) return true;
+  for (int q = 0; q < g_nidentity; q++)
+    if (g_identity[q] == f) return true;
+  return false;
+}
+
+static int check_common(const V *cam, const V *light, const size_t sizes[2], const V *center, const V local[2],
+                        const contour3d_color_t *bg) {
+  if (!cam || !light || !sizes || !center || !local || !bg) {
+    log_error("null scene argument");
+    return 1;
+  }
+  return 0;
+}
+
+static int write_ppm(const char *fname, size_t W, size_t H, const uint8_t *rgb) {
+  FILE *fp = fopen(fname, "w");
+  if (!fp) {
+    log_error("%s: %s", fname, strerror(errno));
+    return 1;
+  }
+  fprintf(fp, "P6\n%zu %zu\n255\n", W, H);
+  const size_t n = fwrite(rgb, 3, W * H, fp);
+  if (n != W * H) {
+    log_error("fwrite failed (%zu expected, %zu returned)", W * H, n);
+    fclose(fp);
+    return 1;
+  }
+  fclose(fp);
+  return 0;
+}
+
+}  // namespace c3d
+
+using namespace c3d;
+
+extern "C" contour3d_vector_t contour3d_gb300_identity(const contour3d_vector_t p) { return p; }
+
+extern "C" int contour3d_gb300_declare_identity(contour3d_vector_t (*fn)(const contour3d_vector_t)) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!fn) return 1;
+  if (is_identity(fn)) return 0;
+  if (g_nidentity >= 16) {
+    log_error("too many identity converters declared");
+    return 1;
+  }
+  g_identity[g_nidentity++] = fn;
+  return 0;
+}
+
+extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
+                                 const contour3d_vector_t *const camera_position,
+                                 const contour3d_vector_t *const camera_look_at,
+                                 const contour3d_vector_t *const light_direction, const size_t screen_sizes[2],
+                                 const contour3d_vector_t *const screen_center,
+                                 const contour3d_vector_t screen_local[2], const contour3d_color_t *const bg_color,
+                                 const size_t num_contours, const contour3d_contour_obj_t *const objs,
+                                 const size_t num_lines, const contour3d_line_obj_t *const lines,
+                                 const char fname[]) {
+  (void)camera_look_at; /* stored but unused by the reference (main.c:13-23) */
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (check_common(camera_position, light_direction, screen_sizes, screen_center, screen_local, bg_color)) return 1;
+  if ((num_contours && !objs) || (num_lines && !lines)) {
+    log_error("null object array");
+    return 1;
+  }
+  if (ctx_init(g_ctx)) return 1;
+  FrameIn f;
+  f.scene = make_scene(camera_position, light_direction, screen_sizes, screen_center, screen_local);
+  f.bg = *bg_color;
+  f.lines = lines;
+  f.nlines = num_lines;
+  f.stream = g_ctx.own_stream;
+  bool multi = false;
+  std::vector<std::vector<double>> ext_store(num_contours);
+  for (size_t n = 0; n < num_contours; n++) {
+    const contour3d_contour_obj_t *o = objs + n;
+    if (!o->array || !o->grids[0] || !o->grids[1] || !o->grids[2]) {
+      log_error("contour object %zu: null array or grid", n);
+      return 1;
+    }
+    BlockInfo b;
+    if (decomp_query(sdecomp_info, o, &b)) {
+      log_error("failed to extend domain");
+      return 1;
+    }
+    ContourIn ci;
+    if (b.single) {
+      ci.data = o->array;
+    } else {
+      multi = true;
+      ext_store[n].resize(b.ext_size[0] * b.ext_size[1] * b.ext_size[2]);
+      if (extend_block(sdecomp_info, o, b, ext_store[n].data())) {
+        log_error("failed to extend domain");
+        return 1;
+      }
+      ci.data = ext_store[n].data();
+    }
+    for (int d = 0; d < 3; d++) {
+      ci.sz[d] = b.single ? b.mysize[d] : b.ext_size[d];
+      ci.off[d] = b.single ? b.offset[d] : b.ext_offset[d];
+      ci.grid[d] = o->grids[d] + ci.off[d];
+    }
+    ci.converter = o->converter;
+    ci.threshold = o->threshold;
+    ci.color = o->color;
+    f.contours.push_back(ci);
+  }
+  MPI_Comm comm = nullptr;
+  sdecomp.get_comm_cart(sdecomp_info, &comm);
+  int myrank = 0;
+  sdecomp.get_comm_rank(sdecomp_info, &myrank);
+  /* the world size decides whether a reduction is needed */
+  multi = multi || comm_size(comm) > 1;
+  const size_t W = screen_sizes[0], H = screen_sizes[1];
+  FrameOut out;
+  std::vector<uint8_t> rgb;
+  std::vector<PixelRec> px;
+  if (multi) {
+    px.resize(W * H);
+    out.pixels_host = px.data();
+  } else {
+    rgb.resize(3 * W * H);
+    out.rgb_host = rgb.data();
+  }
+  if (render_frame(g_ctx, f, out)) return 1;
+  if (multi) {
+    if (reduce_nearest(sdecomp_info, px.data(), W * H)) {
+      log_error("image output failed");
+      return 1;
+    }
+    if (myrank != 0) return 0;
+    rgb.resize(3 * W * H);
+    size_t q = 0;
+    for (size_t j = 0; j < H; j++)
+      for (size_t i = 0; i < W; i++) {
+        const PixelRec &p = px[(H - j - 1) * W + i];
+        rgb[q++] = p.r;
+        rgb[q++] = p.g;
+        rgb[q++] = p.b;
+      }
+  }
+  if (myrank != 0) return 0;
+  if (write_ppm(fname, W, H, rgb.data())) {
+    log_error("image output failed");
+    return 1;
+  }
+  return 0;
+}
+
+static int fill_from_objs(FrameIn &f, size_t num_contours, const contour3d_contour_obj_t *objs) {
+  for (size_t n = 0; n < num_contours; n++) {
+    const contour3d_contour_obj_t *o = objs + n;
+    if (!o->array || !o->grids[0] || !o->grids[1] || !o->grids[2]) {
+      log_error("contour object %zu: null array or grid", n);
+      return 1;
+    }
+    ContourIn ci;
+    ci.data = o->array;
+    for (int d = 0; d < 3; d++) {
+      ci.sz[d] = o->glsizes[d];
+      ci.grid[d] = o->grids[d];
+    }
+    ci.converter = o->converter;
+    ci.threshold = o->threshold;
+    ci.color = o->color;
+    f.contours.push_back(ci);
+  }
+  return 0;
+}
+
+extern "C" int contour3d_gb300_render(const contour3d_vector_t *camera_position,
+                                      const contour3d_vector_t *light_direction, const size_t screen_sizes[2],
+                                      const contour3d_vector_t *screen_center,
+                                      const contour3d_vector_t screen_local[2], const contour3d_color_t *bg_color,
+                                      size_t num_contours, const contour3d_contour_obj_t *objs, size_t num_lines,
+                                      const contour3d_line_obj_t *lines, uint8_t *rgb_out, double *depth_out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (check_common(camera_position, light_direction, screen_sizes, screen_center, screen_local, bg_color)) return 1;
+  if ((num_contours && !objs) || (num_lines && !lines)) {
+    log_error("null object array");
+    return 1;
+  }
+  if (ctx_init(g_ctx)) return 1;
+  FrameIn f;
+  f.scene = make_scene(camera_position, light_direction, screen_sizes, screen_center, screen_local);
+  f.bg = *bg_color;
+  f.lines = lines;
+  f.nlines = num_lines;
+  f.stream = g_ctx.own_stream;
+  if (fill_from_objs(f, num_contours, objs)) return 1;
+  FrameOut out;
+  out.rgb_host = rgb_out;
+  out.depth_host = depth_out;
+  return render_frame(g_ctx, f, out);
+}
+
+extern "C" int contour3d_gb300_render_device(const contour3d_vector_t *camera_position,
+                                             const contour3d_vector_t *light_direction, const size_t screen_sizes[2],
+                                             const contour3d_vector_t *screen_center,
+                                             const contour3d_vector_t screen_local[2],
+                                             const contour3d_color_t *bg_color, size_t num_fields,
+                                             const contour3d_gb300_field_t *fields, size_t num_lines,
+                                             const contour3d_line_obj_t *lines, uint8_t *rgb_out, void *stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (check_common(camera_position, light_direction, screen_sizes, screen_center, screen_local, bg_color)) return 1;
+  if ((num_fields && !fields) || (num_lines && !lines) || !rgb_out) {
+    log_error("null field, line or output pointer");
+    return 1;
+  }
+  if (ctx_init(g_ctx)) return 1;
+  FrameIn f;
+  f.scene = make_scene(camera_position, light_direction, screen_sizes, screen_center, screen_local);
+  f.bg = *bg_color;
+  f.lines = lines;
+  f.nlines = num_lines;
+  f.stream = stream ? static_cast<cudaStream_t>(stream) : g_ctx.own_stream;
+  for (size_t n = 0; n < num_fields; n++) {
+    const contour3d_gb300_field_t *fd = fields + n;
+    if (!fd->device_array || !fd->grids[0] || !fd->grids[1] || !fd->grids[2] ||
+        (fd->dtype != CONTOUR3D_GB300_F64 && fd->dtype != CONTOUR3D_GB300_F32)) {
+      log_error("field %zu: null array/grid or unknown dtype", n);
+      return 1;
+    }
+    ContourIn ci;
+    ci.data = fd->device_array;
+    ci.on_device = true;
+    ci.f32 = fd->dtype == CONTOUR3D_GB300_F32;
+    for (int d = 0; d < 3; d++) {
+      ci.sz[d] = fd->sizes[d];
+      ci.grid[d] = fd->grids[d];
+    }
+    ci.converter = fd->converter;
+    ci.threshold = fd->threshold;
+    ci.color = fd->color;
+    f.contours.push_back(ci);
+  }
+  FrameOut out;
+  out.rgb_dev = rgb_out;
+  return render_frame(g_ctx, f, out);
+}
+
+extern "C" int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out) {
+  if (!out) return 1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  *out = g_ctx.stats;
+  return 0;
+}
+
+extern "C" int contour3d_gb300_set_stage_timing(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_ctx.stage_timing = on != 0;
+  return 0;
+}
+
+extern "C" int contour3d_gb300_set_slab_cells(uint64_t max_cells) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (max_cells < 64) {
+    log_error("slab size must be at least 64 cells");
+    return 1;
+  }
+  g_ctx.slab_cells = max_cells;
+  return 0;
+}
+
+extern "C" long contour3d_gb300_debug_triangles(const contour3d_contour_obj_t *obj, void *out, long capacity,
+                                                long *num_triangulated) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!obj) return -1;
+  if (ctx_init(g_ctx)) return -1;
+  FrameIn f;
+  const V cam = {0., 0., 0.}, light = {0., 0., 1.}, center = {0., 0., 0.};
+  const V local[2] = {{1., 0., 0.}, {0., 1., 0.}};
+  const size_t sizes[2] = {1, 1};
+  f.scene = make_scene(&cam, &light, sizes, &center, local);
+  f.bg = {0, 0, 0};
+  f.stream = g_ctx.own_stream;
+  if (fill_from_objs(f, 1, obj)) return -1;
+  DebugSink sink;
+  sink.out = static_cast<TriRecord *>(out);
+  sink.capacity = out ? capacity : 0;
+  sink.triangulated_only = true;
+  if (g_ctx.canvas.ensure(sizeof(Slot)) || g_ctx.xy.ensure(16)) return -1;
+  const SceneDev sd = scene_dev(f.scene);
+  unsigned long long order = 1;
+  if (render_contour(g_ctx, f, sd, f.contours[0], order, g_ctx.xy.as<double>(), g_ctx.xy.as<double>() + 1, &sink))
+    return -1;
+  if (num_triangulated) *num_triangulated = sink.triangulated;
+  return sink.count;
+}
+
+extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t *obj, uint8_t *counts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!obj || !obj->array) return -1;
+  if (ctx_init(g_ctx)) return -1;
+  const long long nx = (long long)obj->glsizes[0], ny = (long long)obj->glsizes[1], nz = (long long)obj->glsizes[2];
+  if (nx < 2 || ny < 2 || nz < 2) return 0;
+  Ctx &c = g_ctx;
+  cudaStream_t st = c.own_stream;
+  const size_t nn = (size_t)(nx * ny * nz);
+  if (c.field.ensure(8 * nn) || c.counts.ensure((size_t)((nx - 1) * (ny - 1) * (nz - 1)))) return -1;
+  c.field_src = nullptr;
+  if (cudaMemcpyAsync(c.field.p, obj->array, 8 * nn, cudaMemcpyHostToDevice, st) != cudaSuccess) return -1;
+  FieldDev F = {};
+  F.data = c.field.p;
+  F.nx = nx;
+  F.ny = ny;
+  F.nz = nz;
+  F.threshold = obj->threshold;
+  F.thr_key = h_key(obj->threshold);
+  F.thr_nan = std::isnan(obj->threshold) ? 1 : 0;
+  SlabDev S = {0, nz - 1, 0, 0};
+  launch_classify(F, S, c.counts.as<unsigned char>(), st);
+  const size_t ncell = (size_t)((nx - 1) * (ny - 1) * (nz - 1));
+  std::vector<uint8_t> h(ncell);
+  if (cudaMemcpyAsync(h.data(), c.counts.p, ncell, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  long total = 0;
+  for (size_t q = 0; q < ncell; q++) total += h[q];
+  if (counts) memcpy(counts, h.data(), ncell);
+  return total;
+}
+
+extern "C" int contour3d_gb300_release(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx &c = g_ctx;
+  Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs};
+  for (Buf *b : bufs) b->release();
+  c.h_small.release();
+  c.h_rgb.release();
+  c.h_slots.release();
+  if (c.ready) {
+    cudaStreamDestroy(c.own_stream);
+    cudaEventDestroy(c.ev0);
+    cudaEventDestroy(c.ev1);
+    for (auto &e : c.evs) cudaEventDestroy(e);
+  }
+  c.ready = false;
+  c.device = -1;
+  return 0;
+}

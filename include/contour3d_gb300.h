@@ -1,0 +1,171 @@
+/*
+ * contour3d_gb300.h -- extensions of the GB300 isosurface library beside the
+ * unchanged drop-in entry point of contour3d.h.
+ *
+ * All entry points are plain C: host or device pointers and sizes, int
+ * return codes (0 = success, 1 = failure, with a "[CONTOUR3D ERROR] " line on
+ * stderr), as in the reference library (src/contour3d/main.c:68-146).
+ * None of them exists in the reference; each comment says which reference
+ * behaviour it shares.
+ */
+#if !defined(CONTOUR3D_GB300_H)
+#define CONTOUR3D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "contour3d.h"
+
+#if defined(__cplusplus)
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* converters                                                          */
+/* ------------------------------------------------------------------ */
+
+/*
+ * The identity map.  Passing it (or NULL) as a converter tells the library
+ * that grid coordinates are Cartesian, so node positions are read from the
+ * grids on the device.  Any other converter is called once per grid node on
+ * the host and its results are uploaded (the reference calls it for every
+ * tetrahedron corner, triangulate.c:156-173; the results are the same).
+ */
+contour3d_vector_t contour3d_gb300_identity(const contour3d_vector_t orthogonal);
+
+/* declare a caller's own converter to be the identity (up to 16 may be declared) */
+int contour3d_gb300_declare_identity(contour3d_vector_t (*converter)(const contour3d_vector_t));
+
+/* ------------------------------------------------------------------ */
+/* single-process rendering into caller memory                          */
+/* ------------------------------------------------------------------ */
+
+/*
+ * contour3d_execute on one process, without the file: `rgb_out` receives the
+ * ppm body (width * height * 3 bytes, rows flipped as output.c:113-123
+ * writes them); `depth_out` (optional, width * height doubles, canvas order)
+ * the final depth buffer, -DBL_MAX where nothing was drawn.
+ * Fields and grids are host pointers, as in contour3d_execute.
+ */
+int contour3d_gb300_render(const contour3d_vector_t *camera_position,
+                           const contour3d_vector_t *light_direction,
+                           const size_t screen_sizes[2],
+                           const contour3d_vector_t *screen_center,
+                           const contour3d_vector_t screen_local[2],
+                           const contour3d_color_t *bg_color, size_t num_contours,
+                           const contour3d_contour_obj_t *contour_objs, size_t num_lines,
+                           const contour3d_line_obj_t *line_objs, uint8_t *rgb_out,
+                           double *depth_out);
+
+/* ------------------------------------------------------------------ */
+/* device-resident fields                                              */
+/* ------------------------------------------------------------------ */
+
+#define CONTOUR3D_GB300_F64 0
+#define CONTOUR3D_GB300_F32 1
+
+/*
+ * A whole field already resident in device memory (x fastest), as an in-situ
+ * solver on the same GPU holds it.  float32 fields are widened to double
+ * exactly when read, so they give the result the double path gives for the
+ * widened field.  `grids` are host node coordinates (sizes[d] values each).
+ */
+typedef struct {
+  const void *device_array;
+  int dtype;
+  size_t sizes[3];
+  const double *grids[3];
+  contour3d_vector_t (*converter)(const contour3d_vector_t);
+  double threshold;
+  contour3d_color_t color;
+} contour3d_gb300_field_t;
+
+/*
+ * Render device-resident fields.  `rgb_out` is a DEVICE pointer to
+ * width * height * 3 bytes (ppm row order); `stream` a cudaStream_t (NULL =
+ * the library's own stream).  The call returns when the image is complete.
+ */
+int contour3d_gb300_render_device(const contour3d_vector_t *camera_position,
+                                  const contour3d_vector_t *light_direction,
+                                  const size_t screen_sizes[2],
+                                  const contour3d_vector_t *screen_center,
+                                  const contour3d_vector_t screen_local[2],
+                                  const contour3d_color_t *bg_color, size_t num_fields,
+                                  const contour3d_gb300_field_t *fields, size_t num_lines,
+                                  const contour3d_line_obj_t *line_objs, uint8_t *rgb_out,
+                                  void *stream);
+
+/* per-call statistics of the last render on this thread */
+typedef struct {
+  uint64_t cells;             /* cells classified (cell x threshold) */
+  uint64_t triangles;         /* triangles emitted (triangulated set, all slabs) */
+  uint64_t rendered;          /* triangles in the rendered (interior) set */
+  uint64_t slabs;             /* slab passes */
+  uint64_t kernel_launches;   /* kernels launched by the library */
+  double ms_total;            /* device time of the whole frame (events) */
+  double ms_classify, ms_scan, ms_emit, ms_normals, ms_raster; /* per stage, when timing is on */
+} contour3d_gb300_stats_t;
+
+int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);
+/* 1 = record per-stage CUDA events (adds synchronisation), 0 = off (default) */
+int contour3d_gb300_set_stage_timing(int on);
+/* upper bound on cells per slab (default 2^27); smaller slabs use less memory */
+int contour3d_gb300_set_slab_cells(uint64_t max_cells);
+
+/* ------------------------------------------------------------------ */
+/* inspection                                                          */
+/* ------------------------------------------------------------------ */
+
+/*
+ * Every rendered triangle of one contour object (single process) in the
+ * reference's drawing order (contour/main.c:92-112): per triangle 9 vertex
+ * coordinates, 9 vertex-normal components, 3 face-normal components, area
+ * (22 doubles), then cell (i, j, k) and the 3 cube-edge ids (6 int64) --
+ * 224 bytes.  Returns the rendered count (writes at most `capacity`) or -1.
+ * *num_triangulated receives the count over all triangulated cells.
+ */
+long contour3d_gb300_debug_triangles(const contour3d_contour_obj_t *obj, void *out,
+                                     long capacity, long *num_triangulated);
+
+/* per-cell triangle counts (uint8, (nx-1)(ny-1)(nz-1), x fastest); returns the total or -1 */
+long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t *obj, uint8_t *counts);
+
+/* ------------------------------------------------------------------ */
+/* multi-process transport (builds without MPI)                          */
+/* ------------------------------------------------------------------ */
+
+/*
+ * Point-to-point exchange used for the halo exchange of extend.c:10-147 and
+ * the nearest-depth reduction of output.c:32-88 when the library is built
+ * without MPI.  sendrecv sends `sendbytes` to `dest` and receives
+ * `recvbytes` from `source`; either peer may be MPI_PROC_NULL (that half is
+ * skipped).  Returns 0 on success.
+ */
+typedef struct {
+  int size;
+  int rank;
+  int (*sendrecv)(void *user, const void *sendbuf, size_t sendbytes, int dest, void *recvbuf,
+                  size_t recvbytes, int source);
+  void *user;
+} contour3d_gb300_transport_t;
+
+/* install (or, with NULL, remove) the transport behind MPI_COMM_WORLD */
+int contour3d_gb300_install_transport(const contour3d_gb300_transport_t *transport);
+
+/*
+ * Host-side array extension of one contour object (extend.c:150-282): the
+ * pencil-local block widened by two layers towards every neighbour rank and
+ * clipped at the global boundary.  Call once with ext == NULL to get sizes
+ * and offsets, then with a buffer of sizes[0]*sizes[1]*sizes[2] doubles.
+ * Collective over the decomposition.
+ */
+int contour3d_gb300_extend(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj,
+                           size_t sizes[3], size_t offsets[3], double *ext);
+
+/* release every device and pinned-host buffer the library holds */
+int contour3d_gb300_release(void);
+
+#if defined(__cplusplus)
+}
+#endif
+
+#endif /* CONTOUR3D_GB300_H */

@@ -1,0 +1,155 @@
+"""Parity of the CUDA path with the reference (golden fixtures) and with the
+CPU oracle on the same seeded inputs.  Everything integer (counts, cells,
+edge ids, pixels) must be bit-exact; the FP64 arithmetic is bit-exact too,
+because the device repeats the reference's unfused operations in the same
+order -- the tolerance stated for floating point (1e-12 relative) is checked
+as well so a failure says which bar was missed."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from contour3d_gb300 import _abi, fields
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+REL_TOL = 1e-12
+
+
+def sha(b):
+    return hashlib.sha256(b).hexdigest()
+
+
+def assert_close_records(a, b):
+    assert len(a) == len(b)
+    for name in ("cell", "edge_ids"):
+        assert np.array_equal(a[name], b[name]), name
+    for name in ("vertices", "vertex_normals", "face_normal", "area"):
+        x, y = a[name], b[name]
+        finite = np.isfinite(y)
+        assert np.array_equal(np.isfinite(x), finite), name
+        scale = np.maximum(np.abs(y[finite]), 1e-300)
+        assert np.all(np.abs(x[finite] - y[finite]) <= REL_TOL * np.maximum(scale, 1.0)), name
+    assert a.tobytes() == b.tobytes(), "records differ in their last bits"
+
+
+@pytest.mark.parametrize("name", sorted(cases.SMALL_CASES))
+def test_image_matches_reference(gpu, name):
+    scene = cases.SMALL_CASES[name]()
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    img = gpu.render(scene)
+    diff = (img != g["rgb"]).any(axis=2)
+    assert diff.sum() == 0, f"{diff.sum()} pixels differ"
+
+
+@pytest.mark.parametrize("name", sorted(cases.SMALL_CASES))
+def test_triangles_match_reference(gpu, name):
+    scene = cases.SMALL_CASES[name]()
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    got = [gpu.triangles(c) for c in scene.contours]
+    assert [len(t) for t, _ in got] == list(g["per_object"])
+    assert [n for _, n in got] == list(g["triangulated"])
+    tris = np.concatenate([t for t, _ in got]) if got else np.zeros(0, dtype=g["triangles"].dtype)
+    if len(tris):
+        assert_close_records(tris, g["triangles"])
+
+
+def test_cell_counts_match_oracle(gpu, oracle):
+    f, std = fields.modes((30, 26, 34), nmodes=24, kmin=1, kmax=6, power=5.0 / 6.0, seed=4)
+    for thr in (-0.5 * std, 0.0, 0.5 * std, 10.0, float(f.flat[77])):
+        a, ta = gpu.cell_counts(f, thr)
+        b, tb = oracle.cell_counts(f, thr)
+        assert ta == tb
+        assert np.array_equal(a, b)
+
+
+def test_config0_matches_reference(gpu):
+    """128^3 blobs, 1024^2: the reference's own ppm hash and triangle hashes."""
+    scene = cases.config0()
+    man = MANIFEST["config0"]
+    img = gpu.render(scene)
+    assert sha(img.tobytes()) == man["ppm_sha256"]
+    t, n = gpu.triangles(scene.contours[0])
+    assert len(t) == man["rendered"] and n == man["triangulated"]
+    assert sha(np.ascontiguousarray(t["vertices"]).tobytes()) == man["vertex_sha256"]
+    assert sha(np.ascontiguousarray(t["vertex_normals"]).tobytes()) == man["normal_sha256"]
+
+
+def test_execute_writes_reference_ppm(gpu, oracle, tmp_path):
+    """The drop-in entry point writes the same file the reference would."""
+    scene = cases.blobs_small()
+    a, b = str(tmp_path / "gpu.ppm"), str(tmp_path / "oracle.ppm")
+    assert gpu.execute(scene, a) == 0
+    assert oracle.execute(scene, b) == 0
+    assert open(a, "rb").read() == open(b, "rb").read()
+
+
+@pytest.mark.parametrize("slab_cells", [64, 700, 5000])
+def test_slab_size_does_not_change_the_image(gpu, slab_cells):
+    scene = cases.nonuniform_multi()
+    g = np.load(os.path.join(GOLDEN, "nonuniform_multi.npz"))
+    try:
+        assert gpu.set_slab_cells(slab_cells) == 0
+        img = gpu.render(scene)
+        tris = [gpu.triangles(c)[0] for c in scene.contours]
+    finally:
+        gpu.set_slab_cells(1 << 27)
+    assert np.array_equal(img, g["rgb"])
+    assert np.concatenate(tris).tobytes() == g["triangles"].tobytes()
+
+
+def test_depth_buffer_matches_oracle(gpu, oracle):
+    scene = cases.camera_inside()
+    img_g, dep_g = gpu.render(scene, with_depth=True)
+    img_o, dep_o = oracle.render(scene, with_depth=True)
+    assert np.array_equal(img_g, img_o)
+    assert dep_g.tobytes() == dep_o.tobytes()
+
+
+def test_short_line_is_an_error(gpu, tmp_path):
+    scene = cases.blobs_small()
+    scene.lines[2].nitems = 1
+    out = tmp_path / "x.ppm"
+    assert gpu.execute(scene, str(out)) == 1
+    assert not out.exists()
+
+
+def test_device_resident_f32_field(gpu, oracle):
+    """A float32 field resident on the device renders as its exact widening to double."""
+    import torch
+    shape = (33, 29, 31)
+    f32, std = fields.modes(shape, nmodes=16, kmin=1, kmax=5, power=5.0 / 6.0, seed=12, dtype=np.float32)
+    dev = torch.from_numpy(f32).cuda()
+    scene = _abi.make_scene(cases.CAM0, cases.CENTRE, 120, 90)
+    out = torch.zeros(90 * 120 * 3, dtype=torch.uint8, device="cuda")
+    grids = [_abi.unit_grid(n) for n in (31, 29, 33)]
+    rc = gpu.render_device(scene, [(dev.data_ptr(), 1, (31, 29, 33), grids, 0.25 * std, (255, 0, 0))],
+                           out.data_ptr())
+    assert rc == 0
+    torch.cuda.synchronize()
+    scene.contours = [_abi.Contour(f32.astype(np.float64), 0.25 * std, (255, 0, 0))]
+    ref = oracle.render(scene)
+    assert np.array_equal(out.cpu().numpy().reshape(90, 120, 3), ref)
+
+
+def test_device_field_generator_matches_host(gpu):
+    import torch
+    shape = (20, 18, 22)
+    host, std = fields.modes(shape, nmodes=32, kmin=1, kmax=8, power=5.0 / 6.0, seed=3)
+    dev = torch.empty(shape, dtype=torch.float64, device="cuda")
+    std2 = gpu.fieldgen_modes_device(dev.data_ptr(), 0, shape, 32, 1, 8, 5.0 / 6.0, 3)
+    assert std2 == std
+    assert dev.cpu().numpy().tobytes() == host.tobytes()
+    h32, _ = fields.modes(shape, nmodes=32, kmin=1, kmax=8, power=5.0 / 6.0, seed=3, dtype=np.float32)
+    d32 = torch.empty(shape, dtype=torch.float32, device="cuda")
+    gpu.fieldgen_modes_device(d32.data_ptr(), 1, shape, 32, 1, 8, 5.0 / 6.0, 3)
+    assert d32.cpu().numpy().tobytes() == h32.tobytes()
+    b = fields.blobs(shape, nblobs=7, seed=8)
+    db = torch.empty(shape, dtype=torch.float64, device="cuda")
+    gpu.fieldgen_blobs_device(db.data_ptr(), shape, 7, 8)
+    assert db.cpu().numpy().tobytes() == b.tobytes()

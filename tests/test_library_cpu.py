@@ -1,0 +1,90 @@
+"""Host-side checks that need no GPU: the native library loads and exports
+every symbol the public headers declare; the built-in decomposition answers
+the queries the reference makes of SimpleDecomp."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in ("contour3d.h", "contour3d_gb300.h", "sdecomp.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:extern\s+)?[A-Za-z_][\w\s\*]*?\b(\w+)\s*\(", src, flags=re.M):
+            name = m.group(1)
+            if name.startswith(("contour3d_", "c3d_")) and not name.endswith("_t"):
+                names.add(name)
+        for m in re.finditer(r"extern\s+const\s+\w+\s+(\w+)\s*;", src):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(built):
+    from contour3d_gb300 import lib
+    so = lib.LIB_PATH
+    out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    want = declared_symbols()
+    assert {"contour3d_execute", "contour3d_gb300_render_device", "sdecomp", "c3d_comm_world"} <= want
+    missing = want - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    L = lib.Library()
+    for name in want:
+        if name != "sdecomp":
+            assert getattr(L.lib, name) is not None
+
+
+def test_library_loads_without_gpu(built):
+    from contour3d_gb300 import lib
+    L = lib.Library()
+    s = lib.Stats()
+    assert L.lib.contour3d_gb300_last_stats(C.byref(s)) == 0
+    assert L.lib.contour3d_gb300_set_slab_cells(C.c_uint64(10)) == 1  # below the minimum
+    assert L.lib.contour3d_gb300_set_slab_cells(C.c_uint64(1 << 27)) == 0
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    from contour3d_gb300 import lib
+    with pytest.raises(lib.NativeLibraryMissing):
+        lib.Library(str(tmp_path / "nope.so"))
+
+
+class SdecompT(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("construct", "destruct", "get_comm_cart", "get_comm_rank",
+                                         "get_nprocs", "get_myrank", "get_neighbours",
+                                         "get_pencil_mysize", "get_pencil_offset")]
+
+
+def _sdecomp(L):
+    return SdecompT.in_dll(L.lib, "sdecomp")
+
+
+def test_single_process_decomposition(built):
+    from contour3d_gb300 import lib
+    L = lib.Library()
+    sd = _sdecomp(L)
+    world = C.CFUNCTYPE(C.c_void_p)(C.cast(L.lib.c3d_comm_world, C.c_void_p).value)()
+    construct = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_bool),
+                            C.POINTER(C.c_void_p))(sd.construct)
+    info = C.c_void_p()
+    assert construct(world, 3, (C.c_size_t * 3)(0, 0, 0), (C.c_bool * 3)(True, True, True), C.byref(info)) == 0
+    mysize = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_size_t))(
+        sd.get_pencil_mysize)
+    offset = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_size_t))(
+        sd.get_pencil_offset)
+    nb = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int))(sd.get_neighbours)
+    for d, g in enumerate((13, 17, 19)):
+        m, o = C.c_size_t(), C.c_size_t()
+        assert mysize(info, 0, d, g, C.byref(m)) == 0 and m.value == g
+        assert offset(info, 0, d, g, C.byref(o)) == 0 and o.value == 0
+        n2 = (C.c_int * 2)()
+        nb(info, 0, d, n2)
+        assert list(n2) == [0, 0]  # periodic with one process: myself
+    destruct = C.CFUNCTYPE(C.c_int, C.c_void_p)(sd.destruct)
+    assert destruct(info) == 0
