@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false",
                      "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-CUDA_SOURCES = ["kernels.cu", "runtime.cu", "fieldgen.cu"]
+CUDA_SOURCES = ["kernels.cu", "runtime.cu", "fieldgen.cu", "noalloc.cu"]
 CXX_SOURCES = ["decomp.cpp"]
 
 

@@ -42,6 +42,7 @@ EXPORTS = [
     "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
+    "contour3d_gb300_cell_offsets_noalloc",
     "c3d_comm_world", "sdecomp",
 ]
 

@@ -94,6 +94,29 @@ int contour3d_gb300_render_device(const contour3d_vector_t *camera_position,
                                   const contour3d_line_obj_t *line_objs, uint8_t *rgb_out,
                                   void *stream);
 
+/*
+ * Per-cell triangle offsets of one iso-level, for callers that cannot let a
+ * library allocate device memory: an in-situ solver whose memory pool owns
+ * the GPU's memory (a cudaMalloc would fail or break its accounting), or a
+ * time-stepping loop that must not stall on the device synchronisation that
+ * cudaFree implies.  No counterpart in the reference.
+ *
+ * `device_field` holds sizes[0] * sizes[1] * sizes[2] values of `dtype`
+ * (x fastest).  Outputs, in device memory: `device_offsets` the exclusive
+ * prefix sum of the triangle count of every cell, (nx-1)(ny-1)(nz-1) + 1
+ * entries, the last one being the total; `device_total` the total again.
+ * The call allocates nothing: its only scratch is a static device array of
+ * 512 KiB that every GPU loading the library keeps until the process exits,
+ * which limits the field to 268,435,455 cells (larger fields are rejected
+ * with an error).  The first call on a device looks up that array's device
+ * address, so make it before any stream capture on the device.  All calls
+ * share the array; calls that overlap on the GPU race and must be serialised
+ * by the caller.  The call returns when the result is in device memory.
+ */
+int contour3d_gb300_cell_offsets_noalloc(const void *device_field, int dtype, const size_t sizes[3],
+                                         double threshold, uint32_t *device_offsets,
+                                         unsigned long long *device_total, void *stream);
+
 /* per-call statistics of the last render on this thread */
 typedef struct {
   uint64_t cells;             /* cells classified (cell x threshold) */
