@@ -237,24 +237,26 @@ def main():
     nodes = float(nx * ny * nz)
     cells = float((nx - 1) * (ny - 1) * (nz - 1))
     stage_ms = {"classify": prof.ms_classify, "scan": prof.ms_scan, "emit": prof.ms_emit,
-                "normals": prof.ms_normals, "raster": prof.ms_raster}
+                "cover": prof.ms_cover, "exact": prof.ms_exact, "shade": prof.ms_shade}
+    C_ = float(prof.candidates)
     # algorithmic bytes per frame (2 objects): see DESIGN.md "Kernels and rooflines"
     stage_bytes = {
         "classify": 2 * (nodes * 8 + cells * 1),
         "scan": 2 * cells * (1 + 4),
-        "emit": T * (4 + 4 + 8 * 8 + 24 + 4 + 72),
-        "normals": T * (4 + 4 + 72) ,
-        "raster": T * (4 + 72 + 72),
+        "emit": T * (4 + 4 + 8 * 8 + 72 + 24 + 4 + 44),
+        "cover": T * (4 + 44 + 4) + C_ * 16,
+        "exact": C_ * (16 + 4 + 72),
+        "shade": WIDTH * HEIGHT * 16 * 2,
     }
     dom = max(stage_ms, key=lambda k: stage_ms[k])
     achieved = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9 if stage_ms[dom] > 0 else 0.0
-    fp64_per_tri = {"emit": 110 + 171, "normals": 150, "raster": 300}
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"
                 if "hbm_gbs" in peaks else "fallback 6800 GB/s",
                 "stage_ms": stage_ms, "stage_gbs": {k: (stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9
                                                         if stage_ms[k] > 0 else None) for k in stage_ms},
-                "note": "emit/normals/raster are FP64-pipe bound on GB300 (~0.6 T FP64 ops/s)"}
+                "candidates_per_frame": int(prof.candidates),
+                "note": "emit is FP64-pipe bound on GB300 (~0.6 T FP64 ops/s)"}
 
     # ---- end to end through the drop-in C entry point ----
     e2e = None

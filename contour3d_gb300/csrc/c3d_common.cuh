@@ -136,6 +136,12 @@ struct SceneDev {
   double lxx;  /* local_x . local_x */
   double lyy;  /* local_y . local_y */
   long long width, height;
+  /* single-precision projection constants (k_emit):
+     x = f_ax + f_bx (q . lx) / (n . q), y = f_ay + f_by (q . ly) / (n . q) */
+  float f_cam[3], f_n[3], f_lx[3], f_ly[3];
+  float f_cam_max, f_n1, f_lx1, f_lxm, f_ly1, f_lym;
+  float f_ax, f_bx, f_ay, f_by, f_dq;
+  int z_descending; /* the camera looks towards -z: traverse slices top down */
 };
 
 /* project.c:9-67; returns false when the point does not reach the screen */
@@ -158,6 +164,34 @@ __device__ __forceinline__ bool project(const SceneDev& s, d3 p, d3& q) {
 __device__ __forceinline__ double edge_fn(d3 v0, d3 v1, d3 v2) {
   return dsub(dmul(dsub(v2.x, v0.x), dsub(v1.y, v0.y)), dmul(dsub(v2.y, v0.y), dsub(v1.x, v0.x)));
 }
+
+/* ------------------------------------------------------------------ */
+/* certified single-precision filters                                  */
+/* ------------------------------------------------------------------ */
+/*
+ * The raster decides coverage and visibility with the reference's FP64
+ * arithmetic, but only for fragments that a single-precision estimate cannot
+ * settle.  Every estimate below carries an error bound, derived from the
+ * standard model |fl(a op b) - (a op b)| <= u |a op b| (u = 2^-24 for FP32,
+ * 2^-53 for FP64) and widened by a safety factor, that covers the distance
+ * between the FP32 value and the value the reference's FP64 code computes.
+ * A decision is "certain" only when the whole error interval lies on one
+ * side of the reference's threshold; everything else goes to the exact path.
+ */
+constexpr float kU32 = 5.9604645e-08f; /* 2^-24 */
+
+/* float key: unsigned order == numeric order, -0 == +0 */
+__device__ __forceinline__ unsigned f_key(float x) {
+  unsigned u = __float_as_uint(x);
+  if ((u << 1) == 0) u = 0;
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float f_from_key(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+/* a double rounded to float, and the distance bound |result - x| */
+__device__ __forceinline__ float to_f(double x) { return __double2float_rn(x); }
 
 /* ------------------------------------------------------------------ */
 /* marching-tetrahedra tables                                           */

@@ -10,6 +10,7 @@ namespace c3d {
 
 struct Slot;
 struct SceneDev;
+struct RasterDev;
 
 /* a scalar field on the device: an extended pencil block, x fastest */
 struct FieldDev {
@@ -35,16 +36,43 @@ struct SlabDev {
 
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {
+  double* vert[9];    /* world vertices (x, y, z) x 3, rendered triangles */
   double* wn[3];      /* area * face normal */
-  unsigned* meta;     /* edge ids (3 x 5 bits) | flags */
-  double* proj[9];    /* projected vertices (x, y, depth) x 3 */
-  double* vn[9];      /* vertex normals x 3 */
-  double* dbg_vert;   /* optional: world vertices, 9 per triangle */
+  unsigned* meta;     /* edge ids (3 x 5 bits) | flags | rank in the cell */
+  float* pf[9];       /* FP32 screen position and depth x 3, rendered triangles */
+  float* perr;        /* bound on |screen x, y - the reference's value| */
+  float* zrel;        /* relative bound on the depth */
+  double* vn[9];      /* optional (inspection): vertex normals x 3 */
   double* dbg_fn;     /* optional: face normals, 3 per triangle */
   double* dbg_area;   /* optional: areas */
 };
 constexpr unsigned kMetaRendered = 1u << 15;
 constexpr unsigned kMetaCulled = 1u << 16;
+constexpr unsigned kMetaRankShift = 17;
+
+/* a fragment that k_exact resolves with the reference's arithmetic */
+struct Candidate {
+  unsigned t;       /* triangle (emission index in the slab) */
+  unsigned pixel;   /* j * width + i */
+  float dhi;        /* upper bound of its depth */
+  unsigned pad;
+};
+
+/* per-frame raster state */
+struct RasterDev {
+  Slot* canvas;             /* 16-byte (depth, order | rgb) slots */
+  unsigned* zlo;            /* per-pixel depth floor (float keys) */
+  const double* xs;         /* pixel centres, render.c:100-104 */
+  const double* ys;
+  const float* xsf;         /* the same rounded to float */
+  const float* ysf;
+  Candidate* cand;
+  unsigned long long cand_cap;
+  unsigned long long* cand_count;
+  unsigned* tiny;           /* triangles the FP32 filter cannot settle */
+  unsigned long long tiny_cap;
+  unsigned long long* tiny_count;
+};
 
 /* one line segment, already projected to pixel units on the host */
 struct LineSegDev {
@@ -68,15 +96,23 @@ void launch_scan(const unsigned char* counts, long long n, unsigned* offsets,
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned* offsets, const unsigned* tri_cell, const unsigned long long* total,
-                 long long tri_bound, const TriDev& tri, cudaStream_t st);
+                 long long tri_bound, const TriDev& tri, unsigned* checks, cudaStream_t st);
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st);
-void launch_raster(const SceneDev& scene, const unsigned long long* total, long long tri_bound, const TriDev& tri,
-                   const double* xs, const double* ys, Slot* canvas, unsigned long long order_base, unsigned rgb,
-                   cudaStream_t st);
+void launch_cover(const SceneDev& scene, const unsigned long long* total, long long tri_bound,
+                  const unsigned* tri_cell, const TriDev& tri, const RasterDev& R, unsigned long long order_base,
+                  unsigned* checks, cudaStream_t st);
+void launch_tiny(const SceneDev& scene, long long tiny_bound, const unsigned* tri_cell, const TriDev& tri,
+                 const RasterDev& R, unsigned long long order_base, unsigned* checks, cudaStream_t st);
+void launch_exact(const SceneDev& scene, long long cand_bound, const unsigned* tri_cell, const TriDev& tri,
+                  const RasterDev& R, unsigned long long order_base, cudaStream_t st);
+void launch_shade(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned* offsets,
+                  const unsigned* tri_cell, const unsigned long long* total, const TriDev& tri, const RasterDev& R,
+                  unsigned long long order_base, unsigned rgb, cudaStream_t st);
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, cudaStream_t st);
-void launch_canvas_init(Slot* canvas, long long n, unsigned long long hi, unsigned long long lo, cudaStream_t st);
+void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,
+                        cudaStream_t st);
 void launch_resolve(const Slot* canvas, long long W, long long H, unsigned char* rgb, double* depth,
                     cudaStream_t st);
 

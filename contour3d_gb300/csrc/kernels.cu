@@ -6,22 +6,30 @@
  *   k_scan       decoupled-look-back exclusive scan of the counts, writing
  *                per-cell offsets and the triangle -> cell map
  *   k_emit       one thread per triangle: vertices, face normal, weighted
- *                normal, cube-edge ids, screen projection      (FP64)
- *   k_normals    one thread per rendered triangle: area-weighted vertex
- *                normals gathered over the cells sharing each cube edge
- *   k_raster     one thread per rendered triangle: bounding-box walk,
- *                barycentric test, harmonic depth, shading, 128-bit
- *                (depth, order) max into the z-buffer
- * and once per frame k_canvas_init, k_lines and k_resolve.
+ *                normal, cube-edge ids (FP64, the reference's arithmetic);
+ *                screen projection in FP32 with certified bounds
+ *   k_cover      one thread per rendered triangle: FP32 coverage and depth
+ *                intervals over its bounding box; certainly drawn fragments
+ *                raise a per-pixel depth floor, the rest become candidates
+ *   k_exact      one thread per candidate that can still reach the floor:
+ *                the reference's projection, barycentric test and harmonic
+ *                depth in FP64, then a 128-bit (depth, order) max into the
+ *                z-buffer
+ *   k_shade      one thread per pixel: for pixels this slab won, the vertex
+ *                normals of the winning triangle (area-weighted over the
+ *                cells sharing each cube edge) and the shading
+ * and once per frame k_canvas_init, k_lines and k_resolve.  k_normals
+ * computes every rendered triangle's vertex normals for inspection only.
  *
- * The FP64 stages run one triangle per thread on compacted triangle lists so
- * that warps stay converged: on GB300 an FP64 warp instruction costs the same
- * whether 2 or 32 lanes are active.
+ * The FP64 work runs one item per thread on compacted lists so that warps
+ * stay converged: on GB300 an FP64 warp instruction costs the same whether 2
+ * or 32 lanes are active.  Vertex normals are needed only for the triangle
+ * that finally owns a pixel, so they are computed for those alone.
  *
  * Reference correspondence (file:line of the reference tree):
  *   k_classify/k_emit  src/contour3d/contour/triangulate.c:95-342
  *   k_normals          src/contour3d/contour/normal.c:6-165
- *   k_raster           src/contour3d/contour/render.c:48-163, project.c:9-67
+ *   k_cover/exact/shade src/contour3d/contour/render.c:48-163, project.c:9-67
  *   k_lines            src/contour3d/line.c:26-119
  *   k_resolve          src/contour3d/output.c:10-30, 113-123
  *   slab / interior    src/contour3d/contour/main.c:38-112
@@ -238,11 +246,53 @@ __device__ __forceinline__ d3 interpolate(double vt, d3 p0, double v0, d3 p1, do
   return v_add(p0, v_mul(f, v_sub(p1, p0)));
 }
 
-template <typename T>
+/*
+ * Screen projection of a world point in single precision, with bounds.
+ * Uses the identity (exact in real arithmetic) of project.c:9-67
+ *   x = [(cam - centre) . lx + D (q . lx) / (n . q)] / (lx . lx),  q = p - cam,
+ *   D = n . centre - n . cam,  depth = n . q,  t = D / (n . q)
+ * q is formed in FP64 (as the reference forms `ray`) and rounded once; each
+ * FP32 dot product a . q is then within 5.2 u sum|a_i q_i| of the real one
+ * (rounding of q, of a, and three operations).
+ * Returns 1 = certainly projects, 0 = certainly fails (render.c:62-72
+ * drops the triangle), -1 = too close to a threshold of project.c:39-46.
+ */
+__device__ __forceinline__ int project_f(const SceneDev& s, d3 qd, float& X, float& Y, float& Z, float& exy,
+                                         float& ez) {
+  const float qx = to_f(qd.x), qy = to_f(qd.y), qz = to_f(qd.z);
+  const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
+  const float nq = s.f_n[0] * qx + s.f_n[1] * qy + s.f_n[2] * qz;
+  const float lq = s.f_lx[0] * qx + s.f_lx[1] * qy + s.f_lx[2] * qz;
+  const float mq = s.f_ly[0] * qx + s.f_ly[1] * qy + s.f_ly[2] * qz;
+  const float e_nq = 5.2f * kU32 * (fabsf(s.f_n[0]) * ax + fabsf(s.f_n[1]) * ay + fabsf(s.f_n[2]) * az);
+  const float e_lq = 5.2f * kU32 * (fabsf(s.f_lx[0]) * ax + fabsf(s.f_lx[1]) * ay + fabsf(s.f_lx[2]) * az);
+  const float e_mq = 5.2f * kU32 * (fabsf(s.f_ly[0]) * ax + fabsf(s.f_ly[1]) * ay + fabsf(s.f_ly[2]) * az);
+  const float anq = fabsf(nq);
+  Z = nq;
+  ez = 1.1f * e_nq + 1e-30f;
+  /* project.c:39-46: |nr| < 1e-8 or t outside (0, 1) => the point is dropped */
+  if (anq + e_nq < 0.99e-8f) return 0;
+  if (anq - e_nq <= 1.01e-8f) return -1;
+  const float t = s.f_dq / nq;
+  const float et = fabsf(t) * (e_nq / (anq - e_nq) + 3.f * kU32) + 1e-30f;
+  if (t + et < 0.f || t - et > 1.f) return 0;
+  if (t - et <= 0.f || t + et >= 1.f) return -1;
+  const float rx = lq / nq, ry = mq / nq;
+  const float erx = (e_lq + fabsf(rx) * e_nq) / (anq - e_nq) + kU32 * fabsf(rx);
+  const float ery = (e_mq + fabsf(ry) * e_nq) / (anq - e_nq) + kU32 * fabsf(ry);
+  X = s.f_ax + s.f_bx * rx;
+  Y = s.f_ay + s.f_by * ry;
+  const float ex = fabsf(s.f_bx) * erx + kU32 * (fabsf(s.f_ax) + 2.f * fabsf(s.f_bx * rx) + fabsf(X)) + 1e-12f;
+  const float ey = fabsf(s.f_by) * ery + kU32 * (fabsf(s.f_ay) + 2.f * fabsf(s.f_by * ry) + fabsf(Y)) + 1e-12f;
+  exy = 1.1f * fmaxf(ex, ey);
+  return 1;
+}
+
+template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
        const unsigned* __restrict__ offsets, const unsigned* __restrict__ tri_cell,
-       const unsigned long long* __restrict__ total_p, TriDev tri) {
+       const unsigned long long* __restrict__ total_p, TriDev tri, unsigned* __restrict__ checks) {
   __shared__ unsigned long long lut[kLutEntries];
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
@@ -254,8 +304,7 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
     const unsigned r = (unsigned)(t - offsets[c]);
     const long long i = c % ncx;
     const long long j = (c / ncx) % ncy;
-    const long long kl = c / (ncx * ncy);
-    const long long k = S.kfirst + kl;
+    const long long k = S.kfirst + c / (ncx * ncy);
     double val[8];
     const unsigned code = cell_code<T>(F, i, j, k, val);
     const unsigned long long e = lut[code * 12 + r];
@@ -276,29 +325,68 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
     tri.wn[1][t] = wn.y;
     tri.wn[2][t] = wn.z;
     /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
-    const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 &&
-                          k >= S.krender0 && k < S.krender1;
-    unsigned meta = edges | (rendered ? kMetaRendered : 0u);
+    const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
+    unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
     if (rendered) {
-      bool ok = true;
 #pragma unroll
       for (int q = 0; q < 3; q++) {
-        d3 p;
-        ok = project(scene, v[q], p) && ok;
-        tri.proj[3 * q + 0][t] = p.x;
-        tri.proj[3 * q + 1][t] = p.y;
-        tri.proj[3 * q + 2][t] = p.z;
+        tri.vert[3 * q + 0][t] = v[q].x;
+        tri.vert[3 * q + 1][t] = v[q].y;
+        tri.vert[3 * q + 2][t] = v[q].z;
       }
-      if (!ok) meta |= kMetaCulled;
+      float X[3], Y[3], Z[3], exy = 0.f, zr = 0.f;
+      int status = 1;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        float ex = 0.f, ez = 0.f;
+        const int st = project_f(scene, v_sub(v[q], scene.cam), X[q], Y[q], Z[q], ex, ez);
+        if (st == 0) status = 0;
+        else if (st < 0 && status != 0) status = -1;
+        exy = fmaxf(exy, ex);
+        zr = fmaxf(zr, ez / fmaxf(fabsf(Z[q]), 1e-30f));
+      }
+      if (status < 0 || CHECK) {
+        /* undecided (or checking): the reference's own projection */
+        bool ok = true;
+        d3 p[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
+        if (CHECK && status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
+        if (CHECK && status == 1 && ok) {
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
+                fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
+              atomicAdd(checks + 1, 1u);
+        }
+        if (status < 0) {
+          status = ok ? 1 : 0;
+          if (ok) {
+            exy = 0.f;
+            zr = 0.f;
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+              X[q] = to_f(p[q].x);
+              Y[q] = to_f(p[q].y);
+              Z[q] = to_f(p[q].z);
+              exy = fmaxf(exy, 2.f * kU32 * fmaxf(fabsf(X[q]), fabsf(Y[q])) + 1e-37f);
+              zr = 2.f * kU32;
+            }
+          }
+        }
+      }
+      if (status == 0) meta |= kMetaCulled;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        tri.pf[3 * q + 0][t] = X[q];
+        tri.pf[3 * q + 1][t] = Y[q];
+        tri.pf[3 * q + 2][t] = Z[q];
+      }
+      tri.perr[t] = exy;
+      tri.zrel[t] = zr;
     }
     tri.meta[t] = meta;
-    if (tri.dbg_vert) {
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        tri.dbg_vert[(9 * t) + 3 * q + 0] = v[q].x;
-        tri.dbg_vert[(9 * t) + 3 * q + 1] = v[q].y;
-        tri.dbg_vert[(9 * t) + 3 * q + 2] = v[q].z;
-      }
+    if (tri.dbg_fn) {
       tri.dbg_fn[3 * t + 0] = fn.x;
       tri.dbg_fn[3 * t + 1] = fn.y;
       tri.dbg_fn[3 * t + 2] = fn.z;
@@ -308,8 +396,34 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
 }
 
 /* ------------------------------------------------------------------ */
-/* k_normals                                                           */
+/* vertex normals (normal.c:6-165)                                      */
 /* ------------------------------------------------------------------ */
+/*
+ * Sum of area * face normal over the triangles of the cells sharing cube
+ * edge `e` of cell `c`, visited in the reference's order (ascending cell,
+ * then triangle order), then normalised.
+ */
+__device__ __forceinline__ d3 vertex_normal(long long c, int e, long long ncx, long long ncy,
+                                            const unsigned* __restrict__ offsets, const TriDev& tri) {
+  d3 sum = {0., 0., 0.};
+  const int nn = c_nb_count[e];
+  for (int q = 0; q < nn; q++) {
+    const long long nc = c + (long long)c_nb[e][q][0] * ncx * ncy + (long long)c_nb[e][q][1] * ncx +
+                         (long long)c_nb[e][q][2];
+    const unsigned le = (unsigned)c_nb[e][q][3];
+    const unsigned u0 = offsets[nc], u1 = offsets[nc + 1];
+    for (unsigned u = u0; u < u1; u++) {
+      const unsigned om = tri.meta[u];
+      if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
+        const d3 w = {tri.wn[0][u], tri.wn[1][u], tri.wn[2][u]};
+        sum = v_add(sum, w);
+      }
+    }
+  }
+  return v_normalise(sum);
+}
+
+/* every rendered triangle's vertex normals (inspection path only) */
 __global__ void __launch_bounds__(256)
 k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const unsigned* __restrict__ tri_cell,
           const unsigned long long* __restrict__ total_p, TriDev tri) {
@@ -322,23 +436,7 @@ k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const uns
     const long long c = tri_cell[t];
 #pragma unroll 1
     for (int m = 0; m < 3; m++) {
-      const int e = (meta >> (5 * m)) & 31;
-      d3 sum = {0., 0., 0.};
-      const int nn = c_nb_count[e];
-      for (int q = 0; q < nn; q++) {
-        const long long nc = c + (long long)c_nb[e][q][0] * ncx * ncy + (long long)c_nb[e][q][1] * ncx +
-                             (long long)c_nb[e][q][2];
-        const unsigned le = (unsigned)c_nb[e][q][3];
-        const unsigned u0 = offsets[nc], u1 = offsets[nc + 1];
-        for (unsigned u = u0; u < u1; u++) {
-          const unsigned om = tri.meta[u];
-          if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
-            const d3 w = {tri.wn[0][u], tri.wn[1][u], tri.wn[2][u]};
-            sum = v_add(sum, w);
-          }
-        }
-      }
-      const d3 n = v_normalise(sum);
+      const d3 n = vertex_normal(c, (meta >> (5 * m)) & 31, ncx, ncy, offsets, tri);
       tri.vn[3 * m + 0][t] = n.x;
       tri.vn[3 * m + 1][t] = n.y;
       tri.vn[3 * m + 2][t] = n.z;
@@ -347,56 +445,353 @@ k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const uns
 }
 
 /* ------------------------------------------------------------------ */
-/* k_raster                                                            */
+/* raster: exact fragment arithmetic (render.c:48-163)                  */
 /* ------------------------------------------------------------------ */
+/* the reference's projected triangle, bounding box and inverse area */
+struct ExactTri {
+  d3 v0, v1, v2;
+  long long imin, imax, jmin, jmax;
+  double area_inv;
+};
+
+__device__ __forceinline__ bool exact_tri(const SceneDev& s, const TriDev& tri, long long t, ExactTri& x) {
+  d3 w[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) w[q] = {tri.vert[3 * q][t], tri.vert[3 * q + 1][t], tri.vert[3 * q + 2][t]};
+  if (!project(s, w[0], x.v0) || !project(s, w[1], x.v1) || !project(s, w[2], x.v2)) return false;
+  const long long W = s.width, H = s.height;
+  const long long xmin = (long long)dsub(dmul(dadd(0.5, fmin(x.v0.x, fmin(x.v1.x, x.v2.x))), (double)W), 1.);
+  const long long xmax = (long long)dadd(dmul(dadd(0.5, fmax(x.v0.x, fmax(x.v1.x, x.v2.x))), (double)W), 1.);
+  const long long ymin = (long long)dsub(dmul(dadd(0.5, fmin(x.v0.y, fmin(x.v1.y, x.v2.y))), (double)H), 1.);
+  const long long ymax = (long long)dadd(dmul(dadd(0.5, fmax(x.v0.y, fmax(x.v1.y, x.v2.y))), (double)H), 1.);
+  x.imin = min(W - 1, max(0LL, xmin));
+  x.imax = min(W - 1, max(0LL, xmax));
+  x.jmin = min(H - 1, max(0LL, ymin));
+  x.jmax = min(H - 1, max(0LL, ymax));
+  const double area = edge_fn(x.v0, x.v1, x.v2);
+  x.area_inv = ddiv(1., area < 0. ? fmin(area, -1.e-16) : fmax(area, +1.e-16));
+  return true;
+}
+
+/* the reference's barycentric weights at pixel (i, j); false when outside */
+__device__ __forceinline__ bool exact_weights(const ExactTri& x, long long i, long long j, const double* xs,
+                                              const double* ys, double& w0, double& w1, double& w2) {
+  if (i < x.imin || i > x.imax || j < x.jmin || j > x.jmax) return false;
+  const d3 v3 = {xs[i], ys[j], 0.};
+  w0 = dmul(x.area_inv, edge_fn(x.v1, x.v2, v3));
+  w1 = dmul(x.area_inv, edge_fn(x.v2, x.v0, v3));
+  w2 = dmul(x.area_inv, edge_fn(x.v0, x.v1, v3));
+  return !(w0 < -1.e-8 || w1 < -1.e-8 || w2 < -1.e-8);
+}
+
+__device__ __forceinline__ double exact_depth(const ExactTri& x, double w0, double w1, double w2) {
+  return ddiv(1., dadd(dadd(ddiv(w0, x.v0.z), ddiv(w1, x.v1.z)), ddiv(w2, x.v2.z)));
+}
+
+/* one fragment through the reference's test and the (depth, order) z-buffer */
+__device__ __forceinline__ void exact_fragment(const SceneDev& s, const TriDev& tri, long long t, long long i,
+                                               long long j, const RasterDev& R, unsigned long long order) {
+  ExactTri x;
+  if (!exact_tri(s, tri, t, x)) return;
+  double w0, w1, w2;
+  if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) return;
+  const double dist0 = exact_depth(x, w0, w1, w2);
+  slot_max(R.canvas + j * s.width + i, depth_key(dist0), order << 24);
+}
+
+/* ------------------------------------------------------------------ */
+/* k_cover: single-precision coverage / depth filter                   */
+/* ------------------------------------------------------------------ */
+/*
+ * Per rendered triangle, every pixel of a (superset of the) reference's
+ * bounding box is classified with certified FP32 bounds:
+ *   certainly outside        -> dropped
+ *   certainly inside         -> raises the pixel's depth floor (zlo) to a
+ *                               certain lower bound of its depth, and is a
+ *                               candidate
+ *   undecided                -> candidate
+ * A candidate carries an upper bound of its depth; k_exact drops it when
+ * that bound is below the final floor (a certainly drawn fragment is nearer,
+ * so it cannot win), and runs the reference's arithmetic otherwise.
+ */
+struct EdgeF {
+  float ax, ay, dby, dbx, e_dby, e_dbx;
+};
+
+__device__ __forceinline__ EdgeF edge_f(float ax, float ay, float bx, float by, float eps) {
+  EdgeF E;
+  E.ax = ax;
+  E.ay = ay;
+  E.dby = by - ay;
+  E.dbx = bx - ax;
+  E.e_dby = 2.f * eps + kU32 * fabsf(E.dby);
+  E.e_dbx = 2.f * eps + kU32 * fabsf(E.dbx);
+  return E;
+}
+
+/* render.c:38-46 at a point known to +-e_p, edge vertex a known to +-eps_a; value and error bound */
+__device__ __forceinline__ float edge_eval(const EdgeF& E, float px, float py, float e_p, float eps_a, float& err) {
+  const float u = px - E.ax, v = py - E.ay;
+  const float eu = e_p + eps_a + kU32 * fabsf(u), ev = e_p + eps_a + kU32 * fabsf(v);
+  const float p1 = u * E.dby, p2 = v * E.dbx;
+  const float e = p1 - p2;
+  err = 1.25f * (fabsf(u) * E.e_dby + fabsf(E.dby) * eu + eu * E.e_dby + fabsf(v) * E.e_dbx + fabsf(E.dbx) * ev +
+                 ev * E.e_dbx + kU32 * (fabsf(p1) + fabsf(p2) + fabsf(e)));
+  return e;
+}
+
+constexpr float kWOut = -1.0e-8f * (1.f + 1e-5f); /* certainly below -1e-8 */
+constexpr float kWIn = -1.0e-8f * (1.f - 1e-5f);  /* certainly above -1e-8 */
+
+/* warp-aggregated append; returns the slot or ~0 when the list is full */
+__device__ __forceinline__ unsigned long long append_slot(unsigned long long* count, bool want) {
+  const unsigned mask = __ballot_sync(__activemask(), want);
+  if (!want) return ~0ULL;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1));
+}
+
+__device__ __forceinline__ void push_candidate(const RasterDev& R, const SceneDev& s, const TriDev& tri, long long t,
+                                               long long i, long long j, float dhi, unsigned long long order,
+                                               bool want) {
+  const unsigned long long idx = append_slot(R.cand_count, want);
+  if (!want) return;
+  if (idx < R.cand_cap) {
+    Candidate c;
+    c.t = (unsigned)t;
+    c.pixel = (unsigned)(j * s.width + i);
+    c.dhi = dhi;
+    c.pad = 0;
+    R.cand[idx] = c;
+  } else {
+    exact_fragment(s, tri, t, i, j, R, order); /* list full: resolve in place */
+  }
+}
+
+/* pixel index range whose centres (i + 0.5) / n - 0.5 may lie in [lo, hi] */
+__device__ __forceinline__ void centre_range(float lo, float hi, long long n, long long& a, long long& b) {
+  const float fa = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + lo) * (float)n - 0.5f - 1e-3f));
+  const float fb = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + hi) * (float)n - 0.5f + 1e-3f));
+  a = max(0LL, (long long)ceilf(fa));
+  b = min(n - 1, (long long)floorf(fb));
+}
+
+/* ------------------------------------------------------------------ */
+/* k_tiny: triangles the single-precision filter cannot settle         */
+/* ------------------------------------------------------------------ */
+/*
+ * Triangles whose projected area is too small (or too uncertain) for the
+ * FP32 bounds.  The reference's projection and area are computed once per
+ * triangle; when the area is not clamped (|area| >= 1e-16, render.c:108-111)
+ * the covered pixel centres lie in the triangle's extent, which holds no
+ * pixel centre for most of these triangles; otherwise the reference's whole
+ * box is tested.  Fragments go straight to the z-buffer.
+ */
+template <bool CHECK>
+__device__ void tiny_triangle(const SceneDev& s, const TriDev& tri, long long t, const RasterDev& R,
+                              unsigned long long order, unsigned* checks) {
+  ExactTri x;
+  if (!exact_tri(s, tri, t, x)) return;
+  long long imin = x.imin, imax = x.imax, jmin = x.jmin, jmax = x.jmax;
+  const double area = edge_fn(x.v0, x.v1, x.v2);
+  const bool unclamped = fabs(area) >= 1.e-16;
+  if (unclamped) {
+    const double xlo = fmin(x.v0.x, fmin(x.v1.x, x.v2.x)), xhi = fmax(x.v0.x, fmax(x.v1.x, x.v2.x));
+    const double ylo = fmin(x.v0.y, fmin(x.v1.y, x.v2.y)), yhi = fmax(x.v0.y, fmax(x.v1.y, x.v2.y));
+    const double mb = 1e-6 * ((xhi - xlo) + (yhi - ylo)) + 1e-14;
+    const long long W = s.width, H = s.height;
+    const double ia = ceil((0.5 + (xlo - mb)) * (double)W - 0.5 - 1e-6), ib = floor((0.5 + (xhi + mb)) * (double)W - 0.5 + 1e-6);
+    const double ja = ceil((0.5 + (ylo - mb)) * (double)H - 0.5 - 1e-6), jb = floor((0.5 + (yhi + mb)) * (double)H - 0.5 + 1e-6);
+    imin = max(imin, (long long)fmax(ia, -1.0));
+    imax = min(imax, (long long)fmin(ib, (double)W));
+    jmin = max(jmin, (long long)fmax(ja, -1.0));
+    jmax = min(jmax, (long long)fmin(jb, (double)H));
+  }
+  if (CHECK) {
+    for (long long j = x.jmin; j <= x.jmax; j++)
+      for (long long i = x.imin; i <= x.imax; i++) {
+        double w0, w1, w2;
+        if (exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2) && (i < imin || i > imax || j < jmin || j > jmax))
+          atomicAdd(checks + 2, 1u);
+      }
+  }
+  for (long long j = jmin; j <= jmax; j++)
+    for (long long i = imin; i <= imax; i++) {
+      double w0, w1, w2;
+      if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) continue;
+      slot_max(R.canvas + j * s.width + i, depth_key(exact_depth(x, w0, w1, w2)), order << 24);
+    }
+}
+
+template <bool CHECK>
 __global__ void __launch_bounds__(256)
-k_raster(SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri,
-         const double* __restrict__ xs, const double* __restrict__ ys, Slot* __restrict__ canvas,
-         unsigned long long order_base, unsigned rgb_in) {
+k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const unsigned* __restrict__ tri_cell,
+        TriDev tri, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
   const long long T_ = (long long)*total_p;
   const long long W = scene.width, H = scene.height;
-  const double cr = (double)((rgb_in >> 16) & 255), cg = (double)((rgb_in >> 8) & 255),
-               cb = (double)(rgb_in & 255);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
-       t += (long long)gridDim.x * blockDim.x) {
+  /* traverse front to back along z (the order of the emission index) so that
+     near surfaces raise the floors before far ones are classified */
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < T_; q += (long long)gridDim.x * blockDim.x) {
+    const long long t = scene.z_descending ? T_ - 1 - q : q;
     const unsigned meta = tri.meta[t];
     if (!(meta & kMetaRendered) || (meta & kMetaCulled)) continue;
-    d3 v0 = {tri.proj[0][t], tri.proj[1][t], tri.proj[2][t]};
-    d3 v1 = {tri.proj[3][t], tri.proj[4][t], tri.proj[5][t]};
-    d3 v2 = {tri.proj[6][t], tri.proj[7][t], tri.proj[8][t]};
-    /* render.c:81-89 */
-    const long long xmin = (long long)dsub(dmul(dadd(0.5, fmin(v0.x, fmin(v1.x, v2.x))), (double)W), 1.);
-    const long long xmax = (long long)dadd(dmul(dadd(0.5, fmax(v0.x, fmax(v1.x, v2.x))), (double)W), 1.);
-    const long long ymin = (long long)dsub(dmul(dadd(0.5, fmin(v0.y, fmin(v1.y, v2.y))), (double)H), 1.);
-    const long long ymax = (long long)dadd(dmul(dadd(0.5, fmax(v0.y, fmax(v1.y, v2.y))), (double)H), 1.);
-    const long long imin = min(W - 1, max(0LL, xmin)), imax = min(W - 1, max(0LL, xmax));
-    const long long jmin = min(H - 1, max(0LL, ymin)), jmax = min(H - 1, max(0LL, ymax));
-    const double area = edge_fn(v0, v1, v2);
-    const double area_inv = ddiv(1., area < 0. ? fmin(area, -1.e-16) : fmax(area, +1.e-16));
-    const d3 n0 = {tri.vn[0][t], tri.vn[1][t], tri.vn[2][t]};
-    const d3 n1 = {tri.vn[3][t], tri.vn[4][t], tri.vn[5][t]};
-    const d3 n2 = {tri.vn[6][t], tri.vn[7][t], tri.vn[8][t]};
-    const unsigned long long order = order_base + (unsigned long long)t;
+    float X[3], Y[3], Z[3];
+#pragma unroll
+    for (int v = 0; v < 3; v++) {
+      X[v] = tri.pf[3 * v][t];
+      Y[v] = tri.pf[3 * v + 1][t];
+      Z[v] = tri.pf[3 * v + 2][t];
+    }
+    const float eps = tri.perr[t], zr = tri.zrel[t];
+    const unsigned long long order = order_base + 12ULL * tri_cell[t] + ((meta >> kMetaRankShift) & 15);
+    /* inverse area (render.c:102-107) with its bound */
+    const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
+    const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
+    const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
+    float errA;
+    const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
+    const float rai = errA / (fabsf(A) - errA) + 1.1f * kU32;
+    /* regular: the reference's area is certainly not clamped to +-1e-16 and
+       its sign and size are known to within half; then every covered pixel
+       centre lies inside the triangle's extent (its weights are barycentric
+       up to the -1e-8 slack) */
+    const bool regular = isfinite(A) && isfinite(eps) && fabsf(A) - errA > 1e-15f && rai < 0.5f && eps < 1e-3f &&
+                         zr < 1e-3f;
+    const bool in_tiny = !regular;
+    const unsigned long long ti = append_slot(R.tiny_count, in_tiny);
+    if (in_tiny) {
+      if (ti < R.tiny_cap) R.tiny[ti] = (unsigned)t;
+      else tiny_triangle<false>(scene, tri, t, R, order, nullptr);
+      continue;
+    }
+    const float ai = 1.f / A;
+    const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
+    const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
+    const float mb = eps + 1e-6f * (xext + yext) + 1e-12f;
+    long long imin, imax, jmin, jmax;
+    centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
+    centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+    /* depth of any covered fragment: the harmonic mean of the vertex depths
+       with weights >= -1e-8 summing to 1, so within their range */
+    const float zmin = fminf(Z[0], fminf(Z[1], Z[2])), zmax = fmaxf(Z[0], fmaxf(Z[1], Z[2]));
+    const float m = zr + 4e-6f;
+    const float dlo = zmin - m * fabsf(zmin), dhi = zmax + m * fabsf(zmax);
+    ExactTri ex;
+    bool ex_ok = false;
+    if (CHECK) ex_ok = exact_tri(scene, tri, t, ex);
+    if (CHECK && ex_ok) {
+      /* every covered pixel of the reference's box must lie in the tight range */
+      for (long long j = ex.jmin; j <= ex.jmax; j++)
+        for (long long i = ex.imin; i <= ex.imax; i++) {
+          double w0, w1, w2;
+          if (exact_weights(ex, i, j, R.xs, R.ys, w0, w1, w2)) {
+            if (i < imin || i > imax || j < jmin || j > jmax) atomicAdd(checks + 2, 1u);
+            const double d = exact_depth(ex, w0, w1, w2);
+            if (!(d <= (double)dhi && d >= (double)dlo)) atomicAdd(checks + 4, 1u);
+          }
+        }
+    }
     for (long long j = jmin; j <= jmax; j++) {
+      const float py = R.ysf[j];
       for (long long i = imin; i <= imax; i++) {
-        const d3 v3 = {xs[i], ys[j], 0.};
-        const double w0 = dmul(area_inv, edge_fn(v1, v2, v3));
-        const double w1 = dmul(area_inv, edge_fn(v2, v0, v3));
-        const double w2 = dmul(area_inv, edge_fn(v0, v1, v3));
-        if (w0 < -1.e-8 || w1 < -1.e-8 || w2 < -1.e-8) continue;
-        const double dist0 = ddiv(1., dadd(dadd(ddiv(w0, v0.z), ddiv(w1, v1.z)), ddiv(w2, v2.z)));
-        const unsigned long long key = depth_key(dist0);
-        Slot* s = canvas + j * W + i;
-        const unsigned long long seen = *(volatile unsigned long long*)&s->hi;
-        if (key < seen) continue;
-        const d3 n = v_normalise(v_add(v_mul(w0, n0), v_add(v_mul(w1, n1), v_mul(w2, n2))));
-        const double factor = fmax(0.15, fabs(v_dot(n, scene.light)));
-        const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
-        const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
-        const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
-        slot_max(s, key, (order << 24) | (r8 << 16) | (g8 << 8) | b8);
+        const float px = R.xsf[i];
+        const float ep = 0.5f * kU32;
+        float e0, e1, e2;
+        const float w0 = ai * edge_eval(E0, px, py, ep, eps, e0);
+        const float w1 = ai * edge_eval(E1, px, py, ep, eps, e1);
+        const float w2 = ai * edge_eval(E2, px, py, ep, eps, e2);
+        const float k = fabsf(ai) * (1.f + rai);
+        const float ew0 = 1.25f * (k * e0 + fabsf(w0) * (rai + kU32)) + 1e-30f;
+        const float ew1 = 1.25f * (k * e1 + fabsf(w1) * (rai + kU32)) + 1e-30f;
+        const float ew2 = 1.25f * (k * e2 + fabsf(w2) * (rai + kU32)) + 1e-30f;
+        const bool out = (w0 + ew0 < kWOut) || (w1 + ew1 < kWOut) || (w2 + ew2 < kWOut);
+        const bool inside = !out && (w0 - ew0 > kWIn) && (w1 - ew1 > kWIn) && (w2 - ew2 > kWIn);
+        if (CHECK && ex_ok) {
+          double x0, x1, x2;
+          const bool cov = exact_weights(ex, i, j, R.xs, R.ys, x0, x1, x2);
+          if (cov && out) atomicAdd(checks + 2, 1u);     /* dropped a covered pixel */
+          if (!cov && inside) atomicAdd(checks + 3, 1u); /* called an uncovered pixel inside */
+        }
+        if (inside) atomicMax(R.zlo + j * W + i, f_key(dlo));
+        push_candidate(R, scene, tri, t, i, j, dhi, order, !out);
       }
     }
+  }
+}
+
+template <bool CHECK>
+__global__ void __launch_bounds__(256)
+k_tiny(SceneDev scene, const unsigned* __restrict__ tri_cell, TriDev tri, RasterDev R, unsigned long long order_base,
+       unsigned* __restrict__ checks) {
+  const unsigned long long n = min(*R.tiny_count, R.tiny_cap);
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const long long t = R.tiny[q];
+    const unsigned long long order = order_base + 12ULL * tri_cell[t] + ((tri.meta[t] >> kMetaRankShift) & 15);
+    tiny_triangle<CHECK>(scene, tri, t, R, order, checks);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* k_exact: the reference's arithmetic for the surviving candidates    */
+/* ------------------------------------------------------------------ */
+__global__ void __launch_bounds__(256)
+k_exact(SceneDev scene, const unsigned* __restrict__ tri_cell, TriDev tri, RasterDev R,
+        unsigned long long order_base) {
+  const unsigned long long n = min(*R.cand_count, R.cand_cap);
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const Candidate c = R.cand[q];
+    /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
+    if (f_key(c.dhi) < R.zlo[c.pixel]) continue;
+    const long long i = c.pixel % scene.width, j = c.pixel / scene.width;
+    const unsigned long long order = order_base + 12ULL * tri_cell[c.t] + ((tri.meta[c.t] >> kMetaRankShift) & 15);
+    exact_fragment(scene, tri, c.t, i, j, R, order);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* k_shade: colour of the pixels this slab won (render.c:137-159)       */
+/* ------------------------------------------------------------------ */
+__global__ void __launch_bounds__(256)
+k_shade(FieldDev F, SlabDev S, SceneDev scene, const unsigned* __restrict__ offsets,
+        const unsigned* __restrict__ tri_cell, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
+        unsigned long long order_base, unsigned rgb_in) {
+  const unsigned long long T_ = *total_p;
+  const long long W = scene.width, npx = scene.width * scene.height;
+  const long long ncx = F.nx - 1, ncy = F.ny - 1;
+  const double cr = (double)((rgb_in >> 16) & 255), cg = (double)((rgb_in >> 8) & 255),
+               cb = (double)(rgb_in & 255);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long lo = R.canvas[p].lo;
+    const unsigned long long order = lo >> 24;
+    /* did one of this slab's rendered slices win the pixel? */
+    if (order < order_base) continue;
+    const unsigned long long rel = order - order_base;
+    const unsigned long long cl = rel / 12;
+    if (cl >= (unsigned long long)(S.nslices * ncx * ncy)) continue;
+    const long long kk = S.kfirst + (long long)(cl / (unsigned long long)(ncx * ncy));
+    if (kk < S.krender0 || kk >= S.krender1) continue;
+    const long long t = (long long)offsets[cl] + (long long)(rel % 12);
+    if ((unsigned long long)t >= T_) continue;
+    ExactTri x;
+    double w0, w1, w2;
+    if (!exact_tri(scene, tri, t, x) || !exact_weights(x, p % W, p / W, R.xs, R.ys, w0, w1, w2)) continue;
+    const unsigned meta = tri.meta[t];
+    const long long c = (long long)cl;
+    const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, offsets, tri);
+    const d3 n1 = vertex_normal(c, (meta >> 5) & 31, ncx, ncy, offsets, tri);
+    const d3 n2 = vertex_normal(c, (meta >> 10) & 31, ncx, ncy, offsets, tri);
+    const d3 n = v_normalise(v_add(v_mul(w0, n0), v_add(v_mul(w1, n1), v_mul(w2, n2))));
+    const double factor = fmax(0.15, fabs(v_dot(n, scene.light)));
+    const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
+    const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
+    const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
+    R.canvas[p].lo = (lo & ~0xFFFFFFULL) | (r8 << 16) | (g8 << 8) | b8;
   }
 }
 
@@ -438,10 +833,12 @@ __global__ void k_lines(const LineSegDev* __restrict__ segs, int nseg, long long
   }
 }
 
-__global__ void k_canvas_init(Slot* canvas, long long n, unsigned long long hi, unsigned long long lo) {
+__global__ void k_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo) {
+  const unsigned floor_key = f_key(-__int_as_float(0x7f800000));
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     canvas[p].hi = hi;
     canvas[p].lo = lo;
+    zlo[p] = floor_key;
   }
 }
 
@@ -506,10 +903,15 @@ long long scan_tiles(long long n) { return (n + kScanTile) / kScanTile; }
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned* offsets, const unsigned* tri_cell, const unsigned long long* total,
-                 long long tri_bound, const TriDev& tri, cudaStream_t st) {
+                 long long tri_bound, const TriDev& tri, unsigned* checks, cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
-  if (F.is_f32) k_emit<float><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri);
-  else k_emit<double><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri);
+  if (checks) {
+    if (F.is_f32) k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
+    else k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
+  } else {
+    if (F.is_f32) k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
+    else k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
+  }
 }
 
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
@@ -518,11 +920,32 @@ void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets
   k_normals<<<g, 256, 0, st>>>(F, S, offsets, tri_cell, total, tri);
 }
 
-void launch_raster(const SceneDev& scene, const unsigned long long* total, long long tri_bound, const TriDev& tri,
-                   const double* xs, const double* ys, Slot* canvas, unsigned long long order_base, unsigned rgb,
-                   cudaStream_t st) {
+void launch_cover(const SceneDev& scene, const unsigned long long* total, long long tri_bound,
+                  const unsigned* tri_cell, const TriDev& tri, const RasterDev& R, unsigned long long order_base,
+                  unsigned* checks, cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
-  k_raster<<<g, 256, 0, st>>>(scene, total, tri, xs, ys, canvas, order_base, rgb);
+  if (checks) k_cover<true><<<g, 256, 0, st>>>(scene, total, tri_cell, tri, R, order_base, checks);
+  else k_cover<false><<<g, 256, 0, st>>>(scene, total, tri_cell, tri, R, order_base, checks);
+}
+
+void launch_tiny(const SceneDev& scene, long long tiny_bound, const unsigned* tri_cell, const TriDev& tri,
+                 const RasterDev& R, unsigned long long order_base, unsigned* checks, cudaStream_t st) {
+  const int g = grid_for(tiny_bound, 256, 8);
+  if (checks) k_tiny<true><<<g, 256, 0, st>>>(scene, tri_cell, tri, R, order_base, checks);
+  else k_tiny<false><<<g, 256, 0, st>>>(scene, tri_cell, tri, R, order_base, checks);
+}
+
+void launch_exact(const SceneDev& scene, long long cand_bound, const unsigned* tri_cell, const TriDev& tri,
+                  const RasterDev& R, unsigned long long order_base, cudaStream_t st) {
+  const int g = grid_for(cand_bound, 256, 8);
+  k_exact<<<g, 256, 0, st>>>(scene, tri_cell, tri, R, order_base);
+}
+
+void launch_shade(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned* offsets,
+                  const unsigned* tri_cell, const unsigned long long* total, const TriDev& tri, const RasterDev& R,
+                  unsigned long long order_base, unsigned rgb, cudaStream_t st) {
+  const int g = grid_for(scene.width * scene.height, 256, 8);
+  k_shade<<<g, 256, 0, st>>>(F, S, scene, offsets, tri_cell, total, tri, R, order_base, rgb);
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
@@ -530,8 +953,9 @@ void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Sl
   if (nseg > 0) k_lines<<<nseg, 128, 0, st>>>(segs, nseg, W, H, canvas, order_base);
 }
 
-void launch_canvas_init(Slot* canvas, long long n, unsigned long long hi, unsigned long long lo, cudaStream_t st) {
-  k_canvas_init<<<grid_for(n, 256, 8), 256, 0, st>>>(canvas, n, hi, lo);
+void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,
+                        cudaStream_t st) {
+  k_canvas_init<<<grid_for(n, 256, 8), 256, 0, st>>>(canvas, zlo, n, hi, lo);
 }
 
 void launch_resolve(const Slot* canvas, long long W, long long H, unsigned char* rgb, double* depth,

@@ -86,6 +86,40 @@ static SceneDev scene_dev(const HostScene &s) {
   d.lyy = h_dot(s.ly, s.ly);
   d.width = (long long)s.W;
   d.height = (long long)s.H;
+  /* single-precision projection constants (see project_f in kernels.cu) */
+  const V cam = s.cam, n = s.normal, lx = s.lx, ly = s.ly;
+  const double cm[3] = {cam.x, cam.y, cam.z}, nn[3] = {n.x, n.y, n.z}, ax[3] = {lx.x, lx.y, lx.z},
+               ay[3] = {ly.x, ly.y, ly.z};
+  d.f_cam_max = 0.f;
+  d.f_n1 = d.f_lx1 = d.f_lxm = d.f_ly1 = d.f_lym = 0.f;
+  for (int q = 0; q < 3; q++) {
+    d.f_cam[q] = (float)cm[q];
+    d.f_n[q] = (float)nn[q];
+    d.f_lx[q] = (float)ax[q];
+    d.f_ly[q] = (float)ay[q];
+    d.f_cam_max = std::max(d.f_cam_max, (float)fabs(cm[q]));
+    d.f_n1 += (float)fabs(nn[q]);
+    d.f_lx1 += (float)fabs(ax[q]);
+    d.f_ly1 += (float)fabs(ay[q]);
+    d.f_lxm = std::max(d.f_lxm, (float)fabs(ax[q]));
+    d.f_lym = std::max(d.f_lym, (float)fabs(ay[q]));
+  }
+  /* widen the norms by a few ulps so the bounds built from them stay upper bounds */
+  d.f_n1 *= 1.0001f;
+  d.f_lx1 *= 1.0001f;
+  d.f_ly1 *= 1.0001f;
+  d.f_lxm *= 1.0001f;
+  d.f_lym *= 1.0001f;
+  d.f_cam_max *= 1.0001f;
+  const V cc = h_sub(s.cam, s.center);
+  const double dq = d.d - d.nc;
+  d.f_ax = (float)(h_dot(cc, lx) / d.lxx);
+  d.f_bx = (float)(dq / d.lxx);
+  d.f_ay = (float)(h_dot(cc, ly) / d.lyy);
+  d.f_by = (float)(dq / d.lyy);
+  d.f_dq = (float)dq;
+  /* emission order is z-major: when the view points down z, high slices are near */
+  d.z_descending = (s.center.z - s.cam.z) < 0. ? 1 : 0;
   return d;
 }
 
@@ -251,6 +285,8 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
+  Buf zlo, xyf, cand, tiny, checks;
+  bool filter_check = false;
   HostBuf h_small, h_rgb, h_slots;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[8] = {};
   bool stage_timing = false;
@@ -285,7 +321,7 @@ static int ctx_init(Ctx &c) {
   }
   if (c.lut.ensure(sizeof(unsigned long long) * kLutEntries)) return 1;
   C3D_CUDA(cudaMemcpy(c.lut.p, lut.data(), sizeof(unsigned long long) * kLutEntries, cudaMemcpyHostToDevice));
-  if (c.h_small.ensure(64)) return 1;
+  if (c.h_small.ensure(128)) return 1;
   c.device = dev;
   c.ready = true;
   return 0;
@@ -347,16 +383,22 @@ struct FrameOut {
   DebugSink *sink = nullptr;
 };
 
-static const size_t kTriBytes = 21 * sizeof(double) + sizeof(unsigned);
+/* bytes per triangle of the slab arrays (see TriDev) */
+static const size_t kTriBytes = 12 * sizeof(double) + sizeof(unsigned) + 11 * sizeof(float);
+/* doubles per triangle of the inspection arrays: vertex normals, face normal, area */
+static const size_t kDbgDoubles = 13;
 
 static TriDev tri_layout(void *base, size_t cap, double *dbg) {
   TriDev t;
   double *d = static_cast<double *>(base);
-  for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
-  for (int q = 0; q < 9; q++) t.proj[q] = d + (3 + q) * cap;
-  for (int q = 0; q < 9; q++) t.vn[q] = d + (12 + q) * cap;
-  t.meta = reinterpret_cast<unsigned *>(d + 21 * cap);
-  t.dbg_vert = dbg;
+  for (int q = 0; q < 9; q++) t.vert[q] = d + q * cap;
+  for (int q = 0; q < 3; q++) t.wn[q] = d + (9 + q) * cap;
+  float *f = reinterpret_cast<float *>(d + 12 * cap);
+  for (int q = 0; q < 9; q++) t.pf[q] = f + q * cap;
+  t.perr = f + 9 * cap;
+  t.zrel = f + 10 * cap;
+  t.meta = reinterpret_cast<unsigned *>(f + 11 * cap);
+  for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + q * cap : nullptr;
   t.dbg_fn = dbg ? dbg + 9 * cap : nullptr;
   t.dbg_area = dbg ? dbg + 12 * cap : nullptr;
   return t;
@@ -370,7 +412,7 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 /* one contour object through all of its slabs */
 static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn &ci,
-                          unsigned long long &order_base, const double *xs, const double *ys, DebugSink *sink) {
+                          unsigned long long &order_base, const RasterDev &R, DebugSink *sink) {
   cudaStream_t st = f.stream;
   const long long nx = (long long)ci.sz[0], ny = (long long)ci.sz[1], nz = (long long)ci.sz[2];
   if (nx < 2 || ny < 2 || nz < 2) return 0;
@@ -431,16 +473,22 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   c.stats.cells += (uint64_t)(ncx * ncy * ncz);
 
   /* rendered cell slices are [1, ncz - 2]; each slab also triangulates one
-     slice below and above for the vertex normals (contour/main.c:49-112) */
+     slice below and above for the vertex normals (contour/main.c:49-112).
+     Slabs are visited front to back (the z-buffer result does not depend on
+     the order: fragments carry their position in the reference's drawing
+     sequence), except for inspection, which reports triangles in order. */
   const long long per_slice = ncx * ncy;
   long long slab_slices = (long long)(c.slab_cells / (unsigned long long)per_slice) - 2;
   if (slab_slices < 1) slab_slices = 1;
   const bool want_all = sink != nullptr;
-  /* a debug pass also counts the triangulated set over every slice */
   const long long kr0 = want_all ? 0 : 1, kr1 = want_all ? ncz : ncz - 1;
+  std::vector<long long> starts;
+  for (long long k0 = kr0; k0 < kr1; k0 += slab_slices) starts.push_back(k0);
+  if (sd.z_descending && !want_all) std::reverse(starts.begin(), starts.end());
   unsigned *h_small = c.h_small.as<unsigned>();
   unsigned long long *h_total = reinterpret_cast<unsigned long long *>(h_small + 4);
-  for (long long k0 = kr0; k0 < kr1; k0 += slab_slices) {
+  const unsigned rgb = ((unsigned)ci.color.r << 16) | ((unsigned)ci.color.g << 8) | ci.color.b;
+  for (const long long k0 : starts) {
     const long long k1 = std::min(k0 + slab_slices, kr1);
     SlabDev S;
     S.kfirst = std::max(k0 - 1, 0LL);
@@ -486,40 +534,67 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     const size_t cap = c.tri.cap / kTriBytes;
     double *dbg = nullptr;
     if (sink) {
-      if (c.dbg.ensure(sizeof(double) * 13 * cap)) return 1;
+      if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap)) return 1;
       dbg = c.dbg.as<double>();
     }
     const TriDev tri = tri_layout(c.tri.p, cap, dbg);
+    unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
     launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
     if (c.stage_timing) cudaEventRecord(c.evs[3], st);
     launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total,
-                (long long)T, tri, st);
+                (long long)T, tri, checks, st);
     if (c.stage_timing) cudaEventRecord(c.evs[4], st);
-    launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
-    if (c.stage_timing) cudaEventRecord(c.evs[5], st);
-    c.stats.kernel_launches += 3;
-    if (!(sink && sink->triangulated_only)) {
-      launch_raster(sd, d_total, (long long)T, tri, xs, ys, c.canvas.as<Slot>(), order_base,
-                    ((unsigned)ci.color.r << 16) | ((unsigned)ci.color.g << 8) | ci.color.b, st);
+    c.stats.kernel_launches += 2;
+    const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
+    if (sink) {
+      launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
       c.stats.kernel_launches += 1;
+    } else {
+      /* candidates: about one per covered pixel; the list falls back to in-place
+         resolution when full, so its size only affects speed */
+      const unsigned long long want = std::max<unsigned long long>(2ULL * T, 1ULL << 20);
+      if (c.cand.ensure(sizeof(Candidate) * want)) return 1;
+      const unsigned long long tiny_want = std::max<unsigned long long>(T / 8, 1ULL << 16);
+      if (c.tiny.ensure(sizeof(unsigned) * tiny_want)) return 1;
+      RasterDev RS = R;
+      RS.cand = c.cand.as<Candidate>();
+      RS.cand_cap = c.cand.cap / sizeof(Candidate);
+      RS.cand_count = reinterpret_cast<unsigned long long *>(d_counter + 4);
+      RS.tiny = c.tiny.as<unsigned>();
+      RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
+      RS.tiny_count = reinterpret_cast<unsigned long long *>(d_counter + 6);
+      C3D_CUDA(cudaMemsetAsync(RS.cand_count, 0, 2 * sizeof(unsigned long long), st));
+      launch_cover(sd, d_total, (long long)T, c.tri_cell.as<unsigned>(), tri, RS, slab_order, checks, st);
+      launch_tiny(sd, (long long)RS.tiny_cap, c.tri_cell.as<unsigned>(), tri, RS, slab_order, checks, st);
+      c.stats.kernel_launches += 1;
+      if (c.stage_timing) cudaEventRecord(c.evs[5], st);
+      launch_exact(sd, (long long)RS.cand_cap, c.tri_cell.as<unsigned>(), tri, RS, slab_order, st);
+      if (c.stage_timing) cudaEventRecord(c.evs[6], st);
+      launch_shade(F, S, sd, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, tri, RS, slab_order, rgb, st);
+      c.stats.kernel_launches += 3;
+      if (c.stage_timing) cudaEventRecord(c.evs[7], st);
+      unsigned long long *h_cand = h_total + 1;
+      C3D_CUDA(cudaMemcpyAsync(h_cand, RS.cand_count, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaStreamSynchronize(st));
+      c.stats.candidates += h_cand[0];
+      c.stats.tiny += h_cand[1];
+      if (*h_cand > RS.cand_cap) c.stats.candidate_overflows += *h_cand - RS.cand_cap;
+      if (c.stage_timing) {
+        c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
+        c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);
+        c.stats.ms_exact += elapsed(c.evs[5], c.evs[6]);
+        c.stats.ms_shade += elapsed(c.evs[6], c.evs[7]);
+      }
     }
-    if (c.stage_timing) {
-      cudaEventRecord(c.evs[6], st);
-      C3D_CUDA(cudaEventSynchronize(c.evs[6]));
-      c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
-      c.stats.ms_normals += elapsed(c.evs[4], c.evs[5]);
-      c.stats.ms_raster += elapsed(c.evs[5], c.evs[6]);
-    }
-    order_base += T;
     if (sink) {
       /* copy this slab's triangles back and keep the rendered ones in order */
       std::vector<unsigned> meta(T), cellv(T);
-      std::vector<double> vn(9 * T), dv(13 * cap);
+      std::vector<double> vert(9 * T), dv(kDbgDoubles * cap);
       C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
       for (int q = 0; q < 9; q++)
-        C3D_CUDA(cudaMemcpyAsync(vn.data() + q * T, tri.vn[q], sizeof(double) * T, cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * 13 * cap, cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaMemcpyAsync(vert.data() + q * T, tri.vert[q], sizeof(double) * T, cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * kDbgDoubles * cap, cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
       for (unsigned long long t = 0; t < T; t++) {
         const long long cl = cellv[t];
@@ -528,8 +603,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         if (!(meta[t] & kMetaRendered)) continue;
         if (sink->out && sink->count < sink->capacity) {
           TriRecord &r = sink->out[sink->count];
-          for (int q = 0; q < 9; q++) r.vertices[q] = dv[9 * t + q];
-          for (int q = 0; q < 9; q++) r.vertex_normals[q] = vn[q * T + t];
+          for (int q = 0; q < 9; q++) r.vertices[q] = vert[q * T + t];
+          for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[q * cap + t];
           for (int q = 0; q < 3; q++) r.face_normal[q] = dv[9 * cap + 3 * t + q];
           r.area = dv[12 * cap + t];
           r.cell[0] = i + (long long)ci.off[0];
@@ -541,6 +616,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       }
     }
   }
+  order_base += 12ULL * (unsigned long long)(ncx * ncy * ncz);
   return 0;
 }
 
@@ -610,16 +686,28 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   std::vector<double> xy(W + H);
   for (size_t i = 0; i < W; i++) xy[i] = 1. * (i + 0.5) / W - 0.5;
   for (size_t j = 0; j < H; j++) xy[W + j] = 1. * (j + 0.5) / H - 0.5;
-  if (c.xy.ensure(sizeof(double) * (W + H)) || c.canvas.ensure(sizeof(Slot) * npx)) return 1;
+  std::vector<float> xyf(W + H);
+  for (size_t q = 0; q < W + H; q++) xyf[q] = (float)xy[q];
+  if (c.xy.ensure(sizeof(double) * (W + H)) || c.xyf.ensure(sizeof(float) * (W + H)) ||
+      c.canvas.ensure(sizeof(Slot) * npx) || c.zlo.ensure(sizeof(unsigned) * npx) || c.checks.ensure(64))
+    return 1;
   C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy.data(), sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
-  const double *xs = c.xy.as<double>(), *ys = xs + W;
-  /* canvas: background colour at depth -DBL_MAX (main.c:90-103) */
+  C3D_CUDA(cudaMemcpyAsync(c.xyf.p, xyf.data(), sizeof(float) * (W + H), cudaMemcpyHostToDevice, st));
+  if (c.filter_check) C3D_CUDA(cudaMemsetAsync(c.checks.p, 0, 64, st));
+  RasterDev R = {};
+  R.canvas = c.canvas.as<Slot>();
+  R.zlo = c.zlo.as<unsigned>();
+  R.xs = c.xy.as<double>();
+  R.ys = R.xs + W;
+  R.xsf = c.xyf.as<float>();
+  R.ysf = R.xsf + W;
+  /* canvas: background colour at depth -DBL_MAX (main.c:90-103); depth floors at -inf */
   const unsigned bg = ((unsigned)f.bg.r << 16) | ((unsigned)f.bg.g << 8) | f.bg.b;
-  launch_canvas_init(c.canvas.as<Slot>(), (long long)npx, h_depth_key(-1. * DBL_MAX), bg, st);
+  launch_canvas_init(c.canvas.as<Slot>(), R.zlo, (long long)npx, h_depth_key(-1. * DBL_MAX), bg, st);
   c.stats.kernel_launches += 1;
   unsigned long long order_base = 1;
   for (size_t n = 0; n < f.contours.size(); n++) {
-    if (render_contour(c, f, sd, f.contours[n], order_base, xs, ys, o.sink)) {
+    if (render_contour(c, f, sd, f.contours[n], order_base, R, o.sink)) {
       log_error("contour processing failed");
       return 1;
     }
@@ -644,9 +732,13 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     C3D_CUDA(cudaMemcpyAsync(c.h_slots.p, c.canvas.p, sizeof(Slot) * npx, cudaMemcpyDeviceToHost, st));
   }
   C3D_CUDA(cudaEventRecord(c.ev1, st));
+  unsigned h_checks[5] = {0, 0, 0, 0, 0};
+  if (c.filter_check)
+    C3D_CUDA(cudaMemcpyAsync(h_checks, c.checks.p, sizeof h_checks, cudaMemcpyDeviceToHost, st));
   C3D_CUDA(cudaStreamSynchronize(st));
   C3D_CUDA(cudaGetLastError());
   c.stats.ms_total = elapsed(c.ev0, c.ev1);
+  for (int q = 0; q < 5; q++) c.stats.filter_violations[q] = h_checks[q];
   if (o.rgb_host) memcpy(o.rgb_host, c.h_rgb.p, 3 * npx);
   if (o.depth_host || o.pixels_host) {
     const Slot *sl = c.h_slots.as<Slot>();
@@ -922,6 +1014,12 @@ extern "C" int contour3d_gb300_set_stage_timing(int on) {
   return 0;
 }
 
+extern "C" int contour3d_gb300_set_filter_check(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_ctx.filter_check = on != 0;
+  return 0;
+}
+
 extern "C" int contour3d_gb300_set_slab_cells(uint64_t max_cells) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (max_cells < 64) {
@@ -949,11 +1047,10 @@ extern "C" long contour3d_gb300_debug_triangles(const contour3d_contour_obj_t *o
   sink.out = static_cast<TriRecord *>(out);
   sink.capacity = out ? capacity : 0;
   sink.triangulated_only = true;
-  if (g_ctx.canvas.ensure(sizeof(Slot)) || g_ctx.xy.ensure(16)) return -1;
   const SceneDev sd = scene_dev(f.scene);
   unsigned long long order = 1;
-  if (render_contour(g_ctx, f, sd, f.contours[0], order, g_ctx.xy.as<double>(), g_ctx.xy.as<double>() + 1, &sink))
-    return -1;
+  RasterDev R = {};
+  if (render_contour(g_ctx, f, sd, f.contours[0], order, R, &sink)) return -1;
   if (num_triangulated) *num_triangulated = sink.triangulated;
   return sink.count;
 }
@@ -994,7 +1091,8 @@ extern "C" int contour3d_gb300_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx &c = g_ctx;
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs};
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.tiny,
+                 &c.checks};
   for (Buf *b : bufs) b->release();
   c.h_small.release();
   c.h_rgb.release();

@@ -20,10 +20,11 @@ class NativeLibraryMissing(RuntimeError):
 
 
 class Stats(C.Structure):
-    _fields_ = [("cells", C.c_uint64), ("triangles", C.c_uint64), ("rendered", C.c_uint64),
-                ("slabs", C.c_uint64), ("kernel_launches", C.c_uint64), ("ms_total", C.c_double),
-                ("ms_classify", C.c_double), ("ms_scan", C.c_double), ("ms_emit", C.c_double),
-                ("ms_normals", C.c_double), ("ms_raster", C.c_double)]
+    _fields_ = [("cells", C.c_uint64), ("triangles", C.c_uint64), ("candidates", C.c_uint64),
+                ("candidate_overflows", C.c_uint64), ("tiny", C.c_uint64), ("slabs", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("ms_total", C.c_double), ("ms_classify", C.c_double), ("ms_scan", C.c_double),
+                ("ms_emit", C.c_double), ("ms_cover", C.c_double), ("ms_exact", C.c_double),
+                ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5)]
 
 
 class Field(C.Structure):
@@ -39,7 +40,7 @@ F64, F32 = 0, 1
 EXPORTS = [
     "contour3d_execute", "contour3d_gb300_identity", "contour3d_gb300_declare_identity",
     "contour3d_gb300_render", "contour3d_gb300_render_device", "contour3d_gb300_last_stats",
-    "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells",
+    "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells", "contour3d_gb300_set_filter_check",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
     "contour3d_gb300_cell_offsets_noalloc",
@@ -127,6 +128,9 @@ class Library:
 
     def set_stage_timing(self, on: bool) -> None:
         self.lib.contour3d_gb300_set_stage_timing(1 if on else 0)
+
+    def set_filter_check(self, on: bool) -> None:
+        self.lib.contour3d_gb300_set_filter_check(1 if on else 0)
 
     def set_slab_cells(self, n: int) -> int:
         return self.lib.contour3d_gb300_set_slab_cells(C.c_uint64(n))

@@ -117,20 +117,34 @@ int contour3d_gb300_cell_offsets_noalloc(const void *device_field, int dtype, co
                                          double threshold, uint32_t *device_offsets,
                                          unsigned long long *device_total, void *stream);
 
-/* per-call statistics of the last render on this thread */
+/* statistics of the last render call */
 typedef struct {
   uint64_t cells;             /* cells classified (cell x threshold) */
   uint64_t triangles;         /* triangles emitted (triangulated set, all slabs) */
-  uint64_t rendered;          /* triangles in the rendered (interior) set */
+  uint64_t candidates;        /* fragments the single-precision filter could not settle */
+  uint64_t candidate_overflows; /* of those, resolved in place because the list was full */
+  uint64_t tiny;              /* triangles too small for the FP32 filter (resolved in FP64) */
   uint64_t slabs;             /* slab passes */
   uint64_t kernel_launches;   /* kernels launched by the library */
   double ms_total;            /* device time of the whole frame (events) */
-  double ms_classify, ms_scan, ms_emit, ms_normals, ms_raster; /* per stage, when timing is on */
+  /* per stage, when stage timing is on */
+  double ms_classify, ms_scan, ms_emit, ms_cover, ms_exact, ms_shade;
+  /* self-check counters when the filter check is on (all must stay 0):
+     [0] projection cull decided wrongly, [1] projection outside its bound,
+     [2] covered pixel dropped, [3] uncovered pixel called inside,
+     [4] depth outside its interval */
+  uint64_t filter_violations[5];
 } contour3d_gb300_stats_t;
 
 int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);
 /* 1 = record per-stage CUDA events (adds synchronisation), 0 = off (default) */
 int contour3d_gb300_set_stage_timing(int on);
+/*
+ * 1 = also run the reference's FP64 arithmetic for every pixel the
+ * single-precision filter classifies and count disagreements with its
+ * certified bounds (slow; for tests), 0 = off (default)
+ */
+int contour3d_gb300_set_filter_check(int on);
 /* upper bound on cells per slab (default 2^27); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);
 

@@ -153,3 +153,31 @@ def test_device_field_generator_matches_host(gpu):
     db = torch.empty(shape, dtype=torch.float64, device="cuda")
     gpu.fieldgen_blobs_device(db.data_ptr(), shape, 7, 8)
     assert db.cpu().numpy().tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("name", sorted(cases.SMALL_CASES) + ["config0"])
+def test_single_precision_filter_bounds_hold(gpu, name):
+    """With the self-check on, every pixel the FP32 filter classifies is also
+    classified with the reference's FP64 arithmetic: no certain decision may
+    disagree, no depth may leave its interval, and the image is unchanged."""
+    scene = cases.config0() if name == "config0" else cases.SMALL_CASES[name]()
+    gpu.set_filter_check(True)
+    try:
+        img = gpu.render(scene)
+        st = gpu.stats()
+    finally:
+        gpu.set_filter_check(False)
+    assert list(st.filter_violations) == [0, 0, 0, 0, 0]
+    if name == "config0":
+        assert sha(img.tobytes()) == MANIFEST["config0"]["ppm_sha256"]
+    else:
+        assert np.array_equal(img, np.load(os.path.join(GOLDEN, f"{name}.npz"))["rgb"])
+
+
+def test_filter_settles_most_fragments(gpu):
+    """The FP32 filter must leave only a small share of fragments to the exact path."""
+    scene = cases.config0()
+    gpu.render(scene)
+    st = gpu.stats()
+    assert st.candidate_overflows == 0
+    assert 0 < st.candidates < 4 * st.triangles
