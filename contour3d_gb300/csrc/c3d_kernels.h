@@ -36,19 +36,31 @@ struct SlabDev {
 
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {
-  double* vert[9];    /* world vertices (x, y, z) x 3, rendered triangles */
-  double* wn[3];      /* area * face normal */
+  double* wn[3];      /* area * face normal, where requested */
   unsigned* meta;     /* edge ids (3 x 5 bits) | flags | rank in the cell */
   float* pf[9];       /* FP32 screen position and depth x 3, rendered triangles */
   float* perr;        /* bound on |screen x, y - the reference's value| */
   float* zrel;        /* relative bound on the depth */
-  double* vn[9];      /* optional (inspection): vertex normals x 3 */
-  double* dbg_fn;     /* optional: face normals, 3 per triangle */
-  double* dbg_area;   /* optional: areas */
+  unsigned* need;     /* 1 once the weighted normal was requested */
+  double* vert[9];    /* inspection: exact vertices */
+  double* vn[9];      /* inspection: vertex normals */
+  double* dbg_fn;     /* inspection: face normals, 3 per triangle */
+  double* dbg_area;   /* inspection: areas */
 };
 constexpr unsigned kMetaRendered = 1u << 15;
 constexpr unsigned kMetaCulled = 1u << 16;
 constexpr unsigned kMetaRankShift = 17;
+constexpr unsigned kMetaUndecided = 1u << 21;
+
+/* what the exact path needs to rebuild a triangle from the field */
+struct Geo {
+  FieldDev F;
+  SlabDev S;
+  const unsigned long long* lut;
+  const unsigned* tri_cell;
+  const unsigned* offsets;
+  const unsigned* meta;
+};
 
 /* a fragment that k_exact resolves with the reference's arithmetic */
 struct Candidate {
@@ -72,6 +84,10 @@ struct RasterDev {
   unsigned* tiny;           /* triangles the FP32 filter cannot settle */
   unsigned long long tiny_cap;
   unsigned long long* tiny_count;
+  uint2* win;               /* (pixel, triangle) won by the current slab */
+  unsigned long long* win_count;
+  unsigned* need;           /* triangles whose weighted normal shading needs */
+  unsigned long long* need_count;
 };
 
 /* one line segment, already projected to pixel units on the host */
@@ -97,18 +113,20 @@ void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_ce
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned* offsets, const unsigned* tri_cell, const unsigned long long* total,
                  long long tri_bound, const TriDev& tri, unsigned* checks, cudaStream_t st);
+void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
+                      cudaStream_t st);
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st);
-void launch_cover(const SceneDev& scene, const unsigned long long* total, long long tri_bound,
-                  const unsigned* tri_cell, const TriDev& tri, const RasterDev& R, unsigned long long order_base,
-                  unsigned* checks, cudaStream_t st);
-void launch_tiny(const SceneDev& scene, long long tiny_bound, const unsigned* tri_cell, const TriDev& tri,
-                 const RasterDev& R, unsigned long long order_base, unsigned* checks, cudaStream_t st);
-void launch_exact(const SceneDev& scene, long long cand_bound, const unsigned* tri_cell, const TriDev& tri,
-                  const RasterDev& R, unsigned long long order_base, cudaStream_t st);
-void launch_shade(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned* offsets,
-                  const unsigned* tri_cell, const unsigned long long* total, const TriDev& tri, const RasterDev& R,
-                  unsigned long long order_base, unsigned rgb, cudaStream_t st);
+void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
+                  const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned* checks,
+                  cudaStream_t st);
+void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
+                 unsigned long long order_base, unsigned* checks, cudaStream_t st);
+void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
+                  unsigned long long order_base, cudaStream_t st);
+void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
+                    const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
+                    cudaStream_t st);
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, cudaStream_t st);
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,

@@ -5,26 +5,32 @@
  *   k_classify   cell codes -> triangle count per cell          (HBM: field read)
  *   k_scan       decoupled-look-back exclusive scan of the counts, writing
  *                per-cell offsets and the triangle -> cell map
- *   k_emit       one thread per triangle: vertices, face normal, weighted
- *                normal, cube-edge ids (FP64, the reference's arithmetic);
- *                screen projection in FP32 with certified bounds
+ *   k_emit       one thread per triangle: cube-edge ids; for rendered
+ *                triangles the vertices and their screen projection in FP32
+ *                with certified bounds (two FP64 subtractions per vertex)
  *   k_cover      one thread per rendered triangle: FP32 coverage and depth
  *                intervals over its bounding box; certainly drawn fragments
  *                raise a per-pixel depth floor, the rest become candidates
+ *   k_tiny       one thread per triangle too small for FP32 bounds: the
+ *                reference's arithmetic for its few possible pixels
  *   k_exact      one thread per candidate that can still reach the floor:
- *                the reference's projection, barycentric test and harmonic
- *                depth in FP64, then a 128-bit (depth, order) max into the
- *                z-buffer
- *   k_shade      one thread per pixel: for pixels this slab won, the vertex
- *                normals of the winning triangle (area-weighted over the
- *                cells sharing each cube edge) and the shading
- * and once per frame k_canvas_init, k_lines and k_resolve.  k_normals
- * computes every rendered triangle's vertex normals for inspection only.
+ *                the reference's vertices (recomputed from the field),
+ *                projection, barycentric test and harmonic depth in FP64,
+ *                then a 128-bit (depth, order) max into the z-buffer
+ *   k_winners    one thread per pixel: the pixels this slab won, and the
+ *                triangles sharing a cube edge with their vertices
+ *   k_wn         one thread per such triangle: its exact area-weighted
+ *                face normal
+ *   k_shade      one thread per won pixel: vertex normals (normal.c order)
+ *                and the shading
+ * and once per frame k_canvas_init, k_lines and k_resolve.  k_exact_all and
+ * k_normals compute every triangle's exact data for inspection only.
  *
  * The FP64 work runs one item per thread on compacted lists so that warps
  * stay converged: on GB300 an FP64 warp instruction costs the same whether 2
- * or 32 lanes are active.  Vertex normals are needed only for the triangle
- * that finally owns a pixel, so they are computed for those alone.
+ * or 32 lanes are active.  Exact vertices are needed only for fragments that
+ * can win, and weighted normals only around the triangles that finally own a
+ * pixel, so they are computed for those alone.
  *
  * Reference correspondence (file:line of the reference tree):
  *   k_classify/k_emit  src/contour3d/contour/triangulate.c:95-342
@@ -227,7 +233,7 @@ k_fill_tri_cell(const unsigned* __restrict__ offsets, long long n, unsigned* __r
 }
 
 /* ------------------------------------------------------------------ */
-/* k_emit                                                              */
+/* exact triangles on demand (triangulate.c:40-93)                      */
 /* ------------------------------------------------------------------ */
 __device__ __forceinline__ d3 corner_pos(const FieldDev& F, long long i, long long j, long long k, int c) {
   const long long ii = i + (c & 1), jj = j + ((c >> 1) & 1), kk = k + (c >> 2);
@@ -246,30 +252,105 @@ __device__ __forceinline__ d3 interpolate(double vt, d3 p0, double v0, d3 p1, do
   return v_add(p0, v_mul(f, v_sub(p1, p0)));
 }
 
+/* corner values and code of cell (i, j, k), element type chosen at run time */
+__device__ __forceinline__ unsigned cell_code_any(const FieldDev& F, long long i, long long j, long long k,
+                                                  double vals[8]) {
+  return F.is_f32 ? cell_code<float>(F, i, j, k, vals) : cell_code<double>(F, i, j, k, vals);
+}
+
 /*
- * Screen projection of a world point in single precision, with bounds.
- * Uses the identity (exact in real arithmetic) of project.c:9-67
- *   x = [(cam - centre) . lx + D (q . lx) / (n . q)] / (lx . lx),  q = p - cam,
- *   D = n . centre - n . cam,  depth = n . q,  t = D / (n . q)
- * q is formed in FP64 (as the reference forms `ray`) and rounded once; each
- * FP32 dot product a . q is then within 5.2 u sum|a_i q_i| of the real one
- * (rounding of q, of a, and three operations).
- * Returns 1 = certainly projects, 0 = certainly fails (render.c:62-72
- * drops the triangle), -1 = too close to a threshold of project.c:39-46.
+ * The reference's triangle (vertices in winding order) for emission index t
+ * of the slab, recomputed from the field: the same operations as k_emit's
+ * FP32 estimate stands for.  Returns the cube-edge ids in *edges.
  */
-__device__ __forceinline__ int project_f(const SceneDev& s, d3 qd, float& X, float& Y, float& Z, float& exy,
-                                         float& ez) {
-  const float qx = to_f(qd.x), qy = to_f(qd.y), qz = to_f(qd.z);
-  const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
-  const float nq = s.f_n[0] * qx + s.f_n[1] * qy + s.f_n[2] * qz;
-  const float lq = s.f_lx[0] * qx + s.f_lx[1] * qy + s.f_lx[2] * qz;
-  const float mq = s.f_ly[0] * qx + s.f_ly[1] * qy + s.f_ly[2] * qz;
-  const float e_nq = 5.2f * kU32 * (fabsf(s.f_n[0]) * ax + fabsf(s.f_n[1]) * ay + fabsf(s.f_n[2]) * az);
-  const float e_lq = 5.2f * kU32 * (fabsf(s.f_lx[0]) * ax + fabsf(s.f_lx[1]) * ay + fabsf(s.f_lx[2]) * az);
-  const float e_mq = 5.2f * kU32 * (fabsf(s.f_ly[0]) * ax + fabsf(s.f_ly[1]) * ay + fabsf(s.f_ly[2]) * az);
+__device__ __forceinline__ void exact_vertices(const Geo& G, long long t, d3 v[3]) {
+  const unsigned c = G.tri_cell[t];
+  const unsigned r = (G.meta[t] >> kMetaRankShift) & 15;
+  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
+  const long long i = c % ncx, j = (c / ncx) % ncy, k = G.S.kfirst + c / (ncx * ncy);
+  double val[8];
+  const unsigned code = cell_code_any(G.F, i, j, k, val);
+  const unsigned long long e = __ldg(G.lut + code * 12 + r);
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+    v[q] = interpolate(G.F.threshold, corner_pos(G.F, i, j, k, a), val[a], corner_pos(G.F, i, j, k, b), val[b]);
+  }
+}
+
+/* triangulate.c:75-93 and normal.c:39-40: face normal, area, area * face normal */
+__device__ __forceinline__ void face_normal(const d3 v[3], d3& fn, double& area, d3& wn) {
+  fn = v_cross(v_sub(v[1], v[0]), v_sub(v[2], v[0]));
+  area = dsqrt(v_dot(fn, fn));
+  fn = v_mul(ddiv(1., area), fn);
+  wn = v_mul(area, fn);
+}
+
+/* ------------------------------------------------------------------ */
+/* k_emit: single-precision triangles with certified bounds             */
+/* ------------------------------------------------------------------ */
+/*
+ * FP32 estimate of one vertex (triangulate.c:40-73) relative to the camera,
+ * q = vertex - camera, with a bound per component on the distance to the
+ * reference's FP64 value.  Only the two value differences are formed in FP64
+ * (they cancel); everything else is single precision:
+ *   f = (vt - v0) / (v1 - v0)          relative error <= 3.1 u
+ *   p = p0 + f (p1 - p0)               per component, bounded below
+ */
+__device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, d3 p0, double v0, d3 p1, double v1, float q[3],
+                                         float eq[3]) {
+  const double dv = dsub(v1, v0);
+  const float pc[3] = {s.f_cam[0], s.f_cam[1], s.f_cam[2]};
+  const double a0[3] = {p0.x, p0.y, p0.z}, a1[3] = {p1.x, p1.y, p1.z};
+  if (abs_lt_1e8(dv)) {
+    /* the reference keeps p0 itself */
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float p = to_f(a0[i]);
+      q[i] = p - pc[i];
+      eq[i] = 1.1f * kU32 * (fabsf(p) + fabsf(pc[i]) + fabsf(q[i])) + 1e-30f;
+    }
+    return;
+  }
+  const float f = to_f(dsub(vt, v0)) / to_f(dv);
+  const float af = fabsf(f);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float x0 = to_f(a0[i]), x1 = to_f(a1[i]);
+    const float d = x1 - x0;
+    const float p = x0 + f * d;
+    q[i] = p - pc[i];
+    const float ep = kU32 * (fabsf(x0) + fabsf(p) + af * (fabsf(x0) + fabsf(x1) + 5.1f * fabsf(d)));
+    eq[i] = 1.1f * (ep + kU32 * (fabsf(pc[i]) + fabsf(q[i]))) + 1e-30f;
+  }
+}
+
+/*
+ * Screen projection in single precision from q (bounded per component).
+ * Uses the identity (exact in real arithmetic) of project.c:9-67
+ *   x = [(cam - centre) . lx + D (q . lx) / (n . q)] / (lx . lx),
+ *   D = n . centre - n . cam,  depth = n . q,  t = D / (n . q)
+ * Each FP32 dot product a . q is within sum|a_i| eq_i + 4.2 u sum|a_i q_i|
+ * of the real one.  Returns 1 = certainly projects, 0 = certainly fails
+ * (render.c:62-72 drops the triangle), -1 = too close to a threshold of
+ * project.c:39-46.
+ */
+__device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], const float eq[3], float& X, float& Y,
+                                         float& Z, float& exy, float& ez) {
+  const float ax = fabsf(q[0]), ay = fabsf(q[1]), az = fabsf(q[2]);
+  const float nq = s.f_n[0] * q[0] + s.f_n[1] * q[1] + s.f_n[2] * q[2];
+  const float lq = s.f_lx[0] * q[0] + s.f_lx[1] * q[1] + s.f_lx[2] * q[2];
+  const float mq = s.f_ly[0] * q[0] + s.f_ly[1] * q[1] + s.f_ly[2] * q[2];
+  const float e_nq = fabsf(s.f_n[0]) * eq[0] + fabsf(s.f_n[1]) * eq[1] + fabsf(s.f_n[2]) * eq[2] +
+                     4.2f * kU32 * (fabsf(s.f_n[0]) * ax + fabsf(s.f_n[1]) * ay + fabsf(s.f_n[2]) * az);
+  const float e_lq = fabsf(s.f_lx[0]) * eq[0] + fabsf(s.f_lx[1]) * eq[1] + fabsf(s.f_lx[2]) * eq[2] +
+                     4.2f * kU32 * (fabsf(s.f_lx[0]) * ax + fabsf(s.f_lx[1]) * ay + fabsf(s.f_lx[2]) * az);
+  const float e_mq = fabsf(s.f_ly[0]) * eq[0] + fabsf(s.f_ly[1]) * eq[1] + fabsf(s.f_ly[2]) * eq[2] +
+                     4.2f * kU32 * (fabsf(s.f_ly[0]) * ax + fabsf(s.f_ly[1]) * ay + fabsf(s.f_ly[2]) * az);
   const float anq = fabsf(nq);
   Z = nq;
   ez = 1.1f * e_nq + 1e-30f;
+  if (!isfinite(nq) || !isfinite(lq) || !isfinite(mq)) return -1;
   /* project.c:39-46: |nr| < 1e-8 or t outside (0, 1) => the point is dropped */
   if (anq + e_nq < 0.99e-8f) return 0;
   if (anq - e_nq <= 1.01e-8f) return -1;
@@ -288,6 +369,11 @@ __device__ __forceinline__ int project_f(const SceneDev& s, d3 qd, float& X, flo
   return 1;
 }
 
+/*
+ * One thread per triangle: cube-edge ids and, for rendered triangles, the
+ * FP32 screen vertices and their bounds.  Triangles whose culling the bounds
+ * cannot decide are flagged for the exact path (k_tiny).
+ */
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
@@ -308,74 +394,48 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
     double val[8];
     const unsigned code = cell_code<T>(F, i, j, k, val);
     const unsigned long long e = lut[code * 12 + r];
-    d3 v[3];
     unsigned edges = 0;
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-      v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), val[a], corner_pos(F, i, j, k, b), val[b]);
-      edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
-    }
-    /* triangulate.c:75-93 */
-    d3 fn = v_cross(v_sub(v[1], v[0]), v_sub(v[2], v[0]));
-    const double area = dsqrt(v_dot(fn, fn));
-    fn = v_mul(ddiv(1., area), fn);
-    const d3 wn = v_mul(area, fn); /* normal.c:39-40 */
-    tri.wn[0][t] = wn.x;
-    tri.wn[1][t] = wn.y;
-    tri.wn[2][t] = wn.z;
+    for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
     /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
     const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
     unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
     if (rendered) {
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        tri.vert[3 * q + 0][t] = v[q].x;
-        tri.vert[3 * q + 1][t] = v[q].y;
-        tri.vert[3 * q + 2][t] = v[q].z;
-      }
       float X[3], Y[3], Z[3], exy = 0.f, zr = 0.f;
       int status = 1;
 #pragma unroll
       for (int q = 0; q < 3; q++) {
-        float ex = 0.f, ez = 0.f;
-        const int st = project_f(scene, v_sub(v[q], scene.cam), X[q], Y[q], Z[q], ex, ez);
+        const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+        float qv[3], eq[3], ex = 0.f, ez = 0.f;
+        vertex_q(scene, F.threshold, corner_pos(F, i, j, k, a), val[a], corner_pos(F, i, j, k, b), val[b], qv, eq);
+        const int st = project_f(scene, qv, eq, X[q], Y[q], Z[q], ex, ez);
         if (st == 0) status = 0;
         else if (st < 0 && status != 0) status = -1;
         exy = fmaxf(exy, ex);
         zr = fmaxf(zr, ez / fmaxf(fabsf(Z[q]), 1e-30f));
       }
-      if (status < 0 || CHECK) {
-        /* undecided (or checking): the reference's own projection */
+      if (CHECK) {
+        /* the reference's own vertices and projection */
+        d3 v[3], p[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+          v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), val[a], corner_pos(F, i, j, k, b), val[b]);
+        }
         bool ok = true;
-        d3 p[3];
 #pragma unroll
         for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
-        if (CHECK && status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
-        if (CHECK && status == 1 && ok) {
+        if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
+        if (status == 1 && ok) {
 #pragma unroll
           for (int q = 0; q < 3; q++)
             if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
                 fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
               atomicAdd(checks + 1, 1u);
         }
-        if (status < 0) {
-          status = ok ? 1 : 0;
-          if (ok) {
-            exy = 0.f;
-            zr = 0.f;
-#pragma unroll
-            for (int q = 0; q < 3; q++) {
-              X[q] = to_f(p[q].x);
-              Y[q] = to_f(p[q].y);
-              Z[q] = to_f(p[q].z);
-              exy = fmaxf(exy, 2.f * kU32 * fmaxf(fabsf(X[q]), fabsf(Y[q])) + 1e-37f);
-              zr = 2.f * kU32;
-            }
-          }
-        }
       }
       if (status == 0) meta |= kMetaCulled;
+      if (status < 0) meta |= kMetaUndecided;
 #pragma unroll
       for (int q = 0; q < 3; q++) {
         tri.pf[3 * q + 0][t] = X[q];
@@ -386,12 +446,31 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
       tri.zrel[t] = zr;
     }
     tri.meta[t] = meta;
-    if (tri.dbg_fn) {
-      tri.dbg_fn[3 * t + 0] = fn.x;
-      tri.dbg_fn[3 * t + 1] = fn.y;
-      tri.dbg_fn[3 * t + 2] = fn.z;
-      tri.dbg_area[t] = area;
+  }
+}
+
+/* inspection: every triangle's exact vertices, face normal, area and weighted normal */
+__global__ void __launch_bounds__(256) k_exact_all(Geo G, const unsigned long long* __restrict__ total_p, TriDev tri) {
+  const long long T_ = (long long)*total_p;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
+       t += (long long)gridDim.x * blockDim.x) {
+    d3 v[3], fn, wn;
+    double area;
+    exact_vertices(G, t, v);
+    face_normal(v, fn, area, wn);
+    tri.wn[0][t] = wn.x;
+    tri.wn[1][t] = wn.y;
+    tri.wn[2][t] = wn.z;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      tri.vert[3 * q + 0][t] = v[q].x;
+      tri.vert[3 * q + 1][t] = v[q].y;
+      tri.vert[3 * q + 2][t] = v[q].z;
     }
+    tri.dbg_fn[3 * t + 0] = fn.x;
+    tri.dbg_fn[3 * t + 1] = fn.y;
+    tri.dbg_fn[3 * t + 2] = fn.z;
+    tri.dbg_area[t] = area;
   }
 }
 
@@ -401,7 +480,8 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
 /*
  * Sum of area * face normal over the triangles of the cells sharing cube
  * edge `e` of cell `c`, visited in the reference's order (ascending cell,
- * then triangle order), then normalised.
+ * then triangle order), then normalised.  wn must be present for every
+ * triangle touching the edge.
  */
 __device__ __forceinline__ d3 vertex_normal(long long c, int e, long long ncx, long long ncy,
                                             const unsigned* __restrict__ offsets, const TriDev& tri) {
@@ -423,7 +503,7 @@ __device__ __forceinline__ d3 vertex_normal(long long c, int e, long long ncx, l
   return v_normalise(sum);
 }
 
-/* every rendered triangle's vertex normals (inspection path only) */
+/* inspection: every rendered triangle's vertex normals */
 __global__ void __launch_bounds__(256)
 k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const unsigned* __restrict__ tri_cell,
           const unsigned long long* __restrict__ total_p, TriDev tri) {
@@ -451,13 +531,11 @@ k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const uns
 struct ExactTri {
   d3 v0, v1, v2;
   long long imin, imax, jmin, jmax;
+  double area;
   double area_inv;
 };
 
-__device__ __forceinline__ bool exact_tri(const SceneDev& s, const TriDev& tri, long long t, ExactTri& x) {
-  d3 w[3];
-#pragma unroll
-  for (int q = 0; q < 3; q++) w[q] = {tri.vert[3 * q][t], tri.vert[3 * q + 1][t], tri.vert[3 * q + 2][t]};
+__device__ __forceinline__ bool exact_tri(const SceneDev& s, const d3 w[3], ExactTri& x) {
   if (!project(s, w[0], x.v0) || !project(s, w[1], x.v1) || !project(s, w[2], x.v2)) return false;
   const long long W = s.width, H = s.height;
   const long long xmin = (long long)dsub(dmul(dadd(0.5, fmin(x.v0.x, fmin(x.v1.x, x.v2.x))), (double)W), 1.);
@@ -468,8 +546,8 @@ __device__ __forceinline__ bool exact_tri(const SceneDev& s, const TriDev& tri, 
   x.imax = min(W - 1, max(0LL, xmax));
   x.jmin = min(H - 1, max(0LL, ymin));
   x.jmax = min(H - 1, max(0LL, ymax));
-  const double area = edge_fn(x.v0, x.v1, x.v2);
-  x.area_inv = ddiv(1., area < 0. ? fmin(area, -1.e-16) : fmax(area, +1.e-16));
+  x.area = edge_fn(x.v0, x.v1, x.v2);
+  x.area_inv = ddiv(1., x.area < 0. ? fmin(x.area, -1.e-16) : fmax(x.area, +1.e-16));
   return true;
 }
 
@@ -488,23 +566,29 @@ __device__ __forceinline__ double exact_depth(const ExactTri& x, double w0, doub
   return ddiv(1., dadd(dadd(ddiv(w0, x.v0.z), ddiv(w1, x.v1.z)), ddiv(w2, x.v2.z)));
 }
 
+__device__ __forceinline__ unsigned long long order_of(const Geo& G, unsigned long long order_base, long long t) {
+  return order_base + 12ULL * G.tri_cell[t] + ((G.meta[t] >> kMetaRankShift) & 15);
+}
+
 /* one fragment through the reference's test and the (depth, order) z-buffer */
-__device__ __forceinline__ void exact_fragment(const SceneDev& s, const TriDev& tri, long long t, long long i,
-                                               long long j, const RasterDev& R, unsigned long long order) {
+__device__ __forceinline__ void exact_fragment(const Geo& G, const SceneDev& s, long long t, long long i, long long j,
+                                               const RasterDev& R, unsigned long long order_base) {
+  d3 w[3];
+  exact_vertices(G, t, w);
   ExactTri x;
-  if (!exact_tri(s, tri, t, x)) return;
+  if (!exact_tri(s, w, x)) return;
   double w0, w1, w2;
   if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) return;
   const double dist0 = exact_depth(x, w0, w1, w2);
-  slot_max(R.canvas + j * s.width + i, depth_key(dist0), order << 24);
+  slot_max(R.canvas + j * s.width + i, depth_key(dist0), order_of(G, order_base, t) << 24);
 }
 
 /* ------------------------------------------------------------------ */
 /* k_cover: single-precision coverage / depth filter                   */
 /* ------------------------------------------------------------------ */
 /*
- * Per rendered triangle, every pixel of a (superset of the) reference's
- * bounding box is classified with certified FP32 bounds:
+ * Per rendered triangle, every pixel whose centre can lie in the triangle
+ * is classified with certified FP32 bounds:
  *   certainly outside        -> dropped
  *   certainly inside         -> raises the pixel's depth floor (zlo) to a
  *                               certain lower bound of its depth, and is a
@@ -543,7 +627,7 @@ __device__ __forceinline__ float edge_eval(const EdgeF& E, float px, float py, f
 constexpr float kWOut = -1.0e-8f * (1.f + 1e-5f); /* certainly below -1e-8 */
 constexpr float kWIn = -1.0e-8f * (1.f - 1e-5f);  /* certainly above -1e-8 */
 
-/* warp-aggregated append; returns the slot or ~0 when the list is full */
+/* warp-aggregated append; returns the slot index */
 __device__ __forceinline__ unsigned long long append_slot(unsigned long long* count, bool want) {
   const unsigned mask = __ballot_sync(__activemask(), want);
   if (!want) return ~0ULL;
@@ -555,23 +639,6 @@ __device__ __forceinline__ unsigned long long append_slot(unsigned long long* co
   return base + __popc(mask & ((1u << lane) - 1));
 }
 
-__device__ __forceinline__ void push_candidate(const RasterDev& R, const SceneDev& s, const TriDev& tri, long long t,
-                                               long long i, long long j, float dhi, unsigned long long order,
-                                               bool want) {
-  const unsigned long long idx = append_slot(R.cand_count, want);
-  if (!want) return;
-  if (idx < R.cand_cap) {
-    Candidate c;
-    c.t = (unsigned)t;
-    c.pixel = (unsigned)(j * s.width + i);
-    c.dhi = dhi;
-    c.pad = 0;
-    R.cand[idx] = c;
-  } else {
-    exact_fragment(s, tri, t, i, j, R, order); /* list full: resolve in place */
-  }
-}
-
 /* pixel index range whose centres (i + 0.5) / n - 0.5 may lie in [lo, hi] */
 __device__ __forceinline__ void centre_range(float lo, float hi, long long n, long long& a, long long& b) {
   const float fa = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + lo) * (float)n - 0.5f - 1e-3f));
@@ -581,31 +648,34 @@ __device__ __forceinline__ void centre_range(float lo, float hi, long long n, lo
 }
 
 /* ------------------------------------------------------------------ */
-/* k_tiny: triangles the single-precision filter cannot settle         */
+/* triangles the single-precision filter cannot settle                 */
 /* ------------------------------------------------------------------ */
 /*
- * Triangles whose projected area is too small (or too uncertain) for the
- * FP32 bounds.  The reference's projection and area are computed once per
- * triangle; when the area is not clamped (|area| >= 1e-16, render.c:108-111)
- * the covered pixel centres lie in the triangle's extent, which holds no
- * pixel centre for most of these triangles; otherwise the reference's whole
- * box is tested.  Fragments go straight to the z-buffer.
+ * Triangles whose projected area is too small (or whose culling or bounds are
+ * too uncertain) for the FP32 filter.  The reference's vertices, projection
+ * and area are computed once per triangle; when the area is not clamped
+ * (|area| >= 1e-16, render.c:108-111) the covered pixel centres lie in the
+ * triangle's extent, which holds no pixel centre for most of these
+ * triangles; otherwise the reference's whole box is tested.  Fragments go
+ * straight to the z-buffer.
  */
 template <bool CHECK>
-__device__ void tiny_triangle(const SceneDev& s, const TriDev& tri, long long t, const RasterDev& R,
-                              unsigned long long order, unsigned* checks) {
+__device__ void tiny_triangle(const Geo& G, const SceneDev& s, long long t, const RasterDev& R,
+                              unsigned long long order_base, unsigned* checks) {
+  d3 w[3];
+  exact_vertices(G, t, w);
   ExactTri x;
-  if (!exact_tri(s, tri, t, x)) return;
+  if (!exact_tri(s, w, x)) return;
   long long imin = x.imin, imax = x.imax, jmin = x.jmin, jmax = x.jmax;
-  const double area = edge_fn(x.v0, x.v1, x.v2);
-  const bool unclamped = fabs(area) >= 1.e-16;
-  if (unclamped) {
+  if (fabs(x.area) >= 1.e-16) {
     const double xlo = fmin(x.v0.x, fmin(x.v1.x, x.v2.x)), xhi = fmax(x.v0.x, fmax(x.v1.x, x.v2.x));
     const double ylo = fmin(x.v0.y, fmin(x.v1.y, x.v2.y)), yhi = fmax(x.v0.y, fmax(x.v1.y, x.v2.y));
     const double mb = 1e-6 * ((xhi - xlo) + (yhi - ylo)) + 1e-14;
     const long long W = s.width, H = s.height;
-    const double ia = ceil((0.5 + (xlo - mb)) * (double)W - 0.5 - 1e-6), ib = floor((0.5 + (xhi + mb)) * (double)W - 0.5 + 1e-6);
-    const double ja = ceil((0.5 + (ylo - mb)) * (double)H - 0.5 - 1e-6), jb = floor((0.5 + (yhi + mb)) * (double)H - 0.5 + 1e-6);
+    const double ia = ceil((0.5 + (xlo - mb)) * (double)W - 0.5 - 1e-6);
+    const double ib = floor((0.5 + (xhi + mb)) * (double)W - 0.5 + 1e-6);
+    const double ja = ceil((0.5 + (ylo - mb)) * (double)H - 0.5 - 1e-6);
+    const double jb = floor((0.5 + (yhi + mb)) * (double)H - 0.5 + 1e-6);
     imin = max(imin, (long long)fmax(ia, -1.0));
     imax = min(imax, (long long)fmin(ib, (double)W));
     jmin = max(jmin, (long long)fmax(ja, -1.0));
@@ -619,6 +689,7 @@ __device__ void tiny_triangle(const SceneDev& s, const TriDev& tri, long long t,
           atomicAdd(checks + 2, 1u);
       }
   }
+  const unsigned long long order = order_of(G, order_base, t);
   for (long long j = jmin; j <= jmax; j++)
     for (long long i = imin; i <= imax; i++) {
       double w0, w1, w2;
@@ -629,12 +700,12 @@ __device__ void tiny_triangle(const SceneDev& s, const TriDev& tri, long long t,
 
 template <bool CHECK>
 __global__ void __launch_bounds__(256)
-k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const unsigned* __restrict__ tri_cell,
-        TriDev tri, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
+k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
+        unsigned long long order_base, unsigned* __restrict__ checks) {
   const long long T_ = (long long)*total_p;
   const long long W = scene.width, H = scene.height;
   /* traverse front to back along z (the order of the emission index) so that
-     near surfaces raise the floors before far ones are classified */
+     near surfaces raise the floors early */
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < T_; q += (long long)gridDim.x * blockDim.x) {
     const long long t = scene.z_descending ? T_ - 1 - q : q;
     const unsigned meta = tri.meta[t];
@@ -647,7 +718,6 @@ k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const un
       Z[v] = tri.pf[3 * v + 2][t];
     }
     const float eps = tri.perr[t], zr = tri.zrel[t];
-    const unsigned long long order = order_base + 12ULL * tri_cell[t] + ((meta >> kMetaRankShift) & 15);
     /* inverse area (render.c:102-107) with its bound */
     const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
     const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
@@ -659,13 +729,12 @@ k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const un
        its sign and size are known to within half; then every covered pixel
        centre lies inside the triangle's extent (its weights are barycentric
        up to the -1e-8 slack) */
-    const bool regular = isfinite(A) && isfinite(eps) && fabsf(A) - errA > 1e-15f && rai < 0.5f && eps < 1e-3f &&
-                         zr < 1e-3f;
-    const bool in_tiny = !regular;
-    const unsigned long long ti = append_slot(R.tiny_count, in_tiny);
-    if (in_tiny) {
+    const bool regular = !(meta & kMetaUndecided) && isfinite(A) && isfinite(eps) && fabsf(A) - errA > 1e-15f &&
+                         rai < 0.5f && eps < 1e-3f && zr < 1e-3f;
+    const unsigned long long ti = append_slot(R.tiny_count, !regular);
+    if (!regular) {
       if (ti < R.tiny_cap) R.tiny[ti] = (unsigned)t;
-      else tiny_triangle<false>(scene, tri, t, R, order, nullptr);
+      else tiny_triangle<false>(G, scene, t, R, order_base, nullptr);
       continue;
     }
     const float ai = 1.f / A;
@@ -682,18 +751,22 @@ k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const un
     const float dlo = zmin - m * fabsf(zmin), dhi = zmax + m * fabsf(zmax);
     ExactTri ex;
     bool ex_ok = false;
-    if (CHECK) ex_ok = exact_tri(scene, tri, t, ex);
-    if (CHECK && ex_ok) {
-      /* every covered pixel of the reference's box must lie in the tight range */
-      for (long long j = ex.jmin; j <= ex.jmax; j++)
-        for (long long i = ex.imin; i <= ex.imax; i++) {
-          double w0, w1, w2;
-          if (exact_weights(ex, i, j, R.xs, R.ys, w0, w1, w2)) {
-            if (i < imin || i > imax || j < jmin || j > jmax) atomicAdd(checks + 2, 1u);
-            const double d = exact_depth(ex, w0, w1, w2);
-            if (!(d <= (double)dhi && d >= (double)dlo)) atomicAdd(checks + 4, 1u);
+    if (CHECK) {
+      d3 wv[3];
+      exact_vertices(G, t, wv);
+      ex_ok = exact_tri(scene, wv, ex);
+      if (ex_ok) {
+        /* every covered pixel of the reference's box must lie in the tight range */
+        for (long long j = ex.jmin; j <= ex.jmax; j++)
+          for (long long i = ex.imin; i <= ex.imax; i++) {
+            double w0, w1, w2;
+            if (exact_weights(ex, i, j, R.xs, R.ys, w0, w1, w2)) {
+              if (i < imin || i > imax || j < jmin || j > jmax) atomicAdd(checks + 2, 1u);
+              const double d = exact_depth(ex, w0, w1, w2);
+              if (!(d <= (double)dhi && d >= (double)dlo)) atomicAdd(checks + 4, 1u);
+            }
           }
-        }
+      }
     }
     for (long long j = jmin; j <= jmax; j++) {
       const float py = R.ysf[j];
@@ -717,7 +790,19 @@ k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const un
           if (!cov && inside) atomicAdd(checks + 3, 1u); /* called an uncovered pixel inside */
         }
         if (inside) atomicMax(R.zlo + j * W + i, f_key(dlo));
-        push_candidate(R, scene, tri, t, i, j, dhi, order, !out);
+        const unsigned long long idx = append_slot(R.cand_count, !out);
+        if (!out) {
+          if (idx < R.cand_cap) {
+            Candidate cd;
+            cd.t = (unsigned)t;
+            cd.pixel = (unsigned)(j * W + i);
+            cd.dhi = dhi;
+            cd.pad = 0;
+            R.cand[idx] = cd;
+          } else {
+            exact_fragment(G, scene, t, i, j, R, order_base); /* list full: resolve in place */
+          }
+        }
       }
     }
   }
@@ -725,72 +810,130 @@ k_cover(SceneDev scene, const unsigned long long* __restrict__ total_p, const un
 
 template <bool CHECK>
 __global__ void __launch_bounds__(256)
-k_tiny(SceneDev scene, const unsigned* __restrict__ tri_cell, TriDev tri, RasterDev R, unsigned long long order_base,
-       unsigned* __restrict__ checks) {
+k_tiny(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
   const unsigned long long n = min(*R.tiny_count, R.tiny_cap);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    const long long t = R.tiny[q];
-    const unsigned long long order = order_base + 12ULL * tri_cell[t] + ((tri.meta[t] >> kMetaRankShift) & 15);
-    tiny_triangle<CHECK>(scene, tri, t, R, order, checks);
-  }
+       q += (unsigned long long)gridDim.x * blockDim.x)
+    tiny_triangle<CHECK>(G, scene, R.tiny[q], R, order_base, checks);
 }
 
 /* ------------------------------------------------------------------ */
 /* k_exact: the reference's arithmetic for the surviving candidates    */
 /* ------------------------------------------------------------------ */
-__global__ void __launch_bounds__(256)
-k_exact(SceneDev scene, const unsigned* __restrict__ tri_cell, TriDev tri, RasterDev R,
-        unsigned long long order_base) {
+__global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base) {
   const unsigned long long n = min(*R.cand_count, R.cand_cap);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x) {
     const Candidate c = R.cand[q];
     /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
     if (f_key(c.dhi) < R.zlo[c.pixel]) continue;
-    const long long i = c.pixel % scene.width, j = c.pixel / scene.width;
-    const unsigned long long order = order_base + 12ULL * tri_cell[c.t] + ((tri.meta[c.t] >> kMetaRankShift) & 15);
-    exact_fragment(scene, tri, c.t, i, j, R, order);
+    exact_fragment(G, scene, c.t, c.pixel % scene.width, c.pixel / scene.width, R, order_base);
   }
 }
 
 /* ------------------------------------------------------------------ */
-/* k_shade: colour of the pixels this slab won (render.c:137-159)       */
+/* shading: winners, their neighbours' weighted normals, colour         */
 /* ------------------------------------------------------------------ */
+/* the pixel's owner, if one of this slab's rendered slices won it */
+__device__ __forceinline__ bool slab_owner(const Geo& G, unsigned long long lo, unsigned long long order_base,
+                                           unsigned long long T_, long long& t, long long& cl) {
+  const unsigned long long order = lo >> 24;
+  if (order < order_base) return false;
+  const unsigned long long rel = order - order_base;
+  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
+  const unsigned long long c = rel / 12;
+  if (c >= (unsigned long long)(G.S.nslices * ncx * ncy)) return false;
+  const long long kk = G.S.kfirst + (long long)(c / (unsigned long long)(ncx * ncy));
+  if (kk < G.S.krender0 || kk >= G.S.krender1) return false;
+  t = (long long)G.offsets[c] + (long long)(rel % 12);
+  cl = (long long)c;
+  return (unsigned long long)t < T_;
+}
+
+/*
+ * One thread per pixel: list the pixels this slab won, and request the
+ * weighted normal of every triangle that shares a cube edge with a vertex of
+ * a winning triangle (normal.c:78-158 neighbourhoods), each once.
+ */
 __global__ void __launch_bounds__(256)
-k_shade(FieldDev F, SlabDev S, SceneDev scene, const unsigned* __restrict__ offsets,
-        const unsigned* __restrict__ tri_cell, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
-        unsigned long long order_base, unsigned rgb_in) {
+k_winners(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
+          unsigned long long order_base) {
   const unsigned long long T_ = *total_p;
-  const long long W = scene.width, npx = scene.width * scene.height;
-  const long long ncx = F.nx - 1, ncy = F.ny - 1;
+  const long long npx = scene.width * scene.height;
+  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+    long long t = 0, c = 0;
+    const bool won = slab_owner(G, R.canvas[p].lo, order_base, T_, t, c);
+    const unsigned long long w = append_slot(R.win_count, won);
+    if (!won) continue;
+    R.win[w] = make_uint2((unsigned)p, (unsigned)t);
+    const unsigned meta = tri.meta[t];
+    for (int m = 0; m < 3; m++) {
+      const int e = (meta >> (5 * m)) & 31;
+      const int nn = c_nb_count[e];
+      for (int q = 0; q < nn; q++) {
+        const long long nc = c + (long long)c_nb[e][q][0] * ncx * ncy + (long long)c_nb[e][q][1] * ncx +
+                             (long long)c_nb[e][q][2];
+        const unsigned le = (unsigned)c_nb[e][q][3];
+        const unsigned u0 = G.offsets[nc], u1 = G.offsets[nc + 1];
+        for (unsigned u = u0; u < u1; u++) {
+          const unsigned om = tri.meta[u];
+          if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
+            if (atomicOr(tri.need + u, 1u) == 0u) {
+              const unsigned long long s = atomicAdd(R.need_count, 1ULL);
+              R.need[s] = u;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+/* one thread per requested triangle: its exact weighted normal */
+__global__ void __launch_bounds__(256) k_wn(Geo G, TriDev tri, RasterDev R) {
+  const unsigned long long n = *R.need_count;
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const long long u = R.need[q];
+    d3 v[3], fn, wn;
+    double area;
+    exact_vertices(G, u, v);
+    face_normal(v, fn, area, wn);
+    tri.wn[0][u] = wn.x;
+    tri.wn[1][u] = wn.y;
+    tri.wn[2][u] = wn.z;
+  }
+}
+
+/* one thread per won pixel: vertex normals and colour (render.c:137-159) */
+__global__ void __launch_bounds__(256)
+k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
+  const unsigned long long n = *R.win_count;
+  const long long W = scene.width;
+  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
   const double cr = (double)((rgb_in >> 16) & 255), cg = (double)((rgb_in >> 8) & 255),
                cb = (double)(rgb_in & 255);
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long lo = R.canvas[p].lo;
-    const unsigned long long order = lo >> 24;
-    /* did one of this slab's rendered slices win the pixel? */
-    if (order < order_base) continue;
-    const unsigned long long rel = order - order_base;
-    const unsigned long long cl = rel / 12;
-    if (cl >= (unsigned long long)(S.nslices * ncx * ncy)) continue;
-    const long long kk = S.kfirst + (long long)(cl / (unsigned long long)(ncx * ncy));
-    if (kk < S.krender0 || kk >= S.krender1) continue;
-    const long long t = (long long)offsets[cl] + (long long)(rel % 12);
-    if ((unsigned long long)t >= T_) continue;
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint2 wp = R.win[q];
+    const long long p = wp.x, t = wp.y;
+    d3 v[3];
+    exact_vertices(G, t, v);
     ExactTri x;
     double w0, w1, w2;
-    if (!exact_tri(scene, tri, t, x) || !exact_weights(x, p % W, p / W, R.xs, R.ys, w0, w1, w2)) continue;
+    if (!exact_tri(scene, v, x) || !exact_weights(x, p % W, p / W, R.xs, R.ys, w0, w1, w2)) continue;
     const unsigned meta = tri.meta[t];
-    const long long c = (long long)cl;
-    const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, offsets, tri);
-    const d3 n1 = vertex_normal(c, (meta >> 5) & 31, ncx, ncy, offsets, tri);
-    const d3 n2 = vertex_normal(c, (meta >> 10) & 31, ncx, ncy, offsets, tri);
-    const d3 n = v_normalise(v_add(v_mul(w0, n0), v_add(v_mul(w1, n1), v_mul(w2, n2))));
-    const double factor = fmax(0.15, fabs(v_dot(n, scene.light)));
+    const long long c = G.tri_cell[t];
+    const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, G.offsets, tri);
+    const d3 n1 = vertex_normal(c, (meta >> 5) & 31, ncx, ncy, G.offsets, tri);
+    const d3 n2 = vertex_normal(c, (meta >> 10) & 31, ncx, ncy, G.offsets, tri);
+    const d3 nrm = v_normalise(v_add(v_mul(w0, n0), v_add(v_mul(w1, n1), v_mul(w2, n2))));
+    const double factor = fmax(0.15, fabs(v_dot(nrm, scene.light)));
     const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
     const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
     const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
+    const unsigned long long lo = R.canvas[p].lo;
     R.canvas[p].lo = (lo & ~0xFFFFFFULL) | (r8 << 16) | (g8 << 8) | b8;
   }
 }
@@ -914,38 +1057,44 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
   }
 }
 
+void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
+                      cudaStream_t st) {
+  k_exact_all<<<grid_for(tri_bound, 256, 8), 256, 0, st>>>(G, total, tri);
+}
+
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
   k_normals<<<g, 256, 0, st>>>(F, S, offsets, tri_cell, total, tri);
 }
 
-void launch_cover(const SceneDev& scene, const unsigned long long* total, long long tri_bound,
-                  const unsigned* tri_cell, const TriDev& tri, const RasterDev& R, unsigned long long order_base,
-                  unsigned* checks, cudaStream_t st) {
+void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
+                  const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned* checks,
+                  cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
-  if (checks) k_cover<true><<<g, 256, 0, st>>>(scene, total, tri_cell, tri, R, order_base, checks);
-  else k_cover<false><<<g, 256, 0, st>>>(scene, total, tri_cell, tri, R, order_base, checks);
+  if (checks) k_cover<true><<<g, 256, 0, st>>>(G, scene, total, tri, R, order_base, checks);
+  else k_cover<false><<<g, 256, 0, st>>>(G, scene, total, tri, R, order_base, checks);
 }
 
-void launch_tiny(const SceneDev& scene, long long tiny_bound, const unsigned* tri_cell, const TriDev& tri,
-                 const RasterDev& R, unsigned long long order_base, unsigned* checks, cudaStream_t st) {
+void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
+                 unsigned long long order_base, unsigned* checks, cudaStream_t st) {
   const int g = grid_for(tiny_bound, 256, 8);
-  if (checks) k_tiny<true><<<g, 256, 0, st>>>(scene, tri_cell, tri, R, order_base, checks);
-  else k_tiny<false><<<g, 256, 0, st>>>(scene, tri_cell, tri, R, order_base, checks);
+  if (checks) k_tiny<true><<<g, 256, 0, st>>>(G, scene, R, order_base, checks);
+  else k_tiny<false><<<g, 256, 0, st>>>(G, scene, R, order_base, checks);
 }
 
-void launch_exact(const SceneDev& scene, long long cand_bound, const unsigned* tri_cell, const TriDev& tri,
-                  const RasterDev& R, unsigned long long order_base, cudaStream_t st) {
-  const int g = grid_for(cand_bound, 256, 8);
-  k_exact<<<g, 256, 0, st>>>(scene, tri_cell, tri, R, order_base);
+void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
+                  unsigned long long order_base, cudaStream_t st) {
+  k_exact<<<grid_for(cand_bound, 256, 8), 256, 0, st>>>(G, scene, R, order_base);
 }
 
-void launch_shade(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned* offsets,
-                  const unsigned* tri_cell, const unsigned long long* total, const TriDev& tri, const RasterDev& R,
-                  unsigned long long order_base, unsigned rgb, cudaStream_t st) {
-  const int g = grid_for(scene.width * scene.height, 256, 8);
-  k_shade<<<g, 256, 0, st>>>(F, S, scene, offsets, tri_cell, total, tri, R, order_base, rgb);
+void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
+                    const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
+                    cudaStream_t st) {
+  const long long npx = scene.width * scene.height;
+  k_winners<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, total, tri, R, order_base);
+  k_wn<<<grid_for(tri_bound, 256, 8), 256, 0, st>>>(G, tri, R);
+  k_shade<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, tri, R, rgb);
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,

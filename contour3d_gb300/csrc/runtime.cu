@@ -285,7 +285,7 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
-  Buf zlo, xyf, cand, tiny, checks;
+  Buf zlo, xyf, cand, tiny, win, need, checks;
   bool filter_check = false;
   HostBuf h_small, h_rgb, h_slots;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[8] = {};
@@ -321,7 +321,7 @@ static int ctx_init(Ctx &c) {
   }
   if (c.lut.ensure(sizeof(unsigned long long) * kLutEntries)) return 1;
   C3D_CUDA(cudaMemcpy(c.lut.p, lut.data(), sizeof(unsigned long long) * kLutEntries, cudaMemcpyHostToDevice));
-  if (c.h_small.ensure(128)) return 1;
+  if (c.h_small.ensure(256)) return 1;
   c.device = dev;
   c.ready = true;
   return 0;
@@ -384,23 +384,24 @@ struct FrameOut {
 };
 
 /* bytes per triangle of the slab arrays (see TriDev) */
-static const size_t kTriBytes = 12 * sizeof(double) + sizeof(unsigned) + 11 * sizeof(float);
-/* doubles per triangle of the inspection arrays: vertex normals, face normal, area */
-static const size_t kDbgDoubles = 13;
+static const size_t kTriBytes = 3 * sizeof(double) + 2 * sizeof(unsigned) + 11 * sizeof(float);
+/* doubles per triangle of the inspection arrays: vertices, vertex normals, face normal, area */
+static const size_t kDbgDoubles = 22;
 
 static TriDev tri_layout(void *base, size_t cap, double *dbg) {
   TriDev t;
   double *d = static_cast<double *>(base);
-  for (int q = 0; q < 9; q++) t.vert[q] = d + q * cap;
-  for (int q = 0; q < 3; q++) t.wn[q] = d + (9 + q) * cap;
-  float *f = reinterpret_cast<float *>(d + 12 * cap);
+  for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
+  float *f = reinterpret_cast<float *>(d + 3 * cap);
   for (int q = 0; q < 9; q++) t.pf[q] = f + q * cap;
   t.perr = f + 9 * cap;
   t.zrel = f + 10 * cap;
   t.meta = reinterpret_cast<unsigned *>(f + 11 * cap);
-  for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + q * cap : nullptr;
-  t.dbg_fn = dbg ? dbg + 9 * cap : nullptr;
-  t.dbg_area = dbg ? dbg + 12 * cap : nullptr;
+  t.need = t.meta + cap;
+  for (int q = 0; q < 9; q++) t.vert[q] = dbg ? dbg + q * cap : nullptr;
+  for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + (9 + q) * cap : nullptr;
+  t.dbg_fn = dbg ? dbg + 18 * cap : nullptr;
+  t.dbg_area = dbg ? dbg + 21 * cap : nullptr;
   return t;
 }
 
@@ -498,7 +499,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     S.krender1 = std::min(k1, ncz - 1);
     const long long ncell = S.nslices * per_slice;
     if (c.counts.ensure((size_t)ncell) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1)) ||
-        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell)) || c.scratch.ensure(64))
+        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell)) || c.scratch.ensure(128))
       return 1;
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = d_counter + 1;
@@ -546,39 +547,56 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     if (c.stage_timing) cudaEventRecord(c.evs[4], st);
     c.stats.kernel_launches += 2;
     const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
+    Geo G;
+    G.F = F;
+    G.S = S;
+    G.lut = c.lut.as<unsigned long long>();
+    G.tri_cell = c.tri_cell.as<unsigned>();
+    G.offsets = c.offsets.as<unsigned>();
+    G.meta = tri.meta;
     if (sink) {
+      launch_exact_all(G, d_total, (long long)T, tri, st);
       launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
-      c.stats.kernel_launches += 1;
+      c.stats.kernel_launches += 2;
     } else {
-      /* candidates: about one per covered pixel; the list falls back to in-place
-         resolution when full, so its size only affects speed */
-      const unsigned long long want = std::max<unsigned long long>(2ULL * T, 1ULL << 20);
-      if (c.cand.ensure(sizeof(Candidate) * want)) return 1;
+      /* candidates: about one per covered pixel; the lists fall back to
+         in-place resolution when full, so their sizes only affect speed */
+      const unsigned long long want = std::max<unsigned long long>(T / 2, 1ULL << 20);
       const unsigned long long tiny_want = std::max<unsigned long long>(T / 8, 1ULL << 16);
-      if (c.tiny.ensure(sizeof(unsigned) * tiny_want)) return 1;
+      const size_t npx = (size_t)(sd.width * sd.height);
+      if (c.cand.ensure(sizeof(Candidate) * want) || c.tiny.ensure(sizeof(unsigned) * tiny_want) ||
+          c.win.ensure(sizeof(uint2) * npx) || c.need.ensure(sizeof(unsigned) * T))
+        return 1;
       RasterDev RS = R;
+      unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 4);
       RS.cand = c.cand.as<Candidate>();
       RS.cand_cap = c.cand.cap / sizeof(Candidate);
-      RS.cand_count = reinterpret_cast<unsigned long long *>(d_counter + 4);
+      RS.cand_count = counters + 0;
       RS.tiny = c.tiny.as<unsigned>();
       RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
-      RS.tiny_count = reinterpret_cast<unsigned long long *>(d_counter + 6);
-      C3D_CUDA(cudaMemsetAsync(RS.cand_count, 0, 2 * sizeof(unsigned long long), st));
-      launch_cover(sd, d_total, (long long)T, c.tri_cell.as<unsigned>(), tri, RS, slab_order, checks, st);
-      launch_tiny(sd, (long long)RS.tiny_cap, c.tri_cell.as<unsigned>(), tri, RS, slab_order, checks, st);
-      c.stats.kernel_launches += 1;
+      RS.tiny_count = counters + 1;
+      RS.win = c.win.as<uint2>();
+      RS.win_count = counters + 2;
+      RS.need = c.need.as<unsigned>();
+      RS.need_count = counters + 3;
+      C3D_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st));
+      C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
+      launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
+      launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
       if (c.stage_timing) cudaEventRecord(c.evs[5], st);
-      launch_exact(sd, (long long)RS.cand_cap, c.tri_cell.as<unsigned>(), tri, RS, slab_order, st);
+      launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
       if (c.stage_timing) cudaEventRecord(c.evs[6], st);
-      launch_shade(F, S, sd, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, tri, RS, slab_order, rgb, st);
-      c.stats.kernel_launches += 3;
+      launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
+      c.stats.kernel_launches += 6;
       if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-      unsigned long long *h_cand = h_total + 1;
-      C3D_CUDA(cudaMemcpyAsync(h_cand, RS.cand_count, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+      unsigned long long *h_cnt = h_total + 1;
+      C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
-      c.stats.candidates += h_cand[0];
-      c.stats.tiny += h_cand[1];
-      if (*h_cand > RS.cand_cap) c.stats.candidate_overflows += *h_cand - RS.cand_cap;
+      c.stats.candidates += h_cnt[0];
+      if (h_cnt[0] > RS.cand_cap) c.stats.candidate_overflows += h_cnt[0] - RS.cand_cap;
+      c.stats.tiny += h_cnt[1];
+      c.stats.winners += h_cnt[2];
+      c.stats.normals += h_cnt[3];
       if (c.stage_timing) {
         c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
         c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);
@@ -589,11 +607,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     if (sink) {
       /* copy this slab's triangles back and keep the rendered ones in order */
       std::vector<unsigned> meta(T), cellv(T);
-      std::vector<double> vert(9 * T), dv(kDbgDoubles * cap);
+      std::vector<double> dv(kDbgDoubles * cap);
       C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
-      for (int q = 0; q < 9; q++)
-        C3D_CUDA(cudaMemcpyAsync(vert.data() + q * T, tri.vert[q], sizeof(double) * T, cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * kDbgDoubles * cap, cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
       for (unsigned long long t = 0; t < T; t++) {
@@ -603,10 +619,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         if (!(meta[t] & kMetaRendered)) continue;
         if (sink->out && sink->count < sink->capacity) {
           TriRecord &r = sink->out[sink->count];
-          for (int q = 0; q < 9; q++) r.vertices[q] = vert[q * T + t];
-          for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[q * cap + t];
-          for (int q = 0; q < 3; q++) r.face_normal[q] = dv[9 * cap + 3 * t + q];
-          r.area = dv[12 * cap + t];
+          for (int q = 0; q < 9; q++) r.vertices[q] = dv[q * cap + t];
+          for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[(9 + q) * cap + t];
+          for (int q = 0; q < 3; q++) r.face_normal[q] = dv[18 * cap + 3 * t + q];
+          r.area = dv[21 * cap + t];
           r.cell[0] = i + (long long)ci.off[0];
           r.cell[1] = j + (long long)ci.off[1];
           r.cell[2] = k + (long long)ci.off[2];
@@ -1091,7 +1107,7 @@ extern "C" int contour3d_gb300_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx &c = g_ctx;
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.tiny,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.tiny, &c.win, &c.need,
                  &c.checks};
   for (Buf *b : bufs) b->release();
   c.h_small.release();

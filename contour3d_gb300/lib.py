@@ -21,7 +21,8 @@ class NativeLibraryMissing(RuntimeError):
 
 class Stats(C.Structure):
     _fields_ = [("cells", C.c_uint64), ("triangles", C.c_uint64), ("candidates", C.c_uint64),
-                ("candidate_overflows", C.c_uint64), ("tiny", C.c_uint64), ("slabs", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("candidate_overflows", C.c_uint64), ("tiny", C.c_uint64), ("winners", C.c_uint64),
+                ("normals", C.c_uint64), ("slabs", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_classify", C.c_double), ("ms_scan", C.c_double),
                 ("ms_emit", C.c_double), ("ms_cover", C.c_double), ("ms_exact", C.c_double),
                 ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5)]

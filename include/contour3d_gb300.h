@@ -124,6 +124,8 @@ typedef struct {
   uint64_t candidates;        /* fragments the single-precision filter could not settle */
   uint64_t candidate_overflows; /* of those, resolved in place because the list was full */
   uint64_t tiny;              /* triangles too small for the FP32 filter (resolved in FP64) */
+  uint64_t winners;           /* pixels whose owner was shaded (summed over slabs) */
+  uint64_t normals;           /* weighted face normals computed for shading */
   uint64_t slabs;             /* slab passes */
   uint64_t kernel_launches;   /* kernels launched by the library */
   double ms_total;            /* device time of the whole frame (events) */
