@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--shape", type=int, default=512,
+                   help="nodes per axis (512 is the benchmark; smaller sizes are for profiler captures)")
     return p.parse_args()
 
 
@@ -176,6 +178,8 @@ def main():
     torch.cuda.set_device(local)
     from contour3d_gb300 import _abi, lib
     gpu = lib.load()
+    global SHAPE
+    SHAPE = (args.shape,) * 3
     nz, ny, nx = SHAPE
     field = torch.empty(SHAPE, dtype=torch.float64, device="cuda")
     std = gpu.fieldgen_modes_device(field.data_ptr(), 0, SHAPE, NMODES, KMIN, KMAX, POWER, SEED)

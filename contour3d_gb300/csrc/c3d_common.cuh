@@ -190,8 +190,24 @@ __device__ __forceinline__ float f_from_key(unsigned k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
 }
 
-/* a double rounded to float, and the distance bound |result - x| */
-__device__ __forceinline__ float to_f(double x) { return __double2float_rn(x); }
+/*
+ * double -> float with integer operations only (the hardware conversion runs
+ * on the FP64 pipe): the significand is truncated, so |result - x| <= 2^-23
+ * |x| for |x| in the float normal range; smaller magnitudes flush to a
+ * signed zero (error < 2^-126), larger ones become infinite, NaN stays NaN.
+ * Every bound built on a converted value uses 2u for it.
+ */
+__device__ __forceinline__ float to_f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FF);
+  if (e == 0x7FF) return __int_as_float(((hi & 0xFFFFF) | lo) ? 0x7FC00000 : (int)(sign | 0x7F800000u));
+  const int fe = e - 1023 + 127;
+  if (fe >= 255) return __int_as_float((int)(sign | 0x7F800000u));
+  if (fe <= 0) return __int_as_float((int)sign);
+  return __int_as_float((int)(sign | ((unsigned)fe << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29)));
+}
 
 /* ------------------------------------------------------------------ */
 /* marching-tetrahedra tables                                           */

@@ -24,6 +24,9 @@ struct FieldDev {
   double threshold;
   long long thr_key;        /* integer key of the threshold (d_key) */
   int thr_nan;
+  /* float fields: threshold < (double)v  <=>  f_key(v) >= thr_f_key (when thr_f_ok) */
+  unsigned thr_f_key;
+  int thr_f_ok;
 };
 
 /* one z-slab of cells: slices [kfirst, kfirst + nslices), rendered [krender0, krender1) */

@@ -82,21 +82,82 @@ __device__ __forceinline__ unsigned cell_code(const FieldDev& F, long long i, lo
   return code;
 }
 
+/* cell (i, j, k-in-slab) of a slab-local linear cell index; 32-bit arithmetic */
+__device__ __forceinline__ void cell_ijk(unsigned c, unsigned ncx, unsigned ncy, unsigned& i, unsigned& j,
+                                         unsigned& kl) {
+  const unsigned r = c / ncx;
+  i = c - r * ncx;
+  kl = r / ncy;
+  j = r - kl * ncy;
+}
+
 /* ------------------------------------------------------------------ */
 /* k_classify                                                          */
 /* ------------------------------------------------------------------ */
+/*
+ * Tiled over (x, y) and marching in z: each node's "above" bit is computed
+ * once into shared memory (two planes, double-buffered), and each cell
+ * assembles its 8-bit code from the bits of its corners.  A block owns
+ * kClsX x kClsY cells of kClsZ consecutive slices.
+ */
+constexpr int kClsX = 128;
+constexpr int kClsY = 8;
+constexpr int kClsZ = 32;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ counts) {
-  const long long ncx = F.nx - 1, ncy = F.ny - 1;
-  const long long ncell = S.nslices * ncx * ncy;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
-       c += (long long)gridDim.x * blockDim.x) {
-    const long long i = c % ncx;
-    const long long j = (c / ncx) % ncy;
-    const long long k = S.kfirst + c / (ncx * ncy);
-    double v[8];
-    const unsigned code = cell_code<T>(F, i, j, k, v);
-    counts[c] = c_code_count[code];
+__device__ __forceinline__ unsigned char node_above(const FieldDev& F, const T* f, long long idx);
+template <>
+__device__ __forceinline__ unsigned char node_above<double>(const FieldDev& F, const double* f, long long idx) {
+  const double v = __ldg(f + idx);
+  return (!F.thr_nan && !d_isnan(v) && d_key(v) > F.thr_key) ? 1 : 0;
+}
+template <>
+__device__ __forceinline__ unsigned char node_above<float>(const FieldDev& F, const float* f, long long idx) {
+  /* threshold < (double)v  <=>  v >= the least float above the threshold */
+  const float v = __ldg(f + idx);
+  return (F.thr_f_ok && v == v && f_key(v) >= F.thr_f_key) ? 1 : 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ counts) {
+  __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+  __shared__ unsigned char lut[256];
+  for (int q = threadIdx.x; q < 256; q += blockDim.x) lut[q] = c_code_count[q];
+  const T* f = static_cast<const T*>(F.data);
+  const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
+  const unsigned i0 = blockIdx.x * kClsX, j0 = blockIdx.y * kClsY;
+  const long long k0 = (long long)blockIdx.z * kClsZ;
+  const long long k1 = min(k0 + kClsZ, S.nslices);
+  const long long sx = F.nx, sxy = F.nx * F.ny;
+  auto load_plane = [&](int buf, long long k) {
+    for (int q = threadIdx.x; q < (kClsY + 1) * (kClsX + 1); q += blockDim.x) {
+      const unsigned jj = (unsigned)q / (kClsX + 1), ii = (unsigned)q - jj * (kClsX + 1);
+      const long long gi = (long long)i0 + ii, gj = (long long)j0 + jj;
+      unsigned char b = 0;
+      if (gi < F.nx && gj < F.ny) b = node_above<T>(F, f, k * sxy + gj * sx + gi);
+      bits[buf][jj][ii] = b;
+    }
+  };
+  load_plane(0, S.kfirst + k0);
+  for (long long kl = k0; kl < k1; kl++) {
+    const int cur = (int)((kl - k0) & 1), nxt = cur ^ 1;
+    load_plane(nxt, S.kfirst + kl + 1);
+    __syncthreads();
+    const unsigned i = i0 + threadIdx.x;
+    if (i < ncx) {
+      const int tx = threadIdx.x;
+#pragma unroll
+      for (int jj = 0; jj < kClsY; jj++) {
+        const unsigned j = j0 + jj;
+        if (j >= ncy) break;
+        const unsigned code = bits[cur][jj][tx] | (bits[cur][jj][tx + 1] << 1) | (bits[cur][jj + 1][tx] << 2) |
+                              (bits[cur][jj + 1][tx + 1] << 3) | (bits[nxt][jj][tx] << 4) |
+                              (bits[nxt][jj][tx + 1] << 5) | (bits[nxt][jj + 1][tx] << 6) |
+                              (bits[nxt][jj + 1][tx + 1] << 7);
+        counts[((size_t)kl * ncy + j) * ncx + i] = lut[code];
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -125,12 +186,21 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
 
   unsigned char cnt[kScanItems];
   unsigned sum = 0;
+  if (base + kScanItems <= n) {
+    /* one 16-byte load (base is a multiple of 16, the buffer 256-byte aligned) */
+    const uint4 v = *reinterpret_cast<const uint4*>(counts + base);
+    const unsigned wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) {
-    const long long c = base + q;
-    cnt[q] = c < n ? counts[c] : 0;
-    sum += cnt[q];
+    for (int q = 0; q < kScanItems; q++) cnt[q] = (unsigned char)(wv[q >> 2] >> (8 * (q & 3)));
+  } else {
+#pragma unroll
+    for (int q = 0; q < kScanItems; q++) {
+      const long long c = base + q;
+      cnt[q] = c < n ? counts[c] : 0;
+    }
   }
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) sum += cnt[q];
   /* block-wide exclusive scan of the per-thread sums */
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long incl = sum;
@@ -213,12 +283,28 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
   }
   __syncthreads();
   unsigned long long run = s_excl + thread_excl;
+  unsigned out[kScanItems];
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) {
-    const long long c = base + q;
-    if (c <= n) offsets[c] = (unsigned)run;  /* offsets[n] = total */
-    if (c == n) *total = run;
+    out[q] = (unsigned)run;
     run += cnt[q];
+  }
+  if (base + kScanItems <= n) {
+    /* four 16-byte stores (offsets + base is 64-byte aligned) */
+    uint4* o = reinterpret_cast<uint4*>(offsets + base);
+#pragma unroll
+    for (int q = 0; q < kScanItems / 4; q++) o[q] = make_uint4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < kScanItems; q++) {
+      const long long c = base + q;
+      if (c <= n) offsets[c] = out[q]; /* offsets[n] = total */
+    }
+  }
+  if (n >= base && n < base + kScanItems) {
+    unsigned long long tot = s_excl + thread_excl;
+    for (long long c = base; c < n; c++) tot += cnt[c - base];
+    *total = tot;
   }
 }
 
@@ -266,8 +352,9 @@ __device__ __forceinline__ unsigned cell_code_any(const FieldDev& F, long long i
 __device__ __forceinline__ void exact_vertices(const Geo& G, long long t, d3 v[3]) {
   const unsigned c = G.tri_cell[t];
   const unsigned r = (G.meta[t] >> kMetaRankShift) & 15;
-  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
-  const long long i = c % ncx, j = (c / ncx) % ncy, k = G.S.kfirst + c / (ncx * ncy);
+  unsigned ui, uj, ukl;
+  cell_ijk(c, (unsigned)(G.F.nx - 1), (unsigned)(G.F.ny - 1), ui, uj, ukl);
+  const long long i = ui, j = uj, k = G.S.kfirst + ukl;
   double val[8];
   const unsigned code = cell_code_any(G.F, i, j, k, val);
   const unsigned long long e = __ldg(G.lut + code * 12 + r);
@@ -308,10 +395,11 @@ __device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, d3 p0, do
     for (int i = 0; i < 3; i++) {
       const float p = to_f(a0[i]);
       q[i] = p - pc[i];
-      eq[i] = 1.1f * kU32 * (fabsf(p) + fabsf(pc[i]) + fabsf(q[i])) + 1e-30f;
+      eq[i] = 1.1f * kU32 * (2.f * fabsf(p) + fabsf(pc[i]) + fabsf(q[i])) + 1e-30f;
     }
     return;
   }
+  /* f: two truncating conversions (2u each) and a division (u) */
   const float f = to_f(dsub(vt, v0)) / to_f(dv);
   const float af = fabsf(f);
 #pragma unroll
@@ -320,7 +408,7 @@ __device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, d3 p0, do
     const float d = x1 - x0;
     const float p = x0 + f * d;
     q[i] = p - pc[i];
-    const float ep = kU32 * (fabsf(x0) + fabsf(p) + af * (fabsf(x0) + fabsf(x1) + 5.1f * fabsf(d)));
+    const float ep = kU32 * (2.f * fabsf(x0) + fabsf(p) + af * (2.f * fabsf(x0) + 2.f * fabsf(x1) + 7.2f * fabsf(d)));
     eq[i] = 1.1f * (ep + kU32 * (fabsf(pc[i]) + fabsf(q[i]))) + 1e-30f;
   }
 }
@@ -388,9 +476,9 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
        t += (long long)gridDim.x * blockDim.x) {
     const unsigned c = tri_cell[t];
     const unsigned r = (unsigned)(t - offsets[c]);
-    const long long i = c % ncx;
-    const long long j = (c / ncx) % ncy;
-    const long long k = S.kfirst + c / (ncx * ncy);
+    unsigned ui, uj, ukl;
+    cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
+    const long long i = ui, j = uj, k = S.kfirst + ukl;
     double val[8];
     const unsigned code = cell_code<T>(F, i, j, k, val);
     const unsigned long long e = lut[code * 12 + r];
@@ -643,8 +731,10 @@ __device__ __forceinline__ unsigned long long append_slot(unsigned long long* co
 __device__ __forceinline__ void centre_range(float lo, float hi, long long n, long long& a, long long& b) {
   const float fa = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + lo) * (float)n - 0.5f - 1e-3f));
   const float fb = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + hi) * (float)n - 0.5f + 1e-3f));
-  a = max(0LL, (long long)ceilf(fa));
-  b = min(n - 1, (long long)floorf(fb));
+  /* 32-bit conversions (the 64-bit ones run on the FP64 pipe); NaN gives an empty range */
+  const int ia = __float2int_ru(fa), ib = __float2int_rd(fb);
+  a = fa == fa ? max(0LL, (long long)ia) : 1;
+  b = fb == fb ? min(n - 1, (long long)ib) : 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -725,16 +815,17 @@ k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, T
     float errA;
     const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
     const float rai = errA / (fabsf(A) - errA) + 1.1f * kU32;
-    /* regular: the reference's area is certainly not clamped to +-1e-16 and
-       its sign and size are known to within half; then every covered pixel
-       centre lies inside the triangle's extent (its weights are barycentric
-       up to the -1e-8 slack) */
-    const bool regular = !(meta & kMetaUndecided) && isfinite(A) && isfinite(eps) && fabsf(A) - errA > 1e-15f &&
-                         rai < 0.5f && eps < 1e-3f && zr < 1e-3f;
-    const unsigned long long ti = append_slot(R.tiny_count, !regular);
-    if (!regular) {
-      if (ti < R.tiny_cap) R.tiny[ti] = (unsigned)t;
-      else tiny_triangle<false>(G, scene, t, R, order_base, nullptr);
+    /* unclamped: the reference's area is certainly not clamped to +-1e-16
+       (render.c:108-111), so its weights are barycentric up to the -1e-8
+       slack and every covered pixel centre lies inside the triangle's
+       extent; the per-pixel weight bounds are used when they are tight
+       enough to decide anything (rai < 0.5) */
+    const bool unclamped = !(meta & kMetaUndecided) && isfinite(A) && isfinite(eps) && fabsf(A) - errA > 1e-15f &&
+                           eps < 1e-3f && zr < 1e-3f;
+    const bool weights_ok = rai < 0.5f;
+    const unsigned long long ti = append_slot(R.tiny_count, !unclamped);
+    if (!unclamped) {
+      if (ti < R.tiny_cap) R.tiny[ti] = (unsigned)t; /* overflow: the host re-runs the slab */
       continue;
     }
     const float ai = 1.f / A;
@@ -781,8 +872,8 @@ k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, T
         const float ew0 = 1.25f * (k * e0 + fabsf(w0) * (rai + kU32)) + 1e-30f;
         const float ew1 = 1.25f * (k * e1 + fabsf(w1) * (rai + kU32)) + 1e-30f;
         const float ew2 = 1.25f * (k * e2 + fabsf(w2) * (rai + kU32)) + 1e-30f;
-        const bool out = (w0 + ew0 < kWOut) || (w1 + ew1 < kWOut) || (w2 + ew2 < kWOut);
-        const bool inside = !out && (w0 - ew0 > kWIn) && (w1 - ew1 > kWIn) && (w2 - ew2 > kWIn);
+        const bool out = weights_ok && ((w0 + ew0 < kWOut) || (w1 + ew1 < kWOut) || (w2 + ew2 < kWOut));
+        const bool inside = weights_ok && !out && (w0 - ew0 > kWIn) && (w1 - ew1 > kWIn) && (w2 - ew2 > kWIn);
         if (CHECK && ex_ok) {
           double x0, x1, x2;
           const bool cov = exact_weights(ex, i, j, R.xs, R.ys, x0, x1, x2);
@@ -791,17 +882,13 @@ k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, T
         }
         if (inside) atomicMax(R.zlo + j * W + i, f_key(dlo));
         const unsigned long long idx = append_slot(R.cand_count, !out);
-        if (!out) {
-          if (idx < R.cand_cap) {
-            Candidate cd;
-            cd.t = (unsigned)t;
-            cd.pixel = (unsigned)(j * W + i);
-            cd.dhi = dhi;
-            cd.pad = 0;
-            R.cand[idx] = cd;
-          } else {
-            exact_fragment(G, scene, t, i, j, R, order_base); /* list full: resolve in place */
-          }
+        if (!out && idx < R.cand_cap) { /* overflow: the host re-runs the slab */
+          Candidate cd;
+          cd.t = (unsigned)t;
+          cd.pixel = (unsigned)(j * W + i);
+          cd.dhi = dhi;
+          cd.pad = 0;
+          R.cand[idx] = cd;
         }
       }
     }
@@ -827,7 +914,8 @@ __global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev 
     const Candidate c = R.cand[q];
     /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
     if (f_key(c.dhi) < R.zlo[c.pixel]) continue;
-    exact_fragment(G, scene, c.t, c.pixel % scene.width, c.pixel / scene.width, R, order_base);
+    const unsigned pj = c.pixel / (unsigned)scene.width;
+    exact_fragment(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base);
   }
 }
 
@@ -840,53 +928,88 @@ __device__ __forceinline__ bool slab_owner(const Geo& G, unsigned long long lo, 
   const unsigned long long order = lo >> 24;
   if (order < order_base) return false;
   const unsigned long long rel = order - order_base;
-  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
-  const unsigned long long c = rel / 12;
-  if (c >= (unsigned long long)(G.S.nslices * ncx * ncy)) return false;
-  const long long kk = G.S.kfirst + (long long)(c / (unsigned long long)(ncx * ncy));
+  const unsigned long long ncx = (unsigned long long)(G.F.nx - 1), ncy = (unsigned long long)(G.F.ny - 1);
+  if (rel >= 12ULL * (unsigned long long)G.S.nslices * ncx * ncy) return false;
+  const unsigned c = (unsigned)(rel / 12ULL); /* the only 64-bit division, one per pixel */
+  const unsigned r = (unsigned)(rel - 12ULL * c);
+  const long long kk = G.S.kfirst + (long long)(c / (unsigned)(ncx * ncy));
   if (kk < G.S.krender0 || kk >= G.S.krender1) return false;
-  t = (long long)G.offsets[c] + (long long)(rel % 12);
+  t = (long long)G.offsets[c] + (long long)r;
   cl = (long long)c;
   return (unsigned long long)t < T_;
 }
 
-/*
- * One thread per pixel: list the pixels this slab won, and request the
- * weighted normal of every triangle that shares a cube edge with a vertex of
- * a winning triangle (normal.c:78-158 neighbourhoods), each once.
- */
+/* one thread per pixel: list the pixels this slab won */
 __global__ void __launch_bounds__(256)
 k_winners(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
           unsigned long long order_base) {
   const unsigned long long T_ = *total_p;
   const long long npx = scene.width * scene.height;
-  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
     long long t = 0, c = 0;
     const bool won = slab_owner(G, R.canvas[p].lo, order_base, T_, t, c);
     const unsigned long long w = append_slot(R.win_count, won);
     if (!won) continue;
     R.win[w] = make_uint2((unsigned)p, (unsigned)t);
-    const unsigned meta = tri.meta[t];
-    for (int m = 0; m < 3; m++) {
-      const int e = (meta >> (5 * m)) & 31;
-      const int nn = c_nb_count[e];
-      for (int q = 0; q < nn; q++) {
-        const long long nc = c + (long long)c_nb[e][q][0] * ncx * ncy + (long long)c_nb[e][q][1] * ncx +
-                             (long long)c_nb[e][q][2];
-        const unsigned le = (unsigned)c_nb[e][q][3];
-        const unsigned u0 = G.offsets[nc], u1 = G.offsets[nc + 1];
-        for (unsigned u = u0; u < u1; u++) {
-          const unsigned om = tri.meta[u];
-          if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
-            if (atomicOr(tri.need + u, 1u) == 0u) {
-              const unsigned long long s = atomicAdd(R.need_count, 1ULL);
-              R.need[s] = u;
+  }
+}
+
+/*
+ * One thread per won pixel: request the weighted normal of every triangle
+ * that shares a cube edge with a vertex of the owner (normal.c:78-158
+ * neighbourhoods), each triangle once; requests are appended per warp.
+ */
+__global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R) {
+  const unsigned long long n = *R.win_count;
+  const unsigned ncx = (unsigned)(G.F.nx - 1), ncy = (unsigned)(G.F.ny - 1);
+  const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
+  /* every thread of a block runs the same number of iterations so that the
+     warp-wide appends below see all lanes */
+  for (unsigned long long it = blockIdx.x; it < iters; it += gridDim.x) {
+    const unsigned long long q = it * blockDim.x + threadIdx.x;
+    unsigned got[48];
+    int ng = 0;
+    if (q < n) {
+      const long long t = R.win[q].y;
+      const long long c = G.tri_cell[t];
+      const unsigned meta = tri.meta[t];
+      for (int m = 0; m < 3; m++) {
+        const int e = (meta >> (5 * m)) & 31;
+        const int nn = c_nb_count[e];
+        for (int s = 0; s < nn; s++) {
+          const long long nc = c + (long long)c_nb[e][s][0] * ncx * ncy + (long long)c_nb[e][s][1] * ncx +
+                               (long long)c_nb[e][s][2];
+          const unsigned le = (unsigned)c_nb[e][s][3];
+          const unsigned u0 = G.offsets[nc], u1 = G.offsets[nc + 1];
+          for (unsigned u = u0; u < u1; u++) {
+            const unsigned om = tri.meta[u];
+            if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
+              if (atomicOr(tri.need + u, 1u) == 0u) {
+                if (ng < 48) {
+                  got[ng++] = u;
+                } else {
+                  const unsigned long long s1 = atomicAdd(R.need_count, 1ULL);
+                  R.need[s1] = u;
+                }
+              }
             }
           }
         }
       }
     }
+    /* warp-level exclusive scan of the per-thread counts, one atomic per warp */
+    const int lane = threadIdx.x & 31;
+    unsigned incl = (unsigned)ng;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+      if (lane >= d) incl += y;
+    }
+    const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(R.need_count, (unsigned long long)total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31) + (incl - (unsigned)ng);
+    for (int g = 0; g < ng; g++) R.need[base + g] = got[g];
   }
 }
 
@@ -922,7 +1045,8 @@ k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
     exact_vertices(G, t, v);
     ExactTri x;
     double w0, w1, w2;
-    if (!exact_tri(scene, v, x) || !exact_weights(x, p % W, p / W, R.xs, R.ys, w0, w1, w2)) continue;
+    const long long pj = (unsigned)p / (unsigned)W, pi = p - pj * W;
+    if (!exact_tri(scene, v, x) || !exact_weights(x, pi, pj, R.xs, R.ys, w0, w1, w2)) continue;
     const unsigned meta = tri.meta[t];
     const long long c = G.tri_cell[t];
     const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, G.offsets, tri);
@@ -1023,10 +1147,10 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
 }
 
 void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, cudaStream_t st) {
-  const long long n = S.nslices * (F.nx - 1) * (F.ny - 1);
-  const int g = grid_for(n, 256, 16);
-  if (F.is_f32) k_classify<float><<<g, 256, 0, st>>>(F, S, counts);
-  else k_classify<double><<<g, 256, 0, st>>>(F, S, counts);
+  const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
+                  (unsigned)((S.nslices + kClsZ - 1) / kClsZ));
+  if (F.is_f32) k_classify<float><<<grid, kClsX, 0, st>>>(F, S, counts);
+  else k_classify<double><<<grid, kClsX, 0, st>>>(F, S, counts);
 }
 
 void launch_scan(const unsigned char* counts, long long n, unsigned* offsets,
@@ -1091,9 +1215,11 @@ void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, con
 void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                     const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
                     cudaStream_t st) {
+  (void)tri_bound;
   const long long npx = scene.width * scene.height;
   k_winners<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, total, tri, R, order_base);
-  k_wn<<<grid_for(tri_bound, 256, 8), 256, 0, st>>>(G, tri, R);
+  k_request<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, tri, R);
+  k_wn<<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
   k_shade<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, tri, R, rgb);
 }
 

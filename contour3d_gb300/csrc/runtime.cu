@@ -149,6 +149,27 @@ static long long h_key(double x) {
 }
 static unsigned long long h_depth_key(double x) { return (unsigned long long)h_key(x) ^ 0x8000000000000000ULL; }
 
+static unsigned h_fkey(float x) {
+  unsigned u;
+  memcpy(&u, &x, sizeof u);
+  if ((u << 1) == 0) u = 0;
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+/* the least float strictly above the threshold: for a float v,
+   threshold < (double)v  <=>  v >= that float (no such float: never above) */
+static void set_float_threshold(FieldDev &F) {
+  const double t = F.threshold;
+  F.thr_f_ok = 0;
+  F.thr_f_key = 0;
+  if (std::isnan(t) || t == (double)INFINITY) return;
+  /* beyond FLT_MAX only +inf is above; (float) of such t rounds to +inf or FLT_MAX */
+  float f = (float)t;
+  if (!((double)f > t)) f = nextafterf(f, INFINITY);
+  F.thr_f_key = h_fkey(f);
+  F.thr_f_ok = 1;
+}
+
 /* ---------------- marching-tetrahedra tables (triangulate.c) ---------------- */
 /* cube corners of the six tetrahedra sharing the 0-7 diagonal */
 static const int kTet[6][4] = {{0, 7, 3, 1}, {0, 7, 1, 5}, {0, 7, 5, 4}, {0, 7, 4, 6}, {0, 7, 6, 2}, {0, 7, 2, 3}};
@@ -471,6 +492,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   F.threshold = ci.threshold;
   F.thr_key = h_key(ci.threshold);
   F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
+  set_float_threshold(F);
   c.stats.cells += (uint64_t)(ncx * ncy * ncz);
 
   /* rendered cell slices are [1, ncz - 2]; each slab also triangulates one
@@ -559,42 +581,56 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
       c.stats.kernel_launches += 2;
     } else {
-      /* candidates: about one per covered pixel; the lists fall back to
-         in-place resolution when full, so their sizes only affect speed */
-      const unsigned long long want = std::max<unsigned long long>(T / 2, 1ULL << 20);
-      const unsigned long long tiny_want = std::max<unsigned long long>(T / 8, 1ULL << 16);
+      /* candidate and tiny lists: about one entry per covered pixel and a few
+         percent of the triangles; when one overflows, the slab's raster passes
+         run again with larger lists (every z-buffer update is an idempotent
+         maximum, so repeating them is harmless) */
       const size_t npx = (size_t)(sd.width * sd.height);
-      if (c.cand.ensure(sizeof(Candidate) * want) || c.tiny.ensure(sizeof(unsigned) * tiny_want) ||
-          c.win.ensure(sizeof(uint2) * npx) || c.need.ensure(sizeof(unsigned) * T))
-        return 1;
+      if (c.win.ensure(sizeof(uint2) * npx) || c.need.ensure(sizeof(unsigned) * T)) return 1;
+      unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
+      unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
       RasterDev RS = R;
       unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 4);
-      RS.cand = c.cand.as<Candidate>();
-      RS.cand_cap = c.cand.cap / sizeof(Candidate);
-      RS.cand_count = counters + 0;
-      RS.tiny = c.tiny.as<unsigned>();
-      RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
-      RS.tiny_count = counters + 1;
+      unsigned long long *h_cnt = h_total + 1;
+      for (int attempt = 0;; attempt++) {
+        if (c.cand.ensure(sizeof(Candidate) * cand_want) || c.tiny.ensure(sizeof(unsigned) * tiny_want)) return 1;
+        RS.cand = c.cand.as<Candidate>();
+        RS.cand_cap = c.cand.cap / sizeof(Candidate);
+        RS.cand_count = counters + 0;
+        RS.tiny = c.tiny.as<unsigned>();
+        RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
+        RS.tiny_count = counters + 1;
+        C3D_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), st));
+        launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
+        launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
+        if (c.stage_timing) cudaEventRecord(c.evs[5], st);
+        launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
+        if (c.stage_timing) cudaEventRecord(c.evs[6], st);
+        c.stats.kernel_launches += 3;
+        C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaStreamSynchronize(st));
+        if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
+        if (attempt > 4) {
+          log_error("raster candidate lists keep overflowing (%llu, %llu)", h_cnt[0], h_cnt[1]);
+          return 1;
+        }
+        c.stats.candidate_overflows += 1;
+        cand_want = std::max<unsigned long long>(cand_want, h_cnt[0] + h_cnt[0] / 4);
+        tiny_want = std::max<unsigned long long>(tiny_want, h_cnt[1] + h_cnt[1] / 4);
+      }
+      c.stats.candidates += h_cnt[0];
+      c.stats.tiny += h_cnt[1];
       RS.win = c.win.as<uint2>();
       RS.win_count = counters + 2;
       RS.need = c.need.as<unsigned>();
       RS.need_count = counters + 3;
-      C3D_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st));
+      C3D_CUDA(cudaMemsetAsync(counters + 2, 0, 2 * sizeof(unsigned long long), st));
       C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
-      launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
-      launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
-      if (c.stage_timing) cudaEventRecord(c.evs[5], st);
-      launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
-      if (c.stage_timing) cudaEventRecord(c.evs[6], st);
       launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
-      c.stats.kernel_launches += 6;
+      c.stats.kernel_launches += 4;
       if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-      unsigned long long *h_cnt = h_total + 1;
-      C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaMemcpyAsync(h_cnt + 2, counters + 2, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
-      c.stats.candidates += h_cnt[0];
-      if (h_cnt[0] > RS.cand_cap) c.stats.candidate_overflows += h_cnt[0] - RS.cand_cap;
-      c.stats.tiny += h_cnt[1];
       c.stats.winners += h_cnt[2];
       c.stats.normals += h_cnt[3];
       if (c.stage_timing) {
@@ -1091,6 +1127,7 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   F.threshold = obj->threshold;
   F.thr_key = h_key(obj->threshold);
   F.thr_nan = std::isnan(obj->threshold) ? 1 : 0;
+  set_float_threshold(F);
   SlabDev S = {0, nz - 1, 0, 0};
   launch_classify(F, S, c.counts.as<unsigned char>(), st);
   const size_t ncell = (size_t)((nx - 1) * (ny - 1) * (nz - 1));

@@ -122,7 +122,7 @@ typedef struct {
   uint64_t cells;             /* cells classified (cell x threshold) */
   uint64_t triangles;         /* triangles emitted (triangulated set, all slabs) */
   uint64_t candidates;        /* fragments the single-precision filter could not settle */
-  uint64_t candidate_overflows; /* of those, resolved in place because the list was full */
+  uint64_t candidate_overflows; /* raster passes repeated because a list was full */
   uint64_t tiny;              /* triangles too small for the FP32 filter (resolved in FP64) */
   uint64_t winners;           /* pixels whose owner was shaded (summed over slabs) */
   uint64_t normals;           /* weighted face normals computed for shading */

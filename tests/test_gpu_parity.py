@@ -181,3 +181,33 @@ def test_filter_settles_most_fragments(gpu):
     st = gpu.stats()
     assert st.candidate_overflows == 0
     assert 0 < st.candidates < 4 * st.triangles
+
+
+def test_float32_field_threshold_edges(gpu, oracle):
+    """float32 fields classify with a float threshold key; edge thresholds
+    (between floats, at a float, +-0, huge) must count exactly like the
+    double comparison of the widened values."""
+    import torch  # noqa: F401
+    rng = np.random.default_rng(5)
+    f32 = (rng.standard_normal((18, 17, 19)) * 0.5).astype(np.float32)
+    f32.flat[::97] = 0.0
+    f32.flat[5::101] = -0.0
+    as64 = f32.astype(np.float64)
+    for thr in (0.0, -0.0, float(f32.flat[3]), float(np.nextafter(f32.flat[3], 1)) * 0.5 + float(f32.flat[3]) * 0.5,
+                1e-50, -1e-50, 3.5e38, -3.5e38, 0.1):
+        a, ta = gpu.cell_counts(as64, thr)
+        b, tb = oracle.cell_counts(as64, thr)
+        assert ta == tb and np.array_equal(a, b)
+    # the device classify of a float32 field (render path) against the oracle on the widened field
+    scene = _abi.make_scene(cases.CAM0, cases.CENTRE, 64, 48)
+    out = torch.zeros(64 * 48 * 3, dtype=torch.uint8, device="cuda")
+    dev = torch.from_numpy(f32).cuda()
+    grids = [_abi.unit_grid(n) for n in (19, 17, 18)]
+    for thr in (0.0, float(f32.flat[7]), 0.3):
+        assert gpu.render_device(scene, [(dev.data_ptr(), 1, (19, 17, 18), grids, thr, (9, 200, 90))],
+                                 out.data_ptr()) == 0
+        torch.cuda.synchronize()
+        scene.contours = [_abi.Contour(as64, thr, (9, 200, 90))]
+        ref = oracle.render(scene)
+        scene.contours = []
+        assert np.array_equal(out.cpu().numpy().reshape(48, 64, 3), ref)
