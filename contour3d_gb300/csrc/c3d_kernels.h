@@ -21,6 +21,9 @@ struct FieldDev {
   const double* gy;
   const double* gz;
   const double* nodes;      /* Cartesian node positions (3 per node) or null = identity */
+  const float* gxf;         /* node coordinates rounded to float (identity converter) */
+  const float* gyf;
+  const float* gzf;
   double threshold;
   long long thr_key;        /* integer key of the threshold (d_key) */
   int thr_nan;
@@ -41,9 +44,10 @@ struct SlabDev {
 struct TriDev {
   double* wn[3];      /* area * face normal, where requested */
   unsigned* meta;     /* edge ids (3 x 5 bits) | flags | rank in the cell */
-  float* pf[9];       /* FP32 screen position and depth x 3, rendered triangles */
-  float* perr;        /* bound on |screen x, y - the reference's value| */
-  float* zrel;        /* relative bound on the depth */
+  /* k_cover's input, 3 float4 per triangle: x0 y0 z0 x1 | y1 z1 x2 y2 |
+     z2 err_xy err_z meta -- FP32 screen positions and depths, the bound on
+     |screen x, y - the reference's value| and the relative depth bound */
+  float4* rec;
   unsigned* need;     /* 1 once the weighted normal was requested */
   double* vert[9];    /* inspection: exact vertices */
   double* vn[9];      /* inspection: vertex normals */
@@ -60,6 +64,7 @@ struct Geo {
   FieldDev F;
   SlabDev S;
   const unsigned long long* lut;
+  const unsigned char* codes;
   const unsigned* tri_cell;
   const unsigned* offsets;
   const unsigned* meta;
@@ -114,8 +119,9 @@ void launch_scan(const unsigned char* counts, long long n, unsigned* offsets,
                  unsigned* err, cudaStream_t st);
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
-                 const unsigned* offsets, const unsigned* tri_cell, const unsigned long long* total,
-                 long long tri_bound, const TriDev& tri, unsigned* checks, cudaStream_t st);
+                 const unsigned char* codes, const unsigned* offsets, const unsigned* tri_cell,
+                 const unsigned long long* total, long long tri_bound, const TriDev& tri, unsigned* checks,
+                 cudaStream_t st);
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
                       cudaStream_t st);
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,

@@ -62,6 +62,10 @@ __device__ __forceinline__ double load_value(const T* f, long long idx) {
   return (double)__ldg(f + idx);
 }
 
+__device__ __forceinline__ long long corner_index(const FieldDev& F, long long i, long long j, long long k, int c) {
+  return ((k + (c >> 2)) * F.ny + j + ((c >> 1) & 1)) * F.nx + i + (c & 1);
+}
+
 /* bit c of the result: threshold < value at corner c of cell (i, j, k) */
 template <typename T>
 __device__ __forceinline__ unsigned cell_code(const FieldDev& F, long long i, long long j, long long k,
@@ -97,7 +101,9 @@ __device__ __forceinline__ void cell_ijk(unsigned c, unsigned ncx, unsigned ncy,
 /*
  * Tiled over (x, y) and marching in z: each node's "above" bit is computed
  * once into shared memory (two planes, double-buffered), and each cell
- * assembles its 8-bit code from the bits of its corners.  A block owns
+ * assembles its 8-bit code from the bits of its corners.  The codes are
+ * kept: the scan maps them to triangle counts, and the later passes read
+ * them instead of comparing the eight corner values again.  A block owns
  * kClsX x kClsY cells of kClsZ consecutive slices.
  */
 constexpr int kClsX = 128;
@@ -119,10 +125,8 @@ __device__ __forceinline__ unsigned char node_above<float>(const FieldDev& F, co
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ counts) {
+__global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ codes) {
   __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
-  __shared__ unsigned char lut[256];
-  for (int q = threadIdx.x; q < 256; q += blockDim.x) lut[q] = c_code_count[q];
   const T* f = static_cast<const T*>(F.data);
   const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
   const unsigned i0 = blockIdx.x * kClsX, j0 = blockIdx.y * kClsY;
@@ -154,7 +158,7 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
                               (bits[cur][jj + 1][tx + 1] << 3) | (bits[nxt][jj][tx] << 4) |
                               (bits[nxt][jj][tx + 1] << 5) | (bits[nxt][jj + 1][tx] << 6) |
                               (bits[nxt][jj + 1][tx + 1] << 7);
-        counts[((size_t)kl * ncy + j) * ncx + i] = lut[code];
+        codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
       }
     }
     __syncthreads();
@@ -179,7 +183,9 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
   __shared__ unsigned s_tile;
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ unsigned long long s_excl;
+  __shared__ unsigned char s_count[256];
   if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+  s_count[threadIdx.x] = c_code_count[threadIdx.x];
   __syncthreads();
   const unsigned tile = s_tile;
   const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
@@ -191,12 +197,12 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
     const uint4 v = *reinterpret_cast<const uint4*>(counts + base);
     const unsigned wv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int q = 0; q < kScanItems; q++) cnt[q] = (unsigned char)(wv[q >> 2] >> (8 * (q & 3)));
+    for (int q = 0; q < kScanItems; q++) cnt[q] = s_count[(wv[q >> 2] >> (8 * (q & 3))) & 255];
   } else {
 #pragma unroll
     for (int q = 0; q < kScanItems; q++) {
       const long long c = base + q;
-      cnt[q] = c < n ? counts[c] : 0;
+      cnt[q] = c < n ? s_count[counts[c]] : 0;
     }
   }
 #pragma unroll
@@ -338,6 +344,13 @@ __device__ __forceinline__ d3 interpolate(double vt, d3 p0, double v0, d3 p1, do
   return v_add(p0, v_mul(f, v_sub(p1, p0)));
 }
 
+/* value at corner c of cell (i, j, k) */
+__device__ __forceinline__ double corner_value(const FieldDev& F, long long i, long long j, long long k, int c) {
+  const long long idx = ((k + (c >> 2)) * F.ny + j + ((c >> 1) & 1)) * F.nx + i + (c & 1);
+  return F.is_f32 ? (double)__ldg(static_cast<const float*>(F.data) + idx)
+                  : __ldg(static_cast<const double*>(F.data) + idx);
+}
+
 /* corner values and code of cell (i, j, k), element type chosen at run time */
 __device__ __forceinline__ unsigned cell_code_any(const FieldDev& F, long long i, long long j, long long k,
                                                   double vals[8]) {
@@ -355,13 +368,13 @@ __device__ __forceinline__ void exact_vertices(const Geo& G, long long t, d3 v[3
   unsigned ui, uj, ukl;
   cell_ijk(c, (unsigned)(G.F.nx - 1), (unsigned)(G.F.ny - 1), ui, uj, ukl);
   const long long i = ui, j = uj, k = G.S.kfirst + ukl;
-  double val[8];
-  const unsigned code = cell_code_any(G.F, i, j, k, val);
+  const unsigned code = G.codes[c];
   const unsigned long long e = __ldg(G.lut + code * 12 + r);
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-    v[q] = interpolate(G.F.threshold, corner_pos(G.F, i, j, k, a), val[a], corner_pos(G.F, i, j, k, b), val[b]);
+    v[q] = interpolate(G.F.threshold, corner_pos(G.F, i, j, k, a), corner_value(G.F, i, j, k, a),
+                       corner_pos(G.F, i, j, k, b), corner_value(G.F, i, j, k, b));
   }
 }
 
@@ -380,22 +393,22 @@ __device__ __forceinline__ void face_normal(const d3 v[3], d3& fn, double& area,
  * FP32 estimate of one vertex (triangulate.c:40-73) relative to the camera,
  * q = vertex - camera, with a bound per component on the distance to the
  * reference's FP64 value.  Only the two value differences are formed in FP64
- * (they cancel); everything else is single precision:
+ * (they cancel); the corner coordinates come as floats (node coordinates
+ * rounded once on the host); everything else is single precision:
  *   f = (vt - v0) / (v1 - v0)          relative error <= 3.1 u
  *   p = p0 + f (p1 - p0)               per component, bounded below
  */
-__device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, d3 p0, double v0, d3 p1, double v1, float q[3],
-                                         float eq[3]) {
+__device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, const float x0[3], double v0, const float x1[3],
+                                         double v1, float ce, float q[3], float eq[3]) {
+  /* x0, x1: corner coordinates rounded to float with error <= ce u |x| */
   const double dv = dsub(v1, v0);
   const float pc[3] = {s.f_cam[0], s.f_cam[1], s.f_cam[2]};
-  const double a0[3] = {p0.x, p0.y, p0.z}, a1[3] = {p1.x, p1.y, p1.z};
   if (abs_lt_1e8(dv)) {
     /* the reference keeps p0 itself */
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const float p = to_f(a0[i]);
-      q[i] = p - pc[i];
-      eq[i] = 1.1f * kU32 * (2.f * fabsf(p) + fabsf(pc[i]) + fabsf(q[i])) + 1e-30f;
+      q[i] = x0[i] - pc[i];
+      eq[i] = 1.1f * kU32 * (ce * fabsf(x0[i]) + fabsf(pc[i]) + fabsf(q[i])) + 1e-30f;
     }
     return;
   }
@@ -404,13 +417,30 @@ __device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, d3 p0, do
   const float af = fabsf(f);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    const float x0 = to_f(a0[i]), x1 = to_f(a1[i]);
-    const float d = x1 - x0;
-    const float p = x0 + f * d;
+    const float d = x1[i] - x0[i];
+    const float p = x0[i] + f * d;
     q[i] = p - pc[i];
-    const float ep = kU32 * (2.f * fabsf(x0) + fabsf(p) + af * (2.f * fabsf(x0) + 2.f * fabsf(x1) + 7.2f * fabsf(d)));
+    const float ep = kU32 * (ce * fabsf(x0[i]) + fabsf(p) +
+                             af * (ce * fabsf(x0[i]) + ce * fabsf(x1[i]) + 7.2f * fabsf(d)));
     eq[i] = 1.1f * (ep + kU32 * (fabsf(pc[i]) + fabsf(q[i]))) + 1e-30f;
   }
+}
+
+/* corner coordinates as floats, and the bound factor of their rounding */
+__device__ __forceinline__ float corner_pos_f(const FieldDev& F, long long i, long long j, long long k, int c,
+                                              float x[3]) {
+  const long long ii = i + (c & 1), jj = j + ((c >> 1) & 1), kk = k + (c >> 2);
+  if (F.nodes) {
+    const double* p = F.nodes + 3 * ((kk * F.ny + jj) * F.nx + ii);
+    x[0] = to_f(p[0]);
+    x[1] = to_f(p[1]);
+    x[2] = to_f(p[2]);
+    return 2.f;
+  }
+  x[0] = __ldg(F.gxf + ii);
+  x[1] = __ldg(F.gyf + jj);
+  x[2] = __ldg(F.gzf + kk);
+  return 1.f;
 }
 
 /*
@@ -465,8 +495,9 @@ __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], co
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
-       const unsigned* __restrict__ offsets, const unsigned* __restrict__ tri_cell,
-       const unsigned long long* __restrict__ total_p, TriDev tri, unsigned* __restrict__ checks) {
+       const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
+       const unsigned* __restrict__ tri_cell, const unsigned long long* __restrict__ total_p, TriDev tri,
+       unsigned* __restrict__ checks) {
   __shared__ unsigned long long lut[kLutEntries];
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
@@ -479,8 +510,7 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
     unsigned ui, uj, ukl;
     cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
     const long long i = ui, j = uj, k = S.kfirst + ukl;
-    double val[8];
-    const unsigned code = cell_code<T>(F, i, j, k, val);
+    const unsigned code = codes[c];
     const unsigned long long e = lut[code * 12 + r];
     unsigned edges = 0;
 #pragma unroll
@@ -494,8 +524,11 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
 #pragma unroll
       for (int q = 0; q < 3; q++) {
         const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-        float qv[3], eq[3], ex = 0.f, ez = 0.f;
-        vertex_q(scene, F.threshold, corner_pos(F, i, j, k, a), val[a], corner_pos(F, i, j, k, b), val[b], qv, eq);
+        float qv[3], eq[3], ex = 0.f, ez = 0.f, xa[3], xb[3];
+        const float ce = corner_pos_f(F, i, j, k, a, xa);
+        corner_pos_f(F, i, j, k, b, xb);
+        vertex_q(scene, F.threshold, xa, load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, a)), xb,
+                 load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, b)), ce, qv, eq);
         const int st = project_f(scene, qv, eq, X[q], Y[q], Z[q], ex, ez);
         if (st == 0) status = 0;
         else if (st < 0 && status != 0) status = -1;
@@ -508,7 +541,8 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
 #pragma unroll
         for (int q = 0; q < 3; q++) {
           const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-          v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), val[a], corner_pos(F, i, j, k, b), val[b]);
+          v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
+                             corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
         }
         bool ok = true;
 #pragma unroll
@@ -524,14 +558,12 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
       }
       if (status == 0) meta |= kMetaCulled;
       if (status < 0) meta |= kMetaUndecided;
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        tri.pf[3 * q + 0][t] = X[q];
-        tri.pf[3 * q + 1][t] = Y[q];
-        tri.pf[3 * q + 2][t] = Z[q];
-      }
-      tri.perr[t] = exy;
-      tri.zrel[t] = zr;
+      float4* rec = tri.rec + 3 * t;
+      rec[0] = make_float4(X[0], Y[0], Z[0], X[1]);
+      rec[1] = make_float4(Y[1], Z[1], X[2], Y[2]);
+      rec[2] = make_float4(Z[2], exy, zr, __uint_as_float(meta));
+    } else {
+      tri.rec[3 * t + 2] = make_float4(0.f, 0.f, 0.f, __uint_as_float(meta));
     }
     tri.meta[t] = meta;
   }
@@ -789,7 +821,7 @@ __device__ void tiny_triangle(const Geo& G, const SceneDev& s, long long t, cons
 }
 
 template <bool CHECK>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
         unsigned long long order_base, unsigned* __restrict__ checks) {
   const long long T_ = (long long)*total_p;
@@ -798,16 +830,12 @@ k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, T
      near surfaces raise the floors early */
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < T_; q += (long long)gridDim.x * blockDim.x) {
     const long long t = scene.z_descending ? T_ - 1 - q : q;
-    const unsigned meta = tri.meta[t];
+    const float4 r2 = __ldg(tri.rec + 3 * t + 2);
+    const unsigned meta = __float_as_uint(r2.w);
     if (!(meta & kMetaRendered) || (meta & kMetaCulled)) continue;
-    float X[3], Y[3], Z[3];
-#pragma unroll
-    for (int v = 0; v < 3; v++) {
-      X[v] = tri.pf[3 * v][t];
-      Y[v] = tri.pf[3 * v + 1][t];
-      Z[v] = tri.pf[3 * v + 2][t];
-    }
-    const float eps = tri.perr[t], zr = tri.zrel[t];
+    const float4 r0 = __ldg(tri.rec + 3 * t), r1 = __ldg(tri.rec + 3 * t + 1);
+    const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
+    const float eps = r2.y, zr = r2.z;
     /* inverse area (render.c:102-107) with its bound */
     const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
     const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
@@ -1147,6 +1175,7 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
 }
 
 void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, cudaStream_t st) {
+  /* `counts` receives the cell codes; k_scan turns them into counts */
   const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
                   (unsigned)((S.nslices + kClsZ - 1) / kClsZ));
   if (F.is_f32) k_classify<float><<<grid, kClsX, 0, st>>>(F, S, counts);
@@ -1169,15 +1198,16 @@ void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_ce
 long long scan_tiles(long long n) { return (n + kScanTile) / kScanTile; }
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
-                 const unsigned* offsets, const unsigned* tri_cell, const unsigned long long* total,
-                 long long tri_bound, const TriDev& tri, unsigned* checks, cudaStream_t st) {
+                 const unsigned char* codes, const unsigned* offsets, const unsigned* tri_cell,
+                 const unsigned long long* total, long long tri_bound, const TriDev& tri, unsigned* checks,
+                 cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
   if (checks) {
-    if (F.is_f32) k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
-    else k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
+    if (F.is_f32) k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
+    else k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
   } else {
-    if (F.is_f32) k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
-    else k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, offsets, tri_cell, total, tri, checks);
+    if (F.is_f32) k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
+    else k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
   }
 }
 

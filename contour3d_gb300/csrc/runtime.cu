@@ -307,6 +307,7 @@ struct Ctx {
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
   Buf zlo, xyf, cand, tiny, win, need, checks;
+  std::vector<double> h_grids; /* staging for node coordinates (synchronised per slab) */
   bool filter_check = false;
   HostBuf h_small, h_rgb, h_slots;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[8] = {};
@@ -405,7 +406,7 @@ struct FrameOut {
 };
 
 /* bytes per triangle of the slab arrays (see TriDev) */
-static const size_t kTriBytes = 3 * sizeof(double) + 2 * sizeof(unsigned) + 11 * sizeof(float);
+static const size_t kTriBytes = 3 * sizeof(double) + 48 + 2 * sizeof(unsigned);
 /* doubles per triangle of the inspection arrays: vertices, vertex normals, face normal, area */
 static const size_t kDbgDoubles = 22;
 
@@ -413,11 +414,8 @@ static TriDev tri_layout(void *base, size_t cap, double *dbg) {
   TriDev t;
   double *d = static_cast<double *>(base);
   for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
-  float *f = reinterpret_cast<float *>(d + 3 * cap);
-  for (int q = 0; q < 9; q++) t.pf[q] = f + q * cap;
-  t.perr = f + 9 * cap;
-  t.zrel = f + 10 * cap;
-  t.meta = reinterpret_cast<unsigned *>(f + 11 * cap);
+  t.rec = reinterpret_cast<float4 *>(d + 3 * cap);
+  t.meta = reinterpret_cast<unsigned *>(t.rec + 3 * cap);
   t.need = t.meta + cap;
   for (int q = 0; q < 9; q++) t.vert[q] = dbg ? dbg + q * cap : nullptr;
   for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + (9 + q) * cap : nullptr;
@@ -455,12 +453,19 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     dfield = c.field.p;
   }
-  /* node coordinates */
-  if (c.grids.ensure(sizeof(double) * (size_t)(nx + ny + nz))) return 1;
+  /* node coordinates, and their float roundings for the single-precision filter */
+  const size_t ng = (size_t)(nx + ny + nz);
+  if (c.grids.ensure(sizeof(double) * ng + sizeof(float) * ng)) return 1;
   double *g = c.grids.as<double>();
-  C3D_CUDA(cudaMemcpyAsync(g, ci.grid[0], sizeof(double) * nx, cudaMemcpyHostToDevice, st));
-  C3D_CUDA(cudaMemcpyAsync(g + nx, ci.grid[1], sizeof(double) * ny, cudaMemcpyHostToDevice, st));
-  C3D_CUDA(cudaMemcpyAsync(g + nx + ny, ci.grid[2], sizeof(double) * nz, cudaMemcpyHostToDevice, st));
+  float *gf = reinterpret_cast<float *>(g + ng);
+  c.h_grids.resize(ng * 3);
+  double *hg = c.h_grids.data();
+  float *hgf = reinterpret_cast<float *>(hg + ng);
+  memcpy(hg, ci.grid[0], sizeof(double) * nx);
+  memcpy(hg + nx, ci.grid[1], sizeof(double) * ny);
+  memcpy(hg + nx + ny, ci.grid[2], sizeof(double) * nz);
+  for (size_t q = 0; q < ng; q++) hgf[q] = (float)hg[q];
+  C3D_CUDA(cudaMemcpyAsync(g, hg, sizeof(double) * ng + sizeof(float) * ng, cudaMemcpyHostToDevice, st));
   const double *dnodes = nullptr;
   std::vector<double> nodes;
   if (!is_identity(ci.converter)) {
@@ -488,6 +493,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   F.gx = g;
   F.gy = g + nx;
   F.gz = g + nx + ny;
+  F.gxf = gf;
+  F.gyf = gf + nx;
+  F.gzf = gf + nx + ny;
   F.nodes = dnodes;
   F.threshold = ci.threshold;
   F.thr_key = h_key(ci.threshold);
@@ -553,8 +561,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     c.stats.triangles += T;
     c.stats.slabs += 1;
     if (T == 0) continue;
-    if (c.tri_cell.ensure(sizeof(unsigned) * T) || c.tri.ensure(kTriBytes * T)) return 1;
-    const size_t cap = c.tri.cap / kTriBytes;
+    /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
+       every sub-array stays aligned (and over-allocate so that cap >= T) */
+    if (c.tri_cell.ensure(sizeof(unsigned) * T) || c.tri.ensure(kTriBytes * (T + 64))) return 1;
+    const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
+    if (cap < T) {
+      log_error("internal: triangle buffer capacity %zu below %llu", cap, T);
+      return 1;
+    }
     double *dbg = nullptr;
     if (sink) {
       if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap)) return 1;
@@ -564,8 +578,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
     launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
     if (c.stage_timing) cudaEventRecord(c.evs[3], st);
-    launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total,
-                (long long)T, tri, checks, st);
+    launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+                c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, checks, st);
     if (c.stage_timing) cudaEventRecord(c.evs[4], st);
     c.stats.kernel_launches += 2;
     const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
@@ -573,6 +587,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     G.F = F;
     G.S = S;
     G.lut = c.lut.as<unsigned long long>();
+    G.codes = c.counts.as<unsigned char>();
     G.tri_cell = c.tri_cell.as<unsigned>();
     G.offsets = c.offsets.as<unsigned>();
     G.meta = tri.meta;
@@ -1134,8 +1149,14 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   std::vector<uint8_t> h(ncell);
   if (cudaMemcpyAsync(h.data(), c.counts.p, ncell, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  std::vector<unsigned long long> lut;
+  unsigned char count_of[256];
+  build_tables(lut, count_of);
   long total = 0;
-  for (size_t q = 0; q < ncell; q++) total += h[q];
+  for (size_t q = 0; q < ncell; q++) {
+    h[q] = count_of[h[q]]; /* the classify pass stores cell codes */
+    total += h[q];
+  }
   if (counts) memcpy(counts, h.data(), ncell);
   return total;
 }
