@@ -18,7 +18,14 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
 #include <mutex>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 #include "contour3d.h"
 #include "contour3d_gb300.h"
@@ -252,25 +259,31 @@ static void build_tables(std::vector<unsigned long long> &lut, unsigned char cou
 }
 
 /* ---------------- device context ---------------- */
+/* device bytes held by every library buffer of the process */
+static std::atomic<unsigned long long> g_device_bytes{0};
+
 struct Buf {
   void *p = nullptr;
   size_t cap = 0;
   int ensure(size_t bytes) {
     if (bytes <= cap) return 0;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
+    release();
     const size_t want = bytes + bytes / 4 + 256;
     if (cudaMalloc(&p, want) != cudaSuccess) {
       cudaGetLastError();
+      p = nullptr;
       log_error("device allocation of %zu bytes failed", want);
       return 1;
     }
     cap = want;
+    g_device_bytes += want;
     return 0;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_device_bytes -= cap;
+    }
     p = nullptr;
     cap = 0;
   }
@@ -337,9 +350,19 @@ static int ctx_init(Ctx &c) {
   std::vector<unsigned long long> lut;
   unsigned char count[256];
   build_tables(lut, count);
-  if (upload_tables(count, kNb, kNbCount)) {
-    log_error("constant table upload failed");
-    return 1;
+  {
+    /* constant tables: once per device for every context of the process */
+    static std::mutex tables_mu;
+    static bool uploaded[64] = {false};
+    std::lock_guard<std::mutex> lk(tables_mu);
+    if (dev < 0 || dev >= 64) return 1;
+    if (!uploaded[dev]) {
+      if (upload_tables(count, kNb, kNbCount)) {
+        log_error("constant table upload failed");
+        return 1;
+      }
+      uploaded[dev] = true;
+    }
   }
   if (c.lut.ensure(sizeof(unsigned long long) * kLutEntries)) return 1;
   C3D_CUDA(cudaMemcpy(c.lut.p, lut.data(), sizeof(unsigned long long) * kLutEntries, cudaMemcpyHostToDevice));
@@ -1023,31 +1046,39 @@ extern "C" int contour3d_gb300_render(const contour3d_vector_t *camera_position,
   return render_frame(g_ctx, f, out);
 }
 
-extern "C" int contour3d_gb300_render_device(const contour3d_vector_t *camera_position,
-                                             const contour3d_vector_t *light_direction, const size_t screen_sizes[2],
-                                             const contour3d_vector_t *screen_center,
-                                             const contour3d_vector_t screen_local[2],
-                                             const contour3d_color_t *bg_color, size_t num_fields,
-                                             const contour3d_gb300_field_t *fields, size_t num_lines,
-                                             const contour3d_line_obj_t *lines, uint8_t *rgb_out, void *stream) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (check_common(camera_position, light_direction, screen_sizes, screen_center, screen_local, bg_color)) return 1;
-  if ((num_fields && !fields) || (num_lines && !lines) || !rgb_out) {
-    log_error("null field, line or output pointer");
+/* true for memory the device can address (device or managed allocations) */
+static bool is_device_pointer(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+/* a device-resident frame description -> the internal frame */
+static int frame_from_fields(FrameIn &f, const V *camera_position, const V *light_direction, const size_t sizes[2],
+                             const V *screen_center, const V screen_local[2], const contour3d_color_t *bg,
+                             size_t num_fields, const contour3d_gb300_field_t *fields, size_t num_lines,
+                             const contour3d_line_obj_t *lines) {
+  if (check_common(camera_position, light_direction, sizes, screen_center, screen_local, bg)) return 1;
+  if ((num_fields && !fields) || (num_lines && !lines)) {
+    log_error("null field or line array");
     return 1;
   }
-  if (ctx_init(g_ctx)) return 1;
-  FrameIn f;
-  f.scene = make_scene(camera_position, light_direction, screen_sizes, screen_center, screen_local);
-  f.bg = *bg_color;
+  f.scene = make_scene(camera_position, light_direction, sizes, screen_center, screen_local);
+  f.bg = *bg;
   f.lines = lines;
   f.nlines = num_lines;
-  f.stream = stream ? static_cast<cudaStream_t>(stream) : g_ctx.own_stream;
   for (size_t n = 0; n < num_fields; n++) {
     const contour3d_gb300_field_t *fd = fields + n;
     if (!fd->device_array || !fd->grids[0] || !fd->grids[1] || !fd->grids[2] ||
         (fd->dtype != CONTOUR3D_GB300_F64 && fd->dtype != CONTOUR3D_GB300_F32)) {
       log_error("field %zu: null array/grid or unknown dtype", n);
+      return 1;
+    }
+    if (!is_device_pointer(fd->device_array)) {
+      log_error("field %zu: the array is not device memory", n);
       return 1;
     }
     ContourIn ci;
@@ -1063,6 +1094,27 @@ extern "C" int contour3d_gb300_render_device(const contour3d_vector_t *camera_po
     ci.color = fd->color;
     f.contours.push_back(ci);
   }
+  return 0;
+}
+
+extern "C" int contour3d_gb300_render_device(const contour3d_vector_t *camera_position,
+                                             const contour3d_vector_t *light_direction, const size_t screen_sizes[2],
+                                             const contour3d_vector_t *screen_center,
+                                             const contour3d_vector_t screen_local[2],
+                                             const contour3d_color_t *bg_color, size_t num_fields,
+                                             const contour3d_gb300_field_t *fields, size_t num_lines,
+                                             const contour3d_line_obj_t *lines, uint8_t *rgb_out, void *stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!rgb_out || !is_device_pointer(rgb_out)) {
+    log_error("the output pointer is not device memory");
+    return 1;
+  }
+  if (ctx_init(g_ctx)) return 1;
+  FrameIn f;
+  if (frame_from_fields(f, camera_position, light_direction, screen_sizes, screen_center, screen_local, bg_color,
+                        num_fields, fields, num_lines, lines))
+    return 1;
+  f.stream = stream ? static_cast<cudaStream_t>(stream) : g_ctx.own_stream;
   FrameOut out;
   out.rgb_dev = rgb_out;
   return render_frame(g_ctx, f, out);
@@ -1161,9 +1213,15 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   return total;
 }
 
+static void ctx_release(Ctx &c);
+
 extern "C" int contour3d_gb300_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
-  Ctx &c = g_ctx;
+  ctx_release(g_ctx);
+  return 0;
+}
+
+static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
                  &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.tiny, &c.win, &c.need,
                  &c.checks};
@@ -1179,5 +1237,234 @@ extern "C" int contour3d_gb300_release(void) {
   }
   c.ready = false;
   c.device = -1;
+}
+
+/* ------------------------------------------------------------------ */
+/* batched and served forms                                           */
+/* ------------------------------------------------------------------ */
+/*
+ * A server owns `slots` worker threads, each with its own context (stream and
+ * device buffers), fed from one FIFO of requests.  A request starts as soon
+ * as a slot is free and its estimated device working set fits the HBM budget
+ * next to the requests in flight (continuous batching: requests arriving
+ * while others run are admitted as slots and memory free up, and their
+ * kernels overlap on the device).  The pipeline each request runs is the one
+ * of contour3d_gb300_render_device, so a frame's image does not depend on
+ * what else is in flight.
+ */
+namespace c3d {
+
+static double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  const contour3d_gb300_frame_t *frame = nullptr;
+  uint64_t ticket = 0;
+  uint64_t estimate = 0;
+  double t_submit = 0., t_start = 0., t_done = 0.;
+  int rc = 0;
+  bool done = false;
+  double device_ms = 0.;
+};
+
+/* working set of one request: slab codes/offsets, triangles (at an assumed
+   density of one triangle per cell), candidate lists and the z-buffer */
+static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t slab_cells) {
+  uint64_t peak = 0;
+  for (size_t n = 0; n < fr->num_fields; n++) {
+    const size_t *sz = fr->fields[n].sizes;
+    if (sz[0] < 2 || sz[1] < 2 || sz[2] < 2) continue;
+    const uint64_t per_slice = (uint64_t)(sz[0] - 1) * (sz[1] - 1);
+    uint64_t cells = std::min<uint64_t>(per_slice * (sz[2] - 1), std::max<uint64_t>(slab_cells, per_slice * 3));
+    const uint64_t bytes = cells * (1 + 4 + 4) + cells * (kTriBytes + 4 + 4) + cells / 2 * sizeof(Candidate);
+    peak = std::max(peak, bytes);
+  }
+  const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];
+  return peak + px * (sizeof(Slot) + 4 + 8 + 3) + (1ULL << 24);
+}
+
+}  // namespace c3d
+
+struct contour3d_gb300_server {
+  int slots = 0;
+  int device = 0;
+  uint64_t budget = 0;
+  uint64_t resident = 0;
+  uint64_t in_flight = 0;
+  int running = 0;
+  bool stop = false;
+  uint64_t next_ticket = 1;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<c3d::Request *> queue;
+  std::unordered_map<uint64_t, c3d::Request *> requests;
+  std::vector<std::unique_ptr<c3d::Ctx>> ctxs;
+  std::vector<std::thread> threads;
+  std::atomic<int> init_failures{0};
+};
+
+namespace c3d {
+
+static bool admissible(contour3d_gb300_server *sv, const Request *r) {
+  if (sv->running == 0) return true; /* an oversized request runs alone */
+  if (sv->budget == 0) return true;
+  const uint64_t avail = sv->budget > sv->resident ? sv->budget - sv->resident : 0;
+  return sv->in_flight + r->estimate <= avail;
+}
+
+static void worker_main(contour3d_gb300_server *sv, int slot) {
+  cudaSetDevice(sv->device);
+  Ctx &ctx = *sv->ctxs[slot];
+  const bool ok = ctx_init(ctx) == 0;
+  if (!ok) sv->init_failures++;
+  for (;;) {
+    Request *r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      sv->cv_work.wait(lk, [&] { return sv->stop || (!sv->queue.empty() && admissible(sv, sv->queue.front())); });
+      if (sv->queue.empty()) break; /* stop requested and nothing left */
+      if (!admissible(sv, sv->queue.front())) continue;
+      r = sv->queue.front();
+      sv->queue.pop_front();
+      sv->in_flight += r->estimate;
+      sv->running += 1;
+    }
+    r->t_start = now_ms();
+    int rc = ok ? 0 : 1;
+    if (ok) {
+      const contour3d_gb300_frame_t *fr = r->frame;
+      FrameIn f;
+      rc = frame_from_fields(f, &fr->camera_position, &fr->light_direction, fr->screen_sizes, &fr->screen_center,
+                             fr->screen_local, &fr->bg_color, fr->num_fields, fr->fields, fr->num_lines, fr->lines);
+      if (!rc && (!fr->rgb_out || !is_device_pointer(fr->rgb_out))) {
+        log_error("frame output pointer is not device memory");
+        rc = 1;
+      }
+      if (!rc) {
+        f.stream = ctx.own_stream;
+        FrameOut out;
+        out.rgb_dev = fr->rgb_out;
+        rc = render_frame(ctx, f, out);
+        r->device_ms = ctx.stats.ms_total;
+      }
+    }
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      r->rc = rc;
+      r->t_done = now_ms();
+      r->done = true;
+      sv->in_flight -= r->estimate;
+      sv->running -= 1;
+    }
+    sv->cv_done.notify_all();
+    sv->cv_work.notify_all();
+  }
+  ctx_release(ctx);
+}
+
+}  // namespace c3d
+
+extern "C" contour3d_gb300_server_t *contour3d_gb300_server_create(int slots, uint64_t hbm_budget_bytes,
+                                                                   uint64_t resident_bytes) {
+  if (slots < 1 || slots > 64) {
+    log_error("server: slots must be in 1..64 (got %d)", slots);
+    return nullptr;
+  }
+  auto *sv = new contour3d_gb300_server();
+  sv->slots = slots;
+  sv->budget = hbm_budget_bytes;
+  sv->resident = resident_bytes;
+  if (cudaGetDevice(&sv->device) != cudaSuccess) {
+    log_error("server: no current device");
+    delete sv;
+    return nullptr;
+  }
+  for (int q = 0; q < slots; q++) sv->ctxs.emplace_back(new Ctx());
+  for (int q = 0; q < slots; q++) sv->threads.emplace_back(worker_main, sv, q);
+  return sv;
+}
+
+extern "C" int contour3d_gb300_server_submit(contour3d_gb300_server_t *sv, const contour3d_gb300_frame_t *frame,
+                                             uint64_t *ticket) {
+  if (!sv || !frame || !ticket) return 1;
+  auto *r = new Request();
+  r->frame = frame;
+  r->estimate = request_estimate(frame, 1ULL << 27);
+  r->t_submit = now_ms();
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->stop) {
+      delete r;
+      return 1;
+    }
+    r->ticket = sv->next_ticket++;
+    sv->requests[r->ticket] = r;
+    sv->queue.push_back(r);
+    *ticket = r->ticket;
+  }
+  sv->cv_work.notify_all();
   return 0;
+}
+
+extern "C" int contour3d_gb300_server_wait(contour3d_gb300_server_t *sv, uint64_t ticket,
+                                           contour3d_gb300_request_stats_t *stats) {
+  if (!sv) return 1;
+  Request *r = nullptr;
+  {
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->requests.find(ticket);
+    if (it == sv->requests.end()) {
+      log_error("server: unknown ticket %llu", (unsigned long long)ticket);
+      return 1;
+    }
+    r = it->second;
+    sv->cv_done.wait(lk, [&] { return r->done; });
+    sv->requests.erase(it);
+  }
+  if (stats) {
+    stats->latency_ms = r->t_done - r->t_submit;
+    stats->queue_ms = r->t_start - r->t_submit;
+    stats->device_ms = r->device_ms;
+    stats->estimate_bytes = r->estimate;
+  }
+  const int rc = r->rc;
+  delete r;
+  return rc;
+}
+
+extern "C" uint64_t contour3d_gb300_device_bytes(void) { return g_device_bytes.load(); }
+
+extern "C" int contour3d_gb300_server_destroy(contour3d_gb300_server_t *sv) {
+  if (!sv) return 1;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+  }
+  sv->cv_work.notify_all();
+  for (auto &t : sv->threads) t.join();
+  const int rc = sv->init_failures.load() ? 1 : 0;
+  for (auto &kv : sv->requests) delete kv.second;
+  delete sv;
+  return rc;
+}
+
+extern "C" int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frames, size_t num_frames, int workers,
+                                            double *frame_ms) {
+  if (num_frames && !frames) return 1;
+  if (workers < 1) workers = 1;
+  contour3d_gb300_server_t *sv = contour3d_gb300_server_create((int)std::min<size_t>((size_t)workers,
+                                                                                     std::max<size_t>(num_frames, 1)),
+                                                               0, 0);
+  if (!sv) return 1;
+  std::vector<uint64_t> tickets(num_frames);
+  int rc = 0;
+  for (size_t n = 0; n < num_frames; n++) rc |= contour3d_gb300_server_submit(sv, frames + n, &tickets[n]);
+  for (size_t n = 0; n < num_frames; n++) {
+    contour3d_gb300_request_stats_t st;
+    rc |= contour3d_gb300_server_wait(sv, tickets[n], &st);
+    if (frame_ms) frame_ms[n] = st.device_ms;
+  }
+  rc |= contour3d_gb300_server_destroy(sv);
+  return rc ? 1 : 0;
 }

@@ -37,6 +37,55 @@ class Field(C.Structure):
 
 F64, F32 = 0, 1
 
+
+class Frame(C.Structure):
+    """contour3d_gb300_frame_t."""
+    _fields_ = [("camera_position", _abi.Vector), ("light_direction", _abi.Vector),
+                ("screen_sizes", C.c_size_t * 2), ("screen_center", _abi.Vector),
+                ("screen_local", _abi.Vector * 2), ("bg_color", _abi.Color), ("num_fields", C.c_size_t),
+                ("fields", C.POINTER(Field)), ("num_lines", C.c_size_t), ("lines", C.POINTER(_abi.LineObj)),
+                ("rgb_out", C.c_void_p)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("latency_ms", C.c_double), ("queue_ms", C.c_double), ("device_ms", C.c_double),
+                ("estimate_bytes", C.c_uint64)]
+
+
+class FramePack:
+    """A frame of device-resident fields plus everything its pointers refer to."""
+
+    def __init__(self, lib: "Library", scene: _abi.Scene, fields, rgb_dev_ptr: int):
+        self._keep = []
+        self.fields = (Field * max(len(fields), 1))()
+        for n, (ptr, dt, sizes, grids, thr, color) in enumerate(fields):
+            f = self.fields[n]
+            f.device_array = ptr
+            f.dtype = dt
+            for d in range(3):
+                f.sizes[d] = sizes[d]
+                g = np.ascontiguousarray(grids[d], dtype=np.float64)
+                self._keep.append(g)
+                f.grids[d] = g.ctypes.data_as(C.POINTER(C.c_double))
+            f.converter = lib.converters["identity"]
+            f.threshold = float(thr)
+            f.color = _abi.col(color)
+        a = _abi.ExecuteArgs(scene, lib.converters)
+        self._keep.append(a)
+        fr = Frame()
+        fr.camera_position = a.camera
+        fr.light_direction = a.light
+        fr.screen_sizes[0], fr.screen_sizes[1] = scene.width, scene.height
+        fr.screen_center = a.center
+        fr.screen_local[0], fr.screen_local[1] = a.local[0], a.local[1]
+        fr.bg_color = a.bg
+        fr.num_fields = len(fields)
+        fr.fields = C.cast(self.fields, C.POINTER(Field))
+        fr.num_lines = a.num_lines
+        fr.lines = C.cast(a.lines, C.POINTER(_abi.LineObj))
+        fr.rgb_out = rgb_dev_ptr
+        self.frame = fr
+
 # every symbol declared in include/contour3d.h and include/contour3d_gb300.h
 EXPORTS = [
     "contour3d_execute", "contour3d_gb300_identity", "contour3d_gb300_declare_identity",
@@ -44,7 +93,9 @@ EXPORTS = [
     "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells", "contour3d_gb300_set_filter_check",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
-    "contour3d_gb300_cell_offsets_noalloc",
+    "contour3d_gb300_cell_offsets_noalloc", "contour3d_gb300_render_batch", "contour3d_gb300_server_create",
+    "contour3d_gb300_server_submit", "contour3d_gb300_server_wait", "contour3d_gb300_server_destroy",
+    "contour3d_gb300_device_bytes",
     "c3d_comm_world", "sdecomp",
 ]
 
@@ -73,6 +124,25 @@ class Library:
         L.c3d_fieldgen_modes_device.argtypes = [C.c_void_p, C.c_int, C.c_long * 3, C.c_long * 3, C.c_long * 3,
                                                 C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64]
         L.c3d_fieldgen_blobs_device.restype = C.c_int
+        L.contour3d_gb300_render_device.argtypes = [
+            C.POINTER(_abi.Vector), C.POINTER(_abi.Vector), C.POINTER(C.c_size_t), C.POINTER(_abi.Vector),
+            C.POINTER(_abi.Vector), C.POINTER(_abi.Color), C.c_size_t, C.POINTER(Field), C.c_size_t,
+            C.POINTER(_abi.LineObj), C.c_void_p, C.c_void_p]
+        L.contour3d_gb300_render.argtypes = [
+            C.POINTER(_abi.Vector), C.POINTER(_abi.Vector), C.POINTER(C.c_size_t), C.POINTER(_abi.Vector),
+            C.POINTER(_abi.Vector), C.POINTER(_abi.Color), C.c_size_t, C.POINTER(_abi.ContourObj), C.c_size_t,
+            C.POINTER(_abi.LineObj), C.c_void_p, C.c_void_p]
+        L.contour3d_gb300_render_batch.restype = C.c_int
+        L.contour3d_gb300_render_batch.argtypes = [C.POINTER(Frame), C.c_size_t, C.c_int, C.c_void_p]
+        L.contour3d_gb300_server_create.restype = C.c_void_p
+        L.contour3d_gb300_server_create.argtypes = [C.c_int, C.c_uint64, C.c_uint64]
+        L.contour3d_gb300_server_submit.restype = C.c_int
+        L.contour3d_gb300_server_submit.argtypes = [C.c_void_p, C.POINTER(Frame), C.POINTER(C.c_uint64)]
+        L.contour3d_gb300_server_wait.restype = C.c_int
+        L.contour3d_gb300_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(RequestStats)]
+        L.contour3d_gb300_server_destroy.restype = C.c_int
+        L.contour3d_gb300_server_destroy.argtypes = [C.c_void_p]
+        L.contour3d_gb300_device_bytes.restype = C.c_uint64
         identity = C.cast(L.contour3d_gb300_identity, C.c_void_p).value
         self.converters = {"identity": identity}
         if os.path.exists(FIELDGEN_PATH):
@@ -121,6 +191,30 @@ class Library:
             C.byref(a.camera), C.byref(a.light), a.sizes, C.byref(a.center), a.local, C.byref(a.bg),
             C.c_size_t(len(fields)), arr, C.c_size_t(a.num_lines), a.lines, C.c_void_p(rgb_dev_ptr),
             C.c_void_p(stream))
+
+    def render_pack(self, pack: "FramePack", stream: int = 0) -> int:
+        """One FramePack through contour3d_gb300_render_device."""
+        fr = pack.frame
+        return self.lib.contour3d_gb300_render_device(
+            C.byref(fr.camera_position), C.byref(fr.light_direction), fr.screen_sizes, C.byref(fr.screen_center),
+            fr.screen_local, C.byref(fr.bg_color), C.c_size_t(fr.num_fields), fr.fields,
+            C.c_size_t(fr.num_lines), fr.lines, C.c_void_p(fr.rgb_out), C.c_void_p(stream))
+
+    def frame(self, scene: _abi.Scene, fields, rgb_dev_ptr: int) -> FramePack:
+        return FramePack(self, scene, fields, rgb_dev_ptr)
+
+    def render_batch(self, packs, workers: int = 4):
+        """Render FramePacks concurrently; returns per-frame device milliseconds."""
+        n = len(packs)
+        arr = (Frame * max(n, 1))(*[p.frame for p in packs])
+        ms = np.zeros(max(n, 1), dtype=np.float64)
+        rc = self.lib.contour3d_gb300_render_batch(arr, n, workers, ms.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise RuntimeError("contour3d_gb300_render_batch failed")
+        return ms[:n]
+
+    def server(self, slots: int, budget_bytes: int = 0, resident_bytes: int = 0) -> "Server":
+        return Server(self, slots, budget_bytes, resident_bytes)
 
     def stats(self) -> Stats:
         s = Stats()
@@ -186,6 +280,43 @@ class Library:
 
     def release(self) -> None:
         self.lib.contour3d_gb300_release()
+
+
+class Server:
+    """Python face of the served form (contour3d_gb300_server_*)."""
+
+    def __init__(self, lib: Library, slots: int, budget_bytes: int = 0, resident_bytes: int = 0):
+        self.lib = lib
+        self.h = lib.lib.contour3d_gb300_server_create(slots, budget_bytes, resident_bytes)
+        if not self.h:
+            raise RuntimeError("contour3d_gb300_server_create failed")
+        self._packs = {}
+
+    def submit(self, pack: FramePack) -> int:
+        t = C.c_uint64(0)
+        if self.lib.lib.contour3d_gb300_server_submit(self.h, C.byref(pack.frame), C.byref(t)) != 0:
+            raise RuntimeError("submit failed")
+        self._packs[t.value] = pack
+        return t.value
+
+    def wait(self, ticket: int) -> RequestStats:
+        st = RequestStats()
+        rc = self.lib.lib.contour3d_gb300_server_wait(self.h, ticket, C.byref(st))
+        self._packs.pop(ticket, None)
+        if rc != 0:
+            raise RuntimeError(f"request {ticket} failed")
+        return st
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.lib.contour3d_gb300_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 _singleton: Optional[Library] = None

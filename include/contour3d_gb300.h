@@ -117,6 +117,62 @@ int contour3d_gb300_cell_offsets_noalloc(const void *device_field, int dtype, co
                                          double threshold, uint32_t *device_offsets,
                                          unsigned long long *device_total, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* batched and served forms                                           */
+/* ------------------------------------------------------------------ */
+
+/* one frame of device-resident fields (as contour3d_gb300_render_device) */
+typedef struct {
+  contour3d_vector_t camera_position;
+  contour3d_vector_t light_direction;
+  size_t screen_sizes[2];
+  contour3d_vector_t screen_center;
+  contour3d_vector_t screen_local[2];
+  contour3d_color_t bg_color;
+  size_t num_fields;
+  const contour3d_gb300_field_t *fields;
+  size_t num_lines;
+  const contour3d_line_obj_t *lines;
+  uint8_t *rgb_out; /* device, width * height * 3 bytes in ppm row order */
+} contour3d_gb300_frame_t;
+
+/*
+ * Render many frames (each with its own fields, levels and camera) with
+ * `workers` concurrent contexts; returns when all are done.  frame_ms
+ * (optional) receives each frame's device time.  Images equal those of
+ * contour3d_gb300_render_device frame by frame.
+ */
+int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frames, size_t num_frames, int workers,
+                                 double *frame_ms);
+
+/*
+ * Served form: a request loop with `slots` concurrent contexts.  A submitted
+ * frame starts when a slot is free and its estimated device working set fits
+ * `hbm_budget_bytes` (0 = unlimited) minus `resident_bytes` (the caller's
+ * resident fields) next to the requests in flight; requests arriving while
+ * others run are admitted as slots and memory free up.  The frame struct and
+ * everything it points to must stay valid until contour3d_gb300_server_wait
+ * returns for its ticket.
+ */
+typedef struct contour3d_gb300_server contour3d_gb300_server_t;
+typedef struct {
+  double latency_ms;      /* submit -> done */
+  double queue_ms;        /* submit -> start */
+  double device_ms;       /* device time of the frame */
+  uint64_t estimate_bytes; /* admitted working-set estimate */
+} contour3d_gb300_request_stats_t;
+
+contour3d_gb300_server_t *contour3d_gb300_server_create(int slots, uint64_t hbm_budget_bytes,
+                                                        uint64_t resident_bytes);
+int contour3d_gb300_server_submit(contour3d_gb300_server_t *server, const contour3d_gb300_frame_t *frame,
+                                  uint64_t *ticket);
+int contour3d_gb300_server_wait(contour3d_gb300_server_t *server, uint64_t ticket,
+                                contour3d_gb300_request_stats_t *stats);
+int contour3d_gb300_server_destroy(contour3d_gb300_server_t *server);
+
+/* device bytes currently held by the library's buffers (all contexts) */
+uint64_t contour3d_gb300_device_bytes(void);
+
 /* statistics of the last render call */
 typedef struct {
   uint64_t cells;             /* cells classified (cell x threshold) */

@@ -1,0 +1,86 @@
+"""Batched and served forms: every frame's image equals the image the plain
+per-frame entry point gives, alone or in a mix of concurrent requests."""
+import numpy as np
+import pytest
+
+from contour3d_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_set(gpu, n=7, seed=7):
+    import torch
+    rng = np.random.default_rng(seed)
+    fields, frames = [], []
+    for q in range(n):
+        shape = tuple(int(x) for x in rng.integers(24, 72, size=3))
+        if q % 2 == 0:
+            f = workloads.blobs_device(gpu, shape, int(rng.integers(3, 9)), seed=50 + q)
+        else:
+            f, _ = workloads.modes_device(gpu, shape, nmodes=24, kmin=1, kmax=6, seed=80 + q, dtype=torch.float32)
+        fields.append(f)
+        nlev = int(rng.integers(1, 4))
+        frames.append(workloads.FrameSpec(q, workloads.quantile_levels(f, rng, nlev), workloads.PALETTE[:nlev],
+                                          workloads.random_camera(rng), 160, 120))
+    return fields, frames
+
+
+def _single(gpu, fields, spec):
+    import torch
+    out = torch.zeros(spec.width * spec.height * 3, dtype=torch.uint8, device="cuda")
+    assert gpu.render_pack(workloads.frame_pack(gpu, fields[spec.field], spec, out)) == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_batch_matches_single_frames(gpu):
+    import torch
+    fields, frames = _small_set(gpu)
+    ref = [_single(gpu, fields, s) for s in frames]
+    outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
+    packs = [workloads.frame_pack(gpu, fields[s.field], s, o) for s, o in zip(frames, outs)]
+    ms = gpu.render_batch(packs, workers=3)
+    torch.cuda.synchronize()
+    assert len(ms) == len(frames) and all(m > 0 for m in ms)
+    for a, o in zip(ref, outs):
+        assert np.array_equal(a, o.cpu().numpy())
+
+
+def test_server_result_same_alone_and_in_the_mix(gpu):
+    import torch
+    fields, frames = _small_set(gpu, n=9, seed=11)
+    ref = [_single(gpu, fields, s) for s in frames]
+    target = 4
+    with gpu.server(slots=4) as sv:
+        out = torch.zeros(frames[target].width * frames[target].height * 3, dtype=torch.uint8, device="cuda")
+        t = sv.submit(workloads.frame_pack(gpu, fields[target], frames[target], out))
+        st_alone = sv.wait(t)
+        torch.cuda.synchronize()
+        alone = out.cpu().numpy()
+        outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
+        order = np.random.default_rng(3).permutation(len(frames))
+        tickets = {int(q): sv.submit(workloads.frame_pack(gpu, fields[frames[q].field], frames[q], outs[q]))
+                   for q in order}
+        stats = {q: sv.wait(t) for q, t in tickets.items()}
+        torch.cuda.synchronize()
+    assert np.array_equal(alone, ref[target])
+    for q in range(len(frames)):
+        assert np.array_equal(outs[q].cpu().numpy(), ref[q]), f"frame {q} differs in the mix"
+        assert stats[q].latency_ms >= stats[q].queue_ms >= 0
+    assert st_alone.latency_ms > 0
+
+
+def test_server_admits_against_a_budget(gpu):
+    """A budget that fits one request at a time serialises them; results stay exact."""
+    import torch
+    fields, frames = _small_set(gpu, n=5, seed=19)
+    ref = [_single(gpu, fields, s) for s in frames]
+    with gpu.server(slots=3, budget_bytes=1, resident_bytes=0) as sv:
+        outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
+        ts = [sv.submit(workloads.frame_pack(gpu, fields[s.field], s, o)) for s, o in zip(frames, outs)]
+        stats = [sv.wait(t) for t in ts]
+        torch.cuda.synchronize()
+    for q in range(len(frames)):
+        assert np.array_equal(outs[q].cpu().numpy(), ref[q])
+    # with one request admitted at a time, each later request waited for the earlier ones
+    assert stats[-1].queue_ms >= 0 and all(s.estimate_bytes > 0 for s in stats)
