@@ -54,6 +54,12 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--shape", type=int, default=512,
                    help="nodes per axis (512 is the benchmark; smaller sizes are for profiler captures)")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-served", action="store_true")
+    p.add_argument("--workers", type=int, default=6)
+    p.add_argument("--served-rates", default="200,max",
+                   help="comma-separated request rates (req/s); max = submit without waiting")
+    p.add_argument("--served-requests", type=int, default=60)
     return p.parse_args()
 
 
@@ -127,6 +133,151 @@ def cpu_baseline(field_sample: np.ndarray, std: float, cores: int):
     dt = time.perf_counter() - t0
     cells = 2 * (SHAPE[0] - 1) * (SHAPE[1] - 1) * (nz - 1)
     return cells / dt, dt, cells
+
+
+def run_batched(gpu, workers, nfields=64):
+    """64 fields of uneven shape, each with its own levels and camera, 1024^2:
+    the plain per-frame entry point one frame at a time, then the batched form."""
+    import torch
+    from contour3d_gb300 import workloads
+    fields, frames = workloads.batch_set(gpu, nfields=nfields)
+    outs = [torch.empty(f.width * f.height * 3, dtype=torch.uint8, device="cuda") for f in frames]
+    packs = [workloads.frame_pack(gpu, fields[f.field], f, o) for f, o in zip(frames, outs)]
+    cells = sum(len(f.levels) * (fields[f.field].shape[0] - 1) * (fields[f.field].shape[1] - 1) *
+                (fields[f.field].shape[2] - 1) for f in frames)
+    for p in packs[:4]:
+        gpu.render_pack(p)
+    gpu.render_batch(packs[:8], workers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in packs:
+        if gpu.render_pack(p) != 0:
+            raise RuntimeError("plain frame failed")
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    ref = [o.clone() for o in outs]
+    for o in outs:
+        o.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gpu.render_batch(packs, workers)
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - t0
+    same = all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
+    return {"workload": f"{nfields} fields, dims 64..384, half f64 / half f32, 1-4 levels, own camera, 1024x1024",
+            "frames": nfields, "cell_thresholds": int(cells), "workers": workers,
+            "plain": {"cells_per_s": cells / plain_s, "frames_per_s": nfields / plain_s, "s": plain_s},
+            "batched": {"cells_per_s": cells / batch_s, "frames_per_s": nfields / batch_s, "s": batch_s},
+            "speedup": plain_s / batch_s, "images_identical": same}
+
+
+def run_served(gpu, slots, rates, nreq, budget_gb=120.0, seed=99):
+    """Request stream over resident fields (shapes {96^3, 192^3, 256x256x512,
+    384^3, 768^3}, f32 and f64), 1-3 levels and a camera per request,
+    1280x720; every 10 requests one field advances in place by a phase step
+    omega dt (its readers finish first).  The plain path replays the same
+    sequence one request at a time; the served path replays it as a Poisson
+    stream at each rate ("max" submits without waiting).  Fields restart at
+    time 0 before each replay, so every replay does the same work."""
+    import torch
+    from contour3d_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    resident = []
+    for shp in workloads.SERVED_SHAPES:
+        for dt in (torch.float32, torch.float64):
+            f, std = workloads.modes_device(gpu, shp, nmodes=32, kmin=1, kmax=12, seed=len(resident) + 300, dtype=dt)
+            resident.append({"t": f, "std": std, "time": 0.0, "seed": len(resident) + 300, "busy": []})
+    resident_bytes = sum(r["t"].numel() * r["t"].element_size() for r in resident)
+    out = {"workload": "Poisson stream, resident fields {96^3,192^3,256x256x512,384^3,768^3} x {f32,f64}, "
+                       "1-3 levels, 1280x720, phase advance every 10 requests",
+           "slots": slots, "budget_gb": budget_gb, "resident_gb": resident_bytes / 1e9, "rates": []}
+    solver = torch.cuda.Stream()
+
+    def advance(r, time_value):
+        t = r["t"]
+        r["time"] = time_value
+        gpu.fieldgen_modes_device_async(t.data_ptr(), 0 if t.dtype == torch.float64 else 1, tuple(t.shape), 32, 1,
+                                        12, 5.0 / 6.0, r["seed"], time_value, solver.cuda_stream)
+        solver.synchronize()
+
+    def restart():
+        for r in resident:
+            if r["time"] != 0.0:
+                advance(r, 0.0)
+            r["busy"] = []
+
+    reqs = []
+    for _ in range(nreq):
+        fi = int(rng.integers(0, len(resident)))
+        nlev = int(rng.integers(1, 4))
+        lv = sorted(float(x) for x in rng.uniform(-0.8, 0.8, size=nlev) * resident[fi]["std"])
+        reqs.append((fi, workloads.FrameSpec(0, lv, workloads.PALETTE[:nlev], workloads.random_camera(rng),
+                                             1280, 720)))
+    cells = 0
+    for fi, spec in reqs:
+        sh = resident[fi]["t"].shape
+        cells += len(spec.levels) * (sh[0] - 1) * (sh[1] - 1) * (sh[2] - 1)
+    out["cell_thresholds"] = cells
+    outs = [torch.empty(1280 * 720 * 3, dtype=torch.uint8, device="cuda") for _ in range(nreq)]
+    packs = [workloads.frame_pack(gpu, resident[fi]["t"], spec, outs[q]) for q, (fi, spec) in enumerate(reqs)]
+
+    def updated(q):
+        return resident[(q // 10) % len(resident)] if q and q % 10 == 0 else None
+
+    # plain: the same sequence, one request at a time
+    for p in packs[:3]:
+        gpu.render_pack(p)
+    restart()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for q, p in enumerate(packs):
+        r = updated(q)
+        if r is not None:
+            advance(r, r["time"] + 0.01)
+        gpu.render_pack(p)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    out["plain"] = {"frames_per_s": nreq / plain_s, "cells_per_s": cells / plain_s}
+    plain_img = [o.clone() for o in outs]
+    for rate in rates:
+        restart()
+        for o in outs:
+            o.zero_()
+        torch.cuda.synchronize()
+        gaps = rng.exponential(1.0 / rate, size=nreq) if rate else np.zeros(nreq)
+        with gpu.server(slots, int(budget_gb * 1e9), resident_bytes) as sv:
+            tickets, lat = [], []
+            t_start = time.perf_counter()
+            t_next = t_start
+            for q, (fi, spec) in enumerate(reqs):
+                t_next += gaps[q]
+                while True:
+                    d = t_next - time.perf_counter()
+                    if d <= 0:
+                        break
+                    time.sleep(min(d, 0.002))
+                r = updated(q)
+                if r is not None:
+                    for tk in r["busy"]:
+                        lat.append(sv.wait(tk))
+                        tickets.remove(tk)
+                    r["busy"] = []
+                    advance(r, r["time"] + 0.01)
+                tk = sv.submit(packs[q])
+                tickets.append(tk)
+                resident[fi]["busy"].append(tk)
+            for tk in tickets:
+                lat.append(sv.wait(tk))
+            wall = time.perf_counter() - t_start
+        torch.cuda.synchronize()
+        same = all(torch.equal(a, b) for a, b in zip(outs, plain_img))
+        ms = np.array([x.latency_ms for x in lat])
+        out["rates"].append({"rate_req_s": rate if rate else "max", "requests": nreq,
+                             "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                             "frames_per_s": nreq / wall, "cells_per_s": cells / wall,
+                             "queue_p50_ms": float(np.percentile([x.queue_ms for x in lat], 50)),
+                             "images_identical_to_plain": bool(same)})
+    return out
 
 
 def run_reference(args, rank, world):
@@ -286,6 +437,13 @@ def main():
         os.unlink(path)
         os.rmdir(tmp)
 
+    batched = served = None
+    if rank == 0 and not args.no_batched:
+        batched = run_batched(gpu, args.workers)
+    if rank == 0 and not args.no_served:
+        served = run_served(gpu, args.workers, [0.0 if x == "max" else float(x) for x in args.served_rates.split(",")],
+                            args.served_requests)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         sample = field[:CPU_SAMPLE_SLICES].cpu().numpy()
@@ -307,6 +465,7 @@ def main():
             "triangles_per_s": world * st.triangles / (ms / 1000.0),
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "batched": batched, "served": served,
         }
         print(json.dumps(out))
     if world > 1:

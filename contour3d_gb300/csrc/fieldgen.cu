@@ -73,15 +73,25 @@ int grid_blocks(long long n) {
 
 /*
  * Fill a device buffer with the block [off, off + my) of a global Fourier
- * field (dtype 0 = f64, 1 = f32).  Returns the analytic std, or -1 on error.
+ * field (dtype 0 = f64, 1 = f32) at time `time`: every phase advances by
+ * |k| * time turns (omega = |k|), as a solver's field evolves between
+ * frames.  Returns the analytic std, or -1 on error.
  */
 extern "C" double c3d_fieldgen_modes_device(void* out, int dtype, const long gl[3], const long off[3],
                                             const long my[3], int nmodes, int kmin, int kmax, double power,
-                                            uint64_t seed) {
+                                            uint64_t seed, double time) {
   if (nmodes > C3D_MAX_MODES || nmodes < 1) return -1.0;
   c3d_modes_t* m = (c3d_modes_t*)malloc(sizeof(c3d_modes_t));
   if (!m) return -1.0;
   c3d_modes_init(m, nmodes, kmin, kmax, power, seed);
+  if (time != 0.0) {
+    for (int n = 0; n < nmodes; n++) {
+      const double kk = (double)(m->kx[n] * m->kx[n] + m->ky[n] * m->ky[n] + m->kz[n] * m->kz[n]);
+      double ph = m->phase[n] + sqrt(kk) * time;
+      ph = ph - floor(ph);
+      m->phase[n] = ph;
+    }
+  }
   const double std = m->std;
   std::vector<double> tab[3];
   for (int d = 0; d < 3; d++) tab[d].resize(2 * (size_t)nmodes * (size_t)my[d]);
@@ -129,6 +139,69 @@ extern "C" double c3d_fieldgen_modes_device(void* out, int dtype, const long gl[
     return -1.0;
   }
   return std;
+}
+
+/*
+ * The same field launched on `stream` with stream-ordered scratch and no
+ * device-wide synchronisation, so a solver can advance a resident field
+ * while other work runs.  Returns the analytic std, or -1 on error.
+ */
+extern "C" double c3d_fieldgen_modes_device_async(void* out, int dtype, const long gl[3], const long off[3],
+                                                  const long my[3], int nmodes, int kmin, int kmax, double power,
+                                                  uint64_t seed, double time, void* stream_v) {
+  if (nmodes > C3D_MAX_MODES || nmodes < 1) return -1.0;
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  c3d_modes_t* m = (c3d_modes_t*)malloc(sizeof(c3d_modes_t));
+  if (!m) return -1.0;
+  c3d_modes_init(m, nmodes, kmin, kmax, power, seed);
+  for (int n = 0; n < nmodes && time != 0.0; n++) {
+    const double kk = (double)(m->kx[n] * m->kx[n] + m->ky[n] * m->ky[n] + m->kz[n] * m->kz[n]);
+    double ph = m->phase[n] + sqrt(kk) * time;
+    m->phase[n] = ph - floor(ph);
+  }
+  const double std = m->std;
+  const size_t nt = 2 * (size_t)nmodes * (size_t)(my[0] + my[1] + my[2]);
+  std::vector<double> tab(nt + (size_t)nmodes);
+  double* t3[3] = {tab.data(), tab.data() + 2 * (size_t)nmodes * my[0],
+                   tab.data() + 2 * (size_t)nmodes * (my[0] + my[1])};
+  for (int n = 0; n < nmodes; n++) {
+    const int kk[3] = {m->kx[n], m->ky[n], m->kz[n]};
+    double pr, pi;
+    c3d_sincos_turns(m->phase[n], &pi, &pr);
+    for (int d = 0; d < 3; d++)
+      for (long i = 0; i < my[d]; i++) {
+        double re, im;
+        c3d_mode_axis(kk[d], i + off[d], gl[d], &re, &im);
+        if (d == 2) {
+          const double r2 = re * pr - im * pi;
+          const double i2 = re * pi + im * pr;
+          re = r2;
+          im = i2;
+        }
+        t3[d][2 * ((size_t)n * my[d] + i) + 0] = re;
+        t3[d][2 * ((size_t)n * my[d] + i) + 1] = im;
+      }
+  }
+  for (int n = 0; n < nmodes; n++) tab[nt + n] = m->amp[n];
+  free(m);
+  double* d = nullptr;
+  if (cudaMallocAsync(&d, sizeof(double) * tab.size(), stream) != cudaSuccess) return -1.0;
+  int rc = cudaMemcpyAsync(d, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, stream) != cudaSuccess;
+  if (!rc) {
+    const double* dx = d;
+    const double* dy = d + 2 * (size_t)nmodes * my[0];
+    const double* dz = d + 2 * (size_t)nmodes * (my[0] + my[1]);
+    const long long n = (long long)my[0] * my[1] * my[2];
+    if (dtype == 0)
+      k_modes_f64<<<grid_blocks(n), 256, 0, stream>>>((double*)out, dx, dy, dz, d + nt, nmodes, my[0], my[1], my[2]);
+    else
+      k_modes_f32<<<grid_blocks(n), 256, 0, stream>>>((float*)out, dx, dy, dz, d + nt, nmodes, my[0], my[1], my[2]);
+    rc = cudaGetLastError() != cudaSuccess;
+  }
+  /* the pageable copy has been staged when cudaMemcpyAsync returned; the
+     scratch is released in stream order after the kernel */
+  cudaFreeAsync(d, stream);
+  return rc ? -1.0 : std;
 }
 
 /* Gaussian-blob field (f64) into a device buffer; returns 0 or 1 */

@@ -262,14 +262,48 @@ static void build_tables(std::vector<unsigned long long> &lut, unsigned char cou
 /* device bytes held by every library buffer of the process */
 static std::atomic<unsigned long long> g_device_bytes{0};
 
+/*
+ * Device buffers come from one stream-ordered memory pool per device that
+ * keeps freed blocks (release threshold = all), so a buffer that grows while
+ * other contexts render costs no device-wide synchronisation, and a new
+ * context reuses the blocks of released ones.
+ */
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[64];
+
+static cudaMemPool_t device_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    unsigned long long keep = ~0ULL;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pool[dev] = pool;
+  }
+  return g_pool[dev];
+}
+
 struct Buf {
   void *p = nullptr;
   size_t cap = 0;
-  int ensure(size_t bytes) {
+  /* grow to at least `bytes`; the old contents are not kept.  Allocation and
+     release are ordered on `st`, the stream every use of the buffer is on
+     (or whose previous uses have completed) */
+  int ensure(size_t bytes, cudaStream_t st) {
     if (bytes <= cap) return 0;
-    release();
+    release(st);
     const size_t want = bytes + bytes / 4 + 256;
-    if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaMemPool_t pool = device_pool();
+    if (!pool || cudaMallocFromPoolAsync(&p, want, pool, st) != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
       log_error("device allocation of %zu bytes failed", want);
@@ -279,9 +313,9 @@ struct Buf {
     g_device_bytes += want;
     return 0;
   }
-  void release() {
+  void release(cudaStream_t st) {
     if (p) {
-      cudaFree(p);
+      cudaFreeAsync(p, st);
       g_device_bytes -= cap;
     }
     p = nullptr;
@@ -320,7 +354,8 @@ struct Ctx {
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
   Buf zlo, xyf, cand, tiny, win, need, checks;
-  std::vector<double> h_grids; /* staging for node coordinates (synchronised per slab) */
+  HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
+  cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
   bool filter_check = false;
   HostBuf h_small, h_rgb, h_slots;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[8] = {};
@@ -346,6 +381,8 @@ static int ctx_init(Ctx &c) {
   C3D_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
   C3D_CUDA(cudaEventCreate(&c.ev0));
   C3D_CUDA(cudaEventCreate(&c.ev1));
+  C3D_CUDA(cudaEventCreateWithFlags(&c.ev_staged, cudaEventDisableTiming));
+  C3D_CUDA(cudaEventRecord(c.ev_staged, c.own_stream));
   for (auto &e : c.evs) C3D_CUDA(cudaEventCreate(&e));
   std::vector<unsigned long long> lut;
   unsigned char count[256];
@@ -364,8 +401,10 @@ static int ctx_init(Ctx &c) {
       uploaded[dev] = true;
     }
   }
-  if (c.lut.ensure(sizeof(unsigned long long) * kLutEntries)) return 1;
-  C3D_CUDA(cudaMemcpy(c.lut.p, lut.data(), sizeof(unsigned long long) * kLutEntries, cudaMemcpyHostToDevice));
+  if (c.lut.ensure(sizeof(unsigned long long) * kLutEntries, c.own_stream)) return 1;
+  C3D_CUDA(cudaMemcpyAsync(c.lut.p, lut.data(), sizeof(unsigned long long) * kLutEntries, cudaMemcpyHostToDevice,
+                           c.own_stream));
+  C3D_CUDA(cudaStreamSynchronize(c.own_stream));
   if (c.h_small.ensure(256)) return 1;
   c.device = dev;
   c.ready = true;
@@ -468,7 +507,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     /* objects of one call that share a host array (the reference's example
        draws two levels of one field) upload it once */
     if (!(c.field_src == ci.data && c.field_bytes == nnodes * elem && c.field.p)) {
-      if (c.field.ensure(nnodes * elem)) return 1;
+      if (c.field.ensure(nnodes * elem, st)) return 1;
       C3D_CUDA(cudaMemcpyAsync(c.field.p, ci.data, nnodes * elem, cudaMemcpyHostToDevice, st));
       c.field_src = ci.data;
       c.field_bytes = nnodes * elem;
@@ -478,17 +517,20 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   }
   /* node coordinates, and their float roundings for the single-precision filter */
   const size_t ng = (size_t)(nx + ny + nz);
-  if (c.grids.ensure(sizeof(double) * ng + sizeof(float) * ng)) return 1;
+  if (c.grids.ensure(sizeof(double) * ng + sizeof(float) * ng, st)) return 1;
   double *g = c.grids.as<double>();
   float *gf = reinterpret_cast<float *>(g + ng);
-  c.h_grids.resize(ng * 3);
-  double *hg = c.h_grids.data();
+  /* the previous upload from the staging buffer must have left it */
+  C3D_CUDA(cudaEventSynchronize(c.ev_staged));
+  if (c.h_grids.ensure(sizeof(double) * ng + sizeof(float) * ng)) return 1;
+  double *hg = c.h_grids.as<double>();
   float *hgf = reinterpret_cast<float *>(hg + ng);
   memcpy(hg, ci.grid[0], sizeof(double) * nx);
   memcpy(hg + nx, ci.grid[1], sizeof(double) * ny);
   memcpy(hg + nx + ny, ci.grid[2], sizeof(double) * nz);
   for (size_t q = 0; q < ng; q++) hgf[q] = (float)hg[q];
   C3D_CUDA(cudaMemcpyAsync(g, hg, sizeof(double) * ng + sizeof(float) * ng, cudaMemcpyHostToDevice, st));
+  C3D_CUDA(cudaEventRecord(c.ev_staged, st));
   const double *dnodes = nullptr;
   std::vector<double> nodes;
   if (!is_identity(ci.converter)) {
@@ -503,7 +545,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           nodes[q++] = p.y;
           nodes[q++] = p.z;
         }
-    if (c.nodes.ensure(sizeof(double) * 3 * nnodes)) return 1;
+    if (c.nodes.ensure(sizeof(double) * 3 * nnodes, st)) return 1;
     C3D_CUDA(cudaMemcpyAsync(c.nodes.p, nodes.data(), sizeof(double) * 3 * nnodes, cudaMemcpyHostToDevice, st));
     dnodes = c.nodes.as<double>();
   }
@@ -551,8 +593,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     S.krender0 = std::max(k0, 1LL);
     S.krender1 = std::min(k1, ncz - 1);
     const long long ncell = S.nslices * per_slice;
-    if (c.counts.ensure((size_t)ncell) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1)) ||
-        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell)) || c.scratch.ensure(128))
+    if (c.counts.ensure((size_t)ncell, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
+        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell), st) || c.scratch.ensure(128, st))
       return 1;
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = d_counter + 1;
@@ -586,7 +628,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     if (T == 0) continue;
     /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
        every sub-array stays aligned (and over-allocate so that cap >= T) */
-    if (c.tri_cell.ensure(sizeof(unsigned) * T) || c.tri.ensure(kTriBytes * (T + 64))) return 1;
+    if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
     const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
     if (cap < T) {
       log_error("internal: triangle buffer capacity %zu below %llu", cap, T);
@@ -594,7 +636,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     double *dbg = nullptr;
     if (sink) {
-      if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap)) return 1;
+      if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap, st)) return 1;
       dbg = c.dbg.as<double>();
     }
     const TriDev tri = tri_layout(c.tri.p, cap, dbg);
@@ -624,28 +666,38 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
          run again with larger lists (every z-buffer update is an idempotent
          maximum, so repeating them is harmless) */
       const size_t npx = (size_t)(sd.width * sd.height);
-      if (c.win.ensure(sizeof(uint2) * npx) || c.need.ensure(sizeof(unsigned) * T)) return 1;
+      if (c.win.ensure(sizeof(uint2) * npx, st) || c.need.ensure(sizeof(unsigned) * T, st)) return 1;
       unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
       unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
       RasterDev RS = R;
       unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 4);
       unsigned long long *h_cnt = h_total + 1;
+      RS.win = c.win.as<uint2>();
+      RS.win_count = counters + 2;
+      RS.need = c.need.as<unsigned>();
+      RS.need_count = counters + 3;
       for (int attempt = 0;; attempt++) {
-        if (c.cand.ensure(sizeof(Candidate) * cand_want) || c.tiny.ensure(sizeof(unsigned) * tiny_want)) return 1;
+        if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.tiny.ensure(sizeof(unsigned) * tiny_want, st)) return 1;
         RS.cand = c.cand.as<Candidate>();
         RS.cand_cap = c.cand.cap / sizeof(Candidate);
         RS.cand_count = counters + 0;
         RS.tiny = c.tiny.as<unsigned>();
         RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
         RS.tiny_count = counters + 1;
-        C3D_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), st));
+        C3D_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st));
+        C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
         launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
         launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
         if (c.stage_timing) cudaEventRecord(c.evs[5], st);
         launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
         if (c.stage_timing) cudaEventRecord(c.evs[6], st);
-        c.stats.kernel_launches += 3;
-        C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        /* shading runs before the overflow check: when a list overflowed, the
+           whole stage runs again, and the repeated z-buffer maxima and
+           colours are the same values */
+        launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
+        if (c.stage_timing) cudaEventRecord(c.evs[7], st);
+        c.stats.kernel_launches += 7;
+        C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         C3D_CUDA(cudaStreamSynchronize(st));
         if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
         if (attempt > 4) {
@@ -658,17 +710,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       }
       c.stats.candidates += h_cnt[0];
       c.stats.tiny += h_cnt[1];
-      RS.win = c.win.as<uint2>();
-      RS.win_count = counters + 2;
-      RS.need = c.need.as<unsigned>();
-      RS.need_count = counters + 3;
-      C3D_CUDA(cudaMemsetAsync(counters + 2, 0, 2 * sizeof(unsigned long long), st));
-      C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
-      launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
-      c.stats.kernel_launches += 4;
-      if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-      C3D_CUDA(cudaMemcpyAsync(h_cnt + 2, counters + 2, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaStreamSynchronize(st));
       c.stats.winners += h_cnt[2];
       c.stats.normals += h_cnt[3];
       if (c.stage_timing) {
@@ -747,7 +788,7 @@ static int render_lines(Ctx &c, const FrameIn &f, unsigned long long &order_base
     }
   }
   if (segs.empty()) return 0;
-  if (c.segs.ensure(sizeof(LineSegDev) * segs.size())) return 1;
+  if (c.segs.ensure(sizeof(LineSegDev) * segs.size(), f.stream)) return 1;
   C3D_CUDA(cudaMemcpyAsync(c.segs.p, segs.data(), sizeof(LineSegDev) * segs.size(), cudaMemcpyHostToDevice, f.stream));
   launch_lines(c.segs.as<LineSegDev>(), (int)segs.size(), (long long)s.W, (long long)s.H, c.canvas.as<Slot>(),
                order_base, f.stream);
@@ -772,17 +813,20 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   cudaStream_t st = f.stream;
   C3D_CUDA(cudaEventRecord(c.ev0, st));
   const SceneDev sd = scene_dev(s);
-  /* pixel centres (render.c:100-104) */
-  std::vector<double> xy(W + H);
+  /* pixel centres (render.c:100-104), staged through pinned memory */
+  C3D_CUDA(cudaEventSynchronize(c.ev_staged));
+  if (c.h_grids.ensure(sizeof(double) * (W + H) + sizeof(float) * (W + H))) return 1;
+  double *xy = c.h_grids.as<double>();
+  float *xyf = reinterpret_cast<float *>(xy + W + H);
   for (size_t i = 0; i < W; i++) xy[i] = 1. * (i + 0.5) / W - 0.5;
   for (size_t j = 0; j < H; j++) xy[W + j] = 1. * (j + 0.5) / H - 0.5;
-  std::vector<float> xyf(W + H);
   for (size_t q = 0; q < W + H; q++) xyf[q] = (float)xy[q];
-  if (c.xy.ensure(sizeof(double) * (W + H)) || c.xyf.ensure(sizeof(float) * (W + H)) ||
-      c.canvas.ensure(sizeof(Slot) * npx) || c.zlo.ensure(sizeof(unsigned) * npx) || c.checks.ensure(64))
+  if (c.xy.ensure(sizeof(double) * (W + H), st) || c.xyf.ensure(sizeof(float) * (W + H), st) ||
+      c.canvas.ensure(sizeof(Slot) * npx, st) || c.zlo.ensure(sizeof(unsigned) * npx, st) || c.checks.ensure(64, st))
     return 1;
-  C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy.data(), sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
-  C3D_CUDA(cudaMemcpyAsync(c.xyf.p, xyf.data(), sizeof(float) * (W + H), cudaMemcpyHostToDevice, st));
+  C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy, sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
+  C3D_CUDA(cudaMemcpyAsync(c.xyf.p, xyf, sizeof(float) * (W + H), cudaMemcpyHostToDevice, st));
+  C3D_CUDA(cudaEventRecord(c.ev_staged, st));
   if (c.filter_check) C3D_CUDA(cudaMemsetAsync(c.checks.p, 0, 64, st));
   RasterDev R = {};
   R.canvas = c.canvas.as<Slot>();
@@ -806,7 +850,7 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   /* resolve */
   uint8_t *rgb_dev = o.rgb_dev;
   if (!rgb_dev && o.rgb_host) {
-    if (c.rgb.ensure(3 * npx)) return 1;
+    if (c.rgb.ensure(3 * npx, st)) return 1;
     rgb_dev = c.rgb.as<uint8_t>();
   }
   if (rgb_dev) {
@@ -1183,7 +1227,7 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   Ctx &c = g_ctx;
   cudaStream_t st = c.own_stream;
   const size_t nn = (size_t)(nx * ny * nz);
-  if (c.field.ensure(8 * nn) || c.counts.ensure((size_t)((nx - 1) * (ny - 1) * (nz - 1)))) return -1;
+  if (c.field.ensure(8 * nn, st) || c.counts.ensure((size_t)((nx - 1) * (ny - 1) * (nz - 1)), st)) return -1;
   c.field_src = nullptr;
   if (cudaMemcpyAsync(c.field.p, obj->array, 8 * nn, cudaMemcpyHostToDevice, st) != cudaSuccess) return -1;
   FieldDev F = {};
@@ -1218,6 +1262,10 @@ static void ctx_release(Ctx &c);
 extern "C" int contour3d_gb300_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   ctx_release(g_ctx);
+  /* hand the pool's unused blocks back to the device */
+  std::lock_guard<std::mutex> lp(g_pool_mu);
+  for (cudaMemPool_t pool : g_pool)
+    if (pool) cudaMemPoolTrimTo(pool, 0);
   return 0;
 }
 
@@ -1225,14 +1273,19 @@ static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
                  &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.tiny, &c.win, &c.need,
                  &c.checks};
-  for (Buf *b : bufs) b->release();
+  /* every call of the context has completed, so its buffers go back to the
+     pool in order on its own stream */
+  for (Buf *b : bufs) b->release(c.own_stream);
+  if (c.ready) cudaStreamSynchronize(c.own_stream);
   c.h_small.release();
   c.h_rgb.release();
   c.h_slots.release();
+  c.h_grids.release();
   if (c.ready) {
     cudaStreamDestroy(c.own_stream);
     cudaEventDestroy(c.ev0);
     cudaEventDestroy(c.ev1);
+    cudaEventDestroy(c.ev_staged);
     for (auto &e : c.evs) cudaEventDestroy(e);
   }
   c.ready = false;
@@ -1457,9 +1510,17 @@ extern "C" int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frame
                                                                                      std::max<size_t>(num_frames, 1)),
                                                                0, 0);
   if (!sv) return 1;
+  /* largest first, so that the last frames of the batch do not run alone */
+  std::vector<size_t> order(num_frames);
+  std::vector<uint64_t> est(num_frames);
+  for (size_t n = 0; n < num_frames; n++) {
+    order[n] = n;
+    est[n] = request_estimate(frames + n, 1ULL << 27);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return est[a] > est[b]; });
   std::vector<uint64_t> tickets(num_frames);
   int rc = 0;
-  for (size_t n = 0; n < num_frames; n++) rc |= contour3d_gb300_server_submit(sv, frames + n, &tickets[n]);
+  for (size_t q = 0; q < num_frames; q++) rc |= contour3d_gb300_server_submit(sv, frames + order[q], &tickets[order[q]]);
   for (size_t n = 0; n < num_frames; n++) {
     contour3d_gb300_request_stats_t st;
     rc |= contour3d_gb300_server_wait(sv, tickets[n], &st);

@@ -122,8 +122,12 @@ class Library:
         L.contour3d_gb300_debug_cell_counts.argtypes = [C.POINTER(_abi.ContourObj), C.c_void_p]
         L.c3d_fieldgen_modes_device.restype = C.c_double
         L.c3d_fieldgen_modes_device.argtypes = [C.c_void_p, C.c_int, C.c_long * 3, C.c_long * 3, C.c_long * 3,
-                                                C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64]
+                                                C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, C.c_double]
         L.c3d_fieldgen_blobs_device.restype = C.c_int
+        L.c3d_fieldgen_modes_device_async.restype = C.c_double
+        L.c3d_fieldgen_modes_device_async.argtypes = [
+            C.c_void_p, C.c_int, C.c_long * 3, C.c_long * 3, C.c_long * 3, C.c_int, C.c_int, C.c_int, C.c_double,
+            C.c_uint64, C.c_double, C.c_void_p]
         L.contour3d_gb300_render_device.argtypes = [
             C.POINTER(_abi.Vector), C.POINTER(_abi.Vector), C.POINTER(C.c_size_t), C.POINTER(_abi.Vector),
             C.POINTER(_abi.Vector), C.POINTER(_abi.Color), C.c_size_t, C.POINTER(Field), C.c_size_t,
@@ -258,13 +262,24 @@ class Library:
         return counts, int(total)
 
     def fieldgen_modes_device(self, ptr: int, dtype: int, shape, nmodes, kmin, kmax, power, seed,
-                              offset=(0, 0, 0), glshape=None) -> float:
+                              offset=(0, 0, 0), glshape=None, time: float = 0.0) -> float:
         nz, ny, nx = shape
         gl = glshape or shape
         std = self.lib.c3d_fieldgen_modes_device(
             C.c_void_p(ptr), dtype, (C.c_long * 3)(gl[2], gl[1], gl[0]),
             (C.c_long * 3)(offset[2], offset[1], offset[0]), (C.c_long * 3)(nx, ny, nz), nmodes, kmin,
-            kmax, power, seed)
+            kmax, power, seed, time)
+        if std < 0:
+            raise RuntimeError("device field generation failed")
+        return std
+
+    def fieldgen_modes_device_async(self, ptr: int, dtype: int, shape, nmodes, kmin, kmax, power, seed,
+                                    time: float, stream: int) -> float:
+        nz, ny, nx = shape
+        z = (C.c_long * 3)(0, 0, 0)
+        std = self.lib.c3d_fieldgen_modes_device_async(
+            C.c_void_p(ptr), dtype, (C.c_long * 3)(nx, ny, nz), z, (C.c_long * 3)(nx, ny, nz), nmodes, kmin, kmax,
+            power, seed, time, C.c_void_p(stream))
         if std < 0:
             raise RuntimeError("device field generation failed")
         return std
