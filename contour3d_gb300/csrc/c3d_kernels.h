@@ -44,9 +44,10 @@ struct SlabDev {
 struct TriDev {
   double* wn[3];      /* area * face normal, where requested */
   unsigned* meta;     /* edge ids (3 x 5 bits) | flags | rank in the cell */
-  /* k_cover's input, 3 float4 per triangle: x0 y0 z0 x1 | y1 z1 x2 y2 |
-     z2 err_xy err_z meta -- FP32 screen positions and depths, the bound on
-     |screen x, y - the reference's value| and the relative depth bound */
+  /* k_cover's input, the compact list of triangles that reach it (k_emit
+     appends them), 3 float4 each: x0 y0 z0 x1 | y1 z1 x2 y2 | z2 err_xy
+     err_z t -- FP32 screen positions and depths, the bound on |screen x, y -
+     the reference's value|, the relative depth bound and the emission index */
   float4* rec;
   unsigned* need;     /* 1 once the weighted normal was requested */
   double* vert[9];    /* inspection: exact vertices */
@@ -92,6 +93,9 @@ struct RasterDev {
   unsigned* tiny;           /* triangles the FP32 filter cannot settle */
   unsigned long long tiny_cap;
   unsigned long long* tiny_count;
+  unsigned long long* cover_count; /* entries of TriDev::rec (at most the slab's triangles) */
+  Candidate* live;          /* candidates that can still win (capacity cand_cap) */
+  unsigned long long* live_count;
   uint2* win;               /* (pixel, triangle) won by the current slab */
   unsigned long long* win_count;
   unsigned* need;           /* triangles whose weighted normal shading needs */
@@ -120,8 +124,8 @@ void launch_scan(const unsigned char* counts, long long n, unsigned* offsets,
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets, const unsigned* tri_cell,
-                 const unsigned long long* total, long long tri_bound, const TriDev& tri, unsigned* checks,
-                 cudaStream_t st);
+                 const unsigned long long* total, long long tri_bound, const TriDev& tri, const RasterDev& R,
+                 unsigned* checks, cudaStream_t st);
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
                       cudaStream_t st);
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
@@ -131,6 +135,7 @@ void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long*
                   cudaStream_t st);
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
                  unsigned long long order_base, unsigned* checks, cudaStream_t st);
+void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st);
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
                   unsigned long long order_base, cudaStream_t st);
 void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,

@@ -487,88 +487,6 @@ __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], co
   return 1;
 }
 
-/*
- * One thread per triangle: cube-edge ids and, for rendered triangles, the
- * FP32 screen vertices and their bounds.  Triangles whose culling the bounds
- * cannot decide are flagged for the exact path (k_tiny).
- */
-template <typename T, bool CHECK>
-__global__ void __launch_bounds__(256)
-k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
-       const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
-       const unsigned* __restrict__ tri_cell, const unsigned long long* __restrict__ total_p, TriDev tri,
-       unsigned* __restrict__ checks) {
-  __shared__ unsigned long long lut[kLutEntries];
-  for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
-  __syncthreads();
-  const long long T_ = (long long)*total_p;
-  const long long ncx = F.nx - 1, ncy = F.ny - 1;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
-       t += (long long)gridDim.x * blockDim.x) {
-    const unsigned c = tri_cell[t];
-    const unsigned r = (unsigned)(t - offsets[c]);
-    unsigned ui, uj, ukl;
-    cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
-    const long long i = ui, j = uj, k = S.kfirst + ukl;
-    const unsigned code = codes[c];
-    const unsigned long long e = lut[code * 12 + r];
-    unsigned edges = 0;
-#pragma unroll
-    for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
-    /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
-    const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
-    unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
-    if (rendered) {
-      float X[3], Y[3], Z[3], exy = 0.f, zr = 0.f;
-      int status = 1;
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-        float qv[3], eq[3], ex = 0.f, ez = 0.f, xa[3], xb[3];
-        const float ce = corner_pos_f(F, i, j, k, a, xa);
-        corner_pos_f(F, i, j, k, b, xb);
-        vertex_q(scene, F.threshold, xa, load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, a)), xb,
-                 load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, b)), ce, qv, eq);
-        const int st = project_f(scene, qv, eq, X[q], Y[q], Z[q], ex, ez);
-        if (st == 0) status = 0;
-        else if (st < 0 && status != 0) status = -1;
-        exy = fmaxf(exy, ex);
-        zr = fmaxf(zr, ez / fmaxf(fabsf(Z[q]), 1e-30f));
-      }
-      if (CHECK) {
-        /* the reference's own vertices and projection */
-        d3 v[3], p[3];
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-          v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
-                             corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
-        }
-        bool ok = true;
-#pragma unroll
-        for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
-        if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
-        if (status == 1 && ok) {
-#pragma unroll
-          for (int q = 0; q < 3; q++)
-            if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
-                fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
-              atomicAdd(checks + 1, 1u);
-        }
-      }
-      if (status == 0) meta |= kMetaCulled;
-      if (status < 0) meta |= kMetaUndecided;
-      float4* rec = tri.rec + 3 * t;
-      rec[0] = make_float4(X[0], Y[0], Z[0], X[1]);
-      rec[1] = make_float4(Y[1], Z[1], X[2], Y[2]);
-      rec[2] = make_float4(Z[2], exy, zr, __uint_as_float(meta));
-    } else {
-      tri.rec[3 * t + 2] = make_float4(0.f, 0.f, 0.f, __uint_as_float(meta));
-    }
-    tri.meta[t] = meta;
-  }
-}
-
 /* inspection: every triangle's exact vertices, face normal, area and weighted normal */
 __global__ void __launch_bounds__(256) k_exact_all(Geo G, const unsigned long long* __restrict__ total_p, TriDev tri) {
   const long long T_ = (long long)*total_p;
@@ -769,6 +687,130 @@ __device__ __forceinline__ void centre_range(float lo, float hi, long long n, lo
   b = fb == fb ? min(n - 1, (long long)ib) : 0;
 }
 
+/*
+ * One thread per triangle: cube-edge ids and, for rendered triangles, the
+ * FP32 screen vertices and their bounds, and the raster path that settles
+ * the triangle: k_tiny (FP64 throughout) when the bounds cannot decide its
+ * culling or whether its area is clamped, none when no pixel centre can lie
+ * in it, k_cover otherwise -- only those are written to the compact list
+ * k_cover reads.  Without raster lists (inspection) only the ids are kept.
+ */
+template <typename T, bool CHECK>
+__global__ void __launch_bounds__(256)
+k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
+       const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
+       const unsigned* __restrict__ tri_cell, const unsigned long long* __restrict__ total_p, TriDev tri,
+       RasterDev R, unsigned* __restrict__ checks) {
+  __shared__ unsigned long long lut[kLutEntries];
+  for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
+  __syncthreads();
+  const long long T_ = (long long)*total_p;
+  const long long ncx = F.nx - 1, ncy = F.ny - 1;
+  const long long W = scene.width, H = scene.height;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
+       t += (long long)gridDim.x * blockDim.x) {
+    const unsigned c = tri_cell[t];
+    const unsigned r = (unsigned)(t - offsets[c]);
+    unsigned ui, uj, ukl;
+    cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
+    const long long i = ui, j = uj, k = S.kfirst + ukl;
+    const unsigned code = codes[c];
+    const unsigned long long e = lut[code * 12 + r];
+    unsigned edges = 0;
+#pragma unroll
+    for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
+    /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
+    const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
+    unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
+    float X[3] = {0.f, 0.f, 0.f}, Y[3] = {0.f, 0.f, 0.f}, Z[3] = {0.f, 0.f, 0.f}, exy = 0.f, zr = 0.f;
+    int route = 0; /* 0 no fragment, 1 k_tiny, 2 k_cover */
+    if (rendered) {
+      int status = 1;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+        float qv[3], eq[3], ex = 0.f, ez = 0.f, xa[3], xb[3];
+        const float ce = corner_pos_f(F, i, j, k, a, xa);
+        corner_pos_f(F, i, j, k, b, xb);
+        vertex_q(scene, F.threshold, xa, load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, a)), xb,
+                 load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, b)), ce, qv, eq);
+        const int st = project_f(scene, qv, eq, X[q], Y[q], Z[q], ex, ez);
+        if (st == 0) status = 0;
+        else if (st < 0 && status != 0) status = -1;
+        exy = fmaxf(exy, ex);
+        zr = fmaxf(zr, ez / fmaxf(fabsf(Z[q]), 1e-30f));
+      }
+      d3 v[3];
+      bool ok = true;
+      if (CHECK) {
+        /* the reference's own vertices and projection */
+        d3 p[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+          v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
+                             corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
+        }
+#pragma unroll
+        for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
+        if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
+        if (status == 1 && ok) {
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
+                fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
+              atomicAdd(checks + 1, 1u);
+        }
+      }
+      if (status == 0) meta |= kMetaCulled;
+      if (status < 0) meta |= kMetaUndecided;
+      if (R.cover_count && status != 0) {
+        /* the reference's area is certainly not clamped to +-1e-16
+           (render.c:108-111): its weights are barycentric up to the -1e-8
+           slack, so every covered pixel centre lies in the triangle's extent */
+        const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
+        float errA;
+        const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
+        const bool unclamped = status > 0 && isfinite(A) && isfinite(exy) && fabsf(A) - errA > 1e-15f &&
+                               exy < 1e-3f && zr < 1e-3f;
+        if (!unclamped) {
+          route = 1;
+        } else {
+          const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
+          const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
+          const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
+          long long imin, imax, jmin, jmax;
+          centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
+          centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+          route = imin <= imax && jmin <= jmax ? 2 : 0;
+          if (CHECK && route == 0 && ok) {
+            /* no pixel of the reference's box may be covered */
+            ExactTri ex;
+            if (exact_tri(scene, v, ex))
+              for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
+                for (long long ii = ex.imin; ii <= ex.imax; ii++) {
+                  double w0, w1, w2;
+                  if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
+                }
+          }
+        }
+      }
+    }
+    tri.meta[t] = meta;
+    if (R.cover_count) {
+      const unsigned long long ti = append_slot(R.tiny_count, route == 1);
+      const unsigned long long ci = append_slot(R.cover_count, route == 2);
+      if (route == 1 && ti < R.tiny_cap) R.tiny[ti] = (unsigned)t; /* overflow: the host re-runs the slab */
+      if (route == 2) {
+        float4* rec = tri.rec + 3 * ci; /* ci < the slab's triangle count */
+        rec[0] = make_float4(X[0], Y[0], Z[0], X[1]);
+        rec[1] = make_float4(Y[1], Z[1], X[2], Y[2]);
+        rec[2] = make_float4(Z[2], exy, zr, __uint_as_float((unsigned)t));
+      }
+    }
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* triangles the single-precision filter cannot settle                 */
 /* ------------------------------------------------------------------ */
@@ -822,40 +864,28 @@ __device__ void tiny_triangle(const Geo& G, const SceneDev& s, long long t, cons
 
 template <bool CHECK>
 __global__ void __launch_bounds__(256, 4)
-k_cover(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
-        unsigned long long order_base, unsigned* __restrict__ checks) {
-  const long long T_ = (long long)*total_p;
+k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
+  const long long n = (long long)*R.cover_count;
   const long long W = scene.width, H = scene.height;
-  /* traverse front to back along z (the order of the emission index) so that
-     near surfaces raise the floors early */
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < T_; q += (long long)gridDim.x * blockDim.x) {
-    const long long t = scene.z_descending ? T_ - 1 - q : q;
-    const float4 r2 = __ldg(tri.rec + 3 * t + 2);
-    const unsigned meta = __float_as_uint(r2.w);
-    if (!(meta & kMetaRendered) || (meta & kMetaCulled)) continue;
-    const float4 r0 = __ldg(tri.rec + 3 * t), r1 = __ldg(tri.rec + 3 * t + 1);
+  /* traverse front to back along z (the list is close to emission order,
+     which follows z) so that near surfaces raise the floors early */
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const long long qq = scene.z_descending ? n - 1 - q : q;
+    const float4 r0 = __ldg(tri.rec + 3 * qq), r1 = __ldg(tri.rec + 3 * qq + 1), r2 = __ldg(tri.rec + 3 * qq + 2);
+    const long long t = (long long)__float_as_uint(r2.w);
     const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
     const float eps = r2.y, zr = r2.z;
-    /* inverse area (render.c:102-107) with its bound */
+    /* inverse area (render.c:102-107) with its bound; k_emit listed only
+       triangles whose area is certainly not clamped and whose extent may
+       hold a pixel centre.  The per-pixel weight bounds are used when they
+       are tight enough to decide anything (rai < 0.5) */
     const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
     const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
     const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
     float errA;
     const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
     const float rai = errA / (fabsf(A) - errA) + 1.1f * kU32;
-    /* unclamped: the reference's area is certainly not clamped to +-1e-16
-       (render.c:108-111), so its weights are barycentric up to the -1e-8
-       slack and every covered pixel centre lies inside the triangle's
-       extent; the per-pixel weight bounds are used when they are tight
-       enough to decide anything (rai < 0.5) */
-    const bool unclamped = !(meta & kMetaUndecided) && isfinite(A) && isfinite(eps) && fabsf(A) - errA > 1e-15f &&
-                           eps < 1e-3f && zr < 1e-3f;
     const bool weights_ok = rai < 0.5f;
-    const unsigned long long ti = append_slot(R.tiny_count, !unclamped);
-    if (!unclamped) {
-      if (ti < R.tiny_cap) R.tiny[ti] = (unsigned)t; /* overflow: the host re-runs the slab */
-      continue;
-    }
     const float ai = 1.f / A;
     const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
     const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
@@ -935,13 +965,28 @@ k_tiny(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsign
 /* ------------------------------------------------------------------ */
 /* k_exact: the reference's arithmetic for the surviving candidates    */
 /* ------------------------------------------------------------------ */
-__global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base) {
+/*
+ * Candidates whose depth bound reaches the pixel's final floor, compacted:
+ * an FP64 warp instruction costs the same with one active lane as with 32,
+ * so k_exact runs only over fragments that can still win.
+ */
+__global__ void __launch_bounds__(256) k_prune(RasterDev R) {
   const unsigned long long n = min(*R.cand_count, R.cand_cap);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x) {
     const Candidate c = R.cand[q];
     /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
-    if (f_key(c.dhi) < R.zlo[c.pixel]) continue;
+    const bool keep = f_key(c.dhi) >= R.zlo[c.pixel];
+    const unsigned long long w = append_slot(R.live_count, keep);
+    if (keep) R.live[w] = c; /* w < n <= cand_cap */
+  }
+}
+
+__global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base) {
+  const unsigned long long n = *R.live_count;
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const Candidate c = R.live[q];
     const unsigned pj = c.pixel / (unsigned)scene.width;
     exact_fragment(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base);
   }
@@ -1199,15 +1244,19 @@ long long scan_tiles(long long n) { return (n + kScanTile) / kScanTile; }
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets, const unsigned* tri_cell,
-                 const unsigned long long* total, long long tri_bound, const TriDev& tri, unsigned* checks,
-                 cudaStream_t st) {
+                 const unsigned long long* total, long long tri_bound, const TriDev& tri, const RasterDev& R,
+                 unsigned* checks, cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
   if (checks) {
-    if (F.is_f32) k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
-    else k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
+    if (F.is_f32)
+      k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
+    else
+      k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
   } else {
-    if (F.is_f32) k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
-    else k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, checks);
+    if (F.is_f32)
+      k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
+    else
+      k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
   }
 }
 
@@ -1225,9 +1274,11 @@ void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets
 void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                   const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned* checks,
                   cudaStream_t st) {
+  (void)total;
+  (void)order_base;
   const int g = grid_for(tri_bound, 256, 8);
-  if (checks) k_cover<true><<<g, 256, 0, st>>>(G, scene, total, tri, R, order_base, checks);
-  else k_cover<false><<<g, 256, 0, st>>>(G, scene, total, tri, R, order_base, checks);
+  if (checks) k_cover<true><<<g, 256, 0, st>>>(G, scene, tri, R, checks);
+  else k_cover<false><<<g, 256, 0, st>>>(G, scene, tri, R, checks);
 }
 
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
@@ -1235,6 +1286,10 @@ void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, cons
   const int g = grid_for(tiny_bound, 256, 8);
   if (checks) k_tiny<true><<<g, 256, 0, st>>>(G, scene, R, order_base, checks);
   else k_tiny<false><<<g, 256, 0, st>>>(G, scene, R, order_base, checks);
+}
+
+void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st) {
+  k_prune<<<grid_for(cand_bound, 256, 8), 256, 0, st>>>(R);
 }
 
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,

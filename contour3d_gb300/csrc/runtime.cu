@@ -353,7 +353,7 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
-  Buf zlo, xyf, cand, tiny, win, need, checks;
+  Buf zlo, xyf, cand, live, tiny, win, need, checks;
   HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
   cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
   bool filter_check = false;
@@ -466,6 +466,10 @@ struct FrameOut {
   PixelRec *pixels_host = nullptr; /* canvas order, for the multi-rank reduction */
   DebugSink *sink = nullptr;
 };
+
+/* device counters of one slab's raster passes: candidates, tiny triangles,
+   won pixels, requested normals, listed triangles, surviving candidates */
+static const int kCounters = 6;
 
 /* bytes per triangle of the slab arrays (see TriDev) */
 static const size_t kTriBytes = 3 * sizeof(double) + 48 + 2 * sizeof(unsigned);
@@ -642,11 +646,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     const TriDev tri = tri_layout(c.tri.p, cap, dbg);
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
     launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
-    if (c.stage_timing) cudaEventRecord(c.evs[3], st);
-    launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
-                c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, checks, st);
-    if (c.stage_timing) cudaEventRecord(c.evs[4], st);
-    c.stats.kernel_launches += 2;
+    c.stats.kernel_launches += 1;
     const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
     Geo G;
     G.F = F;
@@ -657,14 +657,18 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     G.offsets = c.offsets.as<unsigned>();
     G.meta = tri.meta;
     if (sink) {
+      RasterDev none = {};
+      launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+                  c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, checks, st);
       launch_exact_all(G, d_total, (long long)T, tri, st);
       launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
-      c.stats.kernel_launches += 2;
+      c.stats.kernel_launches += 3;
     } else {
       /* candidate and tiny lists: about one entry per covered pixel and a few
-         percent of the triangles; when one overflows, the slab's raster passes
-         run again with larger lists (every z-buffer update is an idempotent
-         maximum, so repeating them is harmless) */
+         percent of the triangles; when one overflows, the slab's emission and
+         raster passes run again with larger lists (every z-buffer update is
+         an idempotent maximum, so repeating them is harmless).  The cover
+         list holds at most one entry per triangle and cannot overflow. */
       const size_t npx = (size_t)(sd.width * sd.height);
       if (c.win.ensure(sizeof(uint2) * npx, st) || c.need.ensure(sizeof(unsigned) * T, st)) return 1;
       unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
@@ -676,19 +680,29 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       RS.win_count = counters + 2;
       RS.need = c.need.as<unsigned>();
       RS.need_count = counters + 3;
+      RS.cover_count = counters + 4;
+      RS.live_count = counters + 5;
       for (int attempt = 0;; attempt++) {
-        if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.tiny.ensure(sizeof(unsigned) * tiny_want, st)) return 1;
+        if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.live.ensure(sizeof(Candidate) * cand_want, st) ||
+            c.tiny.ensure(sizeof(unsigned) * tiny_want, st))
+          return 1;
         RS.cand = c.cand.as<Candidate>();
-        RS.cand_cap = c.cand.cap / sizeof(Candidate);
+        RS.cand_cap = std::min(c.cand.cap, c.live.cap) / sizeof(Candidate);
         RS.cand_count = counters + 0;
+        RS.live = c.live.as<Candidate>();
         RS.tiny = c.tiny.as<unsigned>();
         RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
         RS.tiny_count = counters + 1;
-        C3D_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st));
+        C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
         C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
+        if (c.stage_timing) cudaEventRecord(c.evs[3], st);
+        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+                    c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, checks, st);
+        if (c.stage_timing) cudaEventRecord(c.evs[4], st);
         launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
         launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
         if (c.stage_timing) cudaEventRecord(c.evs[5], st);
+        launch_prune(RS, (long long)RS.cand_cap, st);
         launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
         if (c.stage_timing) cudaEventRecord(c.evs[6], st);
         /* shading runs before the overflow check: when a list overflowed, the
@@ -696,8 +710,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
            colours are the same values */
         launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
         if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-        c.stats.kernel_launches += 7;
-        C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        c.stats.kernel_launches += 9;
+        C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         C3D_CUDA(cudaStreamSynchronize(st));
         if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
         if (attempt > 4) {
@@ -712,6 +726,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.tiny += h_cnt[1];
       c.stats.winners += h_cnt[2];
       c.stats.normals += h_cnt[3];
+      c.stats.cover_triangles += h_cnt[4];
+      c.stats.exact_fragments += h_cnt[5];
       if (c.stage_timing) {
         c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
         c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);
@@ -1271,7 +1287,7 @@ extern "C" int contour3d_gb300_release(void) {
 
 static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.tiny, &c.win, &c.need,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need,
                  &c.checks};
   /* every call of the context has completed, so its buffers go back to the
      pool in order on its own stream */
@@ -1330,7 +1346,8 @@ static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t sla
     if (sz[0] < 2 || sz[1] < 2 || sz[2] < 2) continue;
     const uint64_t per_slice = (uint64_t)(sz[0] - 1) * (sz[1] - 1);
     uint64_t cells = std::min<uint64_t>(per_slice * (sz[2] - 1), std::max<uint64_t>(slab_cells, per_slice * 3));
-    const uint64_t bytes = cells * (1 + 4 + 4) + cells * (kTriBytes + 4 + 4) + cells / 2 * sizeof(Candidate);
+    /* candidates and their surviving copy: half a triangle's worth each */
+    const uint64_t bytes = cells * (1 + 4 + 4) + cells * (kTriBytes + 4 + 4) + cells * sizeof(Candidate);
     peak = std::max(peak, bytes);
   }
   const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];

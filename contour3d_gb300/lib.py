@@ -25,7 +25,8 @@ class Stats(C.Structure):
                 ("normals", C.c_uint64), ("slabs", C.c_uint64), ("kernel_launches", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_classify", C.c_double), ("ms_scan", C.c_double),
                 ("ms_emit", C.c_double), ("ms_cover", C.c_double), ("ms_exact", C.c_double),
-                ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5)]
+                ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5),
+                ("cover_triangles", C.c_uint64), ("exact_fragments", C.c_uint64)]
 
 
 class Field(C.Structure):

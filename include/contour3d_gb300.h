@@ -192,6 +192,8 @@ typedef struct {
      [2] covered pixel dropped, [3] uncovered pixel called inside,
      [4] depth outside its interval */
   uint64_t filter_violations[5];
+  uint64_t cover_triangles;   /* triangles whose extent may hold a pixel centre (FP32 filter input) */
+  uint64_t exact_fragments;   /* candidates that reached the reference's FP64 arithmetic */
 } contour3d_gb300_stats_t;
 
 int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);
