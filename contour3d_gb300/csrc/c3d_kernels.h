@@ -60,6 +60,12 @@ constexpr unsigned kMetaCulled = 1u << 16;
 constexpr unsigned kMetaRankShift = 17;
 constexpr unsigned kMetaUndecided = 1u << 21;
 
+/* FP32 screen vertices of a slab's crossed edges (k_vertices) */
+struct VertDev {
+  float4* pos; /* X, Y, Z, bound on |X, Y - the reference's value| */
+  float* aux;  /* relative depth bound, or -1 (projection fails), -2 (undecided) */
+};
+
 /* what the exact path needs to rebuild a triangle from the field */
 struct Geo {
   FieldDev F;
@@ -118,14 +124,19 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
 long long scan_tiles(long long n);
 
 void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, cudaStream_t st);
-void launch_scan(const unsigned char* counts, long long n, unsigned* offsets,
-                 unsigned long long* tile_state, unsigned* tile_counter, unsigned long long* total,
+/* cells per slab for which the packed triangle and vertex sums of k_scan stay below 2^31 */
+constexpr long long kMaxSlabCells = 178956970;
+
+void launch_scan(const unsigned char* counts, long long n, unsigned* offsets, unsigned* voffsets,
+                 unsigned long long* tile_state, unsigned* tile_counter, unsigned long long* totals,
                  unsigned* err, cudaStream_t st);
+void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
+                     const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
-                 const unsigned char* codes, const unsigned* offsets, const unsigned* tri_cell,
-                 const unsigned long long* total, long long tri_bound, const TriDev& tri, const RasterDev& R,
-                 unsigned* checks, cudaStream_t st);
+                 const unsigned char* codes, const unsigned* offsets, const unsigned* voffsets,
+                 const unsigned* tri_cell, const unsigned long long* total, long long tri_bound, const TriDev& tri,
+                 const RasterDev& R, const VertDev& V, unsigned* checks, cudaStream_t st);
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
                       cudaStream_t st);
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,

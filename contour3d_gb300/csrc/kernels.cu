@@ -168,6 +168,22 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
 /* ------------------------------------------------------------------ */
 /* k_scan: single-pass decoupled look-back exclusive scan              */
 /* ------------------------------------------------------------------ */
+/*
+ * Vertices are owned by cells: cell c owns the crossed edges that start at
+ * its corner 0 and run to corner m = 1..7 (+x, +y, +x+y, +z, +x+z, +y+z,
+ * +x+y+z).  Every edge of the six-tetrahedra split joins corners a, b with
+ * a & b = a or b, so it starts at corner a & b of its cell and runs in
+ * direction a ^ b: it is the edge m = a ^ b owned by the cell at offset a & b.
+ * Bit m - 1 of the result: the iso-level crosses edge m of the cell's corner 0.
+ */
+__device__ __forceinline__ unsigned owned_edges(unsigned code) {
+  const unsigned flip = code ^ (0u - (code & 1u));
+  return (flip >> 1) & 0x7Fu;
+}
+
+__device__ __forceinline__ unsigned long long packed_count(unsigned short c) {
+  return (unsigned long long)(c & 0xFF) | ((unsigned long long)(c >> 8) << 31);
+}
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;  /* cells per thread */
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -175,23 +191,31 @@ constexpr unsigned long long kFlagAgg = 1ULL << 62;
 constexpr unsigned long long kFlagPrefix = 2ULL << 62;
 constexpr unsigned long long kValueMask = (1ULL << 62) - 1;
 
+/*
+ * Both scans in one: per cell, its triangle count and the number of its
+ * owned vertices (edges from its corner 0 that the iso-level crosses), packed
+ * as tri | vert << 31 -- every sum stays below 2^31 in both fields for slabs
+ * of at most kMaxSlabCells cells, so the packed additions never carry.
+ */
+constexpr unsigned long long kTriMask = (1ULL << 31) - 1;
+
 __global__ void __launch_bounds__(kScanThreads)
 k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restrict__ offsets,
-       unsigned long long* __restrict__ tile_state,
+       unsigned* __restrict__ voffsets, unsigned long long* __restrict__ tile_state,
        unsigned* __restrict__ tile_counter, unsigned long long* __restrict__ total,
        unsigned* __restrict__ err) {
   __shared__ unsigned s_tile;
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ unsigned long long s_excl;
-  __shared__ unsigned char s_count[256];
+  __shared__ unsigned short s_count[256];
   if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
-  s_count[threadIdx.x] = c_code_count[threadIdx.x];
+  s_count[threadIdx.x] = (unsigned short)(c_code_count[threadIdx.x] | (__popc(owned_edges(threadIdx.x)) << 8));
   __syncthreads();
   const unsigned tile = s_tile;
   const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
 
-  unsigned char cnt[kScanItems];
-  unsigned sum = 0;
+  unsigned short cnt[kScanItems]; /* triangles | vertices << 8 */
+  unsigned long long sum = 0;
   if (base + kScanItems <= n) {
     /* one 16-byte load (base is a multiple of 16, the buffer 256-byte aligned) */
     const uint4 v = *reinterpret_cast<const uint4*>(counts + base);
@@ -206,7 +230,7 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
     }
   }
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) sum += cnt[q];
+  for (int q = 0; q < kScanItems; q++) sum += packed_count(cnt[q]);
   /* block-wide exclusive scan of the per-thread sums */
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long incl = sum;
@@ -289,28 +313,37 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
   }
   __syncthreads();
   unsigned long long run = s_excl + thread_excl;
-  unsigned out[kScanItems];
+  unsigned out[kScanItems], vout[kScanItems];
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) {
-    out[q] = (unsigned)run;
-    run += cnt[q];
+    out[q] = (unsigned)(run & kTriMask);
+    vout[q] = (unsigned)(run >> 31);
+    run += packed_count(cnt[q]);
   }
   if (base + kScanItems <= n) {
-    /* four 16-byte stores (offsets + base is 64-byte aligned) */
+    /* four 16-byte stores per array (offsets + base is 64-byte aligned) */
     uint4* o = reinterpret_cast<uint4*>(offsets + base);
+    uint4* vo = reinterpret_cast<uint4*>(voffsets + base);
 #pragma unroll
-    for (int q = 0; q < kScanItems / 4; q++) o[q] = make_uint4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+    for (int q = 0; q < kScanItems / 4; q++) {
+      o[q] = make_uint4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+      vo[q] = make_uint4(vout[4 * q], vout[4 * q + 1], vout[4 * q + 2], vout[4 * q + 3]);
+    }
   } else {
 #pragma unroll
     for (int q = 0; q < kScanItems; q++) {
       const long long c = base + q;
-      if (c <= n) offsets[c] = out[q]; /* offsets[n] = total */
+      if (c <= n) { /* offsets[n] = totals */
+        offsets[c] = out[q];
+        voffsets[c] = vout[q];
+      }
     }
   }
   if (n >= base && n < base + kScanItems) {
     unsigned long long tot = s_excl + thread_excl;
-    for (long long c = base; c < n; c++) tot += cnt[c - base];
-    *total = tot;
+    for (long long c = base; c < n; c++) tot += packed_count(cnt[c - base]);
+    total[0] = tot & kTriMask;
+    total[1] = tot >> 31;
   }
 }
 
@@ -389,41 +422,70 @@ __device__ __forceinline__ void face_normal(const d3 v[3], d3& fn, double& area,
 /* ------------------------------------------------------------------ */
 /* k_emit: single-precision triangles with certified bounds             */
 /* ------------------------------------------------------------------ */
+/* a field value as a float and the bound on its conversion error */
+__device__ __forceinline__ float value_f(double v, float& e) {
+  const float a = to_f(v); /* truncation: < 2u |a|, or < 2^-126 when flushed */
+  e = 2.f * kU32 * fabsf(a) + 1.2e-38f;
+  return a;
+}
+__device__ __forceinline__ float value_f(float v, float& e) {
+  e = 0.f;
+  return v;
+}
+
 /*
  * FP32 estimate of one vertex (triangulate.c:40-73) relative to the camera,
  * q = vertex - camera, with a bound per component on the distance to the
- * reference's FP64 value.  Only the two value differences are formed in FP64
- * (they cancel); the corner coordinates come as floats (node coordinates
- * rounded once on the host); everything else is single precision:
- *   f = (vt - v0) / (v1 - v0)          relative error <= 3.1 u
- *   p = p0 + f (p1 - p0)               per component, bounded below
+ * reference's FP64 value.  No FP64 arithmetic: the corner values are
+ * converted to float (exactly for float fields) and the differences
+ *   dv = v1 - v0,  dt = vt - v0,  f = dt / dv,  p = p0 + f (p1 - p0)
+ * are formed in single precision with absolute bounds e_dv, e_dt, e_f.
+ * The reference keeps p0 when |v1 - v0| < 1e-8; returns false when the
+ * bounds cannot decide that test (the triangle then takes the FP64 path).
  */
-__device__ __forceinline__ void vertex_q(const SceneDev& s, double vt, const float x0[3], double v0, const float x1[3],
-                                         double v1, float ce, float q[3], float eq[3]) {
+template <typename T>
+__device__ __forceinline__ bool vertex_q(const SceneDev& s, float vt, float e_vt, const float x0[3], T v0,
+                                         const float x1[3], T v1, float ce, float q[3], float eq[3]) {
   /* x0, x1: corner coordinates rounded to float with error <= ce u |x| */
-  const double dv = dsub(v1, v0);
   const float pc[3] = {s.f_cam[0], s.f_cam[1], s.f_cam[2]};
-  if (abs_lt_1e8(dv)) {
-    /* the reference keeps p0 itself */
+  float e0, e1;
+  const float a0 = value_f(v0, e0), a1 = value_f(v1, e1);
+  const float dv = a1 - a0;
+  const float e_dv = e0 + e1 + 1.01f * kU32 * fabsf(dv);
+  const float adv = fabsf(dv);
+  if (!(adv - e_dv > 1.00001e-8f)) {
+    if (!(adv + e_dv < 0.99999e-8f)) return false;
+    /* certainly |v1 - v0| < 1e-8: the reference keeps p0 itself */
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       q[i] = x0[i] - pc[i];
       eq[i] = 1.1f * kU32 * (ce * fabsf(x0[i]) + fabsf(pc[i]) + fabsf(q[i])) + 1e-30f;
     }
-    return;
+    return true;
   }
-  /* f: two truncating conversions (2u each) and a division (u) */
-  const float f = to_f(dsub(vt, v0)) / to_f(dv);
+  /* 1 / |dv| to 2 ulp (__fdividef, |dv| in [1e-8, 1e30]); 1 / (|dv| - e_dv)
+     <= rdv (1 + 1.02 x) for x = e_dv rdv < 0.01 */
+  if (adv > 1e30f) return false;
+  const float rdv = __fdividef(1.f, adv);
+  const float xr = e_dv * rdv;
+  if (!(xr < 0.01f)) return false;
+  const float dt = vt - a0;
+  const float e_dt = e_vt + e0 + 1.01f * kU32 * fabsf(dt);
+  const float f = __fdividef(dt, dv); /* 2 ulp */
   const float af = fabsf(f);
+  /* |dt/dv - DT/DV| <= (e_dt + |DT/DV| e_dv) / |dv|, |DT/DV| <= fmax */
+  const float fmax = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
+  const float e_f = 1.1f * (1.01f * (e_dt + fmax * e_dv) * rdv + 4.f * kU32 * af);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     const float d = x1[i] - x0[i];
     const float p = x0[i] + f * d;
     q[i] = p - pc[i];
-    const float ep = kU32 * (ce * fabsf(x0[i]) + fabsf(p) +
-                             af * (ce * fabsf(x0[i]) + ce * fabsf(x1[i]) + 7.2f * fabsf(d)));
+    const float ep = e_f * fabsf(d) +
+                     kU32 * (ce * fabsf(x0[i]) + fabsf(p) + af * (ce * fabsf(x0[i]) + ce * fabsf(x1[i]) + 2.2f * fabsf(d)));
     eq[i] = 1.1f * (ep + kU32 * (fabsf(pc[i]) + fabsf(q[i]))) + 1e-30f;
   }
+  return true;
 }
 
 /* corner coordinates as floats, and the bound factor of their rounding */
@@ -471,14 +533,20 @@ __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], co
   if (!isfinite(nq) || !isfinite(lq) || !isfinite(mq)) return -1;
   /* project.c:39-46: |nr| < 1e-8 or t outside (0, 1) => the point is dropped */
   if (anq + e_nq < 0.99e-8f) return 0;
-  if (anq - e_nq <= 1.01e-8f) return -1;
-  const float t = s.f_dq / nq;
-  const float et = fabsf(t) * (e_nq / (anq - e_nq) + 3.f * kU32) + 1e-30f;
+  if (anq - e_nq <= 1.01e-8f || anq > 1e30f) return -1;
+  /* r = 1 / nq to 2 ulp (__fdividef, |nq| in [1e-8, 1e30]); with
+     x = e_nq |r| < 0.01, 1 / (|nq| - e_nq) <= |r| (1 + 1.02 x) (1 + 4u) */
+  const float r = __fdividef(1.f, nq);
+  const float x = e_nq * fabsf(r);
+  if (!(x < 0.01f)) return -1;
+  const float rin = 1.01f * fabsf(r) * (1.f + 1.02f * x);
+  const float t = s.f_dq * r;
+  const float et = fabsf(t) * (1.02f * x + 6.f * kU32) + 1e-30f;
   if (t + et < 0.f || t - et > 1.f) return 0;
   if (t - et <= 0.f || t + et >= 1.f) return -1;
-  const float rx = lq / nq, ry = mq / nq;
-  const float erx = (e_lq + fabsf(rx) * e_nq) / (anq - e_nq) + kU32 * fabsf(rx);
-  const float ery = (e_mq + fabsf(ry) * e_nq) / (anq - e_nq) + kU32 * fabsf(ry);
+  const float rx = lq * r, ry = mq * r;
+  const float erx = (e_lq + fabsf(rx) * e_nq) * rin + 6.f * kU32 * fabsf(rx);
+  const float ery = (e_mq + fabsf(ry) * e_nq) * rin + 6.f * kU32 * fabsf(ry);
   X = s.f_ax + s.f_bx * rx;
   Y = s.f_ay + s.f_by * ry;
   const float ex = fabsf(s.f_bx) * erx + kU32 * (fabsf(s.f_ax) + 2.f * fabsf(s.f_bx * rx) + fabsf(X)) + 1e-12f;
@@ -665,16 +733,52 @@ __device__ __forceinline__ float edge_eval(const EdgeF& E, float px, float py, f
 constexpr float kWOut = -1.0e-8f * (1.f + 1e-5f); /* certainly below -1e-8 */
 constexpr float kWIn = -1.0e-8f * (1.f - 1e-5f);  /* certainly above -1e-8 */
 
-/* warp-aggregated append; returns the slot index */
-__device__ __forceinline__ unsigned long long append_slot(unsigned long long* count, bool want) {
-  const unsigned mask = __ballot_sync(__activemask(), want);
-  if (!want) return ~0ULL;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(mask) - 1;
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(mask));
-  base = __shfl_sync(mask, base, leader);
-  return base + __popc(mask & ((1u << lane) - 1));
+/*
+ * Block-wide reservation of list slots for two lists at once: every thread of
+ * the block calls it at the same point with its item counts (block totals
+ * below 65536 per list).  One global atomic per block and list instead of
+ * one per warp: the list counters are single addresses that every block
+ * appends to, and same-address atomics serialise in the L2.
+ */
+template <int kThreads>
+__device__ __forceinline__ void block_reserve2(unsigned long long* count0, unsigned n0, unsigned long long* count1,
+                                               unsigned n1, unsigned long long& r0, unsigned long long& r1) {
+  __shared__ unsigned s_w[kThreads / 32];
+  __shared__ unsigned long long s_b[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned x = n0 | (n1 << 16);
+  unsigned incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned run = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; w++) {
+      const unsigned v = s_w[w];
+      s_w[w] = run;
+      run += v;
+    }
+    const unsigned t0 = run & 0xFFFFu, t1 = run >> 16;
+    s_b[0] = t0 ? atomicAdd(count0, (unsigned long long)t0) : 0ULL;
+    s_b[1] = t1 ? atomicAdd(count1, (unsigned long long)t1) : 0ULL;
+  }
+  __syncthreads();
+  const unsigned ex = s_w[warp] + incl - x;
+  r0 = s_b[0] + (ex & 0xFFFFu);
+  r1 = s_b[1] + (ex >> 16);
+  __syncthreads();
+}
+
+template <int kThreads>
+__device__ __forceinline__ unsigned long long block_reserve(unsigned long long* count, unsigned n) {
+  unsigned long long r0, r1;
+  block_reserve2<kThreads>(count, n, count, 0u, r0, r1);
+  return r0;
 }
 
 /* pixel index range whose centres (i + 0.5) / n - 0.5 may lie in [lo, hi] */
@@ -688,118 +792,191 @@ __device__ __forceinline__ void centre_range(float lo, float hi, long long n, lo
 }
 
 /*
+ * k_vertices: the FP32 screen position of every crossed edge of the slab,
+ * once per edge (a surface vertex is shared by about six triangles).  A block
+ * takes kVTile consecutive cells, lists their owned crossed edges in shared
+ * memory at their global vertex indices (voffsets), and computes them with
+ * all its threads.  Each record: X, Y, Z, the bound on |X, Y - the
+ * reference's value| and, in aux, the relative depth bound (>= 0), or -1 when
+ * the projection certainly fails, -2 when the bounds cannot decide it.  The
+ * edge runs from the owning corner to corner m; the reference interpolates a
+ * triangle's vertex from its own tail corner, which gives the same point up
+ * to FP64 rounding -- except where it keeps the tail because |v1 - v0| <
+ * 1e-8, so that case is left undecided.
+ */
+constexpr int kVThreads = 256;
+constexpr int kVItems = 8;
+constexpr int kVTile = kVThreads * kVItems;
+
+template <typename T>
+__global__ void __launch_bounds__(kVThreads)
+k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restrict__ codes,
+           const unsigned* __restrict__ voffsets, long long n, VertDev V) {
+  __shared__ unsigned short list[kVTile * 7];
+  const long long c0 = (long long)blockIdx.x * kVTile;
+  if (c0 >= n) return;
+  const long long c1 = min(c0 + kVTile, n);
+  const unsigned va = voffsets[c0], vb = voffsets[c1];
+  for (int q = 0; q < kVItems; q++) {
+    const int lc = threadIdx.x * kVItems + q;
+    const long long c = c0 + lc;
+    if (c >= c1) break;
+    unsigned mask = owned_edges(codes[c]);
+    unsigned at = voffsets[c] - va;
+    while (mask) {
+      const unsigned m = (unsigned)__ffs(mask); /* edge to corner m */
+      mask &= mask - 1;
+      list[at++] = (unsigned short)(lc | (m << 11));
+    }
+  }
+  __syncthreads();
+  const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
+  const T* fd = static_cast<const T*>(F.data);
+  float e_vt;
+  const float vt = value_f(F.threshold, e_vt);
+  for (unsigned e = threadIdx.x; e < vb - va; e += kVThreads) {
+    const unsigned entry = list[e];
+    const unsigned m = entry >> 11;
+    unsigned ui, uj, ukl;
+    cell_ijk((unsigned)(c0 + (entry & 2047)), ncx, ncy, ui, uj, ukl);
+    const long long i = ui, j = uj, k = S.kfirst + ukl;
+    float xa[3], xb[3], qv[3], eq[3];
+    const float ce = corner_pos_f(F, i, j, k, 0, xa);
+    corner_pos_f(F, i, j, k, (int)m, xb);
+    const bool vok = vertex_q<T>(scene, vt, e_vt, xa, __ldg(fd + corner_index(F, i, j, k, 0)), xb,
+                                 __ldg(fd + corner_index(F, i, j, k, (int)m)), ce, qv, eq);
+    float X = 0.f, Y = 0.f, Z = 0.f, exy = 0.f, ez = 0.f;
+    const int st = vok ? project_f(scene, qv, eq, X, Y, Z, exy, ez) : -1;
+    /* |Z| in [1e-8, 1e30] when the projection succeeds: __fdividef is within 2 ulp */
+    const float aux = st > 0 ? 1.01f * __fdividef(ez, fabsf(Z)) : (st == 0 ? -1.f : -2.f);
+    V.pos[va + e] = make_float4(X, Y, Z, exy);
+    V.aux[va + e] = aux;
+  }
+}
+
+/*
  * One thread per triangle: cube-edge ids and, for rendered triangles, the
- * FP32 screen vertices and their bounds, and the raster path that settles
- * the triangle: k_tiny (FP64 throughout) when the bounds cannot decide its
- * culling or whether its area is clamped, none when no pixel centre can lie
- * in it, k_cover otherwise -- only those are written to the compact list
- * k_cover reads.  Without raster lists (inspection) only the ids are kept.
+ * FP32 screen vertices and their bounds (gathered from k_vertices), and the
+ * raster path that settles the triangle: k_tiny (FP64 throughout) when the
+ * bounds cannot decide its culling or whether its area is clamped, none when
+ * no pixel centre can lie in it, k_cover otherwise -- only those are written
+ * to the compact list k_cover reads.  Without raster lists (inspection) only
+ * the ids are kept.
  */
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
        const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
-       const unsigned* __restrict__ tri_cell, const unsigned long long* __restrict__ total_p, TriDev tri,
-       RasterDev R, unsigned* __restrict__ checks) {
+       const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
+       const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R, VertDev V,
+       unsigned* __restrict__ checks) {
   __shared__ unsigned long long lut[kLutEntries];
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
   const long long T_ = (long long)*total_p;
   const long long ncx = F.nx - 1, ncy = F.ny - 1;
   const long long W = scene.width, H = scene.height;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
-       t += (long long)gridDim.x * blockDim.x) {
-    const unsigned c = tri_cell[t];
-    const unsigned r = (unsigned)(t - offsets[c]);
-    unsigned ui, uj, ukl;
-    cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
-    const long long i = ui, j = uj, k = S.kfirst + ukl;
-    const unsigned code = codes[c];
-    const unsigned long long e = lut[code * 12 + r];
-    unsigned edges = 0;
-#pragma unroll
-    for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
-    /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
-    const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
-    unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
-    float X[3] = {0.f, 0.f, 0.f}, Y[3] = {0.f, 0.f, 0.f}, Z[3] = {0.f, 0.f, 0.f}, exy = 0.f, zr = 0.f;
+  const unsigned ncxy = (unsigned)(ncx * ncy);
+  /* every thread of a block runs the same iterations (block-wide appends) */
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < T_; base += (long long)gridDim.x * blockDim.x) {
+    const long long t = base + threadIdx.x;
     int route = 0; /* 0 no fragment, 1 k_tiny, 2 k_cover */
-    if (rendered) {
-      int status = 1;
+    float X[3] = {0.f, 0.f, 0.f}, Y[3] = {0.f, 0.f, 0.f}, Z[3] = {0.f, 0.f, 0.f}, exy = 0.f, zr = 0.f;
+    if (t < T_) {
+      const unsigned c = tri_cell[t];
+      const unsigned r = (unsigned)(t - offsets[c]);
+      unsigned ui, uj, ukl;
+      cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
+      const long long i = ui, j = uj, k = S.kfirst + ukl;
+      const unsigned code = codes[c];
+      const unsigned long long e = lut[code * 12 + r];
+      unsigned edges = 0;
 #pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-        float qv[3], eq[3], ex = 0.f, ez = 0.f, xa[3], xb[3];
-        const float ce = corner_pos_f(F, i, j, k, a, xa);
-        corner_pos_f(F, i, j, k, b, xb);
-        vertex_q(scene, F.threshold, xa, load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, a)), xb,
-                 load_value<T>(static_cast<const T*>(F.data), corner_index(F, i, j, k, b)), ce, qv, eq);
-        const int st = project_f(scene, qv, eq, X[q], Y[q], Z[q], ex, ez);
-        if (st == 0) status = 0;
-        else if (st < 0 && status != 0) status = -1;
-        exy = fmaxf(exy, ex);
-        zr = fmaxf(zr, ez / fmaxf(fabsf(Z[q]), 1e-30f));
-      }
-      d3 v[3];
-      bool ok = true;
-      if (CHECK) {
-        /* the reference's own vertices and projection */
-        d3 p[3];
+      for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
+      /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
+      const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
+      unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
+      if (rendered && R.cover_count) {
+        /* the three vertices from k_vertices: vertex q lies on the edge from
+           corner a to corner b, owned by the cell at corner a & b */
+        int status = 1;
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-          const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-          v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
-                             corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
+          const unsigned a = (unsigned)((e >> (6 * q)) & 7), b = (unsigned)((e >> (6 * q + 3)) & 7);
+          const unsigned o = a & b, m = a ^ b;
+          const unsigned oc = c + (o & 1u) + ((o >> 1) & 1u) * (unsigned)ncx + (o >> 2) * ncxy;
+          const unsigned vi = voffsets[oc] + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
+          const float4 p = __ldg(V.pos + vi);
+          const float aux = __ldg(V.aux + vi);
+          X[q] = p.x;
+          Y[q] = p.y;
+          Z[q] = p.z;
+          exy = fmaxf(exy, p.w);
+          if (aux >= 0.f) zr = fmaxf(zr, aux);
+          else if (aux == -1.f) status = 0;
+          else if (status != 0) status = -1;
         }
+        d3 v[3];
+        bool ok = true;
+        if (CHECK) {
+          /* the reference's own vertices and projection */
+          d3 p[3];
 #pragma unroll
-        for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
-        if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
-        if (status == 1 && ok) {
+          for (int q = 0; q < 3; q++) {
+            const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+            v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
+                               corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
+          }
 #pragma unroll
-          for (int q = 0; q < 3; q++)
-            if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
-                fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
-              atomicAdd(checks + 1, 1u);
+          for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
+          if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
+          if (status == 1 && ok) {
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+              if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
+                  fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
+                atomicAdd(checks + 1, 1u);
+          }
         }
-      }
-      if (status == 0) meta |= kMetaCulled;
-      if (status < 0) meta |= kMetaUndecided;
-      if (R.cover_count && status != 0) {
-        /* the reference's area is certainly not clamped to +-1e-16
-           (render.c:108-111): its weights are barycentric up to the -1e-8
-           slack, so every covered pixel centre lies in the triangle's extent */
-        const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
-        float errA;
-        const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
-        const bool unclamped = status > 0 && isfinite(A) && isfinite(exy) && fabsf(A) - errA > 1e-15f &&
-                               exy < 1e-3f && zr < 1e-3f;
-        if (!unclamped) {
-          route = 1;
-        } else {
-          const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
-          const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
-          const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
-          long long imin, imax, jmin, jmax;
-          centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
-          centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
-          route = imin <= imax && jmin <= jmax ? 2 : 0;
-          if (CHECK && route == 0 && ok) {
-            /* no pixel of the reference's box may be covered */
-            ExactTri ex;
-            if (exact_tri(scene, v, ex))
-              for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
-                for (long long ii = ex.imin; ii <= ex.imax; ii++) {
-                  double w0, w1, w2;
-                  if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
-                }
+        if (status == 0) meta |= kMetaCulled;
+        if (status < 0) meta |= kMetaUndecided;
+        if (R.cover_count && status != 0) {
+          /* the reference's area is certainly not clamped to +-1e-16
+             (render.c:108-111): its weights are barycentric up to the -1e-8
+             slack, so every covered pixel centre lies in the triangle's extent */
+          const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
+          float errA;
+          const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
+          const bool unclamped = status > 0 && isfinite(A) && isfinite(exy) && fabsf(A) - errA > 1e-15f &&
+                                 exy < 1e-3f && zr < 1e-3f;
+          if (!unclamped) {
+            route = 1;
+          } else {
+            const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
+            const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
+            const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
+            long long imin, imax, jmin, jmax;
+            centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
+            centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+            route = imin <= imax && jmin <= jmax ? 2 : 0;
+            if (CHECK && route == 0 && ok) {
+              /* no pixel of the reference's box may be covered */
+              ExactTri ex;
+              if (exact_tri(scene, v, ex))
+                for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
+                  for (long long ii = ex.imin; ii <= ex.imax; ii++) {
+                    double w0, w1, w2;
+                    if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
+                  }
+            }
           }
         }
       }
+      tri.meta[t] = meta;
     }
-    tri.meta[t] = meta;
     if (R.cover_count) {
-      const unsigned long long ti = append_slot(R.tiny_count, route == 1);
-      const unsigned long long ci = append_slot(R.cover_count, route == 2);
+      unsigned long long ti, ci;
+      block_reserve2<256>(R.tiny_count, route == 1, R.cover_count, route == 2, ti, ci);
       if (route == 1 && ti < R.tiny_cap) R.tiny[ti] = (unsigned)t; /* overflow: the host re-runs the slab */
       if (route == 2) {
         float4* rec = tri.rec + 3 * ci; /* ci < the slab's triangle count */
@@ -862,6 +1039,24 @@ __device__ void tiny_triangle(const Geo& G, const SceneDev& s, long long t, cons
     }
 }
 
+/* candidates a k_cover thread keeps before appending */
+constexpr unsigned kCandBuf = 8;
+
+/* candidates (t, pix[u]) at slots [b, b + nb); those past the capacity are
+   dropped (the host sees the count and re-runs the slab) */
+__device__ __forceinline__ void write_candidates(const RasterDev& R, unsigned long long b, unsigned t, float dhi,
+                                                 const unsigned* pix, unsigned nb) {
+  for (unsigned u = 0; u < nb; u++) {
+    if (b + u >= R.cand_cap) break;
+    Candidate cd;
+    cd.t = t;
+    cd.pixel = pix[u];
+    cd.dhi = dhi;
+    cd.pad = 0;
+    R.cand[b + u] = cd;
+  }
+}
+
 template <bool CHECK>
 __global__ void __launch_bounds__(256, 4)
 k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
@@ -869,87 +1064,96 @@ k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ c
   const long long W = scene.width, H = scene.height;
   /* traverse front to back along z (the list is close to emission order,
      which follows z) so that near surfaces raise the floors early */
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-    const long long qq = scene.z_descending ? n - 1 - q : q;
-    const float4 r0 = __ldg(tri.rec + 3 * qq), r1 = __ldg(tri.rec + 3 * qq + 1), r2 = __ldg(tri.rec + 3 * qq + 2);
-    const long long t = (long long)__float_as_uint(r2.w);
-    const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
-    const float eps = r2.y, zr = r2.z;
-    /* inverse area (render.c:102-107) with its bound; k_emit listed only
-       triangles whose area is certainly not clamped and whose extent may
-       hold a pixel centre.  The per-pixel weight bounds are used when they
-       are tight enough to decide anything (rai < 0.5) */
-    const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
-    const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
-    const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
-    float errA;
-    const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
-    const float rai = errA / (fabsf(A) - errA) + 1.1f * kU32;
-    const bool weights_ok = rai < 0.5f;
-    const float ai = 1.f / A;
-    const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
-    const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
-    const float mb = eps + 1e-6f * (xext + yext) + 1e-12f;
-    long long imin, imax, jmin, jmax;
-    centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
-    centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
-    /* depth of any covered fragment: the harmonic mean of the vertex depths
-       with weights >= -1e-8 summing to 1, so within their range */
-    const float zmin = fminf(Z[0], fminf(Z[1], Z[2])), zmax = fmaxf(Z[0], fmaxf(Z[1], Z[2]));
-    const float m = zr + 4e-6f;
-    const float dlo = zmin - m * fabsf(zmin), dhi = zmax + m * fabsf(zmax);
-    ExactTri ex;
-    bool ex_ok = false;
-    if (CHECK) {
-      d3 wv[3];
-      exact_vertices(G, t, wv);
-      ex_ok = exact_tri(scene, wv, ex);
-      if (ex_ok) {
-        /* every covered pixel of the reference's box must lie in the tight range */
-        for (long long j = ex.jmin; j <= ex.jmax; j++)
-          for (long long i = ex.imin; i <= ex.imax; i++) {
-            double w0, w1, w2;
-            if (exact_weights(ex, i, j, R.xs, R.ys, w0, w1, w2)) {
-              if (i < imin || i > imax || j < jmin || j > jmax) atomicAdd(checks + 2, 1u);
-              const double d = exact_depth(ex, w0, w1, w2);
-              if (!(d <= (double)dhi && d >= (double)dlo)) atomicAdd(checks + 4, 1u);
+  /* every thread of a block runs the same iterations: a thread keeps up to
+     kCandBuf candidates of its triangle and the block appends them at once */
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+    const long long q = base + threadIdx.x;
+    unsigned pix[kCandBuf];
+    unsigned nb = 0, t32 = 0;
+    float dhi = 0.f;
+    if (q < n) {
+      const long long qq = scene.z_descending ? n - 1 - q : q;
+      const float4 r0 = __ldg(tri.rec + 3 * qq), r1 = __ldg(tri.rec + 3 * qq + 1), r2 = __ldg(tri.rec + 3 * qq + 2);
+      const long long t = (long long)__float_as_uint(r2.w);
+      const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
+      const float eps = r2.y, zr = r2.z;
+      /* inverse area (render.c:102-107) with its bound; k_emit listed only
+         triangles whose area is certainly not clamped and whose extent may
+         hold a pixel centre.  The per-pixel weight bounds are used when they
+         are tight enough to decide anything (rai < 0.5) */
+      const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
+      const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
+      const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
+      float errA;
+      const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
+      const float rai = errA / (fabsf(A) - errA) + 1.1f * kU32;
+      const bool weights_ok = rai < 0.5f;
+      const float ai = 1.f / A;
+      const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
+      const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
+      const float mb = eps + 1e-6f * (xext + yext) + 1e-12f;
+      long long imin, imax, jmin, jmax;
+      centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
+      centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+      /* depth of any covered fragment: the harmonic mean of the vertex depths
+         with weights >= -1e-8 summing to 1, so within their range */
+      const float zmin = fminf(Z[0], fminf(Z[1], Z[2])), zmax = fmaxf(Z[0], fmaxf(Z[1], Z[2]));
+      const float m = zr + 4e-6f;
+      const float dlo = zmin - m * fabsf(zmin);
+      dhi = zmax + m * fabsf(zmax);
+      t32 = (unsigned)t;
+      ExactTri ex;
+      bool ex_ok = false;
+      if (CHECK) {
+        d3 wv[3];
+        exact_vertices(G, t, wv);
+        ex_ok = exact_tri(scene, wv, ex);
+        if (ex_ok) {
+          /* every covered pixel of the reference's box must lie in the tight range */
+          for (long long j = ex.jmin; j <= ex.jmax; j++)
+            for (long long i = ex.imin; i <= ex.imax; i++) {
+              double w0, w1, w2;
+              if (exact_weights(ex, i, j, R.xs, R.ys, w0, w1, w2)) {
+                if (i < imin || i > imax || j < jmin || j > jmax) atomicAdd(checks + 2, 1u);
+                const double d = exact_depth(ex, w0, w1, w2);
+                if (!(d <= (double)dhi && d >= (double)dlo)) atomicAdd(checks + 4, 1u);
+              }
             }
+        }
+      }
+      for (long long j = jmin; j <= jmax; j++) {
+        const float py = R.ysf[j];
+        for (long long i = imin; i <= imax; i++) {
+          const float px = R.xsf[i];
+          const float ep = 0.5f * kU32;
+          float e0, e1, e2;
+          const float w0 = ai * edge_eval(E0, px, py, ep, eps, e0);
+          const float w1 = ai * edge_eval(E1, px, py, ep, eps, e1);
+          const float w2 = ai * edge_eval(E2, px, py, ep, eps, e2);
+          const float k = fabsf(ai) * (1.f + rai);
+          const float ew0 = 1.25f * (k * e0 + fabsf(w0) * (rai + kU32)) + 1e-30f;
+          const float ew1 = 1.25f * (k * e1 + fabsf(w1) * (rai + kU32)) + 1e-30f;
+          const float ew2 = 1.25f * (k * e2 + fabsf(w2) * (rai + kU32)) + 1e-30f;
+          const bool out = weights_ok && ((w0 + ew0 < kWOut) || (w1 + ew1 < kWOut) || (w2 + ew2 < kWOut));
+          const bool inside = weights_ok && !out && (w0 - ew0 > kWIn) && (w1 - ew1 > kWIn) && (w2 - ew2 > kWIn);
+          if (CHECK && ex_ok) {
+            double x0, x1, x2;
+            const bool cov = exact_weights(ex, i, j, R.xs, R.ys, x0, x1, x2);
+            if (cov && out) atomicAdd(checks + 2, 1u);     /* dropped a covered pixel */
+            if (!cov && inside) atomicAdd(checks + 3, 1u); /* called an uncovered pixel inside */
           }
-      }
-    }
-    for (long long j = jmin; j <= jmax; j++) {
-      const float py = R.ysf[j];
-      for (long long i = imin; i <= imax; i++) {
-        const float px = R.xsf[i];
-        const float ep = 0.5f * kU32;
-        float e0, e1, e2;
-        const float w0 = ai * edge_eval(E0, px, py, ep, eps, e0);
-        const float w1 = ai * edge_eval(E1, px, py, ep, eps, e1);
-        const float w2 = ai * edge_eval(E2, px, py, ep, eps, e2);
-        const float k = fabsf(ai) * (1.f + rai);
-        const float ew0 = 1.25f * (k * e0 + fabsf(w0) * (rai + kU32)) + 1e-30f;
-        const float ew1 = 1.25f * (k * e1 + fabsf(w1) * (rai + kU32)) + 1e-30f;
-        const float ew2 = 1.25f * (k * e2 + fabsf(w2) * (rai + kU32)) + 1e-30f;
-        const bool out = weights_ok && ((w0 + ew0 < kWOut) || (w1 + ew1 < kWOut) || (w2 + ew2 < kWOut));
-        const bool inside = weights_ok && !out && (w0 - ew0 > kWIn) && (w1 - ew1 > kWIn) && (w2 - ew2 > kWIn);
-        if (CHECK && ex_ok) {
-          double x0, x1, x2;
-          const bool cov = exact_weights(ex, i, j, R.xs, R.ys, x0, x1, x2);
-          if (cov && out) atomicAdd(checks + 2, 1u);     /* dropped a covered pixel */
-          if (!cov && inside) atomicAdd(checks + 3, 1u); /* called an uncovered pixel inside */
-        }
-        if (inside) atomicMax(R.zlo + j * W + i, f_key(dlo));
-        const unsigned long long idx = append_slot(R.cand_count, !out);
-        if (!out && idx < R.cand_cap) { /* overflow: the host re-runs the slab */
-          Candidate cd;
-          cd.t = (unsigned)t;
-          cd.pixel = (unsigned)(j * W + i);
-          cd.dhi = dhi;
-          cd.pad = 0;
-          R.cand[idx] = cd;
+          if (inside) atomicMax(R.zlo + j * W + i, f_key(dlo));
+          if (!out) {
+            if (nb == kCandBuf) { /* a large triangle: append the full buffer now */
+              write_candidates(R, atomicAdd(R.cand_count, (unsigned long long)kCandBuf), t32, dhi, pix, nb);
+              nb = 0;
+            }
+            pix[nb++] = (unsigned)(j * W + i);
+          }
         }
       }
     }
+    write_candidates(R, block_reserve<256>(R.cand_count, nb), t32, dhi, pix, nb);
   }
 }
 
@@ -972,12 +1176,17 @@ k_tiny(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsign
  */
 __global__ void __launch_bounds__(256) k_prune(RasterDev R) {
   const unsigned long long n = min(*R.cand_count, R.cand_cap);
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    const Candidate c = R.cand[q];
-    /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
-    const bool keep = f_key(c.dhi) >= R.zlo[c.pixel];
-    const unsigned long long w = append_slot(R.live_count, keep);
+  for (unsigned long long base = blockIdx.x * (unsigned long long)blockDim.x; base < n;
+       base += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long q = base + threadIdx.x;
+    Candidate c = {};
+    bool keep = false;
+    if (q < n) {
+      c = R.cand[q];
+      /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
+      keep = f_key(c.dhi) >= R.zlo[c.pixel];
+    }
+    const unsigned long long w = block_reserve<256>(R.live_count, keep);
     if (keep) R.live[w] = c; /* w < n <= cand_cap */
   }
 }
@@ -1018,12 +1227,12 @@ k_winners(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p,
           unsigned long long order_base) {
   const unsigned long long T_ = *total_p;
   const long long npx = scene.width * scene.height;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < npx; base += (long long)gridDim.x * blockDim.x) {
+    const long long p = base + threadIdx.x;
     long long t = 0, c = 0;
-    const bool won = slab_owner(G, R.canvas[p].lo, order_base, T_, t, c);
-    const unsigned long long w = append_slot(R.win_count, won);
-    if (!won) continue;
-    R.win[w] = make_uint2((unsigned)p, (unsigned)t);
+    const bool won = p < npx && slab_owner(G, R.canvas[p].lo, order_base, T_, t, c);
+    const unsigned long long w = block_reserve<256>(R.win_count, won);
+    if (won) R.win[w] = make_uint2((unsigned)p, (unsigned)t);
   }
 }
 
@@ -1036,8 +1245,7 @@ __global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R)
   const unsigned long long n = *R.win_count;
   const unsigned ncx = (unsigned)(G.F.nx - 1), ncy = (unsigned)(G.F.ny - 1);
   const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
-  /* every thread of a block runs the same number of iterations so that the
-     warp-wide appends below see all lanes */
+  /* every thread of a block runs the same number of iterations (block-wide appends) */
   for (unsigned long long it = blockIdx.x; it < iters; it += gridDim.x) {
     const unsigned long long q = it * blockDim.x + threadIdx.x;
     unsigned got[48];
@@ -1070,18 +1278,7 @@ __global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R)
         }
       }
     }
-    /* warp-level exclusive scan of the per-thread counts, one atomic per warp */
-    const int lane = threadIdx.x & 31;
-    unsigned incl = (unsigned)ng;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-      if (lane >= d) incl += y;
-    }
-    const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    unsigned long long base = 0;
-    if (lane == 31 && total) base = atomicAdd(R.need_count, (unsigned long long)total);
-    base = __shfl_sync(0xFFFFFFFFu, base, 31) + (incl - (unsigned)ng);
+    const unsigned long long base = block_reserve<256>(R.need_count, (unsigned)ng);
     for (int g = 0; g < ng; g++) R.need[base + g] = got[g];
   }
 }
@@ -1227,13 +1424,21 @@ void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts,
   else k_classify<double><<<grid, kClsX, 0, st>>>(F, S, counts);
 }
 
-void launch_scan(const unsigned char* counts, long long n, unsigned* offsets,
-                 unsigned long long* tile_state, unsigned* tile_counter, unsigned long long* total,
+void launch_scan(const unsigned char* counts, long long n, unsigned* offsets, unsigned* voffsets,
+                 unsigned long long* tile_state, unsigned* tile_counter, unsigned long long* totals,
                  unsigned* err, cudaStream_t st) {
   const long long tiles = (n + kScanTile) / kScanTile; /* covers position n too */
   cudaMemsetAsync(tile_state, 0, sizeof(unsigned long long) * tiles, st);
   cudaMemsetAsync(tile_counter, 0, sizeof(unsigned), st);
-  k_scan<<<(unsigned)tiles, kScanThreads, 0, st>>>(counts, n, offsets, tile_state, tile_counter, total, err);
+  k_scan<<<(unsigned)tiles, kScanThreads, 0, st>>>(counts, n, offsets, voffsets, tile_state, tile_counter, totals,
+                                                   err);
+}
+
+void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
+                     const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st) {
+  const unsigned blocks = (unsigned)((n + kVTile - 1) / kVTile);
+  if (F.is_f32) k_vertices<float><<<blocks, kVThreads, 0, st>>>(F, S, scene, codes, voffsets, n, V);
+  else k_vertices<double><<<blocks, kVThreads, 0, st>>>(F, S, scene, codes, voffsets, n, V);
 }
 
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st) {
@@ -1243,20 +1448,25 @@ void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_ce
 long long scan_tiles(long long n) { return (n + kScanTile) / kScanTile; }
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
-                 const unsigned char* codes, const unsigned* offsets, const unsigned* tri_cell,
-                 const unsigned long long* total, long long tri_bound, const TriDev& tri, const RasterDev& R,
-                 unsigned* checks, cudaStream_t st) {
+                 const unsigned char* codes, const unsigned* offsets,
+                 const unsigned* voffsets, const unsigned* tri_cell, const unsigned long long* total,
+                 long long tri_bound, const TriDev& tri, const RasterDev& R, const VertDev& V, unsigned* checks,
+                 cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
   if (checks) {
     if (F.is_f32)
-      k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
+      k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R, V,
+                                             checks);
     else
-      k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
+      k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R, V,
+                                              checks);
   } else {
     if (F.is_f32)
-      k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
+      k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R, V,
+                                              checks);
     else
-      k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, tri_cell, total, tri, R, checks);
+      k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R,
+                                               V, checks);
   }
 }
 

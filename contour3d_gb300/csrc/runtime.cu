@@ -353,7 +353,7 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
-  Buf zlo, xyf, cand, live, tiny, win, need, checks;
+  Buf zlo, xyf, cand, live, tiny, win, need, checks, voffsets, verts;
   HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
   cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
   bool filter_check = false;
@@ -578,8 +578,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
      the order: fragments carry their position in the reference's drawing
      sequence), except for inspection, which reports triangles in order. */
   const long long per_slice = ncx * ncy;
-  long long slab_slices = (long long)(c.slab_cells / (unsigned long long)per_slice) - 2;
+  const unsigned long long slab_cells = std::min<unsigned long long>(c.slab_cells, (unsigned long long)kMaxSlabCells);
+  long long slab_slices = (long long)(slab_cells / (unsigned long long)per_slice) - 2;
   if (slab_slices < 1) slab_slices = 1;
+  if (3 * per_slice > kMaxSlabCells) {
+    log_error("z-slices of %lld cells are too large (a slab of three slices must hold at most %lld cells)",
+              per_slice, kMaxSlabCells);
+    return 1;
+  }
   const bool want_all = sink != nullptr;
   const long long kr0 = want_all ? 0 : 1, kr1 = want_all ? ncz : ncz - 1;
   std::vector<long long> starts;
@@ -598,21 +604,22 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     S.krender1 = std::min(k1, ncz - 1);
     const long long ncell = S.nslices * per_slice;
     if (c.counts.ensure((size_t)ncell, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
+        c.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
         c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell), st) || c.scratch.ensure(128, st))
       return 1;
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = d_counter + 1;
-    unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2);
+    unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2); /* triangles, vertices */
     C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
     launch_classify(F, S, c.counts.as<unsigned char>(), st);
     if (c.stage_timing) cudaEventRecord(c.evs[1], st);
-    launch_scan(c.counts.as<unsigned char>(), ncell, c.offsets.as<unsigned>(), c.tile_state.as<unsigned long long>(),
-                d_counter, d_total, d_err, st);
+    launch_scan(c.counts.as<unsigned char>(), ncell, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(),
+                c.tile_state.as<unsigned long long>(), d_counter, d_total, d_err, st);
     if (c.stage_timing) cudaEventRecord(c.evs[2], st);
     c.stats.kernel_launches += 2;
     C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-    C3D_CUDA(cudaMemcpyAsync(h_total, d_total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     C3D_CUDA(cudaStreamSynchronize(st));
     if (c.stage_timing) {
       c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
@@ -622,11 +629,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       log_error("device scan did not complete (error flags 0x%x)", h_small[0]);
       return 1;
     }
-    const unsigned long long T = *h_total;
-    if (T >= (1ULL << 32)) {
-      log_error("slab holds %llu triangles; lower the slab size", T);
-      return 1;
-    }
+    const unsigned long long T = h_total[0], NV = h_total[1];
     c.stats.triangles += T;
     c.stats.slabs += 1;
     if (T == 0) continue;
@@ -645,8 +648,19 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     const TriDev tri = tri_layout(c.tri.p, cap, dbg);
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
+    /* the emit stage: triangle -> cell map, screen vertices, triangles */
+    if (c.stage_timing) cudaEventRecord(c.evs[3], st);
     launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
     c.stats.kernel_launches += 1;
+    VertDev VD = {};
+    if (!sink) {
+      /* the screen vertices of the slab's crossed edges: float4 records, then the aux floats */
+      if (c.verts.ensure(20 * (size_t)NV + 64, st)) return 1;
+      VD.pos = c.verts.as<float4>();
+      VD.aux = reinterpret_cast<float *>(VD.pos + NV);
+      launch_vertices(F, S, sd, c.counts.as<unsigned char>(), c.voffsets.as<unsigned>(), ncell, VD, st);
+      c.stats.kernel_launches += 1;
+    }
     const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
     Geo G;
     G.F = F;
@@ -659,7 +673,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     if (sink) {
       RasterDev none = {};
       launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
-                  c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, checks, st);
+                  c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
+                  st);
       launch_exact_all(G, d_total, (long long)T, tri, st);
       launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
       c.stats.kernel_launches += 3;
@@ -674,8 +689,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
       unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
       RasterDev RS = R;
-      unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 4);
-      unsigned long long *h_cnt = h_total + 1;
+      unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 6);
+      unsigned long long *h_cnt = h_total + 2;
       RS.win = c.win.as<uint2>();
       RS.win_count = counters + 2;
       RS.need = c.need.as<unsigned>();
@@ -695,9 +710,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         RS.tiny_count = counters + 1;
         C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
         C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
-        if (c.stage_timing) cudaEventRecord(c.evs[3], st);
         launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
-                    c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, checks, st);
+                    c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
+                    st);
         if (c.stage_timing) cudaEventRecord(c.evs[4], st);
         launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
         launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
@@ -1287,7 +1302,7 @@ extern "C" int contour3d_gb300_release(void) {
 
 static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need, &c.voffsets, &c.verts,
                  &c.checks};
   /* every call of the context has completed, so its buffers go back to the
      pool in order on its own stream */
@@ -1337,8 +1352,9 @@ struct Request {
   double device_ms = 0.;
 };
 
-/* working set of one request: slab codes/offsets, triangles (at an assumed
-   density of one triangle per cell), candidate lists and the z-buffer */
+/* working set of one request: slab codes/offsets, triangles and vertices (at
+   an assumed density of one triangle and half a vertex per cell), candidate
+   lists and the z-buffer */
 static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t slab_cells) {
   uint64_t peak = 0;
   for (size_t n = 0; n < fr->num_fields; n++) {
@@ -1347,7 +1363,7 @@ static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t sla
     const uint64_t per_slice = (uint64_t)(sz[0] - 1) * (sz[1] - 1);
     uint64_t cells = std::min<uint64_t>(per_slice * (sz[2] - 1), std::max<uint64_t>(slab_cells, per_slice * 3));
     /* candidates and their surviving copy: half a triangle's worth each */
-    const uint64_t bytes = cells * (1 + 4 + 4) + cells * (kTriBytes + 4 + 4) + cells * sizeof(Candidate);
+    const uint64_t bytes = cells * (1 + 4 + 4 + 4) + cells * (kTriBytes + 4 + 4 + 10) + cells * sizeof(Candidate);
     peak = std::max(peak, bytes);
   }
   const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];
