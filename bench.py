@@ -411,6 +411,11 @@ def main():
                 "stage_ms": stage_ms, "stage_gbs": {k: (stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9
                                                         if stage_ms[k] > 0 else None) for k in stage_ms},
                 "candidates_per_frame": int(prof.candidates),
+                "cover_triangles_per_frame": int(prof.cover_triangles),
+                "tiny_per_frame": int(prof.tiny),
+                "slivers_per_frame": int(prof.slivers),
+                "exact_fragments_per_frame": int(prof.exact_fragments),
+                "normals_per_frame": int(prof.normals),
                 "note": "emit is FP64-pipe bound on GB300 (~0.6 T FP64 ops/s)"}
 
     # ---- end to end through the drop-in C entry point ----

@@ -100,6 +100,9 @@ struct RasterDev {
   unsigned long long tiny_cap;
   unsigned long long* tiny_count;
   unsigned long long* cover_count; /* entries of TriDev::rec (at most the slab's triangles) */
+  float4* sliver_rec;       /* slivers, in the same records, from the top of TriDev::rec
+                               down: entry s at sliver_rec - 3 s (cover + sliver <= triangles) */
+  unsigned long long* sliver_count;
   Candidate* live;          /* candidates that can still win (capacity cand_cap) */
   unsigned long long* live_count;
   uint2* win;               /* (pixel, triangle) won by the current slab */
@@ -144,6 +147,8 @@ void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets
 void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                   const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned* checks,
                   cudaStream_t st);
+void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
+                   unsigned* checks, cudaStream_t st);
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
                  unsigned long long order_base, unsigned* checks, cudaStream_t st);
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st);

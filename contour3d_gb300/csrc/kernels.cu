@@ -185,7 +185,7 @@ __device__ __forceinline__ unsigned long long packed_count(unsigned short c) {
   return (unsigned long long)(c & 0xFF) | ((unsigned long long)(c >> 8) << 31);
 }
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 16;  /* cells per thread */
+constexpr int kScanItems = 32;  /* cells per thread */
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr unsigned long long kFlagAgg = 1ULL << 62;
 constexpr unsigned long long kFlagPrefix = 2ULL << 62;
@@ -199,7 +199,7 @@ constexpr unsigned long long kValueMask = (1ULL << 62) - 1;
  */
 constexpr unsigned long long kTriMask = (1ULL << 31) - 1;
 
-__global__ void __launch_bounds__(kScanThreads)
+__global__ void __launch_bounds__(kScanThreads, 3)
 k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restrict__ offsets,
        unsigned* __restrict__ voffsets, unsigned long long* __restrict__ tile_state,
        unsigned* __restrict__ tile_counter, unsigned long long* __restrict__ total,
@@ -214,23 +214,33 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
   const unsigned tile = s_tile;
   const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
 
-  unsigned short cnt[kScanItems]; /* triangles | vertices << 8 */
+  /* the thread's codes, 4 per word (a code past the end reads as 0, which
+     has no triangles and no vertices) */
+  unsigned wv[kScanItems / 4];
   unsigned long long sum = 0;
   if (base + kScanItems <= n) {
-    /* one 16-byte load (base is a multiple of 16, the buffer 256-byte aligned) */
-    const uint4 v = *reinterpret_cast<const uint4*>(counts + base);
-    const unsigned wv[4] = {v.x, v.y, v.z, v.w};
+    /* 16-byte loads (base is a multiple of 32, the buffer 256-byte aligned) */
 #pragma unroll
-    for (int q = 0; q < kScanItems; q++) cnt[q] = s_count[(wv[q >> 2] >> (8 * (q & 3))) & 255];
+    for (int h = 0; h < kScanItems / 16; h++) {
+      const uint4 v = *reinterpret_cast<const uint4*>(counts + base + 16 * h);
+      wv[4 * h] = v.x;
+      wv[4 * h + 1] = v.y;
+      wv[4 * h + 2] = v.z;
+      wv[4 * h + 3] = v.w;
+    }
   } else {
 #pragma unroll
-    for (int q = 0; q < kScanItems; q++) {
-      const long long c = base + q;
-      cnt[q] = c < n ? s_count[counts[c]] : 0;
+    for (int w = 0; w < kScanItems / 4; w++) {
+      unsigned x = 0;
+      for (int b = 0; b < 4; b++) {
+        const long long c = base + 4 * w + b;
+        if (c < n) x |= (unsigned)counts[c] << (8 * b);
+      }
+      wv[w] = x;
     }
   }
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) sum += packed_count(cnt[q]);
+  for (int q = 0; q < kScanItems; q++) sum += packed_count(s_count[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
   /* block-wide exclusive scan of the per-thread sums */
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long incl = sum;
@@ -313,37 +323,34 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
   }
   __syncthreads();
   unsigned long long run = s_excl + thread_excl;
-  unsigned out[kScanItems], vout[kScanItems];
-#pragma unroll
-  for (int q = 0; q < kScanItems; q++) {
-    out[q] = (unsigned)(run & kTriMask);
-    vout[q] = (unsigned)(run >> 31);
-    run += packed_count(cnt[q]);
-  }
   if (base + kScanItems <= n) {
-    /* four 16-byte stores per array (offsets + base is 64-byte aligned) */
+    /* 16-byte stores (offsets + base is 128-byte aligned) */
     uint4* o = reinterpret_cast<uint4*>(offsets + base);
     uint4* vo = reinterpret_cast<uint4*>(voffsets + base);
 #pragma unroll
-    for (int q = 0; q < kScanItems / 4; q++) {
-      o[q] = make_uint4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
-      vo[q] = make_uint4(vout[4 * q], vout[4 * q + 1], vout[4 * q + 2], vout[4 * q + 3]);
+    for (int w = 0; w < kScanItems / 4; w++) {
+      unsigned out[4], vout[4];
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        out[b] = (unsigned)(run & kTriMask);
+        vout[b] = (unsigned)(run >> 31);
+        run += packed_count(s_count[(wv[w] >> (8 * b)) & 255]);
+      }
+      o[w] = make_uint4(out[0], out[1], out[2], out[3]);
+      vo[w] = make_uint4(vout[0], vout[1], vout[2], vout[3]);
     }
   } else {
-#pragma unroll
     for (int q = 0; q < kScanItems; q++) {
       const long long c = base + q;
-      if (c <= n) { /* offsets[n] = totals */
-        offsets[c] = out[q];
-        voffsets[c] = vout[q];
+      if (c > n) break;
+      offsets[c] = (unsigned)(run & kTriMask); /* offsets[n] = totals */
+      voffsets[c] = (unsigned)(run >> 31);
+      if (c == n) {
+        total[0] = run & kTriMask;
+        total[1] = run >> 31;
       }
+      run += packed_count(s_count[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
     }
-  }
-  if (n >= base && n < base + kScanItems) {
-    unsigned long long tot = s_excl + thread_excl;
-    for (long long c = base; c < n; c++) tot += packed_count(cnt[c - base]);
-    total[0] = tot & kTriMask;
-    total[1] = tot >> 31;
   }
 }
 
@@ -774,6 +781,45 @@ __device__ __forceinline__ void block_reserve2(unsigned long long* count0, unsig
   __syncthreads();
 }
 
+/* the same for three lists of at most one item per thread */
+template <int kThreads>
+__device__ __forceinline__ void block_reserve3(unsigned long long* count0, bool n0, unsigned long long* count1,
+                                               bool n1, unsigned long long* count2, bool n2, unsigned long long& r0,
+                                               unsigned long long& r1, unsigned long long& r2) {
+  static_assert(kThreads < 1024, "10-bit fields");
+  __shared__ unsigned s_w[kThreads / 32];
+  __shared__ unsigned long long s_b[3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned x = (unsigned)n0 | ((unsigned)n1 << 10) | ((unsigned)n2 << 20);
+  unsigned incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned run = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; w++) {
+      const unsigned v = s_w[w];
+      s_w[w] = run;
+      run += v;
+    }
+    const unsigned t0 = run & 1023u, t1 = (run >> 10) & 1023u, t2 = run >> 20;
+    s_b[0] = t0 ? atomicAdd(count0, (unsigned long long)t0) : 0ULL;
+    s_b[1] = t1 ? atomicAdd(count1, (unsigned long long)t1) : 0ULL;
+    s_b[2] = t2 ? atomicAdd(count2, (unsigned long long)t2) : 0ULL;
+  }
+  __syncthreads();
+  const unsigned ex = s_w[warp] + incl - x;
+  r0 = s_b[0] + (ex & 1023u);
+  r1 = s_b[1] + ((ex >> 10) & 1023u);
+  r2 = s_b[2] + (ex >> 20);
+  __syncthreads();
+}
+
 template <int kThreads>
 __device__ __forceinline__ unsigned long long block_reserve(unsigned long long* count, unsigned n) {
   unsigned long long r0, r1;
@@ -858,10 +904,10 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
  * One thread per triangle: cube-edge ids and, for rendered triangles, the
  * FP32 screen vertices and their bounds (gathered from k_vertices), and the
  * raster path that settles the triangle: k_tiny (FP64 throughout) when the
- * bounds cannot decide its culling or whether its area is clamped, none when
- * no pixel centre can lie in it, k_cover otherwise -- only those are written
- * to the compact list k_cover reads.  Without raster lists (inspection) only
- * the ids are kept.
+ * bounds cannot decide its culling, k_sliver when its area may be clamped,
+ * none when no pixel centre can lie in it, k_cover otherwise -- only the
+ * k_cover and k_sliver triangles are written to the compact lists those
+ * read.  Without raster lists (inspection) only the ids are kept.
  */
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
@@ -880,7 +926,7 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
   /* every thread of a block runs the same iterations (block-wide appends) */
   for (long long base = blockIdx.x * (long long)blockDim.x; base < T_; base += (long long)gridDim.x * blockDim.x) {
     const long long t = base + threadIdx.x;
-    int route = 0; /* 0 no fragment, 1 k_tiny, 2 k_cover */
+    int route = 0; /* 0 no fragment, 1 k_tiny, 2 k_cover, 3 k_sliver */
     float X[3] = {0.f, 0.f, 0.f}, Y[3] = {0.f, 0.f, 0.f}, Z[3] = {0.f, 0.f, 0.f}, exy = 0.f, zr = 0.f;
     if (t < T_) {
       const unsigned c = tri_cell[t];
@@ -941,17 +987,20 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
         if (status == 0) meta |= kMetaCulled;
         if (status < 0) meta |= kMetaUndecided;
         if (R.cover_count && status != 0) {
-          /* the reference's area is certainly not clamped to +-1e-16
-             (render.c:108-111): its weights are barycentric up to the -1e-8
-             slack, so every covered pixel centre lies in the triangle's extent */
           const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
           float errA;
           const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
-          const bool unclamped = status > 0 && isfinite(A) && isfinite(exy) && fabsf(A) - errA > 1e-15f &&
-                                 exy < 1e-3f && zr < 1e-3f;
-          if (!unclamped) {
+          const bool decided = status > 0 && isfinite(A) && isfinite(exy) && exy < 1e-3f && zr < 1e-3f;
+          if (!decided) {
             route = 1;
+          } else if (!(fabsf(A) - errA > 1e-15f)) {
+            /* the area may be clamped to +-1e-16 (render.c:108-111): k_sliver
+               tests the reference's whole box */
+            route = 3;
           } else {
+            /* the reference's area is certainly not clamped: its weights are
+               barycentric up to the -1e-8 slack, so every covered pixel centre
+               lies in the triangle's extent */
             const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
             const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
             const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
@@ -975,11 +1024,13 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
       tri.meta[t] = meta;
     }
     if (R.cover_count) {
-      unsigned long long ti, ci;
-      block_reserve2<256>(R.tiny_count, route == 1, R.cover_count, route == 2, ti, ci);
+      unsigned long long ti, ci, si;
+      block_reserve3<256>(R.tiny_count, route == 1, R.cover_count, route == 2, R.sliver_count, route == 3, ti, ci,
+                          si);
       if (route == 1 && ti < R.tiny_cap) R.tiny[ti] = (unsigned)t; /* overflow: the host re-runs the slab */
-      if (route == 2) {
-        float4* rec = tri.rec + 3 * ci; /* ci < the slab's triangle count */
+      if (route >= 2) {
+        /* cover and sliver entries together number at most the slab's triangles */
+        float4* rec = route == 2 ? tri.rec + 3 * ci : R.sliver_rec - 3 * si;
         rec[0] = make_float4(X[0], Y[0], Z[0], X[1]);
         rec[1] = make_float4(Y[1], Z[1], X[2], Y[2]);
         rec[2] = make_float4(Z[2], exy, zr, __uint_as_float((unsigned)t));
@@ -988,12 +1039,27 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
   }
 }
 
+/*
+ * A pixel range holding the reference's bounding box (render.c:90-99):
+ * [(0.5 + lo) n - 1, (0.5 + hi) n + 1] truncated and clamped to [0, n - 1],
+ * for a triangle whose extent lies in [lo, hi].
+ */
+__device__ __forceinline__ void reference_box(float lo, float hi, long long n, long long& a, long long& b) {
+  const float fa = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + lo) * (float)n - 1.f));
+  const float fb = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + hi) * (float)n + 1.f));
+  /* one pixel of slack for the rounding of the FP32 products; NaN gives the whole axis */
+  const int ia = __float2int_rd(fa) - 1, ib = __float2int_ru(fb) + 1;
+  a = fa == fa ? max(0LL, (long long)ia) : 0;
+  b = fb == fb ? min(n - 1, (long long)ib) : n - 1;
+}
+
 /* ------------------------------------------------------------------ */
 /* triangles the single-precision filter cannot settle                 */
 /* ------------------------------------------------------------------ */
 /*
- * Triangles whose projected area is too small (or whose culling or bounds are
- * too uncertain) for the FP32 filter.  The reference's vertices, projection
+ * Triangles whose culling or bounds are too uncertain for the FP32 filter
+ * (a vertex near the camera plane or the edge of the view, or an edge whose
+ * value difference is near 1e-8).  The reference's vertices, projection
  * and area are computed once per triangle; when the area is not clamped
  * (|area| >= 1e-16, render.c:108-111) the covered pixel centres lie in the
  * triangle's extent, which holds no pixel centre for most of these
@@ -1058,13 +1124,13 @@ __device__ __forceinline__ void write_candidates(const RasterDev& R, unsigned lo
 }
 
 template <bool CHECK>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 3)
 k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
   const long long n = (long long)*R.cover_count;
   const long long W = scene.width, H = scene.height;
   /* traverse front to back along z (the list is close to emission order,
-     which follows z) so that near surfaces raise the floors early */
-  /* every thread of a block runs the same iterations: a thread keeps up to
+     which follows z) so that near surfaces raise the floors early.  Every
+     thread of a block runs the same iterations: a thread keeps up to
      kCandBuf candidates of its triangle and the block appends them at once */
   for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
     const long long q = base + threadIdx.x;
@@ -1089,12 +1155,12 @@ k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ c
       const float rai = errA / (fabsf(A) - errA) + 1.1f * kU32;
       const bool weights_ok = rai < 0.5f;
       const float ai = 1.f / A;
-      const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
-      const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
-      const float mb = eps + 1e-6f * (xext + yext) + 1e-12f;
+      const float xlo = fminf(X[0], fminf(X[1], X[2])), xhi = fmaxf(X[0], fmaxf(X[1], X[2]));
+      const float ylo = fminf(Y[0], fminf(Y[1], Y[2])), yhi = fmaxf(Y[0], fmaxf(Y[1], Y[2]));
+      const float mb = eps + 1e-6f * ((xhi - xlo) + (yhi - ylo)) + 1e-12f;
       long long imin, imax, jmin, jmax;
-      centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
-      centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+      centre_range(xlo - mb, xhi + mb, W, imin, imax);
+      centre_range(ylo - mb, yhi + mb, H, jmin, jmax);
       /* depth of any covered fragment: the harmonic mean of the vertex depths
          with weights >= -1e-8 summing to 1, so within their range */
       const float zmin = fminf(Z[0], fminf(Z[1], Z[2])), zmax = fmaxf(Z[0], fmaxf(Z[1], Z[2]));
@@ -1154,6 +1220,81 @@ k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ c
       }
     }
     write_candidates(R, block_reserve<256>(R.cand_count, nb), t32, dhi, pix, nb);
+  }
+}
+
+/*
+ * Slivers: triangles whose area may be clamped to +-1e-16 (render.c:108-111).
+ * A covered pixel then need not lie in the triangle's extent, so the
+ * reference's whole box is tested: with the clamped area a, w_k = e_k / a <
+ * -1e-8 holds certainly when s e_k < -tau for the sign s of a (|a| < tau /
+ * 1e-8), and the weights need not sum to 1.  A sliver whose pixels are all
+ * certainly outside draws nothing; any other goes whole to the exact path
+ * (k_tiny).  One thread per sliver, in a list of their own so that a warp's
+ * loops over these boxes stay converged.
+ */
+template <bool CHECK>
+__global__ void __launch_bounds__(256)
+k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
+  const long long n = (long long)*R.sliver_count;
+  const long long W = scene.width, H = scene.height;
+  for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+    const long long q = base + threadIdx.x;
+    bool to_tiny = false;
+    unsigned t32 = 0;
+    if (q < n) {
+      const float4* rec = R.sliver_rec - 3 * q;
+      const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+      t32 = __float_as_uint(r2.w);
+      const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w};
+      const float eps = r2.y;
+      const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
+      const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
+      const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
+      float errA;
+      const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
+      const float tau = 1.001e-8f * (fabsf(A) + errA + 1e-16f) + 1e-37f;
+      const bool may_pos = A + errA >= 0.f; /* an area of exactly 0 is clamped to +1e-16 */
+      const bool may_neg = A - errA < 0.f;
+      long long imin, imax, jmin, jmax;
+      reference_box(fminf(X[0], fminf(X[1], X[2])) - eps, fmaxf(X[0], fmaxf(X[1], X[2])) + eps, W, imin, imax);
+      reference_box(fminf(Y[0], fminf(Y[1], Y[2])) - eps, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + eps, H, jmin, jmax);
+      ExactTri ex;
+      bool ex_ok = false;
+      if (CHECK) {
+        d3 wv[3];
+        exact_vertices(G, (long long)t32, wv);
+        ex_ok = exact_tri(scene, wv, ex);
+        if (ex_ok)
+          for (long long j = ex.jmin; j <= ex.jmax; j++)
+            for (long long i = ex.imin; i <= ex.imax; i++) {
+              double w0, w1, w2;
+              if (exact_weights(ex, i, j, R.xs, R.ys, w0, w1, w2) && (i < imin || i > imax || j < jmin || j > jmax))
+                atomicAdd(checks + 2, 1u);
+            }
+      }
+      for (long long j = jmin; j <= jmax && (CHECK || !to_tiny); j++) {
+        const float py = R.ysf[j];
+        for (long long i = imin; i <= imax && (CHECK || !to_tiny); i++) {
+          const float px = R.xsf[i];
+          const float ep = 0.5f * kU32;
+          float e0, e1, e2;
+          const float f0 = edge_eval(E0, px, py, ep, eps, e0);
+          const float f1 = edge_eval(E1, px, py, ep, eps, e1);
+          const float f2 = edge_eval(E2, px, py, ep, eps, e2);
+          const bool pos_out = (f0 + e0 < -tau) || (f1 + e1 < -tau) || (f2 + e2 < -tau);
+          const bool neg_out = (f0 - e0 > tau) || (f1 - e1 > tau) || (f2 - e2 > tau);
+          const bool out = (!may_pos || pos_out) && (!may_neg || neg_out);
+          if (CHECK && ex_ok) {
+            double x0, x1, x2;
+            if (exact_weights(ex, i, j, R.xs, R.ys, x0, x1, x2) && out) atomicAdd(checks + 2, 1u);
+          }
+          to_tiny = to_tiny || !out;
+        }
+      }
+    }
+    const unsigned long long rt = block_reserve<256>(R.tiny_count, to_tiny);
+    if (to_tiny && rt < R.tiny_cap) R.tiny[rt] = t32; /* overflow: the host re-runs the slab */
   }
 }
 
@@ -1489,6 +1630,13 @@ void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long*
   const int g = grid_for(tri_bound, 256, 8);
   if (checks) k_cover<true><<<g, 256, 0, st>>>(G, scene, tri, R, checks);
   else k_cover<false><<<g, 256, 0, st>>>(G, scene, tri, R, checks);
+}
+
+void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
+                   unsigned* checks, cudaStream_t st) {
+  const int g = grid_for(sliver_bound, 256, 8);
+  if (checks) k_sliver<true><<<g, 256, 0, st>>>(G, scene, R, checks);
+  else k_sliver<false><<<g, 256, 0, st>>>(G, scene, R, checks);
 }
 
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,

@@ -468,8 +468,9 @@ struct FrameOut {
 };
 
 /* device counters of one slab's raster passes: candidates, tiny triangles,
-   won pixels, requested normals, listed triangles, surviving candidates */
-static const int kCounters = 6;
+   won pixels, requested normals, listed triangles, surviving candidates,
+   slivers */
+static const int kCounters = 7;
 
 /* bytes per triangle of the slab arrays (see TriDev) */
 static const size_t kTriBytes = 3 * sizeof(double) + 48 + 2 * sizeof(unsigned);
@@ -697,6 +698,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       RS.need_count = counters + 3;
       RS.cover_count = counters + 4;
       RS.live_count = counters + 5;
+      RS.sliver_count = counters + 6;
+      RS.sliver_rec = tri.rec + 3 * (cap - 1);
       for (int attempt = 0;; attempt++) {
         if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.live.ensure(sizeof(Candidate) * cand_want, st) ||
             c.tiny.ensure(sizeof(unsigned) * tiny_want, st))
@@ -715,6 +718,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
                     st);
         if (c.stage_timing) cudaEventRecord(c.evs[4], st);
         launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
+        launch_sliver(G, sd, (long long)T, RS, checks, st);
         launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
         if (c.stage_timing) cudaEventRecord(c.evs[5], st);
         launch_prune(RS, (long long)RS.cand_cap, st);
@@ -725,7 +729,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
            colours are the same values */
         launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
         if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-        c.stats.kernel_launches += 9;
+        c.stats.kernel_launches += 10;
         C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         C3D_CUDA(cudaStreamSynchronize(st));
         if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
@@ -743,6 +747,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.normals += h_cnt[3];
       c.stats.cover_triangles += h_cnt[4];
       c.stats.exact_fragments += h_cnt[5];
+      c.stats.slivers += h_cnt[6];
       if (c.stage_timing) {
         c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
         c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);

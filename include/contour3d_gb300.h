@@ -194,6 +194,7 @@ typedef struct {
   uint64_t filter_violations[5];
   uint64_t cover_triangles;   /* triangles whose extent may hold a pixel centre (FP32 filter input) */
   uint64_t exact_fragments;   /* candidates that reached the reference's FP64 arithmetic */
+  uint64_t slivers;           /* triangles whose area may be clamped (reference box tested in FP32) */
 } contour3d_gb300_stats_t;
 
 int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);
