@@ -43,6 +43,16 @@ CENTRE = (0.5, 0.5, 0.5)
 COLORS = ((0, 255, 255), (255, 255, 0))
 CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
 
+# DRAM bytes (read + write) per unit processed, from one ncu capture of each
+# kernel on the 256^3 case (profiles/*_fourier256_f64.md); the full-size
+# launch is scaled by its units
+TRAFFIC_PER_UNIT = {
+    "classify": (8.9, "cells"),     # k_classify: 147.8 MB for 16.6 M cells
+    "scan": (6.5, "cells"),         # k_scan: 107.6 MB for 16.6 M cells
+    "vertices": (39.7, "vertices"), # k_vertices: 260.1 MB for 6.55 M vertices (k_fill_tri_cell not included)
+    "emit": (54.6, "triangles"),    # k_emit: 715.8 MB for 13.1 M triangles
+}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -389,34 +399,47 @@ def main():
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     T = float(prof.triangles)
+    V = float(prof.vertices)
     nodes = float(nx * ny * nz)
     cells = float((nx - 1) * (ny - 1) * (nz - 1))
-    stage_ms = {"classify": prof.ms_classify, "scan": prof.ms_scan, "emit": prof.ms_emit,
-                "cover": prof.ms_cover, "exact": prof.ms_exact, "shade": prof.ms_shade}
-    C_ = float(prof.candidates)
-    # algorithmic bytes per frame (2 objects): see DESIGN.md "Kernels and rooflines"
+    listed = float(prof.cover_triangles + prof.slivers)
+    stage_ms = {"classify": prof.ms_classify, "scan": prof.ms_scan, "vertices": prof.ms_vertices,
+                "emit": prof.ms_emit, "cover": prof.ms_cover, "exact": prof.ms_exact, "normals": prof.ms_normals,
+                "shade": prof.ms_shade}
+    # algorithmic bytes per frame (both objects): the bytes each stage must move
+    # once -- inputs read once, outputs written once, cached re-reads not counted
     stage_bytes = {
         "classify": 2 * (nodes * 8 + cells * 1),
-        "scan": 2 * cells * (1 + 4),
-        "emit": T * (4 + 4 + 8 * 8 + 72 + 24 + 4 + 44),
-        "cover": T * (4 + 44 + 4) + C_ * 16,
-        "exact": C_ * (16 + 4 + 72),
-        "shade": WIDTH * HEIGHT * 16 * 2,
+        "scan": 2 * cells * (1 + 4 + 4),
+        "vertices": 2 * cells * (4 + 1 + 4) + T * 4 + V * (2 * 8 + 20),
+        "emit": T * (4 + 4) + 2 * cells * (4 + 1 + 4) + V * 20 + listed * 48 + float(prof.tiny) * 4,
+        "cover": listed * 48 + float(prof.candidates) * 16,
+        "exact": float(prof.candidates) * (16 + 4) + float(prof.exact_fragments) * 16,
+        "normals": WIDTH * HEIGHT * 16 * 2 + float(prof.normals) * (4 + 24),
+        "shade": float(prof.winners) * (8 + 16) + float(prof.normals) * 24,
     }
     dom = max(stage_ms, key=lambda k: stage_ms[k])
     achieved = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9 if stage_ms[dom] > 0 else 0.0
+    # DRAM bytes per unit of the dominant kernels, from the ncu captures in
+    # profiles/ (256^3 case, scaled by the units processed)
+    traffic = None
+    if dom in TRAFFIC_PER_UNIT:
+        per_unit, unit_name = TRAFFIC_PER_UNIT[dom]
+        units = {"triangles": T, "cells": 2 * cells, "vertices": V}[unit_name]
+        traffic = per_unit * units
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"
-                if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"
+                if "hbm_gbs" in peaks else "fallback 6800 GB/s (of fallback)",
                 "stage_ms": stage_ms, "stage_gbs": {k: (stage_bytes[k] / (stage_ms[k] / 1000.0) / 1e9
                                                         if stage_ms[k] > 0 else None) for k in stage_ms},
+                "triangles_per_frame": int(prof.triangles),
+                "vertices_per_frame": int(prof.vertices),
                 "candidates_per_frame": int(prof.candidates),
                 "cover_triangles_per_frame": int(prof.cover_triangles),
                 "tiny_per_frame": int(prof.tiny),
                 "slivers_per_frame": int(prof.slivers),
                 "exact_fragments_per_frame": int(prof.exact_fragments),
-                "normals_per_frame": int(prof.normals),
-                "note": "emit is FP64-pipe bound on GB300 (~0.6 T FP64 ops/s)"}
+                "normals_per_frame": int(prof.normals)}
 
     # ---- end to end through the drop-in C entry point ----
     e2e = None

@@ -154,9 +154,10 @@ void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, cons
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st);
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
                   unsigned long long order_base, cudaStream_t st);
+/* winners, normal requests, weighted normals; `between` (optional) is recorded before the colour pass */
 void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                     const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
-                    cudaStream_t st);
+                    cudaEvent_t between, cudaStream_t st);
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, cudaStream_t st);
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,

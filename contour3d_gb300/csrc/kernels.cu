@@ -1657,12 +1657,13 @@ void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, con
 
 void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                     const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
-                    cudaStream_t st) {
+                    cudaEvent_t between, cudaStream_t st) {
   (void)tri_bound;
   const long long npx = scene.width * scene.height;
   k_winners<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, total, tri, R, order_base);
   k_request<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, tri, R);
   k_wn<<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
+  if (between) cudaEventRecord(between, st);
   k_shade<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, tri, R, rgb);
 }
 

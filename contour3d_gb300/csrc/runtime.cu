@@ -358,7 +358,7 @@ struct Ctx {
   cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
   bool filter_check = false;
   HostBuf h_small, h_rgb, h_slots;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[8] = {};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[11] = {};
   bool stage_timing = false;
   unsigned long long slab_cells = 1ULL << 27;
   contour3d_gb300_stats_t stats = {};
@@ -649,7 +649,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     const TriDev tri = tri_layout(c.tri.p, cap, dbg);
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
-    /* the emit stage: triangle -> cell map, screen vertices, triangles */
+    /* the vertex stage: triangle -> cell map, screen vertices */
     if (c.stage_timing) cudaEventRecord(c.evs[3], st);
     launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
     c.stats.kernel_launches += 1;
@@ -661,7 +661,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       VD.aux = reinterpret_cast<float *>(VD.pos + NV);
       launch_vertices(F, S, sd, c.counts.as<unsigned char>(), c.voffsets.as<unsigned>(), ncell, VD, st);
       c.stats.kernel_launches += 1;
+      c.stats.vertices += NV;
     }
+    if (c.stage_timing) cudaEventRecord(c.evs[8], st);
     const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
     Geo G;
     G.F = F;
@@ -713,6 +715,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         RS.tiny_count = counters + 1;
         C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
         C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
+        if (c.stage_timing) cudaEventRecord(c.evs[9], st);
         launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
                     c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
                     st);
@@ -727,7 +730,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* shading runs before the overflow check: when a list overflowed, the
            whole stage runs again, and the repeated z-buffer maxima and
            colours are the same values */
-        launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, st);
+        launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, c.stage_timing ? c.evs[10] : nullptr,
+                       st);
         if (c.stage_timing) cudaEventRecord(c.evs[7], st);
         c.stats.kernel_launches += 10;
         C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -749,10 +753,12 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.exact_fragments += h_cnt[5];
       c.stats.slivers += h_cnt[6];
       if (c.stage_timing) {
-        c.stats.ms_emit += elapsed(c.evs[3], c.evs[4]);
+        c.stats.ms_vertices += elapsed(c.evs[3], c.evs[8]);
+        c.stats.ms_emit += elapsed(c.evs[9], c.evs[4]);
         c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);
         c.stats.ms_exact += elapsed(c.evs[5], c.evs[6]);
-        c.stats.ms_shade += elapsed(c.evs[6], c.evs[7]);
+        c.stats.ms_normals += elapsed(c.evs[6], c.evs[10]);
+        c.stats.ms_shade += elapsed(c.evs[10], c.evs[7]);
       }
     }
     if (sink) {

@@ -26,7 +26,8 @@ class Stats(C.Structure):
                 ("ms_total", C.c_double), ("ms_classify", C.c_double), ("ms_scan", C.c_double),
                 ("ms_emit", C.c_double), ("ms_cover", C.c_double), ("ms_exact", C.c_double),
                 ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5),
-                ("cover_triangles", C.c_uint64), ("exact_fragments", C.c_uint64), ("slivers", C.c_uint64)]
+                ("cover_triangles", C.c_uint64), ("exact_fragments", C.c_uint64), ("slivers", C.c_uint64),
+                ("vertices", C.c_uint64), ("ms_vertices", C.c_double), ("ms_normals", C.c_double)]
 
 
 class Field(C.Structure):

@@ -195,6 +195,10 @@ typedef struct {
   uint64_t cover_triangles;   /* triangles whose extent may hold a pixel centre (FP32 filter input) */
   uint64_t exact_fragments;   /* candidates that reached the reference's FP64 arithmetic */
   uint64_t slivers;           /* triangles whose area may be clamped (reference box tested in FP32) */
+  uint64_t vertices;          /* crossed edges whose screen position was computed (all slabs) */
+  double ms_vertices;         /* stage timing: triangle -> cell map and screen vertices */
+  double ms_normals;          /* stage timing: won pixels, normal requests, weighted normals
+                                 (ms_shade is then the colour pass alone) */
 } contour3d_gb300_stats_t;
 
 int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);
