@@ -343,3 +343,27 @@ extern "C" int contour3d_gb300_extend(const sdecomp_info_t *info, const contour3
   if (!ext) return 0;
   return c3d::extend_block(info, obj, b, ext);
 }
+
+extern "C" int contour3d_gb300_reduce_nearest(const sdecomp_info_t *info, double *depth, uint8_t *rgb,
+                                              size_t num_pixels) {
+  if (!info || (num_pixels && (!depth || !rgb))) {
+    c3d::log_error("reduce_nearest: missing argument");
+    return 1;
+  }
+  std::vector<c3d::PixelRec> px(num_pixels);
+  for (size_t p = 0; p < num_pixels; p++) {
+    px[p] = {};
+    px[p].depth = depth[p];
+    px[p].r = rgb[3 * p];
+    px[p].g = rgb[3 * p + 1];
+    px[p].b = rgb[3 * p + 2];
+  }
+  if (c3d::reduce_nearest(info, px.data(), num_pixels)) return 1;
+  for (size_t p = 0; p < num_pixels; p++) {
+    depth[p] = px[p].depth;
+    rgb[3 * p] = px[p].r;
+    rgb[3 * p + 1] = px[p].g;
+    rgb[3 * p + 2] = px[p].b;
+  }
+  return 0;
+}

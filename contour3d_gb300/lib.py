@@ -89,6 +89,17 @@ class FramePack:
         self.frame = fr
 
 # every symbol declared in include/contour3d.h and include/contour3d_gb300.h
+class SdecompTable(C.Structure):
+    """The `sdecomp` function table of include/sdecomp.h (function pointers)."""
+    _fields_ = [(n, C.c_void_p) for n in ("construct", "destruct", "get_comm_cart", "get_comm_rank",
+                                         "get_nprocs", "get_myrank", "get_neighbours",
+                                         "get_pencil_mysize", "get_pencil_offset")]
+
+
+def sdecomp_table(L: "Library") -> SdecompTable:
+    return SdecompTable.in_dll(L.lib, "sdecomp")
+
+
 EXPORTS = [
     "contour3d_execute", "contour3d_gb300_identity", "contour3d_gb300_declare_identity",
     "contour3d_gb300_render", "contour3d_gb300_render_device", "contour3d_gb300_last_stats",
@@ -97,7 +108,7 @@ EXPORTS = [
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
     "contour3d_gb300_cell_offsets_noalloc", "contour3d_gb300_render_batch", "contour3d_gb300_server_create",
     "contour3d_gb300_server_submit", "contour3d_gb300_server_wait", "contour3d_gb300_server_destroy",
-    "contour3d_gb300_device_bytes",
+    "contour3d_gb300_device_bytes", "contour3d_gb300_reduce_nearest",
     "c3d_comm_world", "sdecomp",
 ]
 

@@ -263,6 +263,15 @@ int contour3d_gb300_install_transport(const contour3d_gb300_transport_t *transpo
 int contour3d_gb300_extend(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj,
                            size_t sizes[3], size_t offsets[3], double *ext);
 
+/*
+ * The nearest-depth reduction of per-rank images to rank 0 (output.c:32-88,
+ * reduction_func output.c:10-30: keep the pixel with the larger depth), over
+ * the installed transport.  `depth` holds num_pixels doubles, `rgb`
+ * 3 * num_pixels bytes.  Collective over the decomposition; on rank 0 the
+ * arrays receive the result, on the other ranks they are left partial.
+ */
+int contour3d_gb300_reduce_nearest(const sdecomp_info_t *info, double *depth, uint8_t *rgb, size_t num_pixels);
+
 /* release every device and pinned-host buffer the library holds */
 int contour3d_gb300_release(void);
 

@@ -55,14 +55,9 @@ def test_missing_library_fails_loudly(tmp_path):
         lib.Library(str(tmp_path / "nope.so"))
 
 
-class SdecompT(C.Structure):
-    _fields_ = [(n, C.c_void_p) for n in ("construct", "destruct", "get_comm_cart", "get_comm_rank",
-                                         "get_nprocs", "get_myrank", "get_neighbours",
-                                         "get_pencil_mysize", "get_pencil_offset")]
-
-
 def _sdecomp(L):
-    return SdecompT.in_dll(L.lib, "sdecomp")
+    from contour3d_gb300 import lib
+    return lib.sdecomp_table(L)
 
 
 def test_single_process_decomposition(built):
