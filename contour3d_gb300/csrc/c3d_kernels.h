@@ -121,12 +121,14 @@ struct LineSegDev {
 
 /* device error flags */
 constexpr unsigned kErrScanTimeout = 1u;
+constexpr unsigned kErrClassifyTimeout = 2u;
 
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
                   const unsigned char nb_count[19]);
 long long scan_tiles(long long n);
 
-void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, cudaStream_t st);
+/* TMA-staged planes when the field's layout allows it; `err` receives kErrClassifyTimeout */
+void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, unsigned* err, cudaStream_t st);
 /* cells per slab for which the packed triangle and vertex sums of k_scan stay below 2^31 */
 constexpr long long kMaxSlabCells = 178956970;
 

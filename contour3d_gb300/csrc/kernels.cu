@@ -40,6 +40,8 @@
  *   k_resolve          src/contour3d/output.c:10-30, 113-123
  *   slab / interior    src/contour3d/contour/main.c:38-112
  */
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cuda/atomic>
@@ -124,6 +126,18 @@ __device__ __forceinline__ unsigned char node_above<float>(const FieldDev& F, co
   return (F.thr_f_ok && v == v && f_key(v) >= F.thr_f_key) ? 1 : 0;
 }
 
+/* the same test on a value already loaded */
+template <typename T>
+__device__ __forceinline__ unsigned char node_above_value(const FieldDev& F, T v);
+template <>
+__device__ __forceinline__ unsigned char node_above_value<double>(const FieldDev& F, double v) {
+  return (!F.thr_nan && !d_isnan(v) && d_key(v) > F.thr_key) ? 1 : 0;
+}
+template <>
+__device__ __forceinline__ unsigned char node_above_value<float>(const FieldDev& F, float v) {
+  return (F.thr_f_ok && v == v && f_key(v) >= F.thr_f_key) ? 1 : 0;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ codes) {
   __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
@@ -162,6 +176,133 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
       }
     }
     __syncthreads();
+  }
+}
+
+/*
+ * k_classify_tma: the same codes, with the node planes staged by TMA.  A
+ * block owns kClsX x kClsY cells of kClsZ slices; each of its node planes
+ * (kTmaBoxX x (kClsY + 1) nodes, x from the tile start, so the copy starts on
+ * a 16-byte boundary) is one cp.async.bulk.tensor copy into a ring of
+ * kTmaStages shared-memory buffers, each completed on its own mbarrier, so
+ * kTmaStages planes are in flight while the block turns the current one into
+ * node bits and the previous pair into cell codes.  Copies beyond the field
+ * read zeros (those nodes belong to no cell of the tile).  Every wait is
+ * bounded: on a timeout the block records kErrClassifyTimeout, waits (again
+ * bounded) for its own copies in flight, and returns.
+ */
+constexpr int kTmaStages = 4;
+constexpr int kTmaWaitLimit = 1 << 22;
+
+template <typename T>
+struct TmaBox {
+  static constexpr int kX = sizeof(T) == 8 ? 130 : 132; /* >= kClsX + 1, a multiple of 16 bytes */
+  static constexpr int kBytes = kX * (kClsY + 1) * (int)sizeof(T);
+  static constexpr int kStride = (kBytes + 127) / 128 * 128; /* every stage starts on 128 bytes */
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+/* bounded wait; false when the limit was reached */
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < kTmaWaitLimit; it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kClsX)
+k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, unsigned char* __restrict__ codes,
+               unsigned* __restrict__ err) {
+  constexpr int BX = TmaBox<T>::kX;
+  __shared__ __align__(128) unsigned char stage_mem[kTmaStages][TmaBox<T>::kStride];
+  auto vals_of = [&](int st) { return reinterpret_cast<const T(*)[BX]>(&stage_mem[st][0]); };
+  __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+  __shared__ __align__(8) unsigned long long bar[kTmaStages];
+  __shared__ int s_fail;
+  const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
+  const int i0 = blockIdx.x * kClsX, j0 = blockIdx.y * kClsY;
+  const long long k0 = (long long)blockIdx.z * kClsZ;
+  const long long k1 = min(k0 + kClsZ, S.nslices);
+  const int nplanes = (int)(k1 - k0) + 1; /* node planes k0 .. k1 of the slab */
+  if (threadIdx.x == 0) {
+    s_fail = 0;
+    for (int q = 0; q < kTmaStages; q++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[q])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int p) { /* thread 0: plane p into stage p % kTmaStages */
+    const int st = p % kTmaStages;
+    const unsigned b = smem_u32(&bar[st]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(TmaBox<T>::kBytes)
+                 : "memory");
+    const int z = (int)(S.kfirst + k0 + p);
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(&stage_mem[st][0])), "l"(&tmap), "r"(i0), "r"(j0), "r"(z), "r"(b)
+        : "memory");
+  };
+  if (threadIdx.x == 0)
+    for (int p = 0; p < kTmaStages && p < nplanes; p++) issue(p);
+  const int tx = threadIdx.x;
+  for (int p = 0; p < nplanes; p++) {
+    const int st = p % kTmaStages;
+    if (!mbar_wait(smem_u32(&bar[st]), (unsigned)((p / kTmaStages) & 1))) s_fail = 1;
+    __syncthreads();
+    if (s_fail) {
+      /* give up: record it, let the copies in flight land (bounded), return */
+      if (threadIdx.x == 0) {
+        atomicOr(err, kErrClassifyTimeout);
+        for (int q = p; q < nplanes && q < p + kTmaStages; q++)
+          mbar_wait(smem_u32(&bar[q % kTmaStages]), (unsigned)((q / kTmaStages) & 1));
+      }
+      return;
+    }
+    /* node bits of plane p */
+    unsigned char(*bp)[kClsX + 1] = bits[p & 1];
+    const T(*vp)[BX] = vals_of(st);
+    for (int q = tx; q < (kClsY + 1) * (kClsX + 1); q += kClsX) {
+      const int jj = q / (kClsX + 1), ii = q - jj * (kClsX + 1);
+      bp[jj][ii] = node_above_value<T>(F, vp[jj][ii]);
+    }
+    __syncthreads();
+    /* stage st is free again: refill it with plane p + kTmaStages */
+    if (threadIdx.x == 0 && p + kTmaStages < nplanes) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(p + kTmaStages);
+    }
+    if (p >= 1) {
+      /* cell codes of slice k0 + p - 1 from the bit planes p - 1 and p */
+      const unsigned char(*b0)[kClsX + 1] = bits[(p - 1) & 1];
+      const unsigned char(*b1)[kClsX + 1] = bits[p & 1];
+      const unsigned i = (unsigned)(i0 + tx);
+      if (i < ncx) {
+        const long long kl = k0 + p - 1;
+#pragma unroll
+        for (int jj = 0; jj < kClsY; jj++) {
+          const unsigned j = (unsigned)(j0 + jj);
+          if (j >= ncy) break;
+          const unsigned code = b0[jj][tx] | (b0[jj][tx + 1] << 1) | (b0[jj + 1][tx] << 2) |
+                                (b0[jj + 1][tx + 1] << 3) | (b1[jj][tx] << 4) | (b1[jj][tx + 1] << 5) |
+                                (b1[jj + 1][tx] << 6) | (b1[jj + 1][tx + 1] << 7);
+          codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
+        }
+      }
+    }
+    __syncthreads(); /* bits[(p + 1) & 1] is rewritten next */
   }
 }
 
@@ -1557,10 +1698,55 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
   return 0;
 }
 
-void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, cudaStream_t st) {
+/* cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link) */
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+/* the field as a 3-D tensor map with one node plane of a classify tile per box,
+   or false when TMA cannot address it (row or plane pitch not a multiple of 16
+   bytes, base not 16-byte aligned, more than 2^31 nodes along an axis) */
+static bool classify_tensor_map(const FieldDev& F, CUtensorMap* map) {
+  const size_t es = F.is_f32 ? 4 : 8;
+  if (((uintptr_t)F.data & 15) || (F.nx * es) % 16 || F.nx >= (1LL << 31) || F.ny >= (1LL << 31) ||
+      F.nz >= (1LL << 31))
+    return false;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)F.nx, (cuuint64_t)F.ny, (cuuint64_t)F.nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)(F.nx * es), (cuuint64_t)(F.nx * F.ny * es)};
+  const cuuint32_t box[3] = {(cuuint32_t)(F.is_f32 ? TmaBox<float>::kX : TmaBox<double>::kX), kClsY + 1, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = enc(map, F.is_f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                         const_cast<void*>(F.data), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, unsigned* err, cudaStream_t st) {
   /* `counts` receives the cell codes; k_scan turns them into counts */
   const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
                   (unsigned)((S.nslices + kClsZ - 1) / kClsZ));
+  CUtensorMap map;
+  if (classify_tensor_map(F, &map)) {
+    if (F.is_f32) k_classify_tma<float><<<grid, kClsX, 0, st>>>(map, F, S, counts, err);
+    else k_classify_tma<double><<<grid, kClsX, 0, st>>>(map, F, S, counts, err);
+    return;
+  }
   if (F.is_f32) k_classify<float><<<grid, kClsX, 0, st>>>(F, S, counts);
   else k_classify<double><<<grid, kClsX, 0, st>>>(F, S, counts);
 }

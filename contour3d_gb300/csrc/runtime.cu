@@ -613,7 +613,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2); /* triangles, vertices */
     C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
-    launch_classify(F, S, c.counts.as<unsigned char>(), st);
+    launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
     if (c.stage_timing) cudaEventRecord(c.evs[1], st);
     launch_scan(c.counts.as<unsigned char>(), ncell, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(),
                 c.tile_state.as<unsigned long long>(), d_counter, d_total, d_err, st);
@@ -627,7 +627,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
     }
     if (h_small[0]) {
-      log_error("device scan did not complete (error flags 0x%x)", h_small[0]);
+      log_error("device classification or scan did not complete (error flags 0x%x)", h_small[0]);
       return 1;
     }
     const unsigned long long T = h_total[0], NV = h_total[1];
@@ -1282,11 +1282,20 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   F.thr_nan = std::isnan(obj->threshold) ? 1 : 0;
   set_float_threshold(F);
   SlabDev S = {0, nz - 1, 0, 0};
-  launch_classify(F, S, c.counts.as<unsigned char>(), st);
+  if (c.scratch.ensure(128, st)) return -1;
+  unsigned *d_err = c.scratch.as<unsigned>();
+  if (cudaMemsetAsync(d_err, 0, sizeof(unsigned), st) != cudaSuccess) return -1;
+  launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
   const size_t ncell = (size_t)((nx - 1) * (ny - 1) * (nz - 1));
   std::vector<uint8_t> h(ncell);
+  unsigned herr = 0;
   if (cudaMemcpyAsync(h.data(), c.counts.p, ncell, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+  if (cudaMemcpyAsync(&herr, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  if (herr) {
+    log_error("device classification did not complete (error flags 0x%x)", herr);
+    return -1;
+  }
   std::vector<unsigned long long> lut;
   unsigned char count_of[256];
   build_tables(lut, count_of);
