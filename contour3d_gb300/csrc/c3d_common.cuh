@@ -110,20 +110,33 @@ __device__ __forceinline__ void cas128(Slot* addr, unsigned long long cmp_lo, un
       : "memory");
 }
 
-/* raise the slot to max(slot, (hi, lo)); `seen_hi` from a plain read of slot.hi */
-__device__ __forceinline__ void slot_max(Slot* s, unsigned long long hi, unsigned long long lo) {
+/* raise the slot to max(slot, (hi, lo)); true when this call stored (hi, lo) */
+__device__ __forceinline__ bool slot_max(Slot* s, unsigned long long hi, unsigned long long lo) {
   unsigned long long cur_lo = 0, cur_hi = 0;
   /* an atomic read: a CAS whose compare value is never present (hi = 0 is
      the key of NaN-space and is never stored) returns the live contents */
   cas128(s, 0ULL, 0ULL, 0ULL, 0ULL, cur_lo, cur_hi);
+  /* every failed CAS means another thread stored a larger value: bounded */
   for (int guard = 0; guard < 1 << 20; guard++) {
-    if (hi < cur_hi || (hi == cur_hi && lo <= cur_lo)) return;
+    if (hi < cur_hi || (hi == cur_hi && lo <= cur_lo)) return false;
     unsigned long long o_lo, o_hi;
     cas128(s, cur_lo, cur_hi, lo, hi, o_lo, o_hi);
-    if (o_lo == cur_lo && o_hi == cur_hi) return;
+    if (o_lo == cur_lo && o_hi == cur_hi) return true;
     cur_lo = o_lo;
     cur_hi = o_hi;
   }
+  return false;
+}
+
+/* one 16-byte word stored atomically (atom.exch.b128) */
+__device__ __forceinline__ void store128_atomic(void* addr, unsigned long long lo, unsigned long long hi) {
+  asm volatile(
+      "{\n\t.reg .b128 d, b;\n\t"
+      "mov.b128 b, {%0, %1};\n\t"
+      "atom.global.exch.b128 d, [%2], b;\n\t}"
+      :
+      : "l"(lo), "l"(hi), "l"(addr)
+      : "memory");
 }
 
 /* ------------------------------------------------------------------ */

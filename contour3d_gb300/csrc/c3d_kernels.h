@@ -105,6 +105,11 @@ struct RasterDev {
   unsigned long long* sliver_count;
   Candidate* live;          /* candidates that can still win (capacity cand_cap) */
   unsigned long long* live_count;
+  /* per pixel, the exact weights of the fragment that last won its CAS: three
+     16-byte words (weight k, tag), tag = order << 24 | epoch, each stored
+     atomically; shading uses them when all three tags name the final owner */
+  ulonglong2* winfo;
+  unsigned long long epoch; /* 1 .. 2^24 - 1, per frame */
   uint2* win;               /* (pixel, triangle) won by the current slab */
   unsigned long long* win_count;
   unsigned* need;           /* triangles whose weighted normal shading needs */

@@ -824,6 +824,16 @@ __device__ __forceinline__ unsigned long long order_of(const Geo& G, unsigned lo
   return order_base + 12ULL * G.tri_cell[t] + ((G.meta[t] >> kMetaRankShift) & 15);
 }
 
+/* the winning fragment's exact weights for shading (see RasterDev::winfo) */
+__device__ __forceinline__ void keep_weights(const RasterDev& R, long long p, unsigned long long order, double w0,
+                                             double w1, double w2) {
+  const unsigned long long tag = (order << 24) | R.epoch;
+  ulonglong2* w = R.winfo + 3 * p;
+  store128_atomic(w, (unsigned long long)__double_as_longlong(w0), tag);
+  store128_atomic(w + 1, (unsigned long long)__double_as_longlong(w1), tag);
+  store128_atomic(w + 2, (unsigned long long)__double_as_longlong(w2), tag);
+}
+
 /* one fragment through the reference's test and the (depth, order) z-buffer */
 __device__ __forceinline__ void exact_fragment(const Geo& G, const SceneDev& s, long long t, long long i, long long j,
                                                const RasterDev& R, unsigned long long order_base) {
@@ -834,7 +844,9 @@ __device__ __forceinline__ void exact_fragment(const Geo& G, const SceneDev& s, 
   double w0, w1, w2;
   if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) return;
   const double dist0 = exact_depth(x, w0, w1, w2);
-  slot_max(R.canvas + j * s.width + i, depth_key(dist0), order_of(G, order_base, t) << 24);
+  const unsigned long long order = order_of(G, order_base, t);
+  const long long p = j * s.width + i;
+  if (slot_max(R.canvas + p, depth_key(dist0), order << 24)) keep_weights(R, p, order, w0, w1, w2);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1242,7 +1254,9 @@ __device__ void tiny_triangle(const Geo& G, const SceneDev& s, long long t, cons
     for (long long i = imin; i <= imax; i++) {
       double w0, w1, w2;
       if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) continue;
-      slot_max(R.canvas + j * s.width + i, depth_key(exact_depth(x, w0, w1, w2)), order << 24);
+      const long long p = j * s.width + i;
+      if (slot_max(R.canvas + p, depth_key(exact_depth(x, w0, w1, w2)), order << 24))
+        keep_weights(R, p, order, w0, w1, w2);
     }
 }
 
@@ -1593,12 +1607,23 @@ k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
        q += (unsigned long long)gridDim.x * blockDim.x) {
     const uint2 wp = R.win[q];
     const long long p = wp.x, t = wp.y;
-    d3 v[3];
-    exact_vertices(G, t, v);
-    ExactTri x;
+    const unsigned long long lo = R.canvas[p].lo;
+    const unsigned long long tag = ((lo >> 24) << 24) | R.epoch;
+    const ulonglong2 k0 = R.winfo[3 * p], k1 = R.winfo[3 * p + 1], k2 = R.winfo[3 * p + 2];
     double w0, w1, w2;
-    const long long pj = (unsigned)p / (unsigned)W, pi = p - pj * W;
-    if (!exact_tri(scene, v, x) || !exact_weights(x, pi, pj, R.xs, R.ys, w0, w1, w2)) continue;
+    if (k0.y == tag && k1.y == tag && k2.y == tag) {
+      /* the weights the winning fragment was drawn with */
+      w0 = __longlong_as_double((long long)k0.x);
+      w1 = __longlong_as_double((long long)k1.x);
+      w2 = __longlong_as_double((long long)k2.x);
+    } else {
+      /* a stale or mixed record: the same arithmetic again (render.c:102-133) */
+      d3 v[3];
+      exact_vertices(G, t, v);
+      ExactTri x;
+      const long long pj = (unsigned)p / (unsigned)W, pi = p - pj * W;
+      if (!exact_tri(scene, v, x) || !exact_weights(x, pi, pj, R.xs, R.ys, w0, w1, w2)) continue;
+    }
     const unsigned meta = tri.meta[t];
     const long long c = G.tri_cell[t];
     const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, G.offsets, tri);
@@ -1609,7 +1634,6 @@ k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
     const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
     const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
     const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
-    const unsigned long long lo = R.canvas[p].lo;
     R.canvas[p].lo = (lo & ~0xFFFFFFULL) | (r8 << 16) | (g8 << 8) | b8;
   }
 }

@@ -353,7 +353,8 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
-  Buf zlo, xyf, cand, live, tiny, win, need, checks, voffsets, verts;
+  Buf zlo, xyf, cand, live, tiny, win, need, checks, voffsets, verts, winfo;
+  unsigned long long epoch = 0; /* frame counter for the winner-weight tags (1 .. 2^24 - 1) */
   HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
   cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
   bool filter_check = false;
@@ -866,6 +867,14 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   if (c.xy.ensure(sizeof(double) * (W + H), st) || c.xyf.ensure(sizeof(float) * (W + H), st) ||
       c.canvas.ensure(sizeof(Slot) * npx, st) || c.zlo.ensure(sizeof(unsigned) * npx, st) || c.checks.ensure(64, st))
     return 1;
+  /* per-pixel winner weights: tags carry a frame epoch, so the buffer is
+     cleared only when it is new or the epoch wraps */
+  const void *winfo_before = c.winfo.p;
+  if (c.winfo.ensure(3 * sizeof(ulonglong2) * npx, st)) return 1;
+  if (c.winfo.p != winfo_before || ++c.epoch >= (1ULL << 24)) {
+    C3D_CUDA(cudaMemsetAsync(c.winfo.p, 0, c.winfo.cap, st));
+    c.epoch = 1;
+  }
   C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy, sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
   C3D_CUDA(cudaMemcpyAsync(c.xyf.p, xyf, sizeof(float) * (W + H), cudaMemcpyHostToDevice, st));
   C3D_CUDA(cudaEventRecord(c.ev_staged, st));
@@ -873,6 +882,8 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   RasterDev R = {};
   R.canvas = c.canvas.as<Slot>();
   R.zlo = c.zlo.as<unsigned>();
+  R.winfo = c.winfo.as<ulonglong2>();
+  R.epoch = c.epoch;
   R.xs = c.xy.as<double>();
   R.ys = R.xs + W;
   R.xsf = c.xyf.as<float>();
@@ -1322,7 +1333,7 @@ extern "C" int contour3d_gb300_release(void) {
 
 static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need, &c.voffsets, &c.verts,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need, &c.voffsets, &c.verts, &c.winfo,
                  &c.checks};
   /* every call of the context has completed, so its buffers go back to the
      pool in order on its own stream */
@@ -1374,7 +1385,7 @@ struct Request {
 
 /* working set of one request: slab codes/offsets, triangles and vertices (at
    an assumed density of one triangle and half a vertex per cell), candidate
-   lists and the z-buffer */
+   lists, the z-buffer and the per-pixel winner weights */
 static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t slab_cells) {
   uint64_t peak = 0;
   for (size_t n = 0; n < fr->num_fields; n++) {
@@ -1387,7 +1398,7 @@ static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t sla
     peak = std::max(peak, bytes);
   }
   const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];
-  return peak + px * (sizeof(Slot) + 4 + 8 + 3) + (1ULL << 24);
+  return peak + px * (sizeof(Slot) + 4 + 8 + 3 + 48) + (1ULL << 24);
 }
 
 }  // namespace c3d
