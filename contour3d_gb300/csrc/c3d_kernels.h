@@ -12,6 +12,16 @@ struct Slot;
 struct SceneDev;
 struct RasterDev;
 
+/*
+ * Unsigned division by an invariant d >= 1 (Granlund and Montgomery, 1994):
+ * with l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1,
+ * n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0), t = mulhi(m, n),
+ * for every 32-bit n.
+ */
+struct FastDiv {
+  unsigned m, s1, s2;
+};
+
 /* a scalar field on the device: an extended pencil block, x fastest */
 struct FieldDev {
   const void* data;
@@ -30,7 +40,19 @@ struct FieldDev {
   /* float fields: threshold < (double)v  <=>  f_key(v) >= thr_f_key (when thr_f_ok) */
   unsigned thr_f_key;
   int thr_f_ok;
+  FastDiv div_cx, div_cy;   /* division by the cells per row (nx - 1) and per column (ny - 1) */
 };
+
+/* the constants of FastDiv for d >= 1 */
+inline FastDiv make_fast_div(unsigned d) {
+  unsigned l = 0;
+  while (l < 32 && (1ULL << l) < d) l++;
+  FastDiv f;
+  f.m = (unsigned)((((1ULL << 32) * ((1ULL << l) - d)) / d) + 1);
+  f.s1 = l < 1 ? l : 1;
+  f.s2 = l > 1 ? l - 1 : 0;
+  return f;
+}
 
 /* one z-slab of cells: slices [kfirst, kfirst + nslices), rendered [krender0, krender1) */
 struct SlabDev {
@@ -60,11 +82,17 @@ constexpr unsigned kMetaCulled = 1u << 16;
 constexpr unsigned kMetaRankShift = 17;
 constexpr unsigned kMetaUndecided = 1u << 21;
 
-/* FP32 screen vertices of a slab's crossed edges (k_vertices) */
+/* FP32 screen vertices of a slab's crossed edges (k_vertices), 16 bytes each:
+   X, Y, Z and two bfloat16 rounded up (a bound only loosens): the bound on
+   |X, Y - the reference's value| (high half), and the relative depth bound,
+   or -1 (projection fails), -2 (undecided) (low half) */
 struct VertDev {
-  float4* pos; /* X, Y, Z, bound on |X, Y - the reference's value| */
-  float* aux;  /* relative depth bound, or -1 (projection fails), -2 (undecided) */
+  float4* pos;
 };
+
+/* triangle -> cell map entries: cell | rank << 28 (slabs hold fewer than 2^28 cells) */
+constexpr unsigned kTcCellMask = 0x0FFFFFFFu;
+constexpr unsigned kTcRankShift = 28;
 
 /* what the exact path needs to rebuild a triangle from the field */
 struct Geo {
@@ -125,21 +153,24 @@ struct LineSegDev {
 };
 
 /* device error flags */
-constexpr unsigned kErrScanTimeout = 1u;
 constexpr unsigned kErrClassifyTimeout = 2u;
 
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
                   const unsigned char nb_count[19]);
-long long scan_tiles(long long n);
 
 /* TMA-staged planes when the field's layout allows it; `err` receives kErrClassifyTimeout */
 void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, unsigned* err, cudaStream_t st);
 /* cells per slab for which the packed triangle and vertex sums of k_scan stay below 2^31 */
 constexpr long long kMaxSlabCells = 178956970;
 
-void launch_scan(const unsigned char* counts, long long n, unsigned* offsets, unsigned* voffsets,
-                 unsigned long long* tile_state, unsigned* tile_counter, unsigned long long* totals,
-                 unsigned* err, cudaStream_t st);
+/* segments of the scan over n cells */
+long long scan_segments(long long n);
+/* offsets[0..n], voffsets[0..n], totals = (triangles, vertices); the
+   triangle -> cell map too when the triangles fit tri_cap.  seg_sums and
+   seg_base hold scan_segments(n) entries each */
+void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
+                 unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
+                 unsigned* tri_cell, unsigned long long tri_cap, cudaStream_t st);
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);

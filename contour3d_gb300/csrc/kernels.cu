@@ -88,13 +88,57 @@ __device__ __forceinline__ unsigned cell_code(const FieldDev& F, long long i, lo
   return code;
 }
 
+__device__ __forceinline__ unsigned fast_div(unsigned n, const FastDiv& d) {
+  const unsigned t = __umulhi(d.m, n);
+  return (t + ((n - t) >> d.s1)) >> d.s2;
+}
+
 /* cell (i, j, k-in-slab) of a slab-local linear cell index; 32-bit arithmetic */
-__device__ __forceinline__ void cell_ijk(unsigned c, unsigned ncx, unsigned ncy, unsigned& i, unsigned& j,
-                                         unsigned& kl) {
-  const unsigned r = c / ncx;
+__device__ __forceinline__ void cell_ijk(const FieldDev& F, unsigned c, unsigned& i, unsigned& j, unsigned& kl) {
+  const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
+  const unsigned r = fast_div(c, F.div_cx);
   i = c - r * ncx;
-  kl = r / ncy;
+  kl = fast_div(r, F.div_cy);
   j = r - kl * ncy;
+}
+
+/* ------------------------------------------------------------------ */
+/* counts per cell                                                     */
+/* ------------------------------------------------------------------ */
+/*
+ * Per cell, its triangle count and the number of its owned vertices (edges
+ * from its corner 0 that the iso-level crosses), packed as tri | vert << 31:
+ * every sum over a slab stays below 2^31 in both fields for slabs of at most
+ * kMaxSlabCells cells, so packed additions never carry.  The scan runs over
+ * segments of kScanTile cells: k_seg_reduce sums each segment, k_seg_scan
+ * turns the sums into segment offsets, and k_scan_write writes every cell's
+ * offsets from them -- no block waits on another.
+ *
+ * Vertices are owned by cells: cell c owns the crossed edges that start at
+ * its corner 0 and run to corner m = 1..7 (+x, +y, +x+y, +z, +x+z, +y+z,
+ * +x+y+z).  Every edge of the six-tetrahedra split joins corners a, b with
+ * a & b = a or b, so it starts at corner a & b of its cell and runs in
+ * direction a ^ b: it is the edge m = a ^ b owned by the cell at offset a & b.
+ */
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 32;  /* cells per thread */
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr unsigned long long kTriMask = (1ULL << 31) - 1;
+
+/* bit m - 1: the iso-level crosses edge m of the cell's corner 0 */
+__device__ __forceinline__ unsigned owned_edges(unsigned code) {
+  const unsigned flip = code ^ (0u - (code & 1u));
+  return (flip >> 1) & 0x7Fu;
+}
+
+/* triangles | vertices << 16 of every code, in shared memory */
+__device__ __forceinline__ void load_count_lut(unsigned* lut) {
+  for (int q = threadIdx.x; q < 256; q += blockDim.x)
+    lut[q] = (unsigned)c_code_count[q] | ((unsigned)__popc(owned_edges((unsigned)q)) << 16);
+}
+
+__device__ __forceinline__ unsigned long long packed_count(unsigned c) {
+  return (unsigned long long)(c & 0xFFFFu) | ((unsigned long long)(c >> 16) << 31);
 }
 
 /* ------------------------------------------------------------------ */
@@ -162,18 +206,17 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
     load_plane(nxt, S.kfirst + kl + 1);
     __syncthreads();
     const unsigned i = i0 + threadIdx.x;
-    if (i < ncx) {
-      const int tx = threadIdx.x;
+    const bool in_x = i < ncx;
+    const int tx = threadIdx.x;
 #pragma unroll
-      for (int jj = 0; jj < kClsY; jj++) {
-        const unsigned j = j0 + jj;
-        if (j >= ncy) break;
-        const unsigned code = bits[cur][jj][tx] | (bits[cur][jj][tx + 1] << 1) | (bits[cur][jj + 1][tx] << 2) |
-                              (bits[cur][jj + 1][tx + 1] << 3) | (bits[nxt][jj][tx] << 4) |
-                              (bits[nxt][jj][tx + 1] << 5) | (bits[nxt][jj + 1][tx] << 6) |
-                              (bits[nxt][jj + 1][tx + 1] << 7);
-        codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
-      }
+    for (int jj = 0; jj < kClsY; jj++) {
+      const unsigned j = j0 + jj;
+      if (j >= ncy) break; /* the same for the whole block */
+      const unsigned code = bits[cur][jj][tx] | (bits[cur][jj][tx + 1] << 1) | (bits[cur][jj + 1][tx] << 2) |
+                            (bits[cur][jj + 1][tx + 1] << 3) | (bits[nxt][jj][tx] << 4) |
+                            (bits[nxt][jj][tx + 1] << 5) | (bits[nxt][jj + 1][tx] << 6) |
+                            (bits[nxt][jj + 1][tx + 1] << 7);
+      if (in_x) codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
     }
     __syncthreads();
   }
@@ -289,17 +332,16 @@ k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, 
       const unsigned char(*b0)[kClsX + 1] = bits[(p - 1) & 1];
       const unsigned char(*b1)[kClsX + 1] = bits[p & 1];
       const unsigned i = (unsigned)(i0 + tx);
-      if (i < ncx) {
-        const long long kl = k0 + p - 1;
+      const bool in_x = i < ncx;
+      const long long kl = k0 + p - 1;
 #pragma unroll
-        for (int jj = 0; jj < kClsY; jj++) {
-          const unsigned j = (unsigned)(j0 + jj);
-          if (j >= ncy) break;
-          const unsigned code = b0[jj][tx] | (b0[jj][tx + 1] << 1) | (b0[jj + 1][tx] << 2) |
-                                (b0[jj + 1][tx + 1] << 3) | (b1[jj][tx] << 4) | (b1[jj][tx + 1] << 5) |
-                                (b1[jj + 1][tx] << 6) | (b1[jj + 1][tx + 1] << 7);
-          codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
-        }
+      for (int jj = 0; jj < kClsY; jj++) {
+        const unsigned j = (unsigned)(j0 + jj);
+        if (j >= ncy) break; /* the same for the whole block */
+        const unsigned code = b0[jj][tx] | (b0[jj][tx + 1] << 1) | (b0[jj + 1][tx] << 2) |
+                              (b0[jj + 1][tx + 1] << 3) | (b1[jj][tx] << 4) | (b1[jj][tx + 1] << 5) |
+                              (b1[jj + 1][tx] << 6) | (b1[jj + 1][tx + 1] << 7);
+        if (in_x) codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
       }
     }
     __syncthreads(); /* bits[(p + 1) & 1] is rewritten next */
@@ -307,63 +349,19 @@ k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, 
 }
 
 /* ------------------------------------------------------------------ */
-/* k_scan: single-pass decoupled look-back exclusive scan              */
+/* the scan: segment offsets, then every cell's offsets                 */
 /* ------------------------------------------------------------------ */
-/*
- * Vertices are owned by cells: cell c owns the crossed edges that start at
- * its corner 0 and run to corner m = 1..7 (+x, +y, +x+y, +z, +x+z, +y+z,
- * +x+y+z).  Every edge of the six-tetrahedra split joins corners a, b with
- * a & b = a or b, so it starts at corner a & b of its cell and runs in
- * direction a ^ b: it is the edge m = a ^ b owned by the cell at offset a & b.
- * Bit m - 1 of the result: the iso-level crosses edge m of the cell's corner 0.
- */
-__device__ __forceinline__ unsigned owned_edges(unsigned code) {
-  const unsigned flip = code ^ (0u - (code & 1u));
-  return (flip >> 1) & 0x7Fu;
-}
+constexpr int kSegScanThreads = 1024;
 
-__device__ __forceinline__ unsigned long long packed_count(unsigned short c) {
-  return (unsigned long long)(c & 0xFF) | ((unsigned long long)(c >> 8) << 31);
-}
-constexpr int kScanThreads = 256;
-constexpr int kScanItems = 32;  /* cells per thread */
-constexpr int kScanTile = kScanThreads * kScanItems;
-constexpr unsigned long long kFlagAgg = 1ULL << 62;
-constexpr unsigned long long kFlagPrefix = 2ULL << 62;
-constexpr unsigned long long kValueMask = (1ULL << 62) - 1;
-
-/*
- * Both scans in one: per cell, its triangle count and the number of its
- * owned vertices (edges from its corner 0 that the iso-level crosses), packed
- * as tri | vert << 31 -- every sum stays below 2^31 in both fields for slabs
- * of at most kMaxSlabCells cells, so the packed additions never carry.
- */
-constexpr unsigned long long kTriMask = (1ULL << 31) - 1;
-
-__global__ void __launch_bounds__(kScanThreads, 3)
-k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restrict__ offsets,
-       unsigned* __restrict__ voffsets, unsigned long long* __restrict__ tile_state,
-       unsigned* __restrict__ tile_counter, unsigned long long* __restrict__ total,
-       unsigned* __restrict__ err) {
-  __shared__ unsigned s_tile;
-  __shared__ unsigned long long s_warp[kScanThreads / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ unsigned short s_count[256];
-  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
-  s_count[threadIdx.x] = (unsigned short)(c_code_count[threadIdx.x] | (__popc(owned_edges(threadIdx.x)) << 8));
-  __syncthreads();
-  const unsigned tile = s_tile;
-  const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
-
-  /* the thread's codes, 4 per word (a code past the end reads as 0, which
-     has no triangles and no vertices) */
-  unsigned wv[kScanItems / 4];
-  unsigned long long sum = 0;
+/* the thread's kScanItems codes, 4 per word (a code past the end reads as 0:
+   no triangles, no vertices) */
+__device__ __forceinline__ void load_scan_codes(const unsigned char* __restrict__ codes, long long base, long long n,
+                                                unsigned wv[kScanItems / 4]) {
   if (base + kScanItems <= n) {
     /* 16-byte loads (base is a multiple of 32, the buffer 256-byte aligned) */
 #pragma unroll
     for (int h = 0; h < kScanItems / 16; h++) {
-      const uint4 v = *reinterpret_cast<const uint4*>(counts + base + 16 * h);
+      const uint4 v = *reinterpret_cast<const uint4*>(codes + base + 16 * h);
       wv[4 * h] = v.x;
       wv[4 * h + 1] = v.y;
       wv[4 * h + 2] = v.z;
@@ -375,14 +373,48 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
       unsigned x = 0;
       for (int b = 0; b < 4; b++) {
         const long long c = base + 4 * w + b;
-        if (c < n) x |= (unsigned)counts[c] << (8 * b);
+        if (c < n) x |= (unsigned)codes[c] << (8 * b);
       }
       wv[w] = x;
     }
   }
+}
+
+/* one block per segment: its packed total */
+__global__ void __launch_bounds__(kScanThreads)
+k_seg_reduce(const unsigned char* __restrict__ codes, long long n, unsigned long long* __restrict__ seg_sums) {
+  __shared__ unsigned s_cnt[256];
+  __shared__ unsigned long long s_warp[kScanThreads / 32];
+  load_count_lut(s_cnt);
+  __syncthreads();
+  unsigned wv[kScanItems / 4];
+  load_scan_codes(codes, (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems, n, wv);
+  unsigned long long sum = 0;
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) sum += packed_count(s_count[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
-  /* block-wide exclusive scan of the per-thread sums */
+  for (int q = 0; q < kScanItems; q++) sum += packed_count(s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; w++) t += s_warp[w];
+    seg_sums[blockIdx.x] = t;
+  }
+}
+
+/* exclusive scan of the segment totals (one block); writes the slab totals
+   (triangles, vertices) and the end entries offsets[n], voffsets[n] */
+__global__ void __launch_bounds__(kSegScanThreads)
+k_seg_scan(const unsigned long long* __restrict__ seg_sums, long long nseg, unsigned long long* __restrict__ seg_base,
+           long long n, unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
+           unsigned long long* __restrict__ totals) {
+  __shared__ unsigned long long s_warp[kSegScanThreads / 32];
+  const long long per = (nseg + kSegScanThreads - 1) / kSegScanThreads;
+  const long long a = min(nseg, (long long)threadIdx.x * per), b = min(nseg, a + per);
+  unsigned long long sum = 0;
+  for (long long q = a; q < b; q++) sum += seg_sums[q];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long incl = sum;
 #pragma unroll
@@ -393,115 +425,142 @@ k_scan(const unsigned char* __restrict__ counts, long long n, unsigned* __restri
   if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    unsigned long long w = lane < kScanThreads / 32 ? s_warp[lane] : 0;
+    unsigned long long w = s_warp[lane];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, d);
       if (lane >= d) w += y;
     }
-    if (lane < kScanThreads / 32) s_warp[lane] = w;  /* inclusive per warp */
+    s_warp[lane] = w; /* inclusive per warp */
   }
   __syncthreads();
-  const unsigned long long block_agg = s_warp[kScanThreads / 32 - 1];
-  const unsigned long long thread_excl = (warp ? s_warp[warp - 1] : 0) + incl - sum;
+  unsigned long long run = (warp ? s_warp[warp - 1] : 0ULL) + incl - sum;
+  for (long long q = a; q < b; q++) {
+    seg_base[q] = run;
+    run += seg_sums[q];
+  }
+  if (threadIdx.x == kSegScanThreads - 1) {
+    const unsigned long long tot = s_warp[kSegScanThreads / 32 - 1];
+    totals[0] = tot & kTriMask;
+    totals[1] = tot >> 31;
+    offsets[n] = (unsigned)(tot & kTriMask);
+    voffsets[n] = (unsigned)(tot >> 31);
+  }
+}
 
-  /* publish and look back (warp 0) */
+/*
+ * One block per segment: every cell's triangle and vertex offsets (the
+ * segment's base plus a block-wide exclusive scan), and, when the slab's
+ * triangles fit `tri_cap`, the triangle -> cell map.
+ */
+constexpr int kFillList = 12288; /* triangles of a segment listed in shared memory */
+constexpr int kStagePitch = 33;  /* words per staged row: conflict-free transposes */
+constexpr size_t kScanWriteSmem =
+    sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch + sizeof(unsigned short) * kFillList;
+
+/*
+ * One block per segment: every cell's triangle and vertex offsets (the
+ * segment's base plus a block-wide exclusive scan), and, when the slab's
+ * triangles fit `tri_cap`, the triangle -> cell map.  A thread owns 32
+ * consecutive cells; its offsets go through a per-warp shared-memory stage
+ * (rows of kStagePitch words) so that every global store of a warp covers
+ * 128 contiguous bytes.  The map goes through a shared list of the segment's
+ * triangles when they fit it (then coalesced), else directly.
+ */
+__global__ void __launch_bounds__(kScanThreads, 3)
+k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigned long long* __restrict__ seg_base,
+             unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
+             const unsigned long long* __restrict__ totals, unsigned* __restrict__ tri_cell,
+             unsigned long long tri_cap) {
+  extern __shared__ __align__(16) unsigned char scan_smem[];
+  __shared__ unsigned long long s_warp[kScanThreads / 32];
+  __shared__ unsigned s_cnt[256];
+  unsigned* stage_all = reinterpret_cast<unsigned*>(scan_smem);
+  unsigned short* s_list = /* segment-local cell of each of the segment's triangles */
+      reinterpret_cast<unsigned short*>(scan_smem + sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch);
+  load_count_lut(s_cnt);
+  __syncthreads();
+  const long long c0 = (long long)blockIdx.x * kScanTile;
+  const long long base = c0 + (long long)threadIdx.x * kScanItems;
+  unsigned wv[kScanItems / 4];
+  load_scan_codes(codes, base, n, wv);
+  unsigned long long sum = 0;
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) sum += packed_count(s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long incl = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
   if (warp == 0) {
-    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> my(tile_state[tile]);
-    if (lane == 0)
-      my.store((tile == 0 ? kFlagPrefix : kFlagAgg) | block_agg, cuda::memory_order_release);
-    unsigned long long excl = 0;
-    if (tile > 0) {
-      long long pred = (long long)tile - 1;
-      int spins = 0;
-      bool done = false;
-      while (!done) {
-        /* each lane inspects one predecessor, nearest first */
-        const long long p = pred - lane;
-        unsigned long long st = kFlagPrefix;  /* beyond tile 0: neutral */
-        if (p >= 0) {
-          cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> ps(tile_state[p]);
-          st = ps.load(cuda::memory_order_acquire);
-        }
-        const unsigned invalid = __ballot_sync(0xFFFFFFFFu, p >= 0 && (st >> 62) == 0);
-        const unsigned prefix = __ballot_sync(0xFFFFFFFFu, p >= 0 && (st >> 62) == 2);
-        /* lanes up to (excluding) the first invalid one are usable; stop at the first prefix */
-        const unsigned first_invalid = invalid ? __ffs(invalid) - 1 : 32;
-        const unsigned first_prefix = prefix ? __ffs(prefix) - 1 : 32;
-        if (first_prefix < first_invalid) {
-          unsigned long long v = (lane <= (int)first_prefix && p >= 0) ? (st & kValueMask) : 0;
+    unsigned long long w = lane < kScanThreads / 32 ? s_warp[lane] : 0ULL;
 #pragma unroll
-          for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
-          excl += v;
-          done = true;
-        } else if (first_invalid == 32) {
-          /* 32 aggregates and no prefix yet: consume them and move on */
-          unsigned long long v = p >= 0 ? (st & kValueMask) : 0;
-#pragma unroll
-          for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
-          excl += v;
-          pred -= 32;
-          if (pred < 0) done = true;
-        } else if (first_invalid > 0) {
-          /* consume the aggregates before the first invalid predecessor */
-          unsigned long long v = (lane < (int)first_invalid && p >= 0) ? (st & kValueMask) : 0;
-#pragma unroll
-          for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
-          excl += v;
-          pred -= first_invalid;
-        } else {
-          if (++spins > (1 << 22)) {
-            if (lane == 0) atomicOr(err, kErrScanTimeout);
-            done = true;
-          } else {
-            __nanosleep(64);
-          }
-        }
-      }
-      if (lane == 0) my.store(kFlagPrefix | ((excl + block_agg) & kValueMask), cuda::memory_order_release);
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, d);
+      if (lane >= d) w += y;
     }
-    if (lane == 0) s_excl = excl;
+    if (lane < kScanThreads / 32) s_warp[lane] = w;
   }
   __syncthreads();
-  unsigned long long run = s_excl + thread_excl;
-  if (base + kScanItems <= n) {
-    /* 16-byte stores (offsets + base is 128-byte aligned) */
-    uint4* o = reinterpret_cast<uint4*>(offsets + base);
-    uint4* vo = reinterpret_cast<uint4*>(voffsets + base);
+  const unsigned long long seg0 = seg_base[blockIdx.x];
+  const unsigned long long first = seg0 + (warp ? s_warp[warp - 1] : 0ULL) + incl - sum;
+  const unsigned seg_tris = (unsigned)(s_warp[kScanThreads / 32 - 1] & kTriMask);
+  const unsigned ta = (unsigned)(seg0 & kTriMask);
+  const bool fill = totals[0] <= tri_cap;
+  const bool listed = fill && seg_tris <= (unsigned)kFillList;
+  const bool direct = fill && !listed;
+  unsigned* stage = stage_all + warp * 32 * kStagePitch;
+  const long long wbase = c0 + (long long)warp * 32 * kScanItems; /* the warp's first cell */
+  for (int half = 1; half >= 0; half--) {
+    /* half 1: vertex offsets; half 0: triangle offsets and the map (the
+       staged triangle offsets stay for the copy of the map below) */
+    unsigned long long run = first;
 #pragma unroll
-    for (int w = 0; w < kScanItems / 4; w++) {
-      unsigned out[4], vout[4];
-#pragma unroll
-      for (int b = 0; b < 4; b++) {
-        out[b] = (unsigned)(run & kTriMask);
-        vout[b] = (unsigned)(run >> 31);
-        run += packed_count(s_count[(wv[w] >> (8 * b)) & 255]);
-      }
-      o[w] = make_uint4(out[0], out[1], out[2], out[3]);
-      vo[w] = make_uint4(vout[0], vout[1], vout[2], vout[3]);
-    }
-  } else {
     for (int q = 0; q < kScanItems; q++) {
-      const long long c = base + q;
-      if (c > n) break;
-      offsets[c] = (unsigned)(run & kTriMask); /* offsets[n] = totals */
-      voffsets[c] = (unsigned)(run >> 31);
-      if (c == n) {
-        total[0] = run & kTriMask;
-        total[1] = run >> 31;
+      const unsigned cnt = s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
+      const unsigned t0 = (unsigned)(run & kTriMask);
+      stage[kStagePitch * lane + q] = half == 0 ? t0 : (unsigned)(run >> 31);
+      if (half == 0 && (listed || direct) && base + q < n) {
+        const unsigned nt = cnt & 0xFFFFu;
+        if (listed)
+          for (unsigned r = 0; r < nt; r++) s_list[t0 - ta + r] = (unsigned short)(base + q - c0);
+        else
+          for (unsigned r = 0; r < nt; r++) tri_cell[t0 + r] = (unsigned)(base + q) | (r << kTcRankShift);
       }
-      run += packed_count(s_count[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
+      run += packed_count(cnt);
+    }
+    __syncwarp();
+    unsigned* dst = half == 0 ? offsets : voffsets;
+#pragma unroll 4
+    for (int k = 0; k < 32; k++) {
+      const long long c = wbase + 32 * k + lane;
+      if (c < n) dst[c] = stage[kStagePitch * k + lane];
+    }
+    __syncwarp();
+  }
+  if (listed) {
+    __syncthreads();
+    for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) {
+      /* the cell's first triangle from the staged offsets: cell l of the
+         segment was lane (l % 1024) / 32, item l % 32 of warp l / 1024 */
+      const unsigned l = s_list[e];
+      const unsigned t0 = stage_all[(l >> 10) * 32 * kStagePitch + kStagePitch * ((l >> 5) & 31) + (l & 31)];
+      tri_cell[ta + e] = ((unsigned)c0 + l) | ((ta + e - t0) << kTcRankShift);
     }
   }
 }
 
-/* triangle -> cell map from the offsets: tri_cell[offsets[c] + r] = c */
+/* triangle -> cell map from the offsets: tri_cell[offsets[c] + r] = c | r << 28 */
 __global__ void __launch_bounds__(256)
 k_fill_tri_cell(const unsigned* __restrict__ offsets, long long n, unsigned* __restrict__ tri_cell) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x) {
     const unsigned a = offsets[c], b = offsets[c + 1];
-    for (unsigned u = a; u < b; u++) tri_cell[u] = (unsigned)c;
+    for (unsigned u = a; u < b; u++) tri_cell[u] = (unsigned)c | ((u - a) << kTcRankShift);
   }
 }
 
@@ -544,10 +603,10 @@ __device__ __forceinline__ unsigned cell_code_any(const FieldDev& F, long long i
  * FP32 estimate stands for.  Returns the cube-edge ids in *edges.
  */
 __device__ __forceinline__ void exact_vertices(const Geo& G, long long t, d3 v[3]) {
-  const unsigned c = G.tri_cell[t];
-  const unsigned r = (G.meta[t] >> kMetaRankShift) & 15;
+  const unsigned tc = G.tri_cell[t];
+  const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
   unsigned ui, uj, ukl;
-  cell_ijk(c, (unsigned)(G.F.nx - 1), (unsigned)(G.F.ny - 1), ui, uj, ukl);
+  cell_ijk(G.F, c, ui, uj, ukl);
   const long long i = ui, j = uj, k = G.S.kfirst + ukl;
   const unsigned code = G.codes[c];
   const unsigned long long e = __ldg(G.lut + code * 12 + r);
@@ -570,6 +629,13 @@ __device__ __forceinline__ void face_normal(const d3 v[3], d3& fn, double& area,
 /* ------------------------------------------------------------------ */
 /* k_emit: single-precision triangles with certified bounds             */
 /* ------------------------------------------------------------------ */
+/* x >= 0 (or -1, -2) as a bfloat16 no smaller than x (bits of the high half) */
+__device__ __forceinline__ unsigned bf16_up(float x) {
+  const unsigned b = __float_as_uint(x);
+  return (b >> 16) + ((b & 0xFFFFu) != 0u && !(b >> 31) ? 1u : 0u);
+}
+__device__ __forceinline__ float bf16_value(unsigned h) { return __uint_as_float(h << 16); }
+
 /* a field value as a float and the bound on its conversion error */
 __device__ __forceinline__ float value_f(double v, float& e) {
   const float a = to_f(v); /* truncation: < 2u |a|, or < 2^-126 when flushed */
@@ -767,7 +833,7 @@ k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const uns
        t += (long long)gridDim.x * blockDim.x) {
     const unsigned meta = tri.meta[t];
     if (!(meta & kMetaRendered)) continue;
-    const long long c = tri_cell[t];
+    const long long c = tri_cell[t] & kTcCellMask;
 #pragma unroll 1
     for (int m = 0; m < 3; m++) {
       const d3 n = vertex_normal(c, (meta >> (5 * m)) & 31, ncx, ncy, offsets, tri);
@@ -821,7 +887,8 @@ __device__ __forceinline__ double exact_depth(const ExactTri& x, double w0, doub
 }
 
 __device__ __forceinline__ unsigned long long order_of(const Geo& G, unsigned long long order_base, long long t) {
-  return order_base + 12ULL * G.tri_cell[t] + ((G.meta[t] >> kMetaRankShift) & 15);
+  const unsigned tc = G.tri_cell[t];
+  return order_base + 12ULL * (tc & kTcCellMask) + (tc >> kTcRankShift);
 }
 
 /* the winning fragment's exact weights for shading (see RasterDev::winfo) */
@@ -934,12 +1001,12 @@ __device__ __forceinline__ void block_reserve2(unsigned long long* count0, unsig
   __syncthreads();
 }
 
-/* the same for three lists of at most one item per thread */
-template <int kThreads>
-__device__ __forceinline__ void block_reserve3(unsigned long long* count0, bool n0, unsigned long long* count1,
-                                               bool n1, unsigned long long* count2, bool n2, unsigned long long& r0,
-                                               unsigned long long& r1, unsigned long long& r2) {
-  static_assert(kThreads < 1024, "10-bit fields");
+/* the same for three lists of at most kPer items per thread */
+template <int kThreads, int kPer>
+__device__ __forceinline__ void block_reserve3(unsigned long long* count0, unsigned n0, unsigned long long* count1,
+                                               unsigned n1, unsigned long long* count2, unsigned n2,
+                                               unsigned long long& r0, unsigned long long& r1, unsigned long long& r2) {
+  static_assert(kThreads * kPer < 1024, "10-bit fields: at most kPer items per thread and list");
   __shared__ unsigned s_w[kThreads / 32];
   __shared__ unsigned long long s_b[3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1029,7 +1096,6 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     }
   }
   __syncthreads();
-  const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
   const T* fd = static_cast<const T*>(F.data);
   float e_vt;
   const float vt = value_f(F.threshold, e_vt);
@@ -1037,7 +1103,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     const unsigned entry = list[e];
     const unsigned m = entry >> 11;
     unsigned ui, uj, ukl;
-    cell_ijk((unsigned)(c0 + (entry & 2047)), ncx, ncy, ui, uj, ukl);
+    cell_ijk(F, (unsigned)(c0 + (entry & 2047)), ui, uj, ukl);
     const long long i = ui, j = uj, k = S.kfirst + ukl;
     float xa[3], xb[3], qv[3], eq[3];
     const float ce = corner_pos_f(F, i, j, k, 0, xa);
@@ -1048,8 +1114,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     const int st = vok ? project_f(scene, qv, eq, X, Y, Z, exy, ez) : -1;
     /* |Z| in [1e-8, 1e30] when the projection succeeds: __fdividef is within 2 ulp */
     const float aux = st > 0 ? 1.01f * __fdividef(ez, fabsf(Z)) : (st == 0 ? -1.f : -2.f);
-    V.pos[va + e] = make_float4(X, Y, Z, exy);
-    V.aux[va + e] = aux;
+    V.pos[va + e] = make_float4(X, Y, Z, __uint_as_float((bf16_up(exy) << 16) | bf16_up(aux)));
   }
 }
 
@@ -1062,6 +1127,131 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
  * k_cover and k_sliver triangles are written to the compact lists those
  * read.  Without raster lists (inspection) only the ids are kept.
  */
+/* what k_emit decided for one triangle */
+struct EmitOut {
+  int route; /* 0 no fragment, 1 k_tiny, 2 k_cover, 3 k_sliver */
+  float X[3], Y[3], Z[3], exy, zr;
+};
+
+template <typename T, bool CHECK>
+__device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, const SceneDev& scene,
+                                         const unsigned long long* lut, const unsigned char* __restrict__ codes,
+                                         const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
+                                         const TriDev& tri, const RasterDev& R, const VertDev& V,
+                                         unsigned* __restrict__ checks, long long t, EmitOut& out) {
+  const long long ncx = F.nx - 1, ncy = F.ny - 1;
+  const long long W = scene.width, H = scene.height;
+  const unsigned ncxy = (unsigned)(ncx * ncy);
+  int& route = out.route;
+  float* X = out.X;
+  float* Y = out.Y;
+  float* Z = out.Z;
+  float& exy = out.exy;
+  float& zr = out.zr;
+  route = 0;
+  exy = 0.f;
+  zr = 0.f;
+#pragma unroll
+  for (int q = 0; q < 3; q++) X[q] = Y[q] = Z[q] = 0.f;
+  const unsigned tc = tri_cell[t];
+  const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
+  unsigned ui, uj, ukl;
+  cell_ijk(F, c, ui, uj, ukl);
+  const long long i = ui, j = uj, k = S.kfirst + ukl;
+  const unsigned code = codes[c];
+  const unsigned long long e = lut[code * 12 + r];
+  unsigned edges = 0;
+#pragma unroll
+  for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
+  /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
+  const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
+  unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
+  if (rendered && R.cover_count) {
+    /* the three vertices from k_vertices: vertex q lies on the edge from
+       corner a to corner b, owned by the cell at corner a & b */
+    int status = 1;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const unsigned a = (unsigned)((e >> (6 * q)) & 7), b = (unsigned)((e >> (6 * q + 3)) & 7);
+      const unsigned o = a & b, m = a ^ b;
+      const unsigned oc = c + (o & 1u) + ((o >> 1) & 1u) * (unsigned)ncx + (o >> 2) * ncxy;
+      const unsigned vi = voffsets[oc] + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
+      const float4 p = __ldg(V.pos + vi);
+      const unsigned pk = __float_as_uint(p.w);
+      const float aux = bf16_value(pk & 0xFFFFu);
+      X[q] = p.x;
+      Y[q] = p.y;
+      Z[q] = p.z;
+      exy = fmaxf(exy, bf16_value(pk >> 16));
+      if (aux >= 0.f) zr = fmaxf(zr, aux);
+      else if (aux == -1.f) status = 0;
+      else if (status != 0) status = -1;
+    }
+    d3 v[3];
+    bool ok = true;
+    if (CHECK) {
+      /* the reference's own vertices and projection */
+      d3 p[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+        v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
+                           corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
+      }
+#pragma unroll
+      for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
+      if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
+      if (status == 1 && ok) {
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+          if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
+              fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
+            atomicAdd(checks + 1, 1u);
+      }
+    }
+    if (status == 0) meta |= kMetaCulled;
+    if (status < 0) meta |= kMetaUndecided;
+    if (R.cover_count && status != 0) {
+      const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
+      float errA;
+      const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
+      const bool decided = status > 0 && isfinite(A) && isfinite(exy) && exy < 1e-3f && zr < 1e-3f;
+      if (!decided) {
+        route = 1;
+      } else if (!(fabsf(A) - errA > 1e-15f)) {
+        /* the area may be clamped to +-1e-16 (render.c:108-111): k_sliver
+           tests the reference's whole box */
+        route = 3;
+      } else {
+        /* the reference's area is certainly not clamped: its weights are
+           barycentric up to the -1e-8 slack, so every covered pixel centre
+           lies in the triangle's extent */
+        const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
+        const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
+        const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
+        long long imin, imax, jmin, jmax;
+        centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
+        centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+        route = imin <= imax && jmin <= jmax ? 2 : 0;
+        if (CHECK && route == 0 && ok) {
+          /* no pixel of the reference's box may be covered */
+          ExactTri ex;
+          if (exact_tri(scene, v, ex))
+            for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
+              for (long long ii = ex.imin; ii <= ex.imax; ii++) {
+                double w0, w1, w2;
+                if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
+              }
+        }
+      }
+    }
+  }
+  tri.meta[t] = meta;
+  tri.meta[t] = meta;
+}
+
+constexpr int kEmitPer = 2; /* triangles per thread and iteration: two gather chains in flight */
+
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
@@ -1069,124 +1259,45 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
        const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
        const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R, VertDev V,
        unsigned* __restrict__ checks) {
+  (void)offsets;
   __shared__ unsigned long long lut[kLutEntries];
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
   const long long T_ = (long long)*total_p;
-  const long long ncx = F.nx - 1, ncy = F.ny - 1;
-  const long long W = scene.width, H = scene.height;
-  const unsigned ncxy = (unsigned)(ncx * ncy);
+  const long long step = (long long)blockDim.x * kEmitPer;
   /* every thread of a block runs the same iterations (block-wide appends) */
-  for (long long base = blockIdx.x * (long long)blockDim.x; base < T_; base += (long long)gridDim.x * blockDim.x) {
-    const long long t = base + threadIdx.x;
-    int route = 0; /* 0 no fragment, 1 k_tiny, 2 k_cover, 3 k_sliver */
-    float X[3] = {0.f, 0.f, 0.f}, Y[3] = {0.f, 0.f, 0.f}, Z[3] = {0.f, 0.f, 0.f}, exy = 0.f, zr = 0.f;
-    if (t < T_) {
-      const unsigned c = tri_cell[t];
-      const unsigned r = (unsigned)(t - offsets[c]);
-      unsigned ui, uj, ukl;
-      cell_ijk(c, (unsigned)ncx, (unsigned)ncy, ui, uj, ukl);
-      const long long i = ui, j = uj, k = S.kfirst + ukl;
-      const unsigned code = codes[c];
-      const unsigned long long e = lut[code * 12 + r];
-      unsigned edges = 0;
+  for (long long base = blockIdx.x * step; base < T_; base += (long long)gridDim.x * step) {
+    EmitOut o[kEmitPer];
 #pragma unroll
-      for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
-      /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
-      const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
-      unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
-      if (rendered && R.cover_count) {
-        /* the three vertices from k_vertices: vertex q lies on the edge from
-           corner a to corner b, owned by the cell at corner a & b */
-        int status = 1;
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          const unsigned a = (unsigned)((e >> (6 * q)) & 7), b = (unsigned)((e >> (6 * q + 3)) & 7);
-          const unsigned o = a & b, m = a ^ b;
-          const unsigned oc = c + (o & 1u) + ((o >> 1) & 1u) * (unsigned)ncx + (o >> 2) * ncxy;
-          const unsigned vi = voffsets[oc] + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
-          const float4 p = __ldg(V.pos + vi);
-          const float aux = __ldg(V.aux + vi);
-          X[q] = p.x;
-          Y[q] = p.y;
-          Z[q] = p.z;
-          exy = fmaxf(exy, p.w);
-          if (aux >= 0.f) zr = fmaxf(zr, aux);
-          else if (aux == -1.f) status = 0;
-          else if (status != 0) status = -1;
-        }
-        d3 v[3];
-        bool ok = true;
-        if (CHECK) {
-          /* the reference's own vertices and projection */
-          d3 p[3];
-#pragma unroll
-          for (int q = 0; q < 3; q++) {
-            const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-            v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
-                               corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
-          }
-#pragma unroll
-          for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
-          if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
-          if (status == 1 && ok) {
-#pragma unroll
-            for (int q = 0; q < 3; q++)
-              if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
-                  fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
-                atomicAdd(checks + 1, 1u);
-          }
-        }
-        if (status == 0) meta |= kMetaCulled;
-        if (status < 0) meta |= kMetaUndecided;
-        if (R.cover_count && status != 0) {
-          const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
-          float errA;
-          const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
-          const bool decided = status > 0 && isfinite(A) && isfinite(exy) && exy < 1e-3f && zr < 1e-3f;
-          if (!decided) {
-            route = 1;
-          } else if (!(fabsf(A) - errA > 1e-15f)) {
-            /* the area may be clamped to +-1e-16 (render.c:108-111): k_sliver
-               tests the reference's whole box */
-            route = 3;
-          } else {
-            /* the reference's area is certainly not clamped: its weights are
-               barycentric up to the -1e-8 slack, so every covered pixel centre
-               lies in the triangle's extent */
-            const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
-            const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
-            const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
-            long long imin, imax, jmin, jmax;
-            centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
-            centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
-            route = imin <= imax && jmin <= jmax ? 2 : 0;
-            if (CHECK && route == 0 && ok) {
-              /* no pixel of the reference's box may be covered */
-              ExactTri ex;
-              if (exact_tri(scene, v, ex))
-                for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
-                  for (long long ii = ex.imin; ii <= ex.imax; ii++) {
-                    double w0, w1, w2;
-                    if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
-                  }
-            }
-          }
-        }
-      }
-      tri.meta[t] = meta;
+    for (int u = 0; u < kEmitPer; u++) {
+      o[u].route = 0;
+      const long long t = base + u * (long long)blockDim.x + threadIdx.x;
+      if (t < T_) emit_one<T, CHECK>(F, S, scene, lut, codes, voffsets, tri_cell, tri, R, V, checks, t, o[u]);
     }
     if (R.cover_count) {
+      unsigned n1 = 0, n2 = 0, n3 = 0;
+#pragma unroll
+      for (int u = 0; u < kEmitPer; u++) {
+        n1 += o[u].route == 1;
+        n2 += o[u].route == 2;
+        n3 += o[u].route == 3;
+      }
       unsigned long long ti, ci, si;
-      block_reserve3<256>(R.tiny_count, route == 1, R.cover_count, route == 2, R.sliver_count, route == 3, ti, ci,
-                          si);
-      if (route == 1 && ti < R.tiny_cap) R.tiny[ti] = (unsigned)t; /* overflow: the host re-runs the slab */
-      if (route >= 2) {
-        /* cover and sliver entries together number at most the slab's triangles */
-        float4* rec = route == 2 ? tri.rec + 3 * ci : R.sliver_rec - 3 * si;
-        rec[0] = make_float4(X[0], Y[0], Z[0], X[1]);
-        rec[1] = make_float4(Y[1], Z[1], X[2], Y[2]);
-        rec[2] = make_float4(Z[2], exy, zr, __uint_as_float((unsigned)t));
+      block_reserve3<256, kEmitPer>(R.tiny_count, n1, R.cover_count, n2, R.sliver_count, n3, ti, ci, si);
+#pragma unroll
+      for (int u = 0; u < kEmitPer; u++) {
+        const unsigned t = (unsigned)(base + u * (long long)blockDim.x + threadIdx.x);
+        const EmitOut& e = o[u];
+        if (e.route == 1) {
+          if (ti < R.tiny_cap) R.tiny[ti] = t; /* overflow: the host re-runs the slab */
+          ti++;
+        } else if (e.route >= 2) {
+          /* cover and sliver entries together number at most the slab's triangles */
+          float4* rec = e.route == 2 ? tri.rec + 3 * (ci++) : R.sliver_rec - 3 * (si++);
+          rec[0] = make_float4(e.X[0], e.Y[0], e.Z[0], e.X[1]);
+          rec[1] = make_float4(e.Y[1], e.Z[1], e.X[2], e.Y[2]);
+          rec[2] = make_float4(e.Z[2], e.exy, e.zr, __uint_as_float(t));
+        }
       }
     }
   }
@@ -1548,7 +1659,7 @@ __global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R)
     int ng = 0;
     if (q < n) {
       const long long t = R.win[q].y;
-      const long long c = G.tri_cell[t];
+      const long long c = G.tri_cell[t] & kTcCellMask;
       const unsigned meta = tri.meta[t];
       for (int m = 0; m < 3; m++) {
         const int e = (meta >> (5 * m)) & 31;
@@ -1625,7 +1736,7 @@ k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
       if (!exact_tri(scene, v, x) || !exact_weights(x, pi, pj, R.xs, R.ys, w0, w1, w2)) continue;
     }
     const unsigned meta = tri.meta[t];
-    const long long c = G.tri_cell[t];
+    const long long c = G.tri_cell[t] & kTcCellMask;
     const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, G.offsets, tri);
     const d3 n1 = vertex_normal(c, (meta >> 5) & 31, ncx, ncy, G.offsets, tri);
     const d3 n2 = vertex_normal(c, (meta >> 10) & 31, ncx, ncy, G.offsets, tri);
@@ -1775,14 +1886,19 @@ void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts,
   else k_classify<double><<<grid, kClsX, 0, st>>>(F, S, counts);
 }
 
-void launch_scan(const unsigned char* counts, long long n, unsigned* offsets, unsigned* voffsets,
-                 unsigned long long* tile_state, unsigned* tile_counter, unsigned long long* totals,
-                 unsigned* err, cudaStream_t st) {
-  const long long tiles = (n + kScanTile) / kScanTile; /* covers position n too */
-  cudaMemsetAsync(tile_state, 0, sizeof(unsigned long long) * tiles, st);
-  cudaMemsetAsync(tile_counter, 0, sizeof(unsigned), st);
-  k_scan<<<(unsigned)tiles, kScanThreads, 0, st>>>(counts, n, offsets, voffsets, tile_state, tile_counter, totals,
-                                                   err);
+long long scan_segments(long long n) { return (n + kScanTile - 1) / kScanTile; }
+
+void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
+                 unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
+                 unsigned* tri_cell, unsigned long long tri_cap, cudaStream_t st) {
+  const long long nseg = scan_segments(n);
+  if (nseg > 0) k_seg_reduce<<<(unsigned)nseg, kScanThreads, 0, st>>>(codes, n, seg_sums);
+  k_seg_scan<<<1, kSegScanThreads, 0, st>>>(seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
+  /* beyond the default 48 KB of dynamic shared memory: set for the current device */
+  cudaFuncSetAttribute(k_scan_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanWriteSmem);
+  if (nseg > 0)
+    k_scan_write<<<(unsigned)nseg, kScanThreads, kScanWriteSmem, st>>>(codes, n, seg_base, offsets, voffsets, totals,
+                                                                       tri_cell, tri_cap);
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
@@ -1796,7 +1912,6 @@ void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_ce
   k_fill_tri_cell<<<grid_for(n, 256, 16), 256, 0, st>>>(offsets, n, tri_cell);
 }
 
-long long scan_tiles(long long n) { return (n + kScanTile) / kScanTile; }
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets,

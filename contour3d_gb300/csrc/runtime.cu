@@ -571,6 +571,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   F.threshold = ci.threshold;
   F.thr_key = h_key(ci.threshold);
   F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
+  F.div_cx = make_fast_div((unsigned)(nx - 1));
+  F.div_cy = make_fast_div((unsigned)(ny - 1));
   set_float_threshold(F);
   c.stats.cells += (uint64_t)(ncx * ncy * ncz);
 
@@ -607,19 +609,27 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     const long long ncell = S.nslices * per_slice;
     if (c.counts.ensure((size_t)ncell, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
         c.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
-        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_tiles(ncell), st) || c.scratch.ensure(128, st))
+        c.tile_state.ensure(2 * sizeof(unsigned long long) * (size_t)scan_segments(ncell), st) ||
+        c.scratch.ensure(128, st))
       return 1;
+    /* the triangle -> cell map is written by the scan when the slab's
+       triangles fit: the buffer keeps the size of the largest slab so far, at
+       least one triangle per two cells */
+    if (c.tri_cell.ensure(sizeof(unsigned) * (size_t)(ncell / 2 + 1024), st)) return 1;
+    const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = d_counter + 1;
     unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2); /* triangles, vertices */
+    const long long nseg = scan_segments(ncell);
+    unsigned long long *seg_sums = c.tile_state.as<unsigned long long>(), *seg_base = seg_sums + nseg;
     C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
     launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
     if (c.stage_timing) cudaEventRecord(c.evs[1], st);
-    launch_scan(c.counts.as<unsigned char>(), ncell, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(),
-                c.tile_state.as<unsigned long long>(), d_counter, d_total, d_err, st);
+    launch_scan(c.counts.as<unsigned char>(), ncell, seg_sums, seg_base, c.offsets.as<unsigned>(),
+                c.voffsets.as<unsigned>(), d_total, c.tri_cell.as<unsigned>(), tri_cap, st);
     if (c.stage_timing) cudaEventRecord(c.evs[2], st);
-    c.stats.kernel_launches += 2;
+    c.stats.kernel_launches += 4;
     C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     C3D_CUDA(cudaStreamSynchronize(st));
@@ -628,7 +638,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
     }
     if (h_small[0]) {
-      log_error("device classification or scan did not complete (error flags 0x%x)", h_small[0]);
+      log_error("device classification did not complete (error flags 0x%x)", h_small[0]);
       return 1;
     }
     const unsigned long long T = h_total[0], NV = h_total[1];
@@ -637,6 +647,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     if (T == 0) continue;
     /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
        every sub-array stays aligned (and over-allocate so that cap >= T) */
+    const bool filled = T <= tri_cap; /* the scan wrote the triangle -> cell map */
     if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
     const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
     if (cap < T) {
@@ -652,14 +663,15 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
     /* the vertex stage: triangle -> cell map, screen vertices */
     if (c.stage_timing) cudaEventRecord(c.evs[3], st);
-    launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
-    c.stats.kernel_launches += 1;
+    if (!filled) {
+      launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
+      c.stats.kernel_launches += 1;
+    }
     VertDev VD = {};
     if (!sink) {
-      /* the screen vertices of the slab's crossed edges: float4 records, then the aux floats */
-      if (c.verts.ensure(20 * (size_t)NV + 64, st)) return 1;
+      /* the screen vertices of the slab's crossed edges, 16 bytes each */
+      if (c.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
       VD.pos = c.verts.as<float4>();
-      VD.aux = reinterpret_cast<float *>(VD.pos + NV);
       launch_vertices(F, S, sd, c.counts.as<unsigned char>(), c.voffsets.as<unsigned>(), ncell, VD, st);
       c.stats.kernel_launches += 1;
       c.stats.vertices += NV;
@@ -771,7 +783,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * kDbgDoubles * cap, cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
       for (unsigned long long t = 0; t < T; t++) {
-        const long long cl = cellv[t];
+        const long long cl = cellv[t] & kTcCellMask;
         const long long i = cl % ncx, j = (cl / ncx) % ncy, k = S.kfirst + cl / (ncx * ncy);
         if (k >= k0 && k < k1) sink->triangulated++;
         if (!(meta[t] & kMetaRendered)) continue;
@@ -1291,13 +1303,15 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   F.threshold = obj->threshold;
   F.thr_key = h_key(obj->threshold);
   F.thr_nan = std::isnan(obj->threshold) ? 1 : 0;
+  F.div_cx = make_fast_div((unsigned)(nx - 1));
+  F.div_cy = make_fast_div((unsigned)(ny - 1));
   set_float_threshold(F);
   SlabDev S = {0, nz - 1, 0, 0};
+  const size_t ncell = (size_t)((nx - 1) * (ny - 1) * (nz - 1));
   if (c.scratch.ensure(128, st)) return -1;
   unsigned *d_err = c.scratch.as<unsigned>();
   if (cudaMemsetAsync(d_err, 0, sizeof(unsigned), st) != cudaSuccess) return -1;
   launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
-  const size_t ncell = (size_t)((nx - 1) * (ny - 1) * (nz - 1));
   std::vector<uint8_t> h(ncell);
   unsigned herr = 0;
   if (cudaMemcpyAsync(h.data(), c.counts.p, ncell, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
