@@ -25,6 +25,8 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+/* 1 / a, correctly rounded: the same value as ddiv(1.0, a) */
+__device__ __forceinline__ double drcp(double a) { return __drcp_rn(a); }
 __device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
 
 struct d3 {
@@ -43,7 +45,7 @@ __device__ __forceinline__ d3 v_cross(d3 a, d3 b) {
           dsub(dmul(a.x, b.y), dmul(a.y, b.x))};
 }
 __device__ __forceinline__ d3 v_normalise(d3 a) {
-  const double inv = ddiv(1.0, dsqrt(v_dot(a, a)));
+  const double inv = drcp(dsqrt(v_dot(a, a)));
   return {dmul(a.x, inv), dmul(a.y, inv), dmul(a.z, inv)};
 }
 

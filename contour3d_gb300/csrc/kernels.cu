@@ -622,7 +622,7 @@ __device__ __forceinline__ void exact_vertices(const Geo& G, long long t, d3 v[3
 __device__ __forceinline__ void face_normal(const d3 v[3], d3& fn, double& area, d3& wn) {
   fn = v_cross(v_sub(v[1], v[0]), v_sub(v[2], v[0]));
   area = dsqrt(v_dot(fn, fn));
-  fn = v_mul(ddiv(1., area), fn);
+  fn = v_mul(drcp(area), fn);
   wn = v_mul(area, fn);
 }
 
@@ -867,7 +867,7 @@ __device__ __forceinline__ bool exact_tri(const SceneDev& s, const d3 w[3], Exac
   x.jmin = min(H - 1, max(0LL, ymin));
   x.jmax = min(H - 1, max(0LL, ymax));
   x.area = edge_fn(x.v0, x.v1, x.v2);
-  x.area_inv = ddiv(1., x.area < 0. ? fmin(x.area, -1.e-16) : fmax(x.area, +1.e-16));
+  x.area_inv = drcp(x.area < 0. ? fmin(x.area, -1.e-16) : fmax(x.area, +1.e-16));
   return true;
 }
 
@@ -883,7 +883,7 @@ __device__ __forceinline__ bool exact_weights(const ExactTri& x, long long i, lo
 }
 
 __device__ __forceinline__ double exact_depth(const ExactTri& x, double w0, double w1, double w2) {
-  return ddiv(1., dadd(dadd(ddiv(w0, x.v0.z), ddiv(w1, x.v1.z)), ddiv(w2, x.v2.z)));
+  return drcp(dadd(dadd(ddiv(w0, x.v0.z), ddiv(w1, x.v1.z)), ddiv(w2, x.v2.z)));
 }
 
 __device__ __forceinline__ unsigned long long order_of(const Geo& G, unsigned long long order_base, long long t) {
@@ -1083,16 +1083,30 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
   if (c0 >= n) return;
   const long long c1 = min(c0 + kVTile, n);
   const unsigned va = voffsets[c0], vb = voffsets[c1];
-  for (int q = 0; q < kVItems; q++) {
-    const int lc = threadIdx.x * kVItems + q;
-    const long long c = c0 + lc;
-    if (c >= c1) break;
-    unsigned mask = owned_edges(codes[c]);
-    unsigned at = voffsets[c] - va;
-    while (mask) {
-      const unsigned m = (unsigned)__ffs(mask); /* edge to corner m */
-      mask &= mask - 1;
-      list[at++] = (unsigned short)(lc | (m << 11));
+  {
+    /* the thread's kVItems cells: one 8-byte load of their codes (a code
+       past the end reads as 0: no owned edges); their vertices are
+       consecutive from the first cell's offset */
+    const long long cf = c0 + (long long)threadIdx.x * kVItems;
+    unsigned long long cw = 0;
+    if (cf + kVItems <= c1) {
+      cw = *reinterpret_cast<const unsigned long long*>(codes + cf); /* cf is a multiple of 8 */
+    } else {
+      for (int q = 0; q < kVItems; q++)
+        if (cf + q < c1) cw |= (unsigned long long)codes[cf + q] << (8 * q);
+    }
+    if (cw != 0ULL && cw != ~0ULL) { /* all-outside or all-inside cells own no crossed edge */
+      unsigned at = (cf < c1 ? voffsets[cf] : vb) - va;
+#pragma unroll
+      for (int q = 0; q < kVItems; q++) {
+        unsigned mask = owned_edges((unsigned)(cw >> (8 * q)) & 255u);
+        const unsigned lc = threadIdx.x * kVItems + q;
+        while (mask) {
+          const unsigned m = (unsigned)__ffs(mask); /* edge to corner m */
+          mask &= mask - 1;
+          list[at++] = (unsigned short)(lc | (m << 11));
+        }
+      }
     }
   }
   __syncthreads();
@@ -1108,8 +1122,9 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     float xa[3], xb[3], qv[3], eq[3];
     const float ce = corner_pos_f(F, i, j, k, 0, xa);
     corner_pos_f(F, i, j, k, (int)m, xb);
-    const bool vok = vertex_q<T>(scene, vt, e_vt, xa, __ldg(fd + corner_index(F, i, j, k, 0)), xb,
-                                 __ldg(fd + corner_index(F, i, j, k, (int)m)), ce, qv, eq);
+    const long long i0 = (k * F.ny + j) * F.nx + i;
+    const long long i1 = i0 + (long long)(m & 1u) + ((m >> 1) & 1u) * F.nx + (long long)(m >> 2) * F.nx * F.ny;
+    const bool vok = vertex_q<T>(scene, vt, e_vt, xa, __ldg(fd + i0), xb, __ldg(fd + i1), ce, qv, eq);
     float X = 0.f, Y = 0.f, Z = 0.f, exy = 0.f, ez = 0.f;
     const int st = vok ? project_f(scene, qv, eq, X, Y, Z, exy, ez) : -1;
     /* |Z| in [1e-8, 1e30] when the projection succeeds: __fdividef is within 2 ulp */
@@ -1780,7 +1795,7 @@ __global__ void k_lines(const LineSegDev* __restrict__ segs, int nseg, long long
     const double distance = ddiv(dmul(num, num), ab2);
     if (thr < distance) continue;
     const double param = ddiv(dmul(-1., dadd(dmul(dsub(p1x, p0x), dsub(p0x, di)), dmul(dsub(p1y, p0y), dsub(p0y, dj)))), dd);
-    const double dist0 = ddiv(1., dadd(ddiv(param, p1z), ddiv(dsub(1., param), p0z)));
+    const double dist0 = drcp(dadd(ddiv(param, p1z), ddiv(dsub(1., param), p0z)));
     const unsigned long long key = depth_key(dist0);
     Slot* s = canvas + j * W + i;
     slot_max(s, key, (order << 24) | L.rgb);
