@@ -156,6 +156,7 @@ struct SceneDev {
   float f_cam[3], f_n[3], f_lx[3], f_ly[3];
   float f_cam_max, f_n1, f_lx1, f_lxm, f_ly1, f_lym;
   float f_ax, f_bx, f_ay, f_by, f_dq;
+  float f_light[3]; /* the light direction rounded to float */
   int z_descending; /* the camera looks towards -z: traverse slices top down */
 };
 

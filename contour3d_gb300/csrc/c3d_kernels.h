@@ -41,6 +41,13 @@ struct FieldDev {
   unsigned thr_f_key;
   int thr_f_ok;
   FastDiv div_cx, div_cy;   /* division by the cells per row (nx - 1) and per column (ny - 1) */
+  /* single-precision shading (identity converter only, else null): node
+     spacings g[i + 1] - g[i] rounded to float, and an absolute allowance for
+     the rounding of the reference's FP64 vertex coordinates */
+  const float* dgx;
+  const float* dgy;
+  const float* dgz;
+  float coord_eps;
 };
 
 /* the constants of FastDiv for d >= 1 */
@@ -71,7 +78,8 @@ struct TriDev {
      err_z t -- FP32 screen positions and depths, the bound on |screen x, y -
      the reference's value|, the relative depth bound and the emission index */
   float4* rec;
-  unsigned* need;     /* 1 once the weighted normal was requested */
+  unsigned* need;     /* bit 0: FP32 weighted normal requested, bit 1: FP64 one */
+  float4* wnf;        /* FP32 area-weighted face normal and the bound on each component */
   double* vert[9];    /* inspection: exact vertices */
   double* vn[9];      /* inspection: vertex normals */
   double* dbg_fn;     /* inspection: face normals, 3 per triangle */
@@ -142,6 +150,11 @@ struct RasterDev {
   unsigned long long* win_count;
   unsigned* need;           /* triangles whose weighted normal shading needs */
   unsigned long long* need_count;
+  uint2* amb;               /* won pixels whose FP32 colour is not certain (shaded in FP64) */
+  unsigned long long* amb_count;
+  unsigned long long* need64_count; /* the FP64 requests of those, in `need` again */
+  unsigned clamp_rgb;       /* the colour at the reference's factor 0.15, computed exactly */
+  unsigned* shade_check;    /* self-check: per pixel, 1 << 24 | the FP32 colour when certain */
 };
 
 /* one line segment, already projected to pixel units on the host */
@@ -192,10 +205,12 @@ void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, cons
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st);
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
                   unsigned long long order_base, cudaStream_t st);
-/* winners, normal requests, weighted normals; `between` (optional) is recorded before the colour pass */
+/* winners, normal requests, weighted normals, colours; `between` (optional)
+   is recorded before the colour passes; `checks` (self-check) counts FP32
+   colours that differ from the FP64 ones */
 void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                     const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
-                    cudaEvent_t between, cudaStream_t st);
+                    unsigned* checks, cudaEvent_t between, cudaStream_t st);
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, cudaStream_t st);
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,

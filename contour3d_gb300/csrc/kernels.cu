@@ -648,28 +648,66 @@ __device__ __forceinline__ float value_f(float v, float& e) {
 }
 
 /*
+ * The interpolation parameter f = (vt - v0) / (v1 - v0) of triangulate.c:40-73
+ * in FP32 with a bound e_f on its distance to the reference's value.
+ * Returns 1 (f valid), 0 (the reference keeps p0: |v1 - v0| < 1e-8) or -1
+ * (the bounds cannot decide that test).
+ *   double fields: the two differences are formed in FP64 exactly as the
+ *     reference forms them, then truncated to float (2u each), so the 1e-8
+ *     test is exact and cancellation costs no accuracy;
+ *   float fields: the values are exact floats and the differences are FP32
+ *     (u each), with the 1e-8 test decided by the bounds.
+ */
+__device__ __forceinline__ int interp_param(double vt, float, float, double v0, double v1, float& f, float& e_f) {
+  const double dvd = dsub(v1, v0);
+  if (abs_lt_1e8(dvd)) return 0;
+  const float dv = to_f(dvd), dt = to_f(dsub(vt, v0));
+  const float adv = fabsf(dv);
+  const float e_dv = 2.f * kU32 * adv + 1.2e-38f, e_dt = 2.f * kU32 * fabsf(dt) + 1.2e-38f;
+  if (!(adv > 1e-30f) || adv > 1e30f) return -1;
+  const float rdv = __fdividef(1.f, adv); /* 2 ulp on [1e-30, 1e30] */
+  const float xr = e_dv * rdv;
+  f = __fdividef(dt, dv);
+  const float fmax_ = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
+  e_f = 1.1f * (1.01f * (e_dt + fmax_ * e_dv) * rdv + 4.f * kU32 * fabsf(f));
+  return 1;
+}
+__device__ __forceinline__ int interp_param(double, float vt, float e_vt, float v0, float v1, float& f, float& e_f) {
+  const float dv = v1 - v0;
+  const float e_dv = 1.01f * kU32 * fabsf(dv);
+  const float adv = fabsf(dv);
+  if (!(adv - e_dv > 1.00001e-8f)) return adv + e_dv < 0.99999e-8f ? 0 : -1;
+  if (adv > 1e30f) return -1;
+  /* 1 / |dv| to 2 ulp; 1 / (|dv| - e_dv) <= rdv (1 + 1.02 x) for x = e_dv rdv < 0.01 */
+  const float rdv = __fdividef(1.f, adv);
+  const float xr = e_dv * rdv;
+  if (!(xr < 0.01f)) return -1;
+  const float dt = vt - v0;
+  const float e_dt = e_vt + 1.01f * kU32 * fabsf(dt);
+  f = __fdividef(dt, dv); /* 2 ulp */
+  /* |dt/dv - DT/DV| <= (e_dt + |DT/DV| e_dv) / |dv|, |DT/DV| <= fmax */
+  const float fmax_ = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
+  e_f = 1.1f * (1.01f * (e_dt + fmax_ * e_dv) * rdv + 4.f * kU32 * fabsf(f));
+  return 1;
+}
+
+/*
  * FP32 estimate of one vertex (triangulate.c:40-73) relative to the camera,
  * q = vertex - camera, with a bound per component on the distance to the
- * reference's FP64 value.  No FP64 arithmetic: the corner values are
- * converted to float (exactly for float fields) and the differences
- *   dv = v1 - v0,  dt = vt - v0,  f = dt / dv,  p = p0 + f (p1 - p0)
- * are formed in single precision with absolute bounds e_dv, e_dt, e_f.
- * The reference keeps p0 when |v1 - v0| < 1e-8; returns false when the
- * bounds cannot decide that test (the triangle then takes the FP64 path).
+ * reference's FP64 value: p = p0 + f (p1 - p0) with f from interp_param.
+ * Returns false when interp_param cannot decide the reference's 1e-8 test
+ * (the triangle then takes the FP64 path).
  */
 template <typename T>
-__device__ __forceinline__ bool vertex_q(const SceneDev& s, float vt, float e_vt, const float x0[3], T v0,
+__device__ __forceinline__ bool vertex_q(const SceneDev& s, double vtd, float vt, float e_vt, const float x0[3], T v0,
                                          const float x1[3], T v1, float ce, float q[3], float eq[3]) {
   /* x0, x1: corner coordinates rounded to float with error <= ce u |x| */
   const float pc[3] = {s.f_cam[0], s.f_cam[1], s.f_cam[2]};
-  float e0, e1;
-  const float a0 = value_f(v0, e0), a1 = value_f(v1, e1);
-  const float dv = a1 - a0;
-  const float e_dv = e0 + e1 + 1.01f * kU32 * fabsf(dv);
-  const float adv = fabsf(dv);
-  if (!(adv - e_dv > 1.00001e-8f)) {
-    if (!(adv + e_dv < 0.99999e-8f)) return false;
-    /* certainly |v1 - v0| < 1e-8: the reference keeps p0 itself */
+  float f = 0.f, e_f = 0.f;
+  const int st = interp_param(vtd, vt, e_vt, v0, v1, f, e_f);
+  if (st < 0) return false;
+  if (st == 0) {
+    /* the reference keeps p0 itself */
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       q[i] = x0[i] - pc[i];
@@ -677,19 +715,7 @@ __device__ __forceinline__ bool vertex_q(const SceneDev& s, float vt, float e_vt
     }
     return true;
   }
-  /* 1 / |dv| to 2 ulp (__fdividef, |dv| in [1e-8, 1e30]); 1 / (|dv| - e_dv)
-     <= rdv (1 + 1.02 x) for x = e_dv rdv < 0.01 */
-  if (adv > 1e30f) return false;
-  const float rdv = __fdividef(1.f, adv);
-  const float xr = e_dv * rdv;
-  if (!(xr < 0.01f)) return false;
-  const float dt = vt - a0;
-  const float e_dt = e_vt + e0 + 1.01f * kU32 * fabsf(dt);
-  const float f = __fdividef(dt, dv); /* 2 ulp */
   const float af = fabsf(f);
-  /* |dt/dv - DT/DV| <= (e_dt + |DT/DV| e_dv) / |dv|, |DT/DV| <= fmax */
-  const float fmax = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
-  const float e_f = 1.1f * (1.01f * (e_dt + fmax * e_dv) * rdv + 4.f * kU32 * af);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     const float d = x1[i] - x0[i];
@@ -1124,7 +1150,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     corner_pos_f(F, i, j, k, (int)m, xb);
     const long long i0 = (k * F.ny + j) * F.nx + i;
     const long long i1 = i0 + (long long)(m & 1u) + ((m >> 1) & 1u) * F.nx + (long long)(m >> 2) * F.nx * F.ny;
-    const bool vok = vertex_q<T>(scene, vt, e_vt, xa, __ldg(fd + i0), xb, __ldg(fd + i1), ce, qv, eq);
+    const bool vok = vertex_q<T>(scene, F.threshold, vt, e_vt, xa, __ldg(fd + i0), xb, __ldg(fd + i1), ce, qv, eq);
     float X = 0.f, Y = 0.f, Z = 0.f, exy = 0.f, ez = 0.f;
     const int st = vok ? project_f(scene, qv, eq, X, Y, Z, exy, ez) : -1;
     /* |Z| in [1e-8, 1e30] when the projection succeeds: __fdividef is within 2 ulp */
@@ -1663,8 +1689,10 @@ k_winners(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p,
  * that shares a cube edge with a vertex of the owner (normal.c:78-158
  * neighbourhoods), each triangle once; requests are appended per warp.
  */
-__global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R) {
-  const unsigned long long n = *R.win_count;
+__global__ void __launch_bounds__(256)
+k_request(Geo G, TriDev tri, RasterDev R, const uint2* __restrict__ pixels, const unsigned long long* __restrict__ count,
+          unsigned flag, unsigned long long* __restrict__ need_count) {
+  const unsigned long long n = *count;
   const unsigned ncx = (unsigned)(G.F.nx - 1), ncy = (unsigned)(G.F.ny - 1);
   const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
   /* every thread of a block runs the same number of iterations (block-wide appends) */
@@ -1673,7 +1701,7 @@ __global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R)
     unsigned got[48];
     int ng = 0;
     if (q < n) {
-      const long long t = R.win[q].y;
+      const long long t = pixels[q].y;
       const long long c = G.tri_cell[t] & kTcCellMask;
       const unsigned meta = tri.meta[t];
       for (int m = 0; m < 3; m++) {
@@ -1687,11 +1715,11 @@ __global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R)
           for (unsigned u = u0; u < u1; u++) {
             const unsigned om = tri.meta[u];
             if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
-              if (atomicOr(tri.need + u, 1u) == 0u) {
+              if (!(atomicOr(tri.need + u, flag) & flag)) {
                 if (ng < 48) {
                   got[ng++] = u;
                 } else {
-                  const unsigned long long s1 = atomicAdd(R.need_count, 1ULL);
+                  const unsigned long long s1 = atomicAdd(need_count, 1ULL);
                   R.need[s1] = u;
                 }
               }
@@ -1700,14 +1728,15 @@ __global__ void __launch_bounds__(256) k_request(Geo G, TriDev tri, RasterDev R)
         }
       }
     }
-    const unsigned long long base = block_reserve<256>(R.need_count, (unsigned)ng);
+    const unsigned long long base = block_reserve<256>(need_count, (unsigned)ng);
     for (int g = 0; g < ng; g++) R.need[base + g] = got[g];
   }
 }
 
 /* one thread per requested triangle: its exact weighted normal */
-__global__ void __launch_bounds__(256) k_wn(Geo G, TriDev tri, RasterDev R) {
-  const unsigned long long n = *R.need_count;
+__global__ void __launch_bounds__(256)
+k_wn(Geo G, TriDev tri, RasterDev R, const unsigned long long* __restrict__ count) {
+  const unsigned long long n = *count;
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x) {
     const long long u = R.need[q];
@@ -1722,16 +1751,18 @@ __global__ void __launch_bounds__(256) k_wn(Geo G, TriDev tri, RasterDev R) {
 }
 
 /* one thread per won pixel: vertex normals and colour (render.c:137-159) */
+template <bool CHECK>
 __global__ void __launch_bounds__(256)
-k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
-  const unsigned long long n = *R.win_count;
+k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in, const uint2* __restrict__ pixels,
+        const unsigned long long* __restrict__ count, unsigned* __restrict__ checks) {
+  const unsigned long long n = *count;
   const long long W = scene.width;
   const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
   const double cr = (double)((rgb_in >> 16) & 255), cg = (double)((rgb_in >> 8) & 255),
                cb = (double)(rgb_in & 255);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x) {
-    const uint2 wp = R.win[q];
+    const uint2 wp = pixels[q];
     const long long p = wp.x, t = wp.y;
     const unsigned long long lo = R.canvas[p].lo;
     const unsigned long long tag = ((lo >> 24) << 24) | R.epoch;
@@ -1760,7 +1791,234 @@ k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
     const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
     const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
     const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
-    R.canvas[p].lo = (lo & ~0xFFFFFFULL) | (r8 << 16) | (g8 << 8) | b8;
+    const unsigned rgb = (r8 << 16) | (g8 << 8) | b8;
+    if (CHECK) {
+      /* the FP32 colour, where it was certain, must be this one */
+      const unsigned f = R.shade_check[p];
+      if ((f >> 24) && (f & 0xFFFFFFu) != rgb) atomicAdd(checks + 5, 1u);
+    }
+    R.canvas[p].lo = (lo & ~0xFFFFFFULL) | rgb;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* single-precision shading with certified bounds                       */
+/* ------------------------------------------------------------------ */
+/*
+ * The colour of a won pixel is (unsigned char)(int)(max(0.15, |n . L|) c)
+ * per channel (render.c:137-159), with n the normalised blend of the three
+ * vertex normals (normal.c:6-43: normalised sums of area-weighted face
+ * normals).  Only the truncated integers matter, so the whole chain runs in
+ * FP32 with a bound on every quantity's distance to the reference's FP64
+ * value, and a pixel is settled here when each channel's truncation is
+ * certain; the others go through the FP64 passes (k_request, k_wn, k_shade).
+ */
+
+/* |a - b| bound of a product of bounded factors, plus its rounding */
+__device__ __forceinline__ float prod_err(float a, float ea, float b, float eb) {
+  return fabsf(a) * eb + ea * fabsf(b) + ea * eb + kU32 * fabsf(a * b);
+}
+
+/*
+ * One thread per requested triangle: its area-weighted face normal in FP32.
+ * The reference's area * unit normal equals the cross product of two edges
+ * up to a few FP64 ulps; the vertices are taken relative to the cell's corner
+ * 0 (offsets from the rounded node spacings, interpolation as in vertex_q),
+ * so the edge vectors keep their relative accuracy.  w: the largest bound of
+ * the three components (infinite when none can be given).
+ */
+template <typename T>
+__global__ void __launch_bounds__(256) k_wn_f(Geo G, TriDev tri, RasterDev R) {
+  const unsigned long long n = *R.need_count;
+  const FieldDev& F = G.F;
+  const T* fd = static_cast<const T*>(F.data);
+  float e_vt;
+  const float vt = value_f(F.threshold, e_vt);
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned u = R.need[q];
+    const unsigned tc = G.tri_cell[u];
+    const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
+    unsigned ui, uj, ukl;
+    cell_ijk(F, c, ui, uj, ukl);
+    const long long i = ui, j = uj, k = G.S.kfirst + ukl;
+    const unsigned long long e = __ldg(G.lut + G.codes[c] * 12 + r);
+    const float sp[3] = {__ldg(F.dgx + i), __ldg(F.dgy + j), __ldg(F.dgz + k)};
+    const long long base = (k * F.ny + j) * F.nx + i;
+    float rv[3][3], er[3][3];
+    bool ok = true;
+#pragma unroll
+    for (int v = 0; v < 3; v++) {
+      const unsigned a = (unsigned)((e >> (6 * v)) & 7), b = (unsigned)((e >> (6 * v + 3)) & 7);
+      const long long ia = base + (a & 1u) + ((a >> 1) & 1u) * F.nx + (long long)(a >> 2) * F.nx * F.ny;
+      const long long ib = base + (b & 1u) + ((b >> 1) & 1u) * F.nx + (long long)(b >> 2) * F.nx * F.ny;
+      float f = 0.f, e_f = 0.f;
+      if (interp_param(F.threshold, vt, e_vt, __ldg(fd + ia), __ldg(fd + ib), f, e_f) < 0) ok = false;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        /* corner offsets from corner 0 along axis d: the rounded spacing or 0 */
+        const float oa = ((a >> d) & 1u) ? sp[d] : 0.f, ob = ((b >> d) & 1u) ? sp[d] : 0.f;
+        const float dd = ob - oa;
+        const float p = oa + f * dd;
+        rv[v][d] = p;
+        er[v][d] = 1.1f * (1.01f * kU32 * (fabsf(oa) + fabsf(f) * (fabsf(oa) + fabsf(ob))) + e_f * fabsf(dd) +
+                           kU32 * (2.2f * fabsf(f * dd) + fabsf(p))) +
+                   F.coord_eps;
+      }
+    }
+    /* edges from vertex 0 and their cross product (triangulate.c:75-93) */
+    float x1[3], x2[3], e1[3], e2[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      x1[d] = rv[1][d] - rv[0][d];
+      x2[d] = rv[2][d] - rv[0][d];
+      e1[d] = er[1][d] + er[0][d] + kU32 * fabsf(x1[d]);
+      e2[d] = er[2][d] + er[0][d] + kU32 * fabsf(x2[d]);
+    }
+    float C[3], eC = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+      const float p1 = x1[d1] * x2[d2], p2 = x1[d2] * x2[d1];
+      C[d] = p1 - p2;
+      const float ec = prod_err(x1[d1], e1[d1], x2[d2], e2[d2]) + prod_err(x1[d2], e1[d2], x2[d1], e2[d1]) +
+                       kU32 * fabsf(C[d]);
+      eC = fmaxf(eC, 1.1f * ec + 1e-15f * (fabsf(p1) + fabsf(p2)));
+    }
+    /* a zero cross product (area exactly 0, also by FP64 underflow) makes the
+       reference's weighted normal 0 * (0 * inf) = NaN, which propagates to the
+       pixel: unless some component is certainly away from 0, the triangle is
+       left to the FP64 passes (a small but nonzero one only adds its small
+       absolute bound) */
+    const float cmax = fmaxf(fabsf(C[0]), fmaxf(fabsf(C[1]), fabsf(C[2])));
+    if (!ok || !isfinite(cmax) || !isfinite(eC) || !(cmax - eC > 1e-30f)) eC = INFINITY;
+    tri.wnf[u] = make_float4(C[0], C[1], C[2], eC);
+  }
+}
+
+/* bound on |A / |A| - B / |B||, componentwise, from a componentwise bound e
+   on |A - B| with |A| = len computed in FP32; infinite when |A| is too small */
+__device__ __forceinline__ float unit_err(float len, float e) {
+  const float ee = 1.7321f * e; /* Euclidean */
+  if (!(len > 4.f * ee) || !(len > 1e-30f)) return INFINITY;
+  return 2.f * ee / (len - ee) + 4.f * kU32;
+}
+
+/* one won pixel: the reference's colour in FP32 with bounds; false when a
+   channel's truncation is not certain */
+__device__ __forceinline__ bool shade_f(const Geo& G, const SceneDev& scene, const TriDev& tri, const RasterDev& R,
+                                        long long p, long long t, unsigned rgb_in, unsigned& rgb_out) {
+  const unsigned long long lo = R.canvas[p].lo;
+  const unsigned long long tag = ((lo >> 24) << 24) | R.epoch;
+  const ulonglong2 k0 = R.winfo[3 * p], k1 = R.winfo[3 * p + 1], k2 = R.winfo[3 * p + 2];
+  if (!(k0.y == tag && k1.y == tag && k2.y == tag)) return false;
+  float w[3], ew[3];
+  const ulonglong2 kk[3] = {k0, k1, k2};
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    w[m] = to_f(__longlong_as_double((long long)kk[m].x));
+    ew[m] = 2.f * kU32 * fabsf(w[m]) + 1e-37f;
+  }
+  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
+  const unsigned meta = tri.meta[t];
+  const long long c = G.tri_cell[t] & kTcCellMask;
+  float M[3] = {0.f, 0.f, 0.f}, eM = 0.f, wsum = 0.f;
+#pragma unroll 1
+  for (int m = 0; m < 3; m++) {
+    /* vertex normal: the normalised sum over the triangles around the edge (normal.c:78-158) */
+    const int ed = (meta >> (5 * m)) & 31;
+    float S[3] = {0.f, 0.f, 0.f}, eS = 0.f, asum = 0.f;
+    int cnt = 0;
+    const int nn = c_nb_count[ed];
+    for (int q = 0; q < nn; q++) {
+      const long long nc = c + (long long)c_nb[ed][q][0] * ncx * ncy + (long long)c_nb[ed][q][1] * ncx +
+                           (long long)c_nb[ed][q][2];
+      const unsigned le = (unsigned)c_nb[ed][q][3];
+      const unsigned u0 = G.offsets[nc], u1 = G.offsets[nc + 1];
+      for (unsigned u = u0; u < u1; u++) {
+        const unsigned om = tri.meta[u];
+        if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
+          const float4 wn = tri.wnf[u];
+          S[0] += wn.x;
+          S[1] += wn.y;
+          S[2] += wn.z;
+          eS += wn.w;
+          asum += fabsf(wn.x) + fabsf(wn.y) + fabsf(wn.z);
+          cnt++;
+        }
+      }
+    }
+    eS += (float)(cnt + 1) * kU32 * asum + 1e-15f * asum; /* FP32 and the reference's FP64 summation */
+    const float len = sqrtf(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+    const float en = unit_err(len, eS);
+    if (!isfinite(en)) return false;
+    const float il = 1.f / len;
+#pragma unroll
+    for (int d = 0; d < 3; d++) M[d] += w[m] * (S[d] * il);
+    eM += ew[m] * 1.01f + fabsf(w[m]) * en;
+    wsum += fabsf(w[m]);
+  }
+  eM += 4.f * kU32 * wsum * 1.01f;
+  const float lenM = sqrtf(M[0] * M[0] + M[1] * M[1] + M[2] * M[2]);
+  const float eN = unit_err(lenM, eM);
+  if (!isfinite(eN)) return false;
+  const float iM = 1.f / lenM;
+  const float* L = scene.f_light;
+  const float dotv = (M[0] * iM) * L[0] + (M[1] * iM) * L[1] + (M[2] * iM) * L[2];
+  const float l1 = fabsf(L[0]) + fabsf(L[1]) + fabsf(L[2]);
+  /* the unit vector's bound, the light's rounding to float, and the dot
+     product's rounding (bounded by the sum of |n_i L_i| <= l1 (1 + eN)) */
+  const float ed = eN * l1 + 5.f * kU32 * (1.f + eN) * l1 + 1e-30f;
+  const float alo = fmaxf(0.f, fabsf(dotv) - ed), ahi = fabsf(dotv) + ed;
+  /* factor = max(0.15, |d|): certainly clamped, certainly not, or undecided */
+  const bool clamped = ahi < 0.149999f, free = alo > 0.150001f;
+  if (clamped) {
+    rgb_out = R.clamp_rgb;
+    return true;
+  }
+  if (!free) return false;
+  unsigned out = 0;
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    const float cc = (float)((rgb_in >> (16 - 8 * ch)) & 255u);
+    const float xl = alo * cc * (1.f - 4.f * kU32), xh = ahi * cc * (1.f + 4.f * kU32);
+    const float fl = floorf(xl);
+    if (floorf(xh) != fl || !(xl >= 0.f)) return false;
+    out |= ((unsigned)(int)fl & 255u) << (16 - 8 * ch);
+  }
+  rgb_out = out;
+  return true;
+}
+
+/*
+ * One thread per won pixel: the colour when the FP32 chain settles it, else
+ * the pixel is listed for the FP64 passes.  Self-check: every pixel is
+ * listed, and the FP32 colour is kept for the FP64 pass to compare.
+ */
+template <bool CHECK>
+__global__ void __launch_bounds__(256) k_shade_f(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
+  const unsigned long long n = *R.win_count;
+  for (unsigned long long base = blockIdx.x * (unsigned long long)blockDim.x; base < n;
+       base += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long q = base + threadIdx.x;
+    bool listed = false;
+    uint2 wp = make_uint2(0u, 0u);
+    if (q < n) {
+      wp = R.win[q];
+      unsigned rgb = 0;
+      const bool sure = shade_f(G, scene, tri, R, wp.x, wp.y, rgb_in, rgb);
+      if (CHECK) {
+        R.shade_check[wp.x] = sure ? (1u << 24) | rgb : 0u;
+        listed = true;
+      } else if (sure) {
+        const unsigned long long lo = R.canvas[wp.x].lo;
+        R.canvas[wp.x].lo = (lo & ~0xFFFFFFULL) | rgb;
+      } else {
+        listed = true;
+      }
+    }
+    const unsigned long long a = block_reserve<256>(R.amb_count, listed);
+    if (listed) R.amb[a] = wp; /* a < n <= the list's capacity */
   }
 }
 
@@ -1997,14 +2255,31 @@ void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, con
 
 void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
                     const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
-                    cudaEvent_t between, cudaStream_t st) {
+                    unsigned* checks, cudaEvent_t between, cudaStream_t st) {
   (void)tri_bound;
   const long long npx = scene.width * scene.height;
-  k_winners<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, total, tri, R, order_base);
-  k_request<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, tri, R);
-  k_wn<<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
+  const int gp = grid_for(npx, 256, 8);
+  k_winners<<<gp, 256, 0, st>>>(G, scene, total, tri, R, order_base);
+  if (!G.F.dgx) {
+    /* no single-precision shading (non-Cartesian nodes): FP64 throughout */
+    k_request<<<gp, 256, 0, st>>>(G, tri, R, R.win, R.win_count, 2u, R.need_count);
+    k_wn<<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R, R.need_count);
+    if (between) cudaEventRecord(between, st);
+    k_shade<false><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb, R.win, R.win_count, checks);
+    return;
+  }
+  /* FP32 weighted normals and colours; the pixels they cannot settle again
+     through FP64 weighted normals and colours (the request list is reused) */
+  k_request<<<gp, 256, 0, st>>>(G, tri, R, R.win, R.win_count, 1u, R.need_count);
+  if (G.F.is_f32) k_wn_f<float><<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
+  else k_wn_f<double><<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
   if (between) cudaEventRecord(between, st);
-  k_shade<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, scene, tri, R, rgb);
+  if (R.shade_check) k_shade_f<true><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb);
+  else k_shade_f<false><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb);
+  k_request<<<gp, 256, 0, st>>>(G, tri, R, R.amb, R.amb_count, 2u, R.need64_count);
+  k_wn<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, tri, R, R.need64_count);
+  if (R.shade_check) k_shade<true><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb, R.amb, R.amb_count, checks);
+  else k_shade<false><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb, R.amb, R.amb_count, checks);
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,

@@ -125,6 +125,9 @@ static SceneDev scene_dev(const HostScene &s) {
   d.f_ay = (float)(h_dot(cc, ly) / d.lyy);
   d.f_by = (float)(dq / d.lyy);
   d.f_dq = (float)dq;
+  d.f_light[0] = (float)s.light.x;
+  d.f_light[1] = (float)s.light.y;
+  d.f_light[2] = (float)s.light.z;
   /* emission order is z-major: when the view points down z, high slices are near */
   d.z_descending = (s.center.z - s.cam.z) < 0. ? 1 : 0;
   return d;
@@ -353,7 +356,7 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
-  Buf zlo, xyf, cand, live, tiny, win, need, checks, voffsets, verts, winfo;
+  Buf zlo, xyf, cand, live, tiny, win, need, checks, voffsets, verts, winfo, amb, shade_check;
   unsigned long long epoch = 0; /* frame counter for the winner-weight tags (1 .. 2^24 - 1) */
   HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
   cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
@@ -470,11 +473,11 @@ struct FrameOut {
 
 /* device counters of one slab's raster passes: candidates, tiny triangles,
    won pixels, requested normals, listed triangles, surviving candidates,
-   slivers */
-static const int kCounters = 7;
+   slivers, pixels shaded in FP64, their FP64 normal requests */
+static const int kCounters = 9;
 
 /* bytes per triangle of the slab arrays (see TriDev) */
-static const size_t kTriBytes = 3 * sizeof(double) + 48 + 2 * sizeof(unsigned);
+static const size_t kTriBytes = 3 * sizeof(double) + 48 + 16 + 2 * sizeof(unsigned);
 /* doubles per triangle of the inspection arrays: vertices, vertex normals, face normal, area */
 static const size_t kDbgDoubles = 22;
 
@@ -483,7 +486,8 @@ static TriDev tri_layout(void *base, size_t cap, double *dbg) {
   double *d = static_cast<double *>(base);
   for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
   t.rec = reinterpret_cast<float4 *>(d + 3 * cap);
-  t.meta = reinterpret_cast<unsigned *>(t.rec + 3 * cap);
+  t.wnf = t.rec + 3 * cap;
+  t.meta = reinterpret_cast<unsigned *>(t.wnf + cap);
   t.need = t.meta + cap;
   for (int q = 0; q < 9; q++) t.vert[q] = dbg ? dbg + q * cap : nullptr;
   for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + (9 + q) * cap : nullptr;
@@ -522,20 +526,35 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     dfield = c.field.p;
   }
   /* node coordinates, and their float roundings for the single-precision filter */
+  /* node coordinates, their float roundings, and the node spacings g[i + 1] -
+     g[i] rounded to float (single-precision shading) */
   const size_t ng = (size_t)(nx + ny + nz);
-  if (c.grids.ensure(sizeof(double) * ng + sizeof(float) * ng, st)) return 1;
+  const size_t gbytes = sizeof(double) * ng + sizeof(float) * (2 * ng - 3);
+  if (c.grids.ensure(gbytes, st)) return 1;
   double *g = c.grids.as<double>();
   float *gf = reinterpret_cast<float *>(g + ng);
+  float *gd = gf + ng;
   /* the previous upload from the staging buffer must have left it */
   C3D_CUDA(cudaEventSynchronize(c.ev_staged));
-  if (c.h_grids.ensure(sizeof(double) * ng + sizeof(float) * ng)) return 1;
+  if (c.h_grids.ensure(gbytes)) return 1;
   double *hg = c.h_grids.as<double>();
   float *hgf = reinterpret_cast<float *>(hg + ng);
+  float *hgd = hgf + ng;
   memcpy(hg, ci.grid[0], sizeof(double) * nx);
   memcpy(hg + nx, ci.grid[1], sizeof(double) * ny);
   memcpy(hg + nx + ny, ci.grid[2], sizeof(double) * nz);
   for (size_t q = 0; q < ng; q++) hgf[q] = (float)hg[q];
-  C3D_CUDA(cudaMemcpyAsync(g, hg, sizeof(double) * ng + sizeof(float) * ng, cudaMemcpyHostToDevice, st));
+  double coord_max = 0.;
+  {
+    const long long n3[3] = {nx, ny, nz};
+    size_t at = 0, out = 0;
+    for (int d = 0; d < 3; d++) {
+      for (long long q = 0; q + 1 < n3[d]; q++) hgd[out++] = (float)(hg[at + q + 1] - hg[at + q]);
+      for (long long q = 0; q < n3[d]; q++) coord_max = std::max(coord_max, std::fabs(hg[at + q]));
+      at += (size_t)n3[d];
+    }
+  }
+  C3D_CUDA(cudaMemcpyAsync(g, hg, gbytes, cudaMemcpyHostToDevice, st));
   C3D_CUDA(cudaEventRecord(c.ev_staged, st));
   const double *dnodes = nullptr;
   std::vector<double> nodes;
@@ -573,6 +592,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
   F.div_cx = make_fast_div((unsigned)(nx - 1));
   F.div_cy = make_fast_div((unsigned)(ny - 1));
+  /* single-precision shading needs Cartesian nodes and finite coordinates */
+  const bool fp32_shading = dnodes == nullptr && std::isfinite(coord_max) && coord_max < 1e30;
+  F.dgx = fp32_shading ? gd : nullptr;
+  F.dgy = fp32_shading ? gd + (nx - 1) : nullptr;
+  F.dgz = fp32_shading ? gd + (nx - 1) + (ny - 1) : nullptr;
+  /* the reference's vertex p0 + f (p1 - p0) and its differences carry FP64
+     rounding of a few 2^-53 |coordinate|: 1e-15 covers it */
+  F.coord_eps = (float)(1e-15 * coord_max) + 1e-37f;
   set_float_threshold(F);
   c.stats.cells += (uint64_t)(ncx * ncy * ncz);
 
@@ -701,7 +728,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
          an idempotent maximum, so repeating them is harmless).  The cover
          list holds at most one entry per triangle and cannot overflow. */
       const size_t npx = (size_t)(sd.width * sd.height);
-      if (c.win.ensure(sizeof(uint2) * npx, st) || c.need.ensure(sizeof(unsigned) * T, st)) return 1;
+      if (c.win.ensure(sizeof(uint2) * npx, st) || c.amb.ensure(sizeof(uint2) * npx, st) ||
+          c.need.ensure(sizeof(unsigned) * T, st))
+        return 1;
+      if (c.filter_check && c.shade_check.ensure(sizeof(unsigned) * npx, st)) return 1;
       unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
       unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
       RasterDev RS = R;
@@ -715,6 +745,17 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       RS.live_count = counters + 5;
       RS.sliver_count = counters + 6;
       RS.sliver_rec = tri.rec + 3 * (cap - 1);
+      RS.amb = c.amb.as<uint2>();
+      RS.amb_count = counters + 7;
+      RS.need64_count = counters + 8;
+      {
+        /* render.c:150-159 at the clamped factor: (unsigned char)(int)(0.15 * c) in FP64 */
+        const int r8 = (int)(0.15 * (double)ci.color.r), g8 = (int)(0.15 * (double)ci.color.g),
+                  b8 = (int)(0.15 * (double)ci.color.b);
+        RS.clamp_rgb = ((unsigned)(unsigned char)r8 << 16) | ((unsigned)(unsigned char)g8 << 8) |
+                       (unsigned)(unsigned char)b8;
+      }
+      RS.shade_check = c.filter_check ? c.shade_check.as<unsigned>() : nullptr;
       for (int attempt = 0;; attempt++) {
         if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.live.ensure(sizeof(Candidate) * cand_want, st) ||
             c.tiny.ensure(sizeof(unsigned) * tiny_want, st))
@@ -743,10 +784,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* shading runs before the overflow check: when a list overflowed, the
            whole stage runs again, and the repeated z-buffer maxima and
            colours are the same values */
-        launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, c.stage_timing ? c.evs[10] : nullptr,
-                       st);
+        launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, checks,
+                       c.stage_timing ? c.evs[10] : nullptr, st);
         if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-        c.stats.kernel_launches += 10;
+        c.stats.kernel_launches += F.dgx ? 13 : 10;
         C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         C3D_CUDA(cudaStreamSynchronize(st));
         if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
@@ -765,6 +806,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.cover_triangles += h_cnt[4];
       c.stats.exact_fragments += h_cnt[5];
       c.stats.slivers += h_cnt[6];
+      c.stats.shade_exact += h_cnt[7];
       if (c.stage_timing) {
         c.stats.ms_vertices += elapsed(c.evs[3], c.evs[8]);
         c.stats.ms_emit += elapsed(c.evs[9], c.evs[4]);
@@ -931,13 +973,14 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     C3D_CUDA(cudaMemcpyAsync(c.h_slots.p, c.canvas.p, sizeof(Slot) * npx, cudaMemcpyDeviceToHost, st));
   }
   C3D_CUDA(cudaEventRecord(c.ev1, st));
-  unsigned h_checks[5] = {0, 0, 0, 0, 0};
+  unsigned h_checks[6] = {0, 0, 0, 0, 0, 0};
   if (c.filter_check)
     C3D_CUDA(cudaMemcpyAsync(h_checks, c.checks.p, sizeof h_checks, cudaMemcpyDeviceToHost, st));
   C3D_CUDA(cudaStreamSynchronize(st));
   C3D_CUDA(cudaGetLastError());
   c.stats.ms_total = elapsed(c.ev0, c.ev1);
   for (int q = 0; q < 5; q++) c.stats.filter_violations[q] = h_checks[q];
+  c.stats.shade_violations = h_checks[5];
   if (o.rgb_host) memcpy(o.rgb_host, c.h_rgb.p, 3 * npx);
   if (o.depth_host || o.pixels_host) {
     const Slot *sl = c.h_slots.as<Slot>();
@@ -1347,7 +1390,7 @@ extern "C" int contour3d_gb300_release(void) {
 
 static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need, &c.voffsets, &c.verts, &c.winfo,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need, &c.voffsets, &c.verts, &c.winfo, &c.amb, &c.shade_check,
                  &c.checks};
   /* every call of the context has completed, so its buffers go back to the
      pool in order on its own stream */

@@ -27,7 +27,8 @@ class Stats(C.Structure):
                 ("ms_emit", C.c_double), ("ms_cover", C.c_double), ("ms_exact", C.c_double),
                 ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5),
                 ("cover_triangles", C.c_uint64), ("exact_fragments", C.c_uint64), ("slivers", C.c_uint64),
-                ("vertices", C.c_uint64), ("ms_vertices", C.c_double), ("ms_normals", C.c_double)]
+                ("vertices", C.c_uint64), ("ms_vertices", C.c_double), ("ms_normals", C.c_double),
+                ("shade_exact", C.c_uint64), ("shade_violations", C.c_uint64)]
 
 
 class Field(C.Structure):

@@ -198,7 +198,9 @@ typedef struct {
   uint64_t vertices;          /* crossed edges whose screen position was computed (all slabs) */
   double ms_vertices;         /* stage timing: triangle -> cell map and screen vertices */
   double ms_normals;          /* stage timing: won pixels, normal requests, weighted normals
-                                 (ms_shade is then the colour pass alone) */
+                                 (ms_shade is then the colour passes) */
+  uint64_t shade_exact;       /* won pixels whose colour the FP32 shading could not settle (shaded in FP64) */
+  uint64_t shade_violations;  /* self-check: FP32 colours that differ from the FP64 ones (must stay 0) */
 } contour3d_gb300_stats_t;
 
 int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);

@@ -168,6 +168,7 @@ def test_single_precision_filter_bounds_hold(gpu, name):
     finally:
         gpu.set_filter_check(False)
     assert list(st.filter_violations) == [0, 0, 0, 0, 0]
+    assert st.shade_violations == 0, "an FP32 colour differs from the FP64 one"
     if name == "config0":
         assert sha(img.tobytes()) == MANIFEST["config0"]["ppm_sha256"]
     else:
@@ -181,6 +182,8 @@ def test_filter_settles_most_fragments(gpu):
     st = gpu.stats()
     assert st.candidate_overflows == 0
     assert 0 < st.candidates < 4 * st.triangles
+    # the FP32 shading settles all but a small share of the won pixels
+    assert st.winners > 0 and st.shade_exact < 0.05 * st.winners
 
 
 def test_float32_field_threshold_edges(gpu, oracle):
