@@ -47,10 +47,10 @@ CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
 # kernel on the 256^3 case (profiles/*_fourier256_f64.md); the full-size
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
-    "classify": (8.9, "cells"),     # k_classify: 147.8 MB for 16.6 M cells
-    "scan": (6.5, "cells"),         # k_scan: 107.6 MB for 16.6 M cells
-    "vertices": (39.7, "vertices"), # k_vertices: 260.1 MB for 6.55 M vertices (k_fill_tri_cell not included)
-    "emit": (54.6, "triangles"),    # k_emit: 715.8 MB for 13.1 M triangles
+    "classify": (8.77, "cells"),     # k_classify_tma: 145.6 MB for 16.6 M cells
+    "scan": (9.46, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 157.0 MB for 16.6 M cells
+    "vertices": (36.6, "vertices"),  # k_vertices: 239.6 MB for 6.55 M vertices
+    "emit": (44.8, "triangles"),     # k_emit: 586.6 MB for 13.1 M triangles
 }
 
 
