@@ -535,10 +535,21 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
     }
     __syncwarp();
     unsigned* dst = half == 0 ? offsets : voffsets;
+    if (wbase + 32 * kScanItems <= n) {
+      /* the warp's 1024 cells: each store instruction writes 512 contiguous
+         bytes (lane L: cells 4L .. 4L + 3 of a 128-cell chunk, all in one
+         staged row; wbase is a multiple of 1024, dst 256-byte aligned) */
 #pragma unroll 4
-    for (int k = 0; k < 32; k++) {
-      const long long c = wbase + 32 * k + lane;
-      if (c < n) dst[c] = stage[kStagePitch * k + lane];
+      for (int k = 0; k < 8; k++) {
+        const int e = 128 * k + 4 * lane, row = e >> 5, col = e & 31;
+        const unsigned* sr = stage + kStagePitch * row + col;
+        reinterpret_cast<uint4*>(dst + wbase)[32 * k + lane] = make_uint4(sr[0], sr[1], sr[2], sr[3]);
+      }
+    } else {
+      for (int k = 0; k < 32; k++) {
+        const long long c = wbase + 32 * k + lane;
+        if (c < n) dst[c] = stage[kStagePitch * k + lane];
+      }
     }
     __syncwarp();
   }
@@ -1291,7 +1302,7 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
   tri.meta[t] = meta;
 }
 
-constexpr int kEmitPer = 2; /* triangles per thread and iteration: two gather chains in flight */
+constexpr int kEmitPer = 3; /* triangles per thread and iteration: three gather chains in flight */
 
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
