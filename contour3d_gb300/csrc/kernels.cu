@@ -1361,10 +1361,13 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
  * for a triangle whose extent lies in [lo, hi].
  */
 __device__ __forceinline__ void reference_box(float lo, float hi, long long n, long long& a, long long& b) {
+  /* in [-4, n + 4] the FP32 values are within 2u n + u of the exact ones:
+     floor / ceil past a margin of 3u n hold the truncated bounds; NaN gives
+     the whole axis */
   const float fa = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + lo) * (float)n - 1.f));
   const float fb = fmaxf(-4.f, fminf((float)n + 4.f, (0.5f + hi) * (float)n + 1.f));
-  /* one pixel of slack for the rounding of the FP32 products; NaN gives the whole axis */
-  const int ia = __float2int_rd(fa) - 1, ib = __float2int_ru(fb) + 1;
+  const float mg = 3.f * kU32 * (float)n + 1e-4f;
+  const int ia = __float2int_rd(fa - mg), ib = __float2int_ru(fb + mg);
   a = fa == fa ? max(0LL, (long long)ia) : 0;
   b = fb == fb ? min(n - 1, (long long)ib) : n - 1;
 }
@@ -1541,6 +1544,66 @@ k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ c
   }
 }
 
+/* |a - b| bound of a product of bounded factors, plus its rounding */
+__device__ __forceinline__ float prod_err(float a, float ea, float b, float eb) {
+  return fabsf(a) * eb + ea * fabsf(b) + ea * eb + kU32 * fabsf(a * b);
+}
+
+/*
+ * One thread per requested triangle: its area-weighted face normal in FP32.
+ * The reference's area * unit normal equals the cross product of two edges
+ * up to a few FP64 ulps; the vertices are taken relative to the cell's corner
+ * 0 (offsets from the rounded node spacings, interpolation as in vertex_q),
+ * so the edge vectors keep their relative accuracy.  w: the largest bound of
+ * the three components (infinite when none can be given).
+ */
+/*
+ * The vertices of triangle u (triangulate.c:40-73) relative to its cell's
+ * corner 0, in FP32 with a bound on each component's distance to the
+ * reference's FP64 vertex minus that corner: corner offsets from the rounded
+ * node spacings, the interpolation parameter from interp_param, and an
+ * absolute allowance (coord_eps) for the reference's own FP64 rounding.  Edge
+ * vectors formed from these keep their relative accuracy however far the
+ * cell is from the origin.  False when a vertex cannot be bounded.  Needs
+ * the spacing tables (identity converter).
+ */
+template <typename T>
+__device__ __forceinline__ bool cell_rel_vertices(const Geo& G, unsigned u, float rv[3][3], float er[3][3]) {
+  const FieldDev& F = G.F;
+  const T* fd = static_cast<const T*>(F.data);
+  float e_vt;
+  const float vt = value_f(F.threshold, e_vt);
+  const unsigned tc = G.tri_cell[u];
+  const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
+  unsigned ui, uj, ukl;
+  cell_ijk(F, c, ui, uj, ukl);
+  const long long i = ui, j = uj, k = G.S.kfirst + ukl;
+  const unsigned long long e = __ldg(G.lut + G.codes[c] * 12 + r);
+  const float sp[3] = {__ldg(F.dgx + i), __ldg(F.dgy + j), __ldg(F.dgz + k)};
+  const long long base = (k * F.ny + j) * F.nx + i;
+  bool ok = true;
+#pragma unroll
+  for (int v = 0; v < 3; v++) {
+    const unsigned a = (unsigned)((e >> (6 * v)) & 7), b = (unsigned)((e >> (6 * v + 3)) & 7);
+    const long long ia = base + (a & 1u) + ((a >> 1) & 1u) * F.nx + (long long)(a >> 2) * F.nx * F.ny;
+    const long long ib = base + (b & 1u) + ((b >> 1) & 1u) * F.nx + (long long)(b >> 2) * F.nx * F.ny;
+    float f = 0.f, e_f = 0.f;
+    if (interp_param(F.threshold, vt, e_vt, __ldg(fd + ia), __ldg(fd + ib), f, e_f) < 0) ok = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      /* corner offsets from corner 0 along axis d: the rounded spacing or 0 */
+      const float oa = ((a >> d) & 1u) ? sp[d] : 0.f, ob = ((b >> d) & 1u) ? sp[d] : 0.f;
+      const float dd = ob - oa;
+      const float p = oa + f * dd;
+      rv[v][d] = p;
+      er[v][d] = 1.1f * (1.01f * kU32 * (fabsf(oa) + fabsf(f) * (fabsf(oa) + fabsf(ob))) + e_f * fabsf(dd) +
+                         kU32 * (2.2f * fabsf(f * dd) + fabsf(p))) +
+                 F.coord_eps;
+    }
+  }
+  return ok;
+}
+
 /*
  * Slivers: triangles whose area may be clamped to +-1e-16 (render.c:108-111).
  * A covered pixel then need not lie in the triangle's extent, so the
@@ -1551,7 +1614,73 @@ k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ c
  * (k_tiny).  One thread per sliver, in a list of their own so that a warp's
  * loops over these boxes stay converged.
  */
-template <bool CHECK>
+/*
+ * The three screen edge vectors V_b - V_a of triangle t (edge k runs from
+ * vertex (k + 1) % 3 to (k + 2) % 3, as the weights of render.c:115-133)
+ * from its world edges dv (cell_rel_vertices) in the exact form
+ *   dX = b_x ((l_x . dv) - rho_x (n . dv)) / (n . q_a + n . dv),
+ *   rho_x = (X_a - a_x) / b_x = (l_x . q_a) / (n . q_a)
+ * (and the same for Y), q_a = vertex a - camera, with a bound e on each
+ * component.  A point-like triangle keeps the directions of its edges this
+ * way, where its FP32 screen vertices (bounds ~1e-7) cannot.  False when no
+ * bound can be given.
+ */
+template <typename T>
+__device__ __forceinline__ bool screen_edges(const Geo& G, const SceneDev& s, unsigned t, const float X[3],
+                                             const float Y[3], const float Z[3], float eps, float zr, float sdx[3],
+                                             float sdy[3], float sde[3]) {
+  float rv[3][3], er[3][3];
+  if (!G.F.dgx || !cell_rel_vertices<T>(G, t, rv, er)) return false;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int a = (k + 1) % 3, b = (k + 2) % 3;
+    float dv[3], edv[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      dv[d] = rv[b][d] - rv[a][d];
+      edv[d] = er[a][d] + er[b][d] + kU32 * fabsf(dv[d]);
+    }
+    float nd = 0.f, ld = 0.f, md = 0.f, e_nd = 0.f, e_ld = 0.f, e_md = 0.f, an = 0.f, al = 0.f, am = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      nd += s.f_n[d] * dv[d];
+      ld += s.f_lx[d] * dv[d];
+      md += s.f_ly[d] * dv[d];
+      e_nd += fabsf(s.f_n[d]) * edv[d];
+      e_ld += fabsf(s.f_lx[d]) * edv[d];
+      e_md += fabsf(s.f_ly[d]) * edv[d];
+      an += fabsf(s.f_n[d] * dv[d]);
+      al += fabsf(s.f_lx[d] * dv[d]);
+      am += fabsf(s.f_ly[d] * dv[d]);
+    }
+    /* the constants' rounding to float (u) and the dot products' (3u) */
+    e_nd = 1.01f * (e_nd + 4.f * kU32 * an);
+    e_ld = 1.01f * (e_ld + 4.f * kU32 * al);
+    e_md = 1.01f * (e_md + 4.f * kU32 * am);
+    const float nq = Z[a];
+    const float Dn = nq + nd;
+    const float e_Dn = 1.01f * (zr * fabsf(nq) + e_nd + kU32 * fabsf(Dn)) + 1e-37f;
+    if (!(fabsf(Dn) > 4.f * e_Dn) || !isfinite(Dn)) return false;
+    const float rx = (X[a] - s.f_ax) / s.f_bx, ry = (Y[a] - s.f_ay) / s.f_by;
+    const float e_rx = 1.01f * (eps + kU32 * (fabsf(s.f_ax) + fabsf(X[a] - s.f_ax))) / fabsf(s.f_bx) + 3.f * kU32 * fabsf(rx);
+    const float e_ry = 1.01f * (eps + kU32 * (fabsf(s.f_ay) + fabsf(Y[a] - s.f_ay))) / fabsf(s.f_by) + 3.f * kU32 * fabsf(ry);
+    const float Nx = ld - rx * nd, Ny = md - ry * nd;
+    const float e_Nx = e_ld + fabsf(rx) * e_nd + e_rx * fabsf(nd) + e_rx * e_nd + kU32 * (fabsf(ld) + 2.f * fabsf(rx * nd));
+    const float e_Ny = e_md + fabsf(ry) * e_nd + e_ry * fabsf(nd) + e_ry * e_nd + kU32 * (fabsf(md) + 2.f * fabsf(ry * nd));
+    const float iD = 1.f / Dn;
+    sdx[k] = s.f_bx * Nx * iD;
+    sdy[k] = s.f_by * Ny * iD;
+    const float rel = e_Dn / (fabsf(Dn) - e_Dn);
+    /* the reference forms V_b - V_a from two FP64 projections: 1e-15 absolute */
+    const float ex = 1.01f * fabsf(s.f_bx) * (e_Nx + fabsf(Nx) * rel) * fabsf(iD) + 5.f * kU32 * fabsf(sdx[k]) + 1e-15f;
+    const float ey = 1.01f * fabsf(s.f_by) * (e_Ny + fabsf(Ny) * rel) * fabsf(iD) + 5.f * kU32 * fabsf(sdy[k]) + 1e-15f;
+    sde[k] = fmaxf(ex, ey);
+    if (!isfinite(sde[k]) || !isfinite(sdx[k]) || !isfinite(sdy[k])) return false;
+  }
+  return true;
+}
+
+template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
   const long long n = (long long)*R.sliver_count;
@@ -1564,8 +1693,13 @@ k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
       const float4* rec = R.sliver_rec - 3 * q;
       const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
       t32 = __float_as_uint(r2.w);
-      const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w};
-      const float eps = r2.y;
+      const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
+      const float eps = r2.y, zr = r2.z;
+      int refined = 0; /* screen edges from the world edges: 0 not yet, 1 valid, -1 unavailable */
+      float sdx[3], sdy[3], sde[3];
+      /* point-like: the extent is within a few vertex bounds, the FP32 edges decide nothing */
+      const bool point = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2])) < 16.f * eps &&
+                         fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2])) < 16.f * eps;
       const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
       const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
       const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
@@ -1602,7 +1736,28 @@ k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
           const float f2 = edge_eval(E2, px, py, ep, eps, e2);
           const bool pos_out = (f0 + e0 < -tau) || (f1 + e1 < -tau) || (f2 + e2 < -tau);
           const bool neg_out = (f0 - e0 > tau) || (f1 - e1 > tau) || (f2 - e2 > tau);
-          const bool out = (!may_pos || pos_out) && (!may_neg || neg_out);
+          bool out = !point && (!may_pos || pos_out) && (!may_neg || neg_out);
+          if (!out) {
+            /* a point-like sliver: its edge directions from the world edges */
+            if (refined == 0)
+              refined = screen_edges<T>(G, scene, t32, X, Y, Z, eps, zr, sdx, sdy, sde) ? 1 : -1;
+            if (refined > 0) {
+              bool po = false, no = false;
+#pragma unroll
+              for (int k = 0; k < 3; k++) {
+                const int a = (k + 1) % 3;
+                const float ux = px - X[a], uy = py - Y[a];
+                const float eux = eps + ep + kU32 * fabsf(ux), euy = eps + ep + kU32 * fabsf(uy);
+                const float f = ux * sdy[k] - uy * sdx[k];
+                const float ef = 1.1f * (fabsf(ux) * sde[k] + eux * fabsf(sdy[k]) + eux * sde[k] + fabsf(uy) * sde[k] +
+                                         euy * fabsf(sdx[k]) + euy * sde[k] +
+                                         2.f * kU32 * (fabsf(ux * sdy[k]) + fabsf(uy * sdx[k])) + kU32 * fabsf(f));
+                po = po || (f + ef < -tau);
+                no = no || (f - ef > tau);
+              }
+              out = (!may_pos || po) && (!may_neg || no);
+            }
+          }
           if (CHECK && ex_ok) {
             double x0, x1, x2;
             if (exact_weights(ex, i, j, R.xs, R.ys, x0, x1, x2) && out) atomicAdd(checks + 2, 1u);
@@ -1825,58 +1980,14 @@ k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in, const u
  * certain; the others go through the FP64 passes (k_request, k_wn, k_shade).
  */
 
-/* |a - b| bound of a product of bounded factors, plus its rounding */
-__device__ __forceinline__ float prod_err(float a, float ea, float b, float eb) {
-  return fabsf(a) * eb + ea * fabsf(b) + ea * eb + kU32 * fabsf(a * b);
-}
-
-/*
- * One thread per requested triangle: its area-weighted face normal in FP32.
- * The reference's area * unit normal equals the cross product of two edges
- * up to a few FP64 ulps; the vertices are taken relative to the cell's corner
- * 0 (offsets from the rounded node spacings, interpolation as in vertex_q),
- * so the edge vectors keep their relative accuracy.  w: the largest bound of
- * the three components (infinite when none can be given).
- */
 template <typename T>
 __global__ void __launch_bounds__(256) k_wn_f(Geo G, TriDev tri, RasterDev R) {
   const unsigned long long n = *R.need_count;
-  const FieldDev& F = G.F;
-  const T* fd = static_cast<const T*>(F.data);
-  float e_vt;
-  const float vt = value_f(F.threshold, e_vt);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x) {
     const unsigned u = R.need[q];
-    const unsigned tc = G.tri_cell[u];
-    const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
-    unsigned ui, uj, ukl;
-    cell_ijk(F, c, ui, uj, ukl);
-    const long long i = ui, j = uj, k = G.S.kfirst + ukl;
-    const unsigned long long e = __ldg(G.lut + G.codes[c] * 12 + r);
-    const float sp[3] = {__ldg(F.dgx + i), __ldg(F.dgy + j), __ldg(F.dgz + k)};
-    const long long base = (k * F.ny + j) * F.nx + i;
     float rv[3][3], er[3][3];
-    bool ok = true;
-#pragma unroll
-    for (int v = 0; v < 3; v++) {
-      const unsigned a = (unsigned)((e >> (6 * v)) & 7), b = (unsigned)((e >> (6 * v + 3)) & 7);
-      const long long ia = base + (a & 1u) + ((a >> 1) & 1u) * F.nx + (long long)(a >> 2) * F.nx * F.ny;
-      const long long ib = base + (b & 1u) + ((b >> 1) & 1u) * F.nx + (long long)(b >> 2) * F.nx * F.ny;
-      float f = 0.f, e_f = 0.f;
-      if (interp_param(F.threshold, vt, e_vt, __ldg(fd + ia), __ldg(fd + ib), f, e_f) < 0) ok = false;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        /* corner offsets from corner 0 along axis d: the rounded spacing or 0 */
-        const float oa = ((a >> d) & 1u) ? sp[d] : 0.f, ob = ((b >> d) & 1u) ? sp[d] : 0.f;
-        const float dd = ob - oa;
-        const float p = oa + f * dd;
-        rv[v][d] = p;
-        er[v][d] = 1.1f * (1.01f * kU32 * (fabsf(oa) + fabsf(f) * (fabsf(oa) + fabsf(ob))) + e_f * fabsf(dd) +
-                           kU32 * (2.2f * fabsf(f * dd) + fabsf(p))) +
-                   F.coord_eps;
-      }
-    }
+    const bool ok = cell_rel_vertices<T>(G, u, rv, er);
     /* edges from vertex 0 and their cross product (triangulate.c:75-93) */
     float x1[3], x2[3], e1[3], e2[3];
 #pragma unroll
@@ -2244,8 +2355,13 @@ void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long*
 void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
                    unsigned* checks, cudaStream_t st) {
   const int g = grid_for(sliver_bound, 256, 8);
-  if (checks) k_sliver<true><<<g, 256, 0, st>>>(G, scene, R, checks);
-  else k_sliver<false><<<g, 256, 0, st>>>(G, scene, R, checks);
+  if (G.F.is_f32) {
+    if (checks) k_sliver<float, true><<<g, 256, 0, st>>>(G, scene, R, checks);
+    else k_sliver<float, false><<<g, 256, 0, st>>>(G, scene, R, checks);
+  } else {
+    if (checks) k_sliver<double, true><<<g, 256, 0, st>>>(G, scene, R, checks);
+    else k_sliver<double, false><<<g, 256, 0, st>>>(G, scene, R, checks);
+  }
 }
 
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
