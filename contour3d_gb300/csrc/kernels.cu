@@ -1858,7 +1858,8 @@ k_winners(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p,
 __global__ void __launch_bounds__(256)
 k_request(Geo G, TriDev tri, RasterDev R, const uint2* __restrict__ pixels, const unsigned long long* __restrict__ count,
           unsigned flag, unsigned long long* __restrict__ need_count) {
-  const unsigned long long n = *count;
+  /* one thread per (pixel, vertex): the neighbourhood of one edge each */
+  const unsigned long long n = 3 * *count;
   const unsigned ncx = (unsigned)(G.F.nx - 1), ncy = (unsigned)(G.F.ny - 1);
   const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
   /* every thread of a block runs the same number of iterations (block-wide appends) */
@@ -1867,10 +1868,12 @@ k_request(Geo G, TriDev tri, RasterDev R, const uint2* __restrict__ pixels, cons
     unsigned got[48];
     int ng = 0;
     if (q < n) {
-      const long long t = pixels[q].y;
+      const unsigned long long pq = q / 3;
+      const int m = (int)(q - 3 * pq);
+      const long long t = pixels[pq].y;
       const long long c = G.tri_cell[t] & kTcCellMask;
       const unsigned meta = tri.meta[t];
-      for (int m = 0; m < 3; m++) {
+      {
         const int e = (meta >> (5 * m)) & 31;
         const int nn = c_nb_count[e];
         for (int s = 0; s < nn; s++) {
