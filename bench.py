@@ -67,7 +67,8 @@ def parse():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-served", action="store_true")
     p.add_argument("--no-large", action="store_true", help="skip the 1536^3 f32 field")
-    p.add_argument("--workers", type=int, default=6)
+    p.add_argument("--workers", default="auto",
+                   help="worker contexts of the batched and served forms (auto: tuned for the batched frames)")
     p.add_argument("--served-rates", default="200,max",
                    help="comma-separated request rates (req/s); max = submit without waiting")
     p.add_argument("--served-requests", type=int, default=60)
@@ -187,14 +188,22 @@ def run_large(gpu, n=1536, frames=2):
 
 def run_batched(gpu, workers, nfields=64):
     """64 fields of uneven shape, each with its own levels and camera, 1024^2:
-    the plain per-frame entry point one frame at a time, then the batched form."""
+    the plain per-frame entry point one frame at a time, then the batched form
+    (worker count from the autotuner unless given)."""
     import torch
-    from contour3d_gb300 import workloads
+    from contour3d_gb300 import autotune, workloads
     fields, frames = workloads.batch_set(gpu, nfields=nfields)
     outs = [torch.empty(f.width * f.height * 3, dtype=torch.uint8, device="cuda") for f in frames]
     packs = [workloads.frame_pack(gpu, fields[f.field], f, o) for f, o in zip(frames, outs)]
-    cells = sum(len(f.levels) * (fields[f.field].shape[0] - 1) * (fields[f.field].shape[1] - 1) *
-                (fields[f.field].shape[2] - 1) for f in frames)
+    per_frame = [len(f.levels) * (fields[f.field].shape[0] - 1) * (fields[f.field].shape[1] - 1) *
+                 (fields[f.field].shape[2] - 1) for f in frames]
+    cells = sum(per_frame)
+    tuning = None
+    if workers == "auto":
+        tuning = autotune.tune_workers(gpu, packs, per_frame, [f.width * f.height for f in frames],
+                                       torch.cuda.get_device_name())
+        workers = tuning["workers"]
+    workers = int(workers)
     for p in packs[:4]:
         gpu.render_pack(p)
     gpu.render_batch(packs[:8], workers)
@@ -215,7 +224,7 @@ def run_batched(gpu, workers, nfields=64):
     batch_s = time.perf_counter() - t0
     same = all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
     return {"workload": f"{nfields} fields, dims 64..384, half f64 / half f32, 1-4 levels, own camera, 1024x1024",
-            "frames": nfields, "cell_thresholds": int(cells), "workers": workers,
+            "frames": nfields, "cell_thresholds": int(cells), "workers": workers, "tuning": tuning,
             "plain": {"cells_per_s": cells / plain_s, "frames_per_s": nfields / plain_s, "s": plain_s},
             "batched": {"cells_per_s": cells / batch_s, "frames_per_s": nfields / batch_s, "s": batch_s},
             "speedup": plain_s / batch_s, "images_identical": same}
@@ -510,8 +519,9 @@ def main():
         large = run_large(gpu)
     if rank == 0 and not args.no_batched:
         batched = run_batched(gpu, args.workers)
+    slots = batched["workers"] if batched else (6 if args.workers == "auto" else int(args.workers))
     if rank == 0 and not args.no_served:
-        served = run_served(gpu, args.workers, [0.0 if x == "max" else float(x) for x in args.served_rates.split(",")],
+        served = run_served(gpu, slots, [0.0 if x == "max" else float(x) for x in args.served_rates.split(",")],
                             args.served_requests)
 
     cpu = None
