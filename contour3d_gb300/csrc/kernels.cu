@@ -2213,9 +2213,22 @@ __global__ void k_resolve(const Slot* __restrict__ canvas, long long W, long lon
 /* ------------------------------------------------------------------ */
 /* launchers                                                           */
 /* ------------------------------------------------------------------ */
-static int g_num_sms = 0;
+/* SMs of the first device the library runs on (thread-safe one-time query) */
+static int num_sms() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 1;
+    }
+    return v;
+  }();
+  return n;
+}
+
 static int grid_for(long long n, int threads, int per_sm) {
-  if (!g_num_sms) cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, 0);
+  const int g_num_sms = num_sms();
   long long b = (n + threads - 1) / threads;
   const long long cap = (long long)g_num_sms * per_sm;
   if (b > cap) b = cap;
@@ -2231,21 +2244,20 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
   return 0;
 }
 
-/* cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link) */
+/* cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda
+   link); looked up once, thread-safely (a function-local static) */
+static PFN_cuTensorMapEncodeTiled_v12000 lookup_tensor_map_encoder() {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  cudaGetLastError();
+  return nullptr;
+}
+
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      cudaGetLastError();
-  }
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = lookup_tensor_map_encoder();
   return fn;
 }
 
