@@ -48,6 +48,9 @@ struct FieldDev {
   const float* dgy;
   const float* dgz;
   float coord_eps;
+  /* bound on the FP64 rounding of one screen coordinate in the reference's
+     projection (project.c:26-66) of a point of this block, in this scene */
+  float proj_eps;
 };
 
 /* the constants of FastDiv for d >= 1 */

@@ -766,8 +766,8 @@ __device__ __forceinline__ float corner_pos_f(const FieldDev& F, long long i, lo
  * (render.c:62-72 drops the triangle), -1 = too close to a threshold of
  * project.c:39-46.
  */
-__device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], const float eq[3], float& X, float& Y,
-                                         float& Z, float& exy, float& ez) {
+__device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], const float eq[3], float ref_eps,
+                                         float& X, float& Y, float& Z, float& exy, float& ez) {
   const float ax = fabsf(q[0]), ay = fabsf(q[1]), az = fabsf(q[2]);
   const float nq = s.f_n[0] * q[0] + s.f_n[1] * q[1] + s.f_n[2] * q[2];
   const float lq = s.f_lx[0] * q[0] + s.f_lx[1] * q[1] + s.f_lx[2] * q[2];
@@ -800,8 +800,8 @@ __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], co
   const float ery = (e_mq + fabsf(ry) * e_nq) * rin + 6.f * kU32 * fabsf(ry);
   X = s.f_ax + s.f_bx * rx;
   Y = s.f_ay + s.f_by * ry;
-  const float ex = fabsf(s.f_bx) * erx + kU32 * (fabsf(s.f_ax) + 2.f * fabsf(s.f_bx * rx) + fabsf(X)) + 1e-12f;
-  const float ey = fabsf(s.f_by) * ery + kU32 * (fabsf(s.f_ay) + 2.f * fabsf(s.f_by * ry) + fabsf(Y)) + 1e-12f;
+  const float ex = fabsf(s.f_bx) * erx + kU32 * (fabsf(s.f_ax) + 2.f * fabsf(s.f_bx * rx) + fabsf(X)) + ref_eps;
+  const float ey = fabsf(s.f_by) * ery + kU32 * (fabsf(s.f_ay) + 2.f * fabsf(s.f_by * ry) + fabsf(Y)) + ref_eps;
   exy = 1.1f * fmaxf(ex, ey);
   return 1;
 }
@@ -1163,7 +1163,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     const long long i1 = i0 + (long long)(m & 1u) + ((m >> 1) & 1u) * F.nx + (long long)(m >> 2) * F.nx * F.ny;
     const bool vok = vertex_q<T>(scene, F.threshold, vt, e_vt, xa, __ldg(fd + i0), xb, __ldg(fd + i1), ce, qv, eq);
     float X = 0.f, Y = 0.f, Z = 0.f, exy = 0.f, ez = 0.f;
-    const int st = vok ? project_f(scene, qv, eq, X, Y, Z, exy, ez) : -1;
+    const int st = vok ? project_f(scene, qv, eq, fmaxf(1e-12f, F.proj_eps), X, Y, Z, exy, ez) : -1;
     /* |Z| in [1e-8, 1e30] when the projection succeeds: __fdividef is within 2 ulp */
     const float aux = st > 0 ? 1.01f * __fdividef(ez, fabsf(Z)) : (st == 0 ? -1.f : -2.f);
     V.pos[va + e] = make_float4(X, Y, Z, __uint_as_float((bf16_up(exy) << 16) | bf16_up(aux)));
@@ -1671,9 +1671,11 @@ __device__ __forceinline__ bool screen_edges(const Geo& G, const SceneDev& s, un
     sdx[k] = s.f_bx * Nx * iD;
     sdy[k] = s.f_by * Ny * iD;
     const float rel = e_Dn / (fabsf(Dn) - e_Dn);
-    /* the reference forms V_b - V_a from two FP64 projections: 1e-15 absolute */
-    const float ex = 1.01f * fabsf(s.f_bx) * (e_Nx + fabsf(Nx) * rel) * fabsf(iD) + 5.f * kU32 * fabsf(sdx[k]) + 1e-15f;
-    const float ey = 1.01f * fabsf(s.f_by) * (e_Ny + fabsf(Ny) * rel) * fabsf(iD) + 5.f * kU32 * fabsf(sdy[k]) + 1e-15f;
+    /* the reference forms V_b - V_a from two FP64 projections, each rounded by up to proj_eps */
+    const float ex = 1.01f * fabsf(s.f_bx) * (e_Nx + fabsf(Nx) * rel) * fabsf(iD) + 5.f * kU32 * fabsf(sdx[k]) +
+                     2.f * G.F.proj_eps;
+    const float ey = 1.01f * fabsf(s.f_by) * (e_Ny + fabsf(Ny) * rel) * fabsf(iD) + 5.f * kU32 * fabsf(sdy[k]) +
+                     2.f * G.F.proj_eps;
     sde[k] = fmaxf(ex, ey);
     if (!isfinite(sde[k]) || !isfinite(sdx[k]) || !isfinite(sdy[k])) return false;
   }
@@ -1695,22 +1697,41 @@ k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
       t32 = __float_as_uint(r2.w);
       const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
       const float eps = r2.y, zr = r2.z;
-      int refined = 0; /* screen edges from the world edges: 0 not yet, 1 valid, -1 unavailable */
+      /* the screen edges from the world edges (exact form, tight bounds) */
       float sdx[3], sdy[3], sde[3];
-      /* point-like: the extent is within a few vertex bounds, the FP32 edges decide nothing */
-      const bool point = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2])) < 16.f * eps &&
-                         fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2])) < 16.f * eps;
+      const bool refined = screen_edges<T>(G, scene, t32, X, Y, Z, eps, zr, sdx, sdy, sde);
       const EdgeF E0 = edge_f(X[1], Y[1], X[2], Y[2], eps);
       const EdgeF E1 = edge_f(X[2], Y[2], X[0], Y[0], eps);
       const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], eps);
       float errA;
-      const float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
+      float A = edge_eval(E2, X[2], Y[2], eps, eps, errA);
+      if (refined) {
+        /* render.c:38-46 area from the refined edges: (V2 - V0) x (V1 - V0) */
+        const float ax_ = -sdx[1], ay_ = -sdy[1], bx_ = sdx[2], by_ = sdy[2];
+        const float p1 = ax_ * by_, p2 = ay_ * bx_;
+        A = p1 - p2;
+        errA = 1.1f * ((fabsf(ax_) + fabsf(ay_)) * sde[2] + sde[1] * (fabsf(bx_) + fabsf(by_)) +
+                       2.f * sde[1] * sde[2] + kU32 * (fabsf(p1) + fabsf(p2) + fabsf(A))) +
+               1e-15f * (fabsf(p1) + fabsf(p2)) + 1e-37f;
+      }
+      const float xlo = fminf(X[0], fminf(X[1], X[2])), xhi = fmaxf(X[0], fmaxf(X[1], X[2]));
+      const float ylo = fminf(Y[0], fminf(Y[1], Y[2])), yhi = fmaxf(Y[0], fmaxf(Y[1], Y[2]));
+      long long imin, imax, jmin, jmax;
+      /* area certainly not clamped after all: the weights are barycentric up
+         to the -1e-8 slack, so every covered pixel centre lies in the
+         triangle's extent (as in k_cover) and the per-pixel test runs over
+         that box only */
+      if (fabsf(A) - errA > 1e-15f) {
+        const float mb = eps + 1e-6f * ((xhi - xlo) + (yhi - ylo)) + 1e-12f;
+        centre_range(xlo - mb, xhi + mb, W, imin, imax);
+        centre_range(ylo - mb, yhi + mb, H, jmin, jmax);
+      } else {
+        reference_box(xlo - eps, xhi + eps, W, imin, imax);
+        reference_box(ylo - eps, yhi + eps, H, jmin, jmax);
+      }
       const float tau = 1.001e-8f * (fabsf(A) + errA + 1e-16f) + 1e-37f;
       const bool may_pos = A + errA >= 0.f; /* an area of exactly 0 is clamped to +1e-16 */
       const bool may_neg = A - errA < 0.f;
-      long long imin, imax, jmin, jmax;
-      reference_box(fminf(X[0], fminf(X[1], X[2])) - eps, fmaxf(X[0], fmaxf(X[1], X[2])) + eps, W, imin, imax);
-      reference_box(fminf(Y[0], fminf(Y[1], Y[2])) - eps, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + eps, H, jmin, jmax);
       ExactTri ex;
       bool ex_ok = false;
       if (CHECK) {
@@ -1730,33 +1751,31 @@ k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
         for (long long i = imin; i <= imax && (CHECK || !to_tiny); i++) {
           const float px = R.xsf[i];
           const float ep = 0.5f * kU32;
-          float e0, e1, e2;
-          const float f0 = edge_eval(E0, px, py, ep, eps, e0);
-          const float f1 = edge_eval(E1, px, py, ep, eps, e1);
-          const float f2 = edge_eval(E2, px, py, ep, eps, e2);
-          const bool pos_out = (f0 + e0 < -tau) || (f1 + e1 < -tau) || (f2 + e2 < -tau);
-          const bool neg_out = (f0 - e0 > tau) || (f1 - e1 > tau) || (f2 - e2 > tau);
-          bool out = !point && (!may_pos || pos_out) && (!may_neg || neg_out);
-          if (!out) {
-            /* a point-like sliver: its edge directions from the world edges */
-            if (refined == 0)
-              refined = screen_edges<T>(G, scene, t32, X, Y, Z, eps, zr, sdx, sdy, sde) ? 1 : -1;
-            if (refined > 0) {
-              bool po = false, no = false;
+          bool out;
+          if (refined) {
+            /* the edge values from the refined edges, for each possible sign of the area */
+            bool po = false, no = false;
 #pragma unroll
-              for (int k = 0; k < 3; k++) {
-                const int a = (k + 1) % 3;
-                const float ux = px - X[a], uy = py - Y[a];
-                const float eux = eps + ep + kU32 * fabsf(ux), euy = eps + ep + kU32 * fabsf(uy);
-                const float f = ux * sdy[k] - uy * sdx[k];
-                const float ef = 1.1f * (fabsf(ux) * sde[k] + eux * fabsf(sdy[k]) + eux * sde[k] + fabsf(uy) * sde[k] +
-                                         euy * fabsf(sdx[k]) + euy * sde[k] +
-                                         2.f * kU32 * (fabsf(ux * sdy[k]) + fabsf(uy * sdx[k])) + kU32 * fabsf(f));
-                po = po || (f + ef < -tau);
-                no = no || (f - ef > tau);
-              }
-              out = (!may_pos || po) && (!may_neg || no);
+            for (int k = 0; k < 3; k++) {
+              const int a = (k + 1) % 3;
+              const float ux = px - X[a], uy = py - Y[a];
+              const float eux = eps + ep + kU32 * fabsf(ux), euy = eps + ep + kU32 * fabsf(uy);
+              const float f = ux * sdy[k] - uy * sdx[k];
+              const float ef = 1.1f * (fabsf(ux) * sde[k] + eux * fabsf(sdy[k]) + eux * sde[k] + fabsf(uy) * sde[k] +
+                                       euy * fabsf(sdx[k]) + euy * sde[k] +
+                                       2.f * kU32 * (fabsf(ux * sdy[k]) + fabsf(uy * sdx[k])) + kU32 * fabsf(f));
+              po = po || (f + ef < -tau);
+              no = no || (f - ef > tau);
             }
+            out = (!may_pos || po) && (!may_neg || no);
+          } else {
+            float e0, e1, e2;
+            const float f0 = edge_eval(E0, px, py, ep, eps, e0);
+            const float f1 = edge_eval(E1, px, py, ep, eps, e1);
+            const float f2 = edge_eval(E2, px, py, ep, eps, e2);
+            const bool pos_out = (f0 + e0 < -tau) || (f1 + e1 < -tau) || (f2 + e2 < -tau);
+            const bool neg_out = (f0 - e0 > tau) || (f1 - e1 > tau) || (f2 - e2 > tau);
+            out = (!may_pos || pos_out) && (!may_neg || neg_out);
           }
           if (CHECK && ex_ok) {
             double x0, x1, x2;

@@ -133,6 +133,49 @@ static SceneDev scene_dev(const HostScene &s) {
   return d;
 }
 
+/*
+ * A bound on the FP64 rounding of one screen coordinate in project.c:26-66,
+ * for points p with |p_i| <= pmax.  The projection forms ray = p - cam,
+ * nr = n . ray, t = (d - nc) / nr, delta = cam + t ray - center and
+ * x = delta . lx / lxx.  With u = 2^-53 and P = cam + t ray the screen point,
+ * which lies between cam and p (0 < t < 1), so |P_i| <= max(|cam_i|, pmax):
+ *   nr has relative error <= 4.01 u (sum |n_i| |ray_i|) / |nr|, and |nr| > |d - nc|
+ *     because t < 1, so t has relative error <= u kappa - 2u with
+ *     kappa = 4.01 sum |n_i| (pmax + |cam_i|) / |d - nc| + 3;
+ *   t ray_i is off by <= u kappa (|P_i| + |cam_i|), the two sums by
+ *     u |P_i| + u |delta_i| with |delta_i| <= |P_i| + |center_i|;
+ *   the dot product with lx adds 3.01 u sum |delta_i lx_i|, the quotient u |x|,
+ *     and |x| <= sum |delta_i lx_i| / lxx.
+ * The common constants (d - nc, lxx) scale every point's x by the same factor
+ * and change a difference of two points only relatively; that relative
+ * error has to stay far below single precision for the bound to be used,
+ * else the bound is infinite (every single-precision decision defers).
+ */
+static float projection_rounding(const SceneDev &sd, double pmax) {
+  const double u = std::ldexp(1.0, -53);
+  const double cam[3] = {sd.cam.x, sd.cam.y, sd.cam.z}, ctr[3] = {sd.center.x, sd.center.y, sd.center.z};
+  const double n[3] = {sd.normal.x, sd.normal.y, sd.normal.z};
+  const double lx[3] = {sd.lx.x, sd.lx.y, sd.lx.z}, ly[3] = {sd.ly.x, sd.ly.y, sd.ly.z};
+  const double D = std::fabs(sd.d - sd.nc);
+  double g = 0., rel = 0.;
+  for (int i = 0; i < 3; i++) {
+    g += std::fabs(n[i]) * (pmax + std::fabs(cam[i]));
+    rel += 3. * std::fabs(n[i]) * (std::fabs(cam[i]) + std::fabs(ctr[i]));
+  }
+  rel = u * (3. + (std::fabs(sd.d) + std::fabs(sd.nc) + rel) / D);
+  const double kappa = 4.01 * g / D + 3.;
+  double sx = 0., sy = 0.;
+  for (int i = 0; i < 3; i++) {
+    const double P = std::max(std::fabs(cam[i]), pmax), dl = P + std::fabs(ctr[i]);
+    const double term = kappa * (P + std::fabs(cam[i])) + P + 5.02 * dl;
+    sx += std::fabs(lx[i]) * term;
+    sy += std::fabs(ly[i]) * term;
+  }
+  const double e = 1.2 * u * std::max(sx / sd.lxx, sy / sd.lyy);
+  if (!(D > 0.) || !(rel < 1e-9) || !std::isfinite(e) || e > 1e30) return INFINITY;
+  return (float)(e * (1. + 1e-6)) + 1e-37f;
+}
+
 /* project.c:9-67 on the host (line end points) */
 static int h_project(const HostScene &s, V p0, V *p1) {
   const V ray = h_sub(p0, s.cam);
@@ -600,6 +643,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   /* the reference's vertex p0 + f (p1 - p0) and its differences carry FP64
      rounding of a few 2^-53 |coordinate|: 1e-15 covers it */
   F.coord_eps = (float)(1e-15 * coord_max) + 1e-37f;
+  double pos_max = coord_max;
+  for (const double v : nodes) pos_max = std::max(pos_max, std::fabs(v));
+  F.proj_eps = projection_rounding(sd, pos_max);
   set_float_threshold(F);
   c.stats.cells += (uint64_t)(ncx * ncy * ncz);
 
