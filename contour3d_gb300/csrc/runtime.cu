@@ -412,6 +412,9 @@ struct Ctx {
   const void *field_src = nullptr; /* host array currently in `field` (valid within one call) */
   size_t field_bytes = 0;
   uint64_t stats_h2d = 0;
+  cudaStream_t copy_stream = nullptr;  /* host field uploads, overlapped with the slabs */
+  cudaEvent_t ev_field = nullptr;      /* the field buffer may be overwritten once this completed */
+  std::vector<cudaEvent_t> chunk_ev;   /* upload chunk s has arrived */
 };
 
 static Ctx g_ctx;
@@ -431,6 +434,8 @@ static int ctx_init(Ctx &c) {
   C3D_CUDA(cudaEventCreateWithFlags(&c.ev_staged, cudaEventDisableTiming));
   C3D_CUDA(cudaEventRecord(c.ev_staged, c.own_stream));
   for (auto &e : c.evs) C3D_CUDA(cudaEventCreate(&e));
+  C3D_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+  C3D_CUDA(cudaEventCreateWithFlags(&c.ev_field, cudaEventDisableTiming));
   std::vector<unsigned long long> lut;
   unsigned char count[256];
   build_tables(lut, count);
@@ -545,6 +550,58 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+/*
+ * The upload of one host field in z-chunks on the context's copy stream.  A
+ * copy from pageable memory returns only once the driver has staged it, so a
+ * helper thread issues the chunks in the order the slabs need them and
+ * records one event per chunk; the slab loop waits for chunk s to be issued,
+ * then makes its stream wait on the chunk's event, and the slabs compute
+ * while later chunks are still crossing the host link.
+ */
+struct FieldUpload {
+  std::thread th;
+  std::mutex mu;
+  std::condition_variable cv;
+  int issued = 0;
+  bool failed = false;
+  char what[160] = {0};
+  ~FieldUpload() {
+    if (th.joinable()) th.join();
+  }
+  void start(int device, cudaStream_t cs, std::vector<cudaEvent_t> evs, char *dst, const char *src,
+             std::vector<std::pair<size_t, size_t>> ranges) {
+    th = std::thread([this, device, cs, evs, dst, src, ranges]() {
+      cudaError_t e = cudaSetDevice(device);
+      for (size_t q = 0; q < ranges.size(); q++) {
+        const size_t a = ranges[q].first, b = ranges[q].second;
+        if (e == cudaSuccess && b > a) e = cudaMemcpyAsync(dst + a, src + a, b - a, cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess) e = cudaEventRecord(evs[q], cs);
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          if (e != cudaSuccess) {
+            failed = true;
+            snprintf(what, sizeof what, "field upload chunk %zu: %s", q, cudaGetErrorString(e));
+          } else {
+            issued = (int)q + 1;
+          }
+        }
+        cv.notify_all();
+        if (e != cudaSuccess) return;
+      }
+    });
+  }
+  /* chunk s is issued (its event recorded); false when the upload failed */
+  bool wait(int s) {
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return issued > s || failed; });
+    return !failed || issued > s;
+  }
+};
+
+/* fields at least this large are uploaded in chunks overlapped with the slabs */
+constexpr size_t kPipelineBytes = 64ull << 20;
+constexpr long long kUploadSlabs = 4;
+
 /* one contour object through all of its slabs */
 static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn &ci,
                           unsigned long long &order_base, const RasterDev &R, DebugSink *sink) {
@@ -556,12 +613,15 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   const size_t nnodes = (size_t)(nx * ny * nz);
   /* field */
   const void *dfield = ci.data;
+  bool pipelined = false; /* the field arrives in chunks while the slabs run */
   if (!ci.on_device) {
     /* objects of one call that share a host array (the reference's example
        draws two levels of one field) upload it once */
     if (!(c.field_src == ci.data && c.field_bytes == nnodes * elem && c.field.p)) {
       if (c.field.ensure(nnodes * elem, st)) return 1;
-      C3D_CUDA(cudaMemcpyAsync(c.field.p, ci.data, nnodes * elem, cudaMemcpyHostToDevice, st));
+      pipelined = sink == nullptr && nnodes * elem >= kPipelineBytes && ncz >= 4 * kUploadSlabs;
+      if (!pipelined)
+        C3D_CUDA(cudaMemcpyAsync(c.field.p, ci.data, nnodes * elem, cudaMemcpyHostToDevice, st));
       c.field_src = ci.data;
       c.field_bytes = nnodes * elem;
       c.stats_h2d += nnodes * elem;
@@ -658,6 +718,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   const unsigned long long slab_cells = std::min<unsigned long long>(c.slab_cells, (unsigned long long)kMaxSlabCells);
   long long slab_slices = (long long)(slab_cells / (unsigned long long)per_slice) - 2;
   if (slab_slices < 1) slab_slices = 1;
+  if (pipelined) slab_slices = std::min(slab_slices, (ncz - 2 + kUploadSlabs - 1) / kUploadSlabs);
   if (3 * per_slice > kMaxSlabCells) {
     log_error("z-slices of %lld cells are too large (a slab of three slices must hold at most %lld cells)",
               per_slice, kMaxSlabCells);
@@ -668,6 +729,45 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   std::vector<long long> starts;
   for (long long k0 = kr0; k0 < kr1; k0 += slab_slices) starts.push_back(k0);
   if (sd.z_descending && !want_all) std::reverse(starts.begin(), starts.end());
+  FieldUpload up;
+  if (pipelined) {
+    /* chunk s: the node slices slab s reads that earlier slabs did not; the
+       first chunk also takes the slices below (above) the first slab and the
+       last one those beyond the last slab */
+    const size_t slice = (size_t)(nx * ny) * elem;
+    std::vector<std::pair<size_t, size_t>> ranges;
+    long long done_lo = nz, done_hi = 0; /* node slices issued: [done_lo, done_hi) */
+    for (size_t q = 0; q < starts.size(); q++) {
+      const long long k0 = starts[q], k1 = std::min(k0 + slab_slices, kr1);
+      long long a = std::max(k0 - 1, 0LL), b = std::min(k1, ncz - 1) + 2; /* node slices [a, b) */
+      if (q == 0) {
+        if (sd.z_descending) b = nz; else a = 0;
+      }
+      if (q + 1 == starts.size()) {
+        if (sd.z_descending) a = 0; else b = nz;
+      }
+      long long ca = a, cb = b;
+      if (q > 0) {
+        if (sd.z_descending) { cb = std::min(b, done_lo); ca = std::min(a, cb); }
+        else { ca = std::max(a, done_hi); cb = std::max(b, ca); }
+      }
+      done_lo = std::min(done_lo, ca);
+      done_hi = std::max(done_hi, cb);
+      ranges.push_back({(size_t)ca * slice, (size_t)cb * slice});
+    }
+    while (c.chunk_ev.size() < ranges.size()) {
+      cudaEvent_t e;
+      C3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      c.chunk_ev.push_back(e);
+    }
+    /* the copies follow the buffer's allocation and every earlier reader */
+    C3D_CUDA(cudaEventRecord(c.ev_field, st));
+    C3D_CUDA(cudaStreamWaitEvent(c.copy_stream, c.ev_field, 0));
+    up.start(c.device, c.copy_stream,
+             std::vector<cudaEvent_t>(c.chunk_ev.begin(), c.chunk_ev.begin() + (long)ranges.size()),
+             static_cast<char *>(c.field.p), static_cast<const char *>(ci.data), ranges);
+  }
+  int slab_index = 0;
   unsigned *h_small = c.h_small.as<unsigned>();
   unsigned long long *h_total = reinterpret_cast<unsigned long long *>(h_small + 4);
   const unsigned rgb = ((unsigned)ci.color.r << 16) | ((unsigned)ci.color.g << 8) | ci.color.b;
@@ -695,6 +795,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2); /* triangles, vertices */
     const long long nseg = scan_segments(ncell);
     unsigned long long *seg_sums = c.tile_state.as<unsigned long long>(), *seg_base = seg_sums + nseg;
+    if (pipelined) {
+      if (!up.wait(slab_index)) {
+        log_error("%s", up.what);
+        return 1;
+      }
+      C3D_CUDA(cudaStreamWaitEvent(st, c.chunk_ev[slab_index], 0));
+    }
+    slab_index++;
     C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
     launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
@@ -1452,6 +1560,11 @@ static void ctx_release(Ctx &c) {
     cudaEventDestroy(c.ev1);
     cudaEventDestroy(c.ev_staged);
     for (auto &e : c.evs) cudaEventDestroy(e);
+    cudaStreamSynchronize(c.copy_stream);
+    cudaStreamDestroy(c.copy_stream);
+    cudaEventDestroy(c.ev_field);
+    for (auto &e : c.chunk_ev) cudaEventDestroy(e);
+    c.chunk_ev.clear();
   }
   c.ready = false;
   c.device = -1;

@@ -214,3 +214,28 @@ def test_float32_field_threshold_edges(gpu, oracle):
         ref = oracle.render(scene)
         scene.contours = []
         assert np.array_equal(out.cpu().numpy().reshape(48, 64, 3), ref)
+
+
+@pytest.mark.parametrize("camera", [(2.5, 2.0, 1.5), (0.6, 0.4, 3.0)], ids=["ascending-z", "descending-z"])
+def test_pipelined_host_upload_matches_device_field(gpu, camera):
+    """A host field large enough to be uploaded in chunks, with the slabs
+    starting as their node slices arrive (both slab orders), draws the image
+    the device-resident field draws; the second object reuses the upload."""
+    import torch
+    shape = (200, 200, 210)  # 67 MB of float64
+    dev = torch.empty(shape, dtype=torch.float64, device="cuda")
+    std = gpu.fieldgen_modes_device(dev.data_ptr(), 0, shape, 24, 1, 6, 5.0 / 6.0, 21)
+    host = dev.cpu().numpy()
+    sizes = (shape[2], shape[1], shape[0])
+    grids = [_abi.unit_grid(n) for n in sizes]
+    levels = [(0.3 * std, (250, 40, 40)), (-0.4 * std, (40, 80, 250))]
+    scene = _abi.make_scene(camera, cases.CENTRE, 320, 240)
+    out = torch.zeros(240 * 320 * 3, dtype=torch.uint8, device="cuda")
+    assert gpu.render_device(scene, [(dev.data_ptr(), 0, sizes, grids, thr, col) for thr, col in levels],
+                             out.data_ptr()) == 0
+    torch.cuda.synchronize()
+    scene.contours = [_abi.Contour(host, thr, col, grids=tuple(grids)) for thr, col in levels]
+    img = gpu.render(scene)
+    assert np.array_equal(img, out.cpu().numpy().reshape(240, 320, 3))
+    # four slabs while the first object's field arrives, one for the second
+    assert gpu.stats().slabs == 5
