@@ -74,15 +74,13 @@ struct SlabDev {
 
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {
-  double* wn[3];      /* area * face normal, where requested */
+  double* wn[3];      /* inspection: area * face normal */
   unsigned* meta;     /* edge ids (3 x 5 bits) | flags | rank in the cell */
   /* k_cover's input, the compact list of triangles that reach it (k_emit
      appends them), 3 float4 each: x0 y0 z0 x1 | y1 z1 x2 y2 | z2 err_xy
      err_z t -- FP32 screen positions and depths, the bound on |screen x, y -
      the reference's value|, the relative depth bound and the emission index */
   float4* rec;
-  unsigned* need;     /* bit 0: FP32 weighted normal requested, bit 1: FP64 one */
-  float4* wnf;        /* FP32 area-weighted face normal and the bound on each component */
   double* vert[9];    /* inspection: exact vertices */
   double* vn[9];      /* inspection: vertex normals */
   double* dbg_fn;     /* inspection: face normals, 3 per triangle */
@@ -149,13 +147,10 @@ struct RasterDev {
      atomically; shading uses them when all three tags name the final owner */
   ulonglong2* winfo;
   unsigned long long epoch; /* 1 .. 2^24 - 1, per frame */
-  uint2* win;               /* (pixel, triangle) won by the current slab */
+  unsigned* win;            /* pixels won by the object being shaded */
   unsigned long long* win_count;
-  unsigned* need;           /* triangles whose weighted normal shading needs */
-  unsigned long long* need_count;
-  uint2* amb;               /* won pixels whose FP32 colour is not certain (shaded in FP64) */
+  unsigned* amb;            /* won pixels whose FP32 colour is not certain (shaded in FP64) */
   unsigned long long* amb_count;
-  unsigned long long* need64_count; /* the FP64 requests of those, in `need` again */
   unsigned clamp_rgb;       /* the colour at the reference's factor 0.15, computed exactly */
   unsigned* shade_check;    /* self-check: per pixel, 1 << 24 | the FP32 colour when certain */
 };
@@ -211,9 +206,19 @@ void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, con
 /* winners, normal requests, weighted normals, colours; `between` (optional)
    is recorded before the colour passes; `checks` (self-check) counts FP32
    colours that differ from the FP64 ones */
-void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
-                    const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
-                    unsigned* checks, cudaEvent_t between, cudaStream_t st);
+/* after all slabs of a contour object: list the pixels it won (R.win) and
+   colour those the FP32 pass settles; the others go to R.amb */
+void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,
+                    unsigned long long obase, unsigned rgb, cudaStream_t st);
+/* the FP64 colour of npix listed pixels (count on the device): ent (ent_cap
+   entries, ent_count must start at 0), spans (3 per pixel) and wn (3 doubles
+   per entry) are scratch; when *ent_count ends above ent_cap some pixels were
+   left out and the call must be repeated with more entries */
+void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,
+                        const unsigned* pixels, const unsigned long long* count, long long npix,
+                        unsigned long long obase, unsigned long long* ent, unsigned long long ent_cap,
+                        unsigned long long* ent_count, uint2* spans, double* wn, unsigned rgb, unsigned* checks,
+                        cudaStream_t st);
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, cudaStream_t st);
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,

@@ -1567,6 +1567,24 @@ __device__ __forceinline__ float prod_err(float a, float ea, float b, float eb) 
  * cell is from the origin.  False when a vertex cannot be bounded.  Needs
  * the spacing tables (identity converter).
  */
+/* one vertex of that kind: on the edge from corner a to corner b at the
+   interpolation parameter f (bound e_f), with the rounded node spacings sp of
+   the cell */
+__device__ __forceinline__ void rel_pos(const FieldDev& F, const float sp[3], unsigned a, unsigned b, float f,
+                                        float e_f, float rv[3], float er[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    /* corner offsets from corner 0 along axis d: the rounded spacing or 0 */
+    const float oa = ((a >> d) & 1u) ? sp[d] : 0.f, ob = ((b >> d) & 1u) ? sp[d] : 0.f;
+    const float dd = ob - oa;
+    const float p = oa + f * dd;
+    rv[d] = p;
+    er[d] = 1.1f * (1.01f * kU32 * (fabsf(oa) + fabsf(f) * (fabsf(oa) + fabsf(ob))) + e_f * fabsf(dd) +
+                    kU32 * (2.2f * fabsf(f * dd) + fabsf(p))) +
+            F.coord_eps;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ bool cell_rel_vertices(const Geo& G, unsigned u, float rv[3][3], float er[3][3]) {
   const FieldDev& F = G.F;
@@ -1589,17 +1607,7 @@ __device__ __forceinline__ bool cell_rel_vertices(const Geo& G, unsigned u, floa
     const long long ib = base + (b & 1u) + ((b >> 1) & 1u) * F.nx + (long long)(b >> 2) * F.nx * F.ny;
     float f = 0.f, e_f = 0.f;
     if (interp_param(F.threshold, vt, e_vt, __ldg(fd + ia), __ldg(fd + ib), f, e_f) < 0) ok = false;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      /* corner offsets from corner 0 along axis d: the rounded spacing or 0 */
-      const float oa = ((a >> d) & 1u) ? sp[d] : 0.f, ob = ((b >> d) & 1u) ? sp[d] : 0.f;
-      const float dd = ob - oa;
-      const float p = oa + f * dd;
-      rv[v][d] = p;
-      er[v][d] = 1.1f * (1.01f * kU32 * (fabsf(oa) + fabsf(f) * (fabsf(oa) + fabsf(ob))) + e_f * fabsf(dd) +
-                         kU32 * (2.2f * fabsf(f * dd) + fabsf(p))) +
-                 F.coord_eps;
-    }
+    rel_pos(F, sp, a, b, f, e_f, rv[v], er[v]);
   }
   return ok;
 }
@@ -1834,210 +1842,97 @@ __global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev 
   }
 }
 
+/* shading (render.c:137-159, normal.c:6-165), once per contour object     */
 /* ------------------------------------------------------------------ */
-/* shading: winners, their neighbours' weighted normals, colour         */
-/* ------------------------------------------------------------------ */
-/* the pixel's owner, if one of this slab's rendered slices won it */
-__device__ __forceinline__ bool slab_owner(const Geo& G, unsigned long long lo, unsigned long long order_base,
-                                           unsigned long long T_, long long& t, long long& cl) {
+/*
+ * After all slabs of an object, every pixel the object won is shaded from the
+ * field itself: the winner's drawing order gives its cell and rank (order =
+ * base + 12 cell + rank), cell codes are recomputed from the corner values,
+ * and each vertex normal is the normalised sum of the area-weighted face
+ * normals of the triangles that share the vertex's cube edge, over the
+ * neighbour cells in the reference's order.  Four lanes take one pixel: lane
+ * m < 3 builds the normal of vertex m, lane 0 then blends them.  The FP32
+ * pass settles a pixel when each channel's truncation is certain; the
+ * others go to the FP64 pass, which repeats the reference's arithmetic in
+ * its order.
+ */
+struct WinCell {
+  long long i, j, k;
+  unsigned r;
+};
+
+/* the object's triangle that owns a pixel, from the slot's order */
+__device__ __forceinline__ bool winner_cell(const FieldDev& F, unsigned long long lo, unsigned long long obase,
+                                            WinCell& w) {
   const unsigned long long order = lo >> 24;
-  if (order < order_base) return false;
-  const unsigned long long rel = order - order_base;
-  const unsigned long long ncx = (unsigned long long)(G.F.nx - 1), ncy = (unsigned long long)(G.F.ny - 1);
-  if (rel >= 12ULL * (unsigned long long)G.S.nslices * ncx * ncy) return false;
-  const unsigned c = (unsigned)(rel / 12ULL); /* the only 64-bit division, one per pixel */
-  const unsigned r = (unsigned)(rel - 12ULL * c);
-  const long long kk = G.S.kfirst + (long long)(c / (unsigned)(ncx * ncy));
-  if (kk < G.S.krender0 || kk >= G.S.krender1) return false;
-  t = (long long)G.offsets[c] + (long long)r;
-  cl = (long long)c;
-  return (unsigned long long)t < T_;
+  const unsigned long long ncx = (unsigned long long)(F.nx - 1), ncy = (unsigned long long)(F.ny - 1);
+  const unsigned long long ncz = (unsigned long long)(F.nz - 1);
+  if (order < obase || order - obase >= 12ULL * ncx * ncy * ncz) return false;
+  const unsigned long long rel = order - obase, c = rel / 12ULL;
+  w.r = (unsigned)(rel - 12ULL * c);
+  const unsigned long long row = c / ncx;
+  w.i = (long long)(c - row * ncx);
+  w.k = (long long)(row / ncy);
+  w.j = (long long)(row - (unsigned long long)w.k * ncy);
+  return true;
 }
 
-/* one thread per pixel: list the pixels this slab won */
+/* the triangle with LUT entry e has cube edge `le` among its three */
+__device__ __forceinline__ bool uses_edge(unsigned long long e, unsigned le) {
+  return ((e >> 18) & 31) == le || ((e >> 23) & 31) == le || ((e >> 28) & 31) == le;
+}
+
+/* one thread per pixel: the pixels whose owner is one of the object's triangles */
 __global__ void __launch_bounds__(256)
-k_winners(Geo G, SceneDev scene, const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R,
-          unsigned long long order_base) {
-  const unsigned long long T_ = *total_p;
-  const long long npx = scene.width * scene.height;
+k_winners(const Slot* __restrict__ canvas, long long npx, unsigned long long obase, unsigned long long span,
+          unsigned* __restrict__ win, unsigned long long* __restrict__ win_count) {
   for (long long base = blockIdx.x * (long long)blockDim.x; base < npx; base += (long long)gridDim.x * blockDim.x) {
     const long long p = base + threadIdx.x;
-    long long t = 0, c = 0;
-    const bool won = p < npx && slab_owner(G, R.canvas[p].lo, order_base, T_, t, c);
-    const unsigned long long w = block_reserve<256>(R.win_count, won);
-    if (won) R.win[w] = make_uint2((unsigned)p, (unsigned)t);
+    bool won = false;
+    if (p < npx) {
+      const unsigned long long order = canvas[p].lo >> 24;
+      won = order >= obase && order - obase < span;
+    }
+    const unsigned long long w = block_reserve<256>(win_count, won);
+    if (won) win[w] = (unsigned)p;
   }
 }
 
 /*
- * One thread per won pixel: request the weighted normal of every triangle
- * that shares a cube edge with a vertex of the owner (normal.c:78-158
- * neighbourhoods), each triangle once; requests are appended per warp.
+ * Area-weighted face normal in FP32: the reference's area * unit normal
+ * equals the cross product of two edges up to a few FP64 ulps; with vertices
+ * relative to the cell's corner 0 the edge vectors keep their relative
+ * accuracy.  eC: the largest bound of the three components, infinite when
+ * none can be given.
  */
-__global__ void __launch_bounds__(256)
-k_request(Geo G, TriDev tri, RasterDev R, const uint2* __restrict__ pixels, const unsigned long long* __restrict__ count,
-          unsigned flag, unsigned long long* __restrict__ need_count) {
-  /* one thread per (pixel, vertex): the neighbourhood of one edge each */
-  const unsigned long long n = 3 * *count;
-  const unsigned ncx = (unsigned)(G.F.nx - 1), ncy = (unsigned)(G.F.ny - 1);
-  const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
-  /* every thread of a block runs the same number of iterations (block-wide appends) */
-  for (unsigned long long it = blockIdx.x; it < iters; it += gridDim.x) {
-    const unsigned long long q = it * blockDim.x + threadIdx.x;
-    unsigned got[48];
-    int ng = 0;
-    if (q < n) {
-      const unsigned long long pq = q / 3;
-      const int m = (int)(q - 3 * pq);
-      const long long t = pixels[pq].y;
-      const long long c = G.tri_cell[t] & kTcCellMask;
-      const unsigned meta = tri.meta[t];
-      {
-        const int e = (meta >> (5 * m)) & 31;
-        const int nn = c_nb_count[e];
-        for (int s = 0; s < nn; s++) {
-          const long long nc = c + (long long)c_nb[e][s][0] * ncx * ncy + (long long)c_nb[e][s][1] * ncx +
-                               (long long)c_nb[e][s][2];
-          const unsigned le = (unsigned)c_nb[e][s][3];
-          const unsigned u0 = G.offsets[nc], u1 = G.offsets[nc + 1];
-          for (unsigned u = u0; u < u1; u++) {
-            const unsigned om = tri.meta[u];
-            if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
-              if (!(atomicOr(tri.need + u, flag) & flag)) {
-                if (ng < 48) {
-                  got[ng++] = u;
-                } else {
-                  const unsigned long long s1 = atomicAdd(need_count, 1ULL);
-                  R.need[s1] = u;
-                }
-              }
-            }
-          }
-        }
-      }
-    }
-    const unsigned long long base = block_reserve<256>(need_count, (unsigned)ng);
-    for (int g = 0; g < ng; g++) R.need[base + g] = got[g];
-  }
-}
-
-/* one thread per requested triangle: its exact weighted normal */
-__global__ void __launch_bounds__(256)
-k_wn(Geo G, TriDev tri, RasterDev R, const unsigned long long* __restrict__ count) {
-  const unsigned long long n = *count;
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    const long long u = R.need[q];
-    d3 v[3], fn, wn;
-    double area;
-    exact_vertices(G, u, v);
-    face_normal(v, fn, area, wn);
-    tri.wn[0][u] = wn.x;
-    tri.wn[1][u] = wn.y;
-    tri.wn[2][u] = wn.z;
-  }
-}
-
-/* one thread per won pixel: vertex normals and colour (render.c:137-159) */
-template <bool CHECK>
-__global__ void __launch_bounds__(256)
-k_shade(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in, const uint2* __restrict__ pixels,
-        const unsigned long long* __restrict__ count, unsigned* __restrict__ checks) {
-  const unsigned long long n = *count;
-  const long long W = scene.width;
-  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
-  const double cr = (double)((rgb_in >> 16) & 255), cg = (double)((rgb_in >> 8) & 255),
-               cb = (double)(rgb_in & 255);
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    const uint2 wp = pixels[q];
-    const long long p = wp.x, t = wp.y;
-    const unsigned long long lo = R.canvas[p].lo;
-    const unsigned long long tag = ((lo >> 24) << 24) | R.epoch;
-    const ulonglong2 k0 = R.winfo[3 * p], k1 = R.winfo[3 * p + 1], k2 = R.winfo[3 * p + 2];
-    double w0, w1, w2;
-    if (k0.y == tag && k1.y == tag && k2.y == tag) {
-      /* the weights the winning fragment was drawn with */
-      w0 = __longlong_as_double((long long)k0.x);
-      w1 = __longlong_as_double((long long)k1.x);
-      w2 = __longlong_as_double((long long)k2.x);
-    } else {
-      /* a stale or mixed record: the same arithmetic again (render.c:102-133) */
-      d3 v[3];
-      exact_vertices(G, t, v);
-      ExactTri x;
-      const long long pj = (unsigned)p / (unsigned)W, pi = p - pj * W;
-      if (!exact_tri(scene, v, x) || !exact_weights(x, pi, pj, R.xs, R.ys, w0, w1, w2)) continue;
-    }
-    const unsigned meta = tri.meta[t];
-    const long long c = G.tri_cell[t] & kTcCellMask;
-    const d3 n0 = vertex_normal(c, meta & 31, ncx, ncy, G.offsets, tri);
-    const d3 n1 = vertex_normal(c, (meta >> 5) & 31, ncx, ncy, G.offsets, tri);
-    const d3 n2 = vertex_normal(c, (meta >> 10) & 31, ncx, ncy, G.offsets, tri);
-    const d3 nrm = v_normalise(v_add(v_mul(w0, n0), v_add(v_mul(w1, n1), v_mul(w2, n2))));
-    const double factor = fmax(0.15, fabs(v_dot(nrm, scene.light)));
-    const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
-    const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
-    const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
-    const unsigned rgb = (r8 << 16) | (g8 << 8) | b8;
-    if (CHECK) {
-      /* the FP32 colour, where it was certain, must be this one */
-      const unsigned f = R.shade_check[p];
-      if ((f >> 24) && (f & 0xFFFFFFu) != rgb) atomicAdd(checks + 5, 1u);
-    }
-    R.canvas[p].lo = (lo & ~0xFFFFFFULL) | rgb;
-  }
-}
-
-/* ------------------------------------------------------------------ */
-/* single-precision shading with certified bounds                       */
-/* ------------------------------------------------------------------ */
-/*
- * The colour of a won pixel is (unsigned char)(int)(max(0.15, |n . L|) c)
- * per channel (render.c:137-159), with n the normalised blend of the three
- * vertex normals (normal.c:6-43: normalised sums of area-weighted face
- * normals).  Only the truncated integers matter, so the whole chain runs in
- * FP32 with a bound on every quantity's distance to the reference's FP64
- * value, and a pixel is settled here when each channel's truncation is
- * certain; the others go through the FP64 passes (k_request, k_wn, k_shade).
- */
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_wn_f(Geo G, TriDev tri, RasterDev R) {
-  const unsigned long long n = *R.need_count;
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned u = R.need[q];
-    float rv[3][3], er[3][3];
-    const bool ok = cell_rel_vertices<T>(G, u, rv, er);
-    /* edges from vertex 0 and their cross product (triangulate.c:75-93) */
-    float x1[3], x2[3], e1[3], e2[3];
+__device__ __forceinline__ void tri_wn_f(bool ok, const float rv[3][3], const float er[3][3], float C[3],
+                                         float& eC) {
+  /* edges from vertex 0 and their cross product (triangulate.c:75-93) */
+  float x1[3], x2[3], e1[3], e2[3];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      x1[d] = rv[1][d] - rv[0][d];
-      x2[d] = rv[2][d] - rv[0][d];
-      e1[d] = er[1][d] + er[0][d] + kU32 * fabsf(x1[d]);
-      e2[d] = er[2][d] + er[0][d] + kU32 * fabsf(x2[d]);
-    }
-    float C[3], eC = 0.f;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
-      const float p1 = x1[d1] * x2[d2], p2 = x1[d2] * x2[d1];
-      C[d] = p1 - p2;
-      const float ec = prod_err(x1[d1], e1[d1], x2[d2], e2[d2]) + prod_err(x1[d2], e1[d2], x2[d1], e2[d1]) +
-                       kU32 * fabsf(C[d]);
-      eC = fmaxf(eC, 1.1f * ec + 1e-15f * (fabsf(p1) + fabsf(p2)));
-    }
-    /* a zero cross product (area exactly 0, also by FP64 underflow) makes the
-       reference's weighted normal 0 * (0 * inf) = NaN, which propagates to the
-       pixel: unless some component is certainly away from 0, the triangle is
-       left to the FP64 passes (a small but nonzero one only adds its small
-       absolute bound) */
-    const float cmax = fmaxf(fabsf(C[0]), fmaxf(fabsf(C[1]), fabsf(C[2])));
-    if (!ok || !isfinite(cmax) || !isfinite(eC) || !(cmax - eC > 1e-30f)) eC = INFINITY;
-    tri.wnf[u] = make_float4(C[0], C[1], C[2], eC);
+  for (int d = 0; d < 3; d++) {
+    x1[d] = rv[1][d] - rv[0][d];
+    x2[d] = rv[2][d] - rv[0][d];
+    e1[d] = er[1][d] + er[0][d] + kU32 * fabsf(x1[d]);
+    e2[d] = er[2][d] + er[0][d] + kU32 * fabsf(x2[d]);
   }
+  eC = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+    const float p1 = x1[d1] * x2[d2], p2 = x1[d2] * x2[d1];
+    C[d] = p1 - p2;
+    const float ec = prod_err(x1[d1], e1[d1], x2[d2], e2[d2]) + prod_err(x1[d2], e1[d2], x2[d1], e2[d1]) +
+                     kU32 * fabsf(C[d]);
+    eC = fmaxf(eC, 1.1f * ec + 1e-15f * (fabsf(p1) + fabsf(p2)));
+  }
+  /* a zero cross product (area exactly 0, also by FP64 underflow) makes the
+     reference's weighted normal 0 * (0 * inf) = NaN, which propagates to the
+     pixel: unless some component is certainly away from 0, the triangle is
+     left to the FP64 pass (a small but nonzero one only adds its small
+     absolute bound) */
+  const float cmax = fmaxf(fabsf(C[0]), fmaxf(fabsf(C[1]), fabsf(C[2])));
+  if (!ok || !isfinite(cmax) || !isfinite(eC) || !(cmax - eC > 1e-30f)) eC = INFINITY;
 }
 
 /* bound on |A / |A| - B / |B||, componentwise, from a componentwise bound e
@@ -2048,59 +1943,119 @@ __device__ __forceinline__ float unit_err(float len, float e) {
   return 2.f * ee / (len - ee) + 4.f * kU32;
 }
 
-/* one won pixel: the reference's colour in FP32 with bounds; false when a
+/*
+ * A double as an unevaluated float pair hi + lo, by integer operations (the
+ * FP64 pipe stays free): hi carries the top 24 significand bits (truncated),
+ * lo the next 29 rounded to 24; |hi + lo - v| <= 2^-47 |v| + 2^-126.  False
+ * for NaN, infinities and magnitudes beyond float.
+ */
+__device__ __forceinline__ bool split_f(double v, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const int ex = (int)((b >> 52) & 0x7FF);
+  hi = lo = 0.f;
+  if (ex == 0x7FF || ex - 1023 > 127) return false;
+  const int fe = ex - 1023 + 127;
+  if (fe <= 0) { /* below 2^-126: flushed */
+    hi = __uint_as_float(sign);
+    return true;
+  }
+  hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+  /* lo = rem 2^(ex - 1075), the power of two normal or split as 2^(ex - 1011) 2^-64 */
+  const float r = __uint2float_rn((unsigned)(b & 0x1FFFFFFFu));
+  const float x = ex >= 949 ? r * __uint_as_float((unsigned)(ex - 1075 + 127) << 23)
+                            : (r * __uint_as_float((unsigned)(ex - 1011 + 127) << 23)) * 5.421010862427522e-20f;
+  lo = sign ? -x : x;
+  return true;
+}
+
+/* s + t = a - b exactly (Knuth's two-sum; no fused operations in this build) */
+__device__ __forceinline__ void two_diff(float a, float b, float& s, float& t) {
+  s = a - b;
+  const float bb = s - a;
+  t = (a - (s - bb)) - (b + bb);
+}
+
+/* (ah + al) - (bh + bl) in FP32 and a bound on its distance to the
+   difference of the two doubles the pairs stand for */
+__device__ __forceinline__ float pair_diff(float ah, float al, float bh, float bl, float& e) {
+  float s, t;
+  two_diff(ah, bh, s, t);
+  const float dl = al - bl, u = t + dl, d = s + u;
+  e = 1.01f * (kU32 * (fabsf(dl) + fabsf(u) + fabsf(d)) + 1.43e-14f * (fabsf(ah) + fabsf(bh)) + 3e-38f);
+  return d;
+}
+
+/* the threshold in the forms the shading pass uses */
+struct ThrF {
+  float vt, e_vt; /* rounded to float, with its bound (float fields) */
+  float hi, lo;   /* split (double fields) */
+};
+__device__ __forceinline__ ThrF thr_f(double t) {
+  ThrF r;
+  r.vt = value_f(t, r.e_vt);
+  if (!split_f(t, r.hi, r.lo)) r.hi = r.lo = __int_as_float(0x7fc00000);
+  return r;
+}
+
+/* interp_param for the shading pass, FP32 operations only: for a double
+   field the differences are formed from float pairs (pair_diff), accurate to
+   a few float ulps of the differences themselves */
+__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, double v0, double v1, float& f,
+                                            float& e_f) {
+  float h0, l0, h1, l1;
+  if (!split_f(v0, h0, l0) || !split_f(v1, h1, l1) || th.hi != th.hi) return -1;
+  float e_dv, e_dt;
+  const float dv = pair_diff(h1, l1, h0, l0, e_dv);
+  const float adv = fabsf(dv);
+  /* triangulate.c:40-73: |v1 - v0| < 1e-8 keeps p0 */
+  if (!(adv - e_dv > 1.00001e-8f)) return adv + e_dv < 0.99999e-8f ? 0 : -1;
+  if (adv > 1e30f) return -1;
+  const float rdv = __fdividef(1.f, adv);
+  const float xr = e_dv * rdv;
+  if (!(xr < 0.01f)) return -1;
+  const float dt = pair_diff(th.hi, th.lo, h0, l0, e_dt);
+  f = __fdividef(dt, dv); /* 2 ulp */
+  const float fmax_ = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
+  e_f = 1.1f * (1.01f * (e_dt + fmax_ * e_dv) * rdv + 4.f * kU32 * fabsf(f));
+  return 1;
+}
+__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, float v0, float v1, float& f,
+                                            float& e_f) {
+  return interp_param(F.threshold, th.vt, th.e_vt, v0, v1, f, e_f);
+}
+
+/* code and corner values of cell (i, j, k) in the field's own type */
+template <typename T>
+__device__ __forceinline__ unsigned cell_code_t(const FieldDev& F, long long i, long long j, long long k, T vals[8]) {
+  const T* f = static_cast<const T*>(F.data);
+  const long long base = (k * F.ny + j) * F.nx + i;
+  unsigned code = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    vals[c] = __ldg(f + base + (c & 1) + ((c >> 1) & 1) * F.nx + (c >> 2) * F.nx * F.ny);
+    code |= (unsigned)node_above_value<T>(F, vals[c]) << c;
+  }
+  return code;
+}
+
+/* the pixel's colour from the three FP32 vertex normals: false when a
    channel's truncation is not certain */
-__device__ __forceinline__ bool shade_f(const Geo& G, const SceneDev& scene, const TriDev& tri, const RasterDev& R,
-                                        long long p, long long t, unsigned rgb_in, unsigned& rgb_out) {
-  const unsigned long long lo = R.canvas[p].lo;
+__device__ __forceinline__ bool blend_f(const SceneDev& scene, const RasterDev& R, long long p, unsigned long long lo,
+                                        const float N[3][3], const float en[3], unsigned rgb_in, unsigned& rgb_out) {
   const unsigned long long tag = ((lo >> 24) << 24) | R.epoch;
   const ulonglong2 k0 = R.winfo[3 * p], k1 = R.winfo[3 * p + 1], k2 = R.winfo[3 * p + 2];
   if (!(k0.y == tag && k1.y == tag && k2.y == tag)) return false;
-  float w[3], ew[3];
   const ulonglong2 kk[3] = {k0, k1, k2};
-#pragma unroll
-  for (int m = 0; m < 3; m++) {
-    w[m] = to_f(__longlong_as_double((long long)kk[m].x));
-    ew[m] = 2.f * kU32 * fabsf(w[m]) + 1e-37f;
-  }
-  const long long ncx = G.F.nx - 1, ncy = G.F.ny - 1;
-  const unsigned meta = tri.meta[t];
-  const long long c = G.tri_cell[t] & kTcCellMask;
   float M[3] = {0.f, 0.f, 0.f}, eM = 0.f, wsum = 0.f;
-#pragma unroll 1
-  for (int m = 0; m < 3; m++) {
-    /* vertex normal: the normalised sum over the triangles around the edge (normal.c:78-158) */
-    const int ed = (meta >> (5 * m)) & 31;
-    float S[3] = {0.f, 0.f, 0.f}, eS = 0.f, asum = 0.f;
-    int cnt = 0;
-    const int nn = c_nb_count[ed];
-    for (int q = 0; q < nn; q++) {
-      const long long nc = c + (long long)c_nb[ed][q][0] * ncx * ncy + (long long)c_nb[ed][q][1] * ncx +
-                           (long long)c_nb[ed][q][2];
-      const unsigned le = (unsigned)c_nb[ed][q][3];
-      const unsigned u0 = G.offsets[nc], u1 = G.offsets[nc + 1];
-      for (unsigned u = u0; u < u1; u++) {
-        const unsigned om = tri.meta[u];
-        if (((om & 31) == le) || (((om >> 5) & 31) == le) || (((om >> 10) & 31) == le)) {
-          const float4 wn = tri.wnf[u];
-          S[0] += wn.x;
-          S[1] += wn.y;
-          S[2] += wn.z;
-          eS += wn.w;
-          asum += fabsf(wn.x) + fabsf(wn.y) + fabsf(wn.z);
-          cnt++;
-        }
-      }
-    }
-    eS += (float)(cnt + 1) * kU32 * asum + 1e-15f * asum; /* FP32 and the reference's FP64 summation */
-    const float len = sqrtf(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
-    const float en = unit_err(len, eS);
-    if (!isfinite(en)) return false;
-    const float il = 1.f / len;
 #pragma unroll
-    for (int d = 0; d < 3; d++) M[d] += w[m] * (S[d] * il);
-    eM += ew[m] * 1.01f + fabsf(w[m]) * en;
-    wsum += fabsf(w[m]);
+  for (int m = 0; m < 3; m++) {
+    const float w = to_f(__longlong_as_double((long long)kk[m].x));
+    const float ew = 2.f * kU32 * fabsf(w) + 1e-37f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) M[d] += w * N[m][d];
+    eM += ew * 1.01f + fabsf(w) * en[m];
+    wsum += fabsf(w);
   }
   eM += 4.f * kU32 * wsum * 1.01f;
   const float lenM = sqrtf(M[0] * M[0] + M[1] * M[1] + M[2] * M[2]);
@@ -2134,35 +2089,374 @@ __device__ __forceinline__ bool shade_f(const Geo& G, const SceneDev& scene, con
   return true;
 }
 
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+/* appends each flagged lane's pixel to a list, one atomic per warp */
+__device__ __forceinline__ void warp_append(bool flag, unsigned p, unsigned* list, unsigned long long* count) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned bal = __ballot_sync(kFull, flag);
+  unsigned long long a0 = 0;
+  if (lane == 0 && bal) a0 = atomicAdd(count, (unsigned long long)__popc(bal));
+  a0 = __shfl_sync(kFull, a0, 0);
+  if (flag) list[a0 + __popc(bal & ((1u << lane) - 1u))] = p;
+}
+
 /*
- * One thread per won pixel: the colour when the FP32 chain settles it, else
- * the pixel is listed for the FP64 passes.  Self-check: every pixel is
- * listed, and the FP32 colour is kept for the FP64 pass to compare.
+ * FP32 pass over the won pixels, 64 pixels per block and iteration, four
+ * threads per pixel.  Neighbouring pixels share most of their vertices'
+ * neighbourhoods, so each block first gathers the triangles around its
+ * pixels' vertices into a shared hash of (cell, rank) keys, computes each
+ * distinct triangle's FP32 weighted normal once, then every (pixel, vertex)
+ * thread sums its triangles' normals (the bound covers any summation order)
+ * and lane 0 of each pixel blends the three.  A pixel whose neighbourhood
+ * does not fit goes to the FP64 pass.  Self-check: every pixel is listed for
+ * the FP64 pass, and the FP32 colour, where certain, is kept for it to compare.
  */
-template <bool CHECK>
-__global__ void __launch_bounds__(256) k_shade_f(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned rgb_in) {
+constexpr int kShadeHash = 1024;  /* distinct triangles per block and iteration */
+constexpr int kShadeList = 24;    /* triangles around one cube edge (at most 16) */
+constexpr unsigned long long kEmptyKey = ~0ULL;
+
+/* (cell, rank) as a hash key: i, j, k below 2^20 each, rank below 12 (never all ones) */
+__device__ __forceinline__ unsigned long long tri_key(long long i, long long j, long long k, unsigned r) {
+  return ((unsigned long long)k << 44) | ((unsigned long long)j << 24) | ((unsigned long long)i << 4) | r;
+}
+
+/* slot of `key` in the block's table (inserted when absent, fresh = true), -1 when full */
+__device__ __forceinline__ int hash_slot(unsigned long long* keys, unsigned long long key, bool& fresh) {
+  unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ULL) >> 54) & (kShadeHash - 1);
+  for (int probe = 0; probe < kShadeHash; probe++) {
+    const unsigned long long prev = atomicCAS(keys + h, kEmptyKey, key);
+    if (prev == kEmptyKey || prev == key) {
+      fresh = prev == kEmptyKey;
+      return (int)h;
+    }
+    h = (h + 1) & (kShadeHash - 1);
+  }
+  fresh = false;
+  return -1;
+}
+
+template <typename T, bool CHECK>
+__global__ void __launch_bounds__(256)
+k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __restrict__ lut,
+          unsigned long long obase, unsigned rgb_in) {
+  __shared__ unsigned long long keys[kShadeHash];
+  __shared__ float4 wnf[kShadeHash];
+  __shared__ unsigned short lists[kShadeList][256];
+  __shared__ unsigned short todo[kShadeHash];
+  __shared__ unsigned ntodo;
+  for (int q = threadIdx.x; q < kShadeHash; q += blockDim.x) keys[q] = kEmptyKey;
+  if (threadIdx.x == 0) ntodo = 0;
+  __syncthreads();
   const unsigned long long n = *R.win_count;
-  for (unsigned long long base = blockIdx.x * (unsigned long long)blockDim.x; base < n;
-       base += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned long long q = base + threadIdx.x;
-    bool listed = false;
-    uint2 wp = make_uint2(0u, 0u);
+  const unsigned tid = threadIdx.x, lane = tid & 31u, m = tid & 3u, g0 = lane & ~3u;
+  const ThrF th = thr_f(F.threshold);
+  for (unsigned long long base = blockIdx.x * 64ULL; base < n; base += gridDim.x * 64ULL) {
+    const unsigned long long q = base + tid / 4;
+    /* gather: the (cell, rank) of every triangle around this thread's vertex */
+    unsigned p = 0;
+    unsigned long long lo = 0;
+    WinCell wc;
+    bool ok = false, full = false;
+    int cnt = 0;
     if (q < n) {
-      wp = R.win[q];
+      p = R.win[q];
+      lo = R.canvas[p].lo;
+      ok = winner_cell(F, lo, obase, wc);
+    }
+    if (ok && m < 3) {
+      T cv[8];
+      const unsigned code = cell_code_t<T>(F, wc.i, wc.j, wc.k, cv);
+      const int ed = (int)((__ldg(lut + code * 12 + wc.r) >> (18 + 5 * m)) & 31);
+      const int nn = c_nb_count[ed];
+      for (int s = 0; s < nn; s++) {
+        const long long ni = wc.i + c_nb[ed][s][2], nj = wc.j + c_nb[ed][s][1], nk = wc.k + c_nb[ed][s][0];
+        const unsigned le = (unsigned)c_nb[ed][s][3];
+        const unsigned ncode = cell_code_t<T>(F, ni, nj, nk, cv);
+        const int nt = c_code_count[ncode];
+        for (int r = 0; r < nt; r++) {
+          if (!uses_edge(__ldg(lut + ncode * 12 + r), le)) continue;
+          bool fresh;
+          const int slot = hash_slot(keys, tri_key(ni, nj, nk, (unsigned)r), fresh);
+          if (slot < 0 || cnt >= kShadeList) {
+            full = true;
+            continue;
+          }
+          if (fresh) todo[atomicAdd(&ntodo, 1u)] = (unsigned short)slot;
+          lists[cnt++][tid] = (unsigned short)slot;
+        }
+      }
+    }
+    __syncthreads();
+    /* each distinct triangle's FP32 weighted normal, once */
+    const unsigned nd = ntodo;
+    for (unsigned w = tid; w < nd; w += blockDim.x) {
+      const int slot = todo[w];
+      const unsigned long long key = keys[slot];
+      const long long i = (long long)((key >> 4) & 0xFFFFFu), j = (long long)((key >> 24) & 0xFFFFFu);
+      const long long k = (long long)(key >> 44);
+      T cv[8];
+      const unsigned code = cell_code_t<T>(F, i, j, k, cv);
+      const unsigned long long e = __ldg(lut + code * 12 + (key & 15u));
+      const float sp[3] = {__ldg(F.dgx + i), __ldg(F.dgy + j), __ldg(F.dgz + k)};
+      float rv[3][3], er[3][3];
+      bool tok = true;
+#pragma unroll
+      for (int v = 0; v < 3; v++) {
+        const unsigned a = (unsigned)((e >> (6 * v)) & 7), b = (unsigned)((e >> (6 * v + 3)) & 7);
+        float f = 0.f, e_f = 0.f;
+        if (interp_shade(F, th, cv[a], cv[b], f, e_f) < 0) tok = false;
+        rel_pos(F, sp, a, b, f, e_f, rv[v], er[v]);
+      }
+      float C[3], eC;
+      tri_wn_f(tok, rv, er, C, eC);
+      wnf[slot] = make_float4(C[0], C[1], C[2], eC);
+    }
+    __syncthreads();
+    /* vertex normal: the normalised sum over the triangles around the edge (normal.c:78-158) */
+    float N[3] = {0.f, 0.f, 0.f}, en = INFINITY;
+    if (ok && m < 3 && !full) {
+      float S[3] = {0.f, 0.f, 0.f}, eS = 0.f, asum = 0.f;
+      for (int t = 0; t < cnt; t++) {
+        const float4 c = wnf[lists[t][tid]];
+        S[0] += c.x;
+        S[1] += c.y;
+        S[2] += c.z;
+        eS += c.w;
+        asum += fabsf(c.x) + fabsf(c.y) + fabsf(c.z);
+      }
+      eS += (float)(cnt + 1) * kU32 * asum + 1e-15f * asum; /* FP32 and the reference's FP64 summation */
+      const float len = sqrtf(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+      en = unit_err(len, eS);
+      if (isfinite(en)) {
+        const float il = 1.f / len;
+#pragma unroll
+        for (int d = 0; d < 3; d++) N[d] = S[d] * il;
+      }
+    }
+    float Nv[3][3], env[3];
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++) {
+#pragma unroll
+      for (int d = 0; d < 3; d++) Nv[mm][d] = __shfl_sync(kFull, N[d], g0 + mm);
+      env[mm] = __shfl_sync(kFull, en, g0 + mm);
+    }
+    bool listed = false;
+    if (ok && m == 0) {
       unsigned rgb = 0;
-      const bool sure = shade_f(G, scene, tri, R, wp.x, wp.y, rgb_in, rgb);
+      const bool sure = isfinite(env[0]) && isfinite(env[1]) && isfinite(env[2]) &&
+                        blend_f(scene, R, p, lo, Nv, env, rgb_in, rgb);
       if (CHECK) {
-        R.shade_check[wp.x] = sure ? (1u << 24) | rgb : 0u;
+        R.shade_check[p] = sure ? (1u << 24) | rgb : 0u;
         listed = true;
       } else if (sure) {
-        const unsigned long long lo = R.canvas[wp.x].lo;
-        R.canvas[wp.x].lo = (lo & ~0xFFFFFFULL) | rgb;
+        R.canvas[p].lo = (lo & ~0xFFFFFFULL) | rgb;
       } else {
         listed = true;
       }
     }
-    const unsigned long long a = block_reserve<256>(R.amb_count, listed);
-    if (listed) R.amb[a] = wp; /* a < n <= the list's capacity */
+    warp_append(listed, p, R.amb, R.amb_count); /* at most the won pixels: fits */
+    /* empty the table for the next pixels */
+    for (unsigned w = tid; w < nd; w += blockDim.x) keys[todo[w]] = kEmptyKey;
+    __syncthreads();
+    if (tid == 0) ntodo = 0;
+    __syncthreads();
+  }
+}
+
+/*
+ * FP64 pass over the pixels the FP32 pass could not settle, in three steps so
+ * that the FP64 work runs on full warps: list every (pixel, vertex)'s
+ * neighbour triangles in the reference's order, compute each listed
+ * triangle's area-weighted face normal, then sum them in that order and
+ * blend.  A list entry is (global cell) * 16 + rank.
+ */
+__device__ __forceinline__ int vertex_edge(const FieldDev& F, const unsigned long long* lut, const WinCell& wc, int m,
+                                           double vals[8], unsigned long long& e) {
+  const unsigned code = cell_code_any(F, wc.i, wc.j, wc.k, vals);
+  e = lut[code * 12 + wc.r];
+  return (int)((e >> (18 + 5 * m)) & 31);
+}
+
+/* visits the neighbour triangles around cube edge ed of cell (i, j, k) in the
+   reference's order (normal.c:78-158): fn(entry) */
+template <typename Fn>
+__device__ __forceinline__ void for_edge_triangles(const FieldDev& F, const unsigned long long* lut, long long i,
+                                                   long long j, long long k, int ed, Fn fn) {
+  const long long ncx = F.nx - 1, ncy = F.ny - 1;
+  const int nn = c_nb_count[ed];
+  for (int q = 0; q < nn; q++) {
+    const long long ni = i + c_nb[ed][q][2], nj = j + c_nb[ed][q][1], nk = k + c_nb[ed][q][0];
+    const unsigned le = (unsigned)c_nb[ed][q][3];
+    double vals[8];
+    const unsigned code = cell_code_any(F, ni, nj, nk, vals);
+    const int nt = c_code_count[code];
+    const unsigned long long cell = (unsigned long long)((nk * ncy + nj) * ncx + ni);
+    for (int r = 0; r < nt; r++)
+      if (uses_edge(lut[code * 12 + r], le)) fn(cell * 16ULL + (unsigned long long)r);
+  }
+}
+
+/* step 1: one thread per (pixel, vertex); spans[q] = (first entry, count),
+   count 0xFFFFFFFF when the entries did not fit */
+__global__ void __launch_bounds__(256)
+k_nb_list(FieldDev F, RasterDev R, const unsigned long long* __restrict__ lut_g, const unsigned* __restrict__ pixels,
+          const unsigned long long* __restrict__ count, unsigned long long obase, unsigned long long* __restrict__ ent,
+          unsigned long long ent_cap, unsigned long long* __restrict__ ent_count, uint2* __restrict__ spans) {
+  __shared__ unsigned long long lut[kLutEntries];
+  for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
+  __syncthreads();
+  const unsigned long long n = 3 * *count;
+  const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
+  /* every lane of a warp runs the same iterations (warp-wide reservations) */
+  for (unsigned long long it = blockIdx.x; it < iters; it += gridDim.x) {
+    const unsigned long long q = it * blockDim.x + threadIdx.x;
+    WinCell wc;
+    bool ok = false;
+    int ed = 0;
+    unsigned cnt = 0;
+    if (q < n) {
+      const unsigned long long pq = q / 3;
+      const int m = (int)(q - 3 * pq);
+      ok = winner_cell(F, R.canvas[pixels[pq]].lo, obase, wc);
+      if (ok) {
+        double vals[8];
+        unsigned long long e;
+        ed = vertex_edge(F, lut, wc, m, vals, e);
+        for_edge_triangles(F, lut, wc.i, wc.j, wc.k, ed, [&](unsigned long long) { cnt++; });
+      }
+    }
+    /* warp-aggregated reservation */
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned y = __shfl_up_sync(kFull, incl, d);
+      if ((int)lane >= d) incl += y;
+    }
+    unsigned long long w0 = 0;
+    if (lane == 31 && incl) w0 = atomicAdd(ent_count, (unsigned long long)incl);
+    w0 = __shfl_sync(kFull, w0, 31);
+    const unsigned long long first = w0 + (incl - cnt);
+    if (q < n) {
+      const bool fits = first + cnt <= ent_cap;
+      spans[q] = make_uint2((unsigned)first, ok && fits ? cnt : 0xFFFFFFFFu);
+      if (ok && fits) {
+        unsigned long long at = first;
+        for_edge_triangles(F, lut, wc.i, wc.j, wc.k, ed, [&](unsigned long long x) { ent[at++] = x; });
+      }
+    }
+  }
+}
+
+/* step 2: one thread per listed triangle, its exact area-weighted face normal
+   (triangulate.c:40-93, normal.c:39-40) */
+__global__ void __launch_bounds__(256)
+k_nb_wn(FieldDev F, const unsigned long long* __restrict__ lut, const unsigned long long* __restrict__ ent,
+        unsigned long long ent_cap, const unsigned long long* __restrict__ ent_count, double* __restrict__ wn_out) {
+  const unsigned long long n = min(*ent_count, ent_cap);
+  const unsigned long long ncx = (unsigned long long)(F.nx - 1), ncy = (unsigned long long)(F.ny - 1);
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+       q += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long x = ent[q], cell = x >> 4, row = cell / ncx;
+    const long long i = (long long)(cell - row * ncx), k = (long long)(row / ncy);
+    const long long j = (long long)(row - (unsigned long long)k * ncy);
+    double vals[8];
+    const unsigned code = cell_code_any(F, i, j, k, vals);
+    const unsigned long long e = __ldg(lut + code * 12 + (x & 15));
+    d3 v[3], fn, wn;
+    double area;
+#pragma unroll
+    for (int qv = 0; qv < 3; qv++) {
+      const int a = (int)((e >> (6 * qv)) & 7), b = (int)((e >> (6 * qv + 3)) & 7);
+      v[qv] = interpolate(F.threshold, corner_pos(F, i, j, k, a), vals[a], corner_pos(F, i, j, k, b), vals[b]);
+    }
+    face_normal(v, fn, area, wn);
+    wn_out[3 * q + 0] = wn.x;
+    wn_out[3 * q + 1] = wn.y;
+    wn_out[3 * q + 2] = wn.z;
+  }
+}
+
+/* step 3: four lanes per pixel; lane m < 3 sums vertex m's normals in the
+   reference's order and normalises, lane 0 blends and colours (render.c:137-159) */
+template <bool CHECK>
+__global__ void __launch_bounds__(256)
+k_shade(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __restrict__ lut,
+        const unsigned* __restrict__ pixels, const unsigned long long* __restrict__ count, unsigned long long obase,
+        const uint2* __restrict__ spans, const double* __restrict__ wn_in, unsigned rgb_in,
+        unsigned* __restrict__ checks) {
+  const unsigned long long n = *count;
+  const unsigned lane = threadIdx.x & 31u, m = lane & 3u, g0 = lane & ~3u;
+  const long long W = scene.width;
+  const double cr = (double)((rgb_in >> 16) & 255), cg = (double)((rgb_in >> 8) & 255),
+               cb = (double)(rgb_in & 255);
+  const unsigned long long step = (unsigned long long)gridDim.x * (blockDim.x / 4);
+  for (unsigned long long base = ((unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) / 4; base < n;
+       base += step) {
+    const unsigned long long q = base + lane / 4;
+    d3 nm = {0., 0., 0.};
+    int good = 1;
+    if (q < n && m < 3) {
+      const uint2 sp = spans[3 * q + m];
+      if (sp.y == 0xFFFFFFFFu) {
+        good = 0;
+      } else {
+        d3 sum = {0., 0., 0.};
+        for (unsigned t = 0; t < sp.y; t++) {
+          const double* w = wn_in + 3 * ((unsigned long long)sp.x + t);
+          sum = v_add(sum, d3{w[0], w[1], w[2]});
+        }
+        nm = v_normalise(sum);
+      }
+    }
+    d3 n3[3];
+#pragma unroll
+    for (int mm = 0; mm < 3; mm++)
+      n3[mm] = {__shfl_sync(kFull, nm.x, g0 + mm), __shfl_sync(kFull, nm.y, g0 + mm),
+                __shfl_sync(kFull, nm.z, g0 + mm)};
+    good = __shfl_sync(kFull, good, g0) & __shfl_sync(kFull, good, g0 + 1) & __shfl_sync(kFull, good, g0 + 2);
+    if (q >= n || m != 0 || !good) continue;
+    const unsigned p = pixels[q];
+    const unsigned long long lo = R.canvas[p].lo;
+    WinCell wc;
+    if (!winner_cell(F, lo, obase, wc)) continue;
+    const unsigned long long tag = ((lo >> 24) << 24) | R.epoch;
+    const ulonglong2 k0 = R.winfo[3 * p], k1 = R.winfo[3 * p + 1], k2 = R.winfo[3 * p + 2];
+    double w0, w1, w2;
+    if (k0.y == tag && k1.y == tag && k2.y == tag) {
+      /* the weights the winning fragment was drawn with */
+      w0 = __longlong_as_double((long long)k0.x);
+      w1 = __longlong_as_double((long long)k1.x);
+      w2 = __longlong_as_double((long long)k2.x);
+    } else {
+      /* a stale or mixed record: the same arithmetic again (render.c:102-133) */
+      double vals[8];
+      unsigned long long e;
+      vertex_edge(F, lut, wc, 0, vals, e);
+      d3 v[3];
+#pragma unroll
+      for (int qv = 0; qv < 3; qv++) {
+        const int a = (int)((e >> (6 * qv)) & 7), b = (int)((e >> (6 * qv + 3)) & 7);
+        v[qv] = interpolate(F.threshold, corner_pos(F, wc.i, wc.j, wc.k, a), vals[a],
+                            corner_pos(F, wc.i, wc.j, wc.k, b), vals[b]);
+      }
+      ExactTri x;
+      const long long pj = (long long)(p / (unsigned long long)W), pi = (long long)p - pj * W;
+      if (!exact_tri(scene, v, x) || !exact_weights(x, pi, pj, R.xs, R.ys, w0, w1, w2)) continue;
+    }
+    const d3 nrm = v_normalise(v_add(v_mul(w0, n3[0]), v_add(v_mul(w1, n3[1]), v_mul(w2, n3[2]))));
+    const double factor = fmax(0.15, fabs(v_dot(nrm, scene.light)));
+    const unsigned r8 = (unsigned)(unsigned char)(int)dmul(factor, cr);
+    const unsigned g8 = (unsigned)(unsigned char)(int)dmul(factor, cg);
+    const unsigned b8 = (unsigned)(unsigned char)(int)dmul(factor, cb);
+    const unsigned rgb = (r8 << 16) | (g8 << 8) | b8;
+    if (CHECK) {
+      /* the FP32 colour, where it was certain, must be this one */
+      const unsigned f = R.shade_check[p];
+      if ((f >> 24) && (f & 0xFFFFFFu) != rgb) atomicAdd(checks + 5, 1u);
+    }
+    R.canvas[p].lo = (lo & ~0xFFFFFFULL) | rgb;
   }
 }
 
@@ -2414,33 +2708,38 @@ void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, con
   k_exact<<<grid_for(cand_bound, 256, 8), 256, 0, st>>>(G, scene, R, order_base);
 }
 
-void launch_shading(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
-                    const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned rgb,
-                    unsigned* checks, cudaEvent_t between, cudaStream_t st) {
-  (void)tri_bound;
+void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,
+                    unsigned long long obase, unsigned rgb, cudaStream_t st) {
   const long long npx = scene.width * scene.height;
-  const int gp = grid_for(npx, 256, 8);
-  k_winners<<<gp, 256, 0, st>>>(G, scene, total, tri, R, order_base);
-  if (!G.F.dgx) {
-    /* no single-precision shading (non-Cartesian nodes): FP64 throughout */
-    k_request<<<gp, 256, 0, st>>>(G, tri, R, R.win, R.win_count, 2u, R.need_count);
-    k_wn<<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R, R.need_count);
-    if (between) cudaEventRecord(between, st);
-    k_shade<false><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb, R.win, R.win_count, checks);
-    return;
+  const unsigned long long span = 12ULL * (unsigned long long)((F.nx - 1) * (F.ny - 1) * (F.nz - 1));
+  k_winners<<<grid_for(npx, 256, 8), 256, 0, st>>>(R.canvas, npx, obase, span, R.win, R.win_count);
+  /* no single-precision shading without node spacings (a converter) or for
+     axes of 2^20 nodes and more (hash keys): every pixel to the FP64 pass */
+  if (!F.dgx || F.nx > (1 << 20) || F.ny > (1 << 20) || F.nz > (1 << 20)) return;
+  const int gs = grid_for(4 * npx, 256, 8); /* four threads per pixel */
+  if (F.is_f32) {
+    if (R.shade_check) k_shade_f<float, true><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
+    else k_shade_f<float, false><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
+  } else {
+    if (R.shade_check) k_shade_f<double, true><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
+    else k_shade_f<double, false><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
   }
-  /* FP32 weighted normals and colours; the pixels they cannot settle again
-     through FP64 weighted normals and colours (the request list is reused) */
-  k_request<<<gp, 256, 0, st>>>(G, tri, R, R.win, R.win_count, 1u, R.need_count);
-  if (G.F.is_f32) k_wn_f<float><<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
-  else k_wn_f<double><<<grid_for(npx * 8, 256, 8), 256, 0, st>>>(G, tri, R);
-  if (between) cudaEventRecord(between, st);
-  if (R.shade_check) k_shade_f<true><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb);
-  else k_shade_f<false><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb);
-  k_request<<<gp, 256, 0, st>>>(G, tri, R, R.amb, R.amb_count, 2u, R.need64_count);
-  k_wn<<<grid_for(npx, 256, 8), 256, 0, st>>>(G, tri, R, R.need64_count);
-  if (R.shade_check) k_shade<true><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb, R.amb, R.amb_count, checks);
-  else k_shade<false><<<gp, 256, 0, st>>>(G, scene, tri, R, rgb, R.amb, R.amb_count, checks);
+}
+
+void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,
+                        const unsigned* pixels, const unsigned long long* count, long long npix,
+                        unsigned long long obase, unsigned long long* ent, unsigned long long ent_cap,
+                        unsigned long long* ent_count, uint2* spans, double* wn, unsigned rgb, unsigned* checks,
+                        cudaStream_t st) {
+  if (npix <= 0) return;
+  k_nb_list<<<grid_for(3 * npix, 256, 8), 256, 0, st>>>(F, R, lut, pixels, count, obase, ent, ent_cap, ent_count,
+                                                       spans);
+  k_nb_wn<<<grid_for((long long)ent_cap, 256, 8), 256, 0, st>>>(F, lut, ent, ent_cap, ent_count, wn);
+  const int gs = grid_for(4 * npix, 256, 8);
+  if (checks && R.shade_check)
+    k_shade<true><<<gs, 256, 0, st>>>(F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
+  else
+    k_shade<false><<<gs, 256, 0, st>>>(F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,

@@ -399,7 +399,8 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
-  Buf zlo, xyf, cand, live, tiny, win, need, checks, voffsets, verts, winfo, amb, shade_check;
+  Buf nb_ent, nb_wn, nb_span; /* the FP64 shading pass's neighbour lists */
+  Buf zlo, xyf, cand, live, tiny, win, checks, voffsets, verts, winfo, amb, shade_check;
   unsigned long long epoch = 0; /* frame counter for the winner-weight tags (1 .. 2^24 - 1) */
   HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
   cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
@@ -513,6 +514,7 @@ struct DebugSink {
 
 struct FrameOut {
   uint8_t *rgb_host = nullptr;  /* ppm body */
+  bool rgb_pinned = false;      /* leave the ppm body in the context's pinned buffer h_rgb */
   uint8_t *rgb_dev = nullptr;   /* ppm body on the device */
   double *depth_host = nullptr; /* canvas order */
   PixelRec *pixels_host = nullptr; /* canvas order, for the multi-rank reduction */
@@ -525,7 +527,7 @@ struct FrameOut {
 static const int kCounters = 9;
 
 /* bytes per triangle of the slab arrays (see TriDev) */
-static const size_t kTriBytes = 3 * sizeof(double) + 48 + 16 + 2 * sizeof(unsigned);
+static const size_t kTriBytes = 3 * sizeof(double) + 48 + sizeof(unsigned);
 /* doubles per triangle of the inspection arrays: vertices, vertex normals, face normal, area */
 static const size_t kDbgDoubles = 22;
 
@@ -534,9 +536,7 @@ static TriDev tri_layout(void *base, size_t cap, double *dbg) {
   double *d = static_cast<double *>(base);
   for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
   t.rec = reinterpret_cast<float4 *>(d + 3 * cap);
-  t.wnf = t.rec + 3 * cap;
-  t.meta = reinterpret_cast<unsigned *>(t.wnf + cap);
-  t.need = t.meta + cap;
+  t.meta = reinterpret_cast<unsigned *>(t.rec + 3 * cap);
   for (int q = 0; q < 9; q++) t.vert[q] = dbg ? dbg + q * cap : nullptr;
   for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + (9 + q) * cap : nullptr;
   t.dbg_fn = dbg ? dbg + 18 * cap : nullptr;
@@ -602,9 +602,24 @@ struct FieldUpload {
 constexpr size_t kPipelineBytes = 64ull << 20;
 constexpr long long kUploadSlabs = 4;
 
-/* one contour object through all of its slabs */
-static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn &ci,
+/* objects that read one field with one geometry: they share the upload, the
+   node tables and the slabs */
+static bool same_field(const ContourIn &a, const ContourIn &b) {
+  return a.data == b.data && a.on_device == b.on_device && a.f32 == b.f32 && a.converter == b.converter &&
+         a.sz[0] == b.sz[0] && a.sz[1] == b.sz[1] && a.sz[2] == b.sz[2] && a.grid[0] == b.grid[0] &&
+         a.grid[1] == b.grid[1] && a.grid[2] == b.grid[2];
+}
+
+/*
+ * A group of contour objects of one field (same_field) through all of the
+ * field's slabs.  The objects take their slabs in turn (slab 0 of every
+ * object, then slab 1, ...), so that while a host field is still arriving
+ * every object works on the slices that are already there; the result does
+ * not depend on this order (fragments carry their drawing order).
+ */
+static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn *objs, size_t nobj,
                           unsigned long long &order_base, const RasterDev &R, DebugSink *sink) {
+  const ContourIn &ci = objs[0];
   cudaStream_t st = f.stream;
   const long long nx = (long long)ci.sz[0], ny = (long long)ci.sz[1], nz = (long long)ci.sz[2];
   if (nx < 2 || ny < 2 || nz < 2) return 0;
@@ -690,9 +705,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   F.gyf = gf + nx;
   F.gzf = gf + nx + ny;
   F.nodes = dnodes;
-  F.threshold = ci.threshold;
-  F.thr_key = h_key(ci.threshold);
-  F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
   F.div_cx = make_fast_div((unsigned)(nx - 1));
   F.div_cy = make_fast_div((unsigned)(ny - 1));
   /* single-precision shading needs Cartesian nodes and finite coordinates */
@@ -706,8 +718,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   double pos_max = coord_max;
   for (const double v : nodes) pos_max = std::max(pos_max, std::fabs(v));
   F.proj_eps = projection_rounding(sd, pos_max);
-  set_float_threshold(F);
-  c.stats.cells += (uint64_t)(ncx * ncy * ncz);
+  std::vector<FieldDev> Fo(nobj, F);
+  for (size_t q = 0; q < nobj; q++) {
+    Fo[q].threshold = objs[q].threshold;
+    Fo[q].thr_key = h_key(objs[q].threshold);
+    Fo[q].thr_nan = std::isnan(objs[q].threshold) ? 1 : 0;
+    set_float_threshold(Fo[q]);
+  }
+  c.stats.cells += (uint64_t)(ncx * ncy * ncz) * nobj;
 
   /* rendered cell slices are [1, ncz - 2]; each slab also triangulates one
      slice below and above for the vertex normals (contour/main.c:49-112).
@@ -770,7 +788,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   int slab_index = 0;
   unsigned *h_small = c.h_small.as<unsigned>();
   unsigned long long *h_total = reinterpret_cast<unsigned long long *>(h_small + 4);
-  const unsigned rgb = ((unsigned)ci.color.r << 16) | ((unsigned)ci.color.g << 8) | ci.color.b;
   for (const long long k0 : starts) {
     const long long k1 = std::min(k0 + slab_slices, kr1);
     SlabDev S;
@@ -803,202 +820,247 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       C3D_CUDA(cudaStreamWaitEvent(st, c.chunk_ev[slab_index], 0));
     }
     slab_index++;
-    C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
-    if (c.stage_timing) cudaEventRecord(c.evs[0], st);
-    launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
-    if (c.stage_timing) cudaEventRecord(c.evs[1], st);
-    launch_scan(c.counts.as<unsigned char>(), ncell, seg_sums, seg_base, c.offsets.as<unsigned>(),
-                c.voffsets.as<unsigned>(), d_total, c.tri_cell.as<unsigned>(), tri_cap, st);
-    if (c.stage_timing) cudaEventRecord(c.evs[2], st);
-    c.stats.kernel_launches += 4;
-    C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-    C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    C3D_CUDA(cudaStreamSynchronize(st));
-    if (c.stage_timing) {
-      c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
-      c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
-    }
-    if (h_small[0]) {
-      log_error("device classification did not complete (error flags 0x%x)", h_small[0]);
-      return 1;
-    }
-    const unsigned long long T = h_total[0], NV = h_total[1];
-    c.stats.triangles += T;
-    c.stats.slabs += 1;
-    if (T == 0) continue;
-    /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
-       every sub-array stays aligned (and over-allocate so that cap >= T) */
-    const bool filled = T <= tri_cap; /* the scan wrote the triangle -> cell map */
-    if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
-    const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
-    if (cap < T) {
-      log_error("internal: triangle buffer capacity %zu below %llu", cap, T);
-      return 1;
-    }
-    double *dbg = nullptr;
-    if (sink) {
-      if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap, st)) return 1;
-      dbg = c.dbg.as<double>();
-    }
-    const TriDev tri = tri_layout(c.tri.p, cap, dbg);
-    unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
-    /* the vertex stage: triangle -> cell map, screen vertices */
-    if (c.stage_timing) cudaEventRecord(c.evs[3], st);
-    if (!filled) {
-      launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
-      c.stats.kernel_launches += 1;
-    }
-    VertDev VD = {};
-    if (!sink) {
-      /* the screen vertices of the slab's crossed edges, 16 bytes each */
-      if (c.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
-      VD.pos = c.verts.as<float4>();
-      launch_vertices(F, S, sd, c.counts.as<unsigned char>(), c.voffsets.as<unsigned>(), ncell, VD, st);
-      c.stats.kernel_launches += 1;
-      c.stats.vertices += NV;
-    }
-    if (c.stage_timing) cudaEventRecord(c.evs[8], st);
-    const unsigned long long slab_order = order_base + 12ULL * (unsigned long long)(S.kfirst * per_slice);
-    Geo G;
-    G.F = F;
-    G.S = S;
-    G.lut = c.lut.as<unsigned long long>();
-    G.codes = c.counts.as<unsigned char>();
-    G.tri_cell = c.tri_cell.as<unsigned>();
-    G.offsets = c.offsets.as<unsigned>();
-    G.meta = tri.meta;
-    if (sink) {
-      RasterDev none = {};
-      launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
-                  c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
-                  st);
-      launch_exact_all(G, d_total, (long long)T, tri, st);
-      launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
-      c.stats.kernel_launches += 3;
-    } else {
-      /* candidate and tiny lists: about one entry per covered pixel and a few
-         percent of the triangles; when one overflows, the slab's emission and
-         raster passes run again with larger lists (every z-buffer update is
-         an idempotent maximum, so repeating them is harmless).  The cover
-         list holds at most one entry per triangle and cannot overflow. */
-      const size_t npx = (size_t)(sd.width * sd.height);
-      if (c.win.ensure(sizeof(uint2) * npx, st) || c.amb.ensure(sizeof(uint2) * npx, st) ||
-          c.need.ensure(sizeof(unsigned) * T, st))
-        return 1;
-      if (c.filter_check && c.shade_check.ensure(sizeof(unsigned) * npx, st)) return 1;
-      unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
-      unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
-      RasterDev RS = R;
-      unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 6);
-      unsigned long long *h_cnt = h_total + 2;
-      RS.win = c.win.as<uint2>();
-      RS.win_count = counters + 2;
-      RS.need = c.need.as<unsigned>();
-      RS.need_count = counters + 3;
-      RS.cover_count = counters + 4;
-      RS.live_count = counters + 5;
-      RS.sliver_count = counters + 6;
-      RS.sliver_rec = tri.rec + 3 * (cap - 1);
-      RS.amb = c.amb.as<uint2>();
-      RS.amb_count = counters + 7;
-      RS.need64_count = counters + 8;
-      {
-        /* render.c:150-159 at the clamped factor: (unsigned char)(int)(0.15 * c) in FP64 */
-        const int r8 = (int)(0.15 * (double)ci.color.r), g8 = (int)(0.15 * (double)ci.color.g),
-                  b8 = (int)(0.15 * (double)ci.color.b);
-        RS.clamp_rgb = ((unsigned)(unsigned char)r8 << 16) | ((unsigned)(unsigned char)g8 << 8) |
-                       (unsigned)(unsigned char)b8;
-      }
-      RS.shade_check = c.filter_check ? c.shade_check.as<unsigned>() : nullptr;
-      for (int attempt = 0;; attempt++) {
-        if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.live.ensure(sizeof(Candidate) * cand_want, st) ||
-            c.tiny.ensure(sizeof(unsigned) * tiny_want, st))
-          return 1;
-        RS.cand = c.cand.as<Candidate>();
-        RS.cand_cap = std::min(c.cand.cap, c.live.cap) / sizeof(Candidate);
-        RS.cand_count = counters + 0;
-        RS.live = c.live.as<Candidate>();
-        RS.tiny = c.tiny.as<unsigned>();
-        RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
-        RS.tiny_count = counters + 1;
-        C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
-        C3D_CUDA(cudaMemsetAsync(tri.need, 0, sizeof(unsigned) * T, st));
-        if (c.stage_timing) cudaEventRecord(c.evs[9], st);
-        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
-                    c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
-                    st);
-        if (c.stage_timing) cudaEventRecord(c.evs[4], st);
-        launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
-        launch_sliver(G, sd, (long long)T, RS, checks, st);
-        launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
-        if (c.stage_timing) cudaEventRecord(c.evs[5], st);
-        launch_prune(RS, (long long)RS.cand_cap, st);
-        launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
-        if (c.stage_timing) cudaEventRecord(c.evs[6], st);
-        /* shading runs before the overflow check: when a list overflowed, the
-           whole stage runs again, and the repeated z-buffer maxima and
-           colours are the same values */
-        launch_shading(G, sd, d_total, (long long)T, tri, RS, slab_order, rgb, checks,
-                       c.stage_timing ? c.evs[10] : nullptr, st);
-        if (c.stage_timing) cudaEventRecord(c.evs[7], st);
-        c.stats.kernel_launches += F.dgx ? 13 : 10;
-        C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        C3D_CUDA(cudaStreamSynchronize(st));
-        if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
-        if (attempt > 4) {
-          log_error("raster candidate lists keep overflowing (%llu, %llu)", h_cnt[0], h_cnt[1]);
-          return 1;
-        }
-        c.stats.candidate_overflows += 1;
-        cand_want = std::max<unsigned long long>(cand_want, h_cnt[0] + h_cnt[0] / 4);
-        tiny_want = std::max<unsigned long long>(tiny_want, h_cnt[1] + h_cnt[1] / 4);
-      }
-      c.stats.candidates += h_cnt[0];
-      c.stats.tiny += h_cnt[1];
-      c.stats.winners += h_cnt[2];
-      c.stats.normals += h_cnt[3];
-      c.stats.cover_triangles += h_cnt[4];
-      c.stats.exact_fragments += h_cnt[5];
-      c.stats.slivers += h_cnt[6];
-      c.stats.shade_exact += h_cnt[7];
+    for (size_t ob = 0; ob < nobj; ob++) {
+      const FieldDev &F = Fo[ob];
+      const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
+      C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
+      if (c.stage_timing) cudaEventRecord(c.evs[0], st);
+      launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
+      if (c.stage_timing) cudaEventRecord(c.evs[1], st);
+      launch_scan(c.counts.as<unsigned char>(), ncell, seg_sums, seg_base, c.offsets.as<unsigned>(),
+                  c.voffsets.as<unsigned>(), d_total, c.tri_cell.as<unsigned>(), tri_cap, st);
+      if (c.stage_timing) cudaEventRecord(c.evs[2], st);
+      c.stats.kernel_launches += 4;
+      C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaStreamSynchronize(st));
       if (c.stage_timing) {
-        c.stats.ms_vertices += elapsed(c.evs[3], c.evs[8]);
-        c.stats.ms_emit += elapsed(c.evs[9], c.evs[4]);
-        c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);
-        c.stats.ms_exact += elapsed(c.evs[5], c.evs[6]);
+        c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
+        c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
+      }
+      if (h_small[0]) {
+        log_error("device classification did not complete (error flags 0x%x)", h_small[0]);
+        return 1;
+      }
+      const unsigned long long T = h_total[0], NV = h_total[1];
+      c.stats.triangles += T;
+      c.stats.slabs += 1;
+      if (T == 0) continue;
+      /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
+         every sub-array stays aligned (and over-allocate so that cap >= T) */
+      const bool filled = T <= tri_cap; /* the scan wrote the triangle -> cell map */
+      if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
+      const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
+      if (cap < T) {
+        log_error("internal: triangle buffer capacity %zu below %llu", cap, T);
+        return 1;
+      }
+      double *dbg = nullptr;
+      if (sink) {
+        if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap, st)) return 1;
+        dbg = c.dbg.as<double>();
+      }
+      const TriDev tri = tri_layout(c.tri.p, cap, dbg);
+      unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
+      /* the vertex stage: triangle -> cell map, screen vertices */
+      if (c.stage_timing) cudaEventRecord(c.evs[3], st);
+      if (!filled) {
+        launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
+        c.stats.kernel_launches += 1;
+      }
+      VertDev VD = {};
+      if (!sink) {
+        /* the screen vertices of the slab's crossed edges, 16 bytes each */
+        if (c.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
+        VD.pos = c.verts.as<float4>();
+        launch_vertices(F, S, sd, c.counts.as<unsigned char>(), c.voffsets.as<unsigned>(), ncell, VD, st);
+        c.stats.kernel_launches += 1;
+        c.stats.vertices += NV;
+      }
+      if (c.stage_timing) cudaEventRecord(c.evs[8], st);
+      const unsigned long long slab_order = obase + 12ULL * (unsigned long long)(S.kfirst * per_slice);
+      Geo G;
+      G.F = F;
+      G.S = S;
+      G.lut = c.lut.as<unsigned long long>();
+      G.codes = c.counts.as<unsigned char>();
+      G.tri_cell = c.tri_cell.as<unsigned>();
+      G.offsets = c.offsets.as<unsigned>();
+      G.meta = tri.meta;
+      if (sink) {
+        RasterDev none = {};
+        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+                    c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
+                    st);
+        launch_exact_all(G, d_total, (long long)T, tri, st);
+        launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
+        c.stats.kernel_launches += 3;
+      } else {
+        /* candidate and tiny lists: about one entry per covered pixel and a few
+           percent of the triangles; when one overflows, the slab's emission and
+           raster passes run again with larger lists (every z-buffer update is
+           an idempotent maximum, so repeating them is harmless).  The cover
+           list holds at most one entry per triangle and cannot overflow. */
+        unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
+        unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
+        RasterDev RS = R;
+        unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 6);
+        unsigned long long *h_cnt = h_total + 2;
+        RS.cover_count = counters + 4;
+        RS.live_count = counters + 5;
+        RS.sliver_count = counters + 6;
+        RS.sliver_rec = tri.rec + 3 * (cap - 1);
+        for (int attempt = 0;; attempt++) {
+          if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.live.ensure(sizeof(Candidate) * cand_want, st) ||
+              c.tiny.ensure(sizeof(unsigned) * tiny_want, st))
+            return 1;
+          RS.cand = c.cand.as<Candidate>();
+          RS.cand_cap = std::min(c.cand.cap, c.live.cap) / sizeof(Candidate);
+          RS.cand_count = counters + 0;
+          RS.live = c.live.as<Candidate>();
+          RS.tiny = c.tiny.as<unsigned>();
+          RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
+          RS.tiny_count = counters + 1;
+          C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
+          if (c.stage_timing) cudaEventRecord(c.evs[9], st);
+          launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+                      c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
+                      st);
+          if (c.stage_timing) cudaEventRecord(c.evs[4], st);
+          launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
+          launch_sliver(G, sd, (long long)T, RS, checks, st);
+          launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
+          if (c.stage_timing) cudaEventRecord(c.evs[5], st);
+          launch_prune(RS, (long long)RS.cand_cap, st);
+          launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
+          if (c.stage_timing) cudaEventRecord(c.evs[6], st);
+          c.stats.kernel_launches += 6;
+          C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+          C3D_CUDA(cudaStreamSynchronize(st));
+          if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
+          if (attempt > 4) {
+            log_error("raster candidate lists keep overflowing (%llu, %llu)", h_cnt[0], h_cnt[1]);
+            return 1;
+          }
+          c.stats.candidate_overflows += 1;
+          cand_want = std::max<unsigned long long>(cand_want, h_cnt[0] + h_cnt[0] / 4);
+          tiny_want = std::max<unsigned long long>(tiny_want, h_cnt[1] + h_cnt[1] / 4);
+        }
+        c.stats.candidates += h_cnt[0];
+        c.stats.tiny += h_cnt[1];
+        c.stats.cover_triangles += h_cnt[4];
+        c.stats.exact_fragments += h_cnt[5];
+        c.stats.slivers += h_cnt[6];
+        if (c.stage_timing) {
+          c.stats.ms_vertices += elapsed(c.evs[3], c.evs[8]);
+          c.stats.ms_emit += elapsed(c.evs[9], c.evs[4]);
+          c.stats.ms_cover += elapsed(c.evs[4], c.evs[5]);
+          c.stats.ms_exact += elapsed(c.evs[5], c.evs[6]);
+        }
+      }
+      if (sink) {
+        /* copy this slab's triangles back and keep the rendered ones in order */
+        std::vector<unsigned> meta(T), cellv(T);
+        std::vector<double> dv(kDbgDoubles * cap);
+        C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * kDbgDoubles * cap, cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaStreamSynchronize(st));
+        for (unsigned long long t = 0; t < T; t++) {
+          const long long cl = cellv[t] & kTcCellMask;
+          const long long i = cl % ncx, j = (cl / ncx) % ncy, k = S.kfirst + cl / (ncx * ncy);
+          if (k >= k0 && k < k1) sink->triangulated++;
+          if (!(meta[t] & kMetaRendered)) continue;
+          if (sink->out && sink->count < sink->capacity) {
+            TriRecord &r = sink->out[sink->count];
+            for (int q = 0; q < 9; q++) r.vertices[q] = dv[q * cap + t];
+            for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[(9 + q) * cap + t];
+            for (int q = 0; q < 3; q++) r.face_normal[q] = dv[18 * cap + 3 * t + q];
+            r.area = dv[21 * cap + t];
+            r.cell[0] = i + (long long)ci.off[0];
+            r.cell[1] = j + (long long)ci.off[1];
+            r.cell[2] = k + (long long)ci.off[2];
+            for (int q = 0; q < 3; q++) r.edge_ids[q] = (meta[t] >> (5 * q)) & 31;
+          }
+          sink->count++;
+        }
+      }
+    }
+  }
+  if (!sink) {
+    /* every object's won pixels, shaded once after all of its slabs */
+    const size_t npx = (size_t)(sd.width * sd.height);
+    if (c.win.ensure(sizeof(unsigned) * npx, st) || c.amb.ensure(sizeof(unsigned) * npx, st) ||
+        c.scratch.ensure(128, st))
+      return 1;
+    if (c.filter_check && c.shade_check.ensure(sizeof(unsigned) * npx, st)) return 1;
+    unsigned long long *counters = reinterpret_cast<unsigned long long *>(c.scratch.as<unsigned>() + 6);
+    unsigned long long *h_cnt = h_total + 2;
+    unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
+    for (size_t ob = 0; ob < nobj; ob++) {
+      const contour3d_color_t &col = objs[ob].color;
+      RasterDev RS = R;
+      RS.win = c.win.as<unsigned>();
+      RS.win_count = counters + 0;
+      RS.amb = c.amb.as<unsigned>();
+      RS.amb_count = counters + 1;
+      /* render.c:150-159 at the clamped factor: (unsigned char)(int)(0.15 * c) in FP64 */
+      const int r8 = (int)(0.15 * (double)col.r), g8 = (int)(0.15 * (double)col.g), b8 = (int)(0.15 * (double)col.b);
+      RS.clamp_rgb = ((unsigned)(unsigned char)r8 << 16) | ((unsigned)(unsigned char)g8 << 8) |
+                     (unsigned)(unsigned char)b8;
+      RS.shade_check = c.filter_check ? c.shade_check.as<unsigned>() : nullptr;
+      const unsigned rgb = ((unsigned)col.r << 16) | ((unsigned)col.g << 8) | col.b;
+      const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
+      C3D_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st));
+      if (c.stage_timing) cudaEventRecord(c.evs[6], st);
+      launch_shade_f(Fo[ob], sd, RS, c.lut.as<unsigned long long>(), obase, rgb, st);
+      if (c.stage_timing) cudaEventRecord(c.evs[10], st);
+      C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaStreamSynchronize(st));
+      /* without node spacings (a converter) every won pixel takes the FP64 pass */
+      const bool fp32 = Fo[ob].dgx != nullptr && nx <= (1 << 20) && ny <= (1 << 20) && nz <= (1 << 20);
+      const unsigned long long nwin = h_cnt[0], namb = fp32 ? h_cnt[1] : nwin;
+      const unsigned *list = fp32 ? RS.amb : RS.win;
+      const unsigned long long *lcount = fp32 ? RS.amb_count : RS.win_count;
+      unsigned long long entries = 0;
+      if (namb) {
+        /* about six neighbour triangles per vertex; more are listed again */
+        unsigned long long want = 24 * namb + 1024;
+        for (int attempt = 0;; attempt++) {
+          if (c.nb_ent.ensure(sizeof(unsigned long long) * want, st) || c.nb_wn.ensure(3 * sizeof(double) * want, st) ||
+              c.nb_span.ensure(sizeof(uint2) * 3 * namb, st))
+            return 1;
+          const unsigned long long cap =
+              std::min(c.nb_ent.cap / sizeof(unsigned long long), c.nb_wn.cap / (3 * sizeof(double)));
+          C3D_CUDA(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), st));
+          launch_shade_exact(Fo[ob], sd, RS, c.lut.as<unsigned long long>(), list, lcount, (long long)namb, obase,
+                             c.nb_ent.as<unsigned long long>(), cap, counters + 2, c.nb_span.as<uint2>(),
+                             c.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
+          c.stats.kernel_launches += 3;
+          C3D_CUDA(cudaMemcpyAsync(h_cnt + 2, counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+          C3D_CUDA(cudaStreamSynchronize(st));
+          entries = h_cnt[2];
+          if (entries <= cap) break;
+          if (attempt > 3) {
+            log_error("shading neighbour lists keep overflowing (%llu)", entries);
+            return 1;
+          }
+          want = entries + entries / 4;
+        }
+      }
+      if (c.stage_timing) cudaEventRecord(c.evs[7], st);
+      c.stats.kernel_launches += fp32 ? 2 : 1;
+      c.stats.winners += nwin;
+      c.stats.shade_exact += namb;
+      c.stats.normals += entries;
+      if (c.stage_timing) {
+        cudaEventSynchronize(c.evs[7]);
         c.stats.ms_normals += elapsed(c.evs[6], c.evs[10]);
         c.stats.ms_shade += elapsed(c.evs[10], c.evs[7]);
       }
     }
-    if (sink) {
-      /* copy this slab's triangles back and keep the rendered ones in order */
-      std::vector<unsigned> meta(T), cellv(T);
-      std::vector<double> dv(kDbgDoubles * cap);
-      C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * kDbgDoubles * cap, cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaStreamSynchronize(st));
-      for (unsigned long long t = 0; t < T; t++) {
-        const long long cl = cellv[t] & kTcCellMask;
-        const long long i = cl % ncx, j = (cl / ncx) % ncy, k = S.kfirst + cl / (ncx * ncy);
-        if (k >= k0 && k < k1) sink->triangulated++;
-        if (!(meta[t] & kMetaRendered)) continue;
-        if (sink->out && sink->count < sink->capacity) {
-          TriRecord &r = sink->out[sink->count];
-          for (int q = 0; q < 9; q++) r.vertices[q] = dv[q * cap + t];
-          for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[(9 + q) * cap + t];
-          for (int q = 0; q < 3; q++) r.face_normal[q] = dv[18 * cap + 3 * t + q];
-          r.area = dv[21 * cap + t];
-          r.cell[0] = i + (long long)ci.off[0];
-          r.cell[1] = j + (long long)ci.off[1];
-          r.cell[2] = k + (long long)ci.off[2];
-          for (int q = 0; q < 3; q++) r.edge_ids[q] = (meta[t] >> (5 * q)) & 31;
-        }
-        sink->count++;
-      }
-    }
   }
-  order_base += 12ULL * (unsigned long long)(ncx * ncy * ncz);
+  order_base += 12ULL * (unsigned long long)(ncx * ncy * ncz) * nobj;
   return 0;
 }
 
@@ -1101,16 +1163,22 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   launch_canvas_init(c.canvas.as<Slot>(), R.zlo, (long long)npx, h_depth_key(-1. * DBL_MAX), bg, st);
   c.stats.kernel_launches += 1;
   unsigned long long order_base = 1;
-  for (size_t n = 0; n < f.contours.size(); n++) {
-    if (render_contour(c, f, sd, f.contours[n], order_base, R, o.sink)) {
+  for (size_t n = 0; n < f.contours.size();) {
+    size_t m = n + 1;
+    /* inspection reports every object's triangles in turn: one object at a time */
+    if (!o.sink)
+      while (m < f.contours.size() && same_field(f.contours[n], f.contours[m])) m++;
+    if (render_contour(c, f, sd, &f.contours[n], m - n, order_base, R, o.sink)) {
       log_error("contour processing failed");
       return 1;
     }
+    n = m;
   }
   if (render_lines(c, f, order_base)) return 1;
   /* resolve */
   uint8_t *rgb_dev = o.rgb_dev;
-  if (!rgb_dev && o.rgb_host) {
+  const bool want_rgb = o.rgb_host || o.rgb_pinned;
+  if (!rgb_dev && want_rgb) {
     if (c.rgb.ensure(3 * npx, st)) return 1;
     rgb_dev = c.rgb.as<uint8_t>();
   }
@@ -1118,7 +1186,7 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     launch_resolve(c.canvas.as<Slot>(), (long long)W, (long long)H, rgb_dev, nullptr, st);
     c.stats.kernel_launches += 1;
   }
-  if (o.rgb_host) {
+  if (want_rgb) {
     if (c.h_rgb.ensure(3 * npx)) return 1;
     C3D_CUDA(cudaMemcpyAsync(c.h_rgb.p, rgb_dev, 3 * npx, cudaMemcpyDeviceToHost, st));
   }
@@ -1277,8 +1345,7 @@ extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
     px.resize(W * H);
     out.pixels_host = px.data();
   } else {
-    rgb.resize(3 * W * H);
-    out.rgb_host = rgb.data();
+    out.rgb_pinned = true; /* written to the file straight from the pinned copy */
   }
   if (render_frame(g_ctx, f, out)) return 1;
   if (multi) {
@@ -1298,7 +1365,7 @@ extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
       }
   }
   if (myrank != 0) return 0;
-  if (write_ppm(fname, W, H, rgb.data())) {
+  if (write_ppm(fname, W, H, multi ? rgb.data() : g_ctx.h_rgb.as<uint8_t>())) {
     log_error("image output failed");
     return 1;
   }
@@ -1475,7 +1542,7 @@ extern "C" long contour3d_gb300_debug_triangles(const contour3d_contour_obj_t *o
   const SceneDev sd = scene_dev(f.scene);
   unsigned long long order = 1;
   RasterDev R = {};
-  if (render_contour(g_ctx, f, sd, f.contours[0], order, R, &sink)) return -1;
+  if (render_contour(g_ctx, f, sd, &f.contours[0], 1, order, R, &sink)) return -1;
   if (num_triangulated) *num_triangulated = sink.triangulated;
   return sink.count;
 }
@@ -1544,7 +1611,7 @@ extern "C" int contour3d_gb300_release(void) {
 
 static void ctx_release(Ctx &c) {
   Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.need, &c.voffsets, &c.verts, &c.winfo, &c.amb, &c.shade_check,
+                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.voffsets, &c.verts, &c.winfo, &c.amb, &c.shade_check,
                  &c.checks};
   /* every call of the context has completed, so its buffers go back to the
      pool in order on its own stream */

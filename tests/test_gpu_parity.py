@@ -218,9 +218,9 @@ def test_float32_field_threshold_edges(gpu, oracle):
 
 @pytest.mark.parametrize("camera", [(2.5, 2.0, 1.5), (0.6, 0.4, 3.0)], ids=["ascending-z", "descending-z"])
 def test_pipelined_host_upload_matches_device_field(gpu, camera):
-    """A host field large enough to be uploaded in chunks, with the slabs
-    starting as their node slices arrive (both slab orders), draws the image
-    the device-resident field draws; the second object reuses the upload."""
+    """A host field large enough to be uploaded in chunks, with the slabs of
+    both objects starting as their node slices arrive (both slab orders),
+    draws the image the device-resident field draws."""
     import torch
     shape = (200, 200, 210)  # 67 MB of float64
     dev = torch.empty(shape, dtype=torch.float64, device="cuda")
@@ -237,5 +237,5 @@ def test_pipelined_host_upload_matches_device_field(gpu, camera):
     scene.contours = [_abi.Contour(host, thr, col, grids=tuple(grids)) for thr, col in levels]
     img = gpu.render(scene)
     assert np.array_equal(img, out.cpu().numpy().reshape(240, 320, 3))
-    # four slabs while the first object's field arrives, one for the second
-    assert gpu.stats().slabs == 5
+    # both objects take the field in four slabs as it arrives
+    assert gpu.stats().slabs == 8
