@@ -52,14 +52,22 @@ __device__ __forceinline__ d3 v_normalise(d3 a) {
 /* ------------------------------------------------------------------ */
 /* integer keys of doubles                                             */
 /* ------------------------------------------------------------------ */
-__device__ __forceinline__ bool d_isnan(double x) {
-  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+/* on the bit pattern b of a double: integer operations only */
+__device__ __forceinline__ bool d_isnan_bits(long long b) {
+  return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
 }
-/* signed key, monotone in x, equal for -0 and +0 (NaN excluded by callers) */
-__device__ __forceinline__ long long d_key(double x) {
-  long long b = __double_as_longlong(x);
+__device__ __forceinline__ long long d_key_bits(long long b) {
   if ((b << 1) == 0) b = 0;
   return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ bool d_isnan(double x) { return d_isnan_bits(__double_as_longlong(x)); }
+/* signed key, monotone in x, equal for -0 and +0 (NaN excluded by callers) */
+__device__ __forceinline__ long long d_key(double x) { return d_key_bits(__double_as_longlong(x)); }
+/* a double of global memory as its bit pattern, through the read-only path
+   (a value test on the bits then stays on the integer pipes; the same test
+   on the loaded double issued FP64 instructions) */
+__device__ __forceinline__ long long ld_bits(const double* p) {
+  return __ldg(reinterpret_cast<const long long*>(p));
 }
 /* unsigned key for the depth buffer: unsigned order == numeric order */
 __device__ __forceinline__ unsigned long long depth_key(double x) {

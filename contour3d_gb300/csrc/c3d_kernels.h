@@ -167,7 +167,7 @@ struct LineSegDev {
 constexpr unsigned kErrClassifyTimeout = 2u;
 
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
-                  const unsigned char nb_count[19]);
+                  const unsigned char nb_count[19], const unsigned short edge_tris[256 * 19]);
 
 /* TMA-staged planes when the field's layout allows it; `err` receives kErrClassifyTimeout */
 void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, unsigned* err, cudaStream_t st);

@@ -55,6 +55,9 @@ __constant__ unsigned char c_code_count[256];
    cells sharing it, in the reference's accumulation order */
 __constant__ signed char c_nb[19][4][4];
 __constant__ unsigned char c_nb_count[19];
+/* per code and cube edge: bit r set when the cell's triangle of rank r has
+   a vertex on that edge (read by lanes with different codes: global, cached) */
+__device__ unsigned short g_edge_tris[256 * 19];
 
 /* ------------------------------------------------------------------ */
 /* field access                                                        */
@@ -62,6 +65,10 @@ __constant__ unsigned char c_nb_count[19];
 template <typename T>
 __device__ __forceinline__ double load_value(const T* f, long long idx) {
   return (double)__ldg(f + idx);
+}
+template <>
+__device__ __forceinline__ double load_value<double>(const double* f, long long idx) {
+  return __longlong_as_double(ld_bits(f + idx));
 }
 
 __device__ __forceinline__ long long corner_index(const FieldDev& F, long long i, long long j, long long k, int c) {
@@ -160,8 +167,8 @@ template <typename T>
 __device__ __forceinline__ unsigned char node_above(const FieldDev& F, const T* f, long long idx);
 template <>
 __device__ __forceinline__ unsigned char node_above<double>(const FieldDev& F, const double* f, long long idx) {
-  const double v = __ldg(f + idx);
-  return (!F.thr_nan && !d_isnan(v) && d_key(v) > F.thr_key) ? 1 : 0;
+  const long long b = ld_bits(f + idx);
+  return (!F.thr_nan && !d_isnan_bits(b) && d_key_bits(b) > F.thr_key) ? 1 : 0;
 }
 template <>
 __device__ __forceinline__ unsigned char node_above<float>(const FieldDev& F, const float* f, long long idx) {
@@ -1868,18 +1875,23 @@ __device__ __forceinline__ bool winner_cell(const FieldDev& F, unsigned long lon
   const unsigned long long ncx = (unsigned long long)(F.nx - 1), ncy = (unsigned long long)(F.ny - 1);
   const unsigned long long ncz = (unsigned long long)(F.nz - 1);
   if (order < obase || order - obase >= 12ULL * ncx * ncy * ncz) return false;
-  const unsigned long long rel = order - obase, c = rel / 12ULL;
+  /* rel / 12 by a multiply-high (exact for every 64-bit rel), the rest by
+     the 32-bit divisions while the cells fit (no 64-bit division) */
+  const unsigned long long rel = order - obase, c = __umul64hi(rel, 0xAAAAAAAAAAAAAAABULL) >> 3;
   w.r = (unsigned)(rel - 12ULL * c);
-  const unsigned long long row = c / ncx;
-  w.i = (long long)(c - row * ncx);
-  w.k = (long long)(row / ncy);
-  w.j = (long long)(row - (unsigned long long)w.k * ncy);
+  if (c < (1ULL << 32)) {
+    const unsigned row = fast_div((unsigned)c, F.div_cx);
+    w.i = (long long)((unsigned)c - row * (unsigned)ncx);
+    const unsigned kk = fast_div(row, F.div_cy);
+    w.k = kk;
+    w.j = (long long)(row - kk * (unsigned)ncy);
+  } else {
+    const unsigned long long row = c / ncx;
+    w.i = (long long)(c - row * ncx);
+    w.k = (long long)(row / ncy);
+    w.j = (long long)(row - (unsigned long long)w.k * ncy);
+  }
   return true;
-}
-
-/* the triangle with LUT entry e has cube edge `le` among its three */
-__device__ __forceinline__ bool uses_edge(unsigned long long e, unsigned le) {
-  return ((e >> 18) & 31) == le || ((e >> 23) & 31) == le || ((e >> 28) & 31) == le;
 }
 
 /* one thread per pixel: the pixels whose owner is one of the object's triangles */
@@ -1935,22 +1947,42 @@ __device__ __forceinline__ void tri_wn_f(bool ok, const float rv[3][3], const fl
   if (!ok || !isfinite(cmax) || !isfinite(eC) || !(cmax - eC > 1e-30f)) eC = INFINITY;
 }
 
-/* bound on |A / |A| - B / |B||, componentwise, from a componentwise bound e
-   on |A - B| with |A| = len computed in FP32; infinite when |A| is too small */
-__device__ __forceinline__ float unit_err(float len, float e) {
-  const float ee = 1.7321f * e; /* Euclidean */
-  if (!(len > 4.f * ee) || !(len > 1e-30f)) return INFINITY;
-  return 2.f * ee / (len - ee) + 4.f * kU32;
+/* 1 / sqrt(x) by the hardware approximation (PTX rsqrt.approx.f32: relative
+   error below 2^-22.9 = 4.3u; no FP64 pipe, unlike the correctly rounded
+   square root and division of a build without fused multiply-adds) */
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+/*
+ * A / |A| in FP32 as A * rsqrt_approx(A . A): the sum of squares is within
+ * 3u of its value, the approximation within 4.3u, the products within u,
+ * so each component is within 6.9u |component| of the exact unit vector;
+ * len = (A . A) * r stands for |A| within 5u.  The bound on the distance to
+ * the reference's unit vector B / |B| adds 2 e_E / (|A| - e_E) for a
+ * componentwise bound e on |A - B| (e_E = sqrt(3) e, Euclidean); infinite
+ * when |A| is too small.
+ */
+__device__ __forceinline__ float unit_vec(const float A[3], float e, float U[3]) {
+  const float ss = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+  const float r = rsqrt_approx(ss);
+  const float len = ss * r * (1.f - 6.f * kU32);
+  const float ee = 1.7321f * e;
+#pragma unroll
+  for (int d = 0; d < 3; d++) U[d] = A[d] * r;
+  if (!(len > 4.f * ee) || !(len > 1e-30f) || !isfinite(r)) return INFINITY;
+  return 1.01f * 2.f * ee / (len - ee) + 8.f * kU32;
 }
 
 /*
  * A double as an unevaluated float pair hi + lo, by integer operations (the
- * FP64 pipe stays free): hi carries the top 24 significand bits (truncated),
- * lo the next 29 rounded to 24; |hi + lo - v| <= 2^-47 |v| + 2^-126.  False
+ * FP64 pipe stays free): hi carries the top 24 significand bits, lo up to 24
+ * of the next 29, both truncated; |hi + lo - v| <= 2^-47 |v| + 2^-126.  False
  * for NaN, infinities and magnitudes beyond float.
  */
-__device__ __forceinline__ bool split_f(double v, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+__device__ __forceinline__ bool split_bits(unsigned long long b, float& hi, float& lo) {
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const int ex = (int)((b >> 52) & 0x7FF);
   hi = lo = 0.f;
@@ -1961,12 +1993,19 @@ __device__ __forceinline__ bool split_f(double v, float& hi, float& lo) {
     return true;
   }
   hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
-  /* lo = rem 2^(ex - 1075), the power of two normal or split as 2^(ex - 1011) 2^-64 */
-  const float r = __uint2float_rn((unsigned)(b & 0x1FFFFFFFu));
-  const float x = ex >= 949 ? r * __uint_as_float((unsigned)(ex - 1075 + 127) << 23)
-                            : (r * __uint_as_float((unsigned)(ex - 1011 + 127) << 23)) * 5.421010862427522e-20f;
-  lo = sign ? -x : x;
+  /* lo = rem 2^(ex - 1075), rem the low 29 bits, truncated to 24 significant
+     bits (an error below 2^-47 |v|); flushed to 0 below 2^-126 */
+  const unsigned rem = (unsigned)(b & 0x1FFFFFFFu);
+  if (rem == 0) return true;
+  const int lz = __clz(rem);                      /* 3 .. 31 */
+  const int le = (31 - lz) + (ex - 1075) + 127;   /* biased exponent of lo */
+  if (le <= 0) return true;
+  lo = __uint_as_float(sign | ((unsigned)le << 23) | ((rem << (lz + 1)) >> 9));
   return true;
+}
+
+__device__ __forceinline__ bool split_f(double v, float& hi, float& lo) {
+  return split_bits((unsigned long long)__double_as_longlong(v), hi, lo);
 }
 
 /* s + t = a - b exactly (Knuth's two-sum; no fused operations in this build) */
@@ -2001,10 +2040,11 @@ __device__ __forceinline__ ThrF thr_f(double t) {
 /* interp_param for the shading pass, FP32 operations only: for a double
    field the differences are formed from float pairs (pair_diff), accurate to
    a few float ulps of the differences themselves */
-__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, double v0, double v1, float& f,
+__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, long long v0, long long v1, float& f,
                                             float& e_f) {
   float h0, l0, h1, l1;
-  if (!split_f(v0, h0, l0) || !split_f(v1, h1, l1) || th.hi != th.hi) return -1;
+  if (!split_bits((unsigned long long)v0, h0, l0) || !split_bits((unsigned long long)v1, h1, l1) || th.hi != th.hi)
+    return -1;
   float e_dv, e_dt;
   const float dv = pair_diff(h1, l1, h0, l0, e_dv);
   const float adv = fabsf(dv);
@@ -2025,19 +2065,30 @@ __device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, f
   return interp_param(F.threshold, th.vt, th.e_vt, v0, v1, f, e_f);
 }
 
-/* code and corner values of cell (i, j, k) in the field's own type */
+/* code of cell (i, j, k) whose corner 0 is node `base` */
 template <typename T>
-__device__ __forceinline__ unsigned cell_code_t(const FieldDev& F, long long i, long long j, long long k, T vals[8]) {
+__device__ __forceinline__ unsigned cell_code_at(const FieldDev& F, long long base) {
   const T* f = static_cast<const T*>(F.data);
-  const long long base = (k * F.ny + j) * F.nx + i;
   unsigned code = 0;
 #pragma unroll
-  for (int c = 0; c < 8; c++) {
-    vals[c] = __ldg(f + base + (c & 1) + ((c >> 1) & 1) * F.nx + (c >> 2) * F.nx * F.ny);
-    code |= (unsigned)node_above_value<T>(F, vals[c]) << c;
-  }
+  for (int c = 0; c < 8; c++)
+    code |= (unsigned)node_above<T>(F, f, base + (c & 1) + ((c >> 1) & 1) * F.nx + (c >> 2) * F.nx * F.ny) << c;
   return code;
 }
+
+/* a corner value as the shading pass takes it: a double's bit pattern, a float itself */
+template <typename T>
+struct ShadeVal;
+template <>
+struct ShadeVal<double> {
+  typedef long long type;
+  static __device__ __forceinline__ long long load(const double* f, long long idx) { return ld_bits(f + idx); }
+};
+template <>
+struct ShadeVal<float> {
+  typedef float type;
+  static __device__ __forceinline__ float load(const float* f, long long idx) { return __ldg(f + idx); }
+};
 
 /* the pixel's colour from the three FP32 vertex normals: false when a
    channel's truncation is not certain */
@@ -2058,12 +2109,11 @@ __device__ __forceinline__ bool blend_f(const SceneDev& scene, const RasterDev& 
     wsum += fabsf(w);
   }
   eM += 4.f * kU32 * wsum * 1.01f;
-  const float lenM = sqrtf(M[0] * M[0] + M[1] * M[1] + M[2] * M[2]);
-  const float eN = unit_err(lenM, eM);
+  float U[3];
+  const float eN = unit_vec(M, eM, U);
   if (!isfinite(eN)) return false;
-  const float iM = 1.f / lenM;
   const float* L = scene.f_light;
-  const float dotv = (M[0] * iM) * L[0] + (M[1] * iM) * L[1] + (M[2] * iM) * L[2];
+  const float dotv = U[0] * L[0] + U[1] * L[1] + U[2] * L[2];
   const float l1 = fabsf(L[0]) + fabsf(L[1]) + fabsf(L[2]);
   /* the unit vector's bound, the light's rounding to float, and the dot
      product's rounding (bounded by the sum of |n_i L_i| <= l1 (1 + eN)) */
@@ -2165,17 +2215,15 @@ k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __r
       ok = winner_cell(F, lo, obase, wc);
     }
     if (ok && m < 3) {
-      T cv[8];
-      const unsigned code = cell_code_t<T>(F, wc.i, wc.j, wc.k, cv);
+      const unsigned code = cell_code_at<T>(F, (wc.k * F.ny + wc.j) * F.nx + wc.i);
       const int ed = (int)((__ldg(lut + code * 12 + wc.r) >> (18 + 5 * m)) & 31);
       const int nn = c_nb_count[ed];
       for (int s = 0; s < nn; s++) {
         const long long ni = wc.i + c_nb[ed][s][2], nj = wc.j + c_nb[ed][s][1], nk = wc.k + c_nb[ed][s][0];
         const unsigned le = (unsigned)c_nb[ed][s][3];
-        const unsigned ncode = cell_code_t<T>(F, ni, nj, nk, cv);
-        const int nt = c_code_count[ncode];
-        for (int r = 0; r < nt; r++) {
-          if (!uses_edge(__ldg(lut + ncode * 12 + r), le)) continue;
+        const unsigned ncode = cell_code_at<T>(F, (nk * F.ny + nj) * F.nx + ni);
+        for (unsigned mask = __ldg(g_edge_tris + ncode * 19 + le); mask; mask &= mask - 1) {
+          const int r = __ffs(mask) - 1;
           bool fresh;
           const int slot = hash_slot(keys, tri_key(ni, nj, nk, (unsigned)r), fresh);
           if (slot < 0 || cnt >= kShadeList) {
@@ -2195,17 +2243,22 @@ k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __r
       const unsigned long long key = keys[slot];
       const long long i = (long long)((key >> 4) & 0xFFFFFu), j = (long long)((key >> 24) & 0xFFFFFu);
       const long long k = (long long)(key >> 44);
-      T cv[8];
-      const unsigned code = cell_code_t<T>(F, i, j, k, cv);
+      const long long nb = (k * F.ny + j) * F.nx + i;
+      const unsigned code = cell_code_at<T>(F, nb);
       const unsigned long long e = __ldg(lut + code * 12 + (key & 15u));
       const float sp[3] = {__ldg(F.dgx + i), __ldg(F.dgy + j), __ldg(F.dgz + k)};
+      const T* fd = static_cast<const T*>(F.data);
       float rv[3][3], er[3][3];
       bool tok = true;
 #pragma unroll
       for (int v = 0; v < 3; v++) {
         const unsigned a = (unsigned)((e >> (6 * v)) & 7), b = (unsigned)((e >> (6 * v + 3)) & 7);
+        const typename ShadeVal<T>::type va =
+            ShadeVal<T>::load(fd, nb + (a & 1u) + ((a >> 1) & 1u) * F.nx + (long long)(a >> 2) * F.nx * F.ny);
+        const typename ShadeVal<T>::type vb =
+            ShadeVal<T>::load(fd, nb + (b & 1u) + ((b >> 1) & 1u) * F.nx + (long long)(b >> 2) * F.nx * F.ny);
         float f = 0.f, e_f = 0.f;
-        if (interp_shade(F, th, cv[a], cv[b], f, e_f) < 0) tok = false;
+        if (interp_shade(F, th, va, vb, f, e_f) < 0) tok = false;
         rel_pos(F, sp, a, b, f, e_f, rv[v], er[v]);
       }
       float C[3], eC;
@@ -2226,13 +2279,7 @@ k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __r
         asum += fabsf(c.x) + fabsf(c.y) + fabsf(c.z);
       }
       eS += (float)(cnt + 1) * kU32 * asum + 1e-15f * asum; /* FP32 and the reference's FP64 summation */
-      const float len = sqrtf(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
-      en = unit_err(len, eS);
-      if (isfinite(en)) {
-        const float il = 1.f / len;
-#pragma unroll
-        for (int d = 0; d < 3; d++) N[d] = S[d] * il;
-      }
+      en = unit_vec(S, eS, N);
     }
     float Nv[3][3], env[3];
 #pragma unroll
@@ -2290,10 +2337,10 @@ __device__ __forceinline__ void for_edge_triangles(const FieldDev& F, const unsi
     const unsigned le = (unsigned)c_nb[ed][q][3];
     double vals[8];
     const unsigned code = cell_code_any(F, ni, nj, nk, vals);
-    const int nt = c_code_count[code];
     const unsigned long long cell = (unsigned long long)((nk * ncy + nj) * ncx + ni);
-    for (int r = 0; r < nt; r++)
-      if (uses_edge(lut[code * 12 + r], le)) fn(cell * 16ULL + (unsigned long long)r);
+    /* ascending rank: the reference's order within the cell */
+    for (unsigned mask = __ldg(g_edge_tris + code * 19 + le); mask; mask &= mask - 1)
+      fn(cell * 16ULL + (unsigned long long)(__ffs(mask) - 1));
   }
 }
 
@@ -2550,8 +2597,9 @@ static int grid_for(long long n, int threads, int per_sm) {
 }
 
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
-                  const unsigned char nb_count[19]) {
+                  const unsigned char nb_count[19], const unsigned short edge_tris[256 * 19]) {
   if (cudaMemcpyToSymbol(c_code_count, code_count, 256) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(g_edge_tris, edge_tris, sizeof(unsigned short) * 256 * 19) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_nb, nb, sizeof(signed char) * 19 * 16) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_nb_count, nb_count, 19) != cudaSuccess) return 1;
   return 0;

@@ -447,7 +447,17 @@ static int ctx_init(Ctx &c) {
     std::lock_guard<std::mutex> lk(tables_mu);
     if (dev < 0 || dev >= 64) return 1;
     if (!uploaded[dev]) {
-      if (upload_tables(count, kNb, kNbCount)) {
+      /* per code and cube edge, the ranks of the triangles with a vertex on it */
+      std::vector<unsigned short> edge_tris(256 * 19, 0);
+      for (int code = 0; code < 256; code++)
+        for (int r = 0; r < count[code]; r++) {
+          const unsigned long long e = lut[code * 12 + r];
+          for (int q = 0; q < 3; q++) {
+            const unsigned id = (unsigned)((e >> (18 + 5 * q)) & 31);
+            if (id < 19) edge_tris[code * 19 + id] |= (unsigned short)(1u << r);
+          }
+        }
+      if (upload_tables(count, kNb, kNbCount, edge_tris.data())) {
         log_error("constant table upload failed");
         return 1;
       }
