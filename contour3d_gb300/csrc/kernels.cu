@@ -672,9 +672,11 @@ __device__ __forceinline__ float value_f(float v, float& e) {
  * (the bounds cannot decide that test).
  *   double fields: the two differences are formed in FP64 exactly as the
  *     reference forms them, then truncated to float (2u each), so the 1e-8
- *     test is exact and cancellation costs no accuracy;
+ *     test is exact and cancellation costs no accuracy (k_vertices: issue
+ *     bound, two FP64 subtractions cost fewer slots than float pairs);
  *   float fields: the values are exact floats and the differences are FP32
  *     (u each), with the 1e-8 test decided by the bounds.
+ * interp_shade below is the FP64-free form for double fields.
  */
 __device__ __forceinline__ int interp_param(double vt, float, float, double v0, double v1, float& f, float& e_f) {
   const double dvd = dsub(v1, v0);
@@ -710,6 +712,110 @@ __device__ __forceinline__ int interp_param(double, float vt, float e_vt, float 
 }
 
 /*
+ * A double as an unevaluated float pair hi + lo, by integer operations (the
+ * FP64 pipe stays free): hi carries the top 24 significand bits, lo up to 24
+ * of the next 29, both truncated; |hi + lo - v| <= 2^-47 |v| + 2^-126.  False
+ * for NaN, infinities and magnitudes beyond float.
+ */
+__device__ __forceinline__ bool split_bits(unsigned long long b, float& hi, float& lo) {
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const int ex = (int)((b >> 52) & 0x7FF);
+  hi = lo = 0.f;
+  if (ex == 0x7FF || ex - 1023 > 127) return false;
+  const int fe = ex - 1023 + 127;
+  if (fe <= 0) { /* below 2^-126: flushed */
+    hi = __uint_as_float(sign);
+    return true;
+  }
+  hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+  /* lo = rem 2^(ex - 1075), rem the low 29 bits, truncated to 24 significant
+     bits (an error below 2^-47 |v|); flushed to 0 below 2^-126 */
+  const unsigned rem = (unsigned)(b & 0x1FFFFFFFu);
+  if (rem == 0) return true;
+  const int lz = __clz(rem);                      /* 3 .. 31 */
+  const int le = (31 - lz) + (ex - 1075) + 127;   /* biased exponent of lo */
+  if (le <= 0) return true;
+  lo = __uint_as_float(sign | ((unsigned)le << 23) | ((rem << (lz + 1)) >> 9));
+  return true;
+}
+
+__device__ __forceinline__ bool split_f(double v, float& hi, float& lo) {
+  return split_bits((unsigned long long)__double_as_longlong(v), hi, lo);
+}
+
+/* s + t = a - b exactly (Knuth's two-sum; no fused operations in this build) */
+__device__ __forceinline__ void two_diff(float a, float b, float& s, float& t) {
+  s = a - b;
+  const float bb = s - a;
+  t = (a - (s - bb)) - (b + bb);
+}
+
+/* (ah + al) - (bh + bl) in FP32 and a bound on its distance to the
+   difference of the two doubles the pairs stand for */
+__device__ __forceinline__ float pair_diff(float ah, float al, float bh, float bl, float& e) {
+  float s, t;
+  two_diff(ah, bh, s, t);
+  const float dl = al - bl, u = t + dl, d = s + u;
+  e = 1.01f * (kU32 * (fabsf(dl) + fabsf(u) + fabsf(d)) + 1.43e-14f * (fabsf(ah) + fabsf(bh)) + 3e-38f);
+  return d;
+}
+
+/* the threshold in the forms the shading pass uses */
+struct ThrF {
+  float vt, e_vt; /* rounded to float, with its bound (float fields) */
+  float hi, lo;   /* split (double fields) */
+};
+__device__ __forceinline__ ThrF thr_f(double t) {
+  ThrF r;
+  r.vt = value_f(t, r.e_vt);
+  if (!split_f(t, r.hi, r.lo)) r.hi = r.lo = __int_as_float(0x7fc00000);
+  return r;
+}
+
+/* interp_param for the shading pass, FP32 operations only: for a double
+   field the differences are formed from float pairs (pair_diff), accurate to
+   a few float ulps of the differences themselves */
+__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, long long v0, long long v1, float& f,
+                                            float& e_f) {
+  float h0, l0, h1, l1;
+  if (!split_bits((unsigned long long)v0, h0, l0) || !split_bits((unsigned long long)v1, h1, l1) || th.hi != th.hi)
+    return -1;
+  float e_dv, e_dt;
+  const float dv = pair_diff(h1, l1, h0, l0, e_dv);
+  const float adv = fabsf(dv);
+  /* triangulate.c:40-73: |v1 - v0| < 1e-8 keeps p0 */
+  if (!(adv - e_dv > 1.00001e-8f)) return adv + e_dv < 0.99999e-8f ? 0 : -1;
+  if (adv > 1e30f) return -1;
+  const float rdv = __fdividef(1.f, adv);
+  const float xr = e_dv * rdv;
+  if (!(xr < 0.01f)) return -1;
+  const float dt = pair_diff(th.hi, th.lo, h0, l0, e_dt);
+  f = __fdividef(dt, dv); /* 2 ulp */
+  const float fmax_ = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
+  e_f = 1.1f * (1.01f * (e_dt + fmax_ * e_dv) * rdv + 4.f * kU32 * fabsf(f));
+  return 1;
+}
+__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, float v0, float v1, float& f,
+                                            float& e_f) {
+  return interp_param(F.threshold, th.vt, th.e_vt, v0, v1, f, e_f);
+}
+
+/* a corner value as the shading pass takes it: a double's bit pattern, a float itself */
+template <typename T>
+struct ShadeVal;
+template <>
+struct ShadeVal<double> {
+  typedef long long type;
+  static __device__ __forceinline__ long long load(const double* f, long long idx) { return ld_bits(f + idx); }
+};
+template <>
+struct ShadeVal<float> {
+  typedef float type;
+  static __device__ __forceinline__ float load(const float* f, long long idx) { return __ldg(f + idx); }
+};
+
+
+/*
  * FP32 estimate of one vertex (triangulate.c:40-73) relative to the camera,
  * q = vertex - camera, with a bound per component on the distance to the
  * reference's FP64 value: p = p0 + f (p1 - p0) with f from interp_param.
@@ -717,12 +823,12 @@ __device__ __forceinline__ int interp_param(double, float vt, float e_vt, float 
  * (the triangle then takes the FP64 path).
  */
 template <typename T>
-__device__ __forceinline__ bool vertex_q(const SceneDev& s, double vtd, float vt, float e_vt, const float x0[3], T v0,
-                                         const float x1[3], T v1, float ce, float q[3], float eq[3]) {
+__device__ __forceinline__ bool vertex_q(const SceneDev& s, const FieldDev& F, const ThrF& th, const float x0[3],
+                                         T v0, const float x1[3], T v1, float ce, float q[3], float eq[3]) {
   /* x0, x1: corner coordinates rounded to float with error <= ce u |x| */
   const float pc[3] = {s.f_cam[0], s.f_cam[1], s.f_cam[2]};
   float f = 0.f, e_f = 0.f;
-  const int st = interp_param(vtd, vt, e_vt, v0, v1, f, e_f);
+  const int st = interp_param(F.threshold, th.vt, th.e_vt, v0, v1, f, e_f);
   if (st < 0) return false;
   if (st == 0) {
     /* the reference keeps p0 itself */
@@ -1155,8 +1261,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
   }
   __syncthreads();
   const T* fd = static_cast<const T*>(F.data);
-  float e_vt;
-  const float vt = value_f(F.threshold, e_vt);
+  const ThrF th = thr_f(F.threshold);
   for (unsigned e = threadIdx.x; e < vb - va; e += kVThreads) {
     const unsigned entry = list[e];
     const unsigned m = entry >> 11;
@@ -1168,7 +1273,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
     corner_pos_f(F, i, j, k, (int)m, xb);
     const long long i0 = (k * F.ny + j) * F.nx + i;
     const long long i1 = i0 + (long long)(m & 1u) + ((m >> 1) & 1u) * F.nx + (long long)(m >> 2) * F.nx * F.ny;
-    const bool vok = vertex_q<T>(scene, F.threshold, vt, e_vt, xa, __ldg(fd + i0), xb, __ldg(fd + i1), ce, qv, eq);
+    const bool vok = vertex_q<T>(scene, F, th, xa, __ldg(fd + i0), xb, __ldg(fd + i1), ce, qv, eq);
     float X = 0.f, Y = 0.f, Z = 0.f, exy = 0.f, ez = 0.f;
     const int st = vok ? project_f(scene, qv, eq, fmaxf(1e-12f, F.proj_eps), X, Y, Z, exy, ez) : -1;
     /* |Z| in [1e-8, 1e30] when the projection succeeds: __fdividef is within 2 ulp */
@@ -1596,8 +1701,7 @@ template <typename T>
 __device__ __forceinline__ bool cell_rel_vertices(const Geo& G, unsigned u, float rv[3][3], float er[3][3]) {
   const FieldDev& F = G.F;
   const T* fd = static_cast<const T*>(F.data);
-  float e_vt;
-  const float vt = value_f(F.threshold, e_vt);
+  const ThrF th = thr_f(F.threshold);
   const unsigned tc = G.tri_cell[u];
   const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
   unsigned ui, uj, ukl;
@@ -1613,7 +1717,7 @@ __device__ __forceinline__ bool cell_rel_vertices(const Geo& G, unsigned u, floa
     const long long ia = base + (a & 1u) + ((a >> 1) & 1u) * F.nx + (long long)(a >> 2) * F.nx * F.ny;
     const long long ib = base + (b & 1u) + ((b >> 1) & 1u) * F.nx + (long long)(b >> 2) * F.nx * F.ny;
     float f = 0.f, e_f = 0.f;
-    if (interp_param(F.threshold, vt, e_vt, __ldg(fd + ia), __ldg(fd + ib), f, e_f) < 0) ok = false;
+    if (interp_shade(F, th, ShadeVal<T>::load(fd, ia), ShadeVal<T>::load(fd, ib), f, e_f) < 0) ok = false;
     rel_pos(F, sp, a, b, f, e_f, rv[v], er[v]);
   }
   return ok;
@@ -1976,95 +2080,6 @@ __device__ __forceinline__ float unit_vec(const float A[3], float e, float U[3])
   return 1.01f * 2.f * ee / (len - ee) + 8.f * kU32;
 }
 
-/*
- * A double as an unevaluated float pair hi + lo, by integer operations (the
- * FP64 pipe stays free): hi carries the top 24 significand bits, lo up to 24
- * of the next 29, both truncated; |hi + lo - v| <= 2^-47 |v| + 2^-126.  False
- * for NaN, infinities and magnitudes beyond float.
- */
-__device__ __forceinline__ bool split_bits(unsigned long long b, float& hi, float& lo) {
-  const unsigned sign = (unsigned)(b >> 63) << 31;
-  const int ex = (int)((b >> 52) & 0x7FF);
-  hi = lo = 0.f;
-  if (ex == 0x7FF || ex - 1023 > 127) return false;
-  const int fe = ex - 1023 + 127;
-  if (fe <= 0) { /* below 2^-126: flushed */
-    hi = __uint_as_float(sign);
-    return true;
-  }
-  hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
-  /* lo = rem 2^(ex - 1075), rem the low 29 bits, truncated to 24 significant
-     bits (an error below 2^-47 |v|); flushed to 0 below 2^-126 */
-  const unsigned rem = (unsigned)(b & 0x1FFFFFFFu);
-  if (rem == 0) return true;
-  const int lz = __clz(rem);                      /* 3 .. 31 */
-  const int le = (31 - lz) + (ex - 1075) + 127;   /* biased exponent of lo */
-  if (le <= 0) return true;
-  lo = __uint_as_float(sign | ((unsigned)le << 23) | ((rem << (lz + 1)) >> 9));
-  return true;
-}
-
-__device__ __forceinline__ bool split_f(double v, float& hi, float& lo) {
-  return split_bits((unsigned long long)__double_as_longlong(v), hi, lo);
-}
-
-/* s + t = a - b exactly (Knuth's two-sum; no fused operations in this build) */
-__device__ __forceinline__ void two_diff(float a, float b, float& s, float& t) {
-  s = a - b;
-  const float bb = s - a;
-  t = (a - (s - bb)) - (b + bb);
-}
-
-/* (ah + al) - (bh + bl) in FP32 and a bound on its distance to the
-   difference of the two doubles the pairs stand for */
-__device__ __forceinline__ float pair_diff(float ah, float al, float bh, float bl, float& e) {
-  float s, t;
-  two_diff(ah, bh, s, t);
-  const float dl = al - bl, u = t + dl, d = s + u;
-  e = 1.01f * (kU32 * (fabsf(dl) + fabsf(u) + fabsf(d)) + 1.43e-14f * (fabsf(ah) + fabsf(bh)) + 3e-38f);
-  return d;
-}
-
-/* the threshold in the forms the shading pass uses */
-struct ThrF {
-  float vt, e_vt; /* rounded to float, with its bound (float fields) */
-  float hi, lo;   /* split (double fields) */
-};
-__device__ __forceinline__ ThrF thr_f(double t) {
-  ThrF r;
-  r.vt = value_f(t, r.e_vt);
-  if (!split_f(t, r.hi, r.lo)) r.hi = r.lo = __int_as_float(0x7fc00000);
-  return r;
-}
-
-/* interp_param for the shading pass, FP32 operations only: for a double
-   field the differences are formed from float pairs (pair_diff), accurate to
-   a few float ulps of the differences themselves */
-__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, long long v0, long long v1, float& f,
-                                            float& e_f) {
-  float h0, l0, h1, l1;
-  if (!split_bits((unsigned long long)v0, h0, l0) || !split_bits((unsigned long long)v1, h1, l1) || th.hi != th.hi)
-    return -1;
-  float e_dv, e_dt;
-  const float dv = pair_diff(h1, l1, h0, l0, e_dv);
-  const float adv = fabsf(dv);
-  /* triangulate.c:40-73: |v1 - v0| < 1e-8 keeps p0 */
-  if (!(adv - e_dv > 1.00001e-8f)) return adv + e_dv < 0.99999e-8f ? 0 : -1;
-  if (adv > 1e30f) return -1;
-  const float rdv = __fdividef(1.f, adv);
-  const float xr = e_dv * rdv;
-  if (!(xr < 0.01f)) return -1;
-  const float dt = pair_diff(th.hi, th.lo, h0, l0, e_dt);
-  f = __fdividef(dt, dv); /* 2 ulp */
-  const float fmax_ = 1.01f * (fabsf(dt) + e_dt) * rdv * (1.f + 1.02f * xr);
-  e_f = 1.1f * (1.01f * (e_dt + fmax_ * e_dv) * rdv + 4.f * kU32 * fabsf(f));
-  return 1;
-}
-__device__ __forceinline__ int interp_shade(const FieldDev& F, const ThrF& th, float v0, float v1, float& f,
-                                            float& e_f) {
-  return interp_param(F.threshold, th.vt, th.e_vt, v0, v1, f, e_f);
-}
-
 /* code of cell (i, j, k) whose corner 0 is node `base` */
 template <typename T>
 __device__ __forceinline__ unsigned cell_code_at(const FieldDev& F, long long base) {
@@ -2076,19 +2091,6 @@ __device__ __forceinline__ unsigned cell_code_at(const FieldDev& F, long long ba
   return code;
 }
 
-/* a corner value as the shading pass takes it: a double's bit pattern, a float itself */
-template <typename T>
-struct ShadeVal;
-template <>
-struct ShadeVal<double> {
-  typedef long long type;
-  static __device__ __forceinline__ long long load(const double* f, long long idx) { return ld_bits(f + idx); }
-};
-template <>
-struct ShadeVal<float> {
-  typedef float type;
-  static __device__ __forceinline__ float load(const float* f, long long idx) { return __ldg(f + idx); }
-};
 
 /* the pixel's colour from the three FP32 vertex normals: false when a
    channel's truncation is not certain */
