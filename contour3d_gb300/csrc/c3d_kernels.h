@@ -176,12 +176,13 @@ constexpr long long kMaxSlabCells = 178956970;
 
 /* segments of the scan over n cells */
 long long scan_segments(long long n);
-/* offsets[0..n], voffsets[0..n], totals = (triangles, vertices); the
-   triangle -> cell map too when the triangles fit tri_cap.  seg_sums and
+/* voffsets[0..n], totals = (triangles, vertices), offsets[n]; the
+   triangle -> cell map when the triangles fit tri_cap, and offsets[0..n - 1]
+   when want_offsets or when they do not.  seg_sums and
    seg_base hold scan_segments(n) entries each */
 void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
                  unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
-                 unsigned* tri_cell, unsigned long long tri_cap, cudaStream_t st);
+                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, cudaStream_t st);
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);

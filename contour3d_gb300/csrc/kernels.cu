@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(kScanThreads, 3)
 k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigned long long* __restrict__ seg_base,
              unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
              const unsigned long long* __restrict__ totals, unsigned* __restrict__ tri_cell,
-             unsigned long long tri_cap) {
+             unsigned long long tri_cap, int want_offsets) {
   extern __shared__ __align__(16) unsigned char scan_smem[];
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ unsigned s_cnt[256];
@@ -520,6 +520,9 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
   const bool fill = totals[0] <= tri_cap;
   const bool listed = fill && seg_tris <= (unsigned)kFillList;
   const bool direct = fill && !listed;
+  /* the triangle offsets are kept only when asked for or when the map must
+     be filled from them afterwards */
+  const bool keep_offsets = want_offsets || !fill;
   unsigned* stage = stage_all + warp * 32 * kStagePitch;
   const long long wbase = c0 + (long long)warp * 32 * kScanItems; /* the warp's first cell */
   for (int half = 1; half >= 0; half--) {
@@ -542,7 +545,9 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
     }
     __syncwarp();
     unsigned* dst = half == 0 ? offsets : voffsets;
-    if (wbase + 32 * kScanItems <= n) {
+    if (half == 0 && !keep_offsets) {
+      /* nothing to store */
+    } else if (wbase + 32 * kScanItems <= n) {
       /* the warp's 1024 cells: each store instruction writes 512 contiguous
          bytes (lane L: cells 4L .. 4L + 3 of a 128-cell chunk, all in one
          staged row; wbase is a multiple of 1024, dst 256-byte aligned) */
@@ -1410,7 +1415,6 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
       }
     }
   }
-  tri.meta[t] = meta;
   tri.meta[t] = meta;
 }
 
@@ -2663,7 +2667,7 @@ long long scan_segments(long long n) { return (n + kScanTile - 1) / kScanTile; }
 
 void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
                  unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
-                 unsigned* tri_cell, unsigned long long tri_cap, cudaStream_t st) {
+                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, cudaStream_t st) {
   const long long nseg = scan_segments(n);
   if (nseg > 0) k_seg_reduce<<<(unsigned)nseg, kScanThreads, 0, st>>>(codes, n, seg_sums);
   k_seg_scan<<<1, kSegScanThreads, 0, st>>>(seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
@@ -2671,7 +2675,7 @@ void launch_scan(const unsigned char* codes, long long n, unsigned long long* se
   cudaFuncSetAttribute(k_scan_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanWriteSmem);
   if (nseg > 0)
     k_scan_write<<<(unsigned)nseg, kScanThreads, kScanWriteSmem, st>>>(codes, n, seg_base, offsets, voffsets, totals,
-                                                                       tri_cell, tri_cap);
+                                                                       tri_cell, tri_cap, want_offsets ? 1 : 0);
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,

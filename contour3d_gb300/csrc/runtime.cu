@@ -838,7 +838,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
       if (c.stage_timing) cudaEventRecord(c.evs[1], st);
       launch_scan(c.counts.as<unsigned char>(), ncell, seg_sums, seg_base, c.offsets.as<unsigned>(),
-                  c.voffsets.as<unsigned>(), d_total, c.tri_cell.as<unsigned>(), tri_cap, st);
+                  c.voffsets.as<unsigned>(), d_total, c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, st);
       if (c.stage_timing) cudaEventRecord(c.evs[2], st);
       c.stats.kernel_launches += 4;
       C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
