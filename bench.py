@@ -47,10 +47,10 @@ CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
 # kernel on the 256^3 case (profiles/*_fourier256_f64.md); the full-size
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
-    "classify": (8.77, "cells"),     # k_classify_tma: 145.6 MB for 16.6 M cells
-    "scan": (9.46, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 157.0 MB for 16.6 M cells
-    "vertices": (36.6, "vertices"),  # k_vertices: 239.6 MB for 6.55 M vertices
-    "emit": (44.8, "triangles"),     # k_emit: 586.6 MB for 13.1 M triangles
+    "classify": (8.77, "cells"),     # k_classify_tma: 145.4 MB for 16.6 M cells
+    "scan": (5.47, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 90.7 MB for 16.6 M cells
+    "vertices": (36.5, "vertices"),  # k_vertices: 238.7 MB for 6.55 M vertices
+    "emit": (43.9, "triangles"),     # k_emit: 575.2 MB for 13.1 M triangles
 }
 
 
@@ -459,13 +459,13 @@ def main():
     # once -- inputs read once, outputs written once, cached re-reads not counted
     stage_bytes = {
         "classify": 2 * (nodes * 8 + cells * 1),
-        "scan": 2 * cells * (1 + 4 + 4),
-        "vertices": 2 * cells * (4 + 1 + 4) + T * 4 + V * (2 * 8 + 20),
-        "emit": T * (4 + 4) + 2 * cells * (4 + 1 + 4) + V * 20 + listed * 48 + float(prof.tiny) * 4,
+        "scan": 2 * cells * (1 + 4) + T * 4,
+        "vertices": 2 * cells * (4 + 1) + V * (2 * 8 + 16),
+        "emit": T * (4 + 4) + 2 * cells * (4 + 1) + V * 16 + listed * 48 + float(prof.tiny) * 4,
         "cover": listed * 48 + float(prof.candidates) * 16,
         "exact": float(prof.candidates) * (16 + 4) + float(prof.exact_fragments) * 16,
-        "normals": WIDTH * HEIGHT * 16 * 2 + float(prof.normals) * (4 + 24),
-        "shade": float(prof.winners) * (8 + 16) + float(prof.normals) * 24,
+        "normals": WIDTH * HEIGHT * 16 * 2 + float(prof.winners) * (4 + 48 + 8),
+        "shade": float(prof.shade_exact) * (4 + 48 + 8) + float(prof.normals) * (8 + 24),
     }
     dom = max(stage_ms, key=lambda k: stage_ms[k])
     achieved = stage_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9 if stage_ms[dom] > 0 else 0.0

@@ -1418,7 +1418,7 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
   tri.meta[t] = meta;
 }
 
-constexpr int kEmitPer = 3; /* triangles per thread and iteration: three gather chains in flight */
+constexpr int kEmitPer = 1; /* triangles per thread and iteration (one: occupancy hides the gathers better than 2 or 3 chains) */
 
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
