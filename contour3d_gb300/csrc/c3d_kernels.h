@@ -110,8 +110,7 @@ struct Geo {
   const unsigned long long* lut;
   const unsigned char* codes;
   const unsigned* tri_cell;
-  const unsigned* offsets;
-  const unsigned* meta;
+  const unsigned* offsets;  /* triangle offsets per cell (inspection) */
 };
 
 /* a fragment that k_exact resolves with the reference's arithmetic */

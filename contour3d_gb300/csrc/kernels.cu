@@ -1415,6 +1415,9 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
       }
     }
   }
+  /* the edge ids and flags serve inspection (vertex normals in k_normals);
+     the render path writes them too: a conditional store here cost seven
+     registers and a third of the resident warps */
   tri.meta[t] = meta;
 }
 

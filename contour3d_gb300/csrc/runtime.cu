@@ -896,7 +896,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       G.codes = c.counts.as<unsigned char>();
       G.tri_cell = c.tri_cell.as<unsigned>();
       G.offsets = c.offsets.as<unsigned>();
-      G.meta = tri.meta;
       if (sink) {
         RasterDev none = {};
         launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
