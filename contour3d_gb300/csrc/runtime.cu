@@ -816,7 +816,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
        triangles fit: the buffer keeps the size of the largest slab so far, at
        least one triangle per two cells */
     if (c.tri_cell.ensure(sizeof(unsigned) * (size_t)(ncell / 2 + 1024), st)) return 1;
-    const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = d_counter + 1;
     unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2); /* triangles, vertices */
@@ -833,6 +832,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     for (size_t ob = 0; ob < nobj; ob++) {
       const FieldDev &F = Fo[ob];
       const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
+      /* read per object: an earlier object of the slab may have grown the buffer */
+      const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
       C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
       if (c.stage_timing) cudaEventRecord(c.evs[0], st);
       launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
