@@ -168,8 +168,25 @@ constexpr unsigned kErrClassifyTimeout = 2u;
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
                   const unsigned char nb_count[19], const unsigned short edge_tris[256 * 19]);
 
-/* TMA-staged planes when the field's layout allows it; `err` receives kErrClassifyTimeout */
-void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, unsigned* err, cudaStream_t st);
+/* the thresholds of the objects of one field, for one classification pass */
+constexpr int kMaxThr = 4;
+struct ThrSet {
+  int n;
+  long long key[kMaxThr];   /* FieldDev::thr_key */
+  int nan[kMaxThr];         /* FieldDev::thr_nan */
+  unsigned fkey[kMaxThr];   /* FieldDev::thr_f_key */
+  int fok[kMaxThr];         /* FieldDev::thr_f_ok */
+};
+struct CodeOut {
+  unsigned char* codes[kMaxThr];
+};
+
+/* cell codes of nf objects of one field (Fs differ only in the threshold)
+   into codes[q]: TMA-staged planes when the field's layout allows it, one
+   pass over the field per kMaxThr objects; `err` receives kErrClassifyTimeout.
+   Returns the number of kernels launched. */
+int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
+                    cudaStream_t st);
 /* cells per slab for which the packed triangle and vertex sums of k_scan stay below 2^31 */
 constexpr long long kMaxSlabCells = 178956970;
 

@@ -177,6 +177,20 @@ __device__ __forceinline__ unsigned char node_above<float>(const FieldDev& F, co
   return (F.thr_f_ok && v == v && f_key(v) >= F.thr_f_key) ? 1 : 0;
 }
 
+/* the same test against threshold t of a set (k_classify_tma classifies the
+   objects of one field together) */
+template <typename T>
+__device__ __forceinline__ unsigned char node_above_thr(const ThrSet& ts, int t, T v);
+template <>
+__device__ __forceinline__ unsigned char node_above_thr<double>(const ThrSet& ts, int t, double v) {
+  const long long b = __double_as_longlong(v);
+  return (!ts.nan[t] && !d_isnan_bits(b) && d_key_bits(b) > ts.key[t]) ? 1 : 0;
+}
+template <>
+__device__ __forceinline__ unsigned char node_above_thr<float>(const ThrSet& ts, int t, float v) {
+  return (ts.fok[t] && v == v && f_key(v) >= ts.fkey[t]) ? 1 : 0;
+}
+
 /* the same test on a value already loaded */
 template <typename T>
 __device__ __forceinline__ unsigned char node_above_value(const FieldDev& F, T v);
@@ -272,13 +286,14 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
   return false;
 }
 
-template <typename T>
+template <typename T, int NT>
 __global__ void __launch_bounds__(kClsX)
-k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, unsigned char* __restrict__ codes,
+k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, ThrSet ts, CodeOut out,
                unsigned* __restrict__ err) {
   constexpr int BX = TmaBox<T>::kX;
   __shared__ __align__(128) unsigned char stage_mem[kTmaStages][TmaBox<T>::kStride];
   auto vals_of = [&](int st) { return reinterpret_cast<const T(*)[BX]>(&stage_mem[st][0]); };
+  /* bit q of each byte: node above threshold q */
   __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
   __shared__ __align__(8) unsigned long long bar[kTmaStages];
   __shared__ int s_fail;
@@ -326,7 +341,11 @@ k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, 
     const T(*vp)[BX] = vals_of(st);
     for (int q = tx; q < (kClsY + 1) * (kClsX + 1); q += kClsX) {
       const int jj = q / (kClsX + 1), ii = q - jj * (kClsX + 1);
-      bp[jj][ii] = node_above_value<T>(F, vp[jj][ii]);
+      const T v = vp[jj][ii];
+      unsigned b = 0;
+#pragma unroll
+      for (int t = 0; t < NT; t++) b |= (unsigned)node_above_thr<T>(ts, t, v) << t;
+      bp[jj][ii] = (unsigned char)b;
     }
     __syncthreads();
     /* stage st is free again: refill it with plane p + kTmaStages */
@@ -345,10 +364,15 @@ k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, 
       for (int jj = 0; jj < kClsY; jj++) {
         const unsigned j = (unsigned)(j0 + jj);
         if (j >= ncy) break; /* the same for the whole block */
-        const unsigned code = b0[jj][tx] | (b0[jj][tx + 1] << 1) | (b0[jj + 1][tx] << 2) |
-                              (b0[jj + 1][tx + 1] << 3) | (b1[jj][tx] << 4) | (b1[jj][tx + 1] << 5) |
-                              (b1[jj + 1][tx] << 6) | (b1[jj + 1][tx + 1] << 7);
-        if (in_x) codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
+        const unsigned c0 = b0[jj][tx], c1 = b0[jj][tx + 1], c2 = b0[jj + 1][tx], c3 = b0[jj + 1][tx + 1];
+        const unsigned c4 = b1[jj][tx], c5 = b1[jj][tx + 1], c6 = b1[jj + 1][tx], c7 = b1[jj + 1][tx + 1];
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+          const unsigned code = ((c0 >> t) & 1) | (((c1 >> t) & 1) << 1) | (((c2 >> t) & 1) << 2) |
+                                (((c3 >> t) & 1) << 3) | (((c4 >> t) & 1) << 4) | (((c5 >> t) & 1) << 5) |
+                                (((c6 >> t) & 1) << 6) | (((c7 >> t) & 1) << 7);
+          if (in_x) out.codes[t][((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
+        }
       }
     }
     __syncthreads(); /* bits[(p + 1) & 1] is rewritten next */
@@ -2652,18 +2676,48 @@ static bool classify_tensor_map(const FieldDev& F, CUtensorMap* map) {
   return r == CUDA_SUCCESS;
 }
 
-void launch_classify(const FieldDev& F, const SlabDev& S, unsigned char* counts, unsigned* err, cudaStream_t st) {
-  /* `counts` receives the cell codes; k_scan turns them into counts */
+template <typename T>
+static void launch_classify_tma(const CUtensorMap& map, const FieldDev& F, const SlabDev& S, const ThrSet& ts,
+                                const CodeOut& out, unsigned* err, const dim3& grid, cudaStream_t st) {
+  switch (ts.n) {
+    case 1: k_classify_tma<T, 1><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
+    case 2: k_classify_tma<T, 2><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
+    case 3: k_classify_tma<T, 3><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
+    default: k_classify_tma<T, 4><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
+  }
+}
+
+int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
+                    cudaStream_t st) {
+  /* codes[q] receives the cell codes of threshold q; k_scan turns them into counts */
+  const FieldDev& F = Fs[0];
   const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
                   (unsigned)((S.nslices + kClsZ - 1) / kClsZ));
   CUtensorMap map;
   if (classify_tensor_map(F, &map)) {
-    if (F.is_f32) k_classify_tma<float><<<grid, kClsX, 0, st>>>(map, F, S, counts, err);
-    else k_classify_tma<double><<<grid, kClsX, 0, st>>>(map, F, S, counts, err);
-    return;
+    /* one pass over the field for up to kMaxThr thresholds */
+    for (int q0 = 0; q0 < nf; q0 += kMaxThr) {
+      ThrSet ts;
+      CodeOut out;
+      ts.n = min(kMaxThr, nf - q0);
+      for (int t = 0; t < ts.n; t++) {
+        const FieldDev& Ft = Fs[q0 + t];
+        ts.key[t] = Ft.thr_key;
+        ts.nan[t] = Ft.thr_nan;
+        ts.fkey[t] = Ft.thr_f_key;
+        ts.fok[t] = Ft.thr_f_ok;
+        out.codes[t] = codes[q0 + t];
+      }
+      if (F.is_f32) launch_classify_tma<float>(map, F, S, ts, out, err, grid, st);
+      else launch_classify_tma<double>(map, F, S, ts, out, err, grid, st);
+    }
+    return (nf + kMaxThr - 1) / kMaxThr;
   }
-  if (F.is_f32) k_classify<float><<<grid, kClsX, 0, st>>>(F, S, counts);
-  else k_classify<double><<<grid, kClsX, 0, st>>>(F, S, counts);
+  for (int q = 0; q < nf; q++) {
+    if (F.is_f32) k_classify<float><<<grid, kClsX, 0, st>>>(Fs[q], S, codes[q]);
+    else k_classify<double><<<grid, kClsX, 0, st>>>(Fs[q], S, codes[q]);
+  }
+  return nf;
 }
 
 long long scan_segments(long long n) { return (n + kScanTile - 1) / kScanTile; }

@@ -807,7 +807,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     S.krender0 = std::max(k0, 1LL);
     S.krender1 = std::min(k1, ncz - 1);
     const long long ncell = S.nslices * per_slice;
-    if (c.counts.ensure((size_t)ncell, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
+    /* one code array per object, each starting on 256 bytes (the scan and the
+       vertex pass read codes with 16-byte loads) */
+    const size_t code_stride = ((size_t)ncell + 255) & ~(size_t)255;
+    if (c.counts.ensure(code_stride * nobj, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
         c.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
         c.tile_state.ensure(2 * sizeof(unsigned long long) * (size_t)scan_segments(ncell), st) ||
         c.scratch.ensure(128, st))
@@ -829,24 +832,30 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       C3D_CUDA(cudaStreamWaitEvent(st, c.chunk_ev[slab_index], 0));
     }
     slab_index++;
+    /* the cell codes of every object of the slab, one pass over the field
+       for up to four objects */
+    std::vector<unsigned char *> obj_codes(nobj);
+    for (size_t q = 0; q < nobj; q++) obj_codes[q] = c.counts.as<unsigned char>() + code_stride * q;
+    C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
+    if (c.stage_timing) cudaEventRecord(c.evs[0], st);
+    c.stats.kernel_launches += (uint64_t)launch_classify(Fo.data(), (int)nobj, S, obj_codes.data(), d_err, st);
+    if (c.stage_timing) cudaEventRecord(c.evs[1], st);
     for (size_t ob = 0; ob < nobj; ob++) {
       const FieldDev &F = Fo[ob];
+      unsigned char *codes = obj_codes[ob];
       const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
       /* read per object: an earlier object of the slab may have grown the buffer */
       const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
-      C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
-      if (c.stage_timing) cudaEventRecord(c.evs[0], st);
-      launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
-      if (c.stage_timing) cudaEventRecord(c.evs[1], st);
-      launch_scan(c.counts.as<unsigned char>(), ncell, seg_sums, seg_base, c.offsets.as<unsigned>(),
-                  c.voffsets.as<unsigned>(), d_total, c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, st);
+      if (c.stage_timing && ob > 0) cudaEventRecord(c.evs[1], st);
+      launch_scan(codes, ncell, seg_sums, seg_base, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
+                  c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, st);
       if (c.stage_timing) cudaEventRecord(c.evs[2], st);
-      c.stats.kernel_launches += 4;
+      c.stats.kernel_launches += 3;
       C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
       if (c.stage_timing) {
-        c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
+        if (ob == 0) c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
         c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
       }
       if (h_small[0]) {
@@ -884,7 +893,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* the screen vertices of the slab's crossed edges, 16 bytes each */
         if (c.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
         VD.pos = c.verts.as<float4>();
-        launch_vertices(F, S, sd, c.counts.as<unsigned char>(), c.voffsets.as<unsigned>(), ncell, VD, st);
+        launch_vertices(F, S, sd, codes, c.voffsets.as<unsigned>(), ncell, VD, st);
         c.stats.kernel_launches += 1;
         c.stats.vertices += NV;
       }
@@ -894,12 +903,12 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       G.F = F;
       G.S = S;
       G.lut = c.lut.as<unsigned long long>();
-      G.codes = c.counts.as<unsigned char>();
+      G.codes = codes;
       G.tri_cell = c.tri_cell.as<unsigned>();
       G.offsets = c.offsets.as<unsigned>();
       if (sink) {
         RasterDev none = {};
-        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, c.offsets.as<unsigned>(),
                     c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
                     st);
         launch_exact_all(G, d_total, (long long)T, tri, st);
@@ -933,7 +942,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           RS.tiny_count = counters + 1;
           C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
           if (c.stage_timing) cudaEventRecord(c.evs[9], st);
-          launch_emit(F, S, sd, c.lut.as<unsigned long long>(), c.counts.as<unsigned char>(), c.offsets.as<unsigned>(),
+          launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, c.offsets.as<unsigned>(),
                       c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
                       st);
           if (c.stage_timing) cudaEventRecord(c.evs[4], st);
@@ -1585,7 +1594,8 @@ extern "C" long contour3d_gb300_debug_cell_counts(const contour3d_contour_obj_t 
   if (c.scratch.ensure(128, st)) return -1;
   unsigned *d_err = c.scratch.as<unsigned>();
   if (cudaMemsetAsync(d_err, 0, sizeof(unsigned), st) != cudaSuccess) return -1;
-  launch_classify(F, S, c.counts.as<unsigned char>(), d_err, st);
+  unsigned char *codes = c.counts.as<unsigned char>();
+  launch_classify(&F, 1, S, &codes, d_err, st);
   std::vector<uint8_t> h(ncell);
   unsigned herr = 0;
   if (cudaMemcpyAsync(h.data(), c.counts.p, ncell, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
@@ -1686,8 +1696,13 @@ static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t sla
     if (sz[0] < 2 || sz[1] < 2 || sz[2] < 2) continue;
     const uint64_t per_slice = (uint64_t)(sz[0] - 1) * (sz[1] - 1);
     uint64_t cells = std::min<uint64_t>(per_slice * (sz[2] - 1), std::max<uint64_t>(slab_cells, per_slice * 3));
+    /* the objects of one field keep one code array each for the slab */
+    uint64_t sharing = 0;
+    for (size_t q = 0; q < fr->num_fields; q++)
+      sharing += fr->fields[q].device_array == fr->fields[n].device_array ? 1 : 0;
     /* candidates and their surviving copy: half a triangle's worth each */
-    const uint64_t bytes = cells * (1 + 4 + 4 + 4) + cells * (kTriBytes + 4 + 4 + 10) + cells * sizeof(Candidate);
+    const uint64_t bytes =
+        cells * (sharing + 4 + 4 + 4) + cells * (kTriBytes + 4 + 4 + 10) + cells * sizeof(Candidate);
     peak = std::max(peak, bytes);
   }
   const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];
