@@ -484,7 +484,7 @@ k_seg_scan(const unsigned long long* __restrict__ seg_sums, long long nseg, unsi
  * segment's base plus a block-wide exclusive scan), and, when the slab's
  * triangles fit `tri_cap`, the triangle -> cell map.
  */
-constexpr int kFillList = 12288; /* triangles of a segment listed in shared memory */
+constexpr int kFillList = 8192; /* triangles of a segment listed in shared memory (4 blocks per SM) */
 constexpr int kStagePitch = 33;  /* words per staged row: conflict-free transposes */
 constexpr size_t kScanWriteSmem =
     sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch + sizeof(unsigned short) * kFillList;
@@ -498,7 +498,7 @@ constexpr size_t kScanWriteSmem =
  * 128 contiguous bytes.  The map goes through a shared list of the segment's
  * triangles when they fit it (then coalesced), else directly.
  */
-__global__ void __launch_bounds__(kScanThreads, 3)
+__global__ void __launch_bounds__(kScanThreads, 4)
 k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigned long long* __restrict__ seg_base,
              unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
              const unsigned long long* __restrict__ totals, unsigned* __restrict__ tri_cell,
@@ -1588,7 +1588,7 @@ __device__ __forceinline__ void write_candidates(const RasterDev& R, unsigned lo
 }
 
 template <bool CHECK>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
 k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
   const long long n = (long long)*R.cover_count;
   const long long W = scene.width, H = scene.height;
