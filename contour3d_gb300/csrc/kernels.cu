@@ -1445,7 +1445,11 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
   tri.meta[t] = meta;
 }
 
-constexpr int kEmitPer = 1; /* triangles per thread and iteration (one: occupancy hides the gathers better than 2 or 3 chains) */
+/* triangles per thread and iteration: one.  k_emit hides its gathers by
+   occupancy, and it reaches all 64 warps per SM only at 32 registers or
+   fewer: two or three chains per thread, or loading the next triangle's
+   entry one iteration ahead, cost registers and measured slower */
+constexpr int kEmitPer = 1;
 
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
