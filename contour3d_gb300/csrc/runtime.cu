@@ -746,7 +746,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   const unsigned long long slab_cells = std::min<unsigned long long>(c.slab_cells, (unsigned long long)kMaxSlabCells);
   long long slab_slices = (long long)(slab_cells / (unsigned long long)per_slice) - 2;
   if (slab_slices < 1) slab_slices = 1;
-  if (pipelined) slab_slices = std::min(slab_slices, (ncz - 2 + kUploadSlabs - 1) / kUploadSlabs);
   if (3 * per_slice > kMaxSlabCells) {
     log_error("z-slices of %lld cells are too large (a slab of three slices must hold at most %lld cells)",
               per_slice, kMaxSlabCells);
@@ -754,9 +753,32 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   }
   const bool want_all = sink != nullptr;
   const long long kr0 = want_all ? 0 : 1, kr1 = want_all ? ncz : ncz - 1;
-  std::vector<long long> starts;
-  for (long long k0 = kr0; k0 < kr1; k0 += slab_slices) starts.push_back(k0);
-  if (sd.z_descending && !want_all) std::reverse(starts.begin(), starts.end());
+  /* the slabs [k0, k1) of rendered slices, in the order they are visited */
+  std::vector<std::pair<long long, long long>> slabs;
+  const bool descending = sd.z_descending && !want_all;
+  if (pipelined) {
+    /* while the field arrives: slabs growing by 1.4 (a slab computes about
+       1.4 times as long as its slices take to arrive, so each chunk lands as
+       the slab before it ends); the compute starts after a seventh */
+    const long long L = kr1 - kr0, first = std::max(2LL, (long long)((double)L / 7.104));
+    const long long second = (long long)(1.4 * (double)first), third = (long long)(1.96 * (double)first);
+    const long long sizes[kUploadSlabs] = {first, second, third, L - first - second - third};
+    bool fits = true;
+    for (const long long z : sizes) fits = fits && z >= 1 && z <= slab_slices;
+    if (fits) {
+      long long k = descending ? kr1 : kr0;
+      for (const long long z : sizes) {
+        slabs.push_back(descending ? std::make_pair(k - z, k) : std::make_pair(k, k + z));
+        k += descending ? -z : z;
+      }
+    } else {
+      slab_slices = std::min(slab_slices, (L + kUploadSlabs - 1) / kUploadSlabs);
+    }
+  }
+  if (slabs.empty()) {
+    for (long long k0 = kr0; k0 < kr1; k0 += slab_slices) slabs.push_back({k0, std::min(k0 + slab_slices, kr1)});
+    if (descending) std::reverse(slabs.begin(), slabs.end());
+  }
   FieldUpload up;
   if (pipelined) {
     /* chunk s: the node slices slab s reads that earlier slabs did not; the
@@ -765,13 +787,13 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     const size_t slice = (size_t)(nx * ny) * elem;
     std::vector<std::pair<size_t, size_t>> ranges;
     long long done_lo = nz, done_hi = 0; /* node slices issued: [done_lo, done_hi) */
-    for (size_t q = 0; q < starts.size(); q++) {
-      const long long k0 = starts[q], k1 = std::min(k0 + slab_slices, kr1);
+    for (size_t q = 0; q < slabs.size(); q++) {
+      const long long k0 = slabs[q].first, k1 = slabs[q].second;
       long long a = std::max(k0 - 1, 0LL), b = std::min(k1, ncz - 1) + 2; /* node slices [a, b) */
       if (q == 0) {
         if (sd.z_descending) b = nz; else a = 0;
       }
-      if (q + 1 == starts.size()) {
+      if (q + 1 == slabs.size()) {
         if (sd.z_descending) a = 0; else b = nz;
       }
       long long ca = a, cb = b;
@@ -798,8 +820,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   int slab_index = 0;
   unsigned *h_small = c.h_small.as<unsigned>();
   unsigned long long *h_total = reinterpret_cast<unsigned long long *>(h_small + 4);
-  for (const long long k0 : starts) {
-    const long long k1 = std::min(k0 + slab_slices, kr1);
+  for (const auto &slab : slabs) {
+    const long long k0 = slab.first, k1 = slab.second;
     SlabDev S;
     S.kfirst = std::max(k0 - 1, 0LL);
     const long long klast = std::min(k1, ncz - 1); /* inclusive */
