@@ -239,3 +239,34 @@ def test_pipelined_host_upload_matches_device_field(gpu, camera):
     assert np.array_equal(img, out.cpu().numpy().reshape(240, 320, 3))
     # both objects take the field in four slabs as it arrives
     assert gpu.stats().slabs == 8
+
+
+def test_five_levels_of_one_field(gpu, oracle):
+    """Five objects on one host field: the objects are classified together
+    (four thresholds in one pass over the field, then the fifth), each keeps
+    its own cell codes, and the image is the reference's."""
+    f, std = fields.modes((30, 26, 34), nmodes=16, kmin=1, kmax=5, power=5.0 / 6.0, seed=31)
+    levels = [(-1.0, (250, 40, 40)), (-0.5, (40, 250, 40)), (0.0, (40, 40, 250)), (0.5, (250, 250, 40)),
+              (1.0, (40, 250, 250))]
+    s = _abi.make_scene(cases.CAM0, cases.CENTRE, 160, 120)
+    s.contours = [_abi.Contour(f, q * std, c) for q, c in levels]
+    assert np.array_equal(gpu.render(s), oracle.render(s))
+
+
+def test_five_levels_of_one_device_f32_field(gpu, oracle):
+    """The same on a float32 field resident on the device (thresholds compared
+    through float keys in the shared pass)."""
+    import torch
+    shape = (26, 30, 22)
+    f32, std = fields.modes(shape, nmodes=16, kmin=1, kmax=5, power=5.0 / 6.0, seed=33, dtype=np.float32)
+    dev = torch.from_numpy(f32).cuda()
+    sizes = (shape[2], shape[1], shape[0])
+    grids = [_abi.unit_grid(n) for n in sizes]
+    levels = [(-0.8 * std, (250, 40, 40)), (-0.3 * std, (40, 250, 40)), (0.1 * std, (40, 40, 250)),
+              (0.4 * std, (250, 250, 40)), (0.9 * std, (40, 250, 250))]
+    scene = _abi.make_scene(cases.CAM0, cases.CENTRE, 160, 120)
+    out = torch.zeros(120 * 160 * 3, dtype=torch.uint8, device="cuda")
+    assert gpu.render_device(scene, [(dev.data_ptr(), 1, sizes, grids, t, c) for t, c in levels], out.data_ptr()) == 0
+    torch.cuda.synchronize()
+    scene.contours = [_abi.Contour(f32.astype(np.float64), t, c) for t, c in levels]
+    assert np.array_equal(out.cpu().numpy().reshape(120, 160, 3), oracle.render(scene))
