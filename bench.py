@@ -42,6 +42,7 @@ CAM = (2.5, 2.0, 1.5)
 CENTRE = (0.5, 0.5, 0.5)
 COLORS = ((0, 255, 255), (255, 255, 0))
 CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
+CPU_SAMPLE_SLICES_1 = 16  # the same for the single-core point
 
 # DRAM bytes (read + write) per unit processed, from one ncu capture of each
 # kernel on the 256^3 case (profiles/*_fourier256_f64.md); the full-size
@@ -152,7 +153,8 @@ def run_large(gpu, n=1536, frames=2):
     |k| 1..48 with amplitude |k|^-11/6, four levels at +-0.5 and +-1 std,
     3840x2160, generated on the device; device-resident rendering.  The FP32
     field is widened exactly when read, so the result is the reference's FP64
-    arithmetic on those values (no FP32 arithmetic error to report)."""
+    arithmetic on those values; what FP32 storage changes is the input, which
+    fp32_input_vs_fp64 measures on a 256^3 field of the same spectrum."""
     import torch
     from contour3d_gb300 import _abi, workloads
     f, std = workloads.modes_device(gpu, (n, n, n), nmodes=256, kmin=1, kmax=48, power=11.0 / 6.0, seed=4,
@@ -183,6 +185,28 @@ def run_large(gpu, n=1536, frames=2):
            "library_device_gb": gpu.lib.contour3d_gb300_device_bytes() / 1e9, "field_gb": f.numel() * 4 / 1e9}
     del f
     torch.cuda.empty_cache()
+    # the FP32 input against the FP64 one: a 256^3 field of the same mode
+    # spectrum in f64 and its rounding to f32, the same levels, 1024x1024
+    fd, sd = workloads.modes_device(gpu, (256, 256, 256), nmodes=256, kmin=1, kmax=48, power=11.0 / 6.0, seed=4,
+                                    dtype=torch.float64)
+    ff = fd.float().contiguous()
+    s2 = _abi.make_scene(CAM, CENTRE, 1024, 1024)
+    g2 = [_abi.unit_grid(256)] * 3
+    lv2 = [-sd, -0.5 * sd, 0.5 * sd, sd]
+    imgs, tris = [], []
+    for t, dt in ((fd, 0), (ff, 1)):
+        o = torch.empty(1024 * 1024 * 3, dtype=torch.uint8, device="cuda")
+        if gpu.render_device(s2, [(t.data_ptr(), dt, (256, 256, 256), g2, lv, c)
+                                  for lv, c in zip(lv2, workloads.PALETTE)], o.data_ptr()) != 0:
+            raise RuntimeError("fp32 comparison: render failed")
+        torch.cuda.synchronize()
+        imgs.append(o.view(1024 * 1024, 3).cpu().numpy().astype(np.int16))
+        tris.append(int(gpu.stats().triangles))
+    d = np.abs(imgs[0] - imgs[1]).max(axis=1)
+    out["fp32_input_vs_fp64"] = {"field": "256^3, same spectrum; f32 = f64 rounded", "image": "1024x1024, 4 levels",
+                                 "pixels_differing": int((d > 0).sum()), "pixels": 1024 * 1024,
+                                 "max_channel_diff": int(d.max()), "triangles_f64": tris[0], "triangles_f32": tris[1]}
+    del fd, ff
     return out
 
 
@@ -532,6 +556,10 @@ def main():
         cpu = {"value": v, "unit": "cell-thresholds/s", "cores": cores, "kind": "port",
                "sample": f"512x512x{CPU_SAMPLE_SLICES} z-slab of the same field, two thresholds, 1920x1080, "
                          f"oracle/c3d_oracle.c with {cores} threads ({dt:.2f} s)"}
+        # one core, on a thinner slab of the same field
+        v1, dt1, _ = cpu_baseline(field[:CPU_SAMPLE_SLICES_1].cpu().numpy(), std, 1)
+        cpu["sweep"] = [{"cores": 1, "value": v1, "sample": f"512x512x{CPU_SAMPLE_SLICES_1} z-slab ({dt1:.2f} s)"},
+                        {"cores": cores, "value": v, "sample": f"512x512x{CPU_SAMPLE_SLICES} z-slab ({dt:.2f} s)"}]
 
     if rank == 0:
         out = {
