@@ -51,6 +51,9 @@ struct FieldDev {
   /* bound on the FP64 rounding of one screen coordinate in the reference's
      projection (project.c:26-66) of a point of this block, in this scene */
   float proj_eps;
+  /* shading only: the cell codes of the whole block ((k ncy + j) ncx + i), when
+     they are still in memory (the object took one slab), else null */
+  const unsigned char* codes;
 };
 
 /* the constants of FastDiv for d >= 1 */

@@ -2117,6 +2117,16 @@ __device__ __forceinline__ float unit_vec(const float A[3], float e, float U[3])
 
 /* code of cell (i, j, k) whose corner 0 is node `base` */
 template <typename T>
+__device__ __forceinline__ unsigned cell_code_at(const FieldDev& F, long long base);
+
+/* the same, read from the classification's codes when they are kept */
+template <typename T>
+__device__ __forceinline__ unsigned cell_code_ijk(const FieldDev& F, long long i, long long j, long long k) {
+  if (F.codes) return __ldg(F.codes + (k * (F.ny - 1) + j) * (F.nx - 1) + i);
+  return cell_code_at<T>(F, (k * F.ny + j) * F.nx + i);
+}
+
+template <typename T>
 __device__ __forceinline__ unsigned cell_code_at(const FieldDev& F, long long base) {
   const T* f = static_cast<const T*>(F.data);
   unsigned code = 0;
@@ -2252,13 +2262,13 @@ k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __r
       ok = winner_cell(F, lo, obase, wc);
     }
     if (ok && m < 3) {
-      const unsigned code = cell_code_at<T>(F, (wc.k * F.ny + wc.j) * F.nx + wc.i);
+      const unsigned code = cell_code_ijk<T>(F, wc.i, wc.j, wc.k);
       const int ed = (int)((__ldg(lut + code * 12 + wc.r) >> (18 + 5 * m)) & 31);
       const int nn = c_nb_count[ed];
       for (int s = 0; s < nn; s++) {
         const long long ni = wc.i + c_nb[ed][s][2], nj = wc.j + c_nb[ed][s][1], nk = wc.k + c_nb[ed][s][0];
         const unsigned le = (unsigned)c_nb[ed][s][3];
-        const unsigned ncode = cell_code_at<T>(F, (nk * F.ny + nj) * F.nx + ni);
+        const unsigned ncode = cell_code_ijk<T>(F, ni, nj, nk);
         for (unsigned mask = __ldg(g_edge_tris + ncode * 19 + le); mask; mask &= mask - 1) {
           const int r = __ffs(mask) - 1;
           bool fresh;
@@ -2281,7 +2291,7 @@ k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __r
       const long long i = (long long)((key >> 4) & 0xFFFFFu), j = (long long)((key >> 24) & 0xFFFFFu);
       const long long k = (long long)(key >> 44);
       const long long nb = (k * F.ny + j) * F.nx + i;
-      const unsigned code = cell_code_at<T>(F, nb);
+      const unsigned code = cell_code_ijk<T>(F, i, j, k);
       const unsigned long long e = __ldg(lut + code * 12 + (key & 15u));
       const float sp[3] = {__ldg(F.dgx + i), __ldg(F.dgy + j), __ldg(F.dgz + k)};
       const T* fd = static_cast<const T*>(F.data);
@@ -2372,9 +2382,9 @@ __device__ __forceinline__ void for_edge_triangles(const FieldDev& F, const unsi
   for (int q = 0; q < nn; q++) {
     const long long ni = i + c_nb[ed][q][2], nj = j + c_nb[ed][q][1], nk = k + c_nb[ed][q][0];
     const unsigned le = (unsigned)c_nb[ed][q][3];
-    double vals[8];
-    const unsigned code = cell_code_any(F, ni, nj, nk, vals);
     const unsigned long long cell = (unsigned long long)((nk * ncy + nj) * ncx + ni);
+    double vals[8];
+    const unsigned code = F.codes ? (unsigned)__ldg(F.codes + cell) : cell_code_any(F, ni, nj, nk, vals);
     /* ascending rank: the reference's order within the cell */
     for (unsigned mask = __ldg(g_edge_tris + code * 19 + le); mask; mask &= mask - 1)
       fn(cell * 16ULL + (unsigned long long)(__ffs(mask) - 1));

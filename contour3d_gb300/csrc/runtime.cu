@@ -704,6 +704,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   }
   FieldDev F;
   F.data = dfield;
+  F.codes = nullptr;
   F.is_f32 = ci.f32 ? 1 : 0;
   F.nx = nx;
   F.ny = ny;
@@ -818,6 +819,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
              static_cast<char *>(c.field.p), static_cast<const char *>(ci.data), ranges);
   }
   int slab_index = 0;
+  /* the last slab's code arrays: the whole field's when that slab covers it */
+  std::vector<unsigned char *> last_codes(nobj, nullptr);
+  bool codes_whole = false;
   unsigned *h_small = c.h_small.as<unsigned>();
   unsigned long long *h_total = reinterpret_cast<unsigned long long *>(h_small + 4);
   for (const auto &slab : slabs) {
@@ -858,6 +862,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
        for up to four objects */
     std::vector<unsigned char *> obj_codes(nobj);
     for (size_t q = 0; q < nobj; q++) obj_codes[q] = c.counts.as<unsigned char>() + code_stride * q;
+    last_codes = obj_codes;
+    codes_whole = S.kfirst == 0 && S.nslices == ncz;
     C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
     c.stats.kernel_launches += (uint64_t)launch_classify(Fo.data(), (int)nobj, S, obj_codes.data(), d_err, st);
@@ -1054,7 +1060,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
       C3D_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st));
       if (c.stage_timing) cudaEventRecord(c.evs[6], st);
-      launch_shade_f(Fo[ob], sd, RS, c.lut.as<unsigned long long>(), obase, rgb, st);
+      /* the classification's codes, when the slab loop left the whole field's */
+      FieldDev Fs = Fo[ob];
+      Fs.codes = codes_whole ? last_codes[ob] : nullptr;
+      launch_shade_f(Fs, sd, RS, c.lut.as<unsigned long long>(), obase, rgb, st);
       if (c.stage_timing) cudaEventRecord(c.evs[10], st);
       C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
       C3D_CUDA(cudaStreamSynchronize(st));
@@ -1074,7 +1083,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           const unsigned long long cap =
               std::min(c.nb_ent.cap / sizeof(unsigned long long), c.nb_wn.cap / (3 * sizeof(double)));
           C3D_CUDA(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), st));
-          launch_shade_exact(Fo[ob], sd, RS, c.lut.as<unsigned long long>(), list, lcount, (long long)namb, obase,
+          launch_shade_exact(Fs, sd, RS, c.lut.as<unsigned long long>(), list, lcount, (long long)namb, obase,
                              c.nb_ent.as<unsigned long long>(), cap, counters + 2, c.nb_span.as<uint2>(),
                              c.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
           c.stats.kernel_launches += 3;
