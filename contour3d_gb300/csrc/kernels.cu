@@ -549,21 +549,28 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
   const bool keep_offsets = want_offsets || !fill;
   unsigned* stage = stage_all + warp * 32 * kStagePitch;
   const long long wbase = c0 + (long long)warp * 32 * kScanItems; /* the warp's first cell */
+  if (listed) {
+    /* the shared list: each cell writes its first triangle's slot only; the
+       other slots stay marked and find their cell by walking back */
+    for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) s_list[e] = 0xFFFFu;
+    __syncthreads();
+  }
   for (int half = 1; half >= 0; half--) {
-    /* half 1: vertex offsets; half 0: triangle offsets and the map (the
-       staged triangle offsets stay for the copy of the map below) */
+    /* half 1: vertex offsets; half 0: triangle offsets (staged only when
+       they are stored) and the map */
     unsigned long long run = first;
 #pragma unroll
     for (int q = 0; q < kScanItems; q++) {
       const unsigned cnt = s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
       const unsigned t0 = (unsigned)(run & kTriMask);
-      stage[kStagePitch * lane + q] = half == 0 ? t0 : (unsigned)(run >> 31);
+      if (half == 1 || keep_offsets) stage[kStagePitch * lane + q] = half == 0 ? t0 : (unsigned)(run >> 31);
       if (half == 0 && (listed || direct) && base + q < n) {
         const unsigned nt = cnt & 0xFFFFu;
-        if (listed)
-          for (unsigned r = 0; r < nt; r++) s_list[t0 - ta + r] = (unsigned short)(base + q - c0);
-        else
+        if (listed) {
+          if (nt) s_list[t0 - ta] = (unsigned short)(base + q - c0);
+        } else {
           for (unsigned r = 0; r < nt; r++) tri_cell[t0 + r] = (unsigned)(base + q) | (r << kTcRankShift);
+        }
       }
       run += packed_count(cnt);
     }
@@ -592,11 +599,11 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
   if (listed) {
     __syncthreads();
     for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) {
-      /* the cell's first triangle from the staged offsets: cell l of the
-         segment was lane (l % 1024) / 32, item l % 32 of warp l / 1024 */
-      const unsigned l = s_list[e];
-      const unsigned t0 = stage_all[(l >> 10) * 32 * kStagePitch + kStagePitch * ((l >> 5) & 31) + (l & 31)];
-      tri_cell[ta + e] = ((unsigned)c0 + l) | ((ta + e - t0) << kTcRankShift);
+      /* back to the cell's first triangle (a cell has at most 12; slot 0
+         always starts a cell): its cell, and the rank is the distance */
+      unsigned k = e, l = s_list[e];
+      while (l == 0xFFFFu && k > 0) l = s_list[--k];
+      tri_cell[ta + e] = ((unsigned)c0 + l) | ((e - k) << kTcRankShift);
     }
   }
 }
