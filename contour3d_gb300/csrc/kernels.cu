@@ -1844,7 +1844,7 @@ __device__ __forceinline__ bool screen_edges(const Geo& G, const SceneDev& s, un
 }
 
 template <typename T, bool CHECK>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
 k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
   const long long n = (long long)*R.sliver_count;
   const long long W = scene.width, H = scene.height;
