@@ -408,7 +408,7 @@ struct Ctx {
   HostBuf h_small, h_rgb, h_slots;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[11] = {};
   bool stage_timing = false;
-  unsigned long long slab_cells = 1ULL << 27;
+  unsigned long long slab_cells = kMaxSlabCells; /* the most the scan's 32-bit packed sums allow */
   contour3d_gb300_stats_t stats = {};
   const void *field_src = nullptr; /* host array currently in `field` (valid within one call) */
   size_t field_bytes = 0;
@@ -1846,7 +1846,7 @@ extern "C" int contour3d_gb300_server_submit(contour3d_gb300_server_t *sv, const
   if (!sv || !frame || !ticket) return 1;
   auto *r = new Request();
   r->frame = frame;
-  r->estimate = request_estimate(frame, 1ULL << 27);
+  r->estimate = request_estimate(frame, kMaxSlabCells);
   r->t_submit = now_ms();
   {
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -1918,7 +1918,7 @@ extern "C" int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frame
   std::vector<uint64_t> est(num_frames);
   for (size_t n = 0; n < num_frames; n++) {
     order[n] = n;
-    est[n] = request_estimate(frames + n, 1ULL << 27);
+    est[n] = request_estimate(frames + n, kMaxSlabCells);
   }
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return est[a] > est[b]; });
   std::vector<uint64_t> tickets(num_frames);

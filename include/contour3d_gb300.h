@@ -212,7 +212,8 @@ int contour3d_gb300_set_stage_timing(int on);
  * certified bounds (slow; for tests), 0 = off (default)
  */
 int contour3d_gb300_set_filter_check(int on);
-/* upper bound on cells per slab (default 2^27); smaller slabs use less memory */
+/* upper bound on cells per slab (default and maximum 178,956,970, the most the
+   scan's packed 32-bit sums allow); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);
 
 /* ------------------------------------------------------------------ */

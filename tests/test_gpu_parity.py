@@ -98,7 +98,7 @@ def test_slab_size_does_not_change_the_image(gpu, slab_cells):
         img = gpu.render(scene)
         tris = [gpu.triangles(c)[0] for c in scene.contours]
     finally:
-        gpu.set_slab_cells(1 << 27)
+        gpu.set_slab_cells(178956970)  # the default
     assert np.array_equal(img, g["rgb"])
     assert np.concatenate(tris).tobytes() == g["triangles"].tobytes()
 
