@@ -48,10 +48,10 @@ CPU_SAMPLE_SLICES_1 = 16  # the same for the single-core point
 # kernel on the 256^3 case (profiles/*_fourier256_f64.md); the full-size
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
-    "classify": (8.77, "cells"),     # k_classify_tma: 145.4 MB for 16.6 M cells
-    "scan": (5.47, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 90.7 MB for 16.6 M cells
-    "vertices": (36.5, "vertices"),  # k_vertices: 238.7 MB for 6.55 M vertices
-    "emit": (43.9, "triangles"),     # k_emit: 575.2 MB for 13.1 M triangles
+    "classify": (4.60, "cells"),     # k_classify_tma, both levels in one pass: 152.4 MB for 2 x 16.6 M cells
+    "scan": (5.49, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 91.1 MB for 16.6 M cells
+    "vertices": (36.5, "vertices"),  # k_vertices: 239.2 MB for 6.55 M vertices
+    "emit": (43.6, "triangles"),     # k_emit: 571.6 MB for 13.1 M triangles
 }
 
 
@@ -482,7 +482,7 @@ def main():
     # algorithmic bytes per frame (both objects): the bytes each stage must move
     # once -- inputs read once, outputs written once, cached re-reads not counted
     stage_bytes = {
-        "classify": 2 * (nodes * 8 + cells * 1),
+        "classify": nodes * 8 + 2 * cells * 1,  # one pass over the field for both levels
         "scan": 2 * cells * (1 + 4) + T * 4,
         "vertices": 2 * cells * (4 + 1) + V * (2 * 8 + 16),
         "emit": T * (4 + 4) + 2 * cells * (4 + 1) + V * 16 + listed * 48 + float(prof.tiny) * 4,
