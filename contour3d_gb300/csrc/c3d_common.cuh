@@ -210,9 +210,6 @@ __device__ __forceinline__ unsigned f_key(float x) {
   if ((u << 1) == 0) u = 0;
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
-__device__ __forceinline__ float f_from_key(unsigned k) {
-  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
-}
 
 /*
  * double -> float with integer operations only (the hardware conversion runs

@@ -71,10 +71,6 @@ __device__ __forceinline__ double load_value<double>(const double* f, long long 
   return __longlong_as_double(ld_bits(f + idx));
 }
 
-__device__ __forceinline__ long long corner_index(const FieldDev& F, long long i, long long j, long long k, int c) {
-  return ((k + (c >> 2)) * F.ny + j + ((c >> 1) & 1)) * F.nx + i + (c & 1);
-}
-
 /* bit c of the result: threshold < value at corner c of cell (i, j, k) */
 template <typename T>
 __device__ __forceinline__ unsigned cell_code(const FieldDev& F, long long i, long long j, long long k,
@@ -189,18 +185,6 @@ __device__ __forceinline__ unsigned char node_above_thr<double>(const ThrSet& ts
 template <>
 __device__ __forceinline__ unsigned char node_above_thr<float>(const ThrSet& ts, int t, float v) {
   return (ts.fok[t] && v == v && f_key(v) >= ts.fkey[t]) ? 1 : 0;
-}
-
-/* the same test on a value already loaded */
-template <typename T>
-__device__ __forceinline__ unsigned char node_above_value(const FieldDev& F, T v);
-template <>
-__device__ __forceinline__ unsigned char node_above_value<double>(const FieldDev& F, double v) {
-  return (!F.thr_nan && !d_isnan(v) && d_key(v) > F.thr_key) ? 1 : 0;
-}
-template <>
-__device__ __forceinline__ unsigned char node_above_value<float>(const FieldDev& F, float v) {
-  return (F.thr_f_ok && v == v && f_key(v) >= F.thr_f_key) ? 1 : 0;
 }
 
 template <typename T>
