@@ -180,8 +180,8 @@ typedef struct {
   uint64_t candidates;        /* fragments the single-precision filter could not settle */
   uint64_t candidate_overflows; /* raster passes repeated because a list was full */
   uint64_t tiny;              /* triangles too small for the FP32 filter (resolved in FP64) */
-  uint64_t winners;           /* pixels whose owner was shaded (summed over slabs) */
-  uint64_t normals;           /* weighted face normals computed for shading */
+  uint64_t winners;           /* pixels shaded (each object's won pixels, summed over objects) */
+  uint64_t normals;           /* neighbour-triangle normals of the FP64 shading pass */
   uint64_t slabs;             /* slab passes */
   uint64_t kernel_launches;   /* kernels launched by the library */
   double ms_total;            /* device time of the whole frame (events) */
@@ -197,8 +197,8 @@ typedef struct {
   uint64_t slivers;           /* triangles whose area may be clamped (reference box tested in FP32) */
   uint64_t vertices;          /* crossed edges whose screen position was computed (all slabs) */
   double ms_vertices;         /* stage timing: triangle -> cell map and screen vertices */
-  double ms_normals;          /* stage timing: won pixels, normal requests, weighted normals
-                                 (ms_shade is then the colour passes) */
+  double ms_normals;          /* stage timing: won pixels and the FP32 shading pass
+                                 (ms_shade is then the FP64 shading pass) */
   uint64_t shade_exact;       /* won pixels whose colour the FP32 shading could not settle (shaded in FP64) */
   uint64_t shade_violations;  /* self-check: FP32 colours that differ from the FP64 ones (must stay 0) */
 } contour3d_gb300_stats_t;
