@@ -653,7 +653,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     dfield = c.field.p;
   }
-  /* node coordinates, and their float roundings for the single-precision filter */
   /* node coordinates, their float roundings, and the node spacings g[i + 1] -
      g[i] rounded to float (single-precision shading) */
   const size_t ng = (size_t)(nx + ny + nz);
