@@ -58,7 +58,7 @@ TRAFFIC_PER_UNIT = {
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -101,9 +101,14 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # the timed region starts once the sampler is running (its first line is out)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0 and os.path.getsize(self.path) == 0:
+            time.sleep(0.005)
 
     def stop(self):
         if self.proc is None:
