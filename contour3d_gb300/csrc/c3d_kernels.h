@@ -171,14 +171,16 @@ constexpr unsigned kErrClassifyTimeout = 2u;
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
                   const unsigned char nb_count[19], const unsigned short edge_tris[256 * 19]);
 
-/* the thresholds of the objects of one field, for one classification pass */
+/* the thresholds of the objects of one field, for one classification pass,
+   as ranges of sign-folded keys (bits ^ (sign ? 0x7FF..F : 0), signed order
+   == numeric order, -0 just below +0, NaNs beyond +-inf): a node is above
+   threshold t when (key - lo[t]) < cnt[t] as unsigned, i.e. lo <= key <=
+   key(+inf).  cnt 0: nothing is above (NaN threshold, or none above it). */
 constexpr int kMaxThr = 4;
 struct ThrSet {
   int n;
-  long long key[kMaxThr];   /* FieldDev::thr_key */
-  int nan[kMaxThr];         /* FieldDev::thr_nan */
-  unsigned fkey[kMaxThr];   /* FieldDev::thr_f_key */
-  int fok[kMaxThr];         /* FieldDev::thr_f_ok */
+  unsigned long long lo[kMaxThr], cnt[kMaxThr]; /* double fields */
+  unsigned flo[kMaxThr], fcnt[kMaxThr];         /* float fields */
 };
 struct CodeOut {
   unsigned char* codes[kMaxThr];
