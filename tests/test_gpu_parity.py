@@ -216,6 +216,63 @@ def test_float32_field_threshold_edges(gpu, oracle):
         assert np.array_equal(out.cpu().numpy().reshape(48, 64, 3), ref)
 
 
+DBL_MAX = 1.7976931348623157e308
+DBL_TRUE_MIN = 5e-324
+
+
+def test_tma_classify_special_values(gpu, oracle):
+    """The TMA classification (x = 20 nodes: 160-byte rows) on a field holding
+    NaNs of both signs and several payloads, +-inf, +-0, denormals, +-DBL_MAX
+    and values equal to the thresholds, against thresholds at the ends of
+    the key ranges.  Only the codes are compared (no vertex is built), so
+    non-finite values are fine here; triangulate.c's test is thr < value."""
+    rng = np.random.default_rng(8)
+    f = rng.standard_normal((14, 13, 20))
+    nans = np.array([0x7FF8000000000000, 0xFFF8000000000000, 0x7FF0000000000001, 0xFFFFFFFFFFFFFFFF],
+                    dtype=np.uint64).view(np.float64)
+    special = np.concatenate([nans, [np.inf, -np.inf, 0.0, -0.0, DBL_TRUE_MIN, -DBL_TRUE_MIN, DBL_MAX, -DBL_MAX,
+                                     0.5, -0.5]])
+    flat = f.reshape(-1)
+    idx = rng.choice(flat.size, 700, replace=False)
+    flat[idx] = special[rng.integers(0, special.size, idx.size)]
+    for thr in (0.0, -0.0, DBL_TRUE_MIN, -DBL_TRUE_MIN, np.inf, -np.inf, np.nan, DBL_MAX, -DBL_MAX, 0.5, -0.5,
+                float(flat[3]), 1e-300, -1e-300):
+        a, ta = gpu.cell_counts(f, thr)
+        b, tb = oracle.cell_counts(f, thr)
+        assert ta == tb and np.array_equal(a, b), thr
+
+
+def test_tma_classify_float32_threshold_edges(gpu, oracle):
+    """The TMA classification of a float32 field (x = 20 nodes: 80-byte rows),
+    one and two levels per pass, at thresholds between floats, at a float,
+    +-0, beyond FLT_MAX, infinite and NaN, against the oracle on the widened
+    field."""
+    import torch
+    rng = np.random.default_rng(6)
+    f32 = (rng.standard_normal((18, 17, 20)) * 0.5).astype(np.float32)
+    f32.flat[::97] = 0.0
+    f32.flat[5::101] = -0.0
+    as64 = f32.astype(np.float64)
+    v = float(f32.flat[3])
+    between = float(np.nextafter(f32.flat[3], np.float32(1))) * 0.5 + v * 0.5
+    scene = _abi.make_scene(cases.CAM0, cases.CENTRE, 64, 48)
+    out = torch.zeros(64 * 48 * 3, dtype=torch.uint8, device="cuda")
+    dev = torch.from_numpy(f32).cuda()
+    sizes = (20, 17, 18)
+    grids = [_abi.unit_grid(n) for n in sizes]
+    levels = [(0.0,), (-0.0,), (v,), (between,), (1e-50,), (-1e-50,), (3.5e38,), (-3.5e38,), (np.inf,), (-np.inf,),
+              (np.nan,), (0.1, -0.2), (v, between), (-0.0, 0.3)]
+    cols = ((9, 200, 90), (200, 30, 120))
+    for lv in levels:
+        objs = [(dev.data_ptr(), 1, sizes, grids, t, c) for t, c in zip(lv, cols)]
+        assert gpu.render_device(scene, objs, out.data_ptr()) == 0
+        torch.cuda.synchronize()
+        scene.contours = [_abi.Contour(as64, t, c) for t, c in zip(lv, cols)]
+        ref = oracle.render(scene)
+        scene.contours = []
+        assert np.array_equal(out.cpu().numpy().reshape(48, 64, 3), ref), lv
+
+
 @pytest.mark.parametrize("camera", [(2.5, 2.0, 1.5), (0.6, 0.4, 3.0)], ids=["ascending-z", "descending-z"])
 def test_pipelined_host_upload_matches_device_field(gpu, camera):
     """A host field large enough to be uploaded in chunks, with the slabs of
