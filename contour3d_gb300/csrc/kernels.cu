@@ -442,10 +442,11 @@ __global__ void __launch_bounds__(kScanThreads)
 k_seg_reduce(const unsigned char* __restrict__ codes, long long n, unsigned long long* __restrict__ seg_sums) {
   __shared__ unsigned s_cnt[256];
   __shared__ unsigned long long s_warp[kScanThreads / 32];
+  unsigned wv[kScanItems / 4];
+  /* the codes are in flight while the count table is built */
+  load_scan_codes(codes, (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems, n, wv);
   load_count_lut(s_cnt);
   __syncthreads();
-  unsigned wv[kScanItems / 4];
-  load_scan_codes(codes, (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems, n, wv);
   unsigned long long sum = 0;
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) sum += packed_count(s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
@@ -535,12 +536,16 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
   unsigned* stage_all = reinterpret_cast<unsigned*>(scan_smem);
   unsigned short* s_list = /* segment-local cell of each of the segment's triangles */
       reinterpret_cast<unsigned short*>(scan_smem + sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch);
-  load_count_lut(s_cnt);
-  __syncthreads();
   const long long c0 = (long long)blockIdx.x * kScanTile;
   const long long base = c0 + (long long)threadIdx.x * kScanItems;
   unsigned wv[kScanItems / 4];
+  /* the codes, the segment base and the slab total are in flight while the
+     count table is built */
   load_scan_codes(codes, base, n, wv);
+  const unsigned long long seg0 = seg_base[blockIdx.x];
+  const unsigned long long slab_tris = totals[0];
+  load_count_lut(s_cnt);
+  __syncthreads();
   unsigned long long sum = 0;
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) sum += packed_count(s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
@@ -563,11 +568,10 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
     if (lane < kScanThreads / 32) s_warp[lane] = w;
   }
   __syncthreads();
-  const unsigned long long seg0 = seg_base[blockIdx.x];
   const unsigned long long first = seg0 + (warp ? s_warp[warp - 1] : 0ULL) + incl - sum;
   const unsigned seg_tris = (unsigned)(s_warp[kScanThreads / 32 - 1] & kTriMask);
   const unsigned ta = (unsigned)(seg0 & kTriMask);
-  const bool fill = totals[0] <= tri_cap;
+  const bool fill = slab_tris <= tri_cap;
   const bool listed = fill && seg_tris <= (unsigned)kFillList;
   const bool direct = fill && !listed;
   /* the triangle offsets are kept only when asked for or when the map must
