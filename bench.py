@@ -135,6 +135,26 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_baseline(field_sample: np.ndarray, std: float, cores: int):
     """The CPU oracle on a z-slab sample of the same field, one thread per core."""
     from contour3d_gb300 import _abi
@@ -394,8 +414,8 @@ def run_reference(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fourier field)",
         "impl": "reference",
         "config": {"workload": "fourier-512^3-f64-2thr-1920x1080", "sample": sample_desc},
-        "cpu_baseline": {"value": value, "unit": "cell-thresholds/s", "cores": cores, "kind": "port",
-                         "sample": sample_desc},
+        "cpu_baseline": {"value": value, "unit": "cell-thresholds/s", "cores": cores, "cpu_model": cpu_model(),
+                         "kind": "port", "sample": sample_desc},
         "e2e": {"value": value, "unit": "cell-thresholds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -560,7 +580,7 @@ def main():
         sample = field[:CPU_SAMPLE_SLICES].cpu().numpy()
         cores = os.cpu_count() or 1
         v, dt, c = cpu_baseline(sample, std, cores)
-        cpu = {"value": v, "unit": "cell-thresholds/s", "cores": cores, "kind": "port",
+        cpu = {"value": v, "unit": "cell-thresholds/s", "cores": cores, "cpu_model": cpu_model(), "kind": "port",
                "sample": f"512x512x{CPU_SAMPLE_SLICES} z-slab of the same field, two thresholds, 1920x1080, "
                          f"oracle/c3d_oracle.c with {cores} threads ({dt:.2f} s)"}
         # one core, on a thinner slab of the same field
