@@ -103,3 +103,42 @@ def test_against_reference_build(tmp_path):
         s.lines = _abi.cube_edges(nitems=2 + seed, width=1.0 + seed)
         assert np.array_equal(ref.render(s, str(tmp_path)), orc.render(s))
         assert ref.triangles(s.contours[0])[0].tobytes() == orc.triangles(s.contours[0])[0].tobytes()
+
+
+def test_against_reference_build_special_values(tmp_path):
+    """NaNs (both signs, several payloads), +-inf, +-0, denormals and
+    +-DBL_MAX in the field, at thresholds on the edges of the comparison
+    (triangulate.c: threshold < value): the oracle's triangle counts and
+    images equal the compiled reference's, and its triangle records equal
+    them value for value, NaN where the reference has NaN.  The NaN bit
+    patterns themselves are not compared: which operand's payload and sign an
+    x86 operation propagates depends on the compiler's operand order, which
+    differs between the two builds."""
+    from oracle import lib as olib
+    from contour3d_gb300 import _abi
+    if not os.path.isdir(olib.REF_TREE):
+        pytest.skip("reference tree not present on this host")
+    olib.build(with_reference=True)
+    ref, orc = olib.Reference(), olib.Oracle()
+    dbl_max, tmin = 1.7976931348623157e308, 5e-324
+    rng = np.random.default_rng(8)
+    f = rng.standard_normal((14, 13, 20))
+    nans = np.array([0x7FF8000000000000, 0xFFF8000000000000, 0x7FF0000000000001, 0xFFFFFFFFFFFFFFFF],
+                    dtype=np.uint64).view(np.float64)
+    special = np.concatenate([nans, [np.inf, -np.inf, 0.0, -0.0, tmin, -tmin, dbl_max, -dbl_max, 0.5, -0.5]])
+    flat = f.reshape(-1)
+    idx = rng.choice(flat.size, 700, replace=False)
+    flat[idx] = special[rng.integers(0, special.size, idx.size)]
+    for thr in (0.0, -0.0, tmin, -tmin, np.inf, -np.inf, np.nan, dbl_max, -dbl_max, 0.5, -0.5):
+        c = _abi.Contour(f, thr, (200, 100, 50))
+        rt, rn = ref.triangles(c)
+        ot, on = orc.triangles(c)
+        assert rn == on and rt.shape == ot.shape, thr
+        for name in rt.dtype.names:
+            if rt[name].dtype.kind == "f":
+                assert np.array_equal(rt[name], ot[name], equal_nan=True), (thr, name)
+            else:
+                assert np.array_equal(rt[name], ot[name]), (thr, name)
+        s = _abi.make_scene((2.5, 2.0, 1.5), (0.5, 0.5, 0.5), 90, 70)
+        s.contours = [c]
+        assert np.array_equal(ref.render(s, str(tmp_path)), orc.render(s)), thr
