@@ -1,28 +1,41 @@
 /*
  * kernels.cu -- sm_103a kernels of the isosurface-to-image path.
  *
- * One contour object is processed in z-slabs of cells.  Per slab:
- *   k_classify   cell codes -> triangle count per cell          (HBM: field read)
- *   k_scan       decoupled-look-back exclusive scan of the counts, writing
- *                per-cell offsets and the triangle -> cell map
- *   k_emit       one thread per triangle: cube-edge ids; for rendered
- *                triangles the vertices and their screen projection in FP32
- *                with certified bounds (two FP64 subtractions per vertex)
- *   k_cover      one thread per rendered triangle: FP32 coverage and depth
- *                intervals over its bounding box; certainly drawn fragments
- *                raise a per-pixel depth floor, the rest become candidates
- *   k_tiny       one thread per triangle too small for FP32 bounds: the
- *                reference's arithmetic for its few possible pixels
- *   k_exact      one thread per candidate that can still reach the floor:
- *                the reference's vertices (recomputed from the field),
- *                projection, barycentric test and harmonic depth in FP64,
- *                then a 128-bit (depth, order) max into the z-buffer
- *   k_winners    one thread per pixel: the pixels this slab won, and the
- *                triangles sharing a cube edge with their vertices
- *   k_wn         one thread per such triangle: its exact area-weighted
- *                face normal
- *   k_shade      one thread per won pixel: vertex normals (normal.c order)
- *                and the shading
+ * The contour objects of one field are classified together, then each
+ * object is processed in z-slabs of cells, then shaded once:
+ *   k_classify_tma  cell codes of up to four thresholds per pass over the
+ *                   field (TMA node planes; k_classify where TMA cannot
+ *                   address the field)                         (HBM: field read)
+ * per slab of an object:
+ *   k_seg_reduce, k_seg_scan, k_scan_write
+ *                   packed (triangle, vertex) counts per segment, a one-block
+ *                   scan of the segments, then every cell's offsets and the
+ *                   triangle -> cell map (no block waits on another;
+ *                   k_fill_tri_cell when the map is filled afterwards)
+ *   k_vertices      one FP32 screen vertex per crossed edge, with certified
+ *                   bounds (two FP64 subtractions per vertex)
+ *   k_emit          one thread per triangle: its three vertices through their
+ *                   owner cells, culling, and the raster route (cover list,
+ *                   sliver list, tiny list, or dropped)
+ *   k_cover         one thread per listed triangle: FP32 coverage and depth
+ *                   intervals over its pixel range; certainly drawn fragments
+ *                   raise a per-pixel depth floor, the rest become candidates
+ *   k_sliver        the same for triangles whose area the reference may clamp
+ *   k_tiny          one thread per triangle too small for FP32 bounds: the
+ *                   reference's arithmetic for its few possible pixels
+ *   k_prune         drops candidates below the final depth floor
+ *   k_exact         one thread per remaining candidate: the reference's
+ *                   vertices (recomputed from the field), projection,
+ *                   barycentric test and harmonic depth in FP64, then a
+ *                   128-bit (depth, order) max into the z-buffer
+ * per object, after its slabs:
+ *   k_winners       the pixels the object owns
+ *   k_shade_f       FP32 vertex normals and colour with certified bounds
+ *                   (block-shared triangle normals)
+ *   k_nb_list, k_nb_wn, k_shade
+ *                   the reference's FP64 colour for the pixels FP32 cannot
+ *                   settle: neighbour triangles in normal.c's order, their
+ *                   weighted normals, ordered sums and the shading
  * and once per frame k_canvas_init, k_lines and k_resolve.  k_exact_all and
  * k_normals compute every triangle's exact data for inspection only.
  *
@@ -33,12 +46,16 @@
  * pixel, so they are computed for those alone.
  *
  * Reference correspondence (file:line of the reference tree):
- *   k_classify/k_emit  src/contour3d/contour/triangulate.c:95-342
- *   k_normals          src/contour3d/contour/normal.c:6-165
- *   k_cover/exact/shade src/contour3d/contour/render.c:48-163, project.c:9-67
- *   k_lines            src/contour3d/line.c:26-119
- *   k_resolve          src/contour3d/output.c:10-30, 113-123
- *   slab / interior    src/contour3d/contour/main.c:38-112
+ *   k_classify*, scan, k_emit   src/contour3d/contour/triangulate.c:95-342
+ *   k_vertices, exact vertices  src/contour3d/contour/triangulate.c:40-73
+ *   k_shade_f, k_nb_*, k_shade, k_normals
+ *                               src/contour3d/contour/normal.c:6-165
+ *   k_cover, k_sliver, k_tiny, k_exact, shading factor
+ *                               src/contour3d/contour/render.c:38-163,
+ *                               src/contour3d/project.c:9-67
+ *   k_lines                     src/contour3d/line.c:26-119
+ *   k_resolve                   src/contour3d/output.c:10-30, 113-123
+ *   slab / interior             src/contour3d/contour/main.c:38-112
  */
 #include <cuda.h>
 #include <cudaTypedefs.h>
