@@ -737,8 +737,11 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   }
   c.stats.cells += (uint64_t)(ncx * ncy * ncz) * nobj;
 
-  /* rendered cell slices are [1, ncz - 2]; each slab also triangulates one
-     slice below and above for the vertex normals (contour/main.c:49-112).
+  /* rendered cell slices are [1, ncz - 2] (contour/main.c:49-112); each slab
+     also classifies and scans the slice above it, whose cells own vertices of
+     the slab's top triangles, and the slice below it (a reader of that slice
+     has not been found since the vertex normals moved to the per-object
+     shading pass; dropping it is untested).
      Slabs are visited front to back (the z-buffer result does not depend on
      the order: fragments carry their position in the reference's drawing
      sequence), except for inspection, which reports triangles in order. */
