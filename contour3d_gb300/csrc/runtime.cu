@@ -739,9 +739,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
 
   /* rendered cell slices are [1, ncz - 2] (contour/main.c:49-112); each slab
      also classifies and scans the slice above it, whose cells own vertices of
-     the slab's top triangles, and the slice below it (a reader of that slice
-     has not been found since the vertex normals moved to the per-object
-     shading pass; dropping it is untested).
+     the slab's top triangles, and the slice below it, whose codes the
+     per-object shading reads when one slab covers the field (the neighbour
+     triangles of slice k lie in slices k - 1 .. k + 1); the scan and vertex
+     work on the slice below is not used. */
      Slabs are visited front to back (the z-buffer result does not depend on
      the order: fragments carry their position in the reference's drawing
      sequence), except for inspection, which reports triangles in order. */
