@@ -742,7 +742,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
      the slab's top triangles, and the slice below it, whose codes the
      per-object shading reads when one slab covers the field (the neighbour
      triangles of slice k lie in slices k - 1 .. k + 1); the scan and vertex
-     work on the slice below is not used. */
+     work on the slice below is not used.
      Slabs are visited front to back (the z-buffer result does not depend on
      the order: fragments carry their position in the reference's drawing
      sequence), except for inspection, which reports triangles in order. */
