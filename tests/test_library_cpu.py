@@ -83,3 +83,30 @@ def test_single_process_decomposition(built):
         assert list(n2) == [0, 0]  # periodic with one process: myself
     destruct = C.CFUNCTYPE(C.c_int, C.c_void_p)(sd.destruct)
     assert destruct(info) == 0
+
+
+def test_execute_without_gpu_fails_loudly(built, tmp_path):
+    """No usable GPU: contour3d_execute returns 1, logs a [CONTOUR3D ERROR]
+    line and writes no file -- nothing falls back to the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible here")
+    import sys
+    out = tmp_path / "frame.ppm"
+    script = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "from contour3d_gb300 import lib\n"
+        "from tests import cases\n"
+        "L = lib.Library()\n"
+        "rc = L.execute(cases.blobs_small(), %r)\n"
+        "print('rc', rc)\n"
+        "try:\n"
+        "    L.render(cases.blobs_small())\n"
+        "    print('render ok')\n"
+        "except RuntimeError:\n"
+        "    print('render raised')\n" % (ROOT, str(out)))
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "rc 1" in r.stdout and "render raised" in r.stdout
+    assert "[CONTOUR3D ERROR]" in r.stderr
+    assert not out.exists()
