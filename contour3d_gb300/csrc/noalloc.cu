@@ -11,9 +11,12 @@
  * scan -- lives in the file-scope array below, which every GPU that loads the
  * library holds (kScratchBytes) until the process exits.
  *
- * The kernel is a variant of k_scan in kernels.cu that computes each cell's
- * triangle count from the field itself (the k_classify rule) instead of
- * reading a counts array, so no intermediate buffer is needed.
+ * The kernel is a single-pass scan with decoupled look-back that computes
+ * each cell's triangle count from the field itself (the classification rule
+ * of kernels.cu) instead of reading a codes array, so no intermediate buffer
+ * is needed.  Tiles are taken in order from an atomic counter, so every tile
+ * a block waits on is running or done; the wait is bounded (2^22 polls) and
+ * raises an error flag that the host reports.
  *
  * Contract:
  *   - at most kMaxCells cells ((nx-1)(ny-1)(nz-1)); larger fields are
