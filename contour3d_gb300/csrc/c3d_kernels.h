@@ -192,7 +192,7 @@ struct CodeOut {
    Returns the number of kernels launched. */
 int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
                     cudaStream_t st);
-/* cells per slab for which the packed triangle and vertex sums of k_scan stay below 2^31 */
+/* cells per slab for which the packed triangle and vertex sums of the scan stay below 2^31 */
 constexpr long long kMaxSlabCells = 178956970;
 
 /* segments of the scan over n cells */

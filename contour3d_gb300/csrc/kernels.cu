@@ -2776,7 +2776,7 @@ static void launch_classify_tma(const CUtensorMap& map, const FieldDev& F, const
 
 int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
                     cudaStream_t st) {
-  /* codes[q] receives the cell codes of threshold q; k_scan turns them into counts */
+  /* codes[q] receives the cell codes of threshold q; the scan turns them into counts */
   const FieldDev& F = Fs[0];
   const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
                   (unsigned)((S.nslices + kClsZ - 1) / kClsZ));
