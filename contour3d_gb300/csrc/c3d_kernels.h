@@ -1,5 +1,5 @@
 /*
- * c3d_kernels.h -- launch interface between the host runtime (host.cpp) and
+ * c3d_kernels.h -- launch interface between the host runtime (runtime.cu) and
  * the device kernels (kernels.cu).  Internal to the library.
  */
 #pragma once
