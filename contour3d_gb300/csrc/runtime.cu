@@ -5,10 +5,14 @@
  *
  * Per call: scene constants on the host (same operations as main.c:25-63 and
  * project.c:9-67, compiled without contraction), one device z-buffer of
- * 16-byte slots, then per contour object the slab pipeline of kernels.cu,
- * then the lines, then one resolve pass and one device->host copy of the
- * image.  Device buffers are kept between calls (grow-only) so that repeated
- * frames do not pay for cudaMalloc; contour3d_gb300_release() frees them.
+ * 16-byte slots, then the contour objects field by field: a host field is
+ * copied to the device once (in chunks on a copy stream, overlapped with the
+ * slabs, when it is large), the objects of one field are classified together
+ * per z-slab and take the slab pipeline of kernels.cu in turn, and each
+ * object is shaded once after its slabs; then the lines, one resolve pass and
+ * one device->host copy of the image.  Device buffers are kept between calls
+ * (grow-only) so that repeated frames do not pay for cudaMalloc;
+ * contour3d_gb300_release() frees them.
  */
 #include <cuda_runtime.h>
 #include <algorithm>
