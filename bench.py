@@ -12,6 +12,17 @@ emit, smooth and rasterise both iso-surfaces into one image.
          in host memory: the host->device copy of the field, the device->host
          copy of the image and the ppm write are inside the timed region
 
+  roofline      the dominant stage's algorithmic bytes over its event time,
+                against the measured HBM peak, with every stage's time
+  cpu_baseline  the oracle on the host cores (a z-slab sample), with the
+                CPU model and a one-core point
+  clocks        nvidia-smi SM clocks and throttle reasons during the timed
+                region
+  batched, served, large
+                the batched form against the plain path on 64 uneven
+                fields; the served form on a Poisson request stream; a
+                1536^3 float32 field at 3840 x 2160
+
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
 --impl reference times the CPU restatement of the reference (oracle/, run
@@ -45,8 +56,8 @@ CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
 CPU_SAMPLE_SLICES_1 = 16  # the same for the single-core point
 
 # DRAM bytes (read + write) per unit processed, from one ncu capture of each
-# kernel on the 256^3 case (profiles/*_fourier256_f64.md); the full-size
-# launch is scaled by its units
+# kernel on the 256^3 case (profiles/kernels_fourier256_f64_1080p.md); the
+# full-size launch is scaled by its units
 TRAFFIC_PER_UNIT = {
     "classify": (4.60, "cells"),     # k_classify_tma, both levels in one pass: 152.4 MB for 2 x 16.6 M cells
     "scan": (5.49, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 91.1 MB for 16.6 M cells
