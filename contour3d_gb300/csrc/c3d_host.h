@@ -35,5 +35,10 @@ int extend_block(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj,
                  double *ext);
 int comm_size(MPI_Comm comm);
 int reduce_nearest(const sdecomp_info_t *info, PixelRec *px, size_t n);
+/* the P6 ppm file of a W x H image, rows as given (output.c:113-148) */
+int write_ppm(const char *fname, size_t W, size_t H, const uint8_t *rgb);
 
 }  // namespace c3d
+
+/* write_ppm with C linkage, for the host-side tests */
+extern "C" int c3d_write_ppm(const char *fname, size_t W, size_t H, const uint8_t *rgb);

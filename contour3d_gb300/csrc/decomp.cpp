@@ -13,7 +13,12 @@
  *                      clipped at the global boundary
  *   c3d_reduce_nearest output.c:10-30,82: the nearest-depth reduction to
  *                      rank 0, as a binary tree of pairwise exchanges
+ *   write_ppm          output.c:113-148: the P6 file
  */
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+#include <cerrno>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -210,6 +215,53 @@ void log_error(const char *fmt, ...) {
   va_end(a);
 }
 
+/*
+ * The header "P6\n<W> <H>\n255\n" and the W x H x 3 bytes, the same bytes as
+ * the reference's fopen("w") + fwrite.  A regular file that already exists
+ * is overwritten in place and then cut to the image's size instead of being
+ * truncated first: a solver rewrites the same file every frame, and on ext4
+ * the truncate-then-rewrite pattern makes close() start writing the new data
+ * back (its auto_da_alloc safeguard), which took 6-7 ms per 1920 x 1080
+ * frame against 0.8 ms in place on one host.  Other files (pipes, devices)
+ * are written sequentially.
+ */
+int write_ppm(const char *fname, size_t W, size_t H, const uint8_t *rgb) {
+  char hdr[64];
+  const int hl = snprintf(hdr, sizeof hdr, "P6\n%zu %zu\n255\n", W, H);
+  const size_t body = 3 * W * H;
+  const int fd = open(fname, O_WRONLY | O_CREAT | O_CLOEXEC, 0666);
+  if (fd < 0) {
+    log_error("%s: %s", fname, strerror(errno));
+    return 1;
+  }
+  struct stat st;
+  const bool regular = fstat(fd, &st) == 0 && S_ISREG(st.st_mode);
+  int err = 0;
+  auto put = [&](const void *p, size_t n, off_t at) {
+    const char *c = static_cast<const char *>(p);
+    while (n > 0 && err == 0) {
+      const ssize_t w = regular ? pwrite(fd, c, n, at) : write(fd, c, n);
+      if (w < 0 && errno == EINTR) continue;
+      if (w <= 0) {
+        err = w < 0 ? errno : EIO;
+        break;
+      }
+      c += w;
+      n -= (size_t)w;
+      at += w;
+    }
+  };
+  put(hdr, (size_t)hl, 0);
+  put(rgb, body, (off_t)hl);
+  if (err == 0 && regular && ftruncate(fd, (off_t)hl + (off_t)body) != 0) err = errno;
+  if (close(fd) != 0 && err == 0) err = errno;
+  if (err != 0) {
+    log_error("%s: %s", fname, strerror(err));
+    return 1;
+  }
+  return 0;
+}
+
 int decomp_query(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj, BlockInfo *b) {
   for (int d = 0; d < 3; d++) {
     const sdecomp_dir_t dir = (sdecomp_dir_t)d;
@@ -366,4 +418,8 @@ extern "C" int contour3d_gb300_reduce_nearest(const sdecomp_info_t *info, double
     rgb[3 * p + 2] = px[p].b;
   }
   return 0;
+}
+
+extern "C" int c3d_write_ppm(const char *fname, size_t W, size_t H, const uint8_t *rgb) {
+  return c3d::write_ppm(fname, W, H, rgb);
 }

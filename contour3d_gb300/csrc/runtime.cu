@@ -1295,23 +1295,6 @@ static int check_common(const V *cam, const V *light, const size_t sizes[2], con
   return 0;
 }
 
-static int write_ppm(const char *fname, size_t W, size_t H, const uint8_t *rgb) {
-  FILE *fp = fopen(fname, "w");
-  if (!fp) {
-    log_error("%s: %s", fname, strerror(errno));
-    return 1;
-  }
-  fprintf(fp, "P6\n%zu %zu\n255\n", W, H);
-  const size_t n = fwrite(rgb, 3, W * H, fp);
-  if (n != W * H) {
-    log_error("fwrite failed (%zu expected, %zu returned)", W * H, n);
-    fclose(fp);
-    return 1;
-  }
-  fclose(fp);
-  return 0;
-}
-
 }  // namespace c3d
 
 using namespace c3d;

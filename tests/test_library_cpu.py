@@ -110,3 +110,30 @@ def test_execute_without_gpu_fails_loudly(built, tmp_path):
     assert "rc 1" in r.stdout and "render raised" in r.stdout
     assert "[CONTOUR3D ERROR]" in r.stderr
     assert not out.exists()
+
+
+def _write_ppm(L, path, rgb, w, h):
+    f = L.lib.c3d_write_ppm
+    f.restype = C.c_int
+    f.argtypes = [C.c_char_p, C.c_size_t, C.c_size_t, C.c_void_p]
+    return f(str(path).encode(), w, h, rgb.ctypes.data)
+
+
+def test_ppm_writer(built, tmp_path):
+    """The ppm file of contour3d_execute (output.c:113-148): header and body
+    as the reference writes them, whether the file is new, longer or shorter
+    than the image (overwritten in place, then cut to size), or a device."""
+    import numpy as np
+    from contour3d_gb300 import lib
+    L = lib.Library()
+    w, h = 37, 23
+    rgb = np.random.default_rng(3).integers(0, 256, (h, w, 3), dtype=np.uint8)
+    want = b"P6\n37 23\n255\n" + rgb.tobytes()
+    p = tmp_path / "a.ppm"
+    assert _write_ppm(L, p, rgb, w, h) == 0 and p.read_bytes() == want
+    p.write_bytes(b"x" * 100000)  # a longer file: cut to the image's size
+    assert _write_ppm(L, p, rgb, w, h) == 0 and p.read_bytes() == want
+    p.write_bytes(b"y" * 10)  # a shorter one
+    assert _write_ppm(L, p, rgb, w, h) == 0 and p.read_bytes() == want
+    assert _write_ppm(L, "/dev/null", rgb, w, h) == 0
+    assert _write_ppm(L, tmp_path / "missing" / "b.ppm", rgb, w, h) == 1
