@@ -1,5 +1,6 @@
-"""Multi-rank host path on CPU: world-size 2 and 4 gloo process groups drive
-the library's point-to-point transport (the stand-in for MPI_Sendrecv).
+"""Multi-rank host path on CPU: gloo process groups of 2, 3, 4 and 6 ranks
+(powers of two and not, one- and two-dimensional process grids) drive the
+library's point-to-point transport (the stand-in for MPI_Sendrecv).
 
   * contour3d_gb300_extend: each rank's pencil block widened by two layers
     towards its neighbours and clipped at the global boundary
@@ -134,7 +135,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-@pytest.mark.parametrize("world", [2, 4])
+@pytest.mark.parametrize("world", [2, 3, 4, 6])
 def test_extend_and_reduce_over_gloo(built, world):
     import torch.multiprocessing as mp
     mp.spawn(_worker, args=(world, _free_port()), nprocs=world, join=True)
