@@ -42,7 +42,7 @@ def _pixels(rank):
     return depth, rgb
 
 
-def _worker(rank, world, port):
+def _worker(rank, world, port, periodic=False):
     import torch
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
@@ -76,7 +76,7 @@ def _worker(rank, world, port):
         construct = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_bool),
                                 C.POINTER(C.c_void_p))(sd.construct)
         info = C.c_void_p()
-        assert construct(world_comm, 3, (C.c_size_t * 3)(0, 0, 0), (C.c_bool * 3)(False, False, False),
+        assert construct(world_comm, 3, (C.c_size_t * 3)(0, 0, 0), (C.c_bool * 3)(periodic, periodic, periodic),
                          C.byref(info)) == 0
         mysize = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_size_t))(
             sd.get_pencil_mysize)
@@ -139,3 +139,13 @@ def _free_port():
 def test_extend_and_reduce_over_gloo(built, world):
     import torch.multiprocessing as mp
     mp.spawn(_worker, args=(world, _free_port()), nprocs=world, join=True)
+
+
+@pytest.mark.parametrize("world", [2, 4])
+def test_extend_periodic_grid(built, world):
+    """A periodic process grid: the halos are exchanged with the wrapped
+    neighbours too, and the global-boundary layers are clipped by rank
+    position as in extend.c:223-252, so every rank's extended block is still
+    the clipped window of the global field."""
+    import torch.multiprocessing as mp
+    mp.spawn(_worker, args=(world, _free_port(), True), nprocs=world, join=True)
