@@ -192,9 +192,13 @@ int xfer(MPI_Comm comm, const void *sbuf, size_t sbytes, int dest, void *rbuf, s
     c3d::log_error("a peer rank was requested but no transport is installed");
     return 1;
   }
-  return comm->t.sendrecv(comm->t.user, dest == MPI_PROC_NULL ? nullptr : sbuf,
-                          dest == MPI_PROC_NULL ? 0 : sbytes, dest,
-                          src == MPI_PROC_NULL ? nullptr : rbuf, src == MPI_PROC_NULL ? 0 : rbytes, src);
+  const int rc = comm->t.sendrecv(comm->t.user, dest == MPI_PROC_NULL ? nullptr : sbuf,
+                                  dest == MPI_PROC_NULL ? 0 : sbytes, dest,
+                                  src == MPI_PROC_NULL ? nullptr : rbuf, src == MPI_PROC_NULL ? 0 : rbytes, src);
+  if (rc != 0)
+    c3d::log_error("rank %d: exchange failed (send to %d, receive from %d; transport returned %d)", comm->rank,
+                   dest, src, rc);
+  return rc != 0 ? 1 : 0;
 }
 
 }  // namespace

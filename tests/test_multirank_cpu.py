@@ -149,3 +149,71 @@ def test_extend_periodic_grid(built, world):
     the clipped window of the global field."""
     import torch.multiprocessing as mp
     mp.spawn(_worker, args=(world, _free_port(), True), nprocs=world, join=True)
+
+
+def _failing_exchange_script(root):
+    return f"""
+import ctypes as C, sys
+import numpy as np
+sys.path.insert(0, {root!r})
+from tests.test_multirank_cpu import SENDRECV, Transport, GLOBAL
+from contour3d_gb300 import _abi, lib
+L = lib.Library()
+calls = []
+def sendrecv(user, sbuf, sbytes, dest, rbuf, rbytes, src):
+    calls.append((dest, src))
+    return 1  # the exchange failed (a peer that left, a dropped message)
+cb = SENDRECV(sendrecv)
+t = Transport(2, 0, cb, None)
+assert L.lib.contour3d_gb300_install_transport(C.byref(t)) == 0
+sd = lib.sdecomp_table(L)
+world = C.CFUNCTYPE(C.c_void_p)(C.cast(L.lib.c3d_comm_world, C.c_void_p).value)()
+construct = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_bool),
+                        C.POINTER(C.c_void_p))(sd.construct)
+info = C.c_void_p()
+assert construct(world, 3, (C.c_size_t * 3)(0, 0, 0), (C.c_bool * 3)(False, False, False), C.byref(info)) == 0
+mysize = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_size_t))(sd.get_pencil_mysize)
+size = []
+for d, g in enumerate(GLOBAL):
+    m = C.c_size_t()
+    assert mysize(info, 0, d, g, C.byref(m)) == 0
+    size.append(m.value)
+local = np.zeros((size[2], size[1], size[0]))
+grids = [np.linspace(0.0, 1.0, g)[:s].copy() for g, s in zip(GLOBAL, size)]
+obj = _abi.ContourObj()
+obj.pencil = 0
+obj.glsizes = (C.c_size_t * 3)(*GLOBAL)
+for d in range(3):
+    obj.grids[d] = grids[d].ctypes.data_as(C.POINTER(C.c_double))
+obj.converter = None
+obj.threshold = 0.0
+obj.array = local.ctypes.data_as(C.POINTER(C.c_double))
+esz, eof = (C.c_size_t * 3)(), (C.c_size_t * 3)()
+ext_fn = L.lib.contour3d_gb300_extend
+ext_fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+assert ext_fn(info, C.byref(obj), esz, eof, None) == 0  # sizes only: no exchange
+ext = np.empty(esz[2] * esz[1] * esz[0])
+print("extend", ext_fn(info, C.byref(obj), esz, eof, ext.ctypes.data))
+depth = np.zeros(16)
+rgb = np.zeros((16, 3), dtype=np.uint8)
+red = L.lib.contour3d_gb300_reduce_nearest
+red.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]
+print("reduce", red(info, depth.ctypes.data, rgb.ctypes.data, 16))
+print("calls", len(calls))
+L.lib.contour3d_gb300_install_transport(None)
+"""
+
+
+def test_failed_exchange_is_reported(built):
+    """Failure on the host: a transport whose exchange reports an error (a
+    rank that left, a dropped message) makes the halo extension and the
+    depth reduction return 1 with a [CONTOUR3D ERROR] line; nothing waits."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _failing_exchange_script(root)], capture_output=True, text=True,
+                       timeout=120, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "extend 1" in r.stdout and "reduce 1" in r.stdout, r.stdout
+    assert "calls 0" not in r.stdout
+    assert "[CONTOUR3D ERROR]" in r.stderr
