@@ -8,9 +8,8 @@ library, or the CPU checkers used by the tests.
 from __future__ import annotations
 
 import ctypes as C
-import math
 from dataclasses import dataclass, field
-from typing import Callable, List, Optional, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 

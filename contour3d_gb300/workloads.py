@@ -13,7 +13,6 @@ served_set()  resident fields of the served stream: shapes drawn from
 """
 from __future__ import annotations
 
-import math
 from dataclasses import dataclass, field
 from typing import List, Tuple
 
