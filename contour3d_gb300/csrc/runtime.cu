@@ -1768,9 +1768,13 @@ static void worker_main(contour3d_gb300_server *sv, int slot) {
     Request *r = nullptr;
     {
       std::unique_lock<std::mutex> lk(sv->mu);
-      sv->cv_work.wait(lk, [&] { return sv->stop || (!sv->queue.empty() && admissible(sv, sv->queue.front())); });
+      /* a request that does not fit waits for one in flight to finish (which
+         notifies); with nothing in flight every request fits, so no wait is
+         endless, also while stopping with requests still queued */
+      sv->cv_work.wait(lk, [&] {
+        return (sv->stop && sv->queue.empty()) || (!sv->queue.empty() && admissible(sv, sv->queue.front()));
+      });
       if (sv->queue.empty()) break; /* stop requested and nothing left */
-      if (!admissible(sv, sv->queue.front())) continue;
       r = sv->queue.front();
       sv->queue.pop_front();
       sv->in_flight += r->estimate;
