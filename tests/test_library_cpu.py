@@ -137,3 +137,19 @@ def test_ppm_writer(built, tmp_path):
     assert _write_ppm(L, p, rgb, w, h) == 0 and p.read_bytes() == want
     assert _write_ppm(L, "/dev/null", rgb, w, h) == 0
     assert _write_ppm(L, tmp_path / "missing" / "b.ppm", rgb, w, h) == 1
+
+
+def test_ppm_writer_matches_the_oracle_file(built, oracle, tmp_path):
+    """The writer's file equals, byte for byte, the one the oracle's
+    contour3d_execute writes (header layout and row order as output.c)."""
+    from contour3d_gb300 import lib
+    from tests import cases
+    L = lib.Library()
+    scene = cases.blobs_small()
+    ref = tmp_path / "oracle.ppm"
+    assert oracle.execute(scene, str(ref)) == 0
+    img = oracle.render(scene)  # rows in ppm order
+    h, w, _ = img.shape
+    mine = tmp_path / "mine.ppm"
+    assert _write_ppm(L, mine, img, w, h) == 0
+    assert mine.read_bytes() == ref.read_bytes()
