@@ -55,9 +55,9 @@ COLORS = ((0, 255, 255), (255, 255, 0))
 CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
 CPU_SAMPLE_SLICES_1 = 16  # the same for the single-core point
 
-# DRAM bytes (read + write) per unit processed, from one ncu capture of each
-# kernel on the 256^3 case (profiles/kernels_fourier256_f64_1080p.md); the
-# full-size launch is scaled by its units
+# DRAM bytes (read + write) per unit processed, from one ncu --set full
+# capture of each kernel on the 256^3 case of this workload; the full-size
+# launch is scaled by its units
 TRAFFIC_PER_UNIT = {
     "classify": (4.60, "cells"),     # k_classify_tma, both levels in one pass: 152.4 MB for 2 x 16.6 M cells
     "scan": (5.49, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 91.1 MB for 16.6 M cells
