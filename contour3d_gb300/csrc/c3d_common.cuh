@@ -120,8 +120,11 @@ __device__ __forceinline__ void cas128(Slot* addr, unsigned long long cmp_lo, un
       : "memory");
 }
 
-/* raise the slot to max(slot, (hi, lo)); true when this call stored (hi, lo) */
-__device__ __forceinline__ bool slot_max(Slot* s, unsigned long long hi, unsigned long long lo) {
+/* raise the slot to max(slot, (hi, lo)); true when this call stored (hi, lo).
+   A call that gives up after its retry bound sets bit 0 of *err, which the
+   host reads after the frame and reports as an error: a fragment is never
+   dropped silently */
+__device__ __forceinline__ bool slot_max(Slot* s, unsigned long long hi, unsigned long long lo, unsigned* err) {
   unsigned long long cur_lo = 0, cur_hi = 0;
   /* an atomic read: a CAS whose compare value is never present (hi = 0 is
      the key of NaN-space and is never stored) returns the live contents */
@@ -135,6 +138,7 @@ __device__ __forceinline__ bool slot_max(Slot* s, unsigned long long hi, unsigne
     cur_lo = o_lo;
     cur_hi = o_hi;
   }
+  if (err) atomicOr(err, 1u);
   return false;
 }
 

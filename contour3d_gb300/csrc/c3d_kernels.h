@@ -155,6 +155,7 @@ struct RasterDev {
   unsigned long long* amb_count;
   unsigned clamp_rgb;       /* the colour at the reference's factor 0.15, computed exactly */
   unsigned* shade_check;    /* self-check: per pixel, 1 << 24 | the FP32 colour when certain */
+  unsigned* zerr;           /* bit 0: a z-buffer update gave up after its retry bound */
 };
 
 /* one line segment, already projected to pixel units on the host */
@@ -242,7 +243,7 @@ void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDe
                         unsigned long long* ent_count, uint2* spans, double* wn, unsigned rgb, unsigned* checks,
                         cudaStream_t st);
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
-                  unsigned long long order_base, cudaStream_t st);
+                  unsigned long long order_base, unsigned* zerr, cudaStream_t st);
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,
                         cudaStream_t st);
 void launch_resolve(const Slot* canvas, long long W, long long H, unsigned char* rgb, double* depth,

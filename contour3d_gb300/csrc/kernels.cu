@@ -1146,7 +1146,7 @@ __device__ __forceinline__ void exact_fragment(const Geo& G, const SceneDev& s, 
   const double dist0 = exact_depth(x, w0, w1, w2);
   const unsigned long long order = order_of(G, order_base, t);
   const long long p = j * s.width + i;
-  if (slot_max(R.canvas + p, depth_key(dist0), order << 24)) keep_weights(R, p, order, w0, w1, w2);
+  if (slot_max(R.canvas + p, depth_key(dist0), order << 24, R.zerr)) keep_weights(R, p, order, w0, w1, w2);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1622,7 +1622,7 @@ __device__ void tiny_triangle(const Geo& G, const SceneDev& s, long long t, cons
       double w0, w1, w2;
       if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) continue;
       const long long p = j * s.width + i;
-      if (slot_max(R.canvas + p, depth_key(exact_depth(x, w0, w1, w2)), order << 24))
+      if (slot_max(R.canvas + p, depth_key(exact_depth(x, w0, w1, w2)), order << 24, R.zerr))
         keep_weights(R, p, order, w0, w1, w2);
     }
 }
@@ -2612,7 +2612,7 @@ k_shade(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __res
 /* lines (line.c:26-119), canvas init, resolve                          */
 /* ------------------------------------------------------------------ */
 __global__ void k_lines(const LineSegDev* __restrict__ segs, int nseg, long long W, long long H,
-                        Slot* __restrict__ canvas, unsigned long long order_base) {
+                        Slot* __restrict__ canvas, unsigned long long order_base, unsigned* zerr) {
   const int sidx = blockIdx.x;
   if (sidx >= nseg) return;
   const LineSegDev L = segs[sidx];
@@ -2642,7 +2642,7 @@ __global__ void k_lines(const LineSegDev* __restrict__ segs, int nseg, long long
     const double dist0 = drcp(dadd(ddiv(param, p1z), ddiv(dsub(1., param), p0z)));
     const unsigned long long key = depth_key(dist0);
     Slot* s = canvas + j * W + i;
-    slot_max(s, key, (order << 24) | L.rgb);
+    slot_max(s, key, (order << 24) | L.rgb, zerr);
   }
 }
 
@@ -2937,8 +2937,8 @@ void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDe
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
-                  unsigned long long order_base, cudaStream_t st) {
-  if (nseg > 0) k_lines<<<nseg, 128, 0, st>>>(segs, nseg, W, H, canvas, order_base);
+                  unsigned long long order_base, unsigned* zerr, cudaStream_t st) {
+  if (nseg > 0) k_lines<<<nseg, 128, 0, st>>>(segs, nseg, W, H, canvas, order_base, zerr);
 }
 
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,

@@ -27,6 +27,12 @@
  *   - every call shares the one scratch array and clears the part it uses at
  *     its start; calls that overlap on the GPU (other streams, other host
  *     threads) race on it and must be serialised by the caller;
+ *   - `stream` must belong to the current device (checked);
+ *   - every call copies the 4-byte error word back to the host and
+ *     synchronises `stream` before it returns, so the return code covers the
+ *     device work too;
+ *   - the cached device address is only valid for the device context it was
+ *     taken in: the library must not be used across a cudaDeviceReset;
  *   - no cudaMalloc, cudaFree or allocating library routine is called.
  */
 #include <cuda_runtime.h>
@@ -248,6 +254,14 @@ extern "C" int contour3d_gb300_cell_offsets_noalloc(const void* device_field, in
     scratch = g_scratch_ptr[dev];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (st) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess || sdev != dev) {
+      cudaGetLastError();
+      c3d::log_error("cell_offsets_noalloc: the stream does not belong to the current device %d", dev);
+      return 1;
+    }
+  }
   const long long tiles = (n + kTile) / kTile;
   /* the counter, the error word and the tile states this call uses start at zero */
   if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (size_t)(2 + tiles), st) != cudaSuccess) {

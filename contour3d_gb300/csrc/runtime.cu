@@ -535,6 +535,9 @@ struct FrameOut {
   DebugSink *sink = nullptr;
 };
 
+/* word of the 64-byte check buffer that holds the z-buffer error flags */
+static const int kZbufErrWord = 8;
+
 /* device counters of one slab's raster passes: candidates, tiny triangles,
    won pixels, requested normals, listed triangles, surviving candidates,
    slivers, pixels shaded in FP64, their FP64 normal requests */
@@ -1161,7 +1164,7 @@ static int render_lines(Ctx &c, const FrameIn &f, unsigned long long &order_base
   if (c.segs.ensure(sizeof(LineSegDev) * segs.size(), f.stream)) return 1;
   C3D_CUDA(cudaMemcpyAsync(c.segs.p, segs.data(), sizeof(LineSegDev) * segs.size(), cudaMemcpyHostToDevice, f.stream));
   launch_lines(c.segs.as<LineSegDev>(), (int)segs.size(), (long long)s.W, (long long)s.H, c.canvas.as<Slot>(),
-               order_base, f.stream);
+               order_base, c.checks.as<unsigned>() + kZbufErrWord, f.stream);
   c.stats.kernel_launches += 1;
   /* the stream is synchronised before `segs` goes out of scope by the caller's resolve copy */
   C3D_CUDA(cudaStreamSynchronize(f.stream));
@@ -1205,8 +1208,10 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy, sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
   C3D_CUDA(cudaMemcpyAsync(c.xyf.p, xyf, sizeof(float) * (W + H), cudaMemcpyHostToDevice, st));
   C3D_CUDA(cudaEventRecord(c.ev_staged, st));
-  if (c.filter_check) C3D_CUDA(cudaMemsetAsync(c.checks.p, 0, 64, st));
+  /* the self-check counters (words 0-5) and the z-buffer error word */
+  C3D_CUDA(cudaMemsetAsync(c.checks.p, 0, 64, st));
   RasterDev R = {};
+  R.zerr = c.checks.as<unsigned>() + kZbufErrWord;
   R.canvas = c.canvas.as<Slot>();
   R.zlo = c.zlo.as<unsigned>();
   R.winfo = c.winfo.as<ulonglong2>();
@@ -1252,11 +1257,14 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     C3D_CUDA(cudaMemcpyAsync(c.h_slots.p, c.canvas.p, sizeof(Slot) * npx, cudaMemcpyDeviceToHost, st));
   }
   C3D_CUDA(cudaEventRecord(c.ev1, st));
-  unsigned h_checks[6] = {0, 0, 0, 0, 0, 0};
-  if (c.filter_check)
-    C3D_CUDA(cudaMemcpyAsync(h_checks, c.checks.p, sizeof h_checks, cudaMemcpyDeviceToHost, st));
+  unsigned *h_checks = c.h_small.as<unsigned>() + 32;
+  C3D_CUDA(cudaMemcpyAsync(h_checks, c.checks.p, 16 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   C3D_CUDA(cudaStreamSynchronize(st));
   C3D_CUDA(cudaGetLastError());
+  if (h_checks[kZbufErrWord]) {
+    log_error("a z-buffer update gave up after its retry bound (error flags 0x%x)", h_checks[kZbufErrWord]);
+    return 1;
+  }
   c.stats.ms_total = elapsed(c.ev0, c.ev1);
   for (int q = 0; q < 5; q++) c.stats.filter_violations[q] = h_checks[q];
   c.stats.shade_violations = h_checks[5];

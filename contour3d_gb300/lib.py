@@ -161,6 +161,9 @@ class Library:
         L.contour3d_gb300_server_destroy.restype = C.c_int
         L.contour3d_gb300_server_destroy.argtypes = [C.c_void_p]
         L.contour3d_gb300_device_bytes.restype = C.c_uint64
+        L.contour3d_gb300_cell_offsets_noalloc.restype = C.c_int
+        L.contour3d_gb300_cell_offsets_noalloc.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t), C.c_double,
+                                                           C.c_void_p, C.c_void_p, C.c_void_p]
         identity = C.cast(L.contour3d_gb300_identity, C.c_void_p).value
         self.converters = {"identity": identity}
         if os.path.exists(FIELDGEN_PATH):

@@ -111,7 +111,9 @@ int contour3d_gb300_render_device(const contour3d_vector_t *camera_position,
  * with an error).  The first call on a device looks up that array's device
  * address, so make it before any stream capture on the device.  All calls
  * share the array; calls that overlap on the GPU race and must be serialised
- * by the caller.  The call returns when the result is in device memory.
+ * by the caller.  `stream` (null: the legacy default stream) must belong to
+ * the current device.  Every call copies a 4-byte error word back to the host
+ * and synchronises `stream`, and returns when the result is in device memory.
  */
 int contour3d_gb300_cell_offsets_noalloc(const void *device_field, int dtype, const size_t sizes[3],
                                          double threshold, uint32_t *device_offsets,

@@ -20,7 +20,10 @@ from contour3d_gb300 import _abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libc3d_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libc3dref.so")
-REF_TREE = "/root/reference"
+# the reference checkout: $C3D_REFERENCE_TREE, else a directory named
+# `reference` beside this repository (absent on GPU hosts: the checker is then
+# not built and the tests that need it skip)
+REF_TREE = os.environ.get("C3D_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 from contour3d_gb300.records import TRI_DTYPE  # noqa: E402
 

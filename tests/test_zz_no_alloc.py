@@ -18,16 +18,20 @@ pytestmark = pytest.mark.gpu
 
 
 def _fn(gpu):
-    f = gpu.lib.contour3d_gb300_cell_offsets_noalloc
-    f.restype = C.c_int
-    f.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
-    return f
+    # argument and result types are declared by contour3d_gb300/lib.py
+    return gpu.lib.contour3d_gb300_cell_offsets_noalloc
 
 
+# (nz, ny, nx) nodes: 44,352 cells (11 scan tiles of 4,096 cells); 4,095 cells,
+# so that the n + 1 offsets fill exactly one tile; 128^3 cells (512 tiles), so
+# that a tile's look-back walks past more than one window of 32 predecessors
+SHAPES = [(37, 29, 45), (22, 14, 16), (129, 129, 129)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=["x".join(map(str, s)) for s in SHAPES])
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
-def test_noalloc_offsets_match_existing_entry_point(gpu, dtype):
+def test_noalloc_offsets_match_existing_entry_point(gpu, oracle, dtype, shape):
     import torch
-    shape = (37, 29, 45)
     host, std = fields.modes(shape, nmodes=24, kmin=1, kmax=7, power=5.0 / 6.0, seed=31,
                              dtype=np.float64 if dtype == "f64" else np.float32)
     fn = _fn(gpu)
@@ -36,7 +40,10 @@ def test_noalloc_offsets_match_existing_entry_point(gpu, dtype):
     sizes = (C.c_size_t * 3)(nx, ny, nz)
     n = (nx - 1) * (ny - 1) * (nz - 1)
     for thr in (0.3 * std, -0.6 * std):
+        # the existing entry point, and the oracle on the same (widened) values
         counts, total = gpu.cell_counts(host.astype(np.float64), thr)
+        ocounts, ototal = oracle.cell_counts(host.astype(np.float64), thr)
+        assert ototal == total and np.array_equal(ocounts, counts)
         expect = np.zeros(n + 1, dtype=np.int64)
         expect[1:] = np.cumsum(counts.ravel().astype(np.int64))
         assert expect[-1] == total
