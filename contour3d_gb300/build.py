@@ -54,27 +54,69 @@ def _run(cmd):
     return r.stdout
 
 
-def build(verbose: bool = False) -> str:
-    os.makedirs(OUT, exist_ok=True)
+def _compile_and_link(out_dir: str, lib: str, extra_flags, link_extra, verbose: bool) -> None:
+    os.makedirs(out_dir, exist_ok=True)
     hdr = _headers_mtime()
     jobs = []
     objs = []
     for s in CUDA_SOURCES:
-        src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")
+        src, obj = os.path.join(CSRC, s), os.path.join(out_dir, s + ".o")
         objs.append(obj)
         if _stale(src, obj, hdr):
-            jobs.append([NVCC] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([NVCC] + list(extra_flags) + NVCC_FLAGS + ["-c", src, "-o", obj])
     for s in CXX_SOURCES:
-        src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")
+        src, obj = os.path.join(CSRC, s), os.path.join(out_dir, s + ".o")
         objs.append(obj)
         if _stale(src, obj, hdr):
-            jobs.append(["g++"] + CXX_FLAGS + ["-c", src, "-o", obj])
+            jobs.append(["g++"] + list(extra_flags) + CXX_FLAGS + ["-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out:
                 print(out)
-    if jobs or not os.path.exists(LIB):
-        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"])
+    if jobs or not os.path.exists(lib):
+        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + list(link_extra) +
+             ["-lcudart_static", "-lrt", "-lpthread", "-ldl"])
+
+
+def _mpi_flags():
+    """Compile and link flags of the MPI installation: $C3D_MPI_CFLAGS and
+    $C3D_MPI_LIBS when set, else what `mpicxx --showme` reports."""
+    cflags, libs = os.environ.get("C3D_MPI_CFLAGS"), os.environ.get("C3D_MPI_LIBS")
+    if cflags is None or libs is None:
+        try:
+            c = subprocess.run(["mpicxx", "--showme:compile"], capture_output=True, text=True, check=True).stdout
+            ln = subprocess.run(["mpicxx", "--showme:link"], capture_output=True, text=True, check=True).stdout
+        except (OSError, subprocess.CalledProcessError):
+            raise RuntimeError("MPI build: set C3D_MPI_CFLAGS and C3D_MPI_LIBS (no mpicxx found)")
+        cflags = c if cflags is None else cflags
+        libs = ln if libs is None else libs
+    return cflags.split(), libs.split()
+
+
+def build_mpi(out_dir: str = os.path.join(HERE, "_build_mpi"), external_sdecomp_include: str = None,
+              cflags=None, libs=None, verbose: bool = False) -> str:
+    """The library for callers that run under MPI: -DCONTOUR3D_USE_MPI, so the
+    halo exchange and the depth reduction use the decomposition's MPI
+    communicator instead of an installed transport.  With
+    `external_sdecomp_include` (the directory of the real SimpleDecomp's
+    sdecomp.h) the library also leaves out its own `sdecomp` table and binds
+    the caller's (-DCONTOUR3D_EXTERNAL_SDECOMP).  The result is
+    out_dir/libcontour3d_gb300_mpi.so; the default build is unchanged."""
+    if cflags is None or libs is None:
+        mc, ml = _mpi_flags()
+        cflags = mc if cflags is None else cflags
+        libs = ml if libs is None else libs
+    flags = ["-DCONTOUR3D_USE_MPI"] + list(cflags)
+    if external_sdecomp_include:
+        # the caller's SimpleDecomp header is found before include/sdecomp.h
+        flags = ["-DCONTOUR3D_EXTERNAL_SDECOMP", "-I" + external_sdecomp_include] + flags
+    lib = os.path.join(out_dir, "libcontour3d_gb300_mpi.so")
+    _compile_and_link(out_dir, lib, flags, list(libs), verbose)
+    return lib
+
+
+def build(verbose: bool = False) -> str:
+    _compile_and_link(OUT, LIB, [], [], verbose)
     fg = os.path.join(OUT, "libc3d_fieldgen.so")
     src = os.path.join(CSRC, "fieldgen_cpu.c")
     if _stale(src, fg, _headers_mtime()):

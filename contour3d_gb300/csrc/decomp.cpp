@@ -1,12 +1,15 @@
 /*
  * decomp.cpp -- pencil decomposition, communicator and host-side array
- * extension for builds without MPI.
+ * extension.
  *
  *   sdecomp object     the subset of SimpleDecomp used by the reference
  *                      (call sites: src/contour3d/contour/extend.c:17-21,
- *                      161-180, 219-220; src/contour3d/output.c:98)
- *   c3d_comm_world     MPI_COMM_WORLD stand-in: one process, or the ranks of
- *                      an installed point-to-point transport
+ *                      161-180, 219-220; src/contour3d/output.c:98); not
+ *                      built with -DCONTOUR3D_EXTERNAL_SDECOMP, where the
+ *                      caller links the real SimpleDecomp
+ *   c3d_comm_world     MPI_COMM_WORLD stand-in of builds without MPI: one
+ *                      process, or the ranks of an installed point-to-point
+ *                      transport
  *   c3d_extend_block   extend.c:150-282: local block + two halo layers from
  *                      each neighbour (x, then y, then z exchange, so edges
  *                      and corners arrive through the neighbours' halos),
@@ -14,6 +17,10 @@
  *   c3d_reduce_nearest output.c:10-30,82: the nearest-depth reduction to
  *                      rank 0, as a binary tree of pairwise exchanges
  *   write_ppm          output.c:113-148: the P6 file
+ *
+ * Every exchange is one pairwise send-and-receive (xfer): MPI_Sendrecv with
+ * -DCONTOUR3D_USE_MPI (as extend.c:36-141 does), else the installed
+ * transport's sendrecv.
  */
 #include <fcntl.h>
 #include <sys/stat.h>
@@ -29,6 +36,31 @@
 #include "contour3d_gb300.h"
 #include "c3d_host.h"
 
+#if defined(CONTOUR3D_EXTERNAL_SDECOMP) && !defined(CONTOUR3D_USE_MPI)
+#error "-DCONTOUR3D_EXTERNAL_SDECOMP needs -DCONTOUR3D_USE_MPI (SimpleDecomp works on MPI communicators)"
+#endif
+
+#if defined(CONTOUR3D_USE_MPI)
+/* exchanges and ranks through MPI; no transport to install */
+extern "C" int contour3d_gb300_install_transport(const contour3d_gb300_transport_t *t) {
+  if (!t) return 0;
+  c3d::log_error("this library is built with MPI: exchanges use the decomposition's MPI communicator");
+  return 1;
+}
+
+namespace {
+int comm_rank_of(MPI_Comm c) {
+  int r = 0;
+  if (MPI_Comm_rank(c, &r) != MPI_SUCCESS) return 0;
+  return r;
+}
+int comm_size_of(MPI_Comm c) {
+  int n = 1;
+  if (MPI_Comm_size(c, &n) != MPI_SUCCESS) return 1;
+  return n;
+}
+}  // namespace
+#else
 struct c3d_comm_s {
   int size;
   int rank;
@@ -56,14 +88,25 @@ extern "C" int contour3d_gb300_install_transport(const contour3d_gb300_transport
   return 0;
 }
 
+namespace {
+int comm_rank_of(MPI_Comm c) { return c ? c->rank : 0; }
+int comm_size_of(MPI_Comm c) { return c ? c->size : 1; }
+}  // namespace
+#endif
+
+#if !defined(CONTOUR3D_EXTERNAL_SDECOMP)
 struct sdecomp_info_t {
   MPI_Comm comm;
-  int p0, p1; /* process grid shared by the two split directions */
-  int c0, c1; /* my coordinates in it */
+  int size, rank; /* of comm, when the decomposition was constructed */
+  int p0, p1;     /* process grid shared by the two split directions */
+  int c0, c1;     /* my coordinates in it */
   bool periods[3];
 };
+#endif
 
 namespace {
+
+#if !defined(CONTOUR3D_EXTERNAL_SDECOMP)
 
 /* (number of processes, my coordinate) of `dir` in `pencil` */
 void pencil_dir(const sdecomp_info_t *info, sdecomp_pencil_t pencil, sdecomp_dir_t dir, int *np, int *me) {
@@ -83,10 +126,10 @@ void pencil_dir(const sdecomp_info_t *info, sdecomp_pencil_t pencil, sdecomp_dir
 }
 
 int s_construct(MPI_Comm comm, size_t ndims, const size_t dims[], const bool periods[], sdecomp_info_t **info) {
-  if (!info || !comm || (ndims != 3 && ndims != 2)) return 1;
+  if (!info || comm == MPI_COMM_NULL || (ndims != 3 && ndims != 2)) return 1;
   sdecomp_info_t *p = static_cast<sdecomp_info_t *>(calloc(1, sizeof(sdecomp_info_t)));
   if (!p) return 1;
-  const int P = comm->size;
+  const int P = comm_size_of(comm);
   int p0 = 0;
   if (dims && ndims == 3 && dims[1] && dims[2] && (int)(dims[1] * dims[2]) == P) {
     p0 = (int)dims[1];
@@ -95,10 +138,12 @@ int s_construct(MPI_Comm comm, size_t ndims, const size_t dims[], const bool per
       if (P % d == 0) p0 = d;
   }
   p->comm = comm;
+  p->size = P;
+  p->rank = comm_rank_of(comm);
   p->p0 = p0;
   p->p1 = P / p0;
-  p->c0 = comm->rank % p0;
-  p->c1 = comm->rank / p0;
+  p->c0 = p->rank % p0;
+  p->c1 = p->rank / p0;
   for (int d = 0; d < 3; d++) p->periods[d] = periods ? periods[d < (int)ndims ? d : 0] : false;
   *info = p;
   return 0;
@@ -110,12 +155,12 @@ int s_destruct(sdecomp_info_t *info) {
 }
 
 int s_comm_cart(const sdecomp_info_t *info, MPI_Comm *c) {
-  *c = info ? info->comm : &g_world;
+  *c = info ? info->comm : MPI_COMM_WORLD;
   return 0;
 }
 
 int s_comm_rank(const sdecomp_info_t *info, int *r) {
-  *r = info ? info->comm->rank : g_world.rank;
+  *r = info ? info->rank : comm_rank_of(MPI_COMM_WORLD);
   return 0;
 }
 
@@ -140,7 +185,7 @@ int s_neighbours(const sdecomp_info_t *info, sdecomp_pencil_t p, sdecomp_dir_t d
   const bool periodic = info->periods[(int)d];
   if ((int)d == undecomposed) {
     /* one process along d: a periodic wrap leads back to myself */
-    if (periodic) nb[0] = nb[1] = info->comm->rank;
+    if (periodic) nb[0] = nb[1] = info->rank;
     return 0;
   }
   const bool swap = (int)p >= 3;
@@ -181,13 +226,36 @@ int s_offset(const sdecomp_info_t *info, sdecomp_pencil_t p, sdecomp_dir_t d, si
   return 0;
 }
 
+#endif  // !CONTOUR3D_EXTERNAL_SDECOMP
+
 /* one pairwise exchange through the communicator */
 int xfer(MPI_Comm comm, const void *sbuf, size_t sbytes, int dest, void *rbuf, size_t rbytes, int src) {
   if (dest == MPI_PROC_NULL && src == MPI_PROC_NULL) return 0;
-  if (dest == comm->rank && src == comm->rank) {
+  const int me = comm_rank_of(comm);
+  if (dest == me && src == me) {
     memcpy(rbuf, sbuf, rbytes < sbytes ? rbytes : sbytes);
     return 0;
   }
+#if defined(CONTOUR3D_USE_MPI)
+  /* MPI counts are int: pieces of at most 1 GiB; both partners of every
+     exchange move the same byte count, so their piece sequences pair up */
+  const size_t piece = (size_t)1 << 30;
+  const size_t sb = dest == MPI_PROC_NULL ? 0 : sbytes, rb = src == MPI_PROC_NULL ? 0 : rbytes;
+  size_t so = 0, ro = 0;
+  do {
+    const size_t sn = sb - so < piece ? sb - so : piece, rn = rb - ro < piece ? rb - ro : piece;
+    const int rc = MPI_Sendrecv(sn ? static_cast<const char *>(sbuf) + so : nullptr, (int)sn, MPI_BYTE, dest, 3141,
+                                rn ? static_cast<char *>(rbuf) + ro : nullptr, (int)rn, MPI_BYTE, src, 3141, comm,
+                                MPI_STATUS_IGNORE);
+    if (rc != MPI_SUCCESS) {
+      c3d::log_error("rank %d: MPI_Sendrecv failed (send to %d, receive from %d; error %d)", me, dest, src, rc);
+      return 1;
+    }
+    so += sn;
+    ro += rn;
+  } while (so < sb || ro < rb);
+  return 0;
+#else
   if (!comm->has_transport) {
     c3d::log_error("a peer rank was requested but no transport is installed");
     return 1;
@@ -199,13 +267,16 @@ int xfer(MPI_Comm comm, const void *sbuf, size_t sbytes, int dest, void *rbuf, s
     c3d::log_error("rank %d: exchange failed (send to %d, receive from %d; transport returned %d)", comm->rank,
                    dest, src, rc);
   return rc != 0 ? 1 : 0;
+#endif
 }
 
 }  // namespace
 
+#if !defined(CONTOUR3D_EXTERNAL_SDECOMP)
 extern "C" const sdecomp_t sdecomp = {
     s_construct, s_destruct, s_comm_cart, s_comm_rank, s_nprocs, s_myrank, s_neighbours, s_mysize, s_offset,
 };
+#endif
 
 namespace c3d {
 
@@ -291,7 +362,7 @@ int decomp_query(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj,
 }
 
 int extend_block(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj, const BlockInfo &b, double *ext) {
-  MPI_Comm comm = nullptr;
+  MPI_Comm comm = MPI_COMM_NULL;
   sdecomp.get_comm_cart(info, &comm);
   const size_t n = 2;
   const size_t tx = b.mysize[0] + 2 * n, ty = b.mysize[1] + 2 * n, tz = b.mysize[2] + 2 * n;
@@ -364,12 +435,12 @@ int extend_block(const sdecomp_info_t *info, const contour3d_contour_obj_t *obj,
   return 0;
 }
 
-int comm_size(MPI_Comm comm) { return comm ? comm->size : 1; }
+int comm_size(MPI_Comm comm) { return comm == MPI_COMM_NULL ? 1 : comm_size_of(comm); }
 
 int reduce_nearest(const sdecomp_info_t *info, PixelRec *px, size_t n) {
-  MPI_Comm comm = nullptr;
+  MPI_Comm comm = MPI_COMM_NULL;
   sdecomp.get_comm_cart(info, &comm);
-  const int P = comm->size, r = comm->rank;
+  const int P = comm_size(comm), r = comm == MPI_COMM_NULL ? 0 : comm_rank_of(comm);
   if (P == 1) return 0;
   std::vector<PixelRec> in(n);
   for (int s = 1; s < P; s <<= 1) {

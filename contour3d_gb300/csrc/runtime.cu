@@ -1379,7 +1379,7 @@ extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
     ci.color = o->color;
     f.contours.push_back(ci);
   }
-  MPI_Comm comm = nullptr;
+  MPI_Comm comm = MPI_COMM_NULL;
   sdecomp.get_comm_cart(sdecomp_info, &comm);
   int myrank = 0;
   sdecomp.get_comm_rank(sdecomp_info, &myrank);

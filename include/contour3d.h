@@ -21,7 +21,11 @@
 
 #include <stddef.h> /* size_t */
 #include <stdint.h> /* uint8_t */
+#if defined(CONTOUR3D_EXTERNAL_SDECOMP)
+#include <sdecomp.h> /* the caller's SimpleDecomp header, found through -I */
+#else
 #include "sdecomp.h"
+#endif
 
 #define CONTOUR3D_NDIMS 3
 

@@ -10,9 +10,12 @@
  *   get_comm_cart/get_neighbours  src/contour3d/contour/extend.c:17-21
  *   get_nprocs/get_myrank         src/contour3d/contour/extend.c:219-220
  *   get_comm_rank                 src/contour3d/output.c:98
- * A deployment that already links the real SimpleDecomp builds the library
- * with -DCONTOUR3D_EXTERNAL_SDECOMP against that project's header instead;
- * the library uses only the names below.
+ * A deployment that already links the real SimpleDecomp (and MPI) builds the
+ * library with -DCONTOUR3D_USE_MPI -DCONTOUR3D_EXTERNAL_SDECOMP and that
+ * project's include directory ahead of this one
+ * (contour3d_gb300.build.build_mpi): contour3d.h then includes that
+ * project's sdecomp.h, the library leaves out its own `sdecomp` table and
+ * calls the caller's, and it uses only the names below.
  *
  * Without MPI (-DCONTOUR3D_USE_MPI not given) the library ships its own
  * `sdecomp` object and a minimal communicator: a single process by default,
