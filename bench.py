@@ -14,8 +14,8 @@ emit, smooth and rasterise both iso-surfaces into one image.
 
   roofline      the dominant stage's algorithmic bytes over its event time,
                 against the measured HBM peak, with every stage's time
-  cpu_baseline  the oracle on the host cores (a z-slab sample), with the
-                CPU model and a one-core point
+  cpu_baseline  the oracle on every host core on the whole workload, with
+                the CPU model and a one-core point on a z-slab sample
   clocks        nvidia-smi SM clocks and throttle reasons during the timed
                 region
   batched, served, large
@@ -26,8 +26,9 @@ emit, smooth and rasterise both iso-surfaces into one image.
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
 --impl reference times the CPU restatement of the reference (oracle/, run
-with one thread per host core as emulated z-split ranks) on a bounded sample
-of the same workload.  Under torchrun, every rank renders its own replica of
+with one thread per host core as emulated z-split ranks) on the whole
+workload every step (about 4 s per step on 16 Grace cores); --cpu-table adds
+the other workloads.  Under torchrun, every rank renders its own replica of
 the workload (the path shards by z-slabs with one final reduction; each GPU
 here renders a whole field).
 """
@@ -36,6 +37,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -52,8 +54,7 @@ WIDTH, HEIGHT = 1920, 1080
 CAM = (2.5, 2.0, 1.5)
 CENTRE = (0.5, 0.5, 0.5)
 COLORS = ((0, 255, 255), (255, 255, 0))
-CPU_SAMPLE_SLICES = 96  # z-nodes of the 512^2 x 512 field timed on the host
-CPU_SAMPLE_SLICES_1 = 16  # the same for the single-core point
+CPU_SAMPLE_SLICES_1 = 16  # z-nodes of the 512^2 x 512 field timed on one host core
 
 # DRAM bytes (read + write) per unit processed, from one ncu --set full
 # capture of each kernel on the 256^3 case of this workload; the full-size
@@ -81,9 +82,11 @@ def parse():
     p.add_argument("--no-large", action="store_true", help="skip the 1536^3 f32 field")
     p.add_argument("--workers", default="auto",
                    help="worker contexts of the batched and served forms (auto: tuned for the batched frames)")
-    p.add_argument("--served-rates", default="200,max",
+    p.add_argument("--served-rates", default="50,100,200,400,max",
                    help="comma-separated request rates (req/s); max = submit without waiting")
-    p.add_argument("--served-requests", type=int, default=60)
+    p.add_argument("--served-requests", type=int, default=500)
+    p.add_argument("--cpu-table", action="store_true",
+                   help="with --impl reference: also time the oracle on the other workloads")
     return p.parse_args()
 
 
@@ -388,52 +391,122 @@ def run_served(gpu, slots, rates, nreq, budget_gb=120.0, seed=99):
             for tk in tickets:
                 lat.append(sv.wait(tk))
             wall = time.perf_counter() - t_start
+            mem = sv.memory()
         torch.cuda.synchronize()
         same = all(torch.equal(a, b) for a, b in zip(outs, plain_img))
         ms = np.array([x.latency_ms for x in lat])
         out["rates"].append({"rate_req_s": rate if rate else "max", "requests": nreq,
                              "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
                              "frames_per_s": nreq / wall, "cells_per_s": cells / wall,
+                             "p90_ms": float(np.percentile(ms, 90)),
                              "queue_p50_ms": float(np.percentile([x.queue_ms for x in lat], 50)),
+                             "queue_p99_ms": float(np.percentile([x.queue_ms for x in lat], 99)),
+                             "device_p50_ms": float(np.percentile([x.device_ms for x in lat], 50)),
+                             "context_peak_gb": mem.peak_bytes / 1e9, "overcommits": int(mem.overcommits),
+                             "idle_trims": int(mem.trims),
                              "images_identical_to_plain": bool(same)})
     return out
 
 
+def cpu_scene_time(scene, cores, repeats=1):
+    """Median seconds of the oracle rendering `scene` with `cores` threads."""
+    from oracle.lib import Oracle
+    orc = Oracle()
+    ts = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        orc.render(scene, nranks=cores)
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts))
+
+
+def cpu_table(cores):
+    """The oracle on the host cores for the other workloads: the 128^3 blob
+    field (1 level, 1024^2), eight frames of the batched workload (float32
+    fields widened, as the reference is double-only), and a 256^3 crop of
+    the 1536^3 float32 field (4 levels, 3840x2160), each at every core and,
+    for the small ones, at one core."""
+    from contour3d_gb300 import _abi, fields, workloads
+    from tests import cases
+    rows = []
+    s0 = cases.config0()
+    c0 = 127 ** 3
+    t_all, t_one = cpu_scene_time(s0, cores, 3), cpu_scene_time(s0, 1, 1)
+    rows.append({"config": "128^3 f64 blobs, 1 level, 1024x1024", "cells": c0,
+                 "cores": cores, "cells_per_s": c0 / t_all, "frames_per_s": 1.0 / t_all,
+                 "one_core": {"cells_per_s": c0 / t_one, "frames_per_s": 1.0 / t_one}})
+    flds, frames = workloads.batch_set(None, nfields=8, host=True)
+    cells = t = 0.0
+    for spec in frames:
+        f = flds[spec.field].astype(np.float64)
+        nz, ny, nx = f.shape
+        grids = tuple(_abi.unit_grid(n) for n in (nx, ny, nz))
+        sc = _abi.make_scene(spec.camera, CENTRE, spec.width, spec.height)
+        sc.contours = [_abi.Contour(f, lv, c, grids=grids) for lv, c in zip(spec.levels, spec.colors)]
+        t += cpu_scene_time(sc, cores)
+        cells += len(spec.levels) * (nx - 1) * (ny - 1) * (nz - 1)
+    rows.append({"config": "batched workload, first 8 of 64 frames (dims 64..384, 1-4 levels, 1024x1024)",
+                 "cells": int(cells), "cores": cores, "cells_per_s": cells / t, "frames_per_s": 8 / t})
+    n = 1536
+    crop = 256
+    off = (n - crop) // 2
+    f32, std = fields.modes_threaded((crop, crop, crop), nmodes=256, kmin=1, kmax=48, power=11.0 / 6.0, seed=4,
+                                     dtype=np.float32, offset=(off, off, off), glshape=(n, n, n))
+    f = f32.astype(np.float64)
+    g = tuple(_abi.unit_grid(n)[off:off + crop] for _ in range(3))
+    sc = _abi.make_scene(CAM, CENTRE, 3840, 2160)
+    sc.contours = [_abi.Contour(f, lv * std, c, grids=g) for lv, c in zip((-1.0, -0.5, 0.5, 1.0), workloads.PALETTE)]
+    t4 = cpu_scene_time(sc, cores)
+    c4 = 4 * (crop - 1) ** 3
+    rows.append({"config": "256^3 centre crop of the 1536^3 f32 field (widened), 4 levels, 3840x2160",
+                 "cells": c4, "cores": cores, "cells_per_s": c4 / t4, "frames_per_s": 1.0 / t4})
+    return rows
+
+
 def run_reference(args, rank, world):
-    """CPU arm: the reference's algorithm restated in C (oracle/), all host cores."""
+    """CPU arm: the reference's algorithm restated in C (oracle/), every host
+    core as an emulated z-split rank, on the full bench workload."""
     if rank != 0:
         return
     from contour3d_gb300 import fields
     cores = os.cpu_count() or 1
-    nz = CPU_SAMPLE_SLICES
-    sample, std = fields.modes((nz, SHAPE[1], SHAPE[2]), NMODES, KMIN, KMAX, POWER, SEED,
-                               glshape=SHAPE)
+    field, std = fields.modes_threaded(SHAPE, NMODES, KMIN, KMAX, POWER, SEED)
     for _ in range(args.warmup):
-        cpu_baseline(sample, std, cores)
+        cpu_baseline(field, std, cores)
     times = []
     cells = 0
     for _ in range(args.steps):
-        v, dt, cells = cpu_baseline(sample, std, cores)
+        v, dt, cells = cpu_baseline(field, std, cores)
         times.append(dt)
     ms = 1000.0 * float(np.mean(times))
     value = cells / (ms / 1000.0)
-    sample_desc = (f"z-slab of {nz} of 512 node layers (512x512x{nz} f64, two thresholds, "
-                   f"1920x1080), oracle with {cores} threads as emulated z-split ranks")
+    sample_desc = (f"the whole workload every step ({SHAPE[0]}^3 f64, two thresholds, 1920x1080), "
+                   f"oracle/c3d_oracle.c with {cores} threads as emulated z-split ranks")
     out = {
         "metric": "cells_per_s", "value": value, "unit": "cell-thresholds/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fourier field)",
         "impl": "reference",
-        "config": {"workload": "fourier-512^3-f64-2thr-1920x1080", "sample": sample_desc},
+        "config": {"workload": workload_name(), "sample": sample_desc},
         "cpu_baseline": {"value": value, "unit": "cell-thresholds/s", "cores": cores, "cpu_model": cpu_model(),
-                         "kind": "port", "sample": sample_desc},
+                         "kind": "port", "sample": sample_desc,
+                         "mpi": "no MPI launcher on the GPU host: ranks are threads of one process"
+                         if not shutil.which("mpirun") else "mpirun present; ranks are still threads"},
         "e2e": {"value": value, "unit": "cell-thresholds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if args.cpu_table:
+        out["cpu_table"] = cpu_table(cores)
     print(json.dumps(out))
 
 
+def workload_name() -> str:
+    return f"fourier-{SHAPE[0]}^3-f64-2thr-{WIDTH}x{HEIGHT}"
+
+
 def main():
+    global SHAPE
     args = parse()
+    SHAPE = (args.shape,) * 3
     rank, world, local = dist_env()
     import torch
     if world > 1:
@@ -448,8 +521,6 @@ def main():
     torch.cuda.set_device(local)
     from contour3d_gb300 import _abi, lib
     gpu = lib.load()
-    global SHAPE
-    SHAPE = (args.shape,) * 3
     nz, ny, nx = SHAPE
     field = torch.empty(SHAPE, dtype=torch.float64, device="cuda")
     std = gpu.fieldgen_modes_device(field.data_ptr(), 0, SHAPE, NMODES, KMIN, KMAX, POWER, SEED)
@@ -588,23 +659,24 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        sample = field[:CPU_SAMPLE_SLICES].cpu().numpy()
+        whole = field.cpu().numpy()
         cores = os.cpu_count() or 1
-        v, dt, c = cpu_baseline(sample, std, cores)
+        v, dt, c = cpu_baseline(whole, std, cores)
         cpu = {"value": v, "unit": "cell-thresholds/s", "cores": cores, "cpu_model": cpu_model(), "kind": "port",
-               "sample": f"512x512x{CPU_SAMPLE_SLICES} z-slab of the same field, two thresholds, 1920x1080, "
+               "sample": f"the whole workload (512^3 f64, two thresholds, 1920x1080), "
                          f"oracle/c3d_oracle.c with {cores} threads ({dt:.2f} s)"}
+        del whole
         # one core, on a thinner slab of the same field
         v1, dt1, _ = cpu_baseline(field[:CPU_SAMPLE_SLICES_1].cpu().numpy(), std, 1)
         cpu["sweep"] = [{"cores": 1, "value": v1, "sample": f"512x512x{CPU_SAMPLE_SLICES_1} z-slab ({dt1:.2f} s)"},
-                        {"cores": cores, "value": v, "sample": f"512x512x{CPU_SAMPLE_SLICES} z-slab ({dt:.2f} s)"}]
+                        {"cores": cores, "value": v, "sample": f"whole 512^3 field ({dt:.2f} s)"}]
 
     if rank == 0:
         out = {
             "metric": "cells_per_s", "value": value, "unit": "cell-thresholds/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fourier field)",
-            "config": {"workload": "fourier-512^3-f64-2thr-1920x1080", "field": "512^3 f64, 64 modes |k| 1..16",
+            "config": {"workload": workload_name(), "field": f"{nx}^3 f64, 64 modes |k| 1..16",
                        "thresholds": "+-0.5 std", "image": "1920x1080",
                        "l2": "inputs larger than L2 (1.07 GB field)", "parallelism": f"replicas x{world}"},
             "frames_per_s": 1000.0 / ms, "triangles_per_frame": int(st.triangles),

@@ -342,9 +342,22 @@ static cudaMemPool_t device_pool() {
   return g_pool[dev];
 }
 
+/*
+ * Device-memory accounting of one context of a server: every growth of one
+ * of the context's buffers is charged before it is allocated (charge may
+ * wait until the server's HBM budget has room) and every release is
+ * credited.  Contexts outside a server have none.
+ */
+struct MemHook {
+  virtual int charge(size_t bytes) = 0;
+  virtual void credit(size_t bytes) = 0;
+  virtual ~MemHook() {}
+};
+
 struct Buf {
   void *p = nullptr;
   size_t cap = 0;
+  MemHook *hook = nullptr;
   /* grow to at least `bytes`; the old contents are not kept.  Allocation and
      release are ordered on `st`, the stream every use of the buffer is on
      (or whose previous uses have completed) */
@@ -352,10 +365,12 @@ struct Buf {
     if (bytes <= cap) return 0;
     release(st);
     const size_t want = bytes + bytes / 4 + 256;
+    if (hook && hook->charge(want)) return 1;
     cudaMemPool_t pool = device_pool();
     if (!pool || cudaMallocFromPoolAsync(&p, want, pool, st) != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
+      if (hook) hook->credit(want);
       log_error("device allocation of %zu bytes failed", want);
       return 1;
     }
@@ -367,6 +382,7 @@ struct Buf {
     if (p) {
       cudaFreeAsync(p, st);
       g_device_bytes -= cap;
+      if (hook) hook->credit(cap);
     }
     p = nullptr;
     cap = 0;
@@ -1018,10 +1034,22 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       if (sink) {
         /* copy this slab's triangles back and keep the rendered ones in order */
         std::vector<unsigned> meta(T), cellv(T);
-        std::vector<double> dv(kDbgDoubles * cap);
+        /* the slab's T entries of each inspection array (the buffers have
+           the capacity of the largest slab so far): vertices and vertex
+           normals as 18 rows of pitch cap, face normals (3 per triangle),
+           areas; nothing when only counts are wanted */
+        const bool want_records = sink->out && sink->count < sink->capacity;
+        std::vector<double> dv(want_records ? kDbgDoubles * T : 0);
         C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
         C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
-        C3D_CUDA(cudaMemcpyAsync(dv.data(), dbg, sizeof(double) * kDbgDoubles * cap, cudaMemcpyDeviceToHost, st));
+        if (want_records) {
+          C3D_CUDA(cudaMemcpy2DAsync(dv.data(), sizeof(double) * T, dbg, sizeof(double) * cap, sizeof(double) * T, 18,
+                                     cudaMemcpyDeviceToHost, st));
+          C3D_CUDA(cudaMemcpyAsync(dv.data() + 18 * T, dbg + 18 * cap, sizeof(double) * 3 * T, cudaMemcpyDeviceToHost,
+                                   st));
+          C3D_CUDA(cudaMemcpyAsync(dv.data() + 21 * T, dbg + 21 * cap, sizeof(double) * T, cudaMemcpyDeviceToHost,
+                                   st));
+        }
         C3D_CUDA(cudaStreamSynchronize(st));
         for (unsigned long long t = 0; t < T; t++) {
           const long long cl = cellv[t] & kTcCellMask;
@@ -1030,10 +1058,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           if (!(meta[t] & kMetaRendered)) continue;
           if (sink->out && sink->count < sink->capacity) {
             TriRecord &r = sink->out[sink->count];
-            for (int q = 0; q < 9; q++) r.vertices[q] = dv[q * cap + t];
-            for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[(9 + q) * cap + t];
-            for (int q = 0; q < 3; q++) r.face_normal[q] = dv[18 * cap + 3 * t + q];
-            r.area = dv[21 * cap + t];
+            for (int q = 0; q < 9; q++) r.vertices[q] = dv[q * T + t];
+            for (int q = 0; q < 9; q++) r.vertex_normals[q] = dv[(9 + q) * T + t];
+            for (int q = 0; q < 3; q++) r.face_normal[q] = dv[18 * T + 3 * t + q];
+            r.area = dv[21 * T + t];
             r.cell[0] = i + (long long)ci.off[0];
             r.cell[1] = j + (long long)ci.off[1];
             r.cell[2] = k + (long long)ci.off[2];
@@ -1658,13 +1686,18 @@ extern "C" int contour3d_gb300_release(void) {
   return 0;
 }
 
+/* every device buffer of a context; the constant table (lut) first */
+static std::vector<Buf *> ctx_bufs(Ctx &c) {
+  return {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
+          &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live,
+          &c.tiny, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.voffsets, &c.verts, &c.winfo, &c.amb,
+          &c.shade_check, &c.checks};
+}
+
 static void ctx_release(Ctx &c) {
-  Buf *bufs[] = {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-                 &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live, &c.tiny, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.voffsets, &c.verts, &c.winfo, &c.amb, &c.shade_check,
-                 &c.checks};
   /* every call of the context has completed, so its buffers go back to the
      pool in order on its own stream */
-  for (Buf *b : bufs) b->release(c.own_stream);
+  for (Buf *b : ctx_bufs(c)) b->release(c.own_stream);
   if (c.ready) cudaStreamSynchronize(c.own_stream);
   c.h_small.release();
   c.h_rgb.release();
@@ -1713,11 +1746,15 @@ struct Request {
   int rc = 0;
   bool done = false;
   double device_ms = 0.;
+  uint64_t held_bytes = 0;
 };
 
-/* working set of one request: slab codes/offsets, triangles and vertices (at
-   an assumed density of one triangle and half a vertex per cell), candidate
-   lists, the z-buffer and the per-pixel winner weights */
+/* the part of a request's working set known before it runs: per slab the
+   code arrays, cell offsets and segment sums, and per frame the z-buffer,
+   depth floors, winner weights and pixel lists.  The triangle-dependent
+   buffers (triangle map and records, screen vertices, candidate lists) are
+   sized from the scan's count after each slab's classification and are
+   charged against the budget then (ServerHook). */
 static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t slab_cells) {
   uint64_t peak = 0;
   for (size_t n = 0; n < fr->num_fields; n++) {
@@ -1729,13 +1766,10 @@ static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t sla
     uint64_t sharing = 0;
     for (size_t q = 0; q < fr->num_fields; q++)
       sharing += fr->fields[q].device_array == fr->fields[n].device_array ? 1 : 0;
-    /* candidates and their surviving copy: half a triangle's worth each */
-    const uint64_t bytes =
-        cells * (sharing + 4 + 4 + 4) + cells * (kTriBytes + 4 + 4 + 10) + cells * sizeof(Candidate);
-    peak = std::max(peak, bytes);
+    peak = std::max(peak, cells * (sharing + 4 + 4) + cells / 256);
   }
   const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];
-  return peak + px * (sizeof(Slot) + 4 + 8 + 3 + 48) + (1ULL << 24);
+  return peak + px * (sizeof(Slot) + 4 + 48 + 4 + 4 + 3) + (1ULL << 20);
 }
 
 }  // namespace c3d
@@ -1745,26 +1779,107 @@ struct contour3d_gb300_server {
   int device = 0;
   uint64_t budget = 0;
   uint64_t resident = 0;
-  uint64_t in_flight = 0;
   int running = 0;
   bool stop = false;
   uint64_t next_ticket = 1;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work, cv_done, cv_budget;
   std::deque<c3d::Request *> queue;
   std::unordered_map<uint64_t, c3d::Request *> requests;
   std::vector<std::unique_ptr<c3d::Ctx>> ctxs;
+  std::vector<std::unique_ptr<c3d::MemHook>> hooks;
   std::vector<std::thread> threads;
   std::atomic<int> init_failures{0};
+  /* device memory of the contexts (under mu): held per slot, in total, and
+     whether the slot is rendering a request */
+  std::vector<uint64_t> held;
+  std::vector<char> busy;
+  uint64_t used = 0;
+  uint64_t peak_used = 0;
+  int blocked = 0;            /* contexts waiting in charge() */
+  uint64_t overcommits = 0;   /* charges let through above the budget to keep the server moving */
+  uint64_t trims = 0;         /* idle contexts whose buffers were released for another's growth */
 };
 
 namespace c3d {
 
+/* bytes the contexts may hold next to the caller's resident fields */
+static uint64_t budget_limit(const contour3d_gb300_server *sv) {
+  return sv->budget > sv->resident ? sv->budget - sv->resident : 0;
+}
+
+/* release every buffer but the constant table of an idle context (its last
+   frame has completed: its stream was synchronised); under sv->mu */
+static void trim_idle(contour3d_gb300_server *sv, int slot) {
+  Ctx &c = *sv->ctxs[slot];
+  if (!c.ready) return;
+  std::vector<Buf *> bufs = ctx_bufs(c);
+  for (size_t q = 1; q < bufs.size(); q++) {
+    Buf *b = bufs[q];
+    if (!b->p) continue;
+    MemHook *h = b->hook;
+    b->hook = nullptr; /* credited here, not through the hook (mu is held) */
+    sv->used -= b->cap;
+    sv->held[slot] -= b->cap;
+    b->release(c.own_stream);
+    b->hook = h;
+  }
+  sv->trims++;
+}
+
+/*
+ * The budget check of a context's buffer growth.  A growth that does not fit
+ * first releases the buffers of idle contexts; if it still does not fit, the
+ * context waits for running requests to finish or shrink -- unless every
+ * other running request is waiting too, in which case it goes ahead above the
+ * budget (counted in overcommits), so that waits always end.
+ */
+struct ServerHook : MemHook {
+  contour3d_gb300_server *sv;
+  int slot;
+  ServerHook(contour3d_gb300_server *s, int q) : sv(s), slot(q) {}
+  int charge(size_t bytes) override {
+    std::unique_lock<std::mutex> lk(sv->mu);
+    const uint64_t limit = budget_limit(sv);
+    if (sv->budget != 0) {
+      for (;;) {
+        if (sv->used + bytes <= limit) break;
+        for (int q = 0; q < sv->slots && sv->used + bytes > limit; q++)
+          if (q != slot && !sv->busy[q] && sv->held[q] > sv->ctxs[q]->lut.cap) trim_idle(sv, q);
+        if (sv->used + bytes <= limit) break;
+        if (sv->blocked + 1 >= sv->running) {
+          sv->overcommits++;
+          break;
+        }
+        sv->blocked++;
+        sv->cv_budget.wait(lk);
+        sv->blocked--;
+      }
+    }
+    sv->used += bytes;
+    sv->held[slot] += bytes;
+    sv->peak_used = std::max(sv->peak_used, sv->used);
+    return 0;
+  }
+  void credit(size_t bytes) override {
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->used -= bytes;
+      sv->held[slot] -= bytes;
+    }
+    sv->cv_budget.notify_all();
+  }
+};
+
+/* a request starts when a slot is free and its known working set fits next
+   to what the running requests hold (an oversized request runs alone) */
 static bool admissible(contour3d_gb300_server *sv, const Request *r) {
-  if (sv->running == 0) return true; /* an oversized request runs alone */
+  if (sv->running == 0) return true;
   if (sv->budget == 0) return true;
-  const uint64_t avail = sv->budget > sv->resident ? sv->budget - sv->resident : 0;
-  return sv->in_flight + r->estimate <= avail;
+  uint64_t busy_held = 0;
+  for (int q = 0; q < sv->slots; q++)
+    if (sv->busy[q]) busy_held += sv->held[q];
+  return busy_held + r->estimate <= budget_limit(sv);
 }
 
 static void worker_main(contour3d_gb300_server *sv, int slot) {
@@ -1785,8 +1900,8 @@ static void worker_main(contour3d_gb300_server *sv, int slot) {
       if (sv->queue.empty()) break; /* stop requested and nothing left */
       r = sv->queue.front();
       sv->queue.pop_front();
-      sv->in_flight += r->estimate;
       sv->running += 1;
+      sv->busy[slot] = 1;
     }
     r->t_start = now_ms();
     int rc = ok ? 0 : 1;
@@ -1812,11 +1927,20 @@ static void worker_main(contour3d_gb300_server *sv, int slot) {
       r->rc = rc;
       r->t_done = now_ms();
       r->done = true;
-      sv->in_flight -= r->estimate;
+      r->held_bytes = sv->held[slot];
       sv->running -= 1;
+      sv->busy[slot] = 0;
     }
     sv->cv_done.notify_all();
     sv->cv_work.notify_all();
+    sv->cv_budget.notify_all(); /* one running request fewer: a waiting growth may now go ahead */
+  }
+  {
+    /* the hook is not called once the context is released: credit by hand */
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (Buf *b : ctx_bufs(ctx)) b->hook = nullptr;
+    sv->used -= sv->held[slot];
+    sv->held[slot] = 0;
   }
   ctx_release(ctx);
 }
@@ -1838,7 +1962,13 @@ extern "C" contour3d_gb300_server_t *contour3d_gb300_server_create(int slots, ui
     delete sv;
     return nullptr;
   }
-  for (int q = 0; q < slots; q++) sv->ctxs.emplace_back(new Ctx());
+  sv->held.assign((size_t)slots, 0);
+  sv->busy.assign((size_t)slots, 0);
+  for (int q = 0; q < slots; q++) {
+    sv->ctxs.emplace_back(new Ctx());
+    sv->hooks.emplace_back(new ServerHook(sv, q));
+    for (Buf *b : ctx_bufs(*sv->ctxs[q])) b->hook = sv->hooks[q].get();
+  }
   for (int q = 0; q < slots; q++) sv->threads.emplace_back(worker_main, sv, q);
   return sv;
 }
@@ -1885,6 +2015,7 @@ extern "C" int contour3d_gb300_server_wait(contour3d_gb300_server_t *sv, uint64_
     stats->queue_ms = r->t_start - r->t_submit;
     stats->device_ms = r->device_ms;
     stats->estimate_bytes = r->estimate;
+    stats->held_bytes = r->held_bytes;
   }
   const int rc = r->rc;
   delete r;
@@ -1892,6 +2023,16 @@ extern "C" int contour3d_gb300_server_wait(contour3d_gb300_server_t *sv, uint64_
 }
 
 extern "C" uint64_t contour3d_gb300_device_bytes(void) { return g_device_bytes.load(); }
+
+extern "C" int contour3d_gb300_server_memory(contour3d_gb300_server_t *sv, contour3d_gb300_server_memory_t *out) {
+  if (!sv || !out) return 1;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  out->used_bytes = sv->used;
+  out->peak_bytes = sv->peak_used;
+  out->overcommits = sv->overcommits;
+  out->trims = sv->trims;
+  return 0;
+}
 
 extern "C" int contour3d_gb300_server_destroy(contour3d_gb300_server_t *sv) {
   if (!sv) return 1;

@@ -67,6 +67,56 @@ def modes(shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=0, dtype=np.f
     return out, float(std)
 
 
+def _zsplit(nz, parts):
+    parts = max(1, min(parts, nz))
+    step = (nz + parts - 1) // parts
+    return [(z, min(z + step, nz)) for z in range(0, nz, step)]
+
+
+def modes_threaded(shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=0, dtype=np.float64,
+                   threads=None, offset=None, glshape=None):
+    """modes() computed in z-slabs on `threads` host threads (default: every
+    core); the bytes are the same as modes() gives, since every value depends
+    on its global node index only."""
+    from concurrent.futures import ThreadPoolExecutor
+    L = _load()
+    nz, ny, nx = shape
+    o = offset if offset is not None else (0, 0, 0)
+    gshape = glshape if glshape is not None else shape
+    out = np.empty(shape, dtype=dtype)
+    fn = L.c3d_fieldgen_modes_f64 if dtype == np.float64 else L.c3d_fieldgen_modes_f32
+    stds = []
+
+    def part(zr):
+        z0, z1 = zr
+        gl, off, my = _block((z1 - z0, ny, nx), (o[0] + z0, o[1], o[2]), gshape)
+        view = out[z0:z1]
+        stds.append(fn(view.ctypes.data_as(C.c_void_p), gl, off, my, C.c_int(nmodes), C.c_int(kmin),
+                       C.c_int(kmax), C.c_double(power), C.c_uint64(seed)))
+
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        list(ex.map(part, _zsplit(nz, threads or os.cpu_count() or 1)))
+    return out, float(stds[0])
+
+
+def blobs_threaded(shape, nblobs=8, seed=0, threads=None) -> np.ndarray:
+    """blobs() computed in z-slabs on `threads` host threads (same bytes)."""
+    from concurrent.futures import ThreadPoolExecutor
+    L = _load()
+    nz, ny, nx = shape
+    out = np.empty(shape, dtype=np.float64)
+
+    def part(zr):
+        z0, z1 = zr
+        gl, off, my = _block((z1 - z0, ny, nx), (z0, 0, 0), shape)
+        L.c3d_fieldgen_blobs_f64(out[z0:z1].ctypes.data_as(C.c_void_p), gl, off, my, C.c_int(nblobs),
+                                 C.c_uint64(seed))
+
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        list(ex.map(part, _zsplit(nz, threads or os.cpu_count() or 1)))
+    return out
+
+
 def modes_std(nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=0) -> float:
     L = _load()
     z = (C.c_long * 3)(2, 2, 2)

@@ -52,7 +52,12 @@ class Frame(C.Structure):
 
 class RequestStats(C.Structure):
     _fields_ = [("latency_ms", C.c_double), ("queue_ms", C.c_double), ("device_ms", C.c_double),
-                ("estimate_bytes", C.c_uint64)]
+                ("estimate_bytes", C.c_uint64), ("held_bytes", C.c_uint64)]
+
+
+class ServerMemory(C.Structure):
+    _fields_ = [("used_bytes", C.c_uint64), ("peak_bytes", C.c_uint64), ("overcommits", C.c_uint64),
+                ("trims", C.c_uint64)]
 
 
 class FramePack:
@@ -109,6 +114,7 @@ EXPORTS = [
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
     "contour3d_gb300_cell_offsets_noalloc", "contour3d_gb300_render_batch", "contour3d_gb300_server_create",
     "contour3d_gb300_server_submit", "contour3d_gb300_server_wait", "contour3d_gb300_server_destroy",
+    "contour3d_gb300_server_memory",
     "contour3d_gb300_device_bytes", "contour3d_gb300_reduce_nearest",
     "c3d_comm_world", "sdecomp",
 ]
@@ -158,6 +164,8 @@ class Library:
         L.contour3d_gb300_server_submit.argtypes = [C.c_void_p, C.POINTER(Frame), C.POINTER(C.c_uint64)]
         L.contour3d_gb300_server_wait.restype = C.c_int
         L.contour3d_gb300_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(RequestStats)]
+        L.contour3d_gb300_server_memory.restype = C.c_int
+        L.contour3d_gb300_server_memory.argtypes = [C.c_void_p, C.POINTER(ServerMemory)]
         L.contour3d_gb300_server_destroy.restype = C.c_int
         L.contour3d_gb300_server_destroy.argtypes = [C.c_void_p]
         L.contour3d_gb300_device_bytes.restype = C.c_uint64
@@ -338,6 +346,12 @@ class Server:
         if rc != 0:
             raise RuntimeError(f"request {ticket} failed")
         return st
+
+    def memory(self) -> ServerMemory:
+        m = ServerMemory()
+        if self.lib.lib.contour3d_gb300_server_memory(self.h, C.byref(m)) != 0:
+            raise RuntimeError("contour3d_gb300_server_memory failed")
+        return m
 
     def close(self) -> None:
         if self.h:

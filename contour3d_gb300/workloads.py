@@ -57,18 +57,25 @@ PALETTE = [(0, 255, 255), (255, 255, 0), (255, 64, 64), (64, 255, 64)]
 
 
 def quantile_levels(dev_field, rng, count, lo=0.3, hi=0.7, samples=200_000):
-    """Levels at uniformly drawn quantiles of a random sample of the values."""
-    import torch
-    flat = dev_field.reshape(-1)
-    idx = torch.from_numpy(rng.integers(0, flat.numel(), size=min(samples, flat.numel()))).to(flat.device)
-    vals = flat[idx].double().cpu().numpy()
+    """Levels at uniformly drawn quantiles of a random sample of the values
+    (a torch tensor, or a numpy array: the same draws give the same levels)."""
+    if isinstance(dev_field, np.ndarray):
+        flat = dev_field.reshape(-1)
+        vals = flat[rng.integers(0, flat.size, size=min(samples, flat.size))].astype(np.float64)
+    else:
+        import torch
+        flat = dev_field.reshape(-1)
+        idx = torch.from_numpy(rng.integers(0, flat.numel(), size=min(samples, flat.numel()))).to(flat.device)
+        vals = flat[idx].double().cpu().numpy()
     qs = np.sort(rng.uniform(lo, hi, size=count))
     return [float(np.quantile(vals, q)) for q in qs]
 
 
-def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=2024):
-    """Device fields and frame specs of the batched workload."""
-    import torch
+def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=2024, host=False):
+    """Fields and frame specs of the batched workload: device tensors, or with
+    host=True the same values as numpy arrays generated on the host cores
+    (no GPU needed; `lib` is then unused)."""
+    from . import fields as hostgen
     rng = np.random.default_rng(seed)
     fields, frames = [], []
     for n in range(nfields):
@@ -76,15 +83,24 @@ def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=
         dtype = "f64" if n % 2 == 0 else "f32"
         kind = "blobs" if rng.random() < 0.5 else "modes"
         if kind == "blobs":
-            dev = blobs_device(lib, shape, int(rng.integers(4, 33)), seed=1000 + n)
-            if dtype == "f32":
-                dev = dev.float()
+            nb = int(rng.integers(4, 33))
+            if host:
+                f = hostgen.blobs_threaded(shape, nb, seed=1000 + n)
+                f = f.astype(np.float32) if dtype == "f32" else f
+            else:
+                f = blobs_device(lib, shape, nb, seed=1000 + n)
+                f = f.float() if dtype == "f32" else f
         else:
-            dev, _ = modes_device(lib, shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=2000 + n,
-                                  dtype=torch.float64 if dtype == "f64" else torch.float32)
-        fields.append(dev)
+            if host:
+                f, _ = hostgen.modes_threaded(shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=2000 + n,
+                                              dtype=np.float64 if dtype == "f64" else np.float32)
+            else:
+                import torch
+                f, _ = modes_device(lib, shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=2000 + n,
+                                    dtype=torch.float64 if dtype == "f64" else torch.float32)
+        fields.append(f)
         nlev = int(rng.integers(1, 5))
-        levels = quantile_levels(dev, rng, nlev)
+        levels = quantile_levels(f, rng, nlev)
         frames.append(FrameSpec(n, levels, PALETTE[:nlev], random_camera(rng), width, height))
     return fields, frames
 

@@ -148,21 +148,40 @@ int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frames, size_t n
                                  double *frame_ms);
 
 /*
- * Served form: a request loop with `slots` concurrent contexts.  A submitted
- * frame starts when a slot is free and its estimated device working set fits
- * `hbm_budget_bytes` (0 = unlimited) minus `resident_bytes` (the caller's
- * resident fields) next to the requests in flight; requests arriving while
- * others run are admitted as slots and memory free up.  The frame struct and
- * everything it points to must stay valid until contour3d_gb300_server_wait
- * returns for its ticket.
+ * Served form: a request loop with `slots` concurrent contexts against an
+ * HBM budget of `hbm_budget_bytes` (0 = unlimited), of which the caller's
+ * resident fields take `resident_bytes`.  A submitted frame starts when a
+ * slot is free and the part of its working set known before it runs (code
+ * and offset arrays of its largest slab, z-buffer and per-pixel arrays) fits
+ * next to what the running requests hold; requests arriving while others
+ * run are admitted as slots and memory free up.  While a request runs, every
+ * growth of its device buffers is charged against the budget when it is
+ * sized -- the triangle-dependent buffers from the triangle count of each
+ * slab's classification -- and waits while it does not fit, after first
+ * releasing the buffers of idle contexts.  A growth that would wait while
+ * every other running request waits too goes ahead above the budget (counted
+ * in contour3d_gb300_server_memory), so no wait is endless.  The frame struct
+ * and everything it points to must stay valid until
+ * contour3d_gb300_server_wait returns for its ticket.
  */
 typedef struct contour3d_gb300_server contour3d_gb300_server_t;
 typedef struct {
   double latency_ms;      /* submit -> done */
   double queue_ms;        /* submit -> start */
   double device_ms;       /* device time of the frame */
-  uint64_t estimate_bytes; /* admitted working-set estimate */
+  uint64_t estimate_bytes; /* the working-set part known at admission */
+  uint64_t held_bytes;    /* device bytes its context held when it finished */
 } contour3d_gb300_request_stats_t;
+
+/* device memory of a server's contexts: bytes held now and at most so far,
+   growths let through above the budget, idle contexts trimmed */
+typedef struct {
+  uint64_t used_bytes;
+  uint64_t peak_bytes;
+  uint64_t overcommits;
+  uint64_t trims;
+} contour3d_gb300_server_memory_t;
+int contour3d_gb300_server_memory(contour3d_gb300_server_t *server, contour3d_gb300_server_memory_t *out);
 
 contour3d_gb300_server_t *contour3d_gb300_server_create(int slots, uint64_t hbm_budget_bytes,
                                                         uint64_t resident_bytes);

@@ -23,6 +23,7 @@ def _structs():
         "contour3d_gb300_field_t": lib.Field,
         "contour3d_gb300_frame_t": lib.Frame,
         "contour3d_gb300_request_stats_t": lib.RequestStats,
+        "contour3d_gb300_server_memory_t": lib.ServerMemory,
         "contour3d_gb300_transport_t": Transport,
     }
 

@@ -84,3 +84,34 @@ def test_server_admits_against_a_budget(gpu):
         assert np.array_equal(outs[q].cpu().numpy(), ref[q])
     # with one request admitted at a time, each later request waited for the earlier ones
     assert stats[-1].queue_ms >= 0 and all(s.estimate_bytes > 0 for s in stats)
+
+
+def test_server_charges_buffer_growth_against_the_budget(gpu):
+    """Buffer growth of running requests is charged against the budget when
+    it is sized (the triangle buffers from each slab's triangle count): with a
+    budget that holds about one and a half requests' buffers, the memory held
+    stays within the budget except for growths that had to go ahead because
+    every other running request was waiting (counted), and every image is
+    still the plain path's."""
+    import torch
+    fields, frames = _small_set(gpu, n=8, seed=23)
+    ref = [_single(gpu, fields, s) for s in frames]
+    # one request's peak: run it alone on a one-slot server without a budget
+    with gpu.server(slots=1) as sv:
+        outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
+        held = [sv.wait(sv.submit(workloads.frame_pack(gpu, fields[s.field], s, o))).held_bytes
+                for s, o in zip(frames, outs)]
+        assert sv.memory().overcommits == 0
+    budget = int(1.5 * max(held))
+    with gpu.server(slots=4, budget_bytes=budget, resident_bytes=0) as sv:
+        outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
+        ts = [sv.submit(workloads.frame_pack(gpu, fields[s.field], s, o)) for s, o in zip(frames, outs)]
+        stats = [sv.wait(t) for t in ts]
+        mem = sv.memory()
+        torch.cuda.synchronize()
+    for q in range(len(frames)):
+        assert np.array_equal(outs[q].cpu().numpy(), ref[q])
+    assert all(s.held_bytes > 0 for s in stats)
+    # the invariant: above the budget only through counted go-aheads
+    assert mem.peak_bytes <= budget or mem.overcommits > 0
+    assert mem.used_bytes <= mem.peak_bytes
