@@ -193,7 +193,7 @@ def run_large(gpu, n=1536, frames=2):
     3840x2160, generated on the device; device-resident rendering.  The FP32
     field is widened exactly when read, so the result is the reference's FP64
     arithmetic on those values; what FP32 storage changes is the input, which
-    fp32_input_vs_fp64 measures on a 256^3 field of the same spectrum."""
+    fp32_input_vs_fp64 measures on a 256^3 crop of this field."""
     import torch
     from contour3d_gb300 import _abi, workloads
     f, std = workloads.modes_device(gpu, (n, n, n), nmodes=256, kmin=1, kmax=48, power=11.0 / 6.0, seed=4,
@@ -224,27 +224,32 @@ def run_large(gpu, n=1536, frames=2):
            "library_device_gb": gpu.lib.contour3d_gb300_device_bytes() / 1e9, "field_gb": f.numel() * 4 / 1e9}
     del f
     torch.cuda.empty_cache()
-    # the FP32 input against the FP64 one: a 256^3 field of the same mode
-    # spectrum in f64 and its rounding to f32, the same levels, 1024x1024
-    fd, sd = workloads.modes_device(gpu, (256, 256, 256), nmodes=256, kmin=1, kmax=48, power=11.0 / 6.0, seed=4,
-                                    dtype=torch.float64)
-    ff = fd.float().contiguous()
-    s2 = _abi.make_scene(CAM, CENTRE, 1024, 1024)
-    g2 = [_abi.unit_grid(256)] * 3
-    lv2 = [-sd, -0.5 * sd, 0.5 * sd, sd]
+    # the FP32 input against the FP64 one on a 256^3 crop of this field (its
+    # centre, generated in both precisions from the same modes): vertex
+    # displacement over every crossed edge, and the image at 3840x2160
+    from contour3d_gb300 import fp32_error
+    crop, off = 256, (n - 256) // 2
+    fd = torch.empty((crop,) * 3, dtype=torch.float64, device="cuda")
+    ff = torch.empty((crop,) * 3, dtype=torch.float32, device="cuda")
+    for t, dt in ((fd, 0), (ff, 1)):
+        gpu.fieldgen_modes_device(t.data_ptr(), dt, (crop,) * 3, 256, 1, 48, 11.0 / 6.0, 4, offset=(off,) * 3,
+                                  glshape=(n, n, n))
+    g2 = [_abi.unit_grid(n)[off:off + crop]] * 3
     imgs, tris = [], []
     for t, dt in ((fd, 0), (ff, 1)):
-        o = torch.empty(1024 * 1024 * 3, dtype=torch.uint8, device="cuda")
-        if gpu.render_device(s2, [(t.data_ptr(), dt, (256, 256, 256), g2, lv, c)
-                                  for lv, c in zip(lv2, workloads.PALETTE)], o.data_ptr()) != 0:
+        o = torch.empty(W * H * 3, dtype=torch.uint8, device="cuda")
+        if gpu.render_device(scene, [(t.data_ptr(), dt, (crop,) * 3, g2, lv, c)
+                                     for lv, c in zip(levels, workloads.PALETTE)], o.data_ptr()) != 0:
             raise RuntimeError("fp32 comparison: render failed")
         torch.cuda.synchronize()
-        imgs.append(o.view(1024 * 1024, 3).cpu().numpy().astype(np.int16))
+        imgs.append(o.cpu().numpy())
         tris.append(int(gpu.stats().triangles))
-    d = np.abs(imgs[0] - imgs[1]).max(axis=1)
-    out["fp32_input_vs_fp64"] = {"field": "256^3, same spectrum; f32 = f64 rounded", "image": "1024x1024, 4 levels",
-                                 "pixels_differing": int((d > 0).sum()), "pixels": 1024 * 1024,
-                                 "max_channel_diff": int(d.max()), "triangles_f64": tris[0], "triangles_f32": tris[1]}
+    out["fp32_input_vs_fp64"] = dict(
+        {"field": f"{crop}^3 centre crop (offset {off}) of this field, generated in f64 and in f32",
+         "image": f"{W}x{H}, the 4 levels", "triangles_f64": tris[0], "triangles_f32": tris[1],
+         "f32_is_f64_rounded": bool(torch.equal(fd.float(), ff)),
+         "vertices": fp32_error.vertex_error(fd, ff, levels, g2)},
+        **fp32_error.image_difference(imgs[0], imgs[1]))
     del fd, ff
     return out
 
@@ -254,8 +259,8 @@ def run_batched(gpu, workers, nfields=64):
     the plain per-frame entry point one frame at a time, then the batched form
     (worker count from the autotuner unless given)."""
     import torch
-    from contour3d_gb300 import autotune, workloads
-    fields, frames = workloads.batch_set(gpu, nfields=nfields)
+    from contour3d_gb300 import _abi, autotune, workloads
+    fields, frames, twins = workloads.batch_set(gpu, nfields=nfields, twins=True)
     outs = [torch.empty(f.width * f.height * 3, dtype=torch.uint8, device="cuda") for f in frames]
     packs = [workloads.frame_pack(gpu, fields[f.field], f, o) for f, o in zip(frames, outs)]
     per_frame = [len(f.levels) * (fields[f.field].shape[0] - 1) * (fields[f.field].shape[1] - 1) *
@@ -286,11 +291,37 @@ def run_batched(gpu, workers, nfields=64):
     torch.cuda.synchronize()
     batch_s = time.perf_counter() - t0
     same = all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
+    # the float32 half against the float64 fields they were rounded from: the
+    # vertices of every crossed edge, and the frames rendered from both
+    from contour3d_gb300 import fp32_error
+    worst, rms2, edges, flips, px, maxd, rounded = 0.0, 0.0, 0, 0, 0, 0, True
+    o64 = torch.empty(1024 * 1024 * 3, dtype=torch.uint8, device="cuda")
+    for q, spec in enumerate(frames):
+        if spec.field not in twins:
+            continue
+        f32, f64 = fields[spec.field], twins[spec.field]
+        rounded = rounded and bool(torch.equal(f64.float(), f32))
+        nz, ny, nx = f32.shape
+        ve = fp32_error.vertex_error(f64, f32, spec.levels, [_abi.unit_grid(m) for m in (nx, ny, nz)])
+        worst = max(worst, ve["max_in_node_spacings"])
+        rms2 += ve["rms_in_node_spacings"] ** 2 * ve["edges_compared"]
+        edges += ve["edges_compared"]
+        flips += ve["edges_crossed_in_one_field_only"]
+        if gpu.render_pack(workloads.frame_pack(gpu, f64, spec, o64)) != 0:
+            raise RuntimeError("fp64 twin frame failed")
+        torch.cuda.synchronize()
+        d = fp32_error.image_difference(o64.cpu().numpy(), ref[q].cpu().numpy())
+        px += d["pixels_differing"]
+        maxd = max(maxd, d["max_channel_diff"])
+    fp32 = {"frames": len(twins), "f32_is_f64_rounded": rounded, "edges_compared": edges,
+            "edges_crossed_in_one_field_only": flips, "vertex_max_in_node_spacings": worst,
+            "vertex_rms_in_node_spacings": (rms2 / edges) ** 0.5 if edges else 0.0,
+            "pixels_differing": px, "pixels": len(twins) * 1024 * 1024, "max_channel_diff": maxd}
     return {"workload": f"{nfields} fields, dims 64..384, half f64 / half f32, 1-4 levels, own camera, 1024x1024",
             "frames": nfields, "cell_thresholds": int(cells), "workers": workers, "tuning": tuning,
             "plain": {"cells_per_s": cells / plain_s, "frames_per_s": nfields / plain_s, "s": plain_s},
             "batched": {"cells_per_s": cells / batch_s, "frames_per_s": nfields / batch_s, "s": batch_s},
-            "speedup": plain_s / batch_s, "images_identical": same}
+            "speedup": plain_s / batch_s, "images_identical": same, "fp32_input_vs_fp64": fp32}
 
 
 def run_served(gpu, slots, rates, nreq, budget_gb=120.0, seed=99):
@@ -570,6 +601,27 @@ def main():
         ms = float(t.item())
     cells_per_step = 2 * (nx - 1) * (ny - 1) * (nz - 1)
     value = world * cells_per_step / (ms / 1000.0)
+    timed_graph = int(gpu.stats().graph)  # 2: the timed frames ran as the recorded CUDA graph
+
+    # the same frame without the graph, and synchronised after every slab
+    # pass (outside the timed region; CUDA events over 5 frames each)
+    def frames_ms(n=5):
+        step()
+        step()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(n):
+            step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    gpu.set_graphs(False)
+    modes = {"graph_ms": ms, "timed_frames_graph": timed_graph, "unsynchronised_ms": frames_ms()}
+    gpu.set_async(False)
+    modes["synchronised_ms"] = frames_ms()
+    gpu.set_async(True)
+    gpu.set_graphs(True)
 
     # ---- roofline of the dominant stage (per-stage event times of one frame) ----
     peaks = {}
@@ -682,7 +734,7 @@ def main():
             "frames_per_s": 1000.0 / ms, "triangles_per_frame": int(st.triangles),
             "triangles_per_s": world * st.triangles / (ms / 1000.0),
             "gpu_launches": launches_per_step * args.steps,
-            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "frame_modes": modes,
             "batched": batched, "served": served, "large": large,
         }
         print(json.dumps(out))

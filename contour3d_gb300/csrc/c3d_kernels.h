@@ -88,6 +88,8 @@ struct TriDev {
   double* vn[9];      /* inspection: vertex normals */
   double* dbg_fn;     /* inspection: face normals, 3 per triangle */
   double* dbg_area;   /* inspection: areas */
+  unsigned long long cap; /* triangles the arrays (and the triangle -> cell map) hold */
+  unsigned* ovf;      /* overflow flags (kOvf*): set when the slab's triangles exceed cap */
 };
 constexpr unsigned kMetaRendered = 1u << 15;
 constexpr unsigned kMetaCulled = 1u << 16;
@@ -100,7 +102,14 @@ constexpr unsigned kMetaUndecided = 1u << 21;
    or -1 (projection fails), -2 (undecided) (low half) */
 struct VertDev {
   float4* pos;
+  unsigned long long cap; /* records pos holds */
+  unsigned* ovf;          /* overflow flags (kOvf*) */
 };
+
+/* overflow flags of a frame whose buffers were sized before the counts were
+   known (the frame is then rendered again with larger buffers) */
+constexpr unsigned kOvfTriangles = 1u; /* triangles beyond the triangle map or arrays */
+constexpr unsigned kOvfVertices = 2u;  /* crossed edges beyond the vertex records */
 
 /* triangle -> cell map entries: cell | rank << 28 (slabs hold fewer than 2^28 cells) */
 constexpr unsigned kTcCellMask = 0x0FFFFFFFu;
@@ -204,7 +213,7 @@ long long scan_segments(long long n);
    seg_base hold scan_segments(n) entries each */
 void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
                  unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
-                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, cudaStream_t st);
+                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, unsigned* ovf, cudaStream_t st);
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);

@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(kScanThreads, 4)
 k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigned long long* __restrict__ seg_base,
              unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
              const unsigned long long* __restrict__ totals, unsigned* __restrict__ tri_cell,
-             unsigned long long tri_cap, int want_offsets) {
+             unsigned long long tri_cap, int want_offsets, unsigned* __restrict__ ovf) {
   extern __shared__ __align__(16) unsigned char scan_smem[];
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ unsigned s_cnt[256];
@@ -589,6 +589,10 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
   const unsigned seg_tris = (unsigned)(s_warp[kScanThreads / 32 - 1] & kTriMask);
   const unsigned ta = (unsigned)(seg0 & kTriMask);
   const bool fill = slab_tris <= tri_cap;
+  /* a map that does not fit: the host fills it afterwards, or, when the
+     buffers were sized before the count was known (ovf given), renders the
+     frame again with a larger map */
+  if (!fill && ovf && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(ovf, kOvfTriangles);
   const bool listed = fill && seg_tris <= (unsigned)kFillList;
   const bool direct = fill && !listed;
   /* the triangle offsets are kept only when asked for or when the map must
@@ -1316,6 +1320,11 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
   if (c0 >= n) return;
   const long long c1 = min(c0 + kVTile, n);
   const unsigned va = voffsets[c0], vb = voffsets[c1];
+  if (vb > V.cap) {
+    /* more crossed edges than records (buffers sized before the count was known) */
+    if (threadIdx.x == 0) atomicOr(V.ovf, kOvfVertices);
+    return;
+  }
   {
     /* the thread's kVItems cells: one 8-byte load of their codes (a code
        past the end reads as 0: no owned edges); their vertices are
@@ -1517,6 +1526,11 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
   const long long T_ = (long long)*total_p;
+  if ((unsigned long long)T_ > tri.cap) {
+    /* more triangles than the arrays hold (sized before the count was known) */
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(tri.ovf, kOvfTriangles);
+    return;
+  }
   const long long step = (long long)blockDim.x * kEmitPer;
   /* every thread of a block runs the same iterations (block-wide appends) */
   for (long long base = blockIdx.x * step; base < T_; base += (long long)gridDim.x * step) {
@@ -2703,6 +2717,10 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
   if (cudaMemcpyToSymbol(g_edge_tris, edge_tris, sizeof(unsigned short) * 256 * 19) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_nb, nb, sizeof(signed char) * 19 * 16) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_nb_count, nb_count, 19) != cudaSuccess) return 1;
+  /* beyond the default 48 KB of dynamic shared memory: set once per device */
+  if (cudaFuncSetAttribute(k_scan_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanWriteSmem) !=
+      cudaSuccess)
+    return 1;
   return 0;
 }
 
@@ -2807,15 +2825,14 @@ long long scan_segments(long long n) { return (n + kScanTile - 1) / kScanTile; }
 
 void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
                  unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
-                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, cudaStream_t st) {
+                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, unsigned* ovf, cudaStream_t st) {
   const long long nseg = scan_segments(n);
   if (nseg > 0) k_seg_reduce<<<(unsigned)nseg, kScanThreads, 0, st>>>(codes, n, seg_sums);
   k_seg_scan<<<1, kSegScanThreads, 0, st>>>(seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
-  /* beyond the default 48 KB of dynamic shared memory: set for the current device */
-  cudaFuncSetAttribute(k_scan_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanWriteSmem);
   if (nseg > 0)
     k_scan_write<<<(unsigned)nseg, kScanThreads, kScanWriteSmem, st>>>(codes, n, seg_base, offsets, voffsets, totals,
-                                                                       tri_cell, tri_cap, want_offsets ? 1 : 0);
+                                                                       tri_cell, tri_cap, want_offsets ? 1 : 0,
+                                                                       ovf);
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,

@@ -348,6 +348,9 @@ static cudaMemPool_t device_pool() {
  * wait until the server's HBM budget has room) and every release is
  * credited.  Contexts outside a server have none.
  */
+/* set when a buffer had to grow while its stream was being captured */
+static thread_local bool t_capture_needs_growth = false;
+
 struct MemHook {
   virtual int charge(size_t bytes) = 0;
   virtual void credit(size_t bytes) = 0;
@@ -363,6 +366,13 @@ struct Buf {
      (or whose previous uses have completed) */
   int ensure(size_t bytes, cudaStream_t st) {
     if (bytes <= cap) return 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (st && cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      /* a frame being recorded into a graph must not allocate: the caller
+         abandons the recording and renders the frame without it */
+      t_capture_needs_growth = true;
+      return 1;
+    }
     release(st);
     const size_t want = bytes + bytes / 4 + 256;
     if (hook && hook->charge(want)) return 1;
@@ -418,12 +428,13 @@ struct Ctx {
   int device = -1;
   bool ready = false;
   cudaStream_t own_stream = nullptr;
-  Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, grids, nodes, canvas, xy, rgb, segs;
+  Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, nodes, canvas, rgb;
   Buf nb_ent, nb_wn, nb_span; /* the FP64 shading pass's neighbour lists */
-  Buf zlo, xyf, cand, live, tiny, win, checks, voffsets, verts, winfo, amb, shade_check;
+  Buf zlo, cand, live, tiny, win, checks, voffsets, verts, winfo, amb, shade_check;
   unsigned long long epoch = 0; /* frame counter for the winner-weight tags (1 .. 2^24 - 1) */
-  HostBuf h_grids;             /* pinned staging: node coordinates and pixel centres */
-  cudaEvent_t ev_staged = nullptr; /* the staging buffer may be rewritten once this completed */
+  Buf consts;                  /* the frame constants (pixel centres, grid blocks, line segments) */
+  HostBuf h_consts;            /* their pinned staging block */
+  cudaEvent_t ev_staged = nullptr; /* the staging block may be rewritten once this completed */
   bool filter_check = false;
   HostBuf h_small, h_rgb, h_slots;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs[11] = {};
@@ -433,6 +444,35 @@ struct Ctx {
   const void *field_src = nullptr; /* host array currently in `field` (valid within one call) */
   size_t field_bytes = 0;
   uint64_t stats_h2d = 0;
+  /* frames without host synchronisation: buffers sized from the largest
+     counts seen so far (caps), the counts of every pass kept in a device
+     status block read once at the frame's end; a frame whose counts exceed
+     the sizes is rendered again with synchronisation, which learns them */
+  bool async_enabled = true;
+  bool frame_async = false;     /* the current frame runs without host synchronisation */
+  struct Caps {
+    unsigned long long T = 0, V = 0, cand = 0, tiny = 0, ent = 0;
+  } caps;
+  bool caps_known = false;      /* a frame completed with synchronisation on this context */
+  Buf status;                   /* device status block of the current frame */
+  HostBuf h_status;             /* its pinned copy */
+  int status_next = 0, status_obj_next = 0;
+  unsigned long long async_cand_cap = 0, async_tiny_cap = 0, async_ent_cap = 0;
+  std::vector<char> async_obj_fp32; /* per object status record: the FP32 shading pass ran */
+  /* the last unsynchronised device frame as a CUDA graph: recorded the second
+     time a frame with the same description (frame_key) comes, launched
+     instead of the individual calls from the third time on */
+  bool graphs_enabled = true;
+  bool capturing = false;
+  uint64_t graph_key = 0;
+  bool graph_key_seen = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  struct GraphFrame {
+    int status_next = 0, status_obj_next = 0;
+    unsigned long long cand_cap = 0, tiny_cap = 0, ent_cap = 0;
+    std::vector<char> obj_fp32;
+    uint64_t kernel_launches = 0, slabs = 0, cells = 0;
+  } graph_frame;
   cudaStream_t copy_stream = nullptr;  /* host field uploads, overlapped with the slabs */
   cudaEvent_t ev_field = nullptr;      /* the field buffer may be overwritten once this completed */
   std::vector<cudaEvent_t> chunk_ev;   /* upload chunk s has arrived */
@@ -551,13 +591,151 @@ struct FrameOut {
   DebugSink *sink = nullptr;
 };
 
-/* word of the 64-byte check buffer that holds the z-buffer error flags */
+/* words of the 64-byte check buffer: 0-5 self-check counters, then the
+   z-buffer error flags, the overflow flags (kOvf*) and, in frames without
+   host synchronisation, the classification's error flags */
 static const int kZbufErrWord = 8;
+static const int kOvfWord = 9;
+static const int kClsErrWord = 10;
+
+/* a field group's block of the frame constants: node coordinates (doubles),
+   their float roundings, the float node spacings, and the largest |coordinate| */
+struct GroupGrid {
+  const double *dev = nullptr;
+  double coord_max = 0.;
+};
+
+static size_t grid_block_bytes(const ContourIn &ci) {
+  const size_t ng = ci.sz[0] + ci.sz[1] + ci.sz[2];
+  return sizeof(double) * ng + sizeof(float) * (2 * ng - 3);
+}
+
+/* the grid block of one field (x, y, z nodes in turn) into hg; returns the largest |coordinate| */
+static double fill_grid_block(const ContourIn &ci, double *hg) {
+  const long long n3[3] = {(long long)ci.sz[0], (long long)ci.sz[1], (long long)ci.sz[2]};
+  const size_t ng = (size_t)(n3[0] + n3[1] + n3[2]);
+  float *hgf = reinterpret_cast<float *>(hg + ng);
+  float *hgd = hgf + ng;
+  memcpy(hg, ci.grid[0], sizeof(double) * n3[0]);
+  memcpy(hg + n3[0], ci.grid[1], sizeof(double) * n3[1]);
+  memcpy(hg + n3[0] + n3[1], ci.grid[2], sizeof(double) * n3[2]);
+  for (size_t q = 0; q < ng; q++) hgf[q] = (float)hg[q];
+  double coord_max = 0.;
+  size_t at = 0, out = 0;
+  for (int d = 0; d < 3; d++) {
+    for (long long q = 0; q + 1 < n3[d]; q++) hgd[out++] = (float)(hg[at + q + 1] - hg[at + q]);
+    for (long long q = 0; q < n3[d]; q++) coord_max = std::max(coord_max, std::fabs(hg[at + q]));
+    at += (size_t)n3[d];
+  }
+  return coord_max;
+}
+
+/* line.c:121-170 on the host: every segment's end points projected to pixel
+   units (render.c's convention); 1 on a line object with fewer than two items */
+static int build_line_segs(const FrameIn &f, std::vector<LineSegDev> &segs) {
+  const HostScene &s = f.scene;
+  for (size_t n = 0; n < f.nlines; n++) {
+    const contour3d_line_obj_t *l = f.lines + n;
+    const size_t np = l->nitems;
+    if (np < 2) {
+      log_error("give more than two points to draw a line, received %zu", np);
+      log_error("line processing failed");
+      return 1;
+    }
+    const conv_fn conv = l->converter ? l->converter : contour3d_gb300_identity;
+    const V *heads = l->edges + 0, *tails = l->edges + 1;
+    const V deltas = h_mul(1. / (np - 1), h_sub(*tails, *heads));
+    const unsigned rgb = ((unsigned)l->color.r << 16) | ((unsigned)l->color.g << 8) | l->color.b;
+    for (size_t q = 0; q < np - 1; q++) {
+      const V a = h_add(*heads, h_mul(q + 0, deltas));
+      const V b = h_add(*heads, h_mul(q + 1, deltas));
+      const V pa = conv(a), pb = conv(b);
+      V p0 = {0., 0., 0.}, p1 = {0., 0., 0.};
+      LineSegDev sg = {};
+      sg.valid = !h_project(s, pa, &p0) && !h_project(s, pb, &p1);
+      if (sg.valid) {
+        sg.p0x = (0.5 + p0.x) * s.W;
+        sg.p0y = (0.5 + p0.y) * s.H;
+        sg.p1x = (0.5 + p1.x) * s.W;
+        sg.p1y = (0.5 + p1.y) * s.H;
+        sg.p0z = p0.z;
+        sg.p1z = p1.z;
+      }
+      sg.width = l->width;
+      sg.rgb = rgb;
+      segs.push_back(sg);
+    }
+  }
+  return 0;
+}
+
+/*
+ * The frame's constant inputs, staged in one pinned block and copied to the
+ * device with one copy: the pixel centres (render.c:100-104) in double and
+ * float, every field group's grid block, and the line segments.  Each region
+ * starts on 256 bytes.
+ */
+struct FrameConsts {
+  const double *xy = nullptr;
+  const float *xyf = nullptr;
+  std::vector<GroupGrid> groups;
+  const LineSegDev *segs = nullptr;
+  int nseg = 0;
+};
+
+static int stage_frame_consts(Ctx &c, const FrameIn &f, const std::vector<std::pair<size_t, size_t>> &groups,
+                              const std::vector<LineSegDev> &segs, FrameConsts &fc) {
+  const size_t W = f.scene.W, H = f.scene.H;
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    const size_t a = at;
+    at = (at + bytes + 255) & ~(size_t)255;
+    return a;
+  };
+  const size_t o_xy = take(sizeof(double) * (W + H)), o_xyf = take(sizeof(float) * (W + H));
+  std::vector<size_t> o_grid(groups.size());
+  for (size_t g = 0; g < groups.size(); g++) o_grid[g] = take(grid_block_bytes(f.contours[groups[g].first]));
+  const size_t o_segs = take(sizeof(LineSegDev) * segs.size());
+  /* the previous frame's copy from the staging block must have left it (a
+     frame being recorded synchronised before the recording began) */
+  if (!c.capturing) C3D_CUDA(cudaEventSynchronize(c.ev_staged));
+  if (c.h_consts.ensure(at) || c.consts.ensure(at, f.stream)) return 1;
+  char *h = c.h_consts.as<char>();
+  char *d = c.consts.as<char>();
+  double *xy = reinterpret_cast<double *>(h + o_xy);
+  float *xyf = reinterpret_cast<float *>(h + o_xyf);
+  for (size_t i = 0; i < W; i++) xy[i] = 1. * (i + 0.5) / W - 0.5;
+  for (size_t j = 0; j < H; j++) xy[W + j] = 1. * (j + 0.5) / H - 0.5;
+  for (size_t q = 0; q < W + H; q++) xyf[q] = (float)xy[q];
+  fc.xy = reinterpret_cast<const double *>(d + o_xy);
+  fc.xyf = reinterpret_cast<const float *>(d + o_xyf);
+  fc.groups.assign(groups.size(), GroupGrid());
+  for (size_t g = 0; g < groups.size(); g++) {
+    fc.groups[g].coord_max = fill_grid_block(f.contours[groups[g].first], reinterpret_cast<double *>(h + o_grid[g]));
+    fc.groups[g].dev = reinterpret_cast<const double *>(d + o_grid[g]);
+  }
+  if (!segs.empty()) memcpy(h + o_segs, segs.data(), sizeof(LineSegDev) * segs.size());
+  fc.segs = reinterpret_cast<const LineSegDev *>(d + o_segs);
+  fc.nseg = (int)segs.size();
+  C3D_CUDA(cudaMemcpyAsync(d, h, at, cudaMemcpyHostToDevice, f.stream));
+  if (!c.capturing) C3D_CUDA(cudaEventRecord(c.ev_staged, f.stream));
+  return 0;
+}
+
+/* the status block of a frame rendered without host synchronisation, in
+   64-bit words: kStatusHead words, then per (slab, object) pass kSlabRec
+   words (triangles, vertices, the kCounters raster counters), then per
+   object three words (won pixels, ambiguous pixels, neighbour entries) */
+static const int kStatusHead = 2;
+static const int kStatusSlabs = 1024;
+static const int kStatusObjs = 256;
 
 /* device counters of one slab's raster passes: candidates, tiny triangles,
    won pixels, requested normals, listed triangles, surviving candidates,
    slivers, pixels shaded in FP64, their FP64 normal requests */
 static const int kCounters = 9;
+static const int kSlabRec = 2 + kCounters;
+static const size_t kStatusWords = kStatusHead + (size_t)kSlabRec * kStatusSlabs + 3 * (size_t)kStatusObjs;
 
 /* bytes per triangle of the slab arrays (see TriDev) */
 static const size_t kTriBytes = 3 * sizeof(double) + 48 + sizeof(unsigned);
@@ -651,7 +829,8 @@ static bool same_field(const ContourIn &a, const ContourIn &b) {
  * not depend on this order (fragments carry their drawing order).
  */
 static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn *objs, size_t nobj,
-                          unsigned long long &order_base, const RasterDev &R, DebugSink *sink) {
+                          unsigned long long &order_base, const RasterDev &R, DebugSink *sink,
+                          const GroupGrid &gg) {
   const ContourIn &ci = objs[0];
   cudaStream_t st = f.stream;
   const long long nx = (long long)ci.sz[0], ny = (long long)ci.sz[1], nz = (long long)ci.sz[2];
@@ -676,36 +855,13 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     dfield = c.field.p;
   }
-  /* node coordinates, their float roundings, and the node spacings g[i + 1] -
-     g[i] rounded to float (single-precision shading) */
+  /* node coordinates, their float roundings and spacings: this group's
+     block of the frame constants */
   const size_t ng = (size_t)(nx + ny + nz);
-  const size_t gbytes = sizeof(double) * ng + sizeof(float) * (2 * ng - 3);
-  if (c.grids.ensure(gbytes, st)) return 1;
-  double *g = c.grids.as<double>();
-  float *gf = reinterpret_cast<float *>(g + ng);
-  float *gd = gf + ng;
-  /* the previous upload from the staging buffer must have left it */
-  C3D_CUDA(cudaEventSynchronize(c.ev_staged));
-  if (c.h_grids.ensure(gbytes)) return 1;
-  double *hg = c.h_grids.as<double>();
-  float *hgf = reinterpret_cast<float *>(hg + ng);
-  float *hgd = hgf + ng;
-  memcpy(hg, ci.grid[0], sizeof(double) * nx);
-  memcpy(hg + nx, ci.grid[1], sizeof(double) * ny);
-  memcpy(hg + nx + ny, ci.grid[2], sizeof(double) * nz);
-  for (size_t q = 0; q < ng; q++) hgf[q] = (float)hg[q];
-  double coord_max = 0.;
-  {
-    const long long n3[3] = {nx, ny, nz};
-    size_t at = 0, out = 0;
-    for (int d = 0; d < 3; d++) {
-      for (long long q = 0; q + 1 < n3[d]; q++) hgd[out++] = (float)(hg[at + q + 1] - hg[at + q]);
-      for (long long q = 0; q < n3[d]; q++) coord_max = std::max(coord_max, std::fabs(hg[at + q]));
-      at += (size_t)n3[d];
-    }
-  }
-  C3D_CUDA(cudaMemcpyAsync(g, hg, gbytes, cudaMemcpyHostToDevice, st));
-  C3D_CUDA(cudaEventRecord(c.ev_staged, st));
+  const double *g = gg.dev;
+  const float *gf = reinterpret_cast<const float *>(g + ng);
+  const float *gd = gf + ng;
+  const double coord_max = gg.coord_max;
   const double *dnodes = nullptr;
   std::vector<double> nodes;
   if (!is_identity(ci.converter)) {
@@ -779,6 +935,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     return 1;
   }
   const bool want_all = sink != nullptr;
+  const bool async = c.frame_async && !sink;
   const long long kr0 = want_all ? 0 : 1, kr1 = want_all ? ncz : ncz - 1;
   /* the slabs [k0, k1) of rendered slices, in the order they are visited */
   std::vector<std::pair<long long, long long>> slabs;
@@ -872,8 +1029,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
        least one triangle per two cells */
     if (c.tri_cell.ensure(sizeof(unsigned) * (size_t)(ncell / 2 + 1024), st)) return 1;
     unsigned *d_counter = c.scratch.as<unsigned>();
-    unsigned *d_err = d_counter + 1;
-    unsigned long long *d_total = reinterpret_cast<unsigned long long *>(d_counter + 2); /* triangles, vertices */
+    unsigned *d_err = async ? c.checks.as<unsigned>() + kClsErrWord : d_counter + 1;
+    unsigned *d_ovf = c.checks.as<unsigned>() + kOvfWord;
     const long long nseg = scan_segments(ncell);
     unsigned long long *seg_sums = c.tile_state.as<unsigned long long>(), *seg_base = seg_sums + nseg;
     if (pipelined) {
@@ -890,7 +1047,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     for (size_t q = 0; q < nobj; q++) obj_codes[q] = c.counts.as<unsigned char>() + code_stride * q;
     last_codes = obj_codes;
     codes_whole = S.kfirst == 0 && S.nslices == ncz;
-    C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
+    if (!async) C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
     c.stats.kernel_launches += (uint64_t)launch_classify(Fo.data(), (int)nobj, S, obj_codes.data(), d_err, st);
     if (c.stage_timing) cudaEventRecord(c.evs[1], st);
@@ -898,31 +1055,59 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       const FieldDev &F = Fo[ob];
       unsigned char *codes = obj_codes[ob];
       const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
+      /* this slab and object's record of the frame status: the scan's totals
+         (triangles, vertices), then the raster counters */
+      unsigned long long *srec = nullptr;
+      if (async) {
+        if (c.status_next >= kStatusSlabs) {
+          log_error("internal: more slab passes than status records");
+          return 1;
+        }
+        srec = c.status.as<unsigned long long>() + kStatusHead + kSlabRec * c.status_next++;
+      }
+      unsigned long long *d_total = async ? srec : reinterpret_cast<unsigned long long *>(d_counter + 2);
+      if (async) {
+        /* sized before the count is known, from the largest slab seen so
+           far; kernels that find more record an overflow and the frame is
+           rendered again */
+        if (c.tri_cell.ensure(sizeof(unsigned) * c.caps.T, st) || c.tri.ensure(kTriBytes * (c.caps.T + 64), st))
+          return 1;
+      }
       /* read per object: an earlier object of the slab may have grown the buffer */
       const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
       if (c.stage_timing && ob > 0) cudaEventRecord(c.evs[1], st);
       launch_scan(codes, ncell, seg_sums, seg_base, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
-                  c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, st);
+                  c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, async ? d_ovf : nullptr, st);
       if (c.stage_timing) cudaEventRecord(c.evs[2], st);
       c.stats.kernel_launches += 3;
-      C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaStreamSynchronize(st));
-      if (c.stage_timing) {
-        if (ob == 0) c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
-        c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
+      unsigned long long T = 0, NV = 0;
+      if (async) {
+        T = c.caps.T;
+        NV = c.caps.V;
+        c.stats.slabs += 1;
+      } else {
+        C3D_CUDA(cudaMemcpyAsync(h_small, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaMemcpyAsync(h_total, d_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaStreamSynchronize(st));
+        if (c.stage_timing) {
+          if (ob == 0) c.stats.ms_classify += elapsed(c.evs[0], c.evs[1]);
+          c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
+        }
+        if (h_small[0]) {
+          log_error("device classification did not complete (error flags 0x%x)", h_small[0]);
+          return 1;
+        }
+        T = h_total[0];
+        NV = h_total[1];
+        c.stats.triangles += T;
+        c.stats.slabs += 1;
+        c.caps.T = std::max(c.caps.T, T);
+        c.caps.V = std::max(c.caps.V, NV);
+        if (T == 0) continue;
       }
-      if (h_small[0]) {
-        log_error("device classification did not complete (error flags 0x%x)", h_small[0]);
-        return 1;
-      }
-      const unsigned long long T = h_total[0], NV = h_total[1];
-      c.stats.triangles += T;
-      c.stats.slabs += 1;
-      if (T == 0) continue;
       /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
          every sub-array stays aligned (and over-allocate so that cap >= T) */
-      const bool filled = T <= tri_cap; /* the scan wrote the triangle -> cell map */
+      const bool filled = async || T <= tri_cap; /* the scan wrote the triangle -> cell map */
       if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
       const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
       if (cap < T) {
@@ -934,7 +1119,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap, st)) return 1;
         dbg = c.dbg.as<double>();
       }
-      const TriDev tri = tri_layout(c.tri.p, cap, dbg);
+      TriDev tri = tri_layout(c.tri.p, cap, dbg);
+      tri.cap = std::min<unsigned long long>(cap, c.tri_cell.cap / sizeof(unsigned));
+      tri.ovf = d_ovf;
       unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
       /* the vertex stage: triangle -> cell map, screen vertices */
       if (c.stage_timing) cudaEventRecord(c.evs[3], st);
@@ -947,9 +1134,11 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* the screen vertices of the slab's crossed edges, 16 bytes each */
         if (c.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
         VD.pos = c.verts.as<float4>();
+        VD.cap = c.verts.cap / 16;
+        VD.ovf = d_ovf;
         launch_vertices(F, S, sd, codes, c.voffsets.as<unsigned>(), ncell, VD, st);
         c.stats.kernel_launches += 1;
-        c.stats.vertices += NV;
+        if (!async) c.stats.vertices += NV;
       }
       if (c.stage_timing) cudaEventRecord(c.evs[8], st);
       const unsigned long long slab_order = obase + 12ULL * (unsigned long long)(S.kfirst * per_slice);
@@ -976,8 +1165,13 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
            list holds at most one entry per triangle and cannot overflow. */
         unsigned long long cand_want = std::max<unsigned long long>(T / 2, 1ULL << 20);
         unsigned long long tiny_want = std::max<unsigned long long>(T / 16, 1ULL << 16);
+        if (async) {
+          cand_want = std::max(cand_want, c.caps.cand);
+          tiny_want = std::max(tiny_want, c.caps.tiny);
+        }
         RasterDev RS = R;
-        unsigned long long *counters = reinterpret_cast<unsigned long long *>(d_counter + 6);
+        /* without host synchronisation the counters stay in the frame status */
+        unsigned long long *counters = async ? srec + 2 : reinterpret_cast<unsigned long long *>(d_counter + 6);
         unsigned long long *h_cnt = h_total + 2;
         RS.cover_count = counters + 4;
         RS.live_count = counters + 5;
@@ -994,7 +1188,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           RS.tiny = c.tiny.as<unsigned>();
           RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
           RS.tiny_count = counters + 1;
-          C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
+          if (!async) C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
           if (c.stage_timing) cudaEventRecord(c.evs[9], st);
           launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, c.offsets.as<unsigned>(),
                       c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
@@ -1008,6 +1202,12 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
           if (c.stage_timing) cudaEventRecord(c.evs[6], st);
           c.stats.kernel_launches += 6;
+          if (async) {
+            /* list capacities of this pass, compared with the counts at the frame's end */
+            c.async_cand_cap = std::min(c.async_cand_cap, RS.cand_cap);
+            c.async_tiny_cap = std::min(c.async_tiny_cap, RS.tiny_cap);
+            break;
+          }
           C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, kCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
           C3D_CUDA(cudaStreamSynchronize(st));
           if (h_cnt[0] <= RS.cand_cap && h_cnt[1] <= RS.tiny_cap) break;
@@ -1019,11 +1219,15 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           cand_want = std::max<unsigned long long>(cand_want, h_cnt[0] + h_cnt[0] / 4);
           tiny_want = std::max<unsigned long long>(tiny_want, h_cnt[1] + h_cnt[1] / 4);
         }
-        c.stats.candidates += h_cnt[0];
-        c.stats.tiny += h_cnt[1];
-        c.stats.cover_triangles += h_cnt[4];
-        c.stats.exact_fragments += h_cnt[5];
-        c.stats.slivers += h_cnt[6];
+        if (!async) {
+          c.stats.candidates += h_cnt[0];
+          c.stats.tiny += h_cnt[1];
+          c.stats.cover_triangles += h_cnt[4];
+          c.stats.exact_fragments += h_cnt[5];
+          c.stats.slivers += h_cnt[6];
+          c.caps.cand = std::max(c.caps.cand, h_cnt[0] + h_cnt[0] / 4);
+          c.caps.tiny = std::max(c.caps.tiny, h_cnt[1] + h_cnt[1] / 4);
+        }
         if (c.stage_timing) {
           c.stats.ms_vertices += elapsed(c.evs[3], c.evs[8]);
           c.stats.ms_emit += elapsed(c.evs[9], c.evs[4]);
@@ -1084,6 +1288,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
     for (size_t ob = 0; ob < nobj; ob++) {
       const contour3d_color_t &col = objs[ob].color;
+      if (async) {
+        /* the object's record of the frame status: won, ambiguous, neighbour entries */
+        if (c.status_obj_next >= kStatusObjs) {
+          log_error("internal: more contour objects than status records");
+          return 1;
+        }
+        counters = c.status.as<unsigned long long>() + kStatusHead + kSlabRec * kStatusSlabs + 3 * c.status_obj_next++;
+      }
       RasterDev RS = R;
       RS.win = c.win.as<unsigned>();
       RS.win_count = counters + 0;
@@ -1096,20 +1308,37 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       RS.shade_check = c.filter_check ? c.shade_check.as<unsigned>() : nullptr;
       const unsigned rgb = ((unsigned)col.r << 16) | ((unsigned)col.g << 8) | col.b;
       const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
-      C3D_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st));
+      if (!async) C3D_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st));
       if (c.stage_timing) cudaEventRecord(c.evs[6], st);
       /* the classification's codes, when the slab loop left the whole field's */
       FieldDev Fs = Fo[ob];
       Fs.codes = codes_whole ? last_codes[ob] : nullptr;
       launch_shade_f(Fs, sd, RS, c.lut.as<unsigned long long>(), obase, rgb, st);
       if (c.stage_timing) cudaEventRecord(c.evs[10], st);
-      C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-      C3D_CUDA(cudaStreamSynchronize(st));
       /* without node spacings (a converter) every won pixel takes the FP64 pass */
       const bool fp32 = Fo[ob].dgx != nullptr && nx <= (1 << 20) && ny <= (1 << 20) && nz <= (1 << 20);
-      const unsigned long long nwin = h_cnt[0], namb = fp32 ? h_cnt[1] : nwin;
       const unsigned *list = fp32 ? RS.amb : RS.win;
       const unsigned long long *lcount = fp32 ? RS.amb_count : RS.win_count;
+      if (async) {
+        /* the FP64 pass over at most every pixel, its neighbour entries
+           sized from the largest count seen; overflow shows in the status */
+        const unsigned long long want = std::max<unsigned long long>(c.caps.ent, 1ULL << 16);
+        if (c.nb_ent.ensure(sizeof(unsigned long long) * want, st) || c.nb_wn.ensure(3 * sizeof(double) * want, st) ||
+            c.nb_span.ensure(sizeof(uint2) * 3 * npx, st))
+          return 1;
+        const unsigned long long cap =
+            std::min(c.nb_ent.cap / sizeof(unsigned long long), c.nb_wn.cap / (3 * sizeof(double)));
+        c.async_ent_cap = std::min(c.async_ent_cap, cap);
+        c.async_obj_fp32.push_back(fp32 ? 1 : 0);
+        launch_shade_exact(Fs, sd, RS, c.lut.as<unsigned long long>(), list, lcount, (long long)npx, obase,
+                           c.nb_ent.as<unsigned long long>(), cap, counters + 2, c.nb_span.as<uint2>(),
+                           c.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
+        c.stats.kernel_launches += 3 + (fp32 ? 2 : 1);
+        continue;
+      }
+      C3D_CUDA(cudaMemcpyAsync(h_cnt, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+      C3D_CUDA(cudaStreamSynchronize(st));
+      const unsigned long long nwin = h_cnt[0], namb = fp32 ? h_cnt[1] : nwin;
       unsigned long long entries = 0;
       if (namb) {
         /* about six neighbour triangles per vertex; more are listed again */
@@ -1141,6 +1370,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       c.stats.winners += nwin;
       c.stats.shade_exact += namb;
       c.stats.normals += entries;
+      c.caps.ent = std::max(c.caps.ent, entries + entries / 4);
       if (c.stage_timing) {
         cudaEventSynchronize(c.evs[7]);
         c.stats.ms_normals += elapsed(c.evs[6], c.evs[10]);
@@ -1152,55 +1382,248 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   return 0;
 }
 
-/* line.c:121-170 on the host (segment end points and projections), pixels on the device */
-static int render_lines(Ctx &c, const FrameIn &f, unsigned long long &order_base) {
-  const HostScene &s = f.scene;
-  std::vector<LineSegDev> segs;
-  for (size_t n = 0; n < f.nlines; n++) {
-    const contour3d_line_obj_t *l = f.lines + n;
-    const size_t np = l->nitems;
-    if (np < 2) {
-      log_error("give more than two points to draw a line, received %zu", np);
-      log_error("line processing failed");
-      return 1;
-    }
-    const conv_fn conv = l->converter ? l->converter : contour3d_gb300_identity;
-    const V *heads = l->edges + 0, *tails = l->edges + 1;
-    const V deltas = h_mul(1. / (np - 1), h_sub(*tails, *heads));
-    const unsigned rgb = ((unsigned)l->color.r << 16) | ((unsigned)l->color.g << 8) | l->color.b;
-    for (size_t q = 0; q < np - 1; q++) {
-      const V a = h_add(*heads, h_mul(q + 0, deltas));
-      const V b = h_add(*heads, h_mul(q + 1, deltas));
-      const V pa = conv(a), pb = conv(b);
-      V p0 = {0., 0., 0.}, p1 = {0., 0., 0.};
-      LineSegDev sg = {};
-      sg.valid = !h_project(s, pa, &p0) && !h_project(s, pb, &p1);
-      if (sg.valid) {
-        sg.p0x = (0.5 + p0.x) * s.W;
-        sg.p0y = (0.5 + p0.y) * s.H;
-        sg.p1x = (0.5 + p1.x) * s.W;
-        sg.p1y = (0.5 + p1.y) * s.H;
-        sg.p0z = p0.z;
-        sg.p1z = p1.z;
-      }
-      sg.width = l->width;
-      sg.rgb = rgb;
-      segs.push_back(sg);
-    }
+/* the field groups of a frame: objects that read one field with one
+   geometry share its upload, node tables and slabs (inspection takes one
+   object at a time) */
+static std::vector<std::pair<size_t, size_t>> field_groups(const FrameIn &f, bool one_each) {
+  std::vector<std::pair<size_t, size_t>> groups;
+  for (size_t n = 0; n < f.contours.size();) {
+    size_t m = n + 1;
+    if (!one_each)
+      while (m < f.contours.size() && same_field(f.contours[n], f.contours[m])) m++;
+    groups.push_back({n, m});
+    n = m;
   }
-  if (segs.empty()) return 0;
-  if (c.segs.ensure(sizeof(LineSegDev) * segs.size(), f.stream)) return 1;
-  C3D_CUDA(cudaMemcpyAsync(c.segs.p, segs.data(), sizeof(LineSegDev) * segs.size(), cudaMemcpyHostToDevice, f.stream));
-  launch_lines(c.segs.as<LineSegDev>(), (int)segs.size(), (long long)s.W, (long long)s.H, c.canvas.as<Slot>(),
-               order_base, c.checks.as<unsigned>() + kZbufErrWord, f.stream);
-  c.stats.kernel_launches += 1;
-  /* the stream is synchronised before `segs` goes out of scope by the caller's resolve copy */
-  C3D_CUDA(cudaStreamSynchronize(f.stream));
-  order_base += segs.size();
+  return groups;
+}
+
+/* a frame rendered without host synchronisation found more work than its
+   buffers were sized for: render it again with synchronisation */
+static const int kFrameRedo = 2;
+
+static int render_frame_pass(Ctx &c, const FrameIn &f, const FrameOut &o, bool async);
+static int frame_status(Ctx &c, bool async);
+
+/* FNV-1a over everything a frame's recorded work depends on besides the
+   field values: the scene, each field's address, type, sizes, node
+   coordinates, converter, level and colour, the lines, the output and the
+   stream */
+struct KeyHash {
+  uint64_t h = 1469598103934665603ULL;
+  void add(const void *p, size_t n) {
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    for (size_t q = 0; q < n; q++) h = (h ^ b[q]) * 1099511628211ULL;
+  }
+  template <typename T> void add(const T &v) { add(&v, sizeof v); }
+};
+
+static uint64_t frame_key(const FrameIn &f, const FrameOut &o) {
+  KeyHash k;
+  const HostScene &s = f.scene;
+  k.add(s.cam);
+  k.add(s.center);
+  k.add(s.lx);
+  k.add(s.ly);
+  k.add(s.light);
+  k.add(s.W);
+  k.add(s.H);
+  k.add(f.bg);
+  for (const ContourIn &ci : f.contours) {
+    k.add(ci.data);
+    k.add(ci.f32);
+    k.add(ci.sz);
+    k.add(ci.converter);
+    k.add(ci.threshold);
+    k.add(ci.color);
+    for (int d = 0; d < 3; d++) k.add(ci.grid[d], sizeof(double) * ci.sz[d]);
+  }
+  if (f.nlines) k.add(f.lines, sizeof(contour3d_line_obj_t) * f.nlines);
+  k.add(o.rgb_dev);
+  k.add(f.stream);
+  return k.h;
+}
+
+/* device-resident identity-grid fields drawn into a device image on a
+   stream of the caller's or the context's (the legacy default stream cannot
+   be recorded) */
+static bool graph_eligible(const Ctx &c, const FrameIn &f, const FrameOut &o) {
+  if (!c.graphs_enabled || !f.stream || o.sink || o.rgb_host || o.rgb_pinned || o.depth_host || o.pixels_host ||
+      !o.rgb_dev || c.filter_check || c.stage_timing)
+    return false;
+  for (const ContourIn &ci : f.contours)
+    if (!ci.on_device || !is_identity(ci.converter)) return false;
+  return true;
+}
+
+static void drop_graph(Ctx &c) {
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  c.graph_exec = nullptr;
+}
+
+/* end the recording of the current frame, keep it as the context's graph and
+   run it on `st` (between the frame's timing events) */
+static int end_capture_and_launch(Ctx &c, cudaStream_t st) {
+  cudaGraph_t g = nullptr;
+  c.capturing = false;
+  cudaError_t e = cudaStreamEndCapture(st, &g);
+  drop_graph(c);
+  if (e == cudaSuccess && g) e = cudaGraphInstantiate(&c.graph_exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess || !c.graph_exec) {
+    log_error("recording the frame as a graph failed: %s", cudaGetErrorString(e));
+    c.graph_exec = nullptr;
+    return 1;
+  }
+  Ctx::GraphFrame &gf = c.graph_frame;
+  gf.status_next = c.status_next;
+  gf.status_obj_next = c.status_obj_next;
+  gf.cand_cap = c.async_cand_cap;
+  gf.tiny_cap = c.async_tiny_cap;
+  gf.ent_cap = c.async_ent_cap;
+  gf.obj_fp32 = c.async_obj_fp32;
+  gf.kernel_launches = c.stats.kernel_launches;
+  gf.slabs = c.stats.slabs;
+  gf.cells = c.stats.cells;
+  C3D_CUDA(cudaEventRecord(c.ev0, st));
+  C3D_CUDA(cudaGraphLaunch(c.graph_exec, st));
+  C3D_CUDA(cudaEventRecord(c.ev1, st));
   return 0;
 }
 
+/* the context's graph run again: the frame's work with its final copies of
+   the status words, then the one synchronisation */
+static int replay_graph(Ctx &c, cudaStream_t st) {
+  const Ctx::GraphFrame &gf = c.graph_frame;
+  c.stats = contour3d_gb300_stats_t{};
+  c.stats.kernel_launches = gf.kernel_launches;
+  c.stats.slabs = gf.slabs;
+  c.stats.cells = gf.cells;
+  c.frame_async = true;
+  c.status_next = gf.status_next;
+  c.status_obj_next = gf.status_obj_next;
+  c.async_cand_cap = gf.cand_cap;
+  c.async_tiny_cap = gf.tiny_cap;
+  c.async_ent_cap = gf.ent_cap;
+  c.async_obj_fp32 = gf.obj_fp32;
+  C3D_CUDA(cudaEventRecord(c.ev0, st));
+  C3D_CUDA(cudaGraphLaunch(c.graph_exec, st));
+  C3D_CUDA(cudaEventRecord(c.ev1, st));
+  C3D_CUDA(cudaStreamSynchronize(st));
+  C3D_CUDA(cudaGetLastError());
+  return frame_status(c, true);
+}
+
+/*
+ * One frame.  The first frame of a context synchronises after every slab
+ * pass and learns the counts; later frames run unsynchronised, sized from
+ * them, and are rendered again with synchronisation if they find more work.
+ * An unsynchronised device frame whose description repeats is recorded as a
+ * CUDA graph the second time and launched as one from the third on (an
+ * in-situ solver's time steps: the same fields, levels and camera, new field
+ * values).
+ */
 static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
+  const bool async = c.async_enabled && c.caps_known && !o.sink && !c.stage_timing;
+  int rc = -1;
+  bool redone = false, replayed = false, recorded = false;
+  if (async && graph_eligible(c, f, o)) {
+    const uint64_t key = frame_key(f, o);
+    if (c.graph_exec && c.graph_key == key) {
+      rc = replay_graph(c, f.stream);
+      replayed = true;
+    } else if (c.graph_key_seen && c.graph_key == key) {
+      C3D_CUDA(cudaEventSynchronize(c.ev_staged));
+      if (cudaStreamBeginCapture(f.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        c.capturing = true;
+        t_capture_needs_growth = false;
+        rc = render_frame_pass(c, f, o, true);
+        if (c.capturing) {
+          /* the recording stopped short (a buffer had to grow, or an error):
+             abandon it and render the frame without it */
+          c.capturing = false;
+          cudaGraph_t g = nullptr;
+          cudaStreamEndCapture(f.stream, &g);
+          if (g) cudaGraphDestroy(g);
+          cudaGetLastError();
+          drop_graph(c);
+          rc = -1;
+        } else {
+          recorded = rc != 1;
+        }
+      } else {
+        cudaGetLastError();
+      }
+    } else {
+      drop_graph(c);
+      c.graph_key = key;
+      c.graph_key_seen = true;
+    }
+  }
+  if (rc == -1) rc = render_frame_pass(c, f, o, async);
+  if (rc == kFrameRedo) {
+    /* the graph (if any) was sized for less work than this frame has */
+    drop_graph(c);
+    c.graph_key_seen = false;
+    rc = render_frame_pass(c, f, o, false);
+    redone = true;
+  }
+  if (rc == 0 && !o.sink) c.caps_known = true;
+  c.stats.unsynchronised = async && !redone ? 1 : 0;
+  c.stats.redone = redone ? 1 : 0;
+  c.stats.graph = replayed && !redone ? 2 : (recorded && !redone ? 1 : 0);
+  return rc;
+}
+
+/* after a frame's final synchronisation: its error words, and for an
+   unsynchronised frame the counts of every pass (statistics, the sizes later
+   frames use, and whether the frame must be rendered again) */
+static int frame_status(Ctx &c, bool async) {
+  const unsigned *h_checks = c.h_small.as<unsigned>() + 32;
+  const unsigned long long *hs = c.h_status.as<unsigned long long>();
+  const size_t obj0 = kStatusHead + (size_t)kSlabRec * kStatusSlabs;
+  if (h_checks[kZbufErrWord]) {
+    log_error("a z-buffer update gave up after its retry bound (error flags 0x%x)", h_checks[kZbufErrWord]);
+    return 1;
+  }
+  if (async) {
+    if (h_checks[kClsErrWord]) {
+      log_error("device classification did not complete (error flags 0x%x)", h_checks[kClsErrWord]);
+      return 1;
+    }
+    /* the counts of every pass: statistics, and the sizes the next frames use */
+    bool over = h_checks[kOvfWord] != 0;
+    for (int q = 0; q < c.status_next; q++) {
+      const unsigned long long *r = hs + kStatusHead + (size_t)kSlabRec * q, *cnt = r + 2;
+      c.stats.triangles += r[0];
+      c.stats.vertices += r[1];
+      c.stats.candidates += cnt[0];
+      c.stats.tiny += cnt[1];
+      c.stats.cover_triangles += cnt[4];
+      c.stats.exact_fragments += cnt[5];
+      c.stats.slivers += cnt[6];
+      over = over || cnt[0] > c.async_cand_cap || cnt[1] > c.async_tiny_cap;
+      c.caps.T = std::max(c.caps.T, r[0]);
+      c.caps.V = std::max(c.caps.V, r[1]);
+      c.caps.cand = std::max(c.caps.cand, cnt[0] + cnt[0] / 4);
+      c.caps.tiny = std::max(c.caps.tiny, cnt[1] + cnt[1] / 4);
+    }
+    for (int q = 0; q < c.status_obj_next; q++) {
+      const unsigned long long *r = hs + obj0 + 3 * (size_t)q;
+      c.stats.winners += r[0];
+      c.stats.shade_exact += c.async_obj_fp32[(size_t)q] ? r[1] : r[0];
+      c.stats.normals += r[2];
+      over = over || r[2] > c.async_ent_cap;
+      c.caps.ent = std::max(c.caps.ent, r[2] + r[2] / 4);
+    }
+    if (over) return kFrameRedo;
+  }
+  c.stats.ms_total = elapsed(c.ev0, c.ev1);
+  for (int q = 0; q < 5; q++) c.stats.filter_violations[q] = h_checks[q];
+  c.stats.shade_violations = h_checks[5];
+  return 0;
+}
+
+static int render_frame_pass(Ctx &c, const FrameIn &f, const FrameOut &o, bool async) {
   const HostScene &s = f.scene;
   const size_t W = s.W, H = s.H, npx = W * H;
   if (W == 0 || H == 0) {
@@ -1208,63 +1631,69 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     return 1;
   }
   c.stats = contour3d_gb300_stats_t{};
+  c.frame_async = async;
+  c.status_next = c.status_obj_next = 0;
+  c.async_cand_cap = c.async_tiny_cap = c.async_ent_cap = ~0ULL;
+  c.async_obj_fp32.clear();
   c.field_src = nullptr;
   c.field_bytes = 0;
   c.stats_h2d = 0;
   cudaStream_t st = f.stream;
-  C3D_CUDA(cudaEventRecord(c.ev0, st));
+  const std::vector<std::pair<size_t, size_t>> groups = field_groups(f, o.sink != nullptr);
+  std::vector<LineSegDev> segs;
+  if (build_line_segs(f, segs)) return 1;
+  if (!c.capturing) C3D_CUDA(cudaEventRecord(c.ev0, st));
   const SceneDev sd = scene_dev(s);
-  /* pixel centres (render.c:100-104), staged through pinned memory */
-  C3D_CUDA(cudaEventSynchronize(c.ev_staged));
-  if (c.h_grids.ensure(sizeof(double) * (W + H) + sizeof(float) * (W + H))) return 1;
-  double *xy = c.h_grids.as<double>();
-  float *xyf = reinterpret_cast<float *>(xy + W + H);
-  for (size_t i = 0; i < W; i++) xy[i] = 1. * (i + 0.5) / W - 0.5;
-  for (size_t j = 0; j < H; j++) xy[W + j] = 1. * (j + 0.5) / H - 0.5;
-  for (size_t q = 0; q < W + H; q++) xyf[q] = (float)xy[q];
-  if (c.xy.ensure(sizeof(double) * (W + H), st) || c.xyf.ensure(sizeof(float) * (W + H), st) ||
-      c.canvas.ensure(sizeof(Slot) * npx, st) || c.zlo.ensure(sizeof(unsigned) * npx, st) || c.checks.ensure(64, st))
+  FrameConsts fc;
+  if (stage_frame_consts(c, f, groups, segs, fc)) return 1;
+  if (c.canvas.ensure(sizeof(Slot) * npx, st) || c.zlo.ensure(sizeof(unsigned) * npx, st) || c.checks.ensure(64, st))
     return 1;
   /* per-pixel winner weights: tags carry a frame epoch, so the buffer is
      cleared only when it is new or the epoch wraps */
   const void *winfo_before = c.winfo.p;
   if (c.winfo.ensure(3 * sizeof(ulonglong2) * npx, st)) return 1;
-  if (c.winfo.p != winfo_before || ++c.epoch >= (1ULL << 24)) {
+  if (c.winfo.p != winfo_before || ++c.epoch >= (1ULL << 24) || c.capturing) {
+    /* a recorded frame runs many times with one epoch: it clears the weights */
     C3D_CUDA(cudaMemsetAsync(c.winfo.p, 0, c.winfo.cap, st));
-    c.epoch = 1;
+    if (!c.capturing) c.epoch = 1;
   }
-  C3D_CUDA(cudaMemcpyAsync(c.xy.p, xy, sizeof(double) * (W + H), cudaMemcpyHostToDevice, st));
-  C3D_CUDA(cudaMemcpyAsync(c.xyf.p, xyf, sizeof(float) * (W + H), cudaMemcpyHostToDevice, st));
-  C3D_CUDA(cudaEventRecord(c.ev_staged, st));
-  /* the self-check counters (words 0-5) and the z-buffer error word */
+  /* the self-check counters (words 0-5), the z-buffer, overflow and
+     classification error words */
   C3D_CUDA(cudaMemsetAsync(c.checks.p, 0, 64, st));
+  if (async) {
+    if (c.status.ensure(sizeof(unsigned long long) * kStatusWords, st) ||
+        c.h_status.ensure(sizeof(unsigned long long) * kStatusWords))
+      return 1;
+    C3D_CUDA(cudaMemsetAsync(c.status.p, 0, sizeof(unsigned long long) * kStatusWords, st));
+  }
   RasterDev R = {};
   R.zerr = c.checks.as<unsigned>() + kZbufErrWord;
   R.canvas = c.canvas.as<Slot>();
   R.zlo = c.zlo.as<unsigned>();
   R.winfo = c.winfo.as<ulonglong2>();
   R.epoch = c.epoch;
-  R.xs = c.xy.as<double>();
+  R.xs = fc.xy;
   R.ys = R.xs + W;
-  R.xsf = c.xyf.as<float>();
+  R.xsf = fc.xyf;
   R.ysf = R.xsf + W;
   /* canvas: background colour at depth -DBL_MAX (main.c:90-103); depth floors at -inf */
   const unsigned bg = ((unsigned)f.bg.r << 16) | ((unsigned)f.bg.g << 8) | f.bg.b;
   launch_canvas_init(c.canvas.as<Slot>(), R.zlo, (long long)npx, h_depth_key(-1. * DBL_MAX), bg, st);
   c.stats.kernel_launches += 1;
   unsigned long long order_base = 1;
-  for (size_t n = 0; n < f.contours.size();) {
-    size_t m = n + 1;
-    /* inspection reports every object's triangles in turn: one object at a time */
-    if (!o.sink)
-      while (m < f.contours.size() && same_field(f.contours[n], f.contours[m])) m++;
-    if (render_contour(c, f, sd, &f.contours[n], m - n, order_base, R, o.sink)) {
-      log_error("contour processing failed");
+  for (size_t g = 0; g < groups.size(); g++) {
+    if (render_contour(c, f, sd, &f.contours[groups[g].first], groups[g].second - groups[g].first, order_base, R,
+                       o.sink, fc.groups[g])) {
+      if (!(c.capturing && t_capture_needs_growth)) log_error("contour processing failed");
       return 1;
     }
-    n = m;
   }
-  if (render_lines(c, f, order_base)) return 1;
+  /* the lines after every contour object (line.c:121-170): pixels on the device */
+  if (fc.nseg > 0) {
+    launch_lines(fc.segs, fc.nseg, (long long)W, (long long)H, c.canvas.as<Slot>(), order_base, R.zerr, st);
+    c.stats.kernel_launches += 1;
+    order_base += (unsigned long long)fc.nseg;
+  }
   /* resolve */
   uint8_t *rgb_dev = o.rgb_dev;
   const bool want_rgb = o.rgb_host || o.rgb_pinned;
@@ -1284,18 +1713,27 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     if (c.h_slots.ensure(sizeof(Slot) * npx)) return 1;
     C3D_CUDA(cudaMemcpyAsync(c.h_slots.p, c.canvas.p, sizeof(Slot) * npx, cudaMemcpyDeviceToHost, st));
   }
-  C3D_CUDA(cudaEventRecord(c.ev1, st));
+  if (!c.capturing) C3D_CUDA(cudaEventRecord(c.ev1, st));
   unsigned *h_checks = c.h_small.as<unsigned>() + 32;
   C3D_CUDA(cudaMemcpyAsync(h_checks, c.checks.p, 16 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  unsigned long long *hs = c.h_status.as<unsigned long long>();
+  const size_t obj0 = kStatusHead + (size_t)kSlabRec * kStatusSlabs;
+  if (async) {
+    C3D_CUDA(cudaMemcpyAsync(hs, c.status.p, sizeof(unsigned long long) * (kStatusHead + kSlabRec * c.status_next),
+                             cudaMemcpyDeviceToHost, st));
+    C3D_CUDA(cudaMemcpyAsync(hs + obj0, c.status.as<unsigned long long>() + obj0,
+                             sizeof(unsigned long long) * 3 * c.status_obj_next, cudaMemcpyDeviceToHost, st));
+  }
+  if (c.capturing) {
+    /* the frame's work is recorded, not run: instantiate it and run it */
+    if (end_capture_and_launch(c, st)) return 1;
+  }
   C3D_CUDA(cudaStreamSynchronize(st));
   C3D_CUDA(cudaGetLastError());
-  if (h_checks[kZbufErrWord]) {
-    log_error("a z-buffer update gave up after its retry bound (error flags 0x%x)", h_checks[kZbufErrWord]);
-    return 1;
+  {
+    const int rs = frame_status(c, async);
+    if (rs) return rs;
   }
-  c.stats.ms_total = elapsed(c.ev0, c.ev1);
-  for (int q = 0; q < 5; q++) c.stats.filter_violations[q] = h_checks[q];
-  c.stats.shade_violations = h_checks[5];
   if (o.rgb_host) memcpy(o.rgb_host, c.h_rgb.p, 3 * npx);
   if (o.depth_host || o.pixels_host) {
     const Slot *sl = c.h_slots.as<Slot>();
@@ -1588,6 +2026,22 @@ extern "C" int contour3d_gb300_set_filter_check(int on) {
   return 0;
 }
 
+extern "C" int contour3d_gb300_set_async(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_ctx.async_enabled = on != 0;
+  return 0;
+}
+
+extern "C" int contour3d_gb300_set_graphs(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_ctx.graphs_enabled = on != 0;
+  if (!on) {
+    drop_graph(g_ctx);
+    g_ctx.graph_key_seen = false;
+  }
+  return 0;
+}
+
 extern "C" int contour3d_gb300_set_slab_cells(uint64_t max_cells) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (max_cells < 64) {
@@ -1618,7 +2072,9 @@ extern "C" long contour3d_gb300_debug_triangles(const contour3d_contour_obj_t *o
   const SceneDev sd = scene_dev(f.scene);
   unsigned long long order = 1;
   RasterDev R = {};
-  if (render_contour(g_ctx, f, sd, &f.contours[0], 1, order, R, &sink)) return -1;
+  FrameConsts fc;
+  if (stage_frame_consts(g_ctx, f, field_groups(f, true), {}, fc)) return -1;
+  if (render_contour(g_ctx, f, sd, &f.contours[0], 1, order, R, &sink, fc.groups[0])) return -1;
   if (num_triangulated) *num_triangulated = sink.triangulated;
   return sink.count;
 }
@@ -1689,9 +2145,9 @@ extern "C" int contour3d_gb300_release(void) {
 /* every device buffer of a context; the constant table (lut) first */
 static std::vector<Buf *> ctx_bufs(Ctx &c) {
   return {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-          &c.field, &c.grids, &c.nodes, &c.canvas, &c.xy, &c.rgb, &c.segs, &c.zlo, &c.xyf, &c.cand, &c.live,
+          &c.field, &c.consts, &c.nodes, &c.canvas, &c.rgb, &c.zlo, &c.cand, &c.live,
           &c.tiny, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.voffsets, &c.verts, &c.winfo, &c.amb,
-          &c.shade_check, &c.checks};
+          &c.shade_check, &c.checks, &c.status};
 }
 
 static void ctx_release(Ctx &c) {
@@ -1702,7 +2158,8 @@ static void ctx_release(Ctx &c) {
   c.h_small.release();
   c.h_rgb.release();
   c.h_slots.release();
-  c.h_grids.release();
+  c.h_consts.release();
+  c.h_status.release();
   if (c.ready) {
     cudaStreamDestroy(c.own_stream);
     cudaEventDestroy(c.ev0);
@@ -1717,6 +2174,11 @@ static void ctx_release(Ctx &c) {
   }
   c.ready = false;
   c.device = -1;
+  /* the sizes learnt for unsynchronised frames and the recorded frame go with the buffers */
+  c.caps = Ctx::Caps();
+  c.caps_known = false;
+  drop_graph(c);
+  c.graph_key_seen = false;
 }
 
 /* ------------------------------------------------------------------ */

@@ -28,7 +28,8 @@ class Stats(C.Structure):
                 ("ms_shade", C.c_double), ("filter_violations", C.c_uint64 * 5),
                 ("cover_triangles", C.c_uint64), ("exact_fragments", C.c_uint64), ("slivers", C.c_uint64),
                 ("vertices", C.c_uint64), ("ms_vertices", C.c_double), ("ms_normals", C.c_double),
-                ("shade_exact", C.c_uint64), ("shade_violations", C.c_uint64)]
+                ("shade_exact", C.c_uint64), ("shade_violations", C.c_uint64), ("unsynchronised", C.c_uint64),
+                ("redone", C.c_uint64), ("graph", C.c_uint64)]
 
 
 class Field(C.Structure):
@@ -110,6 +111,7 @@ EXPORTS = [
     "contour3d_execute", "contour3d_gb300_identity", "contour3d_gb300_declare_identity",
     "contour3d_gb300_render", "contour3d_gb300_render_device", "contour3d_gb300_last_stats",
     "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells", "contour3d_gb300_set_filter_check",
+    "contour3d_gb300_set_async", "contour3d_gb300_set_graphs",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
     "contour3d_gb300_cell_offsets_noalloc", "contour3d_gb300_render_batch", "contour3d_gb300_server_create",
@@ -255,6 +257,12 @@ class Library:
 
     def set_filter_check(self, on: bool) -> None:
         self.lib.contour3d_gb300_set_filter_check(1 if on else 0)
+
+    def set_async(self, on: bool) -> None:
+        self.lib.contour3d_gb300_set_async(1 if on else 0)
+
+    def set_graphs(self, on: bool) -> None:
+        self.lib.contour3d_gb300_set_graphs(1 if on else 0)
 
     def set_slab_cells(self, n: int) -> int:
         return self.lib.contour3d_gb300_set_slab_cells(C.c_uint64(n))

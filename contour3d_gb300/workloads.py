@@ -71,13 +71,15 @@ def quantile_levels(dev_field, rng, count, lo=0.3, hi=0.7, samples=200_000):
     return [float(np.quantile(vals, q)) for q in qs]
 
 
-def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=2024, host=False):
+def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=2024, host=False, twins=False):
     """Fields and frame specs of the batched workload: device tensors, or with
     host=True the same values as numpy arrays generated on the host cores
-    (no GPU needed; `lib` is then unused)."""
+    (no GPU needed; `lib` is then unused).  With twins=True (device only) a
+    third result maps the index of every float32 field to the float64 field
+    it was made from (the same seed in double precision)."""
     from . import fields as hostgen
     rng = np.random.default_rng(seed)
-    fields, frames = [], []
+    fields, frames, twin = [], [], {}
     for n in range(nfields):
         shape = tuple(int(x) for x in rng.integers(nmin, nmax + 1, size=3))
         dtype = "f64" if n % 2 == 0 else "f32"
@@ -89,7 +91,10 @@ def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=
                 f = f.astype(np.float32) if dtype == "f32" else f
             else:
                 f = blobs_device(lib, shape, nb, seed=1000 + n)
-                f = f.float() if dtype == "f32" else f
+                if dtype == "f32":
+                    if twins:
+                        twin[n] = f
+                    f = f.float()
         else:
             if host:
                 f, _ = hostgen.modes_threaded(shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=2000 + n,
@@ -98,11 +103,14 @@ def batch_set(lib, nfields=64, nmin=64, nmax=384, width=1024, height=1024, seed=
                 import torch
                 f, _ = modes_device(lib, shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0, seed=2000 + n,
                                     dtype=torch.float64 if dtype == "f64" else torch.float32)
+                if twins and dtype == "f32":
+                    twin[n], _ = modes_device(lib, shape, nmodes=64, kmin=1, kmax=16, power=5.0 / 6.0,
+                                              seed=2000 + n, dtype=torch.float64)
         fields.append(f)
         nlev = int(rng.integers(1, 5))
         levels = quantile_levels(f, rng, nlev)
         frames.append(FrameSpec(n, levels, PALETTE[:nlev], random_camera(rng), width, height))
-    return fields, frames
+    return (fields, frames, twin) if twins else (fields, frames)
 
 
 SERVED_SHAPES = [(96, 96, 96), (192, 192, 192), (512, 256, 256), (384, 384, 384), (768, 768, 768)]

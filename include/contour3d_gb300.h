@@ -222,6 +222,10 @@ typedef struct {
                                  (ms_shade is then the FP64 shading pass) */
   uint64_t shade_exact;       /* won pixels whose colour the FP32 shading could not settle (shaded in FP64) */
   uint64_t shade_violations;  /* self-check: FP32 colours that differ from the FP64 ones (must stay 0) */
+  uint64_t unsynchronised;    /* 1: the frame ran with one host synchronisation, at its end */
+  uint64_t redone;            /* 1: an unsynchronised pass found more work than its buffers held, and
+                                 the frame was rendered again with synchronisation */
+  uint64_t graph;             /* 1: the frame was recorded as a CUDA graph, 2: it ran as the recorded graph */
 } contour3d_gb300_stats_t;
 
 int contour3d_gb300_last_stats(contour3d_gb300_stats_t *out);
@@ -233,6 +237,27 @@ int contour3d_gb300_set_stage_timing(int on);
  * certified bounds (slow; for tests), 0 = off (default)
  */
 int contour3d_gb300_set_filter_check(int on);
+/*
+ * 1 (default) = a frame of a context that has completed one frame runs with
+ * one host synchronisation, at its end: its buffers are sized from the
+ * largest counts the context has seen, every pass's counts stay on the device
+ * until the end, and a frame that finds more work than the buffers hold is
+ * rendered again with synchronisation (which learns the larger counts);
+ * 0 = synchronise after every slab's scan and raster pass and size every
+ * buffer from the counts just read.  The image is the same either way.
+ */
+int contour3d_gb300_set_async(int on);
+/*
+ * 1 (default) = an unsynchronised frame drawn from device-resident fields
+ * into device memory, on a stream other than the legacy default stream, is
+ * recorded as a CUDA graph the second time in a row that a frame with the
+ * same description comes (fields' addresses, types, sizes, grids and levels,
+ * scene, lines, output and stream), and from the third time on the graph is
+ * launched instead of the frame's individual calls; the field values may
+ * change between frames (an in-situ solver's time steps).  A frame that finds
+ * more work than the recorded sizes drops the graph.  0 = no graphs.
+ */
+int contour3d_gb300_set_graphs(int on);
 /* upper bound on cells per slab (default and maximum 178,956,970, the most the
    scan's packed 32-bit sums allow); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);
