@@ -102,6 +102,22 @@ __device__ __forceinline__ bool abs_lt_1e8(double x) {
  * reference's sequential z-test "dist0 < depth => skip" (render.c:120-125,
  * line.c:109-115), in which the LAST fragment of maximal depth wins.
  */
+/*
+ * Programmatic dependent launch.  A kernel launched with the programmatic
+ * stream serialisation attribute may be scheduled while the kernel before it
+ * on the stream is still finishing; pdl_wait() returns once that kernel has
+ * completed and its memory is visible, so everything that reads (or
+ * overwrites) what earlier work produced comes after it.  pdl_trigger() lets
+ * the next kernel be scheduled once every block of this one has started.
+ * Both are no-ops for a kernel launched without the attribute.
+ */
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() {
+  pdl_trigger();
+  pdl_wait();
+}
+
 struct __align__(16) Slot {
   unsigned long long lo, hi;
 };

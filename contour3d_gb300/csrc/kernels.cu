@@ -214,6 +214,7 @@ __device__ __forceinline__ bool node_above_thr(const ThrSet& ts, int t, int b) {
 
 template <typename T>
 __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ codes) {
+  pdl_enter();
   __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
   const T* f = static_cast<const T*>(F.data);
   const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
@@ -312,6 +313,7 @@ template <typename T, int NT>
 __global__ void __launch_bounds__(kClsX)
 k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, ThrSet ts, CodeOut out,
                unsigned* __restrict__ err) {
+  pdl_enter();
   static_assert(kClsX % 32 == 0 && kClsY + 1 <= 32, "classify tile: whole warps, a column of rows in one warp");
   using B = typename NodeBits<T>::type;
   constexpr int BX = TmaBox<T>::kX;
@@ -457,6 +459,7 @@ __device__ __forceinline__ void load_scan_codes(const unsigned char* __restrict_
 /* one block per segment: its packed total */
 __global__ void __launch_bounds__(kScanThreads)
 k_seg_reduce(const unsigned char* __restrict__ codes, long long n, unsigned long long* __restrict__ seg_sums) {
+  pdl_enter();
   __shared__ unsigned s_cnt[256];
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   unsigned wv[kScanItems / 4];
@@ -485,6 +488,7 @@ __global__ void __launch_bounds__(kSegScanThreads)
 k_seg_scan(const unsigned long long* __restrict__ seg_sums, long long nseg, unsigned long long* __restrict__ seg_base,
            long long n, unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
            unsigned long long* __restrict__ totals) {
+  pdl_enter();
   __shared__ unsigned long long s_warp[kSegScanThreads / 32];
   const long long per = (nseg + kSegScanThreads - 1) / kSegScanThreads;
   const long long a = min(nseg, (long long)threadIdx.x * per), b = min(nseg, a + per);
@@ -547,6 +551,7 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
              unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
              const unsigned long long* __restrict__ totals, unsigned* __restrict__ tri_cell,
              unsigned long long tri_cap, int want_offsets, unsigned* __restrict__ ovf) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char scan_smem[];
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ unsigned s_cnt[256];
@@ -662,6 +667,7 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
 /* triangle -> cell map from the offsets: tri_cell[offsets[c] + r] = c | r << 28 */
 __global__ void __launch_bounds__(256)
 k_fill_tri_cell(const unsigned* __restrict__ offsets, long long n, unsigned* __restrict__ tri_cell) {
+  pdl_enter();
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x) {
     const unsigned a = offsets[c], b = offsets[c + 1];
@@ -1008,6 +1014,7 @@ __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], co
 
 /* inspection: every triangle's exact vertices, face normal, area and weighted normal */
 __global__ void __launch_bounds__(256) k_exact_all(Geo G, const unsigned long long* __restrict__ total_p, TriDev tri) {
+  pdl_enter();
   const long long T_ = (long long)*total_p;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
        t += (long long)gridDim.x * blockDim.x) {
@@ -1064,6 +1071,7 @@ __device__ __forceinline__ d3 vertex_normal(long long c, int e, long long ncx, l
 __global__ void __launch_bounds__(256)
 k_normals(FieldDev F, SlabDev S, const unsigned* __restrict__ offsets, const unsigned* __restrict__ tri_cell,
           const unsigned long long* __restrict__ total_p, TriDev tri) {
+  pdl_enter();
   const long long T_ = (long long)*total_p;
   const long long ncx = F.nx - 1, ncy = F.ny - 1;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < T_;
@@ -1315,6 +1323,7 @@ template <typename T>
 __global__ void __launch_bounds__(kVThreads)
 k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restrict__ codes,
            const unsigned* __restrict__ voffsets, long long n, VertDev V) {
+  pdl_enter();
   __shared__ unsigned short list[kVTile * 7];
   const long long c0 = (long long)blockIdx.x * kVTile;
   if (c0 >= n) return;
@@ -1521,10 +1530,12 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
        const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
        const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R, VertDev V,
        unsigned* __restrict__ checks) {
+  pdl_trigger(); /* the shared-memory table below does not depend on the preceding kernel */
   (void)offsets;
   __shared__ unsigned long long lut[kLutEntries];
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
+  pdl_wait();
   const long long T_ = (long long)*total_p;
   if ((unsigned long long)T_ > tri.cap) {
     /* more triangles than the arrays hold (sized before the count was known) */
@@ -1662,6 +1673,7 @@ __device__ __forceinline__ void write_candidates(const RasterDev& R, unsigned lo
 template <bool CHECK>
 __global__ void __launch_bounds__(256, 4)
 k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
+  pdl_enter();
   const long long n = (long long)*R.cover_count;
   const long long W = scene.width, H = scene.height;
   /* traverse front to back along z (the list is close to emission order,
@@ -1907,6 +1919,7 @@ __device__ __forceinline__ bool screen_edges(const Geo& G, const SceneDev& s, un
 template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256, 4)
 k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
+  pdl_enter();
   const long long n = (long long)*R.sliver_count;
   const long long W = scene.width, H = scene.height;
   for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
@@ -2015,6 +2028,7 @@ k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
 template <bool CHECK>
 __global__ void __launch_bounds__(256)
 k_tiny(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
+  pdl_enter();
   const unsigned long long n = min(*R.tiny_count, R.tiny_cap);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x)
@@ -2030,6 +2044,7 @@ k_tiny(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsign
  * so k_exact runs only over fragments that can still win.
  */
 __global__ void __launch_bounds__(256) k_prune(RasterDev R) {
+  pdl_enter();
   const unsigned long long n = min(*R.cand_count, R.cand_cap);
   for (unsigned long long base = blockIdx.x * (unsigned long long)blockDim.x; base < n;
        base += (unsigned long long)gridDim.x * blockDim.x) {
@@ -2047,6 +2062,7 @@ __global__ void __launch_bounds__(256) k_prune(RasterDev R) {
 }
 
 __global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base) {
+  pdl_enter();
   const unsigned long long n = *R.live_count;
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
        q += (unsigned long long)gridDim.x * blockDim.x) {
@@ -2105,6 +2121,7 @@ __device__ __forceinline__ bool winner_cell(const FieldDev& F, unsigned long lon
 __global__ void __launch_bounds__(256)
 k_winners(const Slot* __restrict__ canvas, long long npx, unsigned long long obase, unsigned long long span,
           unsigned* __restrict__ win, unsigned long long* __restrict__ win_count) {
+  pdl_enter();
   for (long long base = blockIdx.x * (long long)blockDim.x; base < npx; base += (long long)gridDim.x * blockDim.x) {
     const long long p = base + threadIdx.x;
     bool won = false;
@@ -2305,6 +2322,7 @@ template <typename T, bool CHECK>
 __global__ void __launch_bounds__(256)
 k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __restrict__ lut,
           unsigned long long obase, unsigned rgb_in) {
+  pdl_enter();
   __shared__ unsigned long long keys[kShadeHash];
   __shared__ float4 wnf[kShadeHash];
   __shared__ unsigned short lists[kShadeList][256];
@@ -2465,9 +2483,11 @@ __global__ void __launch_bounds__(256)
 k_nb_list(FieldDev F, RasterDev R, const unsigned long long* __restrict__ lut_g, const unsigned* __restrict__ pixels,
           const unsigned long long* __restrict__ count, unsigned long long obase, unsigned long long* __restrict__ ent,
           unsigned long long ent_cap, unsigned long long* __restrict__ ent_count, uint2* __restrict__ spans) {
+  pdl_trigger(); /* the shared-memory table below does not depend on the preceding kernel */
   __shared__ unsigned long long lut[kLutEntries];
   for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
   __syncthreads();
+  pdl_wait();
   const unsigned long long n = 3 * *count;
   const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
   /* every lane of a warp runs the same iterations (warp-wide reservations) */
@@ -2516,6 +2536,7 @@ k_nb_list(FieldDev F, RasterDev R, const unsigned long long* __restrict__ lut_g,
 __global__ void __launch_bounds__(256)
 k_nb_wn(FieldDev F, const unsigned long long* __restrict__ lut, const unsigned long long* __restrict__ ent,
         unsigned long long ent_cap, const unsigned long long* __restrict__ ent_count, double* __restrict__ wn_out) {
+  pdl_enter();
   const unsigned long long n = min(*ent_count, ent_cap);
   const unsigned long long ncx = (unsigned long long)(F.nx - 1), ncy = (unsigned long long)(F.ny - 1);
   for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
@@ -2548,6 +2569,7 @@ k_shade(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __res
         const unsigned* __restrict__ pixels, const unsigned long long* __restrict__ count, unsigned long long obase,
         const uint2* __restrict__ spans, const double* __restrict__ wn_in, unsigned rgb_in,
         unsigned* __restrict__ checks) {
+  pdl_enter();
   const unsigned long long n = *count;
   const unsigned lane = threadIdx.x & 31u, m = lane & 3u, g0 = lane & ~3u;
   const long long W = scene.width;
@@ -2627,6 +2649,7 @@ k_shade(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __res
 /* ------------------------------------------------------------------ */
 __global__ void k_lines(const LineSegDev* __restrict__ segs, int nseg, long long W, long long H,
                         Slot* __restrict__ canvas, unsigned long long order_base, unsigned* zerr) {
+  pdl_enter();
   const int sidx = blockIdx.x;
   if (sidx >= nseg) return;
   const LineSegDev L = segs[sidx];
@@ -2661,6 +2684,7 @@ __global__ void k_lines(const LineSegDev* __restrict__ segs, int nseg, long long
 }
 
 __global__ void k_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo) {
+  pdl_enter();
   const unsigned floor_key = f_key(-__int_as_float(0x7f800000));
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     canvas[p].hi = hi;
@@ -2672,6 +2696,7 @@ __global__ void k_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned
 /* ppm body: rows flipped (output.c:113-123); optional canvas-order depth */
 __global__ void k_resolve(const Slot* __restrict__ canvas, long long W, long long H, unsigned char* __restrict__ rgb,
                           double* __restrict__ depth) {
+  pdl_enter();
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < W * H; p += (long long)gridDim.x * blockDim.x) {
     const long long r = p / W, i = p % W;
     const Slot s = canvas[(H - 1 - r) * W + i];
@@ -2700,6 +2725,24 @@ static int num_sms() {
     return v;
   }();
   return n;
+}
+
+/* every kernel launch of the library: programmatic dependent launch (the
+   kernels call pdl_wait() before they touch what earlier work produced) */
+template <typename... KArgs, typename... Args>
+static void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 static int grid_for(long long n, int threads, int per_sm) {
@@ -2785,10 +2828,10 @@ template <typename T>
 static void launch_classify_tma(const CUtensorMap& map, const FieldDev& F, const SlabDev& S, const ThrSet& ts,
                                 const CodeOut& out, unsigned* err, const dim3& grid, cudaStream_t st) {
   switch (ts.n) {
-    case 1: k_classify_tma<T, 1><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
-    case 2: k_classify_tma<T, 2><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
-    case 3: k_classify_tma<T, 3><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
-    default: k_classify_tma<T, 4><<<grid, kClsX, 0, st>>>(map, F, S, ts, out, err); break;
+    case 1: launch_k(k_classify_tma<T, 1>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    case 2: launch_k(k_classify_tma<T, 2>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    case 3: launch_k(k_classify_tma<T, 3>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    default: launch_k(k_classify_tma<T, 4>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
   }
 }
 
@@ -2815,8 +2858,8 @@ int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char*
     return (nf + kMaxThr - 1) / kMaxThr;
   }
   for (int q = 0; q < nf; q++) {
-    if (F.is_f32) k_classify<float><<<grid, kClsX, 0, st>>>(Fs[q], S, codes[q]);
-    else k_classify<double><<<grid, kClsX, 0, st>>>(Fs[q], S, codes[q]);
+    if (F.is_f32) launch_k(k_classify<float>, grid, kClsX, 0, st, Fs[q], S, codes[q]);
+    else launch_k(k_classify<double>, grid, kClsX, 0, st, Fs[q], S, codes[q]);
   }
   return nf;
 }
@@ -2827,23 +2870,22 @@ void launch_scan(const unsigned char* codes, long long n, unsigned long long* se
                  unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
                  unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, unsigned* ovf, cudaStream_t st) {
   const long long nseg = scan_segments(n);
-  if (nseg > 0) k_seg_reduce<<<(unsigned)nseg, kScanThreads, 0, st>>>(codes, n, seg_sums);
-  k_seg_scan<<<1, kSegScanThreads, 0, st>>>(seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
+  if (nseg > 0) launch_k(k_seg_reduce, (unsigned)nseg, kScanThreads, 0, st, codes, n, seg_sums);
+  launch_k(k_seg_scan, 1, kSegScanThreads, 0, st, seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
   if (nseg > 0)
-    k_scan_write<<<(unsigned)nseg, kScanThreads, kScanWriteSmem, st>>>(codes, n, seg_base, offsets, voffsets, totals,
-                                                                       tri_cell, tri_cap, want_offsets ? 1 : 0,
-                                                                       ovf);
+    launch_k(k_scan_write, (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, seg_base, offsets, voffsets,
+             totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf);
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st) {
   const unsigned blocks = (unsigned)((n + kVTile - 1) / kVTile);
-  if (F.is_f32) k_vertices<float><<<blocks, kVThreads, 0, st>>>(F, S, scene, codes, voffsets, n, V);
-  else k_vertices<double><<<blocks, kVThreads, 0, st>>>(F, S, scene, codes, voffsets, n, V);
+  if (F.is_f32) launch_k(k_vertices<float>, blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
+  else launch_k(k_vertices<double>, blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
 }
 
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st) {
-  k_fill_tri_cell<<<grid_for(n, 256, 16), 256, 0, st>>>(offsets, n, tri_cell);
+  launch_k(k_fill_tri_cell, grid_for(n, 256, 16), 256, 0, st, offsets, n, tri_cell);
 }
 
 
@@ -2855,30 +2897,30 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
   const int g = grid_for(tri_bound, 256, 8);
   if (checks) {
     if (F.is_f32)
-      k_emit<float, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R, V,
-                                             checks);
+      launch_k(k_emit<float, true>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+               R, V, checks);
     else
-      k_emit<double, true><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R, V,
-                                              checks);
+      launch_k(k_emit<double, true>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+               R, V, checks);
   } else {
     if (F.is_f32)
-      k_emit<float, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R, V,
-                                              checks);
+      launch_k(k_emit<float, false>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+               R, V, checks);
     else
-      k_emit<double, false><<<g, 256, 0, st>>>(F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri, R,
-                                               V, checks);
+      launch_k(k_emit<double, false>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+               R, V, checks);
   }
 }
 
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
                       cudaStream_t st) {
-  k_exact_all<<<grid_for(tri_bound, 256, 8), 256, 0, st>>>(G, total, tri);
+  launch_k(k_exact_all, grid_for(tri_bound, 256, 8), 256, 0, st, G, total, tri);
 }
 
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
-  k_normals<<<g, 256, 0, st>>>(F, S, offsets, tri_cell, total, tri);
+  launch_k(k_normals, g, 256, 0, st, F, S, offsets, tri_cell, total, tri);
 }
 
 void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
@@ -2887,53 +2929,53 @@ void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long*
   (void)total;
   (void)order_base;
   const int g = grid_for(tri_bound, 256, 8);
-  if (checks) k_cover<true><<<g, 256, 0, st>>>(G, scene, tri, R, checks);
-  else k_cover<false><<<g, 256, 0, st>>>(G, scene, tri, R, checks);
+  if (checks) launch_k(k_cover<true>, g, 256, 0, st, G, scene, tri, R, checks);
+  else launch_k(k_cover<false>, g, 256, 0, st, G, scene, tri, R, checks);
 }
 
 void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
                    unsigned* checks, cudaStream_t st) {
   const int g = grid_for(sliver_bound, 256, 8);
   if (G.F.is_f32) {
-    if (checks) k_sliver<float, true><<<g, 256, 0, st>>>(G, scene, R, checks);
-    else k_sliver<float, false><<<g, 256, 0, st>>>(G, scene, R, checks);
+    if (checks) launch_k(k_sliver<float, true>, g, 256, 0, st, G, scene, R, checks);
+    else launch_k(k_sliver<float, false>, g, 256, 0, st, G, scene, R, checks);
   } else {
-    if (checks) k_sliver<double, true><<<g, 256, 0, st>>>(G, scene, R, checks);
-    else k_sliver<double, false><<<g, 256, 0, st>>>(G, scene, R, checks);
+    if (checks) launch_k(k_sliver<double, true>, g, 256, 0, st, G, scene, R, checks);
+    else launch_k(k_sliver<double, false>, g, 256, 0, st, G, scene, R, checks);
   }
 }
 
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
                  unsigned long long order_base, unsigned* checks, cudaStream_t st) {
   const int g = grid_for(tiny_bound, 256, 8);
-  if (checks) k_tiny<true><<<g, 256, 0, st>>>(G, scene, R, order_base, checks);
-  else k_tiny<false><<<g, 256, 0, st>>>(G, scene, R, order_base, checks);
+  if (checks) launch_k(k_tiny<true>, g, 256, 0, st, G, scene, R, order_base, checks);
+  else launch_k(k_tiny<false>, g, 256, 0, st, G, scene, R, order_base, checks);
 }
 
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st) {
-  k_prune<<<grid_for(cand_bound, 256, 8), 256, 0, st>>>(R);
+  launch_k(k_prune, grid_for(cand_bound, 256, 8), 256, 0, st, R);
 }
 
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
                   unsigned long long order_base, cudaStream_t st) {
-  k_exact<<<grid_for(cand_bound, 256, 8), 256, 0, st>>>(G, scene, R, order_base);
+  launch_k(k_exact, grid_for(cand_bound, 256, 8), 256, 0, st, G, scene, R, order_base);
 }
 
 void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,
                     unsigned long long obase, unsigned rgb, cudaStream_t st) {
   const long long npx = scene.width * scene.height;
   const unsigned long long span = 12ULL * (unsigned long long)((F.nx - 1) * (F.ny - 1) * (F.nz - 1));
-  k_winners<<<grid_for(npx, 256, 8), 256, 0, st>>>(R.canvas, npx, obase, span, R.win, R.win_count);
+  launch_k(k_winners, grid_for(npx, 256, 8), 256, 0, st, R.canvas, npx, obase, span, R.win, R.win_count);
   /* no single-precision shading without node spacings (a converter) or for
      axes of 2^20 nodes and more (hash keys): every pixel to the FP64 pass */
   if (!F.dgx || F.nx > (1 << 20) || F.ny > (1 << 20) || F.nz > (1 << 20)) return;
   const int gs = grid_for(4 * npx, 256, 8); /* four threads per pixel */
   if (F.is_f32) {
-    if (R.shade_check) k_shade_f<float, true><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
-    else k_shade_f<float, false><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
+    if (R.shade_check) launch_k(k_shade_f<float, true>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    else launch_k(k_shade_f<float, false>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
   } else {
-    if (R.shade_check) k_shade_f<double, true><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
-    else k_shade_f<double, false><<<gs, 256, 0, st>>>(F, scene, R, lut, obase, rgb);
+    if (R.shade_check) launch_k(k_shade_f<double, true>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    else launch_k(k_shade_f<double, false>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
   }
 }
 
@@ -2943,29 +2985,29 @@ void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDe
                         unsigned long long* ent_count, uint2* spans, double* wn, unsigned rgb, unsigned* checks,
                         cudaStream_t st) {
   if (npix <= 0) return;
-  k_nb_list<<<grid_for(3 * npix, 256, 8), 256, 0, st>>>(F, R, lut, pixels, count, obase, ent, ent_cap, ent_count,
-                                                       spans);
-  k_nb_wn<<<grid_for((long long)ent_cap, 256, 8), 256, 0, st>>>(F, lut, ent, ent_cap, ent_count, wn);
+  launch_k(k_nb_list, grid_for(3 * npix, 256, 8), 256, 0, st, F, R, lut, pixels, count, obase, ent, ent_cap,
+           ent_count, spans);
+  launch_k(k_nb_wn, grid_for((long long)ent_cap, 256, 8), 256, 0, st, F, lut, ent, ent_cap, ent_count, wn);
   const int gs = grid_for(4 * npix, 256, 8);
   if (checks && R.shade_check)
-    k_shade<true><<<gs, 256, 0, st>>>(F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
+    launch_k(k_shade<true>, gs, 256, 0, st, F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
   else
-    k_shade<false><<<gs, 256, 0, st>>>(F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
+    launch_k(k_shade<false>, gs, 256, 0, st, F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, unsigned* zerr, cudaStream_t st) {
-  if (nseg > 0) k_lines<<<nseg, 128, 0, st>>>(segs, nseg, W, H, canvas, order_base, zerr);
+  if (nseg > 0) launch_k(k_lines, nseg, 128, 0, st, segs, nseg, W, H, canvas, order_base, zerr);
 }
 
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,
                         cudaStream_t st) {
-  k_canvas_init<<<grid_for(n, 256, 8), 256, 0, st>>>(canvas, zlo, n, hi, lo);
+  launch_k(k_canvas_init, grid_for(n, 256, 8), 256, 0, st, canvas, zlo, n, hi, lo);
 }
 
 void launch_resolve(const Slot* canvas, long long W, long long H, unsigned char* rgb, double* depth,
                     cudaStream_t st) {
-  k_resolve<<<grid_for(W * H, 256, 8), 256, 0, st>>>(canvas, W, H, rgb, depth);
+  launch_k(k_resolve, grid_for(W * H, 256, 8), 256, 0, st, canvas, W, H, rgb, depth);
 }
 
 }  // namespace c3d
