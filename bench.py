@@ -336,20 +336,27 @@ def run_served(gpu, slots, rates, nreq, budget_gb=120.0, seed=99):
     from contour3d_gb300 import workloads
     rng = np.random.default_rng(seed)
     resident = []
+    solver = torch.cuda.Stream()
+    # the solver stand-in computes its fields in single precision (a double
+    # field stores the widened sums): an update of the 768^3 double field
+    # then costs milliseconds, not the ~0.2 s of a double-precision
+    # evaluation on this GPU's FP64 rate, so the stream measures rendering
     for shp in workloads.SERVED_SHAPES:
         for dt in (torch.float32, torch.float64):
-            f, std = workloads.modes_device(gpu, shp, nmodes=32, kmin=1, kmax=12, seed=len(resident) + 300, dtype=dt)
+            f = torch.empty(shp, dtype=dt, device="cuda")
+            std = gpu.fieldgen_modes_device_async(f.data_ptr(), 1 if dt == torch.float32 else 2, shp, 32, 1, 12,
+                                                  5.0 / 6.0, len(resident) + 300, 0.0, solver.cuda_stream)
             resident.append({"t": f, "std": std, "time": 0.0, "seed": len(resident) + 300, "busy": []})
+    solver.synchronize()
     resident_bytes = sum(r["t"].numel() * r["t"].element_size() for r in resident)
     out = {"workload": "Poisson stream, resident fields {96^3,192^3,256x256x512,384^3,768^3} x {f32,f64}, "
-                       "1-3 levels, 1280x720, phase advance every 10 requests",
+                       "1-3 levels, 1280x720, phase advance every 10 requests (single-precision solver stand-in)",
            "slots": slots, "budget_gb": budget_gb, "resident_gb": resident_bytes / 1e9, "rates": []}
-    solver = torch.cuda.Stream()
 
     def advance(r, time_value):
         t = r["t"]
         r["time"] = time_value
-        gpu.fieldgen_modes_device_async(t.data_ptr(), 0 if t.dtype == torch.float64 else 1, tuple(t.shape), 32, 1,
+        gpu.fieldgen_modes_device_async(t.data_ptr(), 2 if t.dtype == torch.float64 else 1, tuple(t.shape), 32, 1,
                                         12, 5.0 / 6.0, r["seed"], time_value, solver.cuda_stream)
         solver.synchronize()
 

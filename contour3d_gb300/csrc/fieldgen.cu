@@ -30,7 +30,9 @@ __global__ void k_modes_f64(double* __restrict__ out, const double* __restrict__
   }
 }
 
-__global__ void k_modes_f32(float* __restrict__ out, const double* __restrict__ tx, const double* __restrict__ ty,
+/* single-precision sums, stored as float, or widened to double (OUT = double) */
+template <typename OUT>
+__global__ void k_modes_f32(OUT* __restrict__ out, const double* __restrict__ tx, const double* __restrict__ ty,
                             const double* __restrict__ tz, const double* __restrict__ amp, int nmodes, long mx,
                             long my, long mz) {
   const long long n = (long long)mx * my * mz;
@@ -47,7 +49,7 @@ __global__ void k_modes_f32(float* __restrict__ out, const double* __restrict__ 
       const float ti = __fadd_rn(__fmul_rn(exr, eyi), __fmul_rn(exi, eyr));
       f = __fadd_rn(f, __fmul_rn((float)amp[m], __fadd_rn(__fmul_rn(tr, ezi), __fmul_rn(ti, ezr))));
     }
-    out[q] = f;
+    out[q] = (OUT)f;
   }
 }
 
@@ -128,7 +130,8 @@ extern "C" double c3d_fieldgen_modes_device(void* out, int dtype, const long gl[
     if (dtype == 0)
       k_modes_f64<<<grid_blocks(n), 256>>>((double*)out, dt[0], dt[1], dt[2], dt[3], nmodes, my[0], my[1], my[2]);
     else
-      k_modes_f32<<<grid_blocks(n), 256>>>((float*)out, dt[0], dt[1], dt[2], dt[3], nmodes, my[0], my[1], my[2]);
+      k_modes_f32<float><<<grid_blocks(n), 256>>>((float*)out, dt[0], dt[1], dt[2], dt[3], nmodes, my[0], my[1],
+                                                  my[2]);
     if (cudaDeviceSynchronize() != cudaSuccess) rc = 1;
   }
   for (int d = 0; d < 4; d++)
@@ -144,7 +147,10 @@ extern "C" double c3d_fieldgen_modes_device(void* out, int dtype, const long gl[
 /*
  * The same field launched on `stream` with stream-ordered scratch and no
  * device-wide synchronisation, so a solver can advance a resident field
- * while other work runs.  Returns the analytic std, or -1 on error.
+ * while other work runs.  dtype 2: double storage of the single-precision
+ * sums (dtype 1's values widened), a cheap stand-in for a solver's double
+ * field on GPUs whose FP64 rate is low.  Returns the analytic std, or -1 on
+ * error.
  */
 extern "C" double c3d_fieldgen_modes_device_async(void* out, int dtype, const long gl[3], const long off[3],
                                                   const long my[3], int nmodes, int kmin, int kmax, double power,
@@ -194,8 +200,12 @@ extern "C" double c3d_fieldgen_modes_device_async(void* out, int dtype, const lo
     const long long n = (long long)my[0] * my[1] * my[2];
     if (dtype == 0)
       k_modes_f64<<<grid_blocks(n), 256, 0, stream>>>((double*)out, dx, dy, dz, d + nt, nmodes, my[0], my[1], my[2]);
+    else if (dtype == 2)
+      k_modes_f32<double><<<grid_blocks(n), 256, 0, stream>>>((double*)out, dx, dy, dz, d + nt, nmodes, my[0], my[1],
+                                                              my[2]);
     else
-      k_modes_f32<<<grid_blocks(n), 256, 0, stream>>>((float*)out, dx, dy, dz, d + nt, nmodes, my[0], my[1], my[2]);
+      k_modes_f32<float><<<grid_blocks(n), 256, 0, stream>>>((float*)out, dx, dy, dz, d + nt, nmodes, my[0], my[1],
+                                                             my[2]);
     rc = cudaGetLastError() != cudaSuccess;
   }
   /* the pageable copy has been staged when cudaMemcpyAsync returned; the
