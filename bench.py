@@ -272,6 +272,14 @@ def run_batched(gpu, workers, nfields=64):
                                        torch.cuda.get_device_name())
         workers = tuning["workers"]
     workers = int(workers)
+    sub = packs[:16]
+
+    def sample():
+        gpu.render_batch(sub, workers)
+        torch.cuda.synchronize()
+
+    shape_tuning = autotune.tune_launch_shape(gpu, sample, per_frame[:16], [f.width * f.height for f in frames[:16]],
+                                              torch.cuda.get_device_name())
     for p in packs[:4]:
         gpu.render_pack(p)
     gpu.render_batch(packs[:8], workers)
@@ -319,6 +327,7 @@ def run_batched(gpu, workers, nfields=64):
             "pixels_differing": px, "pixels": len(twins) * 1024 * 1024, "max_channel_diff": maxd}
     return {"workload": f"{nfields} fields, dims 64..384, half f64 / half f32, 1-4 levels, own camera, 1024x1024",
             "frames": nfields, "cell_thresholds": int(cells), "workers": workers, "tuning": tuning,
+            "launch_shape": shape_tuning,
             "plain": {"cells_per_s": cells / plain_s, "frames_per_s": nfields / plain_s, "s": plain_s},
             "batched": {"cells_per_s": cells / batch_s, "frames_per_s": nfields / batch_s, "s": batch_s},
             "speedup": plain_s / batch_s, "images_identical": same, "fp32_input_vs_fp64": fp32}
@@ -576,6 +585,17 @@ def main():
 
     for _ in range(max(3, args.warmup)):
         step()
+    # the launch shape for this workload (cached per GPU and size class)
+    from contour3d_gb300 import autotune
+
+    def sample():
+        step()
+        step()
+        torch.cuda.synchronize()
+
+    shape_tuning = autotune.tune_launch_shape(gpu, sample, [(nx - 1) * (ny - 1) * (nz - 1)], [WIDTH * HEIGHT],
+                                              torch.cuda.get_device_name())
+    step()
     # untimed per-stage profile of one frame
     gpu.set_stage_timing(True)
     step()
@@ -624,7 +644,8 @@ def main():
         return a.elapsed_time(b) / n
 
     gpu.set_graphs(False)
-    modes = {"graph_ms": ms, "timed_frames_graph": timed_graph, "unsynchronised_ms": frames_ms()}
+    modes = {"graph_ms": ms, "timed_frames_graph": timed_graph, "unsynchronised_ms": frames_ms(),
+             "launch_shape": shape_tuning}
     gpu.set_async(False)
     modes["synchronised_ms"] = frames_ms()
     gpu.set_async(True)

@@ -73,7 +73,19 @@ struct SlabDev {
   long long nslices;
   long long krender0;
   long long krender1;
+  int cls_z = 32; /* slices per classification brick (set from the launch shape) */
 };
+
+/* launch shape of the tunable kernels, process-wide: slices per
+   classification brick, resident blocks per SM of k_emit's grid and of the
+   raster passes' grids (k_cover, k_sliver, k_tiny, k_prune, k_exact) */
+struct LaunchShape {
+  int cls_z;
+  int emit_per_sm;
+  int raster_per_sm;
+};
+int set_launch_shape(const LaunchShape& s);
+LaunchShape launch_shape();
 
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {

@@ -60,6 +60,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cuda/atomic>
 #include "c3d_common.cuh"
@@ -174,7 +175,7 @@ __device__ __forceinline__ unsigned long long packed_count(unsigned c) {
  */
 constexpr int kClsX = 128;
 constexpr int kClsY = 8;
-constexpr int kClsZ = 32;
+constexpr int kClsZ = 32; /* default slices per brick (LaunchShape::cls_z) */
 
 template <typename T>
 __device__ __forceinline__ unsigned char node_above(const FieldDev& F, const T* f, long long idx);
@@ -219,8 +220,8 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
   const T* f = static_cast<const T*>(F.data);
   const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
   const unsigned i0 = blockIdx.x * kClsX, j0 = blockIdx.y * kClsY;
-  const long long k0 = (long long)blockIdx.z * kClsZ;
-  const long long k1 = min(k0 + kClsZ, S.nslices);
+  const long long k0 = (long long)blockIdx.z * S.cls_z;
+  const long long k1 = min(k0 + S.cls_z, S.nslices);
   const long long sx = F.nx, sxy = F.nx * F.ny;
   auto load_plane = [&](int buf, long long k) {
     for (int q = threadIdx.x; q < (kClsY + 1) * (kClsX + 1); q += blockDim.x) {
@@ -325,8 +326,8 @@ k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, 
   __shared__ int s_fail;
   const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
   const int i0 = blockIdx.x * kClsX, j0 = blockIdx.y * kClsY;
-  const long long k0 = (long long)blockIdx.z * kClsZ;
-  const long long k1 = min(k0 + kClsZ, S.nslices);
+  const long long k0 = (long long)blockIdx.z * S.cls_z;
+  const long long k1 = min(k0 + S.cls_z, S.nslices);
   const int nplanes = (int)(k1 - k0) + 1; /* node planes k0 .. k1 of the slab */
   if (threadIdx.x == 0) {
     s_fail = 0;
@@ -2727,6 +2728,20 @@ static int num_sms() {
   return n;
 }
 
+static std::atomic<int> g_cls_z{kClsZ}, g_emit_per_sm{8}, g_raster_per_sm{8};
+
+int set_launch_shape(const LaunchShape& s) {
+  if (s.cls_z < 1 || s.cls_z > 1024 || s.emit_per_sm < 1 || s.emit_per_sm > 32 || s.raster_per_sm < 1 ||
+      s.raster_per_sm > 32)
+    return 1;
+  g_cls_z = s.cls_z;
+  g_emit_per_sm = s.emit_per_sm;
+  g_raster_per_sm = s.raster_per_sm;
+  return 0;
+}
+
+LaunchShape launch_shape() { return LaunchShape{g_cls_z.load(), g_emit_per_sm.load(), g_raster_per_sm.load()}; }
+
 /* every kernel launch of the library: programmatic dependent launch (the
    kernels call pdl_wait() before they touch what earlier work produced) */
 template <typename... KArgs, typename... Args>
@@ -2835,12 +2850,14 @@ static void launch_classify_tma(const CUtensorMap& map, const FieldDev& F, const
   }
 }
 
-int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
+int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S0, unsigned char* const* codes, unsigned* err,
                     cudaStream_t st) {
   /* codes[q] receives the cell codes of threshold q; the scan turns them into counts */
   const FieldDev& F = Fs[0];
+  SlabDev S = S0;
+  S.cls_z = launch_shape().cls_z;
   const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
-                  (unsigned)((S.nslices + kClsZ - 1) / kClsZ));
+                  (unsigned)((S.nslices + S.cls_z - 1) / S.cls_z));
   CUtensorMap map;
   if (classify_tensor_map(F, &map)) {
     /* one pass over the field for up to kMaxThr thresholds */
@@ -2894,7 +2911,7 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
                  const unsigned* voffsets, const unsigned* tri_cell, const unsigned long long* total,
                  long long tri_bound, const TriDev& tri, const RasterDev& R, const VertDev& V, unsigned* checks,
                  cudaStream_t st) {
-  const int g = grid_for(tri_bound, 256, 8);
+  const int g = grid_for(tri_bound, 256, g_emit_per_sm);
   if (checks) {
     if (F.is_f32)
       launch_k(k_emit<float, true>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
@@ -2928,14 +2945,14 @@ void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long*
                   cudaStream_t st) {
   (void)total;
   (void)order_base;
-  const int g = grid_for(tri_bound, 256, 8);
+  const int g = grid_for(tri_bound, 256, g_raster_per_sm);
   if (checks) launch_k(k_cover<true>, g, 256, 0, st, G, scene, tri, R, checks);
   else launch_k(k_cover<false>, g, 256, 0, st, G, scene, tri, R, checks);
 }
 
 void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
                    unsigned* checks, cudaStream_t st) {
-  const int g = grid_for(sliver_bound, 256, 8);
+  const int g = grid_for(sliver_bound, 256, g_raster_per_sm);
   if (G.F.is_f32) {
     if (checks) launch_k(k_sliver<float, true>, g, 256, 0, st, G, scene, R, checks);
     else launch_k(k_sliver<float, false>, g, 256, 0, st, G, scene, R, checks);
@@ -2947,18 +2964,18 @@ void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, 
 
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
                  unsigned long long order_base, unsigned* checks, cudaStream_t st) {
-  const int g = grid_for(tiny_bound, 256, 8);
+  const int g = grid_for(tiny_bound, 256, g_raster_per_sm);
   if (checks) launch_k(k_tiny<true>, g, 256, 0, st, G, scene, R, order_base, checks);
   else launch_k(k_tiny<false>, g, 256, 0, st, G, scene, R, order_base, checks);
 }
 
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st) {
-  launch_k(k_prune, grid_for(cand_bound, 256, 8), 256, 0, st, R);
+  launch_k(k_prune, grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, R);
 }
 
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
                   unsigned long long order_base, cudaStream_t st) {
-  launch_k(k_exact, grid_for(cand_bound, 256, 8), 256, 0, st, G, scene, R, order_base);
+  launch_k(k_exact, grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, G, scene, R, order_base);
 }
 
 void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,

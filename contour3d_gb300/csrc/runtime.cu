@@ -2042,6 +2042,15 @@ extern "C" int contour3d_gb300_set_graphs(int on) {
   return 0;
 }
 
+extern "C" int contour3d_gb300_set_launch_shape(int classify_slices, int emit_blocks_per_sm,
+                                               int raster_blocks_per_sm) {
+  if (set_launch_shape(LaunchShape{classify_slices, emit_blocks_per_sm, raster_blocks_per_sm})) {
+    log_error("launch shape out of range (classify slices 1..1024, blocks per SM 1..32)");
+    return 1;
+  }
+  return 0;
+}
+
 extern "C" int contour3d_gb300_set_slab_cells(uint64_t max_cells) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (max_cells < 64) {

@@ -258,6 +258,14 @@ int contour3d_gb300_set_async(int on);
  * more work than the recorded sizes drops the graph.  0 = no graphs.
  */
 int contour3d_gb300_set_graphs(int on);
+/*
+ * Launch shape of the tunable kernels, for every context of the process:
+ * node slices per classification brick (default 32), resident blocks per SM
+ * of the triangle pass's grid and of the raster passes' grids (default 8
+ * each).  Results do not depend on it.  contour3d_gb300/autotune.py chooses
+ * it per GPU and workload size class.  Returns 1 for values out of range.
+ */
+int contour3d_gb300_set_launch_shape(int classify_slices, int emit_blocks_per_sm, int raster_blocks_per_sm);
 /* upper bound on cells per slab (default and maximum 178,956,970, the most the
    scan's packed 32-bit sums allow); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);

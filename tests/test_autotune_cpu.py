@@ -45,3 +45,32 @@ def test_size_class():
     k = autotune.size_class([1 << 20] * 10, [1 << 20] * 10)
     assert k == "c20-p20-n8"
     assert autotune.size_class([1 << 24] * 64, [1 << 20] * 64) != k
+
+
+def test_launch_shape_is_tuned_and_cached(tmp_path):
+    path = str(tmp_path / "tune.json")
+    calls = []
+
+    def run(shape):
+        calls.append(shape)
+        return 1.0 if shape != (16, 8, 8) else 0.5
+
+    r = autotune.tune_shape("gpu|shape|c20", run, path=path)
+    assert r["shape"] == [16, 8, 8] and not r["cached"]
+    assert len(calls) == len(autotune.SHAPES)
+    r2 = autotune.tune_shape("gpu|shape|c20", run, path=path)
+    assert r2["shape"] == [16, 8, 8] and r2["cached"] and len(calls) == len(autotune.SHAPES)
+
+
+def test_tune_launch_shape_sets_the_choice(tmp_path):
+    class FakeLib:
+        def __init__(self):
+            self.shape = None
+
+        def set_launch_shape(self, *s):
+            self.shape = s
+
+    lib = FakeLib()
+    r = autotune.tune_launch_shape(lib, lambda: None, [1 << 20], [1 << 20], "gpu", candidates=((32, 8, 8), (64, 4, 4)),
+                                   repeats=1, path=str(tmp_path / "t.json"))
+    assert lib.shape == tuple(r["shape"])
