@@ -86,6 +86,8 @@ struct LaunchShape {
 };
 int set_launch_shape(const LaunchShape& s);
 LaunchShape launch_shape();
+/* programmatic dependent launch of the library's kernels on (1) or off (0) */
+void set_dependent_launch(int on);
 
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {

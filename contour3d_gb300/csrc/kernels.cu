@@ -1538,9 +1538,12 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
   __syncthreads();
   pdl_wait();
   const long long T_ = (long long)*total_p;
-  if ((unsigned long long)T_ > tri.cap) {
-    /* more triangles than the arrays hold (sized before the count was known) */
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(tri.ovf, kOvfTriangles);
+  if ((unsigned long long)T_ > tri.cap || (V.pos && total_p[1] > V.cap)) {
+    /* more triangles than the arrays hold, or more crossed edges than vertex
+       records (sized before the counts were known): nothing is read or
+       written, the frame is rendered again */
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+      atomicOr(tri.ovf, (unsigned long long)T_ > tri.cap ? kOvfTriangles : kOvfVertices);
     return;
   }
   const long long step = (long long)blockDim.x * kEmitPer;
@@ -2729,6 +2732,9 @@ static int num_sms() {
 }
 
 static std::atomic<int> g_cls_z{kClsZ}, g_emit_per_sm{8}, g_raster_per_sm{8};
+static std::atomic<int> g_pdl{0};
+
+void set_dependent_launch(int on) { g_pdl = on ? 1 : 0; }
 
 int set_launch_shape(const LaunchShape& s) {
   if (s.cls_z < 1 || s.cls_z > 1024 || s.emit_per_sm < 1 || s.emit_per_sm > 32 || s.raster_per_sm < 1 ||
@@ -2754,7 +2760,7 @@ static void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
   cfg.stream = st;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[0].val.programmaticStreamSerializationAllowed = g_pdl.load() ? 1 : 0;
   cfg.attrs = at;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);

@@ -2051,6 +2051,11 @@ extern "C" int contour3d_gb300_set_launch_shape(int classify_slices, int emit_bl
   return 0;
 }
 
+extern "C" int contour3d_gb300_set_dependent_launch(int on) {
+  set_dependent_launch(on);
+  return 0;
+}
+
 extern "C" int contour3d_gb300_set_slab_cells(uint64_t max_cells) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (max_cells < 64) {

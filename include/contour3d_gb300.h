@@ -266,6 +266,13 @@ int contour3d_gb300_set_graphs(int on);
  * it per GPU and workload size class.  Returns 1 for values out of range.
  */
 int contour3d_gb300_set_launch_shape(int classify_slices, int emit_blocks_per_sm, int raster_blocks_per_sm);
+/*
+ * 1 = launch the library's kernels with programmatic dependent launch (a
+ * kernel may be scheduled while its predecessor finishes and waits in
+ * griddepcontrol.wait before touching earlier results); 0 (default) =
+ * ordinary stream order.
+ */
+int contour3d_gb300_set_dependent_launch(int on);
 /* upper bound on cells per slab (default and maximum 178,956,970, the most the
    scan's packed 32-bit sums allow); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);
