@@ -16,8 +16,14 @@ from tests import cases
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+# counts that depend only on the geometry; not the FP64-shaded pixels and
+# their neighbour entries: the FP32 shading uses a winner's stored weights
+# only when all three of its 16-byte words carry the winner's tag, and a
+# fragment that lost the z-test after winning a CAS may overwrite a word
+# late, so how many pixels fall back to the (exact) FP64 colour depends on
+# timing -- the colours do not
 KEYS = ("triangles", "vertices", "candidates", "tiny", "cover_triangles", "exact_fragments", "slivers", "winners",
-        "shade_exact", "normals", "slabs")
+        "slabs")
 
 
 def _stats(gpu):
