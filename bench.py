@@ -85,6 +85,8 @@ def parse():
     p.add_argument("--served-rates", default="50,100,200,400,max",
                    help="comma-separated request rates (req/s); max = submit without waiting")
     p.add_argument("--served-requests", type=int, default=500)
+    p.add_argument("--no-tune", action="store_true",
+                   help="keep the default launch shape (profiler captures: fewer launches before the timed ones)")
     p.add_argument("--cpu-table", action="store_true",
                    help="with --impl reference: also time the oracle on the other workloads")
     return p.parse_args()
@@ -593,9 +595,11 @@ def main():
         step()
         torch.cuda.synchronize()
 
-    shape_tuning = autotune.tune_launch_shape(gpu, sample, [(nx - 1) * (ny - 1) * (nz - 1)], [WIDTH * HEIGHT],
-                                              torch.cuda.get_device_name())
-    step()
+    shape_tuning = None
+    if not args.no_tune:
+        shape_tuning = autotune.tune_launch_shape(gpu, sample, [(nx - 1) * (ny - 1) * (nz - 1)], [WIDTH * HEIGHT],
+                                                  torch.cuda.get_device_name())
+        step()
     # untimed per-stage profile of one frame
     gpu.set_stage_timing(True)
     step()

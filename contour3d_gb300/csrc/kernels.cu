@@ -62,6 +62,8 @@
 #include <cuda_runtime.h>
 #include <atomic>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cuda/atomic>
 #include "c3d_common.cuh"
 #include "c3d_kernels.h"
@@ -2750,9 +2752,20 @@ LaunchShape launch_shape() { return LaunchShape{g_cls_z.load(), g_emit_per_sm.lo
 
 /* every kernel launch of the library: programmatic dependent launch (the
    kernels call pdl_wait() before they touch what earlier work produced) */
+/* C3D_LAUNCH_CHECK=1 in the environment: every launch is followed by a
+   synchronisation of its stream and an error check that names the kernel
+   (debugging; changes timing) */
+static bool launch_check() {
+  static const bool on = [] {
+    const char* e = getenv("C3D_LAUNCH_CHECK");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+
 template <typename... KArgs, typename... Args>
-static void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                     Args... args) {
+static void launch_k(void (*kernel)(KArgs...), const char* name, dim3 grid, dim3 block, size_t smem,
+                     cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -2763,7 +2776,13 @@ static void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
   at[0].val.programmaticStreamSerializationAllowed = g_pdl.load() ? 1 : 0;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+  if (launch_check()) {
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+      fprintf(stderr, "[CONTOUR3D ERROR] %s (grid %u x %u x %u): %s\n", name, grid.x, grid.y, grid.z,
+              cudaGetErrorString(e));
+  }
 }
 
 static int grid_for(long long n, int threads, int per_sm) {
@@ -2849,10 +2868,10 @@ template <typename T>
 static void launch_classify_tma(const CUtensorMap& map, const FieldDev& F, const SlabDev& S, const ThrSet& ts,
                                 const CodeOut& out, unsigned* err, const dim3& grid, cudaStream_t st) {
   switch (ts.n) {
-    case 1: launch_k(k_classify_tma<T, 1>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
-    case 2: launch_k(k_classify_tma<T, 2>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
-    case 3: launch_k(k_classify_tma<T, 3>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
-    default: launch_k(k_classify_tma<T, 4>, grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    case 1: launch_k(k_classify_tma<T, 1>, "k_classify_tma", grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    case 2: launch_k(k_classify_tma<T, 2>, "k_classify_tma", grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    case 3: launch_k(k_classify_tma<T, 3>, "k_classify_tma", grid, kClsX, 0, st, map, F, S, ts, out, err); break;
+    default: launch_k(k_classify_tma<T, 4>, "k_classify_tma", grid, kClsX, 0, st, map, F, S, ts, out, err); break;
   }
 }
 
@@ -2881,8 +2900,8 @@ int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S0, unsigned char
     return (nf + kMaxThr - 1) / kMaxThr;
   }
   for (int q = 0; q < nf; q++) {
-    if (F.is_f32) launch_k(k_classify<float>, grid, kClsX, 0, st, Fs[q], S, codes[q]);
-    else launch_k(k_classify<double>, grid, kClsX, 0, st, Fs[q], S, codes[q]);
+    if (F.is_f32) launch_k(k_classify<float>, "k_classify", grid, kClsX, 0, st, Fs[q], S, codes[q]);
+    else launch_k(k_classify<double>, "k_classify", grid, kClsX, 0, st, Fs[q], S, codes[q]);
   }
   return nf;
 }
@@ -2893,22 +2912,22 @@ void launch_scan(const unsigned char* codes, long long n, unsigned long long* se
                  unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
                  unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, unsigned* ovf, cudaStream_t st) {
   const long long nseg = scan_segments(n);
-  if (nseg > 0) launch_k(k_seg_reduce, (unsigned)nseg, kScanThreads, 0, st, codes, n, seg_sums);
-  launch_k(k_seg_scan, 1, kSegScanThreads, 0, st, seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
+  if (nseg > 0) launch_k(k_seg_reduce, "k_seg_reduce", (unsigned)nseg, kScanThreads, 0, st, codes, n, seg_sums);
+  launch_k(k_seg_scan, "k_seg_scan", 1, kSegScanThreads, 0, st, seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
   if (nseg > 0)
-    launch_k(k_scan_write, (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, seg_base, offsets, voffsets,
+    launch_k(k_scan_write, "k_scan_write", (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, seg_base, offsets, voffsets,
              totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf);
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st) {
   const unsigned blocks = (unsigned)((n + kVTile - 1) / kVTile);
-  if (F.is_f32) launch_k(k_vertices<float>, blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
-  else launch_k(k_vertices<double>, blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
+  if (F.is_f32) launch_k(k_vertices<float>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
+  else launch_k(k_vertices<double>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
 }
 
 void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st) {
-  launch_k(k_fill_tri_cell, grid_for(n, 256, 16), 256, 0, st, offsets, n, tri_cell);
+  launch_k(k_fill_tri_cell, "k_fill_tri_cell", grid_for(n, 256, 16), 256, 0, st, offsets, n, tri_cell);
 }
 
 
@@ -2920,30 +2939,30 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
   const int g = grid_for(tri_bound, 256, g_emit_per_sm);
   if (checks) {
     if (F.is_f32)
-      launch_k(k_emit<float, true>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+      launch_k(k_emit<float, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
                R, V, checks);
     else
-      launch_k(k_emit<double, true>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+      launch_k(k_emit<double, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
                R, V, checks);
   } else {
     if (F.is_f32)
-      launch_k(k_emit<float, false>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+      launch_k(k_emit<float, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
                R, V, checks);
     else
-      launch_k(k_emit<double, false>, g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
+      launch_k(k_emit<double, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
                R, V, checks);
   }
 }
 
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,
                       cudaStream_t st) {
-  launch_k(k_exact_all, grid_for(tri_bound, 256, 8), 256, 0, st, G, total, tri);
+  launch_k(k_exact_all, "k_exact_all", grid_for(tri_bound, 256, 8), 256, 0, st, G, total, tri);
 }
 
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, 8);
-  launch_k(k_normals, g, 256, 0, st, F, S, offsets, tri_cell, total, tri);
+  launch_k(k_normals, "k_normals", g, 256, 0, st, F, S, offsets, tri_cell, total, tri);
 }
 
 void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
@@ -2952,53 +2971,53 @@ void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long*
   (void)total;
   (void)order_base;
   const int g = grid_for(tri_bound, 256, g_raster_per_sm);
-  if (checks) launch_k(k_cover<true>, g, 256, 0, st, G, scene, tri, R, checks);
-  else launch_k(k_cover<false>, g, 256, 0, st, G, scene, tri, R, checks);
+  if (checks) launch_k(k_cover<true>, "k_cover", g, 256, 0, st, G, scene, tri, R, checks);
+  else launch_k(k_cover<false>, "k_cover", g, 256, 0, st, G, scene, tri, R, checks);
 }
 
 void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
                    unsigned* checks, cudaStream_t st) {
   const int g = grid_for(sliver_bound, 256, g_raster_per_sm);
   if (G.F.is_f32) {
-    if (checks) launch_k(k_sliver<float, true>, g, 256, 0, st, G, scene, R, checks);
-    else launch_k(k_sliver<float, false>, g, 256, 0, st, G, scene, R, checks);
+    if (checks) launch_k(k_sliver<float, true>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
+    else launch_k(k_sliver<float, false>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
   } else {
-    if (checks) launch_k(k_sliver<double, true>, g, 256, 0, st, G, scene, R, checks);
-    else launch_k(k_sliver<double, false>, g, 256, 0, st, G, scene, R, checks);
+    if (checks) launch_k(k_sliver<double, true>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
+    else launch_k(k_sliver<double, false>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
   }
 }
 
 void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
                  unsigned long long order_base, unsigned* checks, cudaStream_t st) {
   const int g = grid_for(tiny_bound, 256, g_raster_per_sm);
-  if (checks) launch_k(k_tiny<true>, g, 256, 0, st, G, scene, R, order_base, checks);
-  else launch_k(k_tiny<false>, g, 256, 0, st, G, scene, R, order_base, checks);
+  if (checks) launch_k(k_tiny<true>, "k_tiny", g, 256, 0, st, G, scene, R, order_base, checks);
+  else launch_k(k_tiny<false>, "k_tiny", g, 256, 0, st, G, scene, R, order_base, checks);
 }
 
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st) {
-  launch_k(k_prune, grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, R);
+  launch_k(k_prune, "k_prune", grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, R);
 }
 
 void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
                   unsigned long long order_base, cudaStream_t st) {
-  launch_k(k_exact, grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, G, scene, R, order_base);
+  launch_k(k_exact, "k_exact", grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, G, scene, R, order_base);
 }
 
 void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,
                     unsigned long long obase, unsigned rgb, cudaStream_t st) {
   const long long npx = scene.width * scene.height;
   const unsigned long long span = 12ULL * (unsigned long long)((F.nx - 1) * (F.ny - 1) * (F.nz - 1));
-  launch_k(k_winners, grid_for(npx, 256, 8), 256, 0, st, R.canvas, npx, obase, span, R.win, R.win_count);
+  launch_k(k_winners, "k_winners", grid_for(npx, 256, 8), 256, 0, st, R.canvas, npx, obase, span, R.win, R.win_count);
   /* no single-precision shading without node spacings (a converter) or for
      axes of 2^20 nodes and more (hash keys): every pixel to the FP64 pass */
   if (!F.dgx || F.nx > (1 << 20) || F.ny > (1 << 20) || F.nz > (1 << 20)) return;
   const int gs = grid_for(4 * npx, 256, 8); /* four threads per pixel */
   if (F.is_f32) {
-    if (R.shade_check) launch_k(k_shade_f<float, true>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
-    else launch_k(k_shade_f<float, false>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    if (R.shade_check) launch_k(k_shade_f<float, true>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    else launch_k(k_shade_f<float, false>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
   } else {
-    if (R.shade_check) launch_k(k_shade_f<double, true>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
-    else launch_k(k_shade_f<double, false>, gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    if (R.shade_check) launch_k(k_shade_f<double, true>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    else launch_k(k_shade_f<double, false>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
   }
 }
 
@@ -3008,29 +3027,29 @@ void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDe
                         unsigned long long* ent_count, uint2* spans, double* wn, unsigned rgb, unsigned* checks,
                         cudaStream_t st) {
   if (npix <= 0) return;
-  launch_k(k_nb_list, grid_for(3 * npix, 256, 8), 256, 0, st, F, R, lut, pixels, count, obase, ent, ent_cap,
+  launch_k(k_nb_list, "k_nb_list", grid_for(3 * npix, 256, 8), 256, 0, st, F, R, lut, pixels, count, obase, ent, ent_cap,
            ent_count, spans);
-  launch_k(k_nb_wn, grid_for((long long)ent_cap, 256, 8), 256, 0, st, F, lut, ent, ent_cap, ent_count, wn);
+  launch_k(k_nb_wn, "k_nb_wn", grid_for((long long)ent_cap, 256, 8), 256, 0, st, F, lut, ent, ent_cap, ent_count, wn);
   const int gs = grid_for(4 * npix, 256, 8);
   if (checks && R.shade_check)
-    launch_k(k_shade<true>, gs, 256, 0, st, F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
+    launch_k(k_shade<true>, "k_shade", gs, 256, 0, st, F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
   else
-    launch_k(k_shade<false>, gs, 256, 0, st, F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
+    launch_k(k_shade<false>, "k_shade", gs, 256, 0, st, F, scene, R, lut, pixels, count, obase, spans, wn, rgb, checks);
 }
 
 void launch_lines(const LineSegDev* segs, int nseg, long long W, long long H, Slot* canvas,
                   unsigned long long order_base, unsigned* zerr, cudaStream_t st) {
-  if (nseg > 0) launch_k(k_lines, nseg, 128, 0, st, segs, nseg, W, H, canvas, order_base, zerr);
+  if (nseg > 0) launch_k(k_lines, "k_lines", nseg, 128, 0, st, segs, nseg, W, H, canvas, order_base, zerr);
 }
 
 void launch_canvas_init(Slot* canvas, unsigned* zlo, long long n, unsigned long long hi, unsigned long long lo,
                         cudaStream_t st) {
-  launch_k(k_canvas_init, grid_for(n, 256, 8), 256, 0, st, canvas, zlo, n, hi, lo);
+  launch_k(k_canvas_init, "k_canvas_init", grid_for(n, 256, 8), 256, 0, st, canvas, zlo, n, hi, lo);
 }
 
 void launch_resolve(const Slot* canvas, long long W, long long H, unsigned char* rgb, double* depth,
                     cudaStream_t st) {
-  launch_k(k_resolve, grid_for(W * H, 256, 8), 256, 0, st, canvas, W, H, rgb, depth);
+  launch_k(k_resolve, "k_resolve", grid_for(W * H, 256, 8), 256, 0, st, canvas, W, H, rgb, depth);
 }
 
 }  // namespace c3d

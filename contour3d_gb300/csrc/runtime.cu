@@ -480,6 +480,8 @@ struct Ctx {
 
 static Ctx g_ctx;
 static std::mutex g_mu;
+/* the unsynchronised-frame and graph settings new contexts (server slots) start with */
+static std::atomic<bool> g_async_default{true}, g_graphs_default{true};
 
 static int ctx_init(Ctx &c) {
   int dev = 0;
@@ -488,6 +490,10 @@ static int ctx_init(Ctx &c) {
   if (c.ready) {
     log_error("the library context is bound to device %d; call contour3d_gb300_release() first", c.device);
     return 1;
+  }
+  if (&c != &g_ctx) {
+    c.async_enabled = g_async_default.load();
+    c.graphs_enabled = g_graphs_default.load();
   }
   C3D_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
   C3D_CUDA(cudaEventCreate(&c.ev0));
@@ -2029,12 +2035,14 @@ extern "C" int contour3d_gb300_set_filter_check(int on) {
 extern "C" int contour3d_gb300_set_async(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_ctx.async_enabled = on != 0;
+  g_async_default = on != 0;
   return 0;
 }
 
 extern "C" int contour3d_gb300_set_graphs(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_ctx.graphs_enabled = on != 0;
+  g_graphs_default = on != 0;
   if (!on) {
     drop_graph(g_ctx);
     g_ctx.graph_key_seen = false;

@@ -245,6 +245,7 @@ int contour3d_gb300_set_filter_check(int on);
  * rendered again with synchronisation (which learns the larger counts);
  * 0 = synchronise after every slab's scan and raster pass and size every
  * buffer from the counts just read.  The image is the same either way.
+ * Applies to the calling context and to server contexts created later.
  */
 int contour3d_gb300_set_async(int on);
 /*
@@ -256,6 +257,7 @@ int contour3d_gb300_set_async(int on);
  * launched instead of the frame's individual calls; the field values may
  * change between frames (an in-situ solver's time steps).  A frame that finds
  * more work than the recorded sizes drops the graph.  0 = no graphs.
+ * Applies to the calling context and to server contexts created later.
  */
 int contour3d_gb300_set_graphs(int on);
 /*
