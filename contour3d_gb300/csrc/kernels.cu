@@ -2915,8 +2915,8 @@ void launch_scan(const unsigned char* codes, long long n, unsigned long long* se
   if (nseg > 0) launch_k(k_seg_reduce, "k_seg_reduce", (unsigned)nseg, kScanThreads, 0, st, codes, n, seg_sums);
   launch_k(k_seg_scan, "k_seg_scan", 1, kSegScanThreads, 0, st, seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
   if (nseg > 0)
-    launch_k(k_scan_write, "k_scan_write", (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, seg_base, offsets, voffsets,
-             totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf);
+    launch_k(k_scan_write, "k_scan_write", (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, seg_base,
+             offsets, voffsets, totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf);
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
@@ -2939,18 +2939,18 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
   const int g = grid_for(tri_bound, 256, g_emit_per_sm);
   if (checks) {
     if (F.is_f32)
-      launch_k(k_emit<float, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
-               R, V, checks);
+      launch_k(k_emit<float, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
+               total, tri, R, V, checks);
     else
-      launch_k(k_emit<double, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
-               R, V, checks);
+      launch_k(k_emit<double, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
+               total, tri, R, V, checks);
   } else {
     if (F.is_f32)
-      launch_k(k_emit<float, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
-               R, V, checks);
+      launch_k(k_emit<float, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
+               total, tri, R, V, checks);
     else
-      launch_k(k_emit<double, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell, total, tri,
-               R, V, checks);
+      launch_k(k_emit<double, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
+               total, tri, R, V, checks);
   }
 }
 
@@ -3027,8 +3027,8 @@ void launch_shade_exact(const FieldDev& F, const SceneDev& scene, const RasterDe
                         unsigned long long* ent_count, uint2* spans, double* wn, unsigned rgb, unsigned* checks,
                         cudaStream_t st) {
   if (npix <= 0) return;
-  launch_k(k_nb_list, "k_nb_list", grid_for(3 * npix, 256, 8), 256, 0, st, F, R, lut, pixels, count, obase, ent, ent_cap,
-           ent_count, spans);
+  launch_k(k_nb_list, "k_nb_list", grid_for(3 * npix, 256, 8), 256, 0, st, F, R, lut, pixels, count, obase, ent,
+           ent_cap, ent_count, spans);
   launch_k(k_nb_wn, "k_nb_wn", grid_for((long long)ent_cap, 256, 8), 256, 0, st, F, lut, ent, ent_cap, ent_count, wn);
   const int gs = grid_for(4 * npix, 256, 8);
   if (checks && R.shade_check)

@@ -480,8 +480,10 @@ struct Ctx {
 
 static Ctx g_ctx;
 static std::mutex g_mu;
-/* the unsynchronised-frame and graph settings new contexts (server slots) start with */
-static std::atomic<bool> g_async_default{true}, g_graphs_default{true};
+/* the unsynchronised-frame and graph settings new contexts (server slots)
+   start with: off, so worker contexts synchronise after every slab pass
+   (see contour3d_gb300_set_async) */
+static std::atomic<bool> g_async_default{false}, g_graphs_default{false};
 
 static int ctx_init(Ctx &c) {
   int dev = 0;
@@ -2035,14 +2037,18 @@ extern "C" int contour3d_gb300_set_filter_check(int on) {
 extern "C" int contour3d_gb300_set_async(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_ctx.async_enabled = on != 0;
+  return 0;
+}
+
+extern "C" int contour3d_gb300_set_server_async(int on) {
   g_async_default = on != 0;
+  g_graphs_default = on != 0;
   return 0;
 }
 
 extern "C" int contour3d_gb300_set_graphs(int on) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_ctx.graphs_enabled = on != 0;
-  g_graphs_default = on != 0;
   if (!on) {
     drop_graph(g_ctx);
     g_ctx.graph_key_seen = false;

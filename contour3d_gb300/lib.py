@@ -111,7 +111,7 @@ EXPORTS = [
     "contour3d_execute", "contour3d_gb300_identity", "contour3d_gb300_declare_identity",
     "contour3d_gb300_render", "contour3d_gb300_render_device", "contour3d_gb300_last_stats",
     "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells", "contour3d_gb300_set_filter_check",
-    "contour3d_gb300_set_async", "contour3d_gb300_set_graphs", "contour3d_gb300_set_launch_shape",
+    "contour3d_gb300_set_async", "contour3d_gb300_set_server_async", "contour3d_gb300_set_graphs", "contour3d_gb300_set_launch_shape",
     "contour3d_gb300_set_dependent_launch",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",

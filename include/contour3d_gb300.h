@@ -245,9 +245,18 @@ int contour3d_gb300_set_filter_check(int on);
  * rendered again with synchronisation (which learns the larger counts);
  * 0 = synchronise after every slab's scan and raster pass and size every
  * buffer from the counts just read.  The image is the same either way.
- * Applies to the calling context and to server contexts created later.
+ * Applies to the library's own context (contour3d_execute, the render
+ * entry points).
  */
 int contour3d_gb300_set_async(int on);
+/*
+ * The same, and graph recording, for the worker contexts of servers (and of
+ * contour3d_gb300_render_batch) created afterwards: 0 (default) = worker
+ * contexts synchronise after every slab pass; 1 = unsynchronised frames and
+ * graphs.  Off by default: a batched run with unsynchronised worker contexts
+ * stopped with an illegal memory access whose cause has not been found.
+ */
+int contour3d_gb300_set_server_async(int on);
 /*
  * 1 (default) = an unsynchronised frame drawn from device-resident fields
  * into device memory, on a stream other than the legacy default stream, is
@@ -257,7 +266,7 @@ int contour3d_gb300_set_async(int on);
  * launched instead of the frame's individual calls; the field values may
  * change between frames (an in-situ solver's time steps).  A frame that finds
  * more work than the recorded sizes drops the graph.  0 = no graphs.
- * Applies to the calling context and to server contexts created later.
+ * Applies to the library's own context.
  */
 int contour3d_gb300_set_graphs(int on);
 /*
