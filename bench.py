@@ -60,10 +60,10 @@ CPU_SAMPLE_SLICES_1 = 16  # z-nodes of the 512^2 x 512 field timed on one host c
 # capture of each kernel on the 256^3 case of this workload; the full-size
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
-    "classify": (4.60, "cells"),     # k_classify_tma, both levels in one pass: 152.4 MB for 2 x 16.6 M cells
+    "classify": (4.63, "cells"),     # k_classify_tma, both levels in one pass: 154.0 MB for 2 x 16.6 M cells
     "scan": (5.49, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 91.1 MB for 16.6 M cells
     "vertices": (36.5, "vertices"),  # k_vertices: 239.2 MB for 6.55 M vertices
-    "emit": (43.6, "triangles"),     # k_emit: 571.6 MB for 13.1 M triangles
+    "emit": (43.5, "triangles"),     # k_emit: 570.3 MB for 13.1 M triangles
 }
 
 

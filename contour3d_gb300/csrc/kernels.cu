@@ -470,9 +470,12 @@ k_seg_reduce(const unsigned char* __restrict__ codes, long long n, unsigned long
   load_scan_codes(codes, (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems, n, wv);
   load_count_lut(s_cnt);
   __syncthreads();
-  unsigned long long sum = 0;
+  /* a thread's 32 cells hold at most 384 triangles and 224 vertices: their
+     sum fits the 16-bit fields of the table entries */
+  unsigned s32 = 0;
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) sum += packed_count(s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
+  for (int q = 0; q < kScanItems; q++) s32 += s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
+  unsigned long long sum = packed_count(s32);
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
   if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = sum;
@@ -571,9 +574,12 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
   const unsigned long long slab_tris = totals[0];
   load_count_lut(s_cnt);
   __syncthreads();
-  unsigned long long sum = 0;
+  /* per-thread sums in the 16-bit fields of the table entries (at most 384
+     triangles and 224 vertices in a thread's 32 cells) */
+  unsigned s32 = 0;
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) sum += packed_count(s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255]);
+  for (int q = 0; q < kScanItems; q++) s32 += s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
+  const unsigned long long sum = packed_count(s32);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long incl = sum;
 #pragma unroll
@@ -614,15 +620,18 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
     for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) s_list[e] = 0xFFFFu;
     __syncthreads();
   }
+  /* the thread's first offsets (both below 2^31), then 32-bit running sums
+     in the table entries' 16-bit fields */
+  const unsigned first_t = (unsigned)(first & kTriMask), first_v = (unsigned)(first >> 31);
   for (int half = 1; half >= 0; half--) {
     /* half 1: vertex offsets; half 0: triangle offsets (staged only when
        they are stored) and the map */
-    unsigned long long run = first;
+    unsigned run = 0;
 #pragma unroll
     for (int q = 0; q < kScanItems; q++) {
       const unsigned cnt = s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
-      const unsigned t0 = (unsigned)(run & kTriMask);
-      if (half == 1 || keep_offsets) stage[kStagePitch * lane + q] = half == 0 ? t0 : (unsigned)(run >> 31);
+      const unsigned t0 = first_t + (run & 0xFFFFu);
+      if (half == 1 || keep_offsets) stage[kStagePitch * lane + q] = half == 0 ? t0 : first_v + (run >> 16);
       if (half == 0 && (listed || direct) && base + q < n) {
         const unsigned nt = cnt & 0xFFFFu;
         if (listed) {
@@ -631,7 +640,7 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
           for (unsigned r = 0; r < nt; r++) tri_cell[t0 + r] = (unsigned)(base + q) | (r << kTcRankShift);
         }
       }
-      run += packed_count(cnt);
+      run += cnt;
     }
     __syncwarp();
     unsigned* dst = half == 0 ? offsets : voffsets;
