@@ -301,6 +301,19 @@ def run_batched(gpu, workers, nfields=64):
     torch.cuda.synchronize()
     batch_s = time.perf_counter() - t0
     same = all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
+    # the same batch with each frame classifying its own fields
+    gpu.set_batch_classify(False)
+    try:
+        for o in outs:
+            o.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gpu.render_batch(packs, workers)
+        torch.cuda.synchronize()
+        own_s = time.perf_counter() - t0
+    finally:
+        gpu.set_batch_classify(True)
+    same = same and all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
     # the float32 half against the float64 fields they were rounded from: the
     # vertices of every crossed edge, and the frames rendered from both
     from contour3d_gb300 import fp32_error
@@ -331,7 +344,10 @@ def run_batched(gpu, workers, nfields=64):
             "frames": nfields, "cell_thresholds": int(cells), "workers": workers, "tuning": tuning,
             "launch_shape": shape_tuning,
             "plain": {"cells_per_s": cells / plain_s, "frames_per_s": nfields / plain_s, "s": plain_s},
-            "batched": {"cells_per_s": cells / batch_s, "frames_per_s": nfields / batch_s, "s": batch_s},
+            "batched": {"cells_per_s": cells / batch_s, "frames_per_s": nfields / batch_s, "s": batch_s,
+                        "classification": "one persistent launch over every frame's (field, brick) items"},
+            "batched_per_frame_classify": {"cells_per_s": cells / own_s, "frames_per_s": nfields / own_s,
+                                           "s": own_s},
             "speedup": plain_s / batch_s, "images_identical": same, "fp32_input_vs_fp64": fp32}
 
 

@@ -216,6 +216,21 @@ struct CodeOut {
    Returns the number of kernels launched. */
 int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
                     cudaStream_t st);
+/* one object's classification in a batch: its field and slab, its code
+   array, its bricks (kClsX x kClsY cells x S.cls_z slices) and the number of
+   its first brick among all items' bricks */
+struct ClsItem {
+  FieldDev F;
+  SlabDev S;
+  unsigned char* codes;
+  unsigned nbx, nby, nbz;
+  unsigned long long first;
+};
+/* the bricks of a classification along x, y and z */
+void classify_bricks(const FieldDev& F, const SlabDev& S, unsigned* nbx, unsigned* nby, unsigned* nbz);
+/* every item's codes in one persistent launch; `next` (device) must start at 0 */
+void launch_classify_queue(const ClsItem* items, int nitems, unsigned long long nunits, unsigned long long* next,
+                           cudaStream_t st);
 /* cells per slab for which the packed triangle and vertex sums of the scan stay below 2^31 */
 constexpr long long kMaxSlabCells = 178956970;
 

@@ -215,14 +215,15 @@ __device__ __forceinline__ bool node_above_thr(const ThrSet& ts, int t, int b) {
   return (unsigned)key - ts.flo[t] < ts.fcnt[t];
 }
 
+/* the cell codes of one brick (kClsX x kClsY cells, S.cls_z slices) */
 template <typename T>
-__global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ codes) {
-  pdl_enter();
-  __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+__device__ __forceinline__ void classify_brick(const FieldDev& F, const SlabDev& S, unsigned char* __restrict__ codes,
+                                               unsigned bx, unsigned by, unsigned bz,
+                                               unsigned char (*bits)[kClsY + 1][kClsX + 1]) {
   const T* f = static_cast<const T*>(F.data);
   const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
-  const unsigned i0 = blockIdx.x * kClsX, j0 = blockIdx.y * kClsY;
-  const long long k0 = (long long)blockIdx.z * S.cls_z;
+  const unsigned i0 = bx * kClsX, j0 = by * kClsY;
+  const long long k0 = (long long)bz * S.cls_z;
   const long long k1 = min(k0 + S.cls_z, S.nslices);
   const long long sx = F.nx, sxy = F.nx * F.ny;
   auto load_plane = [&](int buf, long long k) {
@@ -253,6 +254,51 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
       if (in_x) codes[((size_t)kl * ncy + j) * ncx + i] = (unsigned char)code;
     }
     __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsigned char* __restrict__ codes) {
+  pdl_enter();
+  __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+  classify_brick<T>(F, S, codes, blockIdx.x, blockIdx.y, blockIdx.z, bits);
+}
+
+/*
+ * k_classify_queue: the cell codes of many objects' fields (the frames of a
+ * batch) in one launch of a persistent grid.  The work items are (object,
+ * brick) pairs numbered object by object (ClsItem::first); each block takes
+ * the next item number from a device counter, finds its object by binary
+ * search over the items' first numbers, and classifies that brick.  Every
+ * item number is taken once, so the loop ends after at most nunits / grid
+ * items per block.
+ */
+__global__ void __launch_bounds__(kClsX)
+k_classify_queue(const ClsItem* __restrict__ items, int nitems, unsigned long long nunits,
+                 unsigned long long* __restrict__ next) {
+  pdl_enter();
+  __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+  __shared__ unsigned long long s_unit;
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = atomicAdd(next, 1ULL);
+    __syncthreads();
+    const unsigned long long u = s_unit;
+    __syncthreads(); /* every thread has read s_unit before thread 0 takes the next one */
+    if (u >= nunits) return;
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (items[mid].first <= u) lo = mid;
+      else hi = mid - 1;
+    }
+    const ClsItem& it = items[lo];
+    const unsigned long long r = u - it.first;
+    const unsigned bx = (unsigned)(r % it.nbx), by = (unsigned)((r / it.nbx) % it.nby);
+    const unsigned bz = (unsigned)(r / ((unsigned long long)it.nbx * it.nby));
+    const FieldDev F = it.F;
+    const SlabDev S = it.S;
+    if (F.is_f32) classify_brick<float>(F, S, it.codes, bx, by, bz, bits);
+    else classify_brick<double>(F, S, it.codes, bx, by, bz, bits);
   }
 }
 
@@ -2913,6 +2959,20 @@ int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S0, unsigned char
     else launch_k(k_classify<double>, "k_classify", grid, kClsX, 0, st, Fs[q], S, codes[q]);
   }
   return nf;
+}
+
+void classify_bricks(const FieldDev& F, const SlabDev& S, unsigned* nbx, unsigned* nby, unsigned* nbz) {
+  *nbx = (unsigned)((F.nx - 1 + kClsX - 1) / kClsX);
+  *nby = (unsigned)((F.ny - 1 + kClsY - 1) / kClsY);
+  *nbz = (unsigned)((S.nslices + S.cls_z - 1) / S.cls_z);
+}
+
+void launch_classify_queue(const ClsItem* items, int nitems, unsigned long long nunits, unsigned long long* next,
+                           cudaStream_t st) {
+  if (nitems < 1 || nunits == 0) return;
+  const unsigned long long cap = (unsigned long long)num_sms() * 8;
+  const unsigned grid = (unsigned)(nunits < cap ? nunits : cap);
+  launch_k(k_classify_queue, "k_classify_queue", grid, kClsX, 0, st, items, nitems, nunits, next);
 }
 
 long long scan_segments(long long n) { return (n + kScanTile - 1) / kScanTile; }

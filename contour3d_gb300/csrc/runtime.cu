@@ -560,6 +560,9 @@ struct ContourIn {
   conv_fn converter = nullptr;
   double threshold = 0.;
   contour3d_color_t color = {0, 0, 0};
+  /* the object's cell codes of the whole field, already classified (the
+     batched form classifies every frame in one launch), or null */
+  unsigned char *pre_codes = nullptr;
 };
 
 struct FrameIn {
@@ -1050,14 +1053,19 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     }
     slab_index++;
     /* the cell codes of every object of the slab, one pass over the field
-       for up to four objects */
-    std::vector<unsigned char *> obj_codes(nobj);
-    for (size_t q = 0; q < nobj; q++) obj_codes[q] = c.counts.as<unsigned char>() + code_stride * q;
-    last_codes = obj_codes;
+       for up to four objects -- or the codes the batch classified already,
+       when the slab is the whole field */
     codes_whole = S.kfirst == 0 && S.nslices == ncz;
+    bool pre = codes_whole && slabs.size() == 1;
+    for (size_t q = 0; q < nobj; q++) pre = pre && objs[q].pre_codes != nullptr;
+    std::vector<unsigned char *> obj_codes(nobj);
+    for (size_t q = 0; q < nobj; q++)
+      obj_codes[q] = pre ? objs[q].pre_codes : c.counts.as<unsigned char>() + code_stride * q;
+    last_codes = obj_codes;
     if (!async) C3D_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     if (c.stage_timing) cudaEventRecord(c.evs[0], st);
-    c.stats.kernel_launches += (uint64_t)launch_classify(Fo.data(), (int)nobj, S, obj_codes.data(), d_err, st);
+    if (!pre)
+      c.stats.kernel_launches += (uint64_t)launch_classify(Fo.data(), (int)nobj, S, obj_codes.data(), d_err, st);
     if (c.stage_timing) cudaEventRecord(c.evs[1], st);
     for (size_t ob = 0; ob < nobj; ob++) {
       const FieldDev &F = Fo[ob];
@@ -1459,7 +1467,7 @@ static bool graph_eligible(const Ctx &c, const FrameIn &f, const FrameOut &o) {
       !o.rgb_dev || c.filter_check || c.stage_timing)
     return false;
   for (const ContourIn &ci : f.contours)
-    if (!ci.on_device || !is_identity(ci.converter)) return false;
+    if (!ci.on_device || !is_identity(ci.converter) || ci.pre_codes) return false; /* codes of one batch */
   return true;
 }
 
@@ -2237,6 +2245,10 @@ struct Request {
   bool done = false;
   double device_ms = 0.;
   uint64_t held_bytes = 0;
+  /* per field of the frame, its codes classified by the batch (or null),
+     ready once pre_ev has completed */
+  std::vector<unsigned char *> pre_codes;
+  cudaEvent_t pre_ev = nullptr;
 };
 
 /* the part of a request's working set known before it runs: per slab the
@@ -2406,6 +2418,16 @@ static void worker_main(contour3d_gb300_server *sv, int slot) {
       }
       if (!rc) {
         f.stream = ctx.own_stream;
+        if (r->pre_ev && r->pre_codes.size() == f.contours.size()) {
+          /* the batch's classification of this frame's fields */
+          for (size_t n = 0; n < f.contours.size(); n++) f.contours[n].pre_codes = r->pre_codes[n];
+          if (cudaStreamWaitEvent(ctx.own_stream, r->pre_ev, 0) != cudaSuccess) {
+            log_error("waiting for the batch's classification failed");
+            rc = 1;
+          }
+        }
+      }
+      if (!rc) {
         FrameOut out;
         out.rgb_dev = fr->rgb_out;
         rc = render_frame(ctx, f, out);
@@ -2463,11 +2485,15 @@ extern "C" contour3d_gb300_server_t *contour3d_gb300_server_create(int slots, ui
   return sv;
 }
 
-extern "C" int contour3d_gb300_server_submit(contour3d_gb300_server_t *sv, const contour3d_gb300_frame_t *frame,
-                                             uint64_t *ticket) {
+static int server_submit(contour3d_gb300_server_t *sv, const contour3d_gb300_frame_t *frame, uint64_t *ticket,
+                         const std::vector<unsigned char *> *pre_codes, cudaEvent_t pre_ev) {
   if (!sv || !frame || !ticket) return 1;
   auto *r = new Request();
   r->frame = frame;
+  if (pre_codes && pre_ev) {
+    r->pre_codes = *pre_codes;
+    r->pre_ev = pre_ev;
+  }
   r->estimate = request_estimate(frame, kMaxSlabCells);
   r->t_submit = now_ms();
   {
@@ -2483,6 +2509,11 @@ extern "C" int contour3d_gb300_server_submit(contour3d_gb300_server_t *sv, const
   }
   sv->cv_work.notify_all();
   return 0;
+}
+
+extern "C" int contour3d_gb300_server_submit(contour3d_gb300_server_t *sv, const contour3d_gb300_frame_t *frame,
+                                             uint64_t *ticket) {
+  return server_submit(sv, frame, ticket, nullptr, nullptr);
 }
 
 extern "C" int contour3d_gb300_server_wait(contour3d_gb300_server_t *sv, uint64_t ticket,
@@ -2538,6 +2569,101 @@ extern "C" int contour3d_gb300_server_destroy(contour3d_gb300_server_t *sv) {
   return rc;
 }
 
+namespace c3d {
+
+static std::atomic<bool> g_batch_classify{true};
+
+/* the batch's classification: one persistent launch over (object, brick)
+   work items of every frame whose fields each take one slab */
+struct BatchCodes {
+  char *arena = nullptr;     /* device: the work counter, then 256-byte aligned code arrays */
+  ClsItem *items = nullptr;  /* device: the work items */
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::vector<std::vector<unsigned char *>> codes; /* per frame and field */
+  int nitems = 0;
+  unsigned long long units = 0;
+  ~BatchCodes() {
+    if (st) cudaStreamSynchronize(st);
+    if (items) cudaFree(items);
+    if (arena) cudaFree(arena);
+    if (ev) cudaEventDestroy(ev);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+static int batch_classify(const contour3d_gb300_frame_t *frames, size_t num_frames, BatchCodes &bc) {
+  std::vector<ClsItem> items;
+  std::vector<std::pair<size_t, size_t>> where; /* (frame, field) of each item */
+  std::vector<size_t> offs;
+  size_t bytes = 256; /* the work counter */
+  const int cls_z = launch_shape().cls_z;
+  bc.codes.assign(num_frames, {});
+  for (size_t q = 0; q < num_frames; q++) {
+    const contour3d_gb300_frame_t *fr = frames + q;
+    FrameIn f;
+    if (frame_from_fields(f, &fr->camera_position, &fr->light_direction, fr->screen_sizes, &fr->screen_center,
+                          fr->screen_local, &fr->bg_color, fr->num_fields, fr->fields, fr->num_lines, fr->lines)) {
+      cudaGetLastError();
+      continue; /* the worker reports the frame's error */
+    }
+    bc.codes[q].assign(f.contours.size(), nullptr);
+    for (size_t n = 0; n < f.contours.size(); n++) {
+      const ContourIn &ci = f.contours[n];
+      const long long nx = (long long)ci.sz[0], ny = (long long)ci.sz[1], nz = (long long)ci.sz[2];
+      if (nx < 2 || ny < 2 || nz < 4) continue;
+      const long long per_slice = (nx - 1) * (ny - 1), ncz = nz - 1;
+      /* the slab rule of the slab loop: the whole field in one slab */
+      if (3 * per_slice > kMaxSlabCells || kMaxSlabCells / per_slice - 2 < ncz - 2) continue;
+      ClsItem it;
+      memset(&it, 0, sizeof it);
+      it.F.data = ci.data;
+      it.F.is_f32 = ci.f32 ? 1 : 0;
+      it.F.nx = nx;
+      it.F.ny = ny;
+      it.F.nz = nz;
+      it.F.threshold = ci.threshold;
+      it.F.thr_key = h_key(ci.threshold);
+      it.F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
+      set_float_threshold(it.F);
+      it.S = SlabDev{0, ncz, 1, ncz - 1, cls_z};
+      classify_bricks(it.F, it.S, &it.nbx, &it.nby, &it.nbz);
+      it.first = bc.units;
+      bc.units += (unsigned long long)it.nbx * it.nby * it.nbz;
+      offs.push_back(bytes);
+      bytes += ((size_t)(per_slice * ncz) + 255) & ~(size_t)255;
+      items.push_back(it);
+      where.push_back({q, n});
+    }
+  }
+  if (items.empty()) return 1;
+  if (cudaMalloc(&bc.arena, bytes) != cudaSuccess || cudaMalloc(&bc.items, sizeof(ClsItem) * items.size()) != cudaSuccess) {
+    cudaGetLastError();
+    log_error("batch classification: device allocation of %zu bytes failed", bytes);
+    return 1;
+  }
+  for (size_t t = 0; t < items.size(); t++) {
+    items[t].codes = reinterpret_cast<unsigned char *>(bc.arena + offs[t]);
+    bc.codes[where[t].first][where[t].second] = items[t].codes;
+  }
+  bc.nitems = (int)items.size();
+  C3D_CUDA(cudaStreamCreateWithFlags(&bc.st, cudaStreamNonBlocking));
+  C3D_CUDA(cudaEventCreateWithFlags(&bc.ev, cudaEventDisableTiming));
+  C3D_CUDA(cudaMemcpyAsync(bc.items, items.data(), sizeof(ClsItem) * items.size(), cudaMemcpyHostToDevice, bc.st));
+  C3D_CUDA(cudaMemsetAsync(bc.arena, 0, sizeof(unsigned long long), bc.st));
+  launch_classify_queue(bc.items, bc.nitems, bc.units, reinterpret_cast<unsigned long long *>(bc.arena), bc.st);
+  C3D_CUDA(cudaGetLastError());
+  C3D_CUDA(cudaEventRecord(bc.ev, bc.st));
+  return 0;
+}
+
+}  // namespace c3d
+
+extern "C" int contour3d_gb300_set_batch_classify(int on) {
+  g_batch_classify = on != 0;
+  return 0;
+}
+
 extern "C" int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frames, size_t num_frames, int workers,
                                             double *frame_ms) {
   if (num_frames && !frames) return 1;
@@ -2554,9 +2680,16 @@ extern "C" int contour3d_gb300_render_batch(const contour3d_gb300_frame_t *frame
     est[n] = request_estimate(frames + n, kMaxSlabCells);
   }
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return est[a] > est[b]; });
+  /* every frame's classification first, in one launch; the frames' slab
+     passes wait for it on their own streams */
+  BatchCodes bc;
+  const bool pre = g_batch_classify && num_frames > 0 && batch_classify(frames, num_frames, bc) == 0;
   std::vector<uint64_t> tickets(num_frames);
   int rc = 0;
-  for (size_t q = 0; q < num_frames; q++) rc |= contour3d_gb300_server_submit(sv, frames + order[q], &tickets[order[q]]);
+  for (size_t q = 0; q < num_frames; q++) {
+    const size_t n = order[q];
+    rc |= server_submit(sv, frames + n, &tickets[n], pre ? &bc.codes[n] : nullptr, pre ? bc.ev : nullptr);
+  }
   for (size_t n = 0; n < num_frames; n++) {
     contour3d_gb300_request_stats_t st;
     rc |= contour3d_gb300_server_wait(sv, tickets[n], &st);

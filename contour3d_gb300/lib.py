@@ -112,7 +112,7 @@ EXPORTS = [
     "contour3d_gb300_render", "contour3d_gb300_render_device", "contour3d_gb300_last_stats",
     "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells", "contour3d_gb300_set_filter_check",
     "contour3d_gb300_set_async", "contour3d_gb300_set_server_async", "contour3d_gb300_set_graphs", "contour3d_gb300_set_launch_shape",
-    "contour3d_gb300_set_dependent_launch",
+    "contour3d_gb300_set_dependent_launch", "contour3d_gb300_set_batch_classify",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
     "contour3d_gb300_cell_offsets_noalloc", "contour3d_gb300_render_batch", "contour3d_gb300_server_create",
@@ -267,6 +267,9 @@ class Library:
 
     def set_dependent_launch(self, on: bool) -> None:
         self.lib.contour3d_gb300_set_dependent_launch(1 if on else 0)
+
+    def set_batch_classify(self, on: bool) -> None:
+        self.lib.contour3d_gb300_set_batch_classify(1 if on else 0)
 
     def set_launch_shape(self, classify_slices: int, emit_blocks_per_sm: int, raster_blocks_per_sm: int) -> None:
         if self.lib.contour3d_gb300_set_launch_shape(int(classify_slices), int(emit_blocks_per_sm),

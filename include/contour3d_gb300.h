@@ -284,6 +284,14 @@ int contour3d_gb300_set_launch_shape(int classify_slices, int emit_blocks_per_sm
  * ordinary stream order.
  */
 int contour3d_gb300_set_dependent_launch(int on);
+/*
+ * 1 (default) = contour3d_gb300_render_batch classifies the cells of every
+ * frame whose fields each fit one slab in one persistent launch over
+ * (field, brick) work items taken from a device counter, before the frames'
+ * own passes; 0 = each frame classifies its own fields.  Images do not
+ * depend on it.
+ */
+int contour3d_gb300_set_batch_classify(int on);
 /* upper bound on cells per slab (default and maximum 178,956,970, the most the
    scan's packed 32-bit sums allow); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);

@@ -33,14 +33,19 @@ def _single(gpu, fields, spec):
     return out.cpu().numpy()
 
 
-def test_batch_matches_single_frames(gpu):
+@pytest.mark.parametrize("batch_classify", [True, False], ids=["one-classify-launch", "per-frame-classify"])
+def test_batch_matches_single_frames(gpu, batch_classify):
     import torch
     fields, frames = _small_set(gpu)
     ref = [_single(gpu, fields, s) for s in frames]
     outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
     packs = [workloads.frame_pack(gpu, fields[s.field], s, o) for s, o in zip(frames, outs)]
-    ms = gpu.render_batch(packs, workers=3)
-    torch.cuda.synchronize()
+    gpu.set_batch_classify(batch_classify)
+    try:
+        ms = gpu.render_batch(packs, workers=3)
+        torch.cuda.synchronize()
+    finally:
+        gpu.set_batch_classify(True)
     assert len(ms) == len(frames) and all(m > 0 for m in ms)
     for a, o in zip(ref, outs):
         assert np.array_equal(a, o.cpu().numpy())
