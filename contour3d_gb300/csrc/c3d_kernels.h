@@ -88,6 +88,7 @@ int set_launch_shape(const LaunchShape& s);
 LaunchShape launch_shape();
 /* programmatic dependent launch of the library's kernels on (1) or off (0) */
 void set_dependent_launch(int on);
+int dependent_launch();
 
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {
@@ -191,6 +192,7 @@ struct LineSegDev {
 
 /* device error flags */
 constexpr unsigned kErrClassifyTimeout = 2u;
+constexpr unsigned kErrScanTimeout = 4u;
 
 int upload_tables(const unsigned char code_count[256], const signed char nb[19][4][4],
                   const unsigned char nb_count[19], const unsigned short edge_tris[256 * 19]);
@@ -216,36 +218,42 @@ struct CodeOut {
    Returns the number of kernels launched. */
 int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, unsigned* err,
                     cudaStream_t st);
-/* one object's classification in a batch: its field and slab, its code
-   array, its bricks (kClsX x kClsY cells x S.cls_z slices) and the number of
-   its first brick among all items' bricks */
+/* one field's classification in a batch, for up to kMaxThr objects: its
+   values and sizes, the slab, the thresholds and code arrays, its bricks
+   (kClsX x kClsY cells x S.cls_z slices) and the number of its first brick
+   among all items' bricks */
 struct ClsItem {
-  FieldDev F;
+  const void* data;
+  int is_f32;
+  long long nx, ny;
   SlabDev S;
-  unsigned char* codes;
+  ThrSet ts;
+  CodeOut out;
   unsigned nbx, nby, nbz;
   unsigned long long first;
 };
-/* the bricks of a classification along x, y and z */
-void classify_bricks(const FieldDev& F, const SlabDev& S, unsigned* nbx, unsigned* nby, unsigned* nbz);
+/* the item of objects Fs[0..nf) (one field, nf <= kMaxThr) over slab S */
+void make_cls_item(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, ClsItem* it);
 /* every item's codes in one persistent launch; `next` (device) must start at 0 */
 void launch_classify_queue(const ClsItem* items, int nitems, unsigned long long nunits, unsigned long long* next,
                            cudaStream_t st);
 /* cells per slab for which the packed triangle and vertex sums of the scan stay below 2^31 */
 constexpr long long kMaxSlabCells = 178956970;
 
-/* segments of the scan over n cells */
-long long scan_segments(long long n);
-/* voffsets[0..n], totals = (triangles, vertices), offsets[n]; the
-   triangle -> cell map when the triangles fit tri_cap, and offsets[0..n - 1]
-   when want_offsets or when they do not.  seg_sums and
-   seg_base hold scan_segments(n) entries each */
-void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
-                 unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
-                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, unsigned* ovf, cudaStream_t st);
+/* 64-bit words of the scan's look-back state over n cells (one per segment
+   of cells, then the segment ticket counter) */
+long long scan_state_words(long long n);
+/* voffsets[0..n], totals = (triangles, vertices), offsets[n], and
+   offsets[0..n - 1] when want_offsets; the triangle -> cell map where the
+   triangles fit tri_cap (where they do not, `ovf`, when given, receives
+   kOvfTriangles: the caller scans again with a larger map).  `state` holds
+   scan_state_words(n) words (zeroed here); `err` receives kErrScanTimeout. */
+cudaError_t launch_scan(const unsigned char* codes, long long n, unsigned long long* state, unsigned* offsets,
+                        unsigned* voffsets, unsigned long long* totals, unsigned* tri_cell,
+                        unsigned long long tri_cap, bool want_offsets, unsigned* ovf, unsigned* err,
+                        cudaStream_t st);
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
-void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets, const unsigned* voffsets,
                  const unsigned* tri_cell, const unsigned long long* total, long long tri_bound, const TriDev& tri,

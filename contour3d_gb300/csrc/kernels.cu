@@ -7,11 +7,9 @@
  *                   field (TMA node planes; k_classify where TMA cannot
  *                   address the field)                         (HBM: field read)
  * per slab of an object:
- *   k_seg_reduce, k_seg_scan, k_scan_write
- *                   packed (triangle, vertex) counts per segment, a one-block
- *                   scan of the segments, then every cell's offsets and the
- *                   triangle -> cell map (no block waits on another;
- *                   k_fill_tri_cell when the map is filled afterwards)
+ *   k_scan          packed (triangle, vertex) counts per segment of cells,
+ *                   the segment's prefix by decoupled look-back, then every
+ *                   cell's offsets and the triangle -> cell map, in one pass
  *   k_vertices      one FP32 screen vertex per crossed edge, with certified
  *                   bounds (two FP64 subtractions per vertex)
  *   k_emit          one thread per triangle: its three vertices through their
@@ -64,6 +62,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 #include <cuda/atomic>
 #include "c3d_common.cuh"
 #include "c3d_kernels.h"
@@ -133,9 +132,7 @@ __device__ __forceinline__ void cell_ijk(const FieldDev& F, unsigned c, unsigned
  * from its corner 0 that the iso-level crosses), packed as tri | vert << 31:
  * every sum over a slab stays below 2^31 in both fields for slabs of at most
  * kMaxSlabCells cells, so packed additions never carry.  The scan runs over
- * segments of kScanTile cells: k_seg_reduce sums each segment, k_seg_scan
- * turns the sums into segment offsets, and k_scan_write writes every cell's
- * offsets from them -- no block waits on another.
+ * segments of kScanTile cells, one block each (k_scan).
  *
  * Vertices are owned by cells: cell c owns the crossed edges that start at
  * its corner 0 and run to corner m = 1..7 (+x, +y, +x+y, +z, +x+z, +y+z,
@@ -265,40 +262,164 @@ __global__ void __launch_bounds__(kClsX) k_classify(FieldDev F, SlabDev S, unsig
 }
 
 /*
- * k_classify_queue: the cell codes of many objects' fields (the frames of a
- * batch) in one launch of a persistent grid.  The work items are (object,
- * brick) pairs numbered object by object (ClsItem::first); each block takes
- * the next item number from a device counter, finds its object by binary
- * search over the items' first numbers, and classifies that brick.  Every
- * item number is taken once, so the loop ends after at most nunits / grid
- * items per block.
+ * k_classify_queue: the cell codes of many fields (the frames of a batch) in
+ * one launch of a persistent grid.  A work item is one field with up to
+ * kMaxThr thresholds; its bricks are numbered item by item
+ * (ClsItem::first).  Each block takes the next brick number from a device
+ * counter, finds its item by binary search over the items' first numbers,
+ * and classifies that brick for all of the item's thresholds in one pass
+ * over its nodes.  A node's values of the next plane are loaded into
+ * registers before the current plane pair is turned into codes, so the
+ * loads are in flight during that work.  Node masks hold bit t for
+ * threshold t; a cell's code for threshold t gathers bit t of its eight
+ * corner masks with one multiply (the corner masks as the bytes of a 64-bit
+ * word: bit t of byte c moves to bit c of the top byte).  Every brick number
+ * is taken once, so the loop ends after at most nunits / grid bricks per
+ * block.
  */
-__global__ void __launch_bounds__(kClsX)
+constexpr int kQPlane = (kClsY + 1) * (kClsX + 1); /* nodes of a brick's plane */
+constexpr int kQPer = (kQPlane + kClsX - 1) / kClsX; /* of them per thread */
+
+/* what a block keeps of its current item, in shared memory */
+struct QueueBrick {
+  const void* data;
+  unsigned char* codes[kMaxThr];
+  long long nx, ny, kfirst, k0, k1;
+  unsigned i0, j0, ncx, ncy;
+  int nt;
+};
+
+template <typename T>
+__device__ __forceinline__ void classify_queue_brick(const QueueBrick& qb, const ThrSet& ts,
+                                                     unsigned char (*bits)[kClsY + 1][kClsX + 1]) {
+  using K = typename NodeBits<T>::type;
+  const K* __restrict__ f = static_cast<const K*>(qb.data);
+  const long long nx = qb.nx, ny = qb.ny, sxy = nx * ny;
+  const unsigned i0 = qb.i0, j0 = qb.j0, ncx = qb.ncx, ncy = qb.ncy;
+  const long long k0 = qb.k0, k1 = qb.k1, kfirst = qb.kfirst;
+  const int nt = qb.nt;
+  /* the thresholds as key ranges (see ThrSet) */
+  unsigned long long tlo[kMaxThr], tcnt[kMaxThr];
+#pragma unroll
+  for (int t = 0; t < kMaxThr; t++) {
+    tlo[t] = sizeof(T) == 8 ? ts.lo[t] : ts.flo[t];
+    tcnt[t] = t < nt ? (sizeof(T) == 8 ? ts.cnt[t] : ts.fcnt[t]) : 0ULL;
+  }
+  K v[kQPer];
+  unsigned valid = 0;
+  auto fetch = [&](long long k) {
+    valid = 0;
+#pragma unroll
+    for (int r = 0; r < kQPer; r++) {
+      const int q = threadIdx.x + r * kClsX;
+      const unsigned jj = (unsigned)q / (kClsX + 1), ii = (unsigned)q - jj * (kClsX + 1);
+      const long long gi = (long long)i0 + ii, gj = (long long)j0 + jj;
+      const bool ok = q < kQPlane && gi < nx && gj < ny;
+      v[r] = ok ? __ldg(f + k * sxy + gj * nx + gi) : K(0);
+      valid |= (unsigned)ok << r;
+    }
+  };
+  auto store = [&](int buf) {
+    unsigned char* dst = &bits[buf][0][0];
+#pragma unroll
+    for (int r = 0; r < kQPer; r++) {
+      const int q = threadIdx.x + r * kClsX;
+      if (q < kQPlane) {
+        unsigned m = 0;
+        if ((valid >> r) & 1u) {
+          /* sign-folded key, then one unsigned range check per threshold */
+          const K b = v[r];
+          const K key = b ^ (K)((typename std::make_unsigned<K>::type)(b >> (8 * sizeof(K) - 1)) >> 1);
+#pragma unroll
+          for (int t = 0; t < kMaxThr; t++) {
+            if (sizeof(T) == 8)
+              m |= (unsigned)((unsigned long long)key - tlo[t] < tcnt[t]) << t;
+            else
+              m |= (unsigned)((unsigned)key - (unsigned)tlo[t] < (unsigned)tcnt[t]) << t;
+          }
+        }
+        dst[q] = (unsigned char)m;
+      }
+    }
+  };
+  fetch(kfirst + k0);
+  store(0);
+  fetch(kfirst + k0 + 1);
+  const unsigned i = i0 + threadIdx.x;
+  const bool in_x = i < ncx;
+  const int tx = threadIdx.x;
+  for (long long kl = k0; kl < k1; kl++) {
+    const int cur = (int)((kl - k0) & 1), nxt = cur ^ 1;
+    store(nxt); /* node plane kl + 1 */
+    __syncthreads();
+    if (kl + 1 < k1) fetch(kfirst + kl + 2);
+#pragma unroll
+    for (int jj = 0; jj < kClsY; jj++) {
+      const unsigned j = j0 + jj;
+      if (j >= ncy) break; /* the same for the whole block */
+      const unsigned lo = (unsigned)bits[cur][jj][tx] | ((unsigned)bits[cur][jj][tx + 1] << 8) |
+                          ((unsigned)bits[cur][jj + 1][tx] << 16) | ((unsigned)bits[cur][jj + 1][tx + 1] << 24);
+      const unsigned hi = (unsigned)bits[nxt][jj][tx] | ((unsigned)bits[nxt][jj][tx + 1] << 8) |
+                          ((unsigned)bits[nxt][jj + 1][tx] << 16) | ((unsigned)bits[nxt][jj + 1][tx + 1] << 24);
+      const unsigned long long w = (unsigned long long)lo | ((unsigned long long)hi << 32);
+      const size_t at = ((size_t)kl * ncy + j) * ncx + i;
+#pragma unroll
+      for (int t = 0; t < kMaxThr; t++) {
+        if (t < nt && in_x) {
+          const unsigned code = (unsigned)((((w >> t) & 0x0101010101010101ULL) * 0x0102040810204080ULL) >> 56);
+          qb.codes[t][at] = (unsigned char)code;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kClsX, 6)
 k_classify_queue(const ClsItem* __restrict__ items, int nitems, unsigned long long nunits,
                  unsigned long long* __restrict__ next) {
   pdl_enter();
   __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+  __shared__ QueueBrick s_qb;
+  __shared__ ThrSet s_ts;
+  __shared__ int s_item;
   __shared__ unsigned long long s_unit;
   for (;;) {
-    if (threadIdx.x == 0) s_unit = atomicAdd(next, 1ULL);
-    __syncthreads();
-    const unsigned long long u = s_unit;
-    __syncthreads(); /* every thread has read s_unit before thread 0 takes the next one */
-    if (u >= nunits) return;
-    int lo = 0, hi = nitems - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (items[mid].first <= u) lo = mid;
-      else hi = mid - 1;
+    if (threadIdx.x == 0) {
+      const unsigned long long u = atomicAdd(next, 1ULL);
+      s_unit = u;
+      if (u < nunits) {
+        int lo = 0, hi = nitems - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (items[mid].first <= u) lo = mid;
+          else hi = mid - 1;
+        }
+        const ClsItem& it = items[lo];
+        const unsigned long long r = u - it.first;
+        const unsigned bx = (unsigned)(r % it.nbx), by = (unsigned)((r / it.nbx) % it.nby);
+        const unsigned bz = (unsigned)(r / ((unsigned long long)it.nbx * it.nby));
+        s_item = lo;
+        s_qb.data = it.data;
+        for (int t = 0; t < kMaxThr; t++) s_qb.codes[t] = it.out.codes[t];
+        s_qb.nx = it.nx;
+        s_qb.ny = it.ny;
+        s_qb.kfirst = it.S.kfirst;
+        s_qb.k0 = (long long)bz * it.S.cls_z;
+        s_qb.k1 = min(s_qb.k0 + it.S.cls_z, it.S.nslices);
+        s_qb.i0 = bx * kClsX;
+        s_qb.j0 = by * kClsY;
+        s_qb.ncx = (unsigned)(it.nx - 1);
+        s_qb.ncy = (unsigned)(it.ny - 1);
+        s_qb.nt = it.ts.n;
+        s_ts = it.ts;
+      }
     }
-    const ClsItem& it = items[lo];
-    const unsigned long long r = u - it.first;
-    const unsigned bx = (unsigned)(r % it.nbx), by = (unsigned)((r / it.nbx) % it.nby);
-    const unsigned bz = (unsigned)(r / ((unsigned long long)it.nbx * it.nby));
-    const FieldDev F = it.F;
-    const SlabDev S = it.S;
-    if (F.is_f32) classify_brick<float>(F, S, it.codes, bx, by, bz, bits);
-    else classify_brick<double>(F, S, it.codes, bx, by, bz, bits);
+    __syncthreads();
+    if (s_unit >= nunits) return;
+    if (items[s_item].is_f32) classify_queue_brick<float>(s_qb, s_ts, bits);
+    else classify_queue_brick<double>(s_qb, s_ts, bits);
+    /* the brick ends with a barrier: thread 0 may overwrite s_qb */
   }
 }
 
@@ -476,8 +597,6 @@ k_classify_tma(const __grid_constant__ CUtensorMap tmap, FieldDev F, SlabDev S, 
 /* ------------------------------------------------------------------ */
 /* the scan: segment offsets, then every cell's offsets                 */
 /* ------------------------------------------------------------------ */
-constexpr int kSegScanThreads = 1024;
-
 /* the thread's kScanItems codes, 4 per word (a code past the end reads as 0:
    no triangles, no vertices) */
 __device__ __forceinline__ void load_scan_codes(const unsigned char* __restrict__ codes, long long base, long long n,
@@ -505,121 +624,126 @@ __device__ __forceinline__ void load_scan_codes(const unsigned char* __restrict_
   }
 }
 
-/* one block per segment: its packed total */
-__global__ void __launch_bounds__(kScanThreads)
-k_seg_reduce(const unsigned char* __restrict__ codes, long long n, unsigned long long* __restrict__ seg_sums) {
-  pdl_enter();
-  __shared__ unsigned s_cnt[256];
-  __shared__ unsigned long long s_warp[kScanThreads / 32];
-  unsigned wv[kScanItems / 4];
-  /* the codes are in flight while the count table is built */
-  load_scan_codes(codes, (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems, n, wv);
-  load_count_lut(s_cnt);
-  __syncthreads();
-  /* a thread's 32 cells hold at most 384 triangles and 224 vertices: their
-     sum fits the 16-bit fields of the table entries */
-  unsigned s32 = 0;
-#pragma unroll
-  for (int q = 0; q < kScanItems; q++) s32 += s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
-  unsigned long long sum = packed_count(s32);
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
-  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = sum;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long t = 0;
-#pragma unroll
-    for (int w = 0; w < kScanThreads / 32; w++) t += s_warp[w];
-    seg_sums[blockIdx.x] = t;
-  }
+/*
+ * The scan in one pass with decoupled look-back (Merrill and Garland,
+ * "Single-pass Parallel Prefix Scan with Decoupled Look-back", NVIDIA
+ * technical report NVR-2016-002).  Segment s's state word holds a packed
+ * (triangle, vertex) sum in bits 0-61 and a status in bits 62-63: 1 = the
+ * segment's own total, 2 = the total of segments 0..s.  A block takes the
+ * next segment number from a ticket counter (the word after the states), so
+ * every segment it waits for belongs to a block that is already running and
+ * publishes its own total without waiting on anyone.  Warp 0 then walks back
+ * 32 states at a time, adding own totals until it meets an inclusive one.
+ * The walk is bounded: after kScanWaitLimit rounds the block records
+ * kErrScanTimeout and goes on with what it has; its writes stay inside their
+ * buffers whatever the prefix (the map is written only where it fits).
+ */
+constexpr unsigned long long kStAgg = 1ULL << 62, kStIncl = 2ULL << 62, kStValue = (1ULL << 62) - 1;
+constexpr int kScanWaitLimit = 1 << 20;
+
+__device__ __forceinline__ unsigned long long ld_state(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_state(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-/* exclusive scan of the segment totals (one block); writes the slab totals
-   (triangles, vertices) and the end entries offsets[n], voffsets[n] */
-__global__ void __launch_bounds__(kSegScanThreads)
-k_seg_scan(const unsigned long long* __restrict__ seg_sums, long long nseg, unsigned long long* __restrict__ seg_base,
-           long long n, unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
-           unsigned long long* __restrict__ totals) {
-  pdl_enter();
-  __shared__ unsigned long long s_warp[kSegScanThreads / 32];
-  const long long per = (nseg + kSegScanThreads - 1) / kSegScanThreads;
-  const long long a = min(nseg, (long long)threadIdx.x * per), b = min(nseg, a + per);
-  unsigned long long sum = 0;
-  for (long long q = a; q < b; q++) sum += seg_sums[q];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long incl = sum;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-    if (lane >= d) incl += y;
-  }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    unsigned long long w = s_warp[lane];
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, d);
-      if (lane >= d) w += y;
+/* the exclusive prefix of segment seg >= 1 (warp 0; every lane returns it) */
+__device__ __forceinline__ unsigned long long look_back(const unsigned long long* state, long long seg,
+                                                        unsigned* err) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long prefix = 0;
+  long long p = seg - 1; /* the nearest state not yet added */
+  for (int rounds = 0;;) {
+    const long long q = p - lane;
+    const unsigned long long v = q >= 0 ? ld_state(state + q) : kStIncl; /* before segment 0: an inclusive 0 */
+    const unsigned stt = (unsigned)(v >> 62);
+    if (__any_sync(0xFFFFFFFFu, stt == 0)) {
+      if (++rounds > kScanWaitLimit) {
+        if (lane == 0) atomicOr(err, kErrScanTimeout);
+        break;
+      }
+      __nanosleep(64);
+      continue;
     }
-    s_warp[lane] = w; /* inclusive per warp */
+    const unsigned incl = __ballot_sync(0xFFFFFFFFu, stt == 2);
+    const int stop = incl ? __ffs(incl) - 1 : 31; /* lanes 0..stop are added */
+    unsigned long long x = lane <= stop ? (v & kStValue) : 0ULL;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, d);
+    prefix += x;
+    if (incl) break;
+    p -= 32;
   }
-  __syncthreads();
-  unsigned long long run = (warp ? s_warp[warp - 1] : 0ULL) + incl - sum;
-  for (long long q = a; q < b; q++) {
-    seg_base[q] = run;
-    run += seg_sums[q];
-  }
-  if (threadIdx.x == kSegScanThreads - 1) {
-    const unsigned long long tot = s_warp[kSegScanThreads / 32 - 1];
-    totals[0] = tot & kTriMask;
-    totals[1] = tot >> 31;
-    offsets[n] = (unsigned)(tot & kTriMask);
-    voffsets[n] = (unsigned)(tot >> 31);
-  }
+  return prefix;
 }
 
 /*
- * One block per segment: every cell's triangle and vertex offsets (the
- * segment's base plus a block-wide exclusive scan), and, when the slab's
- * triangles fit `tri_cap`, the triangle -> cell map.
+ * One block per segment: the segment's sum, its prefix by look-back, every
+ * cell's vertex offsets (and triangle offsets when asked for), and the
+ * segment's part of the triangle -> cell map when it fits tri_cap.  A thread
+ * owns 32 consecutive cells; its offsets go through a per-warp shared-memory
+ * stage (rows of kStagePitch words) so that every global store of a warp
+ * covers 128 contiguous bytes.  The stage holds offsets relative to the
+ * segment, so warps 1.. fill it while warp 0 looks back; the prefix is added
+ * as the stage is stored.  The map goes through a shared list of the
+ * segment's triangles when they fit it (positions relative to the segment,
+ * then a coalesced copy), else it is written directly once the prefix is
+ * known.  The block of the last segment writes the slab totals and the end
+ * entries offsets[n], voffsets[n].
  */
 constexpr int kFillList = 8192; /* triangles of a segment listed in shared memory (4 blocks per SM) */
 constexpr int kStagePitch = 33;  /* words per staged row: conflict-free transposes */
 constexpr size_t kScanWriteSmem =
     sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch + sizeof(unsigned short) * kFillList;
 
-/*
- * One block per segment: every cell's triangle and vertex offsets (the
- * segment's base plus a block-wide exclusive scan), and, when the slab's
- * triangles fit `tri_cap`, the triangle -> cell map.  A thread owns 32
- * consecutive cells; its offsets go through a per-warp shared-memory stage
- * (rows of kStagePitch words) so that every global store of a warp covers
- * 128 contiguous bytes.  The map goes through a shared list of the segment's
- * triangles when they fit it (then coalesced), else directly.
- */
+/* a warp's 1024 staged values plus `add` into dst[wbase ..] (cells past n are skipped) */
+__device__ __forceinline__ void store_stage(unsigned* __restrict__ dst, const unsigned* stage, long long wbase,
+                                            long long n, unsigned add) {
+  const int lane = threadIdx.x & 31;
+  if (wbase + 32 * kScanItems <= n) {
+    /* each store instruction writes 512 contiguous bytes (lane L: cells
+       4L .. 4L + 3 of a 128-cell chunk, all in one staged row; wbase is a
+       multiple of 1024, dst 256-byte aligned) */
+#pragma unroll 4
+    for (int k = 0; k < 8; k++) {
+      const int e = 128 * k + 4 * lane, row = e >> 5, col = e & 31;
+      const unsigned* sr = stage + kStagePitch * row + col;
+      reinterpret_cast<uint4*>(dst + wbase)[32 * k + lane] =
+          make_uint4(sr[0] + add, sr[1] + add, sr[2] + add, sr[3] + add);
+    }
+  } else {
+    for (int k = 0; k < 32; k++) {
+      const long long c = wbase + 32 * k + lane;
+      if (c < n) dst[c] = stage[kStagePitch * k + lane] + add;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kScanThreads, 4)
-k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigned long long* __restrict__ seg_base,
-             unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets,
-             const unsigned long long* __restrict__ totals, unsigned* __restrict__ tri_cell,
-             unsigned long long tri_cap, int want_offsets, unsigned* __restrict__ ovf) {
+k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, unsigned long long* __restrict__ state,
+       unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets, unsigned long long* __restrict__ totals,
+       unsigned* __restrict__ tri_cell, unsigned long long tri_cap, int want_offsets, unsigned* __restrict__ ovf,
+       unsigned* __restrict__ err) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char scan_smem[];
   __shared__ unsigned long long s_warp[kScanThreads / 32];
   __shared__ unsigned s_cnt[256];
+  __shared__ unsigned long long s_prefix;
+  __shared__ unsigned s_seg;
   unsigned* stage_all = reinterpret_cast<unsigned*>(scan_smem);
   unsigned short* s_list = /* segment-local cell of each of the segment's triangles */
       reinterpret_cast<unsigned short*>(scan_smem + sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch);
-  const long long c0 = (long long)blockIdx.x * kScanTile;
-  const long long base = c0 + (long long)threadIdx.x * kScanItems;
-  unsigned wv[kScanItems / 4];
-  /* the codes, the segment base and the slab total are in flight while the
-     count table is built */
-  load_scan_codes(codes, base, n, wv);
-  const unsigned long long seg0 = seg_base[blockIdx.x];
-  const unsigned long long slab_tris = totals[0];
+  if (threadIdx.x == 0) s_seg = (unsigned)atomicAdd(state + nseg, 1ULL);
   load_count_lut(s_cnt);
   __syncthreads();
+  const long long seg = s_seg;
+  const long long c0 = seg * kScanTile;
+  const long long base = c0 + (long long)threadIdx.x * kScanItems;
+  unsigned wv[kScanItems / 4];
+  load_scan_codes(codes, base, n, wv);
   /* per-thread sums in the 16-bit fields of the table entries (at most 384
      triangles and 224 vertices in a thread's 32 cells) */
   unsigned s32 = 0;
@@ -643,75 +767,82 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
       if (lane >= d) w += y;
     }
     if (lane < kScanThreads / 32) s_warp[lane] = w;
+    /* the segment's own total goes out at once */
+    const unsigned long long agg = __shfl_sync(0xFFFFFFFFu, w, kScanThreads / 32 - 1);
+    if (lane == 0) st_state(state + seg, (seg == 0 ? kStIncl : kStAgg) | agg);
   }
   __syncthreads();
-  const unsigned long long first = seg0 + (warp ? s_warp[warp - 1] : 0ULL) + incl - sum;
-  const unsigned seg_tris = (unsigned)(s_warp[kScanThreads / 32 - 1] & kTriMask);
-  const unsigned ta = (unsigned)(seg0 & kTriMask);
-  const bool fill = slab_tris <= tri_cap;
-  /* a map that does not fit: the host fills it afterwards, or, when the
-     buffers were sized before the count was known (ovf given), renders the
-     frame again with a larger map */
-  if (!fill && ovf && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(ovf, kOvfTriangles);
-  const bool listed = fill && seg_tris <= (unsigned)kFillList;
-  const bool direct = fill && !listed;
-  /* the triangle offsets are kept only when asked for or when the map must
-     be filled from them afterwards */
-  const bool keep_offsets = want_offsets || !fill;
-  unsigned* stage = stage_all + warp * 32 * kStagePitch;
-  const long long wbase = c0 + (long long)warp * 32 * kScanItems; /* the warp's first cell */
-  if (listed) {
+  const unsigned long long agg = s_warp[kScanThreads / 32 - 1];
+  const unsigned seg_tris = (unsigned)(agg & kTriMask);
+  /* the thread's first offsets relative to the segment (both below 2^31) */
+  const unsigned long long rel = (warp ? s_warp[warp - 1] : 0ULL) + incl - sum;
+  const unsigned rel_t = (unsigned)(rel & kTriMask), rel_v = (unsigned)(rel >> 31);
+  const bool can_list = seg_tris <= (unsigned)kFillList;
+  if (can_list) {
     /* the shared list: each cell writes its first triangle's slot only; the
        other slots stay marked and find their cell by walking back */
     for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) s_list[e] = 0xFFFFu;
     __syncthreads();
   }
-  /* the thread's first offsets (both below 2^31), then 32-bit running sums
-     in the table entries' 16-bit fields */
-  const unsigned first_t = (unsigned)(first & kTriMask), first_v = (unsigned)(first >> 31);
-  for (int half = 1; half >= 0; half--) {
-    /* half 1: vertex offsets; half 0: triangle offsets (staged only when
-       they are stored) and the map */
+  unsigned* stage = stage_all + warp * 32 * kStagePitch;
+  const long long wbase = c0 + (long long)warp * 32 * kScanItems; /* the warp's first cell */
+  /* the vertex offsets (relative) and the list; warp 0 first looks back */
+  auto fill_stage = [&]() {
     unsigned run = 0;
 #pragma unroll
     for (int q = 0; q < kScanItems; q++) {
       const unsigned cnt = s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
-      const unsigned t0 = first_t + (run & 0xFFFFu);
-      if (half == 1 || keep_offsets) stage[kStagePitch * lane + q] = half == 0 ? t0 : first_v + (run >> 16);
-      if (half == 0 && (listed || direct) && base + q < n) {
-        const unsigned nt = cnt & 0xFFFFu;
-        if (listed) {
-          if (nt) s_list[t0 - ta] = (unsigned short)(base + q - c0);
-        } else {
-          for (unsigned r = 0; r < nt; r++) tri_cell[t0 + r] = (unsigned)(base + q) | (r << kTcRankShift);
-        }
+      stage[kStagePitch * lane + q] = rel_v + (run >> 16);
+      if (can_list && (cnt & 0xFFFFu) && base + q < n)
+        s_list[rel_t + (run & 0xFFFFu)] = (unsigned short)(base + q - c0);
+      run += cnt;
+    }
+  };
+  if (warp == 0) {
+    unsigned long long prefix = 0;
+    if (seg > 0) {
+      prefix = look_back(state, seg, err);
+      if (lane == 0) st_state(state + seg, kStIncl | ((prefix + agg) & kStValue));
+    }
+    if (lane == 0) {
+      s_prefix = prefix;
+      if (seg == nseg - 1) {
+        const unsigned long long tot = prefix + agg;
+        totals[0] = tot & kTriMask;
+        totals[1] = tot >> 31;
+        offsets[n] = (unsigned)(tot & kTriMask);
+        voffsets[n] = (unsigned)(tot >> 31);
       }
+    }
+  }
+  fill_stage();
+  __syncthreads();
+  const unsigned long long seg0 = s_prefix;
+  const unsigned ta = (unsigned)(seg0 & kTriMask);
+  store_stage(voffsets, stage, wbase, n, (unsigned)(seg0 >> 31));
+  const bool fill = (unsigned long long)ta + seg_tris <= tri_cap;
+  /* a map that does not fit: the caller runs the scan again with a larger
+     map, or, when the buffers were sized before the count was known (ovf
+     given), renders the frame again */
+  if (!fill && ovf && threadIdx.x == 0) atomicOr(ovf, kOvfTriangles);
+  if (want_offsets || (fill && !can_list)) {
+    /* triangle offsets (inspection) and the direct map: the prefix is known */
+    __syncwarp();
+    unsigned run = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; q++) {
+      const unsigned cnt = s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
+      const unsigned t0 = ta + rel_t + (run & 0xFFFFu);
+      stage[kStagePitch * lane + q] = t0;
+      if (fill && !can_list && base + q < n)
+        for (unsigned r = 0; r < (cnt & 0xFFFFu); r++) tri_cell[t0 + r] = (unsigned)(base + q) | (r << kTcRankShift);
       run += cnt;
     }
     __syncwarp();
-    unsigned* dst = half == 0 ? offsets : voffsets;
-    if (half == 0 && !keep_offsets) {
-      /* nothing to store */
-    } else if (wbase + 32 * kScanItems <= n) {
-      /* the warp's 1024 cells: each store instruction writes 512 contiguous
-         bytes (lane L: cells 4L .. 4L + 3 of a 128-cell chunk, all in one
-         staged row; wbase is a multiple of 1024, dst 256-byte aligned) */
-#pragma unroll 4
-      for (int k = 0; k < 8; k++) {
-        const int e = 128 * k + 4 * lane, row = e >> 5, col = e & 31;
-        const unsigned* sr = stage + kStagePitch * row + col;
-        reinterpret_cast<uint4*>(dst + wbase)[32 * k + lane] = make_uint4(sr[0], sr[1], sr[2], sr[3]);
-      }
-    } else {
-      for (int k = 0; k < 32; k++) {
-        const long long c = wbase + 32 * k + lane;
-        if (c < n) dst[c] = stage[kStagePitch * k + lane];
-      }
-    }
-    __syncwarp();
+    if (want_offsets) store_stage(offsets, stage, wbase, n, 0u);
   }
-  if (listed) {
-    __syncthreads();
+  if (fill && can_list) {
+    /* the list was complete at the barrier above */
     for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) {
       /* back to the cell's first triangle (a cell has at most 12; slot 0
          always starts a cell): its cell, and the rank is the distance */
@@ -719,17 +850,6 @@ k_scan_write(const unsigned char* __restrict__ codes, long long n, const unsigne
       while (l == 0xFFFFu && k > 0) l = s_list[--k];
       tri_cell[ta + e] = ((unsigned)c0 + l) | ((e - k) << kTcRankShift);
     }
-  }
-}
-
-/* triangle -> cell map from the offsets: tri_cell[offsets[c] + r] = c | r << 28 */
-__global__ void __launch_bounds__(256)
-k_fill_tri_cell(const unsigned* __restrict__ offsets, long long n, unsigned* __restrict__ tri_cell) {
-  pdl_enter();
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x) {
-    const unsigned a = offsets[c], b = offsets[c + 1];
-    for (unsigned u = a; u < b; u++) tri_cell[u] = (unsigned)c | ((u - a) << kTcRankShift);
   }
 }
 
@@ -2792,6 +2912,7 @@ static std::atomic<int> g_cls_z{kClsZ}, g_emit_per_sm{8}, g_raster_per_sm{8};
 static std::atomic<int> g_pdl{0};
 
 void set_dependent_launch(int on) { g_pdl = on ? 1 : 0; }
+int dependent_launch() { return g_pdl.load(); }
 
 int set_launch_shape(const LaunchShape& s) {
   if (s.cls_z < 1 || s.cls_z > 1024 || s.emit_per_sm < 1 || s.emit_per_sm > 32 || s.raster_per_sm < 1 ||
@@ -2856,7 +2977,7 @@ int upload_tables(const unsigned char code_count[256], const signed char nb[19][
   if (cudaMemcpyToSymbol(c_nb, nb, sizeof(signed char) * 19 * 16) != cudaSuccess) return 1;
   if (cudaMemcpyToSymbol(c_nb_count, nb_count, 19) != cudaSuccess) return 1;
   /* beyond the default 48 KB of dynamic shared memory: set once per device */
-  if (cudaFuncSetAttribute(k_scan_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanWriteSmem) !=
+  if (cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScanWriteSmem) !=
       cudaSuccess)
     return 1;
   return 0;
@@ -2961,31 +3082,48 @@ int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S0, unsigned char
   return nf;
 }
 
-void classify_bricks(const FieldDev& F, const SlabDev& S, unsigned* nbx, unsigned* nby, unsigned* nbz) {
-  *nbx = (unsigned)((F.nx - 1 + kClsX - 1) / kClsX);
-  *nby = (unsigned)((F.ny - 1 + kClsY - 1) / kClsY);
-  *nbz = (unsigned)((S.nslices + S.cls_z - 1) / S.cls_z);
+void make_cls_item(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, ClsItem* it) {
+  const FieldDev& F = Fs[0];
+  memset(it, 0, sizeof *it);
+  it->data = F.data;
+  it->is_f32 = F.is_f32;
+  it->nx = F.nx;
+  it->ny = F.ny;
+  it->S = S;
+  it->ts.n = min(nf, kMaxThr);
+  for (int t = 0; t < it->ts.n; t++) {
+    thr_range(Fs[t], it->ts, t);
+    it->out.codes[t] = codes[t];
+  }
+  it->nbx = (unsigned)((F.nx - 1 + kClsX - 1) / kClsX);
+  it->nby = (unsigned)((F.ny - 1 + kClsY - 1) / kClsY);
+  it->nbz = (unsigned)((S.nslices + S.cls_z - 1) / S.cls_z);
 }
 
 void launch_classify_queue(const ClsItem* items, int nitems, unsigned long long nunits, unsigned long long* next,
                            cudaStream_t st) {
   if (nitems < 1 || nunits == 0) return;
-  const unsigned long long cap = (unsigned long long)num_sms() * 8;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_classify_queue, kClsX, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 8;
+  const unsigned long long cap = (unsigned long long)num_sms() * (unsigned long long)per_sm;
   const unsigned grid = (unsigned)(nunits < cap ? nunits : cap);
   launch_k(k_classify_queue, "k_classify_queue", grid, kClsX, 0, st, items, nitems, nunits, next);
 }
 
-long long scan_segments(long long n) { return (n + kScanTile - 1) / kScanTile; }
+long long scan_state_words(long long n) { return std::max((n + kScanTile - 1) / kScanTile, 1LL) + 1; }
 
-void launch_scan(const unsigned char* codes, long long n, unsigned long long* seg_sums,
-                 unsigned long long* seg_base, unsigned* offsets, unsigned* voffsets, unsigned long long* totals,
-                 unsigned* tri_cell, unsigned long long tri_cap, bool want_offsets, unsigned* ovf, cudaStream_t st) {
-  const long long nseg = scan_segments(n);
-  if (nseg > 0) launch_k(k_seg_reduce, "k_seg_reduce", (unsigned)nseg, kScanThreads, 0, st, codes, n, seg_sums);
-  launch_k(k_seg_scan, "k_seg_scan", 1, kSegScanThreads, 0, st, seg_sums, nseg, seg_base, n, offsets, voffsets, totals);
-  if (nseg > 0)
-    launch_k(k_scan_write, "k_scan_write", (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, seg_base,
-             offsets, voffsets, totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf);
+cudaError_t launch_scan(const unsigned char* codes, long long n, unsigned long long* state, unsigned* offsets,
+                        unsigned* voffsets, unsigned long long* totals, unsigned* tri_cell,
+                        unsigned long long tri_cap, bool want_offsets, unsigned* ovf, unsigned* err,
+                        cudaStream_t st) {
+  const long long nseg = scan_state_words(n) - 1;
+  const cudaError_t e = cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (size_t)(nseg + 1), st);
+  if (e != cudaSuccess) return e;
+  launch_k(k_scan, "k_scan", (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, nseg, state, offsets,
+           voffsets, totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf, err);
+  return cudaSuccess;
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
@@ -2994,11 +3132,6 @@ void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene,
   if (F.is_f32) launch_k(k_vertices<float>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
   else launch_k(k_vertices<double>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
 }
-
-void launch_fill_tri_cell(const unsigned* offsets, long long n, unsigned* tri_cell, cudaStream_t st) {
-  launch_k(k_fill_tri_cell, "k_fill_tri_cell", grid_for(n, 256, 16), 256, 0, st, offsets, n, tri_cell);
-}
-
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets,

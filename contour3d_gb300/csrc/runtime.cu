@@ -822,7 +822,56 @@ struct FieldUpload {
 
 /* fields at least this large are uploaded in chunks overlapped with the slabs */
 constexpr size_t kPipelineBytes = 64ull << 20;
-constexpr long long kUploadSlabs = 4;
+constexpr long long kPipelineMinSlices = 16;
+/* the upload model (GB300, host field in pinned memory): the link moves
+   about 211 GB/s however the copy is issued (one or four copy streams, or
+   SMs reading mapped host memory); a slab pass costs about 20.6 ps per cell
+   and object (a 512^3 f64 field, two objects, 1920 x 1080) plus 0.12 ms per
+   object and slab of fixed cost (launch tails, the slab's halo slices) */
+constexpr double kLinkBytesPerS = 211e9;
+constexpr double kSlabSPerCell = 20.6e-12;
+constexpr double kSlabFixedS = 0.12e-3;
+constexpr int kMaxUploadSlabs = 24;
+
+/*
+ * Slab sizes (rendered slices, in visiting order) for L slices of a field
+ * that arrives while it is processed.  In units of the whole copy's time:
+ * chunk s has landed at C_s (its slices and every earlier chunk's), and slab
+ * s runs from max(E_{s-1}, C_s) for r per slice's copy time plus o.  A plan
+ * starts with a first slab of L / m slices and makes each next slab as large
+ * as still lands before the slab before it ends, so that the compute does
+ * not wait; the plan with the earliest modelled end over m = 2 .. 24 is
+ * taken.  An empty plan: one slab after the whole copy is modelled faster.
+ */
+static std::vector<long long> upload_plan(long long L, long long max_slab, double r, double o) {
+  std::vector<long long> best;
+  double best_end = 1.0 + r + o; /* the whole copy, then one pass */
+  for (int m = 2; m <= kMaxUploadSlabs; m++) {
+    const long long first = std::max(1LL, L / m);
+    if (first > max_slab) continue;
+    std::vector<long long> plan{first};
+    long long S = first;
+    double E = (double)first / (double)L * (1.0 + r) + o;
+    bool ok = true;
+    while (S < L) {
+      if ((int)plan.size() >= kMaxUploadSlabs) {
+        ok = false;
+        break;
+      }
+      long long z = (long long)(E * (double)L) - S; /* lands before slab s - 1 ends */
+      z = std::max(z, std::max(1LL, first / 2));
+      z = std::min(std::min(z, max_slab), L - S);
+      S += z;
+      E = std::max(E, (double)S / (double)L) + r * (double)z / (double)L + o;
+      plan.push_back(z);
+    }
+    if (ok && E < best_end) {
+      best_end = E;
+      best = plan;
+    }
+  }
+  return best;
+}
 
 /* objects that read one field with one geometry: they share the upload, the
    node tables and the slabs */
@@ -857,7 +906,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
        draws two levels of one field) upload it once */
     if (!(c.field_src == ci.data && c.field_bytes == nnodes * elem && c.field.p)) {
       if (c.field.ensure(nnodes * elem, st)) return 1;
-      pipelined = sink == nullptr && nnodes * elem >= kPipelineBytes && ncz >= 4 * kUploadSlabs;
+      pipelined = sink == nullptr && nnodes * elem >= kPipelineBytes && ncz >= kPipelineMinSlices;
       if (!pipelined)
         C3D_CUDA(cudaMemcpyAsync(c.field.p, ci.data, nnodes * elem, cudaMemcpyHostToDevice, st));
       c.field_src = ci.data;
@@ -952,22 +1001,19 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   std::vector<std::pair<long long, long long>> slabs;
   const bool descending = sd.z_descending && !want_all;
   if (pipelined) {
-    /* while the field arrives: slabs growing by 1.4 (a slab computes about
-       1.4 times as long as its slices take to arrive, so each chunk lands as
-       the slab before it ends); the compute starts after a seventh */
-    const long long L = kr1 - kr0, first = std::max(2LL, (long long)((double)L / 7.104));
-    const long long second = (long long)(1.4 * (double)first), third = (long long)(1.96 * (double)first);
-    const long long sizes[kUploadSlabs] = {first, second, third, L - first - second - third};
-    bool fits = true;
-    for (const long long z : sizes) fits = fits && z >= 1 && z <= slab_slices;
-    if (fits) {
-      long long k = descending ? kr1 : kr0;
-      for (const long long z : sizes) {
-        slabs.push_back(descending ? std::make_pair(k - z, k) : std::make_pair(k, k + z));
-        k += descending ? -z : z;
-      }
-    } else {
-      slab_slices = std::min(slab_slices, (L + kUploadSlabs - 1) / kUploadSlabs);
+    /* while the field arrives: the modelled plan (upload_plan) */
+    const double copy_s = (double)(nnodes * elem) / kLinkBytesPerS;
+    const double r = kSlabSPerCell * (double)(per_slice * ncz) * (double)nobj / copy_s;
+    const double o = kSlabFixedS * (double)nobj / copy_s;
+    const std::vector<long long> sizes = upload_plan(kr1 - kr0, slab_slices, r, o);
+    if (sizes.empty()) {
+      pipelined = false;
+      C3D_CUDA(cudaMemcpyAsync(c.field.p, ci.data, nnodes * elem, cudaMemcpyHostToDevice, st));
+    }
+    long long k = descending ? kr1 : kr0;
+    for (const long long z : sizes) {
+      slabs.push_back(descending ? std::make_pair(k - z, k) : std::make_pair(k, k + z));
+      k += descending ? -z : z;
     }
   }
   if (slabs.empty()) {
@@ -1032,7 +1078,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     const size_t code_stride = ((size_t)ncell + 255) & ~(size_t)255;
     if (c.counts.ensure(code_stride * nobj, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
         c.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
-        c.tile_state.ensure(2 * sizeof(unsigned long long) * (size_t)scan_segments(ncell), st) ||
+        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_state_words(ncell), st) ||
         c.scratch.ensure(128, st))
       return 1;
     /* the triangle -> cell map is written by the scan when the slab's
@@ -1042,8 +1088,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = async ? c.checks.as<unsigned>() + kClsErrWord : d_counter + 1;
     unsigned *d_ovf = c.checks.as<unsigned>() + kOvfWord;
-    const long long nseg = scan_segments(ncell);
-    unsigned long long *seg_sums = c.tile_state.as<unsigned long long>(), *seg_base = seg_sums + nseg;
+    unsigned long long *scan_state = c.tile_state.as<unsigned long long>();
     if (pipelined) {
       if (!up.wait(slab_index)) {
         log_error("%s", up.what);
@@ -1092,10 +1137,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       /* read per object: an earlier object of the slab may have grown the buffer */
       const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
       if (c.stage_timing && ob > 0) cudaEventRecord(c.evs[1], st);
-      launch_scan(codes, ncell, seg_sums, seg_base, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
-                  c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, async ? d_ovf : nullptr, st);
+      C3D_CUDA(launch_scan(codes, ncell, scan_state, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
+                           c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, async ? d_ovf : nullptr, d_err, st));
       if (c.stage_timing) cudaEventRecord(c.evs[2], st);
-      c.stats.kernel_launches += 3;
+      c.stats.kernel_launches += 1;
       unsigned long long T = 0, NV = 0;
       if (async) {
         T = c.caps.T;
@@ -1110,7 +1155,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           c.stats.ms_scan += elapsed(c.evs[1], c.evs[2]);
         }
         if (h_small[0]) {
-          log_error("device classification did not complete (error flags 0x%x)", h_small[0]);
+          log_error("device classification or scan did not complete (error flags 0x%x)", h_small[0]);
           return 1;
         }
         T = h_total[0];
@@ -1123,7 +1168,6 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       }
       /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
          every sub-array stays aligned (and over-allocate so that cap >= T) */
-      const bool filled = async || T <= tri_cap; /* the scan wrote the triangle -> cell map */
       if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
       const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
       if (cap < T) {
@@ -1141,8 +1185,11 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
       /* the vertex stage: triangle -> cell map, screen vertices */
       if (c.stage_timing) cudaEventRecord(c.evs[3], st);
-      if (!filled) {
-        launch_fill_tri_cell(c.offsets.as<unsigned>(), ncell, c.tri_cell.as<unsigned>(), st);
+      if (!async && T > tri_cap) {
+        /* the map did not fit: the scan again, with the grown map */
+        C3D_CUDA(launch_scan(codes, ncell, scan_state, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
+                             c.tri_cell.as<unsigned>(), c.tri_cell.cap / sizeof(unsigned), sink != nullptr, nullptr,
+                             d_err, st));
         c.stats.kernel_launches += 1;
       }
       VertDev VD = {};
@@ -1456,6 +1503,13 @@ static uint64_t frame_key(const FrameIn &f, const FrameOut &o) {
   if (f.nlines) k.add(f.lines, sizeof(contour3d_line_obj_t) * f.nlines);
   k.add(o.rgb_dev);
   k.add(f.stream);
+  /* a recorded graph keeps the launch shapes and launch attributes it was
+     recorded with: another setting is another frame */
+  const LaunchShape ls = launch_shape();
+  k.add(ls.cls_z);
+  k.add(ls.emit_per_sm);
+  k.add(ls.raster_per_sm);
+  k.add(dependent_launch());
   return k.h;
 }
 
@@ -1603,7 +1657,7 @@ static int frame_status(Ctx &c, bool async) {
   }
   if (async) {
     if (h_checks[kClsErrWord]) {
-      log_error("device classification did not complete (error flags 0x%x)", h_checks[kClsErrWord]);
+      log_error("device classification or scan did not complete (error flags 0x%x)", h_checks[kClsErrWord]);
       return 1;
     }
     /* the counts of every pass: statistics, and the sizes the next frames use */
@@ -2573,8 +2627,8 @@ namespace c3d {
 
 static std::atomic<bool> g_batch_classify{true};
 
-/* the batch's classification: one persistent launch over (object, brick)
-   work items of every frame whose fields each take one slab */
+/* the batch's classification: one persistent launch over (field, brick) work
+   items of every frame whose fields each take one slab */
 struct BatchCodes {
   char *arena = nullptr;     /* device: the work counter, then 256-byte aligned code arrays */
   ClsItem *items = nullptr;  /* device: the work items */
@@ -2593,10 +2647,17 @@ struct BatchCodes {
 };
 
 static int batch_classify(const contour3d_gb300_frame_t *frames, size_t num_frames, BatchCodes &bc) {
-  std::vector<ClsItem> items;
-  std::vector<std::pair<size_t, size_t>> where; /* (frame, field) of each item */
-  std::vector<size_t> offs;
-  size_t bytes = 256; /* the work counter */
+  /* objects of one frame that share a field's values, sizes and type are one
+     item (up to kMaxThr of them): one pass over that field */
+  struct Group {
+    size_t frame;
+    std::vector<size_t> objs;
+    FieldDev F[kMaxThr];
+    SlabDev S;
+  };
+  std::vector<Group> groups;
+  std::vector<size_t> code_offs; /* per (group, object), in group order */
+  size_t bytes = 256;             /* the work counter */
   const int cls_z = launch_shape().cls_z;
   bc.codes.assign(num_frames, {});
   for (size_t q = 0; q < num_frames; q++) {
@@ -2608,6 +2669,7 @@ static int batch_classify(const contour3d_gb300_frame_t *frames, size_t num_fram
       continue; /* the worker reports the frame's error */
     }
     bc.codes[q].assign(f.contours.size(), nullptr);
+    const size_t first_group = groups.size();
     for (size_t n = 0; n < f.contours.size(); n++) {
       const ContourIn &ci = f.contours[n];
       const long long nx = (long long)ci.sz[0], ny = (long long)ci.sz[1], nz = (long long)ci.sz[2];
@@ -2615,36 +2677,63 @@ static int batch_classify(const contour3d_gb300_frame_t *frames, size_t num_fram
       const long long per_slice = (nx - 1) * (ny - 1), ncz = nz - 1;
       /* the slab rule of the slab loop: the whole field in one slab */
       if (3 * per_slice > kMaxSlabCells || kMaxSlabCells / per_slice - 2 < ncz - 2) continue;
-      ClsItem it;
-      memset(&it, 0, sizeof it);
-      it.F.data = ci.data;
-      it.F.is_f32 = ci.f32 ? 1 : 0;
-      it.F.nx = nx;
-      it.F.ny = ny;
-      it.F.nz = nz;
-      it.F.threshold = ci.threshold;
-      it.F.thr_key = h_key(ci.threshold);
-      it.F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
-      set_float_threshold(it.F);
-      it.S = SlabDev{0, ncz, 1, ncz - 1, cls_z};
-      classify_bricks(it.F, it.S, &it.nbx, &it.nby, &it.nbz);
-      it.first = bc.units;
-      bc.units += (unsigned long long)it.nbx * it.nby * it.nbz;
-      offs.push_back(bytes);
-      bytes += ((size_t)(per_slice * ncz) + 255) & ~(size_t)255;
-      items.push_back(it);
-      where.push_back({q, n});
+      FieldDev F;
+      memset(&F, 0, sizeof F);
+      F.data = ci.data;
+      F.is_f32 = ci.f32 ? 1 : 0;
+      F.nx = nx;
+      F.ny = ny;
+      F.nz = nz;
+      F.threshold = ci.threshold;
+      F.thr_key = h_key(ci.threshold);
+      F.thr_nan = std::isnan(ci.threshold) ? 1 : 0;
+      set_float_threshold(F);
+      Group *g = nullptr;
+      for (size_t k = first_group; k < groups.size(); k++) {
+        const FieldDev &G = groups[k].F[0];
+        if (G.data == F.data && G.is_f32 == F.is_f32 && G.nx == nx && G.ny == ny && G.nz == nz &&
+            groups[k].objs.size() < (size_t)kMaxThr) {
+          g = &groups[k];
+          break;
+        }
+      }
+      if (!g) {
+        groups.push_back(Group());
+        g = &groups.back();
+        g->frame = q;
+        g->S = SlabDev{0, ncz, 1, ncz - 1, cls_z};
+      }
+      g->F[g->objs.size()] = F;
+      g->objs.push_back(n);
     }
   }
-  if (items.empty()) return 1;
-  if (cudaMalloc(&bc.arena, bytes) != cudaSuccess || cudaMalloc(&bc.items, sizeof(ClsItem) * items.size()) != cudaSuccess) {
+  std::vector<ClsItem> items;
+  for (Group &g : groups) {
+    const long long ncell = (g.F[0].nx - 1) * (g.F[0].ny - 1) * (g.F[0].nz - 1);
+    for (size_t t = 0; t < g.objs.size(); t++) {
+      code_offs.push_back(bytes);
+      bytes += ((size_t)ncell + 255) & ~(size_t)255;
+    }
+  }
+  if (groups.empty()) return 1;
+  if (cudaMalloc(&bc.arena, bytes) != cudaSuccess ||
+      cudaMalloc(&bc.items, sizeof(ClsItem) * groups.size()) != cudaSuccess) {
     cudaGetLastError();
     log_error("batch classification: device allocation of %zu bytes failed", bytes);
     return 1;
   }
-  for (size_t t = 0; t < items.size(); t++) {
-    items[t].codes = reinterpret_cast<unsigned char *>(bc.arena + offs[t]);
-    bc.codes[where[t].first][where[t].second] = items[t].codes;
+  size_t o = 0;
+  for (Group &g : groups) {
+    unsigned char *codes[kMaxThr] = {};
+    for (size_t t = 0; t < g.objs.size(); t++) {
+      codes[t] = reinterpret_cast<unsigned char *>(bc.arena + code_offs[o++]);
+      bc.codes[g.frame][g.objs[t]] = codes[t];
+    }
+    ClsItem it;
+    make_cls_item(g.F, (int)g.objs.size(), g.S, codes, &it);
+    it.first = bc.units;
+    bc.units += (unsigned long long)it.nbx * it.nby * it.nbz;
+    items.push_back(it);
   }
   bc.nitems = (int)items.size();
   C3D_CUDA(cudaStreamCreateWithFlags(&bc.st, cudaStreamNonBlocking));
