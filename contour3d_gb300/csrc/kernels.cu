@@ -733,6 +733,7 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
   __shared__ unsigned s_cnt[256];
   __shared__ unsigned long long s_prefix;
   __shared__ unsigned s_seg;
+  __shared__ unsigned s_first[kFillList / 32]; /* bit e: list slot e starts a cell's triangles */
   unsigned* stage_all = reinterpret_cast<unsigned*>(scan_smem);
   unsigned short* s_list = /* segment-local cell of each of the segment's triangles */
       reinterpret_cast<unsigned short*>(scan_smem + sizeof(unsigned) * (kScanThreads / 32) * 32 * kStagePitch);
@@ -779,9 +780,9 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
   const unsigned rel_t = (unsigned)(rel & kTriMask), rel_v = (unsigned)(rel >> 31);
   const bool can_list = seg_tris <= (unsigned)kFillList;
   if (can_list) {
-    /* the shared list: each cell writes its first triangle's slot only; the
-       other slots stay marked and find their cell by walking back */
-    for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) s_list[e] = 0xFFFFu;
+    /* the shared list: each cell writes its first triangle's slot and marks
+       it in s_first; a slot finds its cell's first slot there */
+    for (unsigned e = threadIdx.x; e < (seg_tris + 31) / 32; e += kScanThreads) s_first[e] = 0u;
     __syncthreads();
   }
   unsigned* stage = stage_all + warp * 32 * kStagePitch;
@@ -793,8 +794,12 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
     for (int q = 0; q < kScanItems; q++) {
       const unsigned cnt = s_cnt[(wv[q >> 2] >> (8 * (q & 3))) & 255];
       stage[kStagePitch * lane + q] = rel_v + (run >> 16);
-      if (can_list && (cnt & 0xFFFFu) && base + q < n)
-        s_list[rel_t + (run & 0xFFFFu)] = (unsigned short)(base + q - c0);
+      /* cells past n read as code 0: no triangles */
+      if (can_list && (cnt & 0xFFFFu)) {
+        const unsigned slot = rel_t + (run & 0xFFFFu);
+        s_list[slot] = (unsigned short)(base + q - c0);
+        atomicOr(&s_first[slot >> 5], 1u << (slot & 31));
+      }
       run += cnt;
     }
   };
@@ -844,11 +849,14 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
   if (fill && can_list) {
     /* the list was complete at the barrier above */
     for (unsigned e = threadIdx.x; e < seg_tris; e += kScanThreads) {
-      /* back to the cell's first triangle (a cell has at most 12; slot 0
-         always starts a cell): its cell, and the rank is the distance */
-      unsigned k = e, l = s_list[e];
-      while (l == 0xFFFFu && k > 0) l = s_list[--k];
-      tri_cell[ta + e] = ((unsigned)c0 + l) | ((e - k) << kTcRankShift);
+      /* the cell's first slot: the last marked slot at or before e (a cell
+         has at most 12 triangles and slot 0 starts one, so it lies in e's
+         word of s_first or the word before); the rank is the distance */
+      const unsigned wd = e >> 5;
+      unsigned m = s_first[wd] & (0xFFFFFFFFu >> (31 - (e & 31)));
+      unsigned first = 32 * wd + 31 - __clz(m);
+      if (m == 0u && wd > 0) first = 32 * (wd - 1) + 31 - __clz(s_first[wd - 1]);
+      tri_cell[ta + e] = ((unsigned)c0 + s_list[first]) | ((e - first) << kTcRankShift);
     }
   }
 }
@@ -3056,7 +3064,13 @@ int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S0, unsigned char
   /* codes[q] receives the cell codes of threshold q; the scan turns them into counts */
   const FieldDev& F = Fs[0];
   SlabDev S = S0;
-  S.cls_z = launch_shape().cls_z;
+  /* bricks of the launch shape's depth, or shallower when the slab is thin:
+     at least 16 bricks per SM, so that every SM has copies in flight (the
+     deeper the brick, the fewer node planes are read twice) */
+  const long long bxy = ((F.nx - 1 + kClsX - 1) / kClsX) * ((F.ny - 1 + kClsY - 1) / kClsY);
+  const long long want_z = ((long long)num_sms() * 16 + bxy - 1) / bxy;
+  S.cls_z = (int)std::max(std::min<long long>(launch_shape().cls_z, (S.nslices + want_z - 1) / want_z),
+                          (long long)std::min(8, launch_shape().cls_z));
   const dim3 grid((unsigned)((F.nx - 1 + kClsX - 1) / kClsX), (unsigned)((F.ny - 1 + kClsY - 1) / kClsY),
                   (unsigned)((S.nslices + S.cls_z - 1) / S.cls_z));
   CUtensorMap map;

@@ -1480,7 +1480,7 @@ struct KeyHash {
   template <typename T> void add(const T &v) { add(&v, sizeof v); }
 };
 
-static uint64_t frame_key(const FrameIn &f, const FrameOut &o) {
+static uint64_t frame_key(const Ctx &c, const FrameIn &f, const FrameOut &o) {
   KeyHash k;
   const HostScene &s = f.scene;
   k.add(s.cam);
@@ -1503,13 +1503,14 @@ static uint64_t frame_key(const FrameIn &f, const FrameOut &o) {
   if (f.nlines) k.add(f.lines, sizeof(contour3d_line_obj_t) * f.nlines);
   k.add(o.rgb_dev);
   k.add(f.stream);
-  /* a recorded graph keeps the launch shapes and launch attributes it was
-     recorded with: another setting is another frame */
+  /* a recorded graph keeps the launch shapes, launch attributes and slab
+     sizes it was recorded with: another setting is another frame */
   const LaunchShape ls = launch_shape();
   k.add(ls.cls_z);
   k.add(ls.emit_per_sm);
   k.add(ls.raster_per_sm);
   k.add(dependent_launch());
+  k.add(c.slab_cells);
   return k.h;
 }
 
@@ -1597,7 +1598,7 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
   int rc = -1;
   bool redone = false, replayed = false, recorded = false;
   if (async && graph_eligible(c, f, o)) {
-    const uint64_t key = frame_key(f, o);
+    const uint64_t key = frame_key(c, f, o);
     if (c.graph_exec && c.graph_key == key) {
       rc = replay_graph(c, f.stream);
       replayed = true;
