@@ -262,16 +262,14 @@ void launch_exact_all(const Geo& G, const unsigned long long* total, long long t
                       cudaStream_t st);
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st);
-void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
-                  const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned* checks,
-                  cudaStream_t st);
-void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
-                   unsigned* checks, cudaStream_t st);
-void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
-                 unsigned long long order_base, unsigned* checks, cudaStream_t st);
+/* the raster passes of one slab: the cover and sliver lists (k_raster),
+   the candidates below the depth floor dropped (k_prune), the surviving
+   candidates and the tiny list in FP64 (k_finish); bounds size the grids */
+void launch_raster(const Geo& G, const SceneDev& scene, long long tri_bound, const TriDev& tri,
+                   const RasterDev& R, unsigned* checks, cudaStream_t st);
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st);
-void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
-                  unsigned long long order_base, cudaStream_t st);
+void launch_finish(const Geo& G, const SceneDev& scene, long long bound, const RasterDev& R,
+                   unsigned long long order_base, unsigned* checks, cudaStream_t st);
 /* winners, normal requests, weighted normals, colours; `between` (optional)
    is recorded before the colour passes; `checks` (self-check) counts FP32
    colours that differ from the FP64 ones */

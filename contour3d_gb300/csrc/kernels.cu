@@ -15,17 +15,19 @@
  *   k_emit          one thread per triangle: its three vertices through their
  *                   owner cells, culling, and the raster route (cover list,
  *                   sliver list, tiny list, or dropped)
- *   k_cover         one thread per listed triangle: FP32 coverage and depth
- *                   intervals over its pixel range; certainly drawn fragments
- *                   raise a per-pixel depth floor, the rest become candidates
- *   k_sliver        the same for triangles whose area the reference may clamp
- *   k_tiny          one thread per triangle too small for FP32 bounds: the
- *                   reference's arithmetic for its few possible pixels
+ *   k_raster        one thread per listed triangle, over the cover list
+ *                   and then the sliver list: FP32 coverage and depth
+ *                   intervals over its pixel range; certainly drawn
+ *                   fragments raise a per-pixel depth floor, the rest become
+ *                   candidates; slivers (area the reference may clamp) the
+ *                   bounds cannot settle go to the tiny list
  *   k_prune         drops candidates below the final depth floor
- *   k_exact         one thread per remaining candidate: the reference's
+ *   k_finish        one thread per remaining candidate: the reference's
  *                   vertices (recomputed from the field), projection,
  *                   barycentric test and harmonic depth in FP64, then a
- *                   128-bit (depth, order) max into the z-buffer
+ *                   128-bit (depth, order) max into the z-buffer; then one
+ *                   thread per tiny-list triangle (too small for FP32
+ *                   bounds): the reference's arithmetic for its few pixels
  * per object, after its slabs:
  *   k_winners       the pixels the object owns
  *   k_shade_f       FP32 vertex normals and colour with certified bounds
@@ -48,7 +50,7 @@
  *   k_vertices, exact vertices  src/contour3d/contour/triangulate.c:40-73
  *   k_shade_f, k_nb_*, k_shade, k_normals
  *                               src/contour3d/contour/normal.c:6-165
- *   k_cover, k_sliver, k_tiny, k_exact, shading factor
+ *   k_raster, k_prune, k_finish, shading factor
  *                               src/contour3d/contour/render.c:38-163,
  *                               src/contour3d/project.c:9-67
  *   k_lines                     src/contour3d/line.c:26-119
@@ -1859,17 +1861,17 @@ __device__ __forceinline__ void write_candidates(const RasterDev& R, unsigned lo
   }
 }
 
+/* one block's 256 entries [base, base + 256) of the cover list (n entries),
+   traversed front to back along z (the list is close to emission order,
+   which follows z) so that near surfaces raise the floors early.  Every
+   thread of the block takes part: a thread keeps up to kCandBuf candidates
+   of its triangle and the block appends them at once */
 template <bool CHECK>
-__global__ void __launch_bounds__(256, 4)
-k_cover(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
-  pdl_enter();
-  const long long n = (long long)*R.cover_count;
+__device__ __noinline__ void cover_block(const Geo& G, const SceneDev& scene, const TriDev& tri,
+                                            const RasterDev& R, unsigned* __restrict__ checks, long long base,
+                                            long long n) {
   const long long W = scene.width, H = scene.height;
-  /* traverse front to back along z (the list is close to emission order,
-     which follows z) so that near surfaces raise the floors early.  Every
-     thread of a block runs the same iterations: a thread keeps up to
-     kCandBuf candidates of its triangle and the block appends them at once */
-  for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+  {
     const long long q = base + threadIdx.x;
     unsigned pix[kCandBuf];
     unsigned nb = 0, t32 = 0;
@@ -2105,13 +2107,13 @@ __device__ __forceinline__ bool screen_edges(const Geo& G, const SceneDev& s, un
   return true;
 }
 
+/* one block's 256 entries [base, base + 256) of the sliver list (n entries);
+   triangles the bounds cannot settle go to the tiny list (block-wide append) */
 template <typename T, bool CHECK>
-__global__ void __launch_bounds__(256, 4)
-k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
-  pdl_enter();
-  const long long n = (long long)*R.sliver_count;
+__device__ __noinline__ void sliver_block(const Geo& G, const SceneDev& scene, const RasterDev& R,
+                                             unsigned* __restrict__ checks, long long base, long long n) {
   const long long W = scene.width, H = scene.height;
-  for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+  {
     const long long q = base + threadIdx.x;
     bool to_tiny = false;
     unsigned t32 = 0;
@@ -2214,14 +2216,22 @@ k_sliver(Geo G, SceneDev scene, RasterDev R, unsigned* __restrict__ checks) {
   }
 }
 
-template <bool CHECK>
-__global__ void __launch_bounds__(256)
-k_tiny(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
+/*
+ * k_raster: the cover list and the sliver list in one grid.  Block
+ * iterations take the cover list's 256-entry blocks first, then the sliver
+ * list's; each iteration is one list's, so the block-wide appends stay
+ * uniform.
+ */
+template <typename T, bool CHECK>
+__global__ void __launch_bounds__(256, 4)
+k_raster(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ checks) {
   pdl_enter();
-  const unsigned long long n = min(*R.tiny_count, R.tiny_cap);
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x)
-    tiny_triangle<CHECK>(G, scene, R.tiny[q], R, order_base, checks);
+  const long long nc = (long long)*R.cover_count, ns = (long long)*R.sliver_count;
+  const long long bc = (nc + 255) / 256, bs = (ns + 255) / 256;
+  for (long long b = blockIdx.x; b < bc + bs; b += gridDim.x) {
+    if (b < bc) cover_block<CHECK>(G, scene, tri, R, checks, 256 * b, nc);
+    else sliver_block<T, CHECK>(G, scene, R, checks, 256 * (b - bc), ns);
+  }
 }
 
 /* ------------------------------------------------------------------ */
@@ -2250,14 +2260,32 @@ __global__ void __launch_bounds__(256) k_prune(RasterDev R) {
   }
 }
 
-__global__ void __launch_bounds__(256) k_exact(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base) {
+/* one tiny-list triangle (a call of its own: its registers stay out of the
+   candidate loop's allocation) */
+template <bool CHECK>
+__device__ __noinline__ void finish_tiny(const Geo& G, const SceneDev& scene, unsigned t, const RasterDev& R,
+                                         unsigned long long order_base, unsigned* checks) {
+  tiny_triangle<CHECK>(G, scene, t, R, order_base, checks);
+}
+
+/* k_finish: the surviving candidates (the reference's fragment test), then
+   the tiny list (the reference's arithmetic for the whole triangle), in one
+   grid; both end in the z-buffer's 128-bit maximum, so their order does not
+   matter */
+template <bool CHECK>
+__global__ void __launch_bounds__(256, 4)
+k_finish(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
   pdl_enter();
-  const unsigned long long n = *R.live_count;
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < n;
+  const unsigned long long nl = *R.live_count, nt = min(*R.tiny_count, R.tiny_cap);
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < nl + nt;
        q += (unsigned long long)gridDim.x * blockDim.x) {
-    const Candidate c = R.live[q];
-    const unsigned pj = c.pixel / (unsigned)scene.width;
-    exact_fragment(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base);
+    if (q < nl) {
+      const Candidate c = R.live[q];
+      const unsigned pj = c.pixel / (unsigned)scene.width;
+      exact_fragment(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base);
+    } else {
+      finish_tiny<CHECK>(G, scene, R.tiny[q - nl], R, order_base, checks);
+    }
   }
 }
 
@@ -3181,42 +3209,28 @@ void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets
   launch_k(k_normals, "k_normals", g, 256, 0, st, F, S, offsets, tri_cell, total, tri);
 }
 
-void launch_cover(const Geo& G, const SceneDev& scene, const unsigned long long* total, long long tri_bound,
-                  const TriDev& tri, const RasterDev& R, unsigned long long order_base, unsigned* checks,
-                  cudaStream_t st) {
-  (void)total;
-  (void)order_base;
+void launch_raster(const Geo& G, const SceneDev& scene, long long tri_bound, const TriDev& tri,
+                   const RasterDev& R, unsigned* checks, cudaStream_t st) {
+  /* cover and sliver entries together number at most the slab's triangles */
   const int g = grid_for(tri_bound, 256, g_raster_per_sm);
-  if (checks) launch_k(k_cover<true>, "k_cover", g, 256, 0, st, G, scene, tri, R, checks);
-  else launch_k(k_cover<false>, "k_cover", g, 256, 0, st, G, scene, tri, R, checks);
-}
-
-void launch_sliver(const Geo& G, const SceneDev& scene, long long sliver_bound, const RasterDev& R,
-                   unsigned* checks, cudaStream_t st) {
-  const int g = grid_for(sliver_bound, 256, g_raster_per_sm);
   if (G.F.is_f32) {
-    if (checks) launch_k(k_sliver<float, true>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
-    else launch_k(k_sliver<float, false>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
+    if (checks) launch_k(k_raster<float, true>, "k_raster", g, 256, 0, st, G, scene, tri, R, checks);
+    else launch_k(k_raster<float, false>, "k_raster", g, 256, 0, st, G, scene, tri, R, checks);
   } else {
-    if (checks) launch_k(k_sliver<double, true>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
-    else launch_k(k_sliver<double, false>, "k_sliver", g, 256, 0, st, G, scene, R, checks);
+    if (checks) launch_k(k_raster<double, true>, "k_raster", g, 256, 0, st, G, scene, tri, R, checks);
+    else launch_k(k_raster<double, false>, "k_raster", g, 256, 0, st, G, scene, tri, R, checks);
   }
-}
-
-void launch_tiny(const Geo& G, const SceneDev& scene, long long tiny_bound, const RasterDev& R,
-                 unsigned long long order_base, unsigned* checks, cudaStream_t st) {
-  const int g = grid_for(tiny_bound, 256, g_raster_per_sm);
-  if (checks) launch_k(k_tiny<true>, "k_tiny", g, 256, 0, st, G, scene, R, order_base, checks);
-  else launch_k(k_tiny<false>, "k_tiny", g, 256, 0, st, G, scene, R, order_base, checks);
 }
 
 void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st) {
   launch_k(k_prune, "k_prune", grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, R);
 }
 
-void launch_exact(const Geo& G, const SceneDev& scene, long long cand_bound, const RasterDev& R,
-                  unsigned long long order_base, cudaStream_t st) {
-  launch_k(k_exact, "k_exact", grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, G, scene, R, order_base);
+void launch_finish(const Geo& G, const SceneDev& scene, long long bound, const RasterDev& R,
+                   unsigned long long order_base, unsigned* checks, cudaStream_t st) {
+  const int g = grid_for(bound, 256, g_raster_per_sm);
+  if (checks) launch_k(k_finish<true>, "k_finish", g, 256, 0, st, G, scene, R, order_base, checks);
+  else launch_k(k_finish<false>, "k_finish", g, 256, 0, st, G, scene, R, order_base, checks);
 }
 
 void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R, const unsigned long long* lut,

@@ -1257,14 +1257,12 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
                       c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
                       st);
           if (c.stage_timing) cudaEventRecord(c.evs[4], st);
-          launch_cover(G, sd, d_total, (long long)T, tri, RS, slab_order, checks, st);
-          launch_sliver(G, sd, (long long)T, RS, checks, st);
-          launch_tiny(G, sd, (long long)RS.tiny_cap, RS, slab_order, checks, st);
+          launch_raster(G, sd, (long long)T, tri, RS, checks, st);
           if (c.stage_timing) cudaEventRecord(c.evs[5], st);
           launch_prune(RS, (long long)RS.cand_cap, st);
-          launch_exact(G, sd, (long long)RS.cand_cap, RS, slab_order, st);
+          launch_finish(G, sd, (long long)(RS.cand_cap + RS.tiny_cap), RS, slab_order, checks, st);
           if (c.stage_timing) cudaEventRecord(c.evs[6], st);
-          c.stats.kernel_launches += 6;
+          c.stats.kernel_launches += 4;
           if (async) {
             /* list capacities of this pass, compared with the counts at the frame's end */
             c.async_cand_cap = std::min(c.async_cand_cap, RS.cand_cap);
