@@ -28,6 +28,7 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -428,9 +429,20 @@ struct Ctx {
   int device = -1;
   bool ready = false;
   cudaStream_t own_stream = nullptr;
-  Buf lut, counts, offsets, tile_state, scratch, tri_cell, tri, dbg, field, nodes, canvas, rgb;
+  Buf lut, counts, scratch, dbg, field, nodes, canvas, rgb;
   Buf nb_ent, nb_wn, nb_span; /* the FP64 shading pass's neighbour lists */
-  Buf zlo, cand, live, tiny, win, checks, voffsets, verts, winfo, amb, shade_check;
+  Buf zlo, win, checks, winfo, amb, shade_check;
+  /* the per-slab arrays of one contour object's pass.  Unsynchronised frames
+     run the objects of a slab on two lanes (the frame's stream and
+     lane_stream), each with its own arrays; the passes of different objects
+     meet only in the z-buffer, the depth floors and the winner weights,
+     whose updates are order-independent maxima and tagged stores */
+  struct Lane {
+    Buf offsets, voffsets, tile_state, tri_cell, tri, verts, cand, live, tiny;
+  };
+  Lane lanes[2];
+  cudaStream_t lane_stream = nullptr;
+  cudaEvent_t ev_lane_fork = nullptr, ev_lane_join = nullptr;
   unsigned long long epoch = 0; /* frame counter for the winner-weight tags (1 .. 2^24 - 1) */
   Buf consts;                  /* the frame constants (pixel centres, grid blocks, line segments) */
   HostBuf h_consts;            /* their pinned staging block */
@@ -476,6 +488,11 @@ struct Ctx {
   cudaStream_t copy_stream = nullptr;  /* host field uploads, overlapped with the slabs */
   cudaEvent_t ev_field = nullptr;      /* the field buffer may be overwritten once this completed */
   std::vector<cudaEvent_t> chunk_ev;   /* upload chunk s has arrived */
+  size_t chunks_used = 0;              /* of them, this frame's */
+  /* C3D_TRACE=1: timing events of the frame's passes, with their labels */
+  std::vector<cudaEvent_t> trace_ev;
+  std::vector<std::string> trace_label;
+  size_t trace_used = 0;
 };
 
 static Ctx g_ctx;
@@ -505,6 +522,9 @@ static int ctx_init(Ctx &c) {
   for (auto &e : c.evs) C3D_CUDA(cudaEventCreate(&e));
   C3D_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
   C3D_CUDA(cudaEventCreateWithFlags(&c.ev_field, cudaEventDisableTiming));
+  C3D_CUDA(cudaStreamCreateWithFlags(&c.lane_stream, cudaStreamNonBlocking));
+  C3D_CUDA(cudaEventCreateWithFlags(&c.ev_lane_fork, cudaEventDisableTiming));
+  C3D_CUDA(cudaEventCreateWithFlags(&c.ev_lane_join, cudaEventDisableTiming));
   std::vector<unsigned long long> lut;
   unsigned char count[256];
   build_tables(lut, count);
@@ -823,14 +843,24 @@ struct FieldUpload {
 /* fields at least this large are uploaded in chunks overlapped with the slabs */
 constexpr size_t kPipelineBytes = 64ull << 20;
 constexpr long long kPipelineMinSlices = 16;
-/* the upload model (GB300, host field in pinned memory): the link moves
-   about 211 GB/s however the copy is issued (one or four copy streams, or
-   SMs reading mapped host memory); a slab pass costs about 20.6 ps per cell
-   and object (a 512^3 f64 field, two objects, 1920 x 1080) plus 0.12 ms per
-   object and slab of fixed cost (launch tails, the slab's halo slices) */
-constexpr double kLinkBytesPerS = 211e9;
-constexpr double kSlabSPerCell = 20.6e-12;
-constexpr double kSlabFixedS = 0.12e-3;
+/* the upload model (GB300, host field in pinned memory; set with
+   contour3d_gb300_set_upload_model): the link moves about 211 GB/s however
+   the copy is issued (one or four copy streams, or SMs reading mapped host
+   memory); a slab pass costs about 18.9 ps per cell and object (a 512^3 f64
+   field, two objects on two lanes, 1920 x 1080) plus about 0.04 ms per
+   object and slab of fixed cost (the kernels' ramp-up and tails, the slab's
+   halo slices) */
+struct UploadModel {
+  double link_bytes_per_s = 211e9;
+  double slab_s_per_cell = 18.9e-12;
+  double slab_fixed_s = 0.04e-3;
+};
+static std::mutex g_upload_mu;
+static UploadModel g_upload_model;
+static UploadModel upload_model() {
+  std::lock_guard<std::mutex> lk(g_upload_mu);
+  return g_upload_model;
+}
 constexpr int kMaxUploadSlabs = 24;
 
 /*
@@ -888,6 +918,54 @@ static bool same_field(const ContourIn &a, const ContourIn &b) {
  * every object works on the slices that are already there; the result does
  * not depend on this order (fragments carry their drawing order).
  */
+/* C3D_TRACE=1 in the environment: every frame prints to stderr when each
+   upload chunk landed and each slab pass and shading pass ended, relative
+   to the frame's start (a debugging aid; off by default) */
+static bool trace_on() {
+  static const bool on = [] {
+    const char *v = getenv("C3D_TRACE");
+    return v && v[0] == '1';
+  }();
+  return on;
+}
+
+static void trace_mark(Ctx &c, cudaStream_t st, const std::string &label) {
+  if (!trace_on() || c.capturing) return;
+  if (c.trace_used == c.trace_ev.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    c.trace_ev.push_back(e);
+    c.trace_label.emplace_back();
+  }
+  c.trace_label[c.trace_used] = label;
+  if (cudaEventRecord(c.trace_ev[c.trace_used], st) == cudaSuccess) c.trace_used++;
+  else cudaGetLastError();
+}
+
+/* after the frame's final synchronisation */
+static void trace_print(Ctx &c) {
+  if (!trace_on()) return;
+  for (size_t q = 0; q < c.chunks_used && q < c.chunk_ev.size(); q++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c.ev0, c.chunk_ev[q]) == cudaSuccess)
+      fprintf(stderr, "[c3d trace] %8.3f ms  upload chunk %zu landed\n", ms, q);
+    else
+      cudaGetLastError();
+  }
+  for (size_t q = 0; q < c.trace_used; q++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c.ev0, c.trace_ev[q]) == cudaSuccess)
+      fprintf(stderr, "[c3d trace] %8.3f ms  %s\n", ms, c.trace_label[q].c_str());
+    else
+      cudaGetLastError();
+  }
+  c.trace_used = 0;
+  c.chunks_used = 0;
+}
+
 static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const ContourIn *objs, size_t nobj,
                           unsigned long long &order_base, const RasterDev &R, DebugSink *sink,
                           const GroupGrid &gg) {
@@ -1002,9 +1080,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   const bool descending = sd.z_descending && !want_all;
   if (pipelined) {
     /* while the field arrives: the modelled plan (upload_plan) */
-    const double copy_s = (double)(nnodes * elem) / kLinkBytesPerS;
-    const double r = kSlabSPerCell * (double)(per_slice * ncz) * (double)nobj / copy_s;
-    const double o = kSlabFixedS * (double)nobj / copy_s;
+    const UploadModel um = upload_model();
+    const double copy_s = (double)(nnodes * elem) / um.link_bytes_per_s;
+    const double r = um.slab_s_per_cell * (double)(per_slice * ncz) * (double)nobj / copy_s;
+    const double o = um.slab_fixed_s * (double)nobj / copy_s;
     const std::vector<long long> sizes = upload_plan(kr1 - kr0, slab_slices, r, o);
     if (sizes.empty()) {
       pipelined = false;
@@ -1047,10 +1126,11 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       ranges.push_back({(size_t)ca * slice, (size_t)cb * slice});
     }
     while (c.chunk_ev.size() < ranges.size()) {
-      cudaEvent_t e;
-      C3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      cudaEvent_t e; /* with timing: the trace reports when each chunk landed */
+      C3D_CUDA(cudaEventCreate(&e));
       c.chunk_ev.push_back(e);
     }
+    c.chunks_used = ranges.size();
     /* the copies follow the buffer's allocation and every earlier reader */
     C3D_CUDA(cudaEventRecord(c.ev_field, st));
     C3D_CUDA(cudaStreamWaitEvent(c.copy_stream, c.ev_field, 0));
@@ -1076,19 +1156,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     /* one code array per object, each starting on 256 bytes (the scan and the
        vertex pass read codes with 16-byte loads) */
     const size_t code_stride = ((size_t)ncell + 255) & ~(size_t)255;
-    if (c.counts.ensure(code_stride * nobj, st) || c.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
-        c.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
-        c.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_state_words(ncell), st) ||
-        c.scratch.ensure(128, st))
-      return 1;
-    /* the triangle -> cell map is written by the scan when the slab's
-       triangles fit: the buffer keeps the size of the largest slab so far, at
-       least one triangle per two cells */
-    if (c.tri_cell.ensure(sizeof(unsigned) * (size_t)(ncell / 2 + 1024), st)) return 1;
+    if (c.counts.ensure(code_stride * nobj, st) || c.scratch.ensure(128, st)) return 1;
     unsigned *d_counter = c.scratch.as<unsigned>();
     unsigned *d_err = async ? c.checks.as<unsigned>() + kClsErrWord : d_counter + 1;
     unsigned *d_ovf = c.checks.as<unsigned>() + kOvfWord;
-    unsigned long long *scan_state = c.tile_state.as<unsigned long long>();
     if (pipelined) {
       if (!up.wait(slab_index)) {
         log_error("%s", up.what);
@@ -1112,9 +1183,29 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
     if (!pre)
       c.stats.kernel_launches += (uint64_t)launch_classify(Fo.data(), (int)nobj, S, obj_codes.data(), d_err, st);
     if (c.stage_timing) cudaEventRecord(c.evs[1], st);
+    /* unsynchronised frames: odd objects on the second lane, after the
+       classification; joined again before the next slab's classification */
+    const int nlanes = async && !sink && !c.stage_timing && nobj > 1 ? 2 : 1;
+    const cudaStream_t st_main = st;
+    if (nlanes > 1) {
+      C3D_CUDA(cudaEventRecord(c.ev_lane_fork, st_main));
+      C3D_CUDA(cudaStreamWaitEvent(c.lane_stream, c.ev_lane_fork, 0));
+    }
     for (size_t ob = 0; ob < nobj; ob++) {
       const FieldDev &F = Fo[ob];
       unsigned char *codes = obj_codes[ob];
+      const bool odd_lane = nlanes > 1 && (ob & 1);
+      Ctx::Lane &L = c.lanes[odd_lane ? 1 : 0];
+      const cudaStream_t st = odd_lane ? c.lane_stream : st_main; /* this object's pass */
+      if (L.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
+          L.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
+          L.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_state_words(ncell), st))
+        return 1;
+      /* the triangle -> cell map is written by the scan when the slab's
+         triangles fit: the buffer keeps the size of the largest slab so far,
+         at least one triangle per two cells */
+      if (L.tri_cell.ensure(sizeof(unsigned) * (size_t)(ncell / 2 + 1024), st)) return 1;
+      unsigned long long *scan_state = L.tile_state.as<unsigned long long>();
       const unsigned long long obase = order_base + 12ULL * (unsigned long long)(ncx * ncy * ncz) * ob;
       /* this slab and object's record of the frame status: the scan's totals
          (triangles, vertices), then the raster counters */
@@ -1131,14 +1222,14 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* sized before the count is known, from the largest slab seen so
            far; kernels that find more record an overflow and the frame is
            rendered again */
-        if (c.tri_cell.ensure(sizeof(unsigned) * c.caps.T, st) || c.tri.ensure(kTriBytes * (c.caps.T + 64), st))
+        if (L.tri_cell.ensure(sizeof(unsigned) * c.caps.T, st) || L.tri.ensure(kTriBytes * (c.caps.T + 64), st))
           return 1;
       }
       /* read per object: an earlier object of the slab may have grown the buffer */
-      const unsigned long long tri_cap = c.tri_cell.cap / sizeof(unsigned);
+      const unsigned long long tri_cap = L.tri_cell.cap / sizeof(unsigned);
       if (c.stage_timing && ob > 0) cudaEventRecord(c.evs[1], st);
-      C3D_CUDA(launch_scan(codes, ncell, scan_state, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
-                           c.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, async ? d_ovf : nullptr, d_err, st));
+      C3D_CUDA(launch_scan(codes, ncell, scan_state, L.offsets.as<unsigned>(), L.voffsets.as<unsigned>(), d_total,
+                           L.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, async ? d_ovf : nullptr, d_err, st));
       if (c.stage_timing) cudaEventRecord(c.evs[2], st);
       c.stats.kernel_launches += 1;
       unsigned long long T = 0, NV = 0;
@@ -1168,8 +1259,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       }
       /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
          every sub-array stays aligned (and over-allocate so that cap >= T) */
-      if (c.tri_cell.ensure(sizeof(unsigned) * T, st) || c.tri.ensure(kTriBytes * (T + 64), st)) return 1;
-      const size_t cap = (c.tri.cap / kTriBytes) & ~(size_t)31;
+      if (L.tri_cell.ensure(sizeof(unsigned) * T, st) || L.tri.ensure(kTriBytes * (T + 64), st)) return 1;
+      const size_t cap = (L.tri.cap / kTriBytes) & ~(size_t)31;
       if (cap < T) {
         log_error("internal: triangle buffer capacity %zu below %llu", cap, T);
         return 1;
@@ -1179,27 +1270,27 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap, st)) return 1;
         dbg = c.dbg.as<double>();
       }
-      TriDev tri = tri_layout(c.tri.p, cap, dbg);
-      tri.cap = std::min<unsigned long long>(cap, c.tri_cell.cap / sizeof(unsigned));
+      TriDev tri = tri_layout(L.tri.p, cap, dbg);
+      tri.cap = std::min<unsigned long long>(cap, L.tri_cell.cap / sizeof(unsigned));
       tri.ovf = d_ovf;
       unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
       /* the vertex stage: triangle -> cell map, screen vertices */
       if (c.stage_timing) cudaEventRecord(c.evs[3], st);
       if (!async && T > tri_cap) {
         /* the map did not fit: the scan again, with the grown map */
-        C3D_CUDA(launch_scan(codes, ncell, scan_state, c.offsets.as<unsigned>(), c.voffsets.as<unsigned>(), d_total,
-                             c.tri_cell.as<unsigned>(), c.tri_cell.cap / sizeof(unsigned), sink != nullptr, nullptr,
+        C3D_CUDA(launch_scan(codes, ncell, scan_state, L.offsets.as<unsigned>(), L.voffsets.as<unsigned>(), d_total,
+                             L.tri_cell.as<unsigned>(), L.tri_cell.cap / sizeof(unsigned), sink != nullptr, nullptr,
                              d_err, st));
         c.stats.kernel_launches += 1;
       }
       VertDev VD = {};
       if (!sink) {
         /* the screen vertices of the slab's crossed edges, 16 bytes each */
-        if (c.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
-        VD.pos = c.verts.as<float4>();
-        VD.cap = c.verts.cap / 16;
+        if (L.verts.ensure(16 * (size_t)NV + 64, st)) return 1;
+        VD.pos = L.verts.as<float4>();
+        VD.cap = L.verts.cap / 16;
         VD.ovf = d_ovf;
-        launch_vertices(F, S, sd, codes, c.voffsets.as<unsigned>(), ncell, VD, st);
+        launch_vertices(F, S, sd, codes, L.voffsets.as<unsigned>(), ncell, VD, st);
         c.stats.kernel_launches += 1;
         if (!async) c.stats.vertices += NV;
       }
@@ -1210,15 +1301,15 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       G.S = S;
       G.lut = c.lut.as<unsigned long long>();
       G.codes = codes;
-      G.tri_cell = c.tri_cell.as<unsigned>();
-      G.offsets = c.offsets.as<unsigned>();
+      G.tri_cell = L.tri_cell.as<unsigned>();
+      G.offsets = L.offsets.as<unsigned>();
       if (sink) {
         RasterDev none = {};
-        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, c.offsets.as<unsigned>(),
-                    c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
+        launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, L.offsets.as<unsigned>(),
+                    L.voffsets.as<unsigned>(), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
                     st);
         launch_exact_all(G, d_total, (long long)T, tri, st);
-        launch_normals(F, S, c.offsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
+        launch_normals(F, S, L.offsets.as<unsigned>(), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
         c.stats.kernel_launches += 3;
       } else {
         /* candidate and tiny lists: about one entry per covered pixel and a few
@@ -1241,20 +1332,20 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         RS.sliver_count = counters + 6;
         RS.sliver_rec = tri.rec + 3 * (cap - 1);
         for (int attempt = 0;; attempt++) {
-          if (c.cand.ensure(sizeof(Candidate) * cand_want, st) || c.live.ensure(sizeof(Candidate) * cand_want, st) ||
-              c.tiny.ensure(sizeof(unsigned) * tiny_want, st))
+          if (L.cand.ensure(sizeof(Candidate) * cand_want, st) || L.live.ensure(sizeof(Candidate) * cand_want, st) ||
+              L.tiny.ensure(sizeof(unsigned) * tiny_want, st))
             return 1;
-          RS.cand = c.cand.as<Candidate>();
-          RS.cand_cap = std::min(c.cand.cap, c.live.cap) / sizeof(Candidate);
+          RS.cand = L.cand.as<Candidate>();
+          RS.cand_cap = std::min(L.cand.cap, L.live.cap) / sizeof(Candidate);
           RS.cand_count = counters + 0;
-          RS.live = c.live.as<Candidate>();
-          RS.tiny = c.tiny.as<unsigned>();
-          RS.tiny_cap = c.tiny.cap / sizeof(unsigned);
+          RS.live = L.live.as<Candidate>();
+          RS.tiny = L.tiny.as<unsigned>();
+          RS.tiny_cap = L.tiny.cap / sizeof(unsigned);
           RS.tiny_count = counters + 1;
           if (!async) C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
           if (c.stage_timing) cudaEventRecord(c.evs[9], st);
-          launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, c.offsets.as<unsigned>(),
-                      c.voffsets.as<unsigned>(), c.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
+          launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, L.offsets.as<unsigned>(),
+                      L.voffsets.as<unsigned>(), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
                       st);
           if (c.stage_timing) cudaEventRecord(c.evs[4], st);
           launch_raster(G, sd, (long long)T, tri, RS, checks, st);
@@ -1262,6 +1353,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           launch_prune(RS, (long long)RS.cand_cap, st);
           launch_finish(G, sd, (long long)(RS.cand_cap + RS.tiny_cap), RS, slab_order, checks, st);
           if (c.stage_timing) cudaEventRecord(c.evs[6], st);
+          trace_mark(c, st, "slab " + std::to_string(slab_index - 1) + " object " + std::to_string(ob) + " (" +
+                                std::to_string(S.nslices) + " slices) raster done");
           c.stats.kernel_launches += 4;
           if (async) {
             /* list capacities of this pass, compared with the counts at the frame's end */
@@ -1306,7 +1399,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         const bool want_records = sink->out && sink->count < sink->capacity;
         std::vector<double> dv(want_records ? kDbgDoubles * T : 0);
         C3D_CUDA(cudaMemcpyAsync(meta.data(), tri.meta, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
-        C3D_CUDA(cudaMemcpyAsync(cellv.data(), c.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
+        C3D_CUDA(cudaMemcpyAsync(cellv.data(), L.tri_cell.p, sizeof(unsigned) * T, cudaMemcpyDeviceToHost, st));
         if (want_records) {
           C3D_CUDA(cudaMemcpy2DAsync(dv.data(), sizeof(double) * T, dbg, sizeof(double) * cap, sizeof(double) * T, 18,
                                      cudaMemcpyDeviceToHost, st));
@@ -1335,6 +1428,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           sink->count++;
         }
       }
+    }
+    if (nlanes > 1) {
+      C3D_CUDA(cudaEventRecord(c.ev_lane_join, c.lane_stream));
+      C3D_CUDA(cudaStreamWaitEvent(st_main, c.ev_lane_join, 0));
     }
   }
   if (!sink) {
@@ -1376,6 +1473,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       Fs.codes = codes_whole ? last_codes[ob] : nullptr;
       launch_shade_f(Fs, sd, RS, c.lut.as<unsigned long long>(), obase, rgb, st);
       if (c.stage_timing) cudaEventRecord(c.evs[10], st);
+      trace_mark(c, st, "object " + std::to_string(ob) + " FP32 shading done");
       /* without node spacings (a converter) every won pixel takes the FP64 pass */
       const bool fp32 = Fo[ob].dgx != nullptr && nx <= (1 << 20) && ny <= (1 << 20) && nz <= (1 << 20);
       const unsigned *list = fp32 ? RS.amb : RS.win;
@@ -1629,6 +1727,7 @@ static int render_frame(Ctx &c, const FrameIn &f, const FrameOut &o) {
     }
   }
   if (rc == -1) rc = render_frame_pass(c, f, o, async);
+  if (rc == 0) trace_print(c);
   if (rc == kFrameRedo) {
     /* the graph (if any) was sized for less work than this frame has */
     drop_graph(c);
@@ -1701,6 +1800,8 @@ static int render_frame_pass(Ctx &c, const FrameIn &f, const FrameOut &o, bool a
   }
   c.stats = contour3d_gb300_stats_t{};
   c.frame_async = async;
+  c.trace_used = 0;
+  c.chunks_used = 0;
   c.status_next = c.status_obj_next = 0;
   c.async_cand_cap = c.async_tiny_cap = c.async_ent_cap = ~0ULL;
   c.async_obj_fp32.clear();
@@ -1782,6 +1883,7 @@ static int render_frame_pass(Ctx &c, const FrameIn &f, const FrameOut &o, bool a
     if (c.h_slots.ensure(sizeof(Slot) * npx)) return 1;
     C3D_CUDA(cudaMemcpyAsync(c.h_slots.p, c.canvas.p, sizeof(Slot) * npx, cudaMemcpyDeviceToHost, st));
   }
+  trace_mark(c, st, "image resolved and copied out");
   if (!c.capturing) C3D_CUDA(cudaEventRecord(c.ev1, st));
   unsigned *h_checks = c.h_small.as<unsigned>() + 32;
   C3D_CUDA(cudaMemcpyAsync(h_checks, c.checks.p, 16 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -1866,6 +1968,7 @@ extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
                                  const size_t num_lines, const contour3d_line_obj_t *const lines,
                                  const char fname[]) {
   (void)camera_look_at; /* stored but unused by the reference (main.c:13-23) */
+  const auto t_enter = std::chrono::steady_clock::now();
   std::lock_guard<std::mutex> lk(g_mu);
   if (check_common(camera_position, light_direction, screen_sizes, screen_center, screen_local, bg_color)) return 1;
   if ((num_contours && !objs) || (num_lines && !lines)) {
@@ -1931,6 +2034,7 @@ extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
     out.rgb_pinned = true; /* written to the file straight from the pinned copy */
   }
   if (render_frame(g_ctx, f, out)) return 1;
+  const auto t_rendered = std::chrono::steady_clock::now();
   if (multi) {
     if (reduce_nearest(sdecomp_info, px.data(), W * H)) {
       log_error("image output failed");
@@ -1951,6 +2055,14 @@ extern "C" int contour3d_execute(const sdecomp_info_t *const sdecomp_info,
   if (write_ppm(fname, W, H, multi ? rgb.data() : g_ctx.h_rgb.as<uint8_t>())) {
     log_error("image output failed");
     return 1;
+  }
+  if (trace_on()) {
+    const auto t_written = std::chrono::steady_clock::now();
+    const auto ms = [&](std::chrono::steady_clock::time_point t) {
+      return std::chrono::duration<double, std::milli>(t - t_enter).count();
+    };
+    fprintf(stderr, "[c3d trace] host: frame rendered %.3f ms, ppm written %.3f ms after the call began\n",
+            ms(t_rendered), ms(t_written));
   }
   return 0;
 }
@@ -2131,6 +2243,18 @@ extern "C" int contour3d_gb300_set_dependent_launch(int on) {
   return 0;
 }
 
+extern "C" int contour3d_gb300_set_upload_model(double link_gb_per_s, double slab_ps_per_cell,
+                                                double slab_fixed_us) {
+  if (!(link_gb_per_s > 0.0) || !(slab_ps_per_cell > 0.0) || !(slab_fixed_us >= 0.0) ||
+      !std::isfinite(link_gb_per_s + slab_ps_per_cell + slab_fixed_us))
+    return 1;
+  std::lock_guard<std::mutex> lk(c3d::g_upload_mu);
+  c3d::g_upload_model.link_bytes_per_s = link_gb_per_s * 1e9;
+  c3d::g_upload_model.slab_s_per_cell = slab_ps_per_cell * 1e-12;
+  c3d::g_upload_model.slab_fixed_s = slab_fixed_us * 1e-6;
+  return 0;
+}
+
 extern "C" int contour3d_gb300_set_slab_cells(uint64_t max_cells) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (max_cells < 64) {
@@ -2233,10 +2357,13 @@ extern "C" int contour3d_gb300_release(void) {
 
 /* every device buffer of a context; the constant table (lut) first */
 static std::vector<Buf *> ctx_bufs(Ctx &c) {
-  return {&c.lut, &c.counts, &c.offsets, &c.tile_state, &c.scratch, &c.tri_cell, &c.tri, &c.dbg,
-          &c.field, &c.consts, &c.nodes, &c.canvas, &c.rgb, &c.zlo, &c.cand, &c.live,
-          &c.tiny, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.voffsets, &c.verts, &c.winfo, &c.amb,
-          &c.shade_check, &c.checks, &c.status};
+  std::vector<Buf *> v = {&c.lut, &c.counts, &c.scratch, &c.dbg, &c.field, &c.consts, &c.nodes, &c.canvas,
+                          &c.rgb, &c.zlo, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.winfo, &c.amb,
+                          &c.shade_check, &c.checks, &c.status};
+  for (Ctx::Lane &L : c.lanes)
+    for (Buf *b : {&L.offsets, &L.voffsets, &L.tile_state, &L.tri_cell, &L.tri, &L.verts, &L.cand, &L.live, &L.tiny})
+      v.push_back(b);
+  return v;
 }
 
 static void ctx_release(Ctx &c) {
@@ -2258,6 +2385,9 @@ static void ctx_release(Ctx &c) {
     cudaStreamSynchronize(c.copy_stream);
     cudaStreamDestroy(c.copy_stream);
     cudaEventDestroy(c.ev_field);
+    cudaStreamDestroy(c.lane_stream);
+    cudaEventDestroy(c.ev_lane_fork);
+    cudaEventDestroy(c.ev_lane_join);
     for (auto &e : c.chunk_ev) cudaEventDestroy(e);
     c.chunk_ev.clear();
   }

@@ -113,6 +113,7 @@ EXPORTS = [
     "contour3d_gb300_set_stage_timing", "contour3d_gb300_set_slab_cells", "contour3d_gb300_set_filter_check",
     "contour3d_gb300_set_async", "contour3d_gb300_set_server_async", "contour3d_gb300_set_graphs", "contour3d_gb300_set_launch_shape",
     "contour3d_gb300_set_dependent_launch", "contour3d_gb300_set_batch_classify",
+    "contour3d_gb300_set_upload_model",
     "contour3d_gb300_debug_triangles", "contour3d_gb300_debug_cell_counts",
     "contour3d_gb300_install_transport", "contour3d_gb300_extend", "contour3d_gb300_release",
     "contour3d_gb300_cell_offsets_noalloc", "contour3d_gb300_render_batch", "contour3d_gb300_server_create",
@@ -270,6 +271,11 @@ class Library:
 
     def set_batch_classify(self, on: bool) -> None:
         self.lib.contour3d_gb300_set_batch_classify(1 if on else 0)
+
+    def set_upload_model(self, link_gb_per_s: float, slab_ps_per_cell: float, slab_fixed_us: float) -> int:
+        f = self.lib.contour3d_gb300_set_upload_model
+        f.argtypes = [C.c_double, C.c_double, C.c_double]
+        return f(link_gb_per_s, slab_ps_per_cell, slab_fixed_us)
 
     def set_launch_shape(self, classify_slices: int, emit_blocks_per_sm: int, raster_blocks_per_sm: int) -> None:
         if self.lib.contour3d_gb300_set_launch_shape(int(classify_slices), int(emit_blocks_per_sm),

@@ -292,6 +292,14 @@ int contour3d_gb300_set_dependent_launch(int on);
  * depend on it.
  */
 int contour3d_gb300_set_batch_classify(int on);
+/*
+ * The model that sizes the slabs of a host field uploaded while it is
+ * processed (fields of 64 MB or more): the host link's rate, the slab
+ * passes' cost per cell and contour object, and their fixed cost per object
+ * and slab.  Defaults measured on GB300: 211 GB/s, 18.9 ps, 40 us.  Images do
+ * not depend on it.  Returns 1 for values out of range.
+ */
+int contour3d_gb300_set_upload_model(double link_gb_per_s, double slab_ps_per_cell, double slab_fixed_us);
 /* upper bound on cells per slab (default and maximum 178,956,970, the most the
    scan's packed 32-bit sums allow); smaller slabs use less memory */
 int contour3d_gb300_set_slab_cells(uint64_t max_cells);
