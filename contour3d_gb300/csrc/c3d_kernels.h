@@ -93,7 +93,7 @@ int dependent_launch();
 /* triangle arrays (structure of arrays, indexed by emission order within a slab) */
 struct TriDev {
   double* wn[3];      /* inspection: area * face normal */
-  unsigned* meta;     /* edge ids (3 x 5 bits) | flags | rank in the cell */
+  unsigned* meta;     /* inspection: edge ids (3 x 5 bits) | flags | rank in the cell */
   /* k_cover's input, the compact list of triangles that reach it (k_emit
      appends them), 3 float4 each: x0 y0 z0 x1 | y1 z1 x2 y2 | z2 err_xy
      err_z t -- FP32 screen positions and depths, the bound on |screen x, y -

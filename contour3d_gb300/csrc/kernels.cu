@@ -1123,12 +1123,15 @@ __device__ __forceinline__ bool vertex_q(const SceneDev& s, const FieldDev& F, c
   const float af = fabsf(f);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
+    /* fused multiply-adds round once where the bound allows for two
+       roundings, so every bound below still holds */
     const float d = x1[i] - x0[i];
-    const float p = x0[i] + f * d;
+    const float p = __fmaf_rn(f, d, x0[i]);
     q[i] = p - pc[i];
-    const float ep = e_f * fabsf(d) +
-                     kU32 * (ce * fabsf(x0[i]) + fabsf(p) + af * (ce * fabsf(x0[i]) + ce * fabsf(x1[i]) + 2.2f * fabsf(d)));
-    eq[i] = 1.1f * (ep + kU32 * (fabsf(pc[i]) + fabsf(q[i]))) + 1e-30f;
+    const float cx0 = ce * fabsf(x0[i]);
+    const float inner = __fmaf_rn(2.2f, fabsf(d), __fmaf_rn(ce, fabsf(x1[i]), cx0));
+    const float ep = __fmaf_rn(e_f, fabsf(d), kU32 * __fmaf_rn(af, inner, cx0 + fabsf(p)));
+    eq[i] = __fmaf_rn(1.1f, __fmaf_rn(kU32, fabsf(pc[i]) + fabsf(q[i]), ep), 1e-30f);
   }
   return true;
 }
@@ -1163,15 +1166,17 @@ __device__ __forceinline__ float corner_pos_f(const FieldDev& F, long long i, lo
 __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], const float eq[3], float ref_eps,
                                          float& X, float& Y, float& Z, float& exy, float& ez) {
   const float ax = fabsf(q[0]), ay = fabsf(q[1]), az = fabsf(q[2]);
-  const float nq = s.f_n[0] * q[0] + s.f_n[1] * q[1] + s.f_n[2] * q[2];
-  const float lq = s.f_lx[0] * q[0] + s.f_lx[1] * q[1] + s.f_lx[2] * q[2];
-  const float mq = s.f_ly[0] * q[0] + s.f_ly[1] * q[1] + s.f_ly[2] * q[2];
-  const float e_nq = fabsf(s.f_n[0]) * eq[0] + fabsf(s.f_n[1]) * eq[1] + fabsf(s.f_n[2]) * eq[2] +
-                     4.2f * kU32 * (fabsf(s.f_n[0]) * ax + fabsf(s.f_n[1]) * ay + fabsf(s.f_n[2]) * az);
-  const float e_lq = fabsf(s.f_lx[0]) * eq[0] + fabsf(s.f_lx[1]) * eq[1] + fabsf(s.f_lx[2]) * eq[2] +
-                     4.2f * kU32 * (fabsf(s.f_lx[0]) * ax + fabsf(s.f_lx[1]) * ay + fabsf(s.f_lx[2]) * az);
-  const float e_mq = fabsf(s.f_ly[0]) * eq[0] + fabsf(s.f_ly[1]) * eq[1] + fabsf(s.f_ly[2]) * eq[2] +
-                     4.2f * kU32 * (fabsf(s.f_ly[0]) * ax + fabsf(s.f_ly[1]) * ay + fabsf(s.f_ly[2]) * az);
+  /* dot products and their bounds with fused multiply-adds: one rounding
+     fewer per step than the unfused sums the bounds allow for */
+  const float nq = __fmaf_rn(s.f_n[2], q[2], __fmaf_rn(s.f_n[1], q[1], s.f_n[0] * q[0]));
+  const float lq = __fmaf_rn(s.f_lx[2], q[2], __fmaf_rn(s.f_lx[1], q[1], s.f_lx[0] * q[0]));
+  const float mq = __fmaf_rn(s.f_ly[2], q[2], __fmaf_rn(s.f_ly[1], q[1], s.f_ly[0] * q[0]));
+  auto bound = [&](const float a[3]) {
+    const float se = __fmaf_rn(fabsf(a[2]), eq[2], __fmaf_rn(fabsf(a[1]), eq[1], fabsf(a[0]) * eq[0]));
+    const float sq = __fmaf_rn(fabsf(a[2]), az, __fmaf_rn(fabsf(a[1]), ay, fabsf(a[0]) * ax));
+    return __fmaf_rn(4.2f * kU32, sq, se);
+  };
+  const float e_nq = bound(s.f_n), e_lq = bound(s.f_lx), e_mq = bound(s.f_ly);
   const float anq = fabsf(nq);
   Z = nq;
   ez = 1.1f * e_nq + 1e-30f;
@@ -1190,12 +1195,14 @@ __device__ __forceinline__ int project_f(const SceneDev& s, const float q[3], co
   if (t + et < 0.f || t - et > 1.f) return 0;
   if (t - et <= 0.f || t + et >= 1.f) return -1;
   const float rx = lq * r, ry = mq * r;
-  const float erx = (e_lq + fabsf(rx) * e_nq) * rin + 6.f * kU32 * fabsf(rx);
-  const float ery = (e_mq + fabsf(ry) * e_nq) * rin + 6.f * kU32 * fabsf(ry);
-  X = s.f_ax + s.f_bx * rx;
-  Y = s.f_ay + s.f_by * ry;
-  const float ex = fabsf(s.f_bx) * erx + kU32 * (fabsf(s.f_ax) + 2.f * fabsf(s.f_bx * rx) + fabsf(X)) + ref_eps;
-  const float ey = fabsf(s.f_by) * ery + kU32 * (fabsf(s.f_ay) + 2.f * fabsf(s.f_by * ry) + fabsf(Y)) + ref_eps;
+  const float erx = __fmaf_rn(__fmaf_rn(fabsf(rx), e_nq, e_lq), rin, 6.f * kU32 * fabsf(rx));
+  const float ery = __fmaf_rn(__fmaf_rn(fabsf(ry), e_nq, e_mq), rin, 6.f * kU32 * fabsf(ry));
+  X = __fmaf_rn(s.f_bx, rx, s.f_ax);
+  Y = __fmaf_rn(s.f_by, ry, s.f_ay);
+  const float ex = __fmaf_rn(fabsf(s.f_bx), erx,
+                             __fmaf_rn(kU32, __fmaf_rn(2.f, fabsf(s.f_bx * rx), fabsf(s.f_ax)) + fabsf(X), ref_eps));
+  const float ey = __fmaf_rn(fabsf(s.f_by), ery,
+                             __fmaf_rn(kU32, __fmaf_rn(2.f, fabsf(s.f_by * ry), fabsf(s.f_ay)) + fabsf(Y), ref_eps));
   exy = 1.1f * fmaxf(ex, ey);
   return 1;
 }
@@ -1382,11 +1389,17 @@ __device__ __forceinline__ EdgeF edge_f(float ax, float ay, float bx, float by, 
 /* render.c:38-46 at a point known to +-e_p, edge vertex a known to +-eps_a; value and error bound */
 __device__ __forceinline__ float edge_eval(const EdgeF& E, float px, float py, float e_p, float eps_a, float& err) {
   const float u = px - E.ax, v = py - E.ay;
-  const float eu = e_p + eps_a + kU32 * fabsf(u), ev = e_p + eps_a + kU32 * fabsf(v);
-  const float p1 = u * E.dby, p2 = v * E.dbx;
-  const float e = p1 - p2;
-  err = 1.25f * (fabsf(u) * E.e_dby + fabsf(E.dby) * eu + eu * E.e_dby + fabsf(v) * E.e_dbx + fabsf(E.dbx) * ev +
-                 ev * E.e_dbx + kU32 * (fabsf(p1) + fabsf(p2) + fabsf(e)));
+  const float eu = __fmaf_rn(kU32, fabsf(u), e_p + eps_a), ev = __fmaf_rn(kU32, fabsf(v), e_p + eps_a);
+  /* u dby - v dbx with one rounding of the product v dbx and one of the
+     fused result; the bound keeps a term for a rounding of u dby as well */
+  const float p2 = v * E.dbx;
+  const float e = __fmaf_rn(u, E.dby, -p2);
+  const float pr = fabsf(u) * fabsf(E.dby) + fabsf(p2) + fabsf(e);
+  float b = __fmaf_rn(fabsf(u), E.e_dby, kU32 * pr);
+  b = __fmaf_rn(fabsf(E.dby) + E.e_dby, eu, b);
+  b = __fmaf_rn(fabsf(v), E.e_dbx, b);
+  b = __fmaf_rn(fabsf(E.dbx) + E.e_dbx, ev, b);
+  err = 1.25f * b;
   return e;
 }
 
@@ -1572,13 +1585,14 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
 }
 
 /*
- * One thread per triangle: cube-edge ids and, for rendered triangles, the
- * FP32 screen vertices and their bounds (gathered from k_vertices), and the
- * raster path that settles the triangle: k_tiny (FP64 throughout) when the
- * bounds cannot decide its culling, k_sliver when its area may be clamped,
- * none when no pixel centre can lie in it, k_cover otherwise -- only the
- * k_cover and k_sliver triangles are written to the compact lists those
- * read.  Without raster lists (inspection) only the ids are kept.
+ * One thread per triangle.  The render form gathers a rendered triangle's
+ * FP32 screen vertices and their bounds (from k_vertices) and picks the
+ * raster path that settles it: the tiny list (FP64 throughout) when the
+ * bounds cannot decide its culling, the sliver list when its area may be
+ * clamped, none when no pixel centre can lie in it, the cover list
+ * otherwise -- only cover and sliver triangles are written, to the compact
+ * lists k_raster reads.  The inspection form keeps the cube-edge ids and
+ * flags of every triangle (tri.meta) and routes nothing.
  */
 /* what k_emit decided for one triangle */
 struct EmitOut {
@@ -1586,15 +1600,21 @@ struct EmitOut {
   float X[3], Y[3], Z[3], exy, zr;
 };
 
-template <typename T, bool CHECK>
+/*
+ * One triangle.  RENDER: for a rendered triangle, its FP32 screen vertices
+ * (gathered from k_vertices), its bounds and its raster route; nothing is
+ * stored per triangle.  Otherwise (inspection): the cube-edge ids, the
+ * rendered flag and the rank in the cell, stored in tri.meta.
+ */
+template <typename T, bool CHECK, bool RENDER>
 __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, const SceneDev& scene,
                                          const unsigned long long* lut, const unsigned char* __restrict__ codes,
                                          const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
                                          const TriDev& tri, const RasterDev& R, const VertDev& V,
                                          unsigned* __restrict__ checks, long long t, EmitOut& out) {
-  const long long ncx = F.nx - 1, ncy = F.ny - 1;
+  const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
   const long long W = scene.width, H = scene.height;
-  const unsigned ncxy = (unsigned)(ncx * ncy);
+  const unsigned ncxy = ncx * ncy;
   int& route = out.route;
   float* X = out.X;
   float* Y = out.Y;
@@ -1610,99 +1630,97 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
   const unsigned c = tc & kTcCellMask, r = tc >> kTcRankShift;
   unsigned ui, uj, ukl;
   cell_ijk(F, c, ui, uj, ukl);
-  const long long i = ui, j = uj, k = S.kfirst + ukl;
+  /* slab slices fit 32 bits (a slab holds fewer than 2^28 cells) */
+  const unsigned uk = (unsigned)S.kfirst + ukl;
   const unsigned code = codes[c];
   const unsigned long long e = lut[code * 12 + r];
-  unsigned edges = 0;
-#pragma unroll
-  for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
   /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
-  const bool rendered = i >= 1 && i <= ncx - 2 && j >= 1 && j <= ncy - 2 && k >= S.krender0 && k < S.krender1;
-  unsigned meta = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
-  if (rendered && R.cover_count) {
-    /* the three vertices from k_vertices: vertex q lies on the edge from
-       corner a to corner b, owned by the cell at corner a & b */
-    int status = 1;
+  const bool rendered = ui >= 1u && ui + 2u <= ncx && uj >= 1u && uj + 2u <= ncy && uk >= (unsigned)S.krender0 &&
+                        uk < (unsigned)S.krender1;
+  if (!RENDER) {
+    unsigned edges = 0;
+#pragma unroll
+    for (int q = 0; q < 3; q++) edges |= (unsigned)((e >> (18 + 5 * q)) & 31) << (5 * q);
+    tri.meta[t] = edges | (rendered ? kMetaRendered : 0u) | (r << kMetaRankShift);
+    return;
+  }
+  if (!rendered) return;
+  /* the three vertices from k_vertices: vertex q lies on the edge from
+     corner a to corner b, owned by the cell at corner a & b */
+  int status = 1;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const unsigned a = (unsigned)((e >> (6 * q)) & 7), b = (unsigned)((e >> (6 * q + 3)) & 7);
+    const unsigned o = a & b, m = a ^ b;
+    const unsigned oc = c + (o & 1u) + ((o >> 1) & 1u) * ncx + (o >> 2) * ncxy;
+    const unsigned vi = voffsets[oc] + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
+    const float4 p = __ldg(V.pos + vi);
+    const unsigned pk = __float_as_uint(p.w);
+    const float aux = bf16_value(pk & 0xFFFFu);
+    X[q] = p.x;
+    Y[q] = p.y;
+    Z[q] = p.z;
+    exy = fmaxf(exy, bf16_value(pk >> 16));
+    if (aux >= 0.f) zr = fmaxf(zr, aux);
+    else if (aux == -1.f) status = 0;
+    else if (status != 0) status = -1;
+  }
+  const long long i = ui, j = uj, k = uk;
+  d3 v[3];
+  bool ok = true;
+  if (CHECK) {
+    /* the reference's own vertices and projection */
+    d3 p[3];
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-      const unsigned a = (unsigned)((e >> (6 * q)) & 7), b = (unsigned)((e >> (6 * q + 3)) & 7);
-      const unsigned o = a & b, m = a ^ b;
-      const unsigned oc = c + (o & 1u) + ((o >> 1) & 1u) * (unsigned)ncx + (o >> 2) * ncxy;
-      const unsigned vi = voffsets[oc] + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
-      const float4 p = __ldg(V.pos + vi);
-      const unsigned pk = __float_as_uint(p.w);
-      const float aux = bf16_value(pk & 0xFFFFu);
-      X[q] = p.x;
-      Y[q] = p.y;
-      Z[q] = p.z;
-      exy = fmaxf(exy, bf16_value(pk >> 16));
-      if (aux >= 0.f) zr = fmaxf(zr, aux);
-      else if (aux == -1.f) status = 0;
-      else if (status != 0) status = -1;
+      const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
+      v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
+                         corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
     }
-    d3 v[3];
-    bool ok = true;
-    if (CHECK) {
-      /* the reference's own vertices and projection */
-      d3 p[3];
 #pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const int a = (int)((e >> (6 * q)) & 7), b = (int)((e >> (6 * q + 3)) & 7);
-        v[q] = interpolate(F.threshold, corner_pos(F, i, j, k, a), corner_value(F, i, j, k, a),
-                           corner_pos(F, i, j, k, b), corner_value(F, i, j, k, b));
-      }
+    for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
+    if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
+    if (status == 1 && ok) {
 #pragma unroll
-      for (int q = 0; q < 3; q++) ok = project(scene, v[q], p[q]) && ok;
-      if (status >= 0 && (status == 1) != ok) atomicAdd(checks + 0, 1u);
-      if (status == 1 && ok) {
-#pragma unroll
-        for (int q = 0; q < 3; q++)
-          if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
-              fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
-            atomicAdd(checks + 1, 1u);
-      }
-    }
-    if (status == 0) meta |= kMetaCulled;
-    if (status < 0) meta |= kMetaUndecided;
-    if (R.cover_count && status != 0) {
-      const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
-      float errA;
-      const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
-      const bool decided = status > 0 && isfinite(A) && isfinite(exy) && exy < 1e-3f && zr < 1e-3f;
-      if (!decided) {
-        route = 1;
-      } else if (!(fabsf(A) - errA > 1e-15f)) {
-        /* the area may be clamped to +-1e-16 (render.c:108-111): k_sliver
-           tests the reference's whole box */
-        route = 3;
-      } else {
-        /* the reference's area is certainly not clamped: its weights are
-           barycentric up to the -1e-8 slack, so every covered pixel centre
-           lies in the triangle's extent */
-        const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
-        const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
-        const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
-        long long imin, imax, jmin, jmax;
-        centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
-        centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
-        route = imin <= imax && jmin <= jmax ? 2 : 0;
-        if (CHECK && route == 0 && ok) {
-          /* no pixel of the reference's box may be covered */
-          ExactTri ex;
-          if (exact_tri(scene, v, ex))
-            for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
-              for (long long ii = ex.imin; ii <= ex.imax; ii++) {
-                double w0, w1, w2;
-                if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
-              }
-        }
-      }
+      for (int q = 0; q < 3; q++)
+        if (fabs((double)X[q] - p[q].x) > exy || fabs((double)Y[q] - p[q].y) > exy ||
+            fabs((double)Z[q] - p[q].z) > (double)zr * fabs((double)Z[q]))
+          atomicAdd(checks + 1, 1u);
     }
   }
-  /* the edge ids and flags serve inspection (vertex normals in k_normals);
-     the render path writes them too: a conditional store here cost seven
-     registers and a third of the resident warps */
-  tri.meta[t] = meta;
+  if (status == 0) return;
+  const EdgeF E2 = edge_f(X[0], Y[0], X[1], Y[1], exy);
+  float errA;
+  const float A = edge_eval(E2, X[2], Y[2], exy, exy, errA);
+  const bool decided = status > 0 && isfinite(A) && isfinite(exy) && exy < 1e-3f && zr < 1e-3f;
+  if (!decided) {
+    route = 1;
+  } else if (!(fabsf(A) - errA > 1e-15f)) {
+    /* the area may be clamped to +-1e-16 (render.c:108-111): the sliver
+       pass tests the reference's whole box */
+    route = 3;
+  } else {
+    /* the reference's area is certainly not clamped: its weights are
+       barycentric up to the -1e-8 slack, so every covered pixel centre
+       lies in the triangle's extent */
+    const float xext = fmaxf(X[0], fmaxf(X[1], X[2])) - fminf(X[0], fminf(X[1], X[2]));
+    const float yext = fmaxf(Y[0], fmaxf(Y[1], Y[2])) - fminf(Y[0], fminf(Y[1], Y[2]));
+    const float mb = exy + 1e-6f * (xext + yext) + 1e-12f;
+    long long imin, imax, jmin, jmax;
+    centre_range(fminf(X[0], fminf(X[1], X[2])) - mb, fmaxf(X[0], fmaxf(X[1], X[2])) + mb, W, imin, imax);
+    centre_range(fminf(Y[0], fminf(Y[1], Y[2])) - mb, fmaxf(Y[0], fmaxf(Y[1], Y[2])) + mb, H, jmin, jmax);
+    route = imin <= imax && jmin <= jmax ? 2 : 0;
+    if (CHECK && route == 0 && ok) {
+      /* no pixel of the reference's box may be covered */
+      ExactTri ex;
+      if (exact_tri(scene, v, ex))
+        for (long long jj = ex.jmin; jj <= ex.jmax; jj++)
+          for (long long ii = ex.imin; ii <= ex.imax; ii++) {
+            double w0, w1, w2;
+            if (exact_weights(ex, ii, jj, R.xs, R.ys, w0, w1, w2)) atomicAdd(checks + 2, 1u);
+          }
+    }
+  }
 }
 
 /* triangles per thread and iteration: one.  k_emit hides its gathers by
@@ -1711,7 +1729,7 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
    entry one iteration ahead, cost registers and measured slower */
 constexpr int kEmitPer = 1;
 
-template <typename T, bool CHECK>
+template <typename T, bool CHECK, bool RENDER>
 __global__ void __launch_bounds__(256)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
        const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
@@ -1741,9 +1759,9 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
     for (int u = 0; u < kEmitPer; u++) {
       o[u].route = 0;
       const long long t = base + u * (long long)blockDim.x + threadIdx.x;
-      if (t < T_) emit_one<T, CHECK>(F, S, scene, lut, codes, voffsets, tri_cell, tri, R, V, checks, t, o[u]);
+      if (t < T_) emit_one<T, CHECK, RENDER>(F, S, scene, lut, codes, voffsets, tri_cell, tri, R, V, checks, t, o[u]);
     }
-    if (R.cover_count) {
+    if (RENDER) {
       unsigned n1 = 0, n2 = 0, n3 = 0;
 #pragma unroll
       for (int u = 0; u < kEmitPer; u++) {
@@ -1936,9 +1954,9 @@ __device__ __noinline__ void cover_block(const Geo& G, const SceneDev& scene, co
           const float w1 = ai * edge_eval(E1, px, py, ep, eps, e1);
           const float w2 = ai * edge_eval(E2, px, py, ep, eps, e2);
           const float k = fabsf(ai) * (1.f + rai);
-          const float ew0 = 1.25f * (k * e0 + fabsf(w0) * (rai + kU32)) + 1e-30f;
-          const float ew1 = 1.25f * (k * e1 + fabsf(w1) * (rai + kU32)) + 1e-30f;
-          const float ew2 = 1.25f * (k * e2 + fabsf(w2) * (rai + kU32)) + 1e-30f;
+          const float ew0 = __fmaf_rn(1.25f, __fmaf_rn(k, e0, fabsf(w0) * (rai + kU32)), 1e-30f);
+          const float ew1 = __fmaf_rn(1.25f, __fmaf_rn(k, e1, fabsf(w1) * (rai + kU32)), 1e-30f);
+          const float ew2 = __fmaf_rn(1.25f, __fmaf_rn(k, e2, fabsf(w2) * (rai + kU32)), 1e-30f);
           const bool out = weights_ok && ((w0 + ew0 < kWOut) || (w1 + ew1 < kWOut) || (w2 + ew2 < kWOut));
           const bool inside = weights_ok && !out && (w0 - ew0 > kWIn) && (w1 - ew1 > kWIn) && (w2 - ew2 > kWIn);
           if (CHECK && ex_ok) {
@@ -3181,20 +3199,24 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
                  long long tri_bound, const TriDev& tri, const RasterDev& R, const VertDev& V, unsigned* checks,
                  cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, g_emit_per_sm);
-  if (checks) {
+  if (!R.cover_count) {
+    /* inspection: edge ids and flags only */
+    launch_k(k_emit<double, false, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+             tri_cell, total, tri, R, V, checks);
+  } else if (checks) {
     if (F.is_f32)
-      launch_k(k_emit<float, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
-               total, tri, R, V, checks);
+      launch_k(k_emit<float, true, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+               tri_cell, total, tri, R, V, checks);
     else
-      launch_k(k_emit<double, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
-               total, tri, R, V, checks);
+      launch_k(k_emit<double, true, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+               tri_cell, total, tri, R, V, checks);
   } else {
     if (F.is_f32)
-      launch_k(k_emit<float, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
-               total, tri, R, V, checks);
+      launch_k(k_emit<float, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+               tri_cell, total, tri, R, V, checks);
     else
-      launch_k(k_emit<double, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets, tri_cell,
-               total, tri, R, V, checks);
+      launch_k(k_emit<double, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+               tri_cell, total, tri, R, V, checks);
   }
 }
 
