@@ -430,8 +430,7 @@ struct Ctx {
   bool ready = false;
   cudaStream_t own_stream = nullptr;
   Buf lut, counts, scratch, dbg, field, nodes, canvas, rgb;
-  Buf nb_ent, nb_wn, nb_span; /* the FP64 shading pass's neighbour lists */
-  Buf zlo, win, checks, winfo, amb, shade_check;
+  Buf zlo, checks, winfo, shade_check;
   /* the per-slab arrays of one contour object's pass.  Unsynchronised frames
      run the objects of a slab on two lanes (the frame's stream and
      lane_stream), each with its own arrays; the passes of different objects
@@ -439,6 +438,11 @@ struct Ctx {
      whose updates are order-independent maxima and tagged stores */
   struct Lane {
     Buf offsets, voffsets, tile_state, tri_cell, tri, verts, cand, live, tiny;
+    /* one object's shading: its won pixels, those left to FP64, and the
+       FP64 pass's neighbour lists (unsynchronised frames shade the objects
+       of a field on both lanes; the passes meet only in the colour bits of
+       disjoint pixels) */
+    Buf win, amb, nb_ent, nb_wn, nb_span;
   };
   Lane lanes[2];
   cudaStream_t lane_stream = nullptr;
@@ -1437,15 +1441,24 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
   if (!sink) {
     /* every object's won pixels, shaded once after all of its slabs */
     const size_t npx = (size_t)(sd.width * sd.height);
-    if (c.win.ensure(sizeof(unsigned) * npx, st) || c.amb.ensure(sizeof(unsigned) * npx, st) ||
-        c.scratch.ensure(128, st))
-      return 1;
+    if (c.scratch.ensure(128, st)) return 1;
     if (c.filter_check && c.shade_check.ensure(sizeof(unsigned) * npx, st)) return 1;
     unsigned long long *counters = reinterpret_cast<unsigned long long *>(c.scratch.as<unsigned>() + 6);
     unsigned long long *h_cnt = h_total + 2;
     unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
+    /* unsynchronised frames: odd objects' shading on the second lane */
+    const int slanes = async && !c.stage_timing && nobj > 1 ? 2 : 1;
+    const cudaStream_t st_main = st;
+    if (slanes > 1) {
+      C3D_CUDA(cudaEventRecord(c.ev_lane_fork, st_main));
+      C3D_CUDA(cudaStreamWaitEvent(c.lane_stream, c.ev_lane_fork, 0));
+    }
     for (size_t ob = 0; ob < nobj; ob++) {
       const contour3d_color_t &col = objs[ob].color;
+      const bool odd_lane = slanes > 1 && (ob & 1);
+      Ctx::Lane &L = c.lanes[odd_lane ? 1 : 0];
+      const cudaStream_t st = odd_lane ? c.lane_stream : st_main; /* this object's shading */
+      if (L.win.ensure(sizeof(unsigned) * npx, st) || L.amb.ensure(sizeof(unsigned) * npx, st)) return 1;
       if (async) {
         /* the object's record of the frame status: won, ambiguous, neighbour entries */
         if (c.status_obj_next >= kStatusObjs) {
@@ -1455,9 +1468,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         counters = c.status.as<unsigned long long>() + kStatusHead + kSlabRec * kStatusSlabs + 3 * c.status_obj_next++;
       }
       RasterDev RS = R;
-      RS.win = c.win.as<unsigned>();
+      RS.win = L.win.as<unsigned>();
       RS.win_count = counters + 0;
-      RS.amb = c.amb.as<unsigned>();
+      RS.amb = L.amb.as<unsigned>();
       RS.amb_count = counters + 1;
       /* render.c:150-159 at the clamped factor: (unsigned char)(int)(0.15 * c) in FP64 */
       const int r8 = (int)(0.15 * (double)col.r), g8 = (int)(0.15 * (double)col.g), b8 = (int)(0.15 * (double)col.b);
@@ -1482,16 +1495,16 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* the FP64 pass over at most every pixel, its neighbour entries
            sized from the largest count seen; overflow shows in the status */
         const unsigned long long want = std::max<unsigned long long>(c.caps.ent, 1ULL << 16);
-        if (c.nb_ent.ensure(sizeof(unsigned long long) * want, st) || c.nb_wn.ensure(3 * sizeof(double) * want, st) ||
-            c.nb_span.ensure(sizeof(uint2) * 3 * npx, st))
+        if (L.nb_ent.ensure(sizeof(unsigned long long) * want, st) || L.nb_wn.ensure(3 * sizeof(double) * want, st) ||
+            L.nb_span.ensure(sizeof(uint2) * 3 * npx, st))
           return 1;
         const unsigned long long cap =
-            std::min(c.nb_ent.cap / sizeof(unsigned long long), c.nb_wn.cap / (3 * sizeof(double)));
+            std::min(L.nb_ent.cap / sizeof(unsigned long long), L.nb_wn.cap / (3 * sizeof(double)));
         c.async_ent_cap = std::min(c.async_ent_cap, cap);
         c.async_obj_fp32.push_back(fp32 ? 1 : 0);
         launch_shade_exact(Fs, sd, RS, c.lut.as<unsigned long long>(), list, lcount, (long long)npx, obase,
-                           c.nb_ent.as<unsigned long long>(), cap, counters + 2, c.nb_span.as<uint2>(),
-                           c.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
+                           L.nb_ent.as<unsigned long long>(), cap, counters + 2, L.nb_span.as<uint2>(),
+                           L.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
         c.stats.kernel_launches += 3 + (fp32 ? 2 : 1);
         continue;
       }
@@ -1503,15 +1516,15 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* about six neighbour triangles per vertex; more are listed again */
         unsigned long long want = 24 * namb + 1024;
         for (int attempt = 0;; attempt++) {
-          if (c.nb_ent.ensure(sizeof(unsigned long long) * want, st) || c.nb_wn.ensure(3 * sizeof(double) * want, st) ||
-              c.nb_span.ensure(sizeof(uint2) * 3 * namb, st))
+          if (L.nb_ent.ensure(sizeof(unsigned long long) * want, st) || L.nb_wn.ensure(3 * sizeof(double) * want, st) ||
+              L.nb_span.ensure(sizeof(uint2) * 3 * namb, st))
             return 1;
           const unsigned long long cap =
-              std::min(c.nb_ent.cap / sizeof(unsigned long long), c.nb_wn.cap / (3 * sizeof(double)));
+              std::min(L.nb_ent.cap / sizeof(unsigned long long), L.nb_wn.cap / (3 * sizeof(double)));
           C3D_CUDA(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), st));
           launch_shade_exact(Fs, sd, RS, c.lut.as<unsigned long long>(), list, lcount, (long long)namb, obase,
-                             c.nb_ent.as<unsigned long long>(), cap, counters + 2, c.nb_span.as<uint2>(),
-                             c.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
+                             L.nb_ent.as<unsigned long long>(), cap, counters + 2, L.nb_span.as<uint2>(),
+                             L.nb_wn.as<double>(), rgb, fp32 ? checks : nullptr, st);
           c.stats.kernel_launches += 3;
           C3D_CUDA(cudaMemcpyAsync(h_cnt + 2, counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
           C3D_CUDA(cudaStreamSynchronize(st));
@@ -1535,6 +1548,10 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         c.stats.ms_normals += elapsed(c.evs[6], c.evs[10]);
         c.stats.ms_shade += elapsed(c.evs[10], c.evs[7]);
       }
+    }
+    if (slanes > 1) {
+      C3D_CUDA(cudaEventRecord(c.ev_lane_join, c.lane_stream));
+      C3D_CUDA(cudaStreamWaitEvent(st_main, c.ev_lane_join, 0));
     }
   }
   order_base += 12ULL * (unsigned long long)(ncx * ncy * ncz) * nobj;
@@ -2358,10 +2375,10 @@ extern "C" int contour3d_gb300_release(void) {
 /* every device buffer of a context; the constant table (lut) first */
 static std::vector<Buf *> ctx_bufs(Ctx &c) {
   std::vector<Buf *> v = {&c.lut, &c.counts, &c.scratch, &c.dbg, &c.field, &c.consts, &c.nodes, &c.canvas,
-                          &c.rgb, &c.zlo, &c.win, &c.nb_ent, &c.nb_wn, &c.nb_span, &c.winfo, &c.amb,
-                          &c.shade_check, &c.checks, &c.status};
+                          &c.rgb, &c.zlo, &c.winfo, &c.shade_check, &c.checks, &c.status};
   for (Ctx::Lane &L : c.lanes)
-    for (Buf *b : {&L.offsets, &L.voffsets, &L.tile_state, &L.tri_cell, &L.tri, &L.verts, &L.cand, &L.live, &L.tiny})
+    for (Buf *b : {&L.offsets, &L.voffsets, &L.tile_state, &L.tri_cell, &L.tri, &L.verts, &L.cand, &L.live, &L.tiny,
+                   &L.win, &L.amb, &L.nb_ent, &L.nb_wn, &L.nb_span})
       v.push_back(b);
   return v;
 }
