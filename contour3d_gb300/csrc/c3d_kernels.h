@@ -104,6 +104,7 @@ struct TriDev {
   double* dbg_fn;     /* inspection: face normals, 3 per triangle */
   double* dbg_area;   /* inspection: areas */
   unsigned long long cap; /* triangles the arrays (and the triangle -> cell map) hold */
+  unsigned long long rec_cap; /* records the cover and sliver region holds (the arrays' size) */
   unsigned* ovf;      /* overflow flags (kOvf*): set when the slab's triangles exceed cap */
 };
 constexpr unsigned kMetaRendered = 1u << 15;
@@ -162,10 +163,13 @@ struct RasterDev {
   unsigned* tiny;           /* triangles the FP32 filter cannot settle */
   unsigned long long tiny_cap;
   unsigned long long* tiny_count;
-  unsigned long long* cover_count; /* entries of TriDev::rec (at most the slab's triangles) */
+  unsigned long long* cover_count; /* entries of TriDev::rec: the cover triangles and the
+                                      empty ends of k_emit's chunks (kNoTri) */
   float4* sliver_rec;       /* slivers, in the same records, from the top of TriDev::rec
-                               down: entry s at sliver_rec - 3 s (cover + sliver <= triangles) */
+                               down: entry s at sliver_rec - 3 s (cover + sliver entries
+                               <= triangles + emit_list_slack) */
   unsigned long long* sliver_count;
+  unsigned long long* listed_count; /* [0] cover, [1] sliver entries, without the empty ones */
   Candidate* live;          /* candidates that can still win (capacity cand_cap) */
   unsigned long long* live_count;
   /* per pixel, the exact weights of the fragment that last won its CAS: three
@@ -254,6 +258,9 @@ cudaError_t launch_scan(const unsigned char* codes, long long n, unsigned long l
                         cudaStream_t st);
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
                      const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
+/* record entries beyond the triangles that k_emit's lists may leave empty
+   for a launch sized by tri_bound (the region must hold triangles + this) */
+unsigned long long emit_list_slack(long long tri_bound);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets, const unsigned* voffsets,
                  const unsigned* tri_cell, const unsigned long long* total, long long tri_bound, const TriDev& tri,

@@ -1729,8 +1729,57 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
    entry one iteration ahead, cost registers and measured slower */
 constexpr int kEmitPer = 1;
 
+/*
+ * List appends without block barriers: each warp takes chunks of entries
+ * from a list's counter (one atomic per chunk) and fills them with warp
+ * ballots; a batch that does not fit the chunk's rest starts the next
+ * chunk.  At the warp's end the rest of its last chunk is marked empty
+ * (kNoTri), so a list holds its entries and fewer than one chunk of empty
+ * ones per warp; the raster passes skip those.  A chunk is the smallest
+ * multiple of the list's unit that holds the rest of a batch; the sparse
+ * sliver list (about 2 % of the triangles) takes a small unit so that its
+ * empty entries stay few.
+ */
+constexpr unsigned kCoverChunk = 32, kSliverChunk = 8;
+constexpr unsigned kEmitRun = 8; /* runs of 32 consecutive triangles per warp and window */
+constexpr unsigned kNoTri = 0xFFFFFFFFu;
+
+/* record entries beyond the triangles that a grid of `blocks` k_emit blocks
+   may leave empty (two lists, one partial chunk per warp and list) */
+__host__ __device__ __forceinline__ unsigned long long emit_slack_for(unsigned long long blocks) {
+  return (unsigned long long)(kCoverChunk + kSliverChunk) * blocks * (256 / 32);
+}
+
+/* the list slot of this lane's entry (when `take`), every lane of the warp
+   calling with the same chunk state */
+template <unsigned kChunk>
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long* count, bool take, unsigned lane,
+                                                          unsigned below, unsigned long long& cbase,
+                                                          unsigned& cfill, unsigned& csize,
+                                                          unsigned long long& taken) {
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, take);
+  if (m == 0u) return 0ULL;
+  const unsigned n = __popc(m), rank = __popc(m & below), room = csize - cfill;
+  taken += n;
+  unsigned long long slot = cbase + cfill + rank;
+  if (n > room) {
+    /* the next chunk: whole multiples of kChunk holding the batch's rest */
+    const unsigned size = (n - room + kChunk - 1) / kChunk * kChunk;
+    unsigned long long nb = 0;
+    if (lane == 0) nb = atomicAdd(count, (unsigned long long)size);
+    nb = __shfl_sync(0xFFFFFFFFu, nb, 0);
+    if (rank >= room) slot = nb + (rank - room);
+    cbase = nb;
+    cfill = n - room;
+    csize = size;
+  } else {
+    cfill += n;
+  }
+  return slot;
+}
+
 template <typename T, bool CHECK, bool RENDER>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, CHECK ? 1 : 8)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
        const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
        const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
@@ -1743,50 +1792,79 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
   __syncthreads();
   pdl_wait();
   const long long T_ = (long long)*total_p;
-  if ((unsigned long long)T_ > tri.cap || (V.pos && total_p[1] > V.cap)) {
+  /* the record region holds the cover and sliver entries (at most the
+     triangles) and every warp's unfilled chunk ends */
+  const unsigned long long slack = RENDER ? emit_slack_for(gridDim.x) : 0ULL;
+  if ((unsigned long long)T_ > tri.cap || (unsigned long long)T_ + slack > tri.rec_cap ||
+      (V.pos && total_p[1] > V.cap)) {
     /* more triangles than the arrays hold, or more crossed edges than vertex
        records (sized before the counts were known): nothing is read or
        written, the frame is rendered again */
     if (blockIdx.x == 0 && threadIdx.x == 0)
-      atomicOr(tri.ovf, (unsigned long long)T_ > tri.cap ? kOvfTriangles : kOvfVertices);
+      atomicOr(tri.ovf, (unsigned long long)T_ + slack > tri.rec_cap || (unsigned long long)T_ > tri.cap
+                            ? kOvfTriangles
+                            : kOvfVertices);
     return;
   }
-  const long long step = (long long)blockDim.x * kEmitPer;
-  /* every thread of a block runs the same iterations (block-wide appends) */
-  for (long long base = blockIdx.x * step; base < T_; base += (long long)gridDim.x * step) {
+  const unsigned lane = threadIdx.x & 31u, below = (1u << lane) - 1u;
+  /* the grid works through windows of the slab's triangles, small enough
+     that a window's cells and vertex records stay in L2 (blocks with ranges
+     of their own measured slower: 1.59 -> 1.82 ms per frame); within a
+     window each warp takes kEmitRun consecutive runs of 32, so the entries
+     of a list chunk lie close together in the field and on screen, as the
+     raster passes like them (a slab's triangles are numbered in 32 bits) */
+  const unsigned long long tcount = (unsigned long long)T_;
+  const unsigned long long window = (unsigned long long)gridDim.x * blockDim.x * kEmitRun;
+  /* this thread's place in a window: its warp's runs, its lane */
+  const unsigned toff = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) * kEmitRun + lane;
+  /* the warp's current chunk of each list: `size` entries from `base` on,
+     `fill` of them taken (size 0: none yet) */
+  unsigned long long cbase = 0, sbase = 0, ctaken = 0, staken = 0;
+  unsigned cfill = 0, csize = 0, sfill = 0, ssize = 0;
+  /* every thread of a block runs the same iterations (warp-wide appends);
+     iteration it is run it % kEmitRun of window it / kEmitRun */
+  for (unsigned long long it = 0;; it++) {
+    const unsigned long long wbase = (it / kEmitRun) * window + (it % kEmitRun) * 32;
+    if (wbase + (unsigned long long)blockIdx.x * blockDim.x * kEmitRun >= tcount) break; /* the block's first */
     EmitOut o[kEmitPer];
+    const unsigned long long tw = wbase + toff;
 #pragma unroll
     for (int u = 0; u < kEmitPer; u++) {
       o[u].route = 0;
-      const long long t = base + u * (long long)blockDim.x + threadIdx.x;
-      if (t < T_) emit_one<T, CHECK, RENDER>(F, S, scene, lut, codes, voffsets, tri_cell, tri, R, V, checks, t, o[u]);
+      if (tw < tcount) emit_one<T, CHECK, RENDER>(F, S, scene, lut, codes, voffsets, tri_cell, tri, R, V, checks,
+                                                  (long long)tw, o[u]);
     }
     if (RENDER) {
-      unsigned n1 = 0, n2 = 0, n3 = 0;
 #pragma unroll
       for (int u = 0; u < kEmitPer; u++) {
-        n1 += o[u].route == 1;
-        n2 += o[u].route == 2;
-        n3 += o[u].route == 3;
-      }
-      unsigned long long ti, ci, si;
-      block_reserve3<256, kEmitPer>(R.tiny_count, n1, R.cover_count, n2, R.sliver_count, n3, ti, ci, si);
-#pragma unroll
-      for (int u = 0; u < kEmitPer; u++) {
-        const unsigned t = (unsigned)(base + u * (long long)blockDim.x + threadIdx.x);
+        const unsigned t = (unsigned)tw;
         const EmitOut& e = o[u];
+        /* the tiny list holds a few thousand entries per frame: one atomic each */
         if (e.route == 1) {
+          const unsigned long long ti = atomicAdd(R.tiny_count, 1ULL);
           if (ti < R.tiny_cap) R.tiny[ti] = t; /* overflow: the host re-runs the slab */
-          ti++;
-        } else if (e.route >= 2) {
-          /* cover and sliver entries together number at most the slab's triangles */
-          float4* rec = e.route == 2 ? tri.rec + 3 * (ci++) : R.sliver_rec - 3 * (si++);
+        }
+        const unsigned long long ci =
+            warp_append<kCoverChunk>(R.cover_count, e.route == 2, lane, below, cbase, cfill, csize, ctaken);
+        const unsigned long long si =
+            warp_append<kSliverChunk>(R.sliver_count, e.route == 3, lane, below, sbase, sfill, ssize, staken);
+        if (e.route >= 2) {
+          float4* rec = e.route == 2 ? tri.rec + 3 * ci : R.sliver_rec - 3 * si;
           rec[0] = make_float4(e.X[0], e.Y[0], e.Z[0], e.X[1]);
           rec[1] = make_float4(e.Y[1], e.Z[1], e.X[2], e.Y[2]);
           rec[2] = make_float4(e.Z[2], e.exy, e.zr, __uint_as_float(t));
         }
       }
     }
+  }
+  if (RENDER) {
+    /* the unfilled ends of the warp's last chunks are marked empty */
+    const float4 none = make_float4(0.f, 0.f, 0.f, __uint_as_float(kNoTri));
+    for (unsigned q = cfill + lane; q < csize; q += 32) tri.rec[3 * (cbase + q) + 2] = none;
+    for (unsigned q = sfill + lane; q < ssize; q += 32) R.sliver_rec[2 - 3 * (long long)(sbase + q)] = none;
+    /* the entries themselves, for the statistics */
+    if (lane == 0 && ctaken) atomicAdd(R.listed_count, ctaken);
+    if (lane == 0 && staken) atomicAdd(R.listed_count + 1, staken);
   }
 }
 
@@ -1894,9 +1972,14 @@ __device__ __noinline__ void cover_block(const Geo& G, const SceneDev& scene, co
     unsigned pix[kCandBuf];
     unsigned nb = 0, t32 = 0;
     float dhi = 0.f;
+    const long long qq = scene.z_descending ? n - 1 - q : q;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = make_float4(0.f, 0.f, 0.f, __uint_as_float(kNoTri));
     if (q < n) {
-      const long long qq = scene.z_descending ? n - 1 - q : q;
-      const float4 r0 = __ldg(tri.rec + 3 * qq), r1 = __ldg(tri.rec + 3 * qq + 1), r2 = __ldg(tri.rec + 3 * qq + 2);
+      r0 = __ldg(tri.rec + 3 * qq);
+      r1 = __ldg(tri.rec + 3 * qq + 1);
+      r2 = __ldg(tri.rec + 3 * qq + 2);
+    }
+    if (__float_as_uint(r2.w) != kNoTri) { /* an entry, not a chunk's empty end */
       const long long t = (long long)__float_as_uint(r2.w);
       const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
       const float eps = r2.y, zr = r2.z;
@@ -2135,9 +2218,14 @@ __device__ __noinline__ void sliver_block(const Geo& G, const SceneDev& scene, c
     const long long q = base + threadIdx.x;
     bool to_tiny = false;
     unsigned t32 = 0;
+    const float4* rec = R.sliver_rec - 3 * q;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = make_float4(0.f, 0.f, 0.f, __uint_as_float(kNoTri));
     if (q < n) {
-      const float4* rec = R.sliver_rec - 3 * q;
-      const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+      r0 = __ldg(rec);
+      r1 = __ldg(rec + 1);
+      r2 = __ldg(rec + 2);
+    }
+    if (__float_as_uint(r2.w) != kNoTri) { /* an entry, not a chunk's empty end */
       t32 = __float_as_uint(r2.w);
       const float X[3] = {r0.x, r0.w, r1.z}, Y[3] = {r0.y, r1.x, r1.w}, Z[3] = {r0.z, r1.y, r2.x};
       const float eps = r2.y, zr = r2.z;
@@ -3218,6 +3306,10 @@ void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, con
       launch_k(k_emit<double, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
                tri_cell, total, tri, R, V, checks);
   }
+}
+
+unsigned long long emit_list_slack(long long tri_bound) {
+  return emit_slack_for((unsigned long long)grid_for(tri_bound, 256, g_emit_per_sm));
 }
 
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,

@@ -766,8 +766,9 @@ static const int kStatusSlabs = 1024;
 static const int kStatusObjs = 256;
 
 /* device counters of one slab's raster passes: candidates, tiny triangles,
-   won pixels, requested normals, listed triangles, surviving candidates,
-   slivers, pixels shaded in FP64, their FP64 normal requests */
+   cover and sliver triangles, the cover list's entries (with the empty ends
+   of k_emit's chunks), surviving candidates, the sliver list's entries, two
+   unused */
 static const int kCounters = 9;
 static const int kSlabRec = 2 + kCounters;
 static const size_t kStatusWords = kStatusHead + (size_t)kSlabRec * kStatusSlabs + 3 * (size_t)kStatusObjs;
@@ -1226,7 +1227,8 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         /* sized before the count is known, from the largest slab seen so
            far; kernels that find more record an overflow and the frame is
            rendered again */
-        if (L.tri_cell.ensure(sizeof(unsigned) * c.caps.T, st) || L.tri.ensure(kTriBytes * (c.caps.T + 64), st))
+        if (L.tri_cell.ensure(sizeof(unsigned) * c.caps.T, st) ||
+            L.tri.ensure(kTriBytes * (c.caps.T + 64 + emit_list_slack((long long)c.caps.T)), st))
           return 1;
       }
       /* read per object: an earlier object of the slab may have grown the buffer */
@@ -1263,10 +1265,12 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       }
       /* the float4 records start at byte 24 * cap: keep cap a multiple of 32 so
          every sub-array stays aligned (and over-allocate so that cap >= T) */
-      if (L.tri_cell.ensure(sizeof(unsigned) * T, st) || L.tri.ensure(kTriBytes * (T + 64), st)) return 1;
+      /* the record region also holds the empty ends of k_emit's list chunks */
+      const unsigned long long slack = sink ? 0ULL : emit_list_slack((long long)T);
+      if (L.tri_cell.ensure(sizeof(unsigned) * T, st) || L.tri.ensure(kTriBytes * (T + 64 + slack), st)) return 1;
       const size_t cap = (L.tri.cap / kTriBytes) & ~(size_t)31;
-      if (cap < T) {
-        log_error("internal: triangle buffer capacity %zu below %llu", cap, T);
+      if (cap < T + slack) {
+        log_error("internal: triangle buffer capacity %zu below %llu", cap, T + slack);
         return 1;
       }
       double *dbg = nullptr;
@@ -1275,6 +1279,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         dbg = c.dbg.as<double>();
       }
       TriDev tri = tri_layout(L.tri.p, cap, dbg);
+      tri.rec_cap = cap;
       tri.cap = std::min<unsigned long long>(cap, L.tri_cell.cap / sizeof(unsigned));
       tri.ovf = d_ovf;
       unsigned *checks = c.filter_check ? c.checks.as<unsigned>() : nullptr;
@@ -1334,6 +1339,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         RS.cover_count = counters + 4;
         RS.live_count = counters + 5;
         RS.sliver_count = counters + 6;
+        RS.listed_count = counters + 2;
         RS.sliver_rec = tri.rec + 3 * (cap - 1);
         for (int attempt = 0;; attempt++) {
           if (L.cand.ensure(sizeof(Candidate) * cand_want, st) || L.live.ensure(sizeof(Candidate) * cand_want, st) ||
@@ -1380,9 +1386,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         if (!async) {
           c.stats.candidates += h_cnt[0];
           c.stats.tiny += h_cnt[1];
-          c.stats.cover_triangles += h_cnt[4];
+          c.stats.cover_triangles += h_cnt[2];
           c.stats.exact_fragments += h_cnt[5];
-          c.stats.slivers += h_cnt[6];
+          c.stats.slivers += h_cnt[3];
           c.caps.cand = std::max(c.caps.cand, h_cnt[0] + h_cnt[0] / 4);
           c.caps.tiny = std::max(c.caps.tiny, h_cnt[1] + h_cnt[1] / 4);
         }
@@ -1783,9 +1789,9 @@ static int frame_status(Ctx &c, bool async) {
       c.stats.vertices += r[1];
       c.stats.candidates += cnt[0];
       c.stats.tiny += cnt[1];
-      c.stats.cover_triangles += cnt[4];
+      c.stats.cover_triangles += cnt[2];
       c.stats.exact_fragments += cnt[5];
-      c.stats.slivers += cnt[6];
+      c.stats.slivers += cnt[3];
       over = over || cnt[0] > c.async_cand_cap || cnt[1] > c.async_tiny_cap;
       c.caps.T = std::max(c.caps.T, r[0]);
       c.caps.V = std::max(c.caps.V, r[1]);
