@@ -61,9 +61,9 @@ CPU_SAMPLE_SLICES_1 = 16  # z-nodes of the 512^2 x 512 field timed on one host c
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
     "classify": (4.63, "cells"),     # k_classify_tma, both levels in one pass: 154.0 MB for 2 x 16.6 M cells
-    "scan": (5.49, "cells"),         # k_seg_reduce + k_seg_scan + k_scan_write: 91.1 MB for 16.6 M cells
+    "scan": (4.49, "cells"),         # k_scan (single pass with look-back): 74.5 MB for 16.6 M cells
     "vertices": (36.5, "vertices"),  # k_vertices: 239.2 MB for 6.55 M vertices
-    "emit": (43.5, "triangles"),     # k_emit: 570.3 MB for 13.1 M triangles
+    "emit": (42.2, "triangles"),     # k_emit: 552.6 MB for 13.1 M triangles
 }
 
 
@@ -692,7 +692,7 @@ def main():
         "classify": nodes * 8 + 2 * cells * 1,  # one pass over the field for both levels
         "scan": 2 * cells * (1 + 4) + T * 4,
         "vertices": 2 * cells * (4 + 1) + V * (2 * 8 + 16),
-        "emit": T * (4 + 4) + 2 * cells * (4 + 1) + V * 16 + listed * 48 + float(prof.tiny) * 4,
+        "emit": T * 4 + 2 * cells * (4 + 1) + V * 16 + listed * 48 + float(prof.tiny) * 4,
         "cover": listed * 48 + float(prof.candidates) * 16,
         "exact": float(prof.candidates) * (16 + 4) + float(prof.exact_fragments) * 16,
         "normals": WIDTH * HEIGHT * 16 * 2 + float(prof.winners) * (4 + 48 + 8),

@@ -1447,45 +1447,6 @@ __device__ __forceinline__ void block_reserve2(unsigned long long* count0, unsig
   __syncthreads();
 }
 
-/* the same for three lists of at most kPer items per thread */
-template <int kThreads, int kPer>
-__device__ __forceinline__ void block_reserve3(unsigned long long* count0, unsigned n0, unsigned long long* count1,
-                                               unsigned n1, unsigned long long* count2, unsigned n2,
-                                               unsigned long long& r0, unsigned long long& r1, unsigned long long& r2) {
-  static_assert(kThreads * kPer < 1024, "10-bit fields: at most kPer items per thread and list");
-  __shared__ unsigned s_w[kThreads / 32];
-  __shared__ unsigned long long s_b[3];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned x = (unsigned)n0 | ((unsigned)n1 << 10) | ((unsigned)n2 << 20);
-  unsigned incl = x;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-    if (lane >= d) incl += y;
-  }
-  if (lane == 31) s_w[warp] = incl;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned run = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; w++) {
-      const unsigned v = s_w[w];
-      s_w[w] = run;
-      run += v;
-    }
-    const unsigned t0 = run & 1023u, t1 = (run >> 10) & 1023u, t2 = run >> 20;
-    s_b[0] = t0 ? atomicAdd(count0, (unsigned long long)t0) : 0ULL;
-    s_b[1] = t1 ? atomicAdd(count1, (unsigned long long)t1) : 0ULL;
-    s_b[2] = t2 ? atomicAdd(count2, (unsigned long long)t2) : 0ULL;
-  }
-  __syncthreads();
-  const unsigned ex = s_w[warp] + incl - x;
-  r0 = s_b[0] + (ex & 1023u);
-  r1 = s_b[1] + ((ex >> 10) & 1023u);
-  r2 = s_b[2] + (ex >> 20);
-  __syncthreads();
-}
-
 template <int kThreads>
 __device__ __forceinline__ unsigned long long block_reserve(unsigned long long* count, unsigned n) {
   unsigned long long r0, r1;
