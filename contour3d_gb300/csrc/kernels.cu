@@ -2810,9 +2810,15 @@ k_nb_list(FieldDev F, RasterDev R, const unsigned long long* __restrict__ lut_g,
     if (q < n) {
       const bool fits = first + cnt <= ent_cap;
       spans[q] = make_uint2((unsigned)first, ok && fits ? cnt : 0xFFFFFFFFu);
-      if (ok && fits) {
+      if (ok) {
+        /* the entries below ent_cap are written even when the span does not
+           fit whole: k_nb_wn takes every entry below min(count, ent_cap),
+           and one left unwritten would hold a stale (cell, rank) word */
         unsigned long long at = first;
-        for_edge_triangles(F, lut, wc.i, wc.j, wc.k, ed, [&](unsigned long long x) { ent[at++] = x; });
+        for_edge_triangles(F, lut, wc.i, wc.j, wc.k, ed, [&](unsigned long long x) {
+          if (at < ent_cap) ent[at] = x;
+          at++;
+        });
       }
     }
   }
@@ -2831,6 +2837,7 @@ k_nb_wn(FieldDev F, const unsigned long long* __restrict__ lut, const unsigned l
     const unsigned long long x = ent[q], cell = x >> 4, row = cell / ncx;
     const long long i = (long long)(cell - row * ncx), k = (long long)(row / ncy);
     const long long j = (long long)(row - (unsigned long long)k * ncy);
+    if (k >= F.nz - 1 || (x & 15) >= 12) continue; /* not a cell of the field: never read past it */
     double vals[8];
     const unsigned code = cell_code_any(F, i, j, k, vals);
     const unsigned long long e = __ldg(lut + code * 12 + (x & 15));

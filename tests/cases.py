@@ -20,9 +20,9 @@ def blobs_small():
     return s
 
 
-def modes_warp():
+def modes_warp(width=128, height=96):
     f, std = fields.modes((17, 13, 21), nmodes=16, kmin=1, kmax=4, power=5.0 / 6.0, seed=7)
-    s = _abi.make_scene((2.2, -1.6, 1.8), CENTRE, 128, 96, light=(1.0, 0.5, -0.5))
+    s = _abi.make_scene((2.2, -1.6, 1.8), CENTRE, width, height, light=(1.0, 0.5, -0.5))
     s.contours = [_abi.Contour(f, -0.5 * std, (255, 128, 0), converter="warp"),
                   _abi.Contour(f, 0.5 * std, (64, 200, 255), converter="warp")]
     return s

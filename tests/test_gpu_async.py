@@ -72,6 +72,32 @@ def test_overflow_renders_the_frame_again(gpu):
     assert gpu.stats().unsynchronised == 1 and np.array_equal(img, img2)
 
 
+def test_shading_list_overflow_renders_the_frame_again(gpu, oracle):
+    """The FP64 shading pass's neighbour lists, sized from another scene, are
+    too small for a scene whose every won pixel takes that pass (a
+    non-identity converter) at a larger image: the unsynchronised frame
+    records the overflow and is rendered again, to the oracle's image.  The
+    pass that overflowed still computes every list entry below the lists'
+    capacity, so none of them is a stale word from an earlier frame."""
+    gpu.release()  # forget the sizes learnt so far
+    # more triangles and candidates than the converter scene, few FP64 pixels
+    learn = cases.config0()
+    gpu.render(learn)
+    gpu.render(learn)
+    st = gpu.stats()
+    assert st.unsynchronised == 1
+    learnt = st.normals
+    big = cases.modes_warp(768, 576)
+    img = gpu.render(big)
+    st = gpu.stats()
+    # the unsynchronised pass had room for about max(1.25 x learnt, 2^16) entries
+    assert st.normals > 2 * max(learnt, 1 << 16), (st.normals, learnt)
+    assert st.redone == 1 and st.unsynchronised == 0
+    assert np.array_equal(img, oracle.render(big))
+    img2 = gpu.render(big)
+    assert gpu.stats().unsynchronised == 1 and np.array_equal(img, img2)
+
+
 def test_repeated_device_frame_runs_as_a_graph(gpu, oracle):
     """An in-situ loop: the same device field, levels and camera every step,
     new field values.  The second frame with one description is recorded as
