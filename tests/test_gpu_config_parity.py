@@ -9,7 +9,9 @@ checked against the oracle at full size:
   the oracle's image byte for byte, per-cell triangle counts equal;
 - three frames of the 64-field batched workload (a float32 field, a frame
   with four levels, the most elongated field near 384 nodes), rendered alone
-  and inside the batched form, against the oracle on the widened field.
+  and inside the batched form, against the oracle on the widened field;
+- the 1536^3 float32 workload's levels, camera and 3840 x 2160 image on the
+  field's 256^3 centre crop, in one slab and in many.
 
 The oracle runs with one emulated z-split rank per host core (the image does
 not depend on the split: the nearest-depth reduction is exact).
@@ -130,3 +132,51 @@ def test_batched_workload_frames_match_oracle(gpu, oracle):
         ref = oracle.render(scene, nranks=CORES).reshape(-1)
         assert np.array_equal(alone[q], ref), f"frame {q} ({tuple(f.shape)}, {f.dtype}) differs alone"
         assert np.array_equal(outs[q].cpu().numpy(), ref), f"frame {q} differs inside the batch"
+
+
+def test_large_workload_crop_matches_oracle(gpu, oracle):
+    """The 1536^3 float32 field's workload (256 Fourier modes, |k| 1..48,
+    |k|^-11/6, four levels at +-0.5 and +-1 std, 3840 x 2160) on the 256^3
+    centre crop of the field: filter self-check on, the oracle's image on
+    the widened values byte for byte, and the crop split into slabs of a few
+    slices each (the 1536^3 frame takes 21 slabs per level) drawing the same
+    image."""
+    import torch
+    n, crop = 1536, 256
+    off = (n - crop) // 2
+    dev = torch.empty((crop,) * 3, dtype=torch.float32, device="cuda")
+    std = gpu.fieldgen_modes_device(dev.data_ptr(), 1, (crop,) * 3, 256, 1, 48, 11.0 / 6.0, 4, offset=(off,) * 3,
+                                    glshape=(n, n, n))
+    grids = [_abi.unit_grid(n)[off:off + crop]] * 3
+    levels = list(zip([-std, -0.5 * std, 0.5 * std, std], workloads.PALETTE))
+    scene = _abi.make_scene(cases.CAM0, cases.CENTRE, 3840, 2160)
+    W, H = scene.width, scene.height
+    fl = [(dev.data_ptr(), 1, (crop,) * 3, grids, t, c) for t, c in levels]
+    out = torch.zeros(W * H * 3, dtype=torch.uint8, device="cuda")
+    gpu.set_filter_check(True)
+    try:
+        rc = gpu.render_device(scene, fl, out.data_ptr())
+        torch.cuda.synchronize()
+        st = gpu.stats()
+    finally:
+        gpu.set_filter_check(False)
+    assert rc == 0
+    assert list(st.filter_violations) == [0, 0, 0, 0, 0], "an FP32 raster decision left its bound"
+    assert st.shade_violations == 0, "an FP32 colour differs from the FP64 one"
+    img = out.cpu().numpy().reshape(H, W, 3)
+    host = dev.double().cpu().numpy()  # the float32 values widened exactly
+    scene.contours = [_abi.Contour(host, t, c, grids=tuple(grids)) for t, c in levels]
+    ref = oracle.render(scene, nranks=CORES)
+    scene.contours = []
+    diff = (img != ref).any(axis=2)
+    assert diff.sum() == 0, f"{int(diff.sum())} pixels differ from the oracle"
+    # many slabs per level: the image does not change
+    gpu.set_slab_cells(12 * (crop - 1) ** 2)
+    try:
+        out.zero_()
+        assert gpu.render_device(scene, fl, out.data_ptr()) == 0
+        torch.cuda.synchronize()
+        assert gpu.stats().slabs > 4 * 4
+    finally:
+        gpu.set_slab_cells(178956970)  # the default
+    assert np.array_equal(out.cpu().numpy().reshape(H, W, 3), ref)
