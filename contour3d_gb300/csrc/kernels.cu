@@ -426,6 +426,41 @@ k_classify_queue(const ClsItem* __restrict__ items, int nitems, unsigned long lo
 }
 
 /*
+ * k_classify_multi: the codes of up to kMaxThr objects of one field in one
+ * pass over its nodes, one brick per block (the brick code of
+ * k_classify_queue) -- the classification of fields whose rows TMA cannot
+ * address (a row pitch that is not a multiple of 16 bytes, such as an odd
+ * node count along x for a double field).
+ */
+template <typename T>
+__global__ void __launch_bounds__(kClsX, 6)
+k_classify_multi(const void* __restrict__ data, long long nx, long long ny, SlabDev S, ThrSet ts, CodeOut out) {
+  pdl_enter();
+  __shared__ unsigned char bits[2][kClsY + 1][kClsX + 1];
+  /* the brick's description in shared memory, as k_classify_queue keeps it
+     (in registers it spilled) */
+  __shared__ QueueBrick s_qb;
+  __shared__ ThrSet s_ts;
+  if (threadIdx.x == 0) {
+    s_qb.data = data;
+    for (int t = 0; t < kMaxThr; t++) s_qb.codes[t] = out.codes[t];
+    s_qb.nx = nx;
+    s_qb.ny = ny;
+    s_qb.kfirst = S.kfirst;
+    s_qb.k0 = (long long)blockIdx.z * S.cls_z;
+    s_qb.k1 = min(s_qb.k0 + S.cls_z, S.nslices);
+    s_qb.i0 = blockIdx.x * kClsX;
+    s_qb.j0 = blockIdx.y * kClsY;
+    s_qb.ncx = (unsigned)(nx - 1);
+    s_qb.ncy = (unsigned)(ny - 1);
+    s_qb.nt = ts.n;
+    s_ts = ts;
+  }
+  __syncthreads();
+  classify_queue_brick<T>(s_qb, s_ts, bits);
+}
+
+/*
  * k_classify_tma: the same codes, with the node planes staged by TMA.  A
  * block owns kClsX x kClsY cells of kClsZ slices; each of its node planes
  * (TmaBox<T>::kX x (kClsY + 1) nodes, x from the tile start, so the copy starts on
@@ -3194,11 +3229,22 @@ int launch_classify(const FieldDev* Fs, int nf, const SlabDev& S0, unsigned char
     }
     return (nf + kMaxThr - 1) / kMaxThr;
   }
-  for (int q = 0; q < nf; q++) {
-    if (F.is_f32) launch_k(k_classify<float>, "k_classify", grid, kClsX, 0, st, Fs[q], S, codes[q]);
-    else launch_k(k_classify<double>, "k_classify", grid, kClsX, 0, st, Fs[q], S, codes[q]);
+  /* rows TMA cannot address: plain loads, still one pass per kMaxThr objects */
+  for (int q0 = 0; q0 < nf; q0 += kMaxThr) {
+    ThrSet ts;
+    CodeOut out;
+    ts.n = min(kMaxThr, nf - q0);
+    for (int t = 0; t < ts.n; t++) {
+      thr_range(Fs[q0 + t], ts, t);
+      out.codes[t] = codes[q0 + t];
+    }
+    for (int t = ts.n; t < kMaxThr; t++) out.codes[t] = nullptr;
+    if (F.is_f32)
+      launch_k(k_classify_multi<float>, "k_classify_multi", grid, kClsX, 0, st, F.data, F.nx, F.ny, S, ts, out);
+    else
+      launch_k(k_classify_multi<double>, "k_classify_multi", grid, kClsX, 0, st, F.data, F.nx, F.ny, S, ts, out);
   }
-  return nf;
+  return (nf + kMaxThr - 1) / kMaxThr;
 }
 
 void make_cls_item(const FieldDev* Fs, int nf, const SlabDev& S, unsigned char* const* codes, ClsItem* it) {
