@@ -51,6 +51,30 @@ def test_batch_matches_single_frames(gpu, batch_classify):
         assert np.array_equal(a, o.cpu().numpy())
 
 
+def test_unsynchronised_workers_match_single_frames(gpu):
+    """Worker contexts that render without per-pass synchronisation
+    (contour3d_gb300_set_server_async): each context sizes a frame's buffers
+    from the frames it rendered before, of other sizes, so overflows and
+    frames rendered again are common; every image still equals the plain
+    single-frame image."""
+    import torch
+    fields, frames = _small_set(gpu, n=12, seed=23)
+    ref = [_single(gpu, fields, s) for s in frames]
+    outs = [torch.zeros(s.width * s.height * 3, dtype=torch.uint8, device="cuda") for s in frames]
+    packs = [workloads.frame_pack(gpu, fields[s.field], s, o) for s, o in zip(frames, outs)]
+    assert gpu.lib.contour3d_gb300_set_server_async(1) == 0
+    try:
+        for _ in range(2):
+            for o in outs:
+                o.zero_()
+            gpu.render_batch(packs, workers=3)
+            torch.cuda.synchronize()
+            for q, (a, o) in enumerate(zip(ref, outs)):
+                assert np.array_equal(a, o.cpu().numpy()), f"frame {q}"
+    finally:
+        gpu.lib.contour3d_gb300_set_server_async(0)
+
+
 def test_server_result_same_alone_and_in_the_mix(gpu):
     import torch
     fields, frames = _small_set(gpu, n=9, seed=11)
