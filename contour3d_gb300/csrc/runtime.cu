@@ -773,17 +773,20 @@ static const int kCounters = 9;
 static const int kSlabRec = 2 + kCounters;
 static const size_t kStatusWords = kStatusHead + (size_t)kSlabRec * kStatusSlabs + 3 * (size_t)kStatusObjs;
 
-/* bytes per triangle of the slab arrays (see TriDev) */
+/* bytes per triangle of the slab arrays (see TriDev): inspection keeps
+   weighted normals, records and flags; the render path the raster records */
 static const size_t kTriBytes = 3 * sizeof(double) + 48 + sizeof(unsigned);
+static const size_t kRecBytes = 48;
+static size_t tri_bytes(bool inspect) { return inspect ? kTriBytes : kRecBytes; }
 /* doubles per triangle of the inspection arrays: vertices, vertex normals, face normal, area */
 static const size_t kDbgDoubles = 22;
 
-static TriDev tri_layout(void *base, size_t cap, double *dbg) {
+static TriDev tri_layout(void *base, size_t cap, double *dbg, bool inspect) {
   TriDev t;
   double *d = static_cast<double *>(base);
-  for (int q = 0; q < 3; q++) t.wn[q] = d + q * cap;
-  t.rec = reinterpret_cast<float4 *>(d + 3 * cap);
-  t.meta = reinterpret_cast<unsigned *>(t.rec + 3 * cap);
+  for (int q = 0; q < 3; q++) t.wn[q] = inspect ? d + q * cap : nullptr;
+  t.rec = reinterpret_cast<float4 *>(inspect ? d + 3 * cap : d);
+  t.meta = inspect ? reinterpret_cast<unsigned *>(t.rec + 3 * cap) : nullptr;
   for (int q = 0; q < 9; q++) t.vert[q] = dbg ? dbg + q * cap : nullptr;
   for (int q = 0; q < 9; q++) t.vn[q] = dbg ? dbg + (9 + q) * cap : nullptr;
   t.dbg_fn = dbg ? dbg + 18 * cap : nullptr;
@@ -1228,7 +1231,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
            far; kernels that find more record an overflow and the frame is
            rendered again */
         if (L.tri_cell.ensure(sizeof(unsigned) * c.caps.T, st) ||
-            L.tri.ensure(kTriBytes * (c.caps.T + 64 + emit_list_slack((long long)c.caps.T)), st))
+            L.tri.ensure(kRecBytes * (c.caps.T + 64 + emit_list_slack((long long)c.caps.T)), st))
           return 1;
       }
       /* read per object: an earlier object of the slab may have grown the buffer */
@@ -1267,8 +1270,9 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
          every sub-array stays aligned (and over-allocate so that cap >= T) */
       /* the record region also holds the empty ends of k_emit's list chunks */
       const unsigned long long slack = sink ? 0ULL : emit_list_slack((long long)T);
-      if (L.tri_cell.ensure(sizeof(unsigned) * T, st) || L.tri.ensure(kTriBytes * (T + 64 + slack), st)) return 1;
-      const size_t cap = (L.tri.cap / kTriBytes) & ~(size_t)31;
+      if (L.tri_cell.ensure(sizeof(unsigned) * T, st) || L.tri.ensure(tri_bytes(sink) * (T + 64 + slack), st))
+        return 1;
+      const size_t cap = (L.tri.cap / tri_bytes(sink)) & ~(size_t)31;
       if (cap < T + slack) {
         log_error("internal: triangle buffer capacity %zu below %llu", cap, T + slack);
         return 1;
@@ -1278,7 +1282,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         if (c.dbg.ensure(sizeof(double) * kDbgDoubles * cap, st)) return 1;
         dbg = c.dbg.as<double>();
       }
-      TriDev tri = tri_layout(L.tri.p, cap, dbg);
+      TriDev tri = tri_layout(L.tri.p, cap, dbg, sink != nullptr);
       tri.rec_cap = cap;
       tri.cap = std::min<unsigned long long>(cap, L.tri_cell.cap / sizeof(unsigned));
       tri.ovf = d_ovf;
