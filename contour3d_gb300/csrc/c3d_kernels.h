@@ -122,6 +122,24 @@ struct VertDev {
   unsigned* ovf;          /* overflow flags (kOvf*) */
 };
 
+/*
+ * The vertex offset of every cell of a slab (its first owned crossed edge's
+ * record in VertDev::pos), as a 16-bit offset from the start of the cell's
+ * scan segment of 2^kVSegShift cells (a segment owns at most 7 of them per
+ * cell: fewer than 2^16) plus the segment's first offset:
+ *   offset(c) = seg[c >> kVSegShift] + rel[c],  c = 0 .. n.
+ * Half the bytes of 32-bit offsets, and the scan stores them without waiting
+ * for its segment's prefix.
+ */
+constexpr int kVSegShift = 13;
+struct VOffDev {
+  unsigned short* rel; /* n + 1 entries */
+  unsigned* seg;       /* segments + 1 entries */
+};
+/* bytes of a VOffDev over n cells, and its layout at `base` (256-byte aligned) */
+size_t voff_bytes(long long n);
+VOffDev voff_layout(void* base, long long n);
+
 /* overflow flags of a frame whose buffers were sized before the counts were
    known (the frame is then rendered again with larger buffers) */
 constexpr unsigned kOvfTriangles = 1u; /* triangles beyond the triangle map or arrays */
@@ -247,22 +265,22 @@ constexpr long long kMaxSlabCells = 178956970;
 /* 64-bit words of the scan's look-back state over n cells (one per segment
    of cells, then the segment ticket counter) */
 long long scan_state_words(long long n);
-/* voffsets[0..n], totals = (triangles, vertices), offsets[n], and
+/* the vertex offsets of cells 0..n, totals = (triangles, vertices), offsets[n], and
    offsets[0..n - 1] when want_offsets; the triangle -> cell map where the
    triangles fit tri_cap (where they do not, `ovf`, when given, receives
    kOvfTriangles: the caller scans again with a larger map).  `state` holds
    scan_state_words(n) words (zeroed here); `err` receives kErrScanTimeout. */
 cudaError_t launch_scan(const unsigned char* codes, long long n, unsigned long long* state, unsigned* offsets,
-                        unsigned* voffsets, unsigned long long* totals, unsigned* tri_cell,
+                        const VOffDev& voff, unsigned long long* totals, unsigned* tri_cell,
                         unsigned long long tri_cap, bool want_offsets, unsigned* ovf, unsigned* err,
                         cudaStream_t st);
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
-                     const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st);
+                     const VOffDev& voff, long long n, const VertDev& V, cudaStream_t st);
 /* record entries beyond the triangles that k_emit's lists may leave empty
    for a launch sized by tri_bound (the region must hold triangles + this) */
 unsigned long long emit_list_slack(long long tri_bound);
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
-                 const unsigned char* codes, const unsigned* offsets, const unsigned* voffsets,
+                 const unsigned char* codes, const unsigned* offsets, const VOffDev& voff,
                  const unsigned* tri_cell, const unsigned long long* total, long long tri_bound, const TriDev& tri,
                  const RasterDev& R, const VertDev& V, unsigned* checks, cudaStream_t st);
 void launch_exact_all(const Geo& G, const unsigned long long* total, long long tri_bound, const TriDev& tri,

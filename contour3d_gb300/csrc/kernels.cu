@@ -145,7 +145,13 @@ __device__ __forceinline__ void cell_ijk(const FieldDev& F, unsigned c, unsigned
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 32;  /* cells per thread */
 constexpr int kScanTile = kScanThreads * kScanItems;
+static_assert(kScanTile == 1 << kVSegShift, "vertex offsets are relative to scan segments");
 constexpr unsigned long long kTriMask = (1ULL << 31) - 1;
+
+/* the vertex offset of cell c */
+__device__ __forceinline__ unsigned voff_at(const VOffDev& o, long long c) {
+  return o.seg[c >> kVSegShift] + o.rel[c];
+}
 
 /* bit m - 1: the iso-level crosses edge m of the cell's corner 0 */
 __device__ __forceinline__ unsigned owned_edges(unsigned code) {
@@ -723,13 +729,14 @@ __device__ __forceinline__ unsigned long long look_back(const unsigned long long
  * segment's part of the triangle -> cell map when it fits tri_cap.  A thread
  * owns 32 consecutive cells; its offsets go through a per-warp shared-memory
  * stage (rows of kStagePitch words) so that every global store of a warp
- * covers 128 contiguous bytes.  The stage holds offsets relative to the
- * segment, so warps 1.. fill it while warp 0 looks back; the prefix is added
- * as the stage is stored.  The map goes through a shared list of the
- * segment's triangles when they fit it (positions relative to the segment,
- * then a coalesced copy), else it is written directly once the prefix is
- * known.  The block of the last segment writes the slab totals and the end
- * entries offsets[n], voffsets[n].
+ * covers 512 contiguous bytes.  The vertex offsets are stored relative to
+ * the segment (VOffDev), so every warp stores them before the prefix is
+ * known, warp 0 then looks back and stores the segment's first offset.  The
+ * map goes through a shared list of the segment's triangles when they fit
+ * it (positions relative to the segment, then a coalesced copy), else it is
+ * written directly once the prefix is known.  The block of the last segment
+ * writes the slab totals and the end entries (triangle offset of cell n,
+ * vertex offset of cell n).
  */
 constexpr int kFillList = 8192; /* triangles of a segment listed in shared memory (4 blocks per SM) */
 constexpr int kStagePitch = 33;  /* words per staged row: conflict-free transposes */
@@ -759,9 +766,33 @@ __device__ __forceinline__ void store_stage(unsigned* __restrict__ dst, const un
   }
 }
 
+/* a warp's 1024 staged values (below 2^16) into dst[wbase ..] as 16-bit
+   words (cells past n are skipped) */
+__device__ __forceinline__ void store_stage16(unsigned short* __restrict__ dst, const unsigned* stage, long long wbase,
+                                              long long n) {
+  const int lane = threadIdx.x & 31;
+  if (wbase + 32 * kScanItems <= n) {
+    /* each store instruction writes 512 contiguous bytes (lane L: cells
+       8L .. 8L + 7 of a 256-cell chunk, all in one staged row; wbase is a
+       multiple of 1024, dst 256-byte aligned) */
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int e = 256 * k + 8 * lane, row = e >> 5, col = e & 31;
+      const unsigned* sr = stage + kStagePitch * row + col;
+      reinterpret_cast<uint4*>(dst + wbase)[32 * k + lane] =
+          make_uint4(sr[0] | (sr[1] << 16), sr[2] | (sr[3] << 16), sr[4] | (sr[5] << 16), sr[6] | (sr[7] << 16));
+    }
+  } else {
+    for (int k = 0; k < 32; k++) {
+      const long long c = wbase + 32 * k + lane;
+      if (c < n) dst[c] = (unsigned short)stage[kStagePitch * k + lane];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kScanThreads, 4)
 k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, unsigned long long* __restrict__ state,
-       unsigned* __restrict__ offsets, unsigned* __restrict__ voffsets, unsigned long long* __restrict__ totals,
+       unsigned* __restrict__ offsets, VOffDev voff, unsigned long long* __restrict__ totals,
        unsigned* __restrict__ tri_cell, unsigned long long tri_cap, int want_offsets, unsigned* __restrict__ ovf,
        unsigned* __restrict__ err) {
   pdl_enter();
@@ -824,7 +855,7 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
   }
   unsigned* stage = stage_all + warp * 32 * kStagePitch;
   const long long wbase = c0 + (long long)warp * 32 * kScanItems; /* the warp's first cell */
-  /* the vertex offsets (relative) and the list; warp 0 first looks back */
+  /* the vertex offsets (relative to the segment) and the list */
   auto fill_stage = [&]() {
     unsigned run = 0;
 #pragma unroll
@@ -840,6 +871,11 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
       run += cnt;
     }
   };
+  /* the vertex offsets are relative to the segment: each warp stores its
+     own at once; warp 0 then looks back */
+  fill_stage();
+  __syncwarp();
+  store_stage16(voff.rel, stage, wbase, n);
   if (warp == 0) {
     unsigned long long prefix = 0;
     if (seg > 0) {
@@ -848,20 +884,21 @@ k_scan(const unsigned char* __restrict__ codes, long long n, long long nseg, uns
     }
     if (lane == 0) {
       s_prefix = prefix;
+      voff.seg[seg] = (unsigned)(prefix >> 31);
       if (seg == nseg - 1) {
         const unsigned long long tot = prefix + agg;
         totals[0] = tot & kTriMask;
         totals[1] = tot >> 31;
         offsets[n] = (unsigned)(tot & kTriMask);
-        voffsets[n] = (unsigned)(tot >> 31);
+        /* cell n: the end of this segment, or the start of segment nseg */
+        voff.seg[nseg] = (unsigned)(tot >> 31);
+        voff.rel[n] = n - c0 < kScanTile ? (unsigned short)(agg >> 31) : (unsigned short)0;
       }
     }
   }
-  fill_stage();
   __syncthreads();
   const unsigned long long seg0 = s_prefix;
   const unsigned ta = (unsigned)(seg0 & kTriMask);
-  store_stage(voffsets, stage, wbase, n, (unsigned)(seg0 >> 31));
   const bool fill = (unsigned long long)ta + seg_tris <= tri_cap;
   /* a map that does not fit: the caller runs the scan again with a larger
      map, or, when the buffers were sized before the count was known (ovf
@@ -1503,8 +1540,8 @@ __device__ __forceinline__ void centre_range(float lo, float hi, long long n, lo
  * k_vertices: the FP32 screen position of every crossed edge of the slab,
  * once per edge (a surface vertex is shared by about six triangles).  A block
  * takes kVTile consecutive cells, lists their owned crossed edges in shared
- * memory at their global vertex indices (voffsets), and computes them with
- * all its threads.  Each record: X, Y, Z, the bound on |X, Y - the
+ * memory at their global vertex indices (the scan's vertex offsets), and
+ * computes them with all its threads.  Each record: X, Y, Z, the bound on |X, Y - the
  * reference's value| and, in aux, the relative depth bound (>= 0), or -1 when
  * the projection certainly fails, -2 when the bounds cannot decide it.  The
  * edge runs from the owning corner to corner m; the reference interpolates a
@@ -1519,13 +1556,13 @@ constexpr int kVTile = kVThreads * kVItems;
 template <typename T>
 __global__ void __launch_bounds__(kVThreads)
 k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restrict__ codes,
-           const unsigned* __restrict__ voffsets, long long n, VertDev V) {
+           VOffDev voff, long long n, VertDev V) {
   pdl_enter();
   __shared__ unsigned short list[kVTile * 7];
   const long long c0 = (long long)blockIdx.x * kVTile;
   if (c0 >= n) return;
   const long long c1 = min(c0 + kVTile, n);
-  const unsigned va = voffsets[c0], vb = voffsets[c1];
+  const unsigned va = voff_at(voff, c0), vb = voff_at(voff, c1);
   if (vb > V.cap) {
     /* more crossed edges than records (buffers sized before the count was known) */
     if (threadIdx.x == 0) atomicOr(V.ovf, kOvfVertices);
@@ -1544,7 +1581,7 @@ k_vertices(FieldDev F, SlabDev S, SceneDev scene, const unsigned char* __restric
         if (cf + q < c1) cw |= (unsigned long long)codes[cf + q] << (8 * q);
     }
     if (cw != 0ULL && cw != ~0ULL) { /* all-outside or all-inside cells own no crossed edge */
-      unsigned at = (cf < c1 ? voffsets[cf] : vb) - va;
+      unsigned at = (cf < c1 ? voff_at(voff, cf) : vb) - va;
 #pragma unroll
       for (int q = 0; q < kVItems; q++) {
         unsigned mask = owned_edges((unsigned)(cw >> (8 * q)) & 255u);
@@ -1605,7 +1642,7 @@ struct EmitOut {
 template <typename T, bool CHECK, bool RENDER, typename LutT>
 __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, const SceneDev& scene,
                                          const LutT* lut, const unsigned char* __restrict__ codes,
-                                         const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
+                                         const VOffDev& voff, const unsigned* __restrict__ tri_cell,
                                          const TriDev& tri, const RasterDev& R, const VertDev& V,
                                          unsigned* __restrict__ checks, long long t, EmitOut& out) {
   const unsigned ncx = (unsigned)(F.nx - 1), ncy = (unsigned)(F.ny - 1);
@@ -1649,7 +1686,7 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
     const unsigned a = (unsigned)((e >> (6 * q)) & 7), b = (unsigned)((e >> (6 * q + 3)) & 7);
     const unsigned o = a & b, m = a ^ b;
     const unsigned oc = c + (o & 1u) + ((o >> 1) & 1u) * ncx + (o >> 2) * ncxy;
-    const unsigned vi = voffsets[oc] + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
+    const unsigned vi = voff_at(voff, oc) + __popc(owned_edges(codes[oc]) & ((1u << (m - 1)) - 1u));
     const float4 p = __ldg(V.pos + vi);
     const unsigned pk = __float_as_uint(p.w);
     const float aux = bf16_value(pk & 0xFFFFu);
@@ -1781,7 +1818,7 @@ template <typename T, bool CHECK, bool RENDER>
 __global__ void __launch_bounds__(256, CHECK ? 1 : 8)
 k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restrict__ lut_g,
        const unsigned char* __restrict__ codes, const unsigned* __restrict__ offsets,
-       const unsigned* __restrict__ voffsets, const unsigned* __restrict__ tri_cell,
+       VOffDev voff, const unsigned* __restrict__ tri_cell,
        const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R, VertDev V,
        unsigned* __restrict__ checks) {
   pdl_trigger(); /* the shared-memory table below does not depend on the preceding kernel */
@@ -1835,7 +1872,7 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
 #pragma unroll
     for (int u = 0; u < kEmitPer; u++) {
       o[u].route = 0;
-      if (tw < tcount) emit_one<T, CHECK, RENDER>(F, S, scene, lut, codes, voffsets, tri_cell, tri, R, V, checks,
+      if (tw < tcount) emit_one<T, CHECK, RENDER>(F, S, scene, lut, codes, voff, tri_cell, tri, R, V, checks,
                                                   (long long)tw, o[u]);
     }
     if (RENDER) {
@@ -3284,48 +3321,60 @@ void launch_classify_queue(const ClsItem* items, int nitems, unsigned long long 
 
 long long scan_state_words(long long n) { return std::max((n + kScanTile - 1) / kScanTile, 1LL) + 1; }
 
+size_t voff_bytes(long long n) {
+  return ((size_t)(n + 1) * sizeof(unsigned short) + 255) / 256 * 256 + sizeof(unsigned) * (size_t)scan_state_words(n);
+}
+
+VOffDev voff_layout(void* base, long long n) {
+  const size_t rel_bytes = ((size_t)(n + 1) * sizeof(unsigned short) + 255) / 256 * 256;
+  VOffDev o;
+  o.rel = static_cast<unsigned short*>(base);
+  o.seg = reinterpret_cast<unsigned*>(static_cast<char*>(base) + rel_bytes);
+  return o;
+}
+
 cudaError_t launch_scan(const unsigned char* codes, long long n, unsigned long long* state, unsigned* offsets,
-                        unsigned* voffsets, unsigned long long* totals, unsigned* tri_cell,
+                        const VOffDev& voff, unsigned long long* totals, unsigned* tri_cell,
                         unsigned long long tri_cap, bool want_offsets, unsigned* ovf, unsigned* err,
                         cudaStream_t st) {
   const long long nseg = scan_state_words(n) - 1;
   const cudaError_t e = cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (size_t)(nseg + 1), st);
   if (e != cudaSuccess) return e;
   launch_k(k_scan, "k_scan", (unsigned)nseg, kScanThreads, kScanWriteSmem, st, codes, n, nseg, state, offsets,
-           voffsets, totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf, err);
+           voff, totals, tri_cell, tri_cap, want_offsets ? 1 : 0, ovf, err);
   return cudaSuccess;
 }
 
 void launch_vertices(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned char* codes,
-                     const unsigned* voffsets, long long n, const VertDev& V, cudaStream_t st) {
+                     const VOffDev& voff, long long n, const VertDev& V, cudaStream_t st) {
   const unsigned blocks = (unsigned)((n + kVTile - 1) / kVTile);
-  if (F.is_f32) launch_k(k_vertices<float>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
-  else launch_k(k_vertices<double>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voffsets, n, V);
+  if (F.is_f32) launch_k(k_vertices<float>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voff, n, V);
+  else launch_k(k_vertices<double>, "k_vertices", blocks, kVThreads, 0, st, F, S, scene, codes, voff, n, V);
 }
 
 void launch_emit(const FieldDev& F, const SlabDev& S, const SceneDev& scene, const unsigned long long* lut,
                  const unsigned char* codes, const unsigned* offsets,
-                 const unsigned* voffsets, const unsigned* tri_cell, const unsigned long long* total,
+                 const VOffDev& voff, const unsigned* tri_cell, const unsigned long long* total,
                  long long tri_bound, const TriDev& tri, const RasterDev& R, const VertDev& V, unsigned* checks,
                  cudaStream_t st) {
   const int g = grid_for(tri_bound, 256, g_emit_per_sm);
   if (!R.cover_count) {
     /* inspection: edge ids and flags only */
-    launch_k(k_emit<double, false, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+    launch_k(k_emit<double, false, false>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voff,
              tri_cell, total, tri, R, V, checks);
   } else if (checks) {
     if (F.is_f32)
-      launch_k(k_emit<float, true, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+      launch_k(k_emit<float, true, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voff,
                tri_cell, total, tri, R, V, checks);
     else
-      launch_k(k_emit<double, true, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+      launch_k(k_emit<double, true, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voff,
                tri_cell, total, tri, R, V, checks);
   } else {
     if (F.is_f32)
-      launch_k(k_emit<float, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+      launch_k(k_emit<float, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voff,
                tri_cell, total, tri, R, V, checks);
     else
-      launch_k(k_emit<double, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voffsets,
+      launch_k(k_emit<double, false, true>, "k_emit", g, 256, 0, st, F, S, scene, lut, codes, offsets, voff,
                tri_cell, total, tri, R, V, checks);
   }
 }

@@ -443,6 +443,8 @@ struct Ctx {
        of a field on both lanes; the passes meet only in the colour bits of
        disjoint pixels) */
     Buf win, amb, nb_ent, nb_wn, nb_span;
+    /* the vertex offsets of a slab of n cells (in voffsets) */
+    VOffDev voff(long long n) const { return voff_layout(voffsets.p, n); }
   };
   Lane lanes[2];
   cudaStream_t lane_stream = nullptr;
@@ -1206,7 +1208,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       Ctx::Lane &L = c.lanes[odd_lane ? 1 : 0];
       const cudaStream_t st = odd_lane ? c.lane_stream : st_main; /* this object's pass */
       if (L.offsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
-          L.voffsets.ensure(sizeof(unsigned) * (size_t)(ncell + 1), st) ||
+          L.voffsets.ensure(voff_bytes(ncell), st) ||
           L.tile_state.ensure(sizeof(unsigned long long) * (size_t)scan_state_words(ncell), st))
         return 1;
       /* the triangle -> cell map is written by the scan when the slab's
@@ -1237,7 +1239,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       /* read per object: an earlier object of the slab may have grown the buffer */
       const unsigned long long tri_cap = L.tri_cell.cap / sizeof(unsigned);
       if (c.stage_timing && ob > 0) cudaEventRecord(c.evs[1], st);
-      C3D_CUDA(launch_scan(codes, ncell, scan_state, L.offsets.as<unsigned>(), L.voffsets.as<unsigned>(), d_total,
+      C3D_CUDA(launch_scan(codes, ncell, scan_state, L.offsets.as<unsigned>(), L.voff(ncell), d_total,
                            L.tri_cell.as<unsigned>(), tri_cap, sink != nullptr, async ? d_ovf : nullptr, d_err, st));
       if (c.stage_timing) cudaEventRecord(c.evs[2], st);
       c.stats.kernel_launches += 1;
@@ -1291,7 +1293,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       if (c.stage_timing) cudaEventRecord(c.evs[3], st);
       if (!async && T > tri_cap) {
         /* the map did not fit: the scan again, with the grown map */
-        C3D_CUDA(launch_scan(codes, ncell, scan_state, L.offsets.as<unsigned>(), L.voffsets.as<unsigned>(), d_total,
+        C3D_CUDA(launch_scan(codes, ncell, scan_state, L.offsets.as<unsigned>(), L.voff(ncell), d_total,
                              L.tri_cell.as<unsigned>(), L.tri_cell.cap / sizeof(unsigned), sink != nullptr, nullptr,
                              d_err, st));
         c.stats.kernel_launches += 1;
@@ -1303,7 +1305,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         VD.pos = L.verts.as<float4>();
         VD.cap = L.verts.cap / 16;
         VD.ovf = d_ovf;
-        launch_vertices(F, S, sd, codes, L.voffsets.as<unsigned>(), ncell, VD, st);
+        launch_vertices(F, S, sd, codes, L.voff(ncell), ncell, VD, st);
         c.stats.kernel_launches += 1;
         if (!async) c.stats.vertices += NV;
       }
@@ -1319,7 +1321,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
       if (sink) {
         RasterDev none = {};
         launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, L.offsets.as<unsigned>(),
-                    L.voffsets.as<unsigned>(), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
+                    L.voff(ncell), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, none, VD, checks,
                     st);
         launch_exact_all(G, d_total, (long long)T, tri, st);
         launch_normals(F, S, L.offsets.as<unsigned>(), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, st);
@@ -1359,7 +1361,7 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           if (!async) C3D_CUDA(cudaMemsetAsync(counters, 0, kCounters * sizeof(unsigned long long), st));
           if (c.stage_timing) cudaEventRecord(c.evs[9], st);
           launch_emit(F, S, sd, c.lut.as<unsigned long long>(), codes, L.offsets.as<unsigned>(),
-                      L.voffsets.as<unsigned>(), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
+                      L.voff(ncell), L.tri_cell.as<unsigned>(), d_total, (long long)T, tri, RS, VD, checks,
                       st);
           if (c.stage_timing) cudaEventRecord(c.evs[4], st);
           launch_raster(G, sd, (long long)T, tri, RS, checks, st);
@@ -2478,7 +2480,9 @@ static uint64_t request_estimate(const contour3d_gb300_frame_t *fr, uint64_t sla
     uint64_t sharing = 0;
     for (size_t q = 0; q < fr->num_fields; q++)
       sharing += fr->fields[q].device_array == fr->fields[n].device_array ? 1 : 0;
-    peak = std::max(peak, cells * (sharing + 4 + 4) + cells / 256);
+    /* codes, triangle offsets (4 bytes), vertex offsets (2 bytes and a
+       word per scan segment), look-back state */
+    peak = std::max(peak, cells * (sharing + 4 + 2) + cells / 256);
   }
   const uint64_t px = (uint64_t)fr->screen_sizes[0] * fr->screen_sizes[1];
   return peak + px * (sizeof(Slot) + 4 + 48 + 4 + 4 + 3) + (1ULL << 20);
