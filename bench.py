@@ -61,9 +61,9 @@ CPU_SAMPLE_SLICES_1 = 16  # z-nodes of the 512^2 x 512 field timed on one host c
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
     "classify": (4.63, "cells"),     # k_classify_tma, both levels in one pass: 154.0 MB for 2 x 16.6 M cells
-    "scan": (4.49, "cells"),         # k_scan (single pass with look-back): 74.5 MB for 16.6 M cells
-    "vertices": (36.5, "vertices"),  # k_vertices: 239.2 MB for 6.55 M vertices
-    "emit": (42.2, "triangles"),     # k_emit: 552.6 MB for 13.1 M triangles
+    "scan": (2.54, "cells"),         # k_scan (16-bit vertex offsets): 42.1 MB for 16.6 M cells
+    "vertices": (32.4, "vertices"),  # k_vertices: 212.2 MB for 6.55 M vertices
+    "emit": (41.6, "triangles"),     # k_emit: 544.6 MB for 13.1 M triangles
 }
 
 
@@ -690,9 +690,11 @@ def main():
     # once -- inputs read once, outputs written once, cached re-reads not counted
     stage_bytes = {
         "classify": nodes * 8 + 2 * cells * 1,  # one pass over the field for both levels
-        "scan": 2 * cells * (1 + 4) + T * 4,
-        "vertices": 2 * cells * (4 + 1) + V * (2 * 8 + 16),
-        "emit": T * 4 + 2 * cells * (4 + 1) + V * 16 + listed * 48 + float(prof.tiny) * 4,
+        # cell codes 1 B; vertex offsets 2 B per cell (16-bit, relative to
+        # the scan's 8192-cell segments), read by k_vertices once per 8 cells
+        "scan": 2 * cells * (1 + 2) + T * 4,
+        "vertices": 2 * cells * (1 + 2 / 8) + V * (2 * 8 + 16),
+        "emit": T * 4 + 2 * cells * (1 + 2) + V * 16 + listed * 48 + float(prof.tiny) * 4,
         "cover": listed * 48 + float(prof.candidates) * 16,
         "exact": float(prof.candidates) * (16 + 4) + float(prof.exact_fragments) * 16,
         "normals": WIDTH * HEIGHT * 16 * 2 + float(prof.winners) * (4 + 48 + 8),
