@@ -1666,7 +1666,7 @@ __device__ __forceinline__ void emit_one(const FieldDev& F, const SlabDev& S, co
   /* slab slices fit 32 bits (a slab holds fewer than 2^28 cells) */
   const unsigned uk = (unsigned)S.kfirst + ukl;
   const unsigned code = codes[c];
-  const unsigned long long e = lut[code * 12 + r];
+  const unsigned long long e = RENDER ? __ldg(lut + code * 12 + r) : lut[code * 12 + r];
   /* rendered set: interior cells of the slab's own slices (contour/main.c:70-112) */
   const bool rendered = ui >= 1u && ui + 2u <= ncx && uj >= 1u && uj + 2u <= ncy && uk >= (unsigned)S.krender0 &&
                         uk < (unsigned)S.krender1;
@@ -1821,16 +1821,21 @@ k_emit(FieldDev F, SlabDev S, SceneDev scene, const unsigned long long* __restri
        VOffDev voff, const unsigned* __restrict__ tri_cell,
        const unsigned long long* __restrict__ total_p, TriDev tri, RasterDev R, VertDev V,
        unsigned* __restrict__ checks) {
-  pdl_trigger(); /* the shared-memory table below does not depend on the preceding kernel */
+  pdl_trigger(); /* the table below does not depend on the preceding kernel */
   (void)offsets;
-  /* the render form needs the corner pairs of the table entries only (bits
-     0-17): 32-bit entries take half the shared memory, which leaves the SM
-     more L1 for the gathers (64-bit entries: 1.57 ms per bench frame, 32-bit:
-     1.47; 16-bit cube-edge ids decoded through a 19-entry table: 1.50) */
-  using LutT = typename std::conditional<RENDER, unsigned, unsigned long long>::type;
-  __shared__ LutT lut[kLutEntries];
-  for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = (LutT)(RENDER ? lut_g[q] & 0x3FFFFULL : lut_g[q]);
-  __syncthreads();
+  /* the render form reads the table through L1 (one 24 KB copy per SM)
+     rather than from a copy in each block's shared memory, which took L1
+     from the gathers and shared memory from the other lane's kernels (per
+     bench frame: 64-bit entries in shared memory 1.57 ms of emit, 32-bit
+     ones 1.47, 16-bit cube-edge ids decoded through a 19-entry table 1.50;
+     through L1 emit 1.52 -> 1.54 alone, but the frame 5.53 -> 5.48 ms) */
+  using LutT = unsigned long long;
+  __shared__ LutT lut_s[RENDER ? 1 : kLutEntries];
+  if (!RENDER) {
+    for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut_s[q] = lut_g[q];
+    __syncthreads();
+  }
+  const LutT* lut = RENDER ? lut_g : lut_s;
   pdl_wait();
   const long long T_ = (long long)*total_p;
   /* the record region holds the cover and sliver entries (at most the
