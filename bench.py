@@ -61,9 +61,9 @@ CPU_SAMPLE_SLICES_1 = 16  # z-nodes of the 512^2 x 512 field timed on one host c
 # launch is scaled by its units
 TRAFFIC_PER_UNIT = {
     "classify": (4.63, "cells"),     # k_classify_tma, both levels in one pass: 154.0 MB for 2 x 16.6 M cells
-    "scan": (2.54, "cells"),         # k_scan (16-bit vertex offsets): 42.1 MB for 16.6 M cells
-    "vertices": (32.4, "vertices"),  # k_vertices: 212.2 MB for 6.55 M vertices
-    "emit": (41.6, "triangles"),     # k_emit: 544.6 MB for 13.1 M triangles
+    "scan": (2.55, "cells"),         # k_scan (16-bit vertex offsets): 42.2 MB for 16.6 M cells
+    "vertices": (32.5, "vertices"),  # k_vertices: 213.0 MB for 6.55 M vertices
+    "emit": (41.5, "triangles"),     # k_emit: 544.3 MB for 13.1 M triangles
 }
 
 
