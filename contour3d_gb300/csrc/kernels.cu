@@ -1367,8 +1367,16 @@ struct ExactTri {
   double area_inv;
 };
 
-__device__ __forceinline__ bool exact_tri(const SceneDev& s, const d3 w[3], ExactTri& x) {
+/* the projected triangle and its inverse area (the box is left unset) */
+__device__ __forceinline__ bool exact_tri_core(const SceneDev& s, const d3 w[3], ExactTri& x) {
   if (!project(s, w[0], x.v0) || !project(s, w[1], x.v1) || !project(s, w[2], x.v2)) return false;
+  x.area = edge_fn(x.v0, x.v1, x.v2);
+  x.area_inv = drcp(x.area < 0. ? fmin(x.area, -1.e-16) : fmax(x.area, +1.e-16));
+  return true;
+}
+
+/* the reference's bounding box of a projected triangle */
+__device__ __forceinline__ void exact_box(const SceneDev& s, ExactTri& x) {
   const long long W = s.width, H = s.height;
   const long long xmin = (long long)dsub(dmul(dadd(0.5, fmin(x.v0.x, fmin(x.v1.x, x.v2.x))), (double)W), 1.);
   const long long xmax = (long long)dadd(dmul(dadd(0.5, fmax(x.v0.x, fmax(x.v1.x, x.v2.x))), (double)W), 1.);
@@ -1378,20 +1386,30 @@ __device__ __forceinline__ bool exact_tri(const SceneDev& s, const d3 w[3], Exac
   x.imax = min(W - 1, max(0LL, xmax));
   x.jmin = min(H - 1, max(0LL, ymin));
   x.jmax = min(H - 1, max(0LL, ymax));
-  x.area = edge_fn(x.v0, x.v1, x.v2);
-  x.area_inv = drcp(x.area < 0. ? fmin(x.area, -1.e-16) : fmax(x.area, +1.e-16));
+}
+
+__device__ __forceinline__ bool exact_tri(const SceneDev& s, const d3 w[3], ExactTri& x) {
+  if (!exact_tri_core(s, w, x)) return false;
+  exact_box(s, x);
   return true;
 }
 
-/* the reference's barycentric weights at pixel (i, j); false when outside */
-__device__ __forceinline__ bool exact_weights(const ExactTri& x, long long i, long long j, const double* xs,
-                                              const double* ys, double& w0, double& w1, double& w2) {
-  if (i < x.imin || i > x.imax || j < x.jmin || j > x.jmax) return false;
+/* the reference's barycentric weights at pixel (i, j) of its box; false when
+   outside the triangle */
+__device__ __forceinline__ bool exact_weights_in(const ExactTri& x, long long i, long long j, const double* xs,
+                                                 const double* ys, double& w0, double& w1, double& w2) {
   const d3 v3 = {xs[i], ys[j], 0.};
   w0 = dmul(x.area_inv, edge_fn(x.v1, x.v2, v3));
   w1 = dmul(x.area_inv, edge_fn(x.v2, x.v0, v3));
   w2 = dmul(x.area_inv, edge_fn(x.v0, x.v1, v3));
   return !(w0 < -1.e-8 || w1 < -1.e-8 || w2 < -1.e-8);
+}
+
+/* the same at any pixel; false when outside the box or the triangle */
+__device__ __forceinline__ bool exact_weights(const ExactTri& x, long long i, long long j, const double* xs,
+                                              const double* ys, double& w0, double& w1, double& w2) {
+  if (i < x.imin || i > x.imax || j < x.jmin || j > x.jmax) return false;
+  return exact_weights_in(x, i, j, xs, ys, w0, w1, w2);
 }
 
 __device__ __forceinline__ double exact_depth(const ExactTri& x, double w0, double w1, double w2) {
@@ -1413,15 +1431,31 @@ __device__ __forceinline__ void keep_weights(const RasterDev& R, long long p, un
   store128_atomic(w + 2, (unsigned long long)__double_as_longlong(w2), tag);
 }
 
-/* one fragment through the reference's test and the (depth, order) z-buffer */
+/*
+ * One candidate fragment through the reference's test and the (depth, order)
+ * z-buffer.  Candidates come from the cover list only: triangles whose area
+ * is certainly not clamped, so a pixel that passes the weight test lies in
+ * the triangle's extent and so inside the reference's box, whose margins are
+ * a pixel wide; the box is not computed (CHECK: it is, and a pixel outside it
+ * counts as a violation and is not drawn).
+ */
+template <bool CHECK>
 __device__ __forceinline__ void exact_fragment(const Geo& G, const SceneDev& s, long long t, long long i, long long j,
-                                               const RasterDev& R, unsigned long long order_base) {
+                                               const RasterDev& R, unsigned long long order_base,
+                                               unsigned* checks) {
   d3 w[3];
   exact_vertices(G, t, w);
   ExactTri x;
-  if (!exact_tri(s, w, x)) return;
+  if (!exact_tri_core(s, w, x)) return;
   double w0, w1, w2;
-  if (!exact_weights(x, i, j, R.xs, R.ys, w0, w1, w2)) return;
+  if (!exact_weights_in(x, i, j, R.xs, R.ys, w0, w1, w2)) return;
+  if (CHECK) {
+    exact_box(s, x);
+    if (i < x.imin || i > x.imax || j < x.jmin || j > x.jmax) {
+      atomicAdd(checks + 2, 1u);
+      return;
+    }
+  }
   const double dist0 = exact_depth(x, w0, w1, w2);
   const unsigned long long order = order_of(G, order_base, t);
   const long long p = j * s.width + i;
@@ -2434,7 +2468,7 @@ k_finish(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsi
     if (q < nl) {
       const Candidate c = R.live[q];
       const unsigned pj = c.pixel / (unsigned)scene.width;
-      exact_fragment(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base);
+      exact_fragment<CHECK>(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base, checks);
     } else {
       finish_tiny<CHECK>(G, scene, R.tiny[q - nl], R, order_base, checks);
     }
