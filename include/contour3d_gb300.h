@@ -253,8 +253,10 @@ int contour3d_gb300_set_async(int on);
  * The same, and graph recording, for the worker contexts of servers (and of
  * contour3d_gb300_render_batch) created afterwards: 0 (default) = worker
  * contexts synchronise after every slab pass; 1 = unsynchronised frames and
- * graphs.  Off by default: a batched run with unsynchronised worker contexts
- * stopped with an illegal memory access whose cause has not been found.
+ * graphs.  Off by default: with unsynchronised workers the batched and
+ * served workloads measured no faster (the other workers keep the GPU busy
+ * while one waits), and a worker's sizes, learnt from frames of every size,
+ * overflow more often.
  */
 int contour3d_gb300_set_server_async(int on);
 /*
