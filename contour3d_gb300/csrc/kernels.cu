@@ -2688,8 +2688,9 @@ __device__ __forceinline__ void warp_append(bool flag, unsigned p, unsigned* lis
 }
 
 /*
- * FP32 pass over the won pixels, 64 pixels per block and iteration, four
- * threads per pixel.  Neighbouring pixels share most of their vertices'
+ * FP32 pass over the won pixels, 32 pixels per block and iteration, four
+ * threads per pixel (blocks of 128 threads: 0.47 -> 0.46 ms per bench frame
+ * against 64 pixels and 256 threads; the block barriers wait for fewer warps).  Neighbouring pixels share most of their vertices'
  * neighbourhoods, so each block first gathers the triangles around its
  * pixels' vertices into a shared hash of (cell, rank) keys, computes each
  * distinct triangle's FP32 weighted normal once, then every (pixel, vertex)
@@ -2698,7 +2699,7 @@ __device__ __forceinline__ void warp_append(bool flag, unsigned p, unsigned* lis
  * does not fit goes to the FP64 pass.  Self-check: every pixel is listed for
  * the FP64 pass, and the FP32 colour, where certain, is kept for it to compare.
  */
-constexpr int kShadeHash = 1024;  /* distinct triangles per block and iteration */
+constexpr int kShadeHash = 512; /* distinct triangles per block and iteration */
 constexpr int kShadeList = 24;    /* triangles around one cube edge (at most 16) */
 constexpr unsigned long long kEmptyKey = ~0ULL;
 
@@ -2723,13 +2724,13 @@ __device__ __forceinline__ int hash_slot(unsigned long long* keys, unsigned long
 }
 
 template <typename T, bool CHECK>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __restrict__ lut,
           unsigned long long obase, unsigned rgb_in) {
   pdl_enter();
   __shared__ unsigned long long keys[kShadeHash];
   __shared__ float4 wnf[kShadeHash];
-  __shared__ unsigned short lists[kShadeList][256];
+  __shared__ unsigned short lists[kShadeList][128];
   __shared__ unsigned short todo[kShadeHash];
   __shared__ unsigned ntodo;
   for (int q = threadIdx.x; q < kShadeHash; q += blockDim.x) keys[q] = kEmptyKey;
@@ -2738,7 +2739,7 @@ k_shade_f(FieldDev F, SceneDev scene, RasterDev R, const unsigned long long* __r
   const unsigned long long n = *R.win_count;
   const unsigned tid = threadIdx.x, lane = tid & 31u, m = tid & 3u, g0 = lane & ~3u;
   const ThrF th = thr_f(F.threshold);
-  for (unsigned long long base = blockIdx.x * 64ULL; base < n; base += gridDim.x * 64ULL) {
+  for (unsigned long long base = blockIdx.x * 32ULL; base < n; base += gridDim.x * 32ULL) {
     const unsigned long long q = base + tid / 4;
     /* gather: the (cell, rank) of every triangle around this thread's vertex */
     unsigned p = 0;
@@ -2887,10 +2888,10 @@ __global__ void __launch_bounds__(256)
 k_nb_list(FieldDev F, RasterDev R, const unsigned long long* __restrict__ lut_g, const unsigned* __restrict__ pixels,
           const unsigned long long* __restrict__ count, unsigned long long obase, unsigned long long* __restrict__ ent,
           unsigned long long ent_cap, unsigned long long* __restrict__ ent_count, uint2* __restrict__ spans) {
-  pdl_trigger(); /* the shared-memory table below does not depend on the preceding kernel */
-  __shared__ unsigned long long lut[kLutEntries];
-  for (int q = threadIdx.x; q < kLutEntries; q += blockDim.x) lut[q] = lut_g[q];
-  __syncthreads();
+  pdl_trigger();
+  /* the table through L1: a copy in each block's shared memory cost every
+     block 24 KB of loads and a barrier */
+  const unsigned long long* lut = lut_g;
   pdl_wait();
   const unsigned long long n = 3 * *count;
   const unsigned long long iters = (n + blockDim.x - 1) / blockDim.x;
@@ -3466,13 +3467,13 @@ void launch_shade_f(const FieldDev& F, const SceneDev& scene, const RasterDev& R
   /* no single-precision shading without node spacings (a converter) or for
      axes of 2^20 nodes and more (hash keys): every pixel to the FP64 pass */
   if (!F.dgx || F.nx > (1 << 20) || F.ny > (1 << 20) || F.nz > (1 << 20)) return;
-  const int gs = grid_for(4 * npx, 256, 8); /* four threads per pixel */
+  const int gs = grid_for(4 * npx, 128, 16); /* four threads per pixel */
   if (F.is_f32) {
-    if (R.shade_check) launch_k(k_shade_f<float, true>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
-    else launch_k(k_shade_f<float, false>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    if (R.shade_check) launch_k(k_shade_f<float, true>, "k_shade_f", gs, 128, 0, st, F, scene, R, lut, obase, rgb);
+    else launch_k(k_shade_f<float, false>, "k_shade_f", gs, 128, 0, st, F, scene, R, lut, obase, rgb);
   } else {
-    if (R.shade_check) launch_k(k_shade_f<double, true>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
-    else launch_k(k_shade_f<double, false>, "k_shade_f", gs, 256, 0, st, F, scene, R, lut, obase, rgb);
+    if (R.shade_check) launch_k(k_shade_f<double, true>, "k_shade_f", gs, 128, 0, st, F, scene, R, lut, obase, rgb);
+    else launch_k(k_shade_f<double, false>, "k_shade_f", gs, 128, 0, st, F, scene, R, lut, obase, rgb);
   }
 }
 
