@@ -732,7 +732,7 @@ def main():
         sc.contours = [_abi.Contour(host_field, thr, col, grids=tuple(grids)) for thr, col in zip(thresholds, COLORS)]
         tmp = tempfile.mkdtemp()
         path = os.path.join(tmp, "frame.ppm")
-        for _ in range(2):
+        for _ in range(max(3, args.warmup)):  # the first calls allocate and page in
             if gpu.execute(sc, path) != 0:
                 raise RuntimeError("contour3d_execute failed")
         steps2 = args.steps  # the same step count as the device-timed value
