@@ -282,35 +282,40 @@ def run_batched(gpu, workers, nfields=64):
 
     shape_tuning = autotune.tune_launch_shape(gpu, sample, per_frame[:16], [f.width * f.height for f in frames[:16]],
                                               torch.cuda.get_device_name())
-    for p in packs[:4]:
-        gpu.render_pack(p)
-    gpu.render_batch(packs[:8], workers)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    # every frame once through each form first (worker contexts and the
+    # library's own size their buffers from the frames they have seen), then
+    # the median of three passes of each
     for p in packs:
-        if gpu.render_pack(p) != 0:
-            raise RuntimeError("plain frame failed")
-    torch.cuda.synchronize()
-    plain_s = time.perf_counter() - t0
-    ref = [o.clone() for o in outs]
-    for o in outs:
-        o.zero_()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
+        gpu.render_pack(p)
     gpu.render_batch(packs, workers)
     torch.cuda.synchronize()
-    batch_s = time.perf_counter() - t0
+
+    def timed(fn, reps=3):
+        ts = []
+        for _ in range(reps):
+            for o in outs:
+                o.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return sorted(ts)[reps // 2]
+
+    def plain_pass():
+        for p in packs:
+            if gpu.render_pack(p) != 0:
+                raise RuntimeError("plain frame failed")
+
+    plain_s = timed(plain_pass)
+    ref = [o.clone() for o in outs]
+    batch_s = timed(lambda: gpu.render_batch(packs, workers))
     same = all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
     # the same batch with each frame classifying its own fields
     gpu.set_batch_classify(False)
     try:
-        for o in outs:
-            o.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
         gpu.render_batch(packs, workers)
-        torch.cuda.synchronize()
-        own_s = time.perf_counter() - t0
+        own_s = timed(lambda: gpu.render_batch(packs, workers))
     finally:
         gpu.set_batch_classify(True)
     same = same and all(bool(torch.equal(a, b)) for a, b in zip(ref, outs))
