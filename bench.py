@@ -701,7 +701,7 @@ def main():
         "vertices": 2 * cells * (1 + 2 / 8) + V * (2 * 8 + 16),
         "emit": T * 4 + 2 * cells * (1 + 2) + V * 16 + listed * 48 + float(prof.tiny) * 4,
         "cover": listed * 48 + float(prof.candidates) * 16,
-        "exact": float(prof.candidates) * (16 + 4) + float(prof.exact_fragments) * 16,
+        "exact": float(prof.candidates) * (16 + 4),  # each candidate and its pixel's depth floor read once
         "normals": WIDTH * HEIGHT * 16 * 2 + float(prof.winners) * (4 + 48 + 8),
         "shade": float(prof.shade_exact) * (4 + 48 + 8) + float(prof.normals) * (8 + 24),
     }

@@ -78,7 +78,7 @@ struct SlabDev {
 
 /* launch shape of the tunable kernels, process-wide: slices per
    classification brick, resident blocks per SM of k_emit's grid and of the
-   raster passes' grids (k_cover, k_sliver, k_tiny, k_prune, k_exact) */
+   raster passes' grids (k_raster, k_finish) */
 struct LaunchShape {
   int cls_z;
   int emit_per_sm;
@@ -188,8 +188,7 @@ struct RasterDev {
                                <= triangles + emit_list_slack) */
   unsigned long long* sliver_count;
   unsigned long long* listed_count; /* [0] cover, [1] sliver entries, without the empty ones */
-  Candidate* live;          /* candidates that can still win (capacity cand_cap) */
-  unsigned long long* live_count;
+  unsigned long long* live_count; /* candidates that can still win (counted by k_finish) */
   /* per pixel, the exact weights of the fragment that last won its CAS: three
      16-byte words (weight k, tag), tag = order << 24 | epoch, each stored
      atomically; shading uses them when all three tags name the final owner */
@@ -288,11 +287,10 @@ void launch_exact_all(const Geo& G, const unsigned long long* total, long long t
 void launch_normals(const FieldDev& F, const SlabDev& S, const unsigned* offsets, const unsigned* tri_cell,
                     const unsigned long long* total, long long tri_bound, const TriDev& tri, cudaStream_t st);
 /* the raster passes of one slab: the cover and sliver lists (k_raster),
-   the candidates below the depth floor dropped (k_prune), the surviving
-   candidates and the tiny list in FP64 (k_finish); bounds size the grids */
+   then the candidates that can still win (those below the depth floor
+   dropped) and the tiny list in FP64 (k_finish); bounds size the grids */
 void launch_raster(const Geo& G, const SceneDev& scene, long long tri_bound, const TriDev& tri,
                    const RasterDev& R, unsigned* checks, cudaStream_t st);
-void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st);
 void launch_finish(const Geo& G, const SceneDev& scene, long long bound, const RasterDev& R,
                    unsigned long long order_base, unsigned* checks, cudaStream_t st);
 /* winners, normal requests, weighted normals, colours; `between` (optional)

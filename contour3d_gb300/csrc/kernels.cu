@@ -21,8 +21,8 @@
  *                   fragments raise a per-pixel depth floor, the rest become
  *                   candidates; slivers (area the reference may clamp) the
  *                   bounds cannot settle go to the tiny list
- *   k_prune         drops candidates below the final depth floor
- *   k_finish        one thread per remaining candidate: the reference's
+ *   k_finish        drops candidates below the final depth floor, then one
+ *                   thread per remaining candidate: the reference's
  *                   vertices (recomputed from the field), projection,
  *                   barycentric test and harmonic depth in FP64, then a
  *                   128-bit (depth, order) max into the z-buffer; then one
@@ -50,7 +50,7 @@
  *   k_vertices, exact vertices  src/contour3d/contour/triangulate.c:40-73
  *   k_shade_f, k_nb_*, k_shade, k_normals
  *                               src/contour3d/contour/normal.c:6-165
- *   k_raster, k_prune, k_finish, shading factor
+ *   k_raster, k_finish, shading factor
  *                               src/contour3d/contour/render.c:38-163,
  *                               src/contour3d/project.c:9-67
  *   k_lines                     src/contour3d/line.c:26-119
@@ -2422,31 +2422,8 @@ k_raster(Geo G, SceneDev scene, TriDev tri, RasterDev R, unsigned* __restrict__ 
 }
 
 /* ------------------------------------------------------------------ */
-/* k_exact: the reference's arithmetic for the surviving candidates    */
+/* k_finish: the reference's arithmetic for the candidates that can win */
 /* ------------------------------------------------------------------ */
-/*
- * Candidates whose depth bound reaches the pixel's final floor, compacted:
- * an FP64 warp instruction costs the same with one active lane as with 32,
- * so k_exact runs only over fragments that can still win.
- */
-__global__ void __launch_bounds__(256) k_prune(RasterDev R) {
-  pdl_enter();
-  const unsigned long long n = min(*R.cand_count, R.cand_cap);
-  for (unsigned long long base = blockIdx.x * (unsigned long long)blockDim.x; base < n;
-       base += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned long long q = base + threadIdx.x;
-    Candidate c = {};
-    bool keep = false;
-    if (q < n) {
-      c = R.cand[q];
-      /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
-      keep = f_key(c.dhi) >= R.zlo[c.pixel];
-    }
-    const unsigned long long w = block_reserve<256>(R.live_count, keep);
-    if (keep) R.live[w] = c; /* w < n <= cand_cap */
-  }
-}
-
 /* one tiny-list triangle (a call of its own: its registers stay out of the
    candidate loop's allocation) */
 template <bool CHECK>
@@ -2455,25 +2432,69 @@ __device__ __noinline__ void finish_tiny(const Geo& G, const SceneDev& scene, un
   tiny_triangle<CHECK>(G, scene, t, R, order_base, checks);
 }
 
-/* k_finish: the surviving candidates (the reference's fragment test), then
-   the tiny list (the reference's arithmetic for the whole triangle), in one
-   grid; both end in the z-buffer's 128-bit maximum, so their order does not
-   matter */
+/*
+ * k_finish: the candidates that can still win (the reference's fragment
+ * test), then the tiny list (the reference's arithmetic for the whole
+ * triangle), in one grid; both end in the z-buffer's 128-bit maximum, so
+ * their order does not matter.  A block filters kFinChunk candidates at a
+ * time against the final depth floors into a shared list and runs the FP64
+ * test in whole rounds of its 256 threads once the list holds kFinRun of
+ * them, keeping the rest for the next round (an FP64 warp instruction costs
+ * the same with one active lane as with 32).
+ */
+constexpr unsigned kFinChunk = 1024, kFinRun = 512;
 template <bool CHECK>
 __global__ void __launch_bounds__(256, 4)
 k_finish(Geo G, SceneDev scene, RasterDev R, unsigned long long order_base, unsigned* __restrict__ checks) {
   pdl_enter();
-  const unsigned long long nl = *R.live_count, nt = min(*R.tiny_count, R.tiny_cap);
-  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < nl + nt;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    if (q < nl) {
-      const Candidate c = R.live[q];
-      const unsigned pj = c.pixel / (unsigned)scene.width;
-      exact_fragment<CHECK>(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base, checks);
-    } else {
-      finish_tiny<CHECK>(G, scene, R.tiny[q - nl], R, order_base, checks);
+  /* before a chunk is filtered the list holds fewer than kFinRun entries */
+  __shared__ Candidate s_live[kFinRun + kFinChunk];
+  __shared__ unsigned s_n;
+  const unsigned long long nc = min(*R.cand_count, R.cand_cap), nt = min(*R.tiny_count, R.tiny_cap);
+  const unsigned long long nb = (nc + kFinChunk - 1) / kFinChunk;
+  if (threadIdx.x == 0) s_n = 0u;
+  __syncthreads();
+  unsigned have = 0; /* entries in the list (s_n between the filter passes) */
+  for (unsigned long long b = blockIdx.x;; b += gridDim.x) {
+    const bool more = b < nb;
+    if (more) {
+#pragma unroll
+      for (unsigned u = 0; u < kFinChunk / 256; u++) {
+        const unsigned long long q = b * kFinChunk + u * 256 + threadIdx.x;
+        if (q < nc) {
+          const Candidate c = R.cand[q];
+          /* a certainly drawn fragment of this pixel is nearer than anything this one can reach */
+          if (f_key(c.dhi) >= R.zlo[c.pixel]) s_live[atomicAdd(&s_n, 1u)] = c;
+        }
+      }
     }
+    __syncthreads();
+    const unsigned n = s_n;
+    __syncthreads(); /* every thread has read n before the next filter pass adds to it */
+    if (threadIdx.x == 0 && n > have) atomicAdd(R.live_count, (unsigned long long)(n - have));
+    have = n;
+    if (n >= kFinRun || !more) {
+      const unsigned take = more ? n / 256 * 256 : n; /* whole rounds, all at the end */
+      for (unsigned e = threadIdx.x; e < take; e += 256) {
+        const Candidate c = s_live[e];
+        const unsigned pj = c.pixel / (unsigned)scene.width;
+        exact_fragment<CHECK>(G, scene, c.t, c.pixel - pj * (unsigned)scene.width, pj, R, order_base, checks);
+      }
+      __syncthreads();
+      /* the rest (fewer than 256, from take >= 256 on) to the front */
+      const unsigned rest = n - take;
+      Candidate c = {};
+      if (threadIdx.x < rest) c = s_live[take + threadIdx.x];
+      __syncthreads();
+      if (threadIdx.x < rest) s_live[threadIdx.x] = c;
+      if (threadIdx.x == 0) s_n = rest;
+      __syncthreads();
+      have = rest;
+    }
+    if (!more) break;
   }
+  for (unsigned long long q = blockIdx.x * 256ULL + threadIdx.x; q < nt; q += (unsigned long long)gridDim.x * 256ULL)
+    finish_tiny<CHECK>(G, scene, R.tiny[q], R, order_base, checks);
 }
 
 /* shading (render.c:137-159, normal.c:6-165), once per contour object     */
@@ -3446,10 +3467,6 @@ void launch_raster(const Geo& G, const SceneDev& scene, long long tri_bound, con
     if (checks) launch_k(k_raster<double, true>, "k_raster", g, 128, 0, st, G, scene, tri, R, checks);
     else launch_k(k_raster<double, false>, "k_raster", g, 128, 0, st, G, scene, tri, R, checks);
   }
-}
-
-void launch_prune(const RasterDev& R, long long cand_bound, cudaStream_t st) {
-  launch_k(k_prune, "k_prune", grid_for(cand_bound, 256, g_raster_per_sm), 256, 0, st, R);
 }
 
 void launch_finish(const Geo& G, const SceneDev& scene, long long bound, const RasterDev& R,

@@ -437,7 +437,7 @@ struct Ctx {
      meet only in the z-buffer, the depth floors and the winner weights,
      whose updates are order-independent maxima and tagged stores */
   struct Lane {
-    Buf offsets, voffsets, tile_state, tri_cell, tri, verts, cand, live, tiny;
+    Buf offsets, voffsets, tile_state, tri_cell, tri, verts, cand, tiny;
     /* one object's shading: its won pixels, those left to FP64, and the
        FP64 pass's neighbour lists (unsynchronised frames shade the objects
        of a field on both lanes; the passes meet only in the colour bits of
@@ -1348,13 +1348,12 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
         RS.listed_count = counters + 2;
         RS.sliver_rec = tri.rec + 3 * (cap - 1);
         for (int attempt = 0;; attempt++) {
-          if (L.cand.ensure(sizeof(Candidate) * cand_want, st) || L.live.ensure(sizeof(Candidate) * cand_want, st) ||
+          if (L.cand.ensure(sizeof(Candidate) * cand_want, st) ||
               L.tiny.ensure(sizeof(unsigned) * tiny_want, st))
             return 1;
           RS.cand = L.cand.as<Candidate>();
-          RS.cand_cap = std::min(L.cand.cap, L.live.cap) / sizeof(Candidate);
+          RS.cand_cap = L.cand.cap / sizeof(Candidate);
           RS.cand_count = counters + 0;
-          RS.live = L.live.as<Candidate>();
           RS.tiny = L.tiny.as<unsigned>();
           RS.tiny_cap = L.tiny.cap / sizeof(unsigned);
           RS.tiny_count = counters + 1;
@@ -1366,12 +1365,11 @@ static int render_contour(Ctx &c, const FrameIn &f, const SceneDev &sd, const Co
           if (c.stage_timing) cudaEventRecord(c.evs[4], st);
           launch_raster(G, sd, (long long)T, tri, RS, checks, st);
           if (c.stage_timing) cudaEventRecord(c.evs[5], st);
-          launch_prune(RS, (long long)RS.cand_cap, st);
           launch_finish(G, sd, (long long)(RS.cand_cap + RS.tiny_cap), RS, slab_order, checks, st);
           if (c.stage_timing) cudaEventRecord(c.evs[6], st);
           trace_mark(c, st, "slab " + std::to_string(slab_index - 1) + " object " + std::to_string(ob) + " (" +
                                 std::to_string(S.nslices) + " slices) raster done");
-          c.stats.kernel_launches += 4;
+          c.stats.kernel_launches += 3;
           if (async) {
             /* list capacities of this pass, compared with the counts at the frame's end */
             c.async_cand_cap = std::min(c.async_cand_cap, RS.cand_cap);
@@ -2389,7 +2387,7 @@ static std::vector<Buf *> ctx_bufs(Ctx &c) {
   std::vector<Buf *> v = {&c.lut, &c.counts, &c.scratch, &c.dbg, &c.field, &c.consts, &c.nodes, &c.canvas,
                           &c.rgb, &c.zlo, &c.winfo, &c.shade_check, &c.checks, &c.status};
   for (Ctx::Lane &L : c.lanes)
-    for (Buf *b : {&L.offsets, &L.voffsets, &L.tile_state, &L.tri_cell, &L.tri, &L.verts, &L.cand, &L.live, &L.tiny,
+    for (Buf *b : {&L.offsets, &L.voffsets, &L.tile_state, &L.tri_cell, &L.tri, &L.verts, &L.cand, &L.tiny,
                    &L.win, &L.amb, &L.nb_ent, &L.nb_wn, &L.nb_span})
       v.push_back(b);
   return v;
